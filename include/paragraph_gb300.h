@@ -1,0 +1,184 @@
+/*
+ * paragraph_gb300.h -- C ABI of the GB300 (sm_103a) per-epoch graph-growth engine.
+ *
+ * One context owns one CUDA device stream and one device arena holding R >= 1 citation graphs
+ * ("replicas").  R == 1 is the plain drop-in for ParAGraph's per-epoch growth step; R > 1 is the
+ * batched ensemble.  Every entry point returns a pg_status; pg_last_error() gives the message.
+ * No C++ exception crosses this boundary and no entry point takes a torch or CUDA type.
+ *
+ * Reference interfaces replaced (paths are inside the ParAGraph project):
+ *   pg_load_graph / pg_load_replica  <- Graph::ParseNodelist / ParseEdgelist / AddEdge and the
+ *                                       per-epoch host CSR rebuild prepareGraph
+ *                                       (src/graph.cu:336-447, src/graph.cu:820-826,
+ *                                        src/utils.cu:75-142)
+ *   pg_grow_epoch                    <- buildOneNodeConnections_timed (src/kernel.cu:1125-1586) plus
+ *                                       the host edge insert and in-degree update that follow it in
+ *                                       execute() (src/kernel.cu:1766-1815, src/graph.cu:537-618)
+ *   pg_grow_epoch_refcompat          <- the same step with the reference's linear score mix, budget
+ *                                       split and uniform fill (src/kernel.cu:196-402,
+ *                                       src/abm.cu:376-565)
+ *   pg_er_epoch                      <- the G(n,p) growth step of the reference's ER model, whose
+ *                                       semantics are recorded in results/slurm-8634746.out:60-73
+ *   pg_copy_edges / pg_epoch_edges   <- append_device_to_host (includes/utils.cuh:151-200) and the
+ *                                       new_edges_vec the step appends to
+ *   pg_copy_degrees                  <- Graph::GetInDegree / GetOutDegree (src/graph.cu:537-618)
+ *   pg_get_stats                     <- EpochTiming / print_epoch_report
+ *                                       (includes/epoch_profiler.cuh:56-242)
+ */
+#ifndef PARAGRAPH_GB300_H
+#define PARAGRAPH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PG_OK = 0,
+    PG_ERR_CUDA = 1,      /* a CUDA runtime call failed */
+    PG_ERR_CAPACITY = 2,  /* a node/edge/agent capacity would be exceeded */
+    PG_ERR_ARG = 3,       /* invalid argument (bad id, size or parameter) */
+    PG_ERR_TIMEOUT = 4,   /* a bounded device wait ran out (status read back from the device) */
+    PG_ERR_IO = 5,        /* file input/output failed */
+    PG_ERR_STATE = 6      /* call made in the wrong state (e.g. grow before load) */
+} pg_status;
+
+/* Weight functors for the preferential-attachment step. */
+enum {
+    PG_WEIGHTS_BASELINE = 0,  /* w_j = f_j^gamma (indeg_j+1)^alpha exp(-(t-t_j)/tau) beta^[j in N_a] */
+    PG_WEIGHTS_REFCOMPAT = 1  /* ParAGraph's pa/rec/fit linear mix with its budget split */
+};
+
+/* Largest out-degree a single agent may draw; the Poisson table saturates here. */
+#define PG_MAX_OUT_DEGREE 256
+/* Most anchors a baseline agent may use for its neighbourhood. */
+#define PG_MAX_ANCHORS 4
+
+typedef struct pg_ctx pg_ctx;
+
+typedef struct {
+    int32_t device;        /* CUDA device ordinal */
+    int32_t num_replicas;  /* R >= 1 */
+    uint64_t seed;         /* Philox key */
+    int32_t weight_model;  /* PG_WEIGHTS_* */
+    int32_t record_trace;  /* 1: keep each epoch's arrival-ordered citations for pg_loglik_* */
+} pg_config;
+
+/* Per-replica model parameters (baseline functor). */
+typedef struct {
+    double alpha;            /* exponent on (indeg+1) */
+    double tau;              /* recency time constant, epochs */
+    double gamma;            /* exponent on fitness */
+    double beta;             /* neighbourhood boost, >= 1 */
+    double mean_out_degree;  /* Poisson mean of the out-degree, clipped to [1, n] */
+    double growth_rate;      /* > 0: new nodes per epoch = ceil(n * growth_rate) */
+    int64_t fixed_new_nodes; /* used when growth_rate <= 0 */
+    int32_t num_anchors;     /* 1..PG_MAX_ANCHORS */
+    int32_t reserved;
+} pg_pa_params;
+
+/* One replica's seed graph and capacities.  Ids are dense in [0, num_nodes). */
+typedef struct {
+    int64_t num_nodes;
+    const int32_t* pub_epoch;  /* [num_nodes] publication epoch (may be negative) */
+    const float* fitness;      /* [num_nodes] > 0 */
+    int64_t num_edges;
+    const int32_t* src;        /* [num_edges] citing node */
+    const int32_t* dst;        /* [num_edges] cited node */
+    int64_t node_capacity;     /* >= num_nodes; 0 derives it from params and planned_epochs */
+    int64_t edge_capacity;     /* 0 derives it */
+    int32_t planned_epochs;    /* epochs the capacities must cover when derived */
+    int32_t reserved;
+    pg_pa_params params;
+} pg_replica_desc;
+
+/* Counters of the last epoch (summed over replicas) and per-kernel device times. */
+typedef struct {
+    int64_t epoch;             /* index of the last epoch run */
+    int64_t new_nodes;
+    int64_t new_edges;
+    int64_t nodes_weighted;    /* nodes whose weight and CDF entry were computed */
+    int64_t rows_expanded;     /* adjacency rows (fwd+bwd pairs) read by the neighbourhood stage */
+    int64_t elems_streamed;    /* neighbourhood elements keyed (with multiplicity) */
+    int64_t draws;             /* global-race draws */
+    int64_t bwd_moved;         /* old backward-CSR entries moved by the append */
+    int64_t bytes_alg;         /* algorithmic bytes of the epoch (byte model in the design doc) */
+    int64_t bytes_alg_agents;  /* algorithmic bytes of the agent kernel alone */
+    double ms_total;           /* device time of the whole epoch, CUDA events */
+    double ms_weights;         /* weights + quantise + CDF scan */
+    double ms_setup;           /* out-degree draw + edge-offset scan */
+    double ms_agents;          /* the agent kernel(s) */
+    double ms_csr;             /* CSR append */
+    double ms_er;              /* ER count + emit (ER epochs) */
+} pg_stats;
+
+/* ---- lifecycle ---- */
+pg_status pg_create(pg_ctx** out, const pg_config* cfg);
+void pg_destroy(pg_ctx* ctx);
+const char* pg_last_error(const pg_ctx* ctx);
+const char* pg_status_string(pg_status s);
+
+/* ---- graph input ---- */
+/* Replica 0 of a context created with num_replicas == 1, default parameters, capacities derived
+ * from planned_epochs.  Edge semantics follow Graph::AddEdge: duplicates collapse, self-loops stay. */
+pg_status pg_load_graph(pg_ctx* ctx, int64_t n, const int32_t* pub_epoch, const float* fitness,
+                        int64_t m, const int32_t* src, const int32_t* dst);
+/* Set all replicas at once (required before the first epoch when R > 1). */
+pg_status pg_load_replicas(pg_ctx* ctx, const pg_replica_desc* descs, int32_t num);
+pg_status pg_set_params(pg_ctx* ctx, int32_t replica, const pg_pa_params* params);
+pg_status pg_default_params(pg_pa_params* out);
+/* Current epoch index (publication epoch of the next cohort); default 0. */
+pg_status pg_set_epoch(pg_ctx* ctx, int64_t epoch);
+
+/* ---- growth ---- */
+/* One preferential-attachment epoch over every replica.  Synchronous: on return new_nodes /
+ * new_edges hold the totals over replicas (either pointer may be NULL). */
+pg_status pg_grow_epoch(pg_ctx* ctx, int64_t* new_nodes, int64_t* new_edges);
+/* num_epochs PA epochs without host synchronisation between them; use_graph != 0 captures the
+ * whole run in one CUDA graph the first time and replays it afterwards. */
+pg_status pg_run_epochs(pg_ctx* ctx, int32_t num_epochs, int32_t use_graph, int64_t* new_edges);
+/* One Erdos-Renyi G(n,p) epoch on replica 0: delta new nodes, each linking to every pre-epoch node
+ * with probability p, by geometric skips. */
+pg_status pg_er_epoch(pg_ctx* ctx, int64_t delta, double p, int64_t* new_edges);
+
+/* ---- output ---- */
+pg_status pg_get_counts(const pg_ctx* ctx, int32_t replica, int64_t* n, int64_t* m);
+/* Range [first, first+count) of the last epoch's edges in forward-CSR order. */
+pg_status pg_epoch_edges(const pg_ctx* ctx, int32_t replica, int64_t* first, int64_t* count);
+/* Edges [first, first+count) in forward-CSR order (source ascending, then target ascending). */
+pg_status pg_copy_edges(pg_ctx* ctx, int32_t replica, int64_t first, int64_t count,
+                        int32_t* src, int32_t* dst);
+pg_status pg_copy_degrees(pg_ctx* ctx, int32_t replica, int32_t* indeg, int32_t* outdeg);
+pg_status pg_copy_nodes(pg_ctx* ctx, int32_t replica, int32_t* pub_epoch, float* fitness);
+/* which: 0 forward (out-edges), 1 backward (in-edges).  off has n+1 entries, col m. */
+pg_status pg_copy_csr(pg_ctx* ctx, int32_t replica, int32_t which, int64_t* off, int32_t* col);
+/* Citations of the last epoch in arrival order ([count] as from pg_epoch_edges); needs
+ * record_trace. */
+pg_status pg_copy_arrivals(pg_ctx* ctx, int32_t replica, int32_t* cited);
+
+/* ---- measurement ---- */
+/* enable != 0 records CUDA events around every kernel group of each epoch (default on). */
+pg_status pg_set_timing(pg_ctx* ctx, int32_t enable);
+pg_status pg_get_stats(const pg_ctx* ctx, pg_stats* out);
+pg_status pg_sync(pg_ctx* ctx);
+/* Reads the device error word; PG_OK when no kernel reported a fault. */
+pg_status pg_check_device(pg_ctx* ctx);
+
+/* ---- host-side building blocks shared with tests ---- */
+/* Philox4x32-10 block (Salmon et al., SC'11) for counter c[4] and key k[2]. */
+void pg_philox4x32_10(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);
+/* Poisson(lambda) CDF thresholds scaled to 2^64, PG_MAX_OUT_DEGREE+1 entries. */
+pg_status pg_poisson_table(double lambda, uint64_t* table);
+/* The library's own elementary functions (identical on host and device). */
+float pg_logf_host(float x);
+float pg_expf_host(float x);
+double pg_log_host(double x);
+double pg_exp_host(double x);
+/* Version string of the build. */
+const char* pg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PARAGRAPH_GB300_H */

@@ -1,0 +1,209 @@
+"""ctypes wrapper of the CPU oracle (oracle/oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the checker for the GPU growth engine and the timed CPU baseline.  The
+product package (paragraph_gb300) never imports this module; tests/, __graft_entry__.smoke() and
+bench.py's CPU legs do.  Parity of this restatement against the reference itself is unpinned (the
+reference has no tests, golden vectors or fixed seeds and cannot be built here).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_DIR = Path(__file__).resolve().parent
+LIB = _DIR / "_build" / "liboracle.so"
+_lib = None
+
+
+def _load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB.exists():
+        import sys
+
+        sys.path.insert(0, str(_DIR.parent))
+        from paragraph_gb300.build import build_oracle
+
+        build_oracle()
+    lib = C.CDLL(str(LIB))
+    vp, i32, i64, u64, u32 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_uint32
+    sig = {
+        "og_philox": (None, [vp, vp, vp]),
+        "og_logf": (C.c_float, [C.c_float]),
+        "og_expf": (C.c_float, [C.c_float]),
+        "og_log": (C.c_double, [C.c_double]),
+        "og_exp": (C.c_double, [C.c_double]),
+        "og_poisson_table": (None, [C.c_double, vp]),
+        "og_fitness": (C.c_float, [u64, u32, u32, u32]),
+        "og_create": (vp, [u64, u32]),
+        "og_destroy": (None, [vp]),
+        "og_load": (i32, [vp, i64, vp, vp, i64, vp, vp]),
+        "og_set_params": (i32, [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                C.c_double, i64, i32]),
+        "og_set_epoch": (None, [vp, i64]),
+        "og_epoch": (i64, [vp]),
+        "og_pa_epoch": (i32, [vp, i32]),
+        "og_er_epoch": (i32, [vp, i64, C.c_double, i32]),
+        "og_num_nodes": (i64, [vp]),
+        "og_num_edges": (i64, [vp]),
+        "og_copy_csr": (None, [vp, i32, vp, vp]),
+        "og_copy_degrees": (None, [vp, vp, vp]),
+        "og_copy_nodes": (None, [vp, vp, vp]),
+        "og_epoch_edges": (None, [vp, C.POINTER(i64), C.POINTER(i64)]),
+        "og_copy_arrivals": (None, [vp, vp]),
+        "og_stats": (None, [vp, vp]),
+        "og_copy_weights": (i64, [vp, vp, vp, C.POINTER(i32)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def philox(counter, key) -> np.ndarray:
+    lib = _load()
+    c = np.ascontiguousarray(counter, np.uint32)
+    k = np.ascontiguousarray(key, np.uint32)
+    o = np.zeros(4, np.uint32)
+    lib.og_philox(_p(c), _p(k), _p(o))
+    return o
+
+
+def logf(x: float) -> float:
+    return _load().og_logf(x)
+
+
+def expf(x: float) -> float:
+    return _load().og_expf(x)
+
+
+def log(x: float) -> float:
+    return _load().og_log(x)
+
+
+def exp(x: float) -> float:
+    return _load().og_exp(x)
+
+
+def poisson_table(lam: float) -> np.ndarray:
+    t = np.zeros(257, np.uint64)
+    _load().og_poisson_table(lam, _p(t))
+    return t
+
+
+def fitness(seed: int, replica: int, epoch: int, unit: int) -> float:
+    return _load().og_fitness(seed, replica, epoch & 0xFFFFFFFF, unit)
+
+
+class OracleGraph:
+    """One replica's graph state, stepped on the CPU."""
+
+    def __init__(self, seed: int = 42, replica: int = 0):
+        self._lib = _load()
+        self._g = self._lib.og_create(seed, replica)
+
+    def close(self):
+        if self._g:
+            self._lib.og_destroy(self._g)
+            self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load(self, pub, fit, src, dst) -> None:
+        pub = np.ascontiguousarray(pub, np.int32)
+        fit = np.ascontiguousarray(fit, np.float32)
+        src = np.ascontiguousarray(src, np.int32)
+        dst = np.ascontiguousarray(dst, np.int32)
+        st = self._lib.og_load(self._g, len(pub), _p(pub), _p(fit), len(src), _p(src), _p(dst))
+        if st:
+            raise ValueError(f"og_load failed ({st})")
+
+    def set_params(self, alpha=1.0, tau=5.0, gamma=1.0, beta=4.0, mean_out_degree=15.0,
+                   growth_rate=0.0, fixed_new_nodes=5000, num_anchors=3) -> None:
+        st = self._lib.og_set_params(self._g, alpha, tau, gamma, beta, mean_out_degree,
+                                     growth_rate, int(fixed_new_nodes), int(num_anchors))
+        if st:
+            raise ValueError(f"og_set_params failed ({st})")
+
+    def set_epoch(self, e: int) -> None:
+        self._lib.og_set_epoch(self._g, e)
+
+    def pa_epoch(self, threads: int = 0) -> None:
+        st = self._lib.og_pa_epoch(self._g, threads)
+        if st:
+            raise ValueError(f"og_pa_epoch failed ({st})")
+
+    def er_epoch(self, delta: int, p: float, threads: int = 0) -> None:
+        st = self._lib.og_er_epoch(self._g, delta, p, threads)
+        if st:
+            raise ValueError(f"og_er_epoch failed ({st})")
+
+    @property
+    def n(self) -> int:
+        return self._lib.og_num_nodes(self._g)
+
+    @property
+    def m(self) -> int:
+        return self._lib.og_num_edges(self._g)
+
+    def csr(self, which: int = 0):
+        off = np.empty(self.n + 1, np.int64)
+        col = np.empty(max(self.m, 1), np.int32)
+        self._lib.og_copy_csr(self._g, which, _p(off), _p(col))
+        return off, col[: self.m]
+
+    def degrees(self):
+        i = np.empty(self.n, np.int32)
+        o = np.empty(self.n, np.int32)
+        self._lib.og_copy_degrees(self._g, _p(i), _p(o))
+        return i, o
+
+    def nodes(self):
+        p = np.empty(self.n, np.int32)
+        f = np.empty(self.n, np.float32)
+        self._lib.og_copy_nodes(self._g, _p(p), _p(f))
+        return p, f
+
+    def epoch_edges(self):
+        f, c = C.c_int64(), C.c_int64()
+        self._lib.og_epoch_edges(self._g, C.byref(f), C.byref(c))
+        return f.value, c.value
+
+    def last_epoch_edges(self):
+        first, cnt = self.epoch_edges()
+        off, col = self.csr(0)
+        src = np.repeat(np.arange(self.n, dtype=np.int32), np.diff(off))
+        return src[first:first + cnt], col[first:first + cnt]
+
+    def arrivals(self):
+        _, c = self.epoch_edges()
+        a = np.empty(max(c, 1), np.int32)
+        self._lib.og_copy_arrivals(self._g, _p(a))
+        return a[:c]
+
+    def stats(self) -> dict:
+        s = np.zeros(5, np.int64)
+        self._lib.og_stats(self._g, _p(s))
+        return dict(nodes_weighted=int(s[0]), rows_expanded=int(s[1]), elems_streamed=int(s[2]),
+                    draws=int(s[3]), new_edges=int(s[4]))
+
+    def weights(self):
+        n = self._lib.og_copy_weights(self._g, None, None, None)
+        w = np.empty(n, np.float32)
+        cdf = np.empty(n, np.uint64)
+        sh = C.c_int32()
+        self._lib.og_copy_weights(self._g, _p(w), _p(cdf), C.byref(sh))
+        return w, cdf, sh.value

@@ -1,0 +1,766 @@
+/*
+ * oracle.c -- CPU restatement of ParAGraph's per-epoch growth step (C99 + OpenMP).
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the GPU engine and the timed CPU baseline.  The
+ * product never calls it.  Parity against the reference is unpinned (the reference has no tests
+ * or fixed seeds and cannot be built here); see oracle.h.
+ *
+ * Built with -O2 -ffp-contract=off and no fast-math so every floating-point operation rounds once,
+ * exactly as the device code does.
+ *
+ * What each part restates:
+ *   og_load           Graph::ParseEdgelist/AddEdge set semantics (src/graph.cu:376-447,820-826):
+ *                     duplicate edges collapse, self-loops stay; rows kept sorted like std::set.
+ *   weights / CDF     the per-epoch score preparation of execute() (src/kernel.cu:1698-1706,
+ *                     src/abm.cu:112-208,324-338), with the baseline weight functor
+ *                     w_j = f_j^g (indeg_j+1)^a exp(-(t-t_j)/tau) instead of the linear mix.
+ *   neighbourhood     the 2-hop undirected ball of GetOneAndTwoHopNeighborhood
+ *                     (src/abm.cu:577-682): forward and backward rows of the anchors and of their
+ *                     neighbours.
+ *   sampling          weighted sampling without replacement.  The reference draws
+ *                     Efraimidis-Spirakis keys log(u)/score and keeps a top-k heap
+ *                     (src/abm.cu:461-565, gpu-std/device_min_heap.cuh:71-145).  Here the same
+ *                     exponential-clock idea is split into two independent races: a global race
+ *                     over all nodes (sequential inverse-CDF draws, without replacement) and a
+ *                     neighbourhood race over the ball with rate (beta-1) w_j (keys E/w_j, k
+ *                     smallest).  The first k distinct arrivals of the merged race are a
+ *                     successive-sampling draw with weights w_j beta^[j in N_a].
+ *   edge emit         ABMKernelStage4 (src/abm.cu:958-994): one (agent, cited) edge per choice.
+ *   CSR append        the host edge insert and updateNodeInDegreeOutDegree
+ *                     (src/kernel.cu:1766-1815, src/graph.cu:537-618).
+ *   ER                G(n,p) against pre-epoch nodes, as recorded in
+ *                     results/slurm-8634746.out:60-73, by geometric skips.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <omp.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ Philox4x32-10 */
+/* Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11. */
+void og_philox(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]) {
+    uint32_t x0 = c[0], x1 = c[1], x2 = c[2], x3 = c[3];
+    uint32_t key0 = k[0], key1 = k[1];
+    for (int round = 0; round < 10; round++) {
+        if (round) {
+            key0 += 0x9E3779B9u;
+            key1 += 0xBB67AE85u;
+        }
+        uint64_t p0 = (uint64_t)0xD2511F53u * x0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * x2;
+        uint32_t y0 = (uint32_t)(p1 >> 32) ^ x1 ^ key0;
+        uint32_t y1 = (uint32_t)p1;
+        uint32_t y2 = (uint32_t)(p0 >> 32) ^ x3 ^ key1;
+        uint32_t y3 = (uint32_t)p0;
+        x0 = y0;
+        x1 = y1;
+        x2 = y2;
+        x3 = y3;
+    }
+    out[0] = x0;
+    out[1] = x1;
+    out[2] = x2;
+    out[3] = x3;
+}
+
+enum { S_OUTDEG = 1, S_ANCHOR = 2, S_GLOBAL = 3, S_BOOST = 4, S_FIT = 5, S_ER = 6 };
+
+static void rng(uint64_t seed, uint32_t stream, uint32_t aux, uint32_t epoch, uint32_t unit,
+                uint32_t i, uint32_t out[4]) {
+    uint32_t c[4] = {i, unit, epoch, (stream << 24) | (aux & 0xFFFFFFu)};
+    uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    og_philox(c, k, out);
+}
+
+static float unif_f(uint32_t x) { return (float)((x >> 8) + 1u) * 0x1p-24f; }
+static double unif_d(uint32_t lo, uint32_t hi) {
+    uint64_t v = ((((uint64_t)hi) << 32) | lo) >> 11;
+    return (double)(v + 1u) * 0x1p-53;
+}
+static uint64_t join64(uint32_t lo, uint32_t hi) { return (((uint64_t)hi) << 32) | lo; }
+static uint64_t hi_mul64(uint64_t a, uint64_t b) {
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+}
+
+/* ------------------------------------------------------------------ elementary functions */
+/* exp: Cody-Waite reduction + Taylor series; log: atanh series on the mantissa.  Same published
+ * methods and the same rounded series coefficients as the engine, written out independently. */
+static float f_from_bits(uint32_t u) {
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+static uint32_t bits_of_f(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+}
+static double d_from_bits(uint64_t u) {
+    double d;
+    memcpy(&d, &u, 8);
+    return d;
+}
+static uint64_t bits_of_d(double d) {
+    uint64_t u;
+    memcpy(&u, &d, 8);
+    return u;
+}
+
+float og_expf(float x) {
+    if (isnan(x)) return x;
+    if (x > 88.0f) return INFINITY;
+    if (x < -87.0f) return 0.0f;
+    float k = rintf(x * 0x1.715476p+0f);
+    float r = fmaf(-k, 0x1.62e430p-1f, x);
+    r = fmaf(-k, -0x1.05c610p-29f, r);
+    static const float c[8] = {0x1.a01a02p-13f, 0x1.6c16c2p-10f, 0x1.111112p-7f, 0x1.555556p-5f,
+                               0x1.555556p-3f,  0x1.0p-1f,       1.0f,           1.0f};
+    float p = c[0];
+    for (int i = 1; i < 8; i++) p = fmaf(p, r, c[i]);
+    int ki = (int)k;
+    return p * f_from_bits((uint32_t)(ki + 127) << 23);
+}
+
+float og_logf(float x) {
+    if (!(x > 0.0f)) return x == 0.0f ? -INFINITY : NAN;
+    if (isinf(x)) return x;
+    int adj = 0;
+    if (x < 0x1p-126f) {
+        x *= 0x1p23f;
+        adj = -23;
+    }
+    uint32_t b = bits_of_f(x);
+    int e = (int)(b >> 23) - 127 + adj;
+    float m = f_from_bits((b & 0x7FFFFFu) | 0x3F800000u);
+    if (m > 0x1.6a09e6p+0f) {
+        m *= 0.5f;
+        e++;
+    }
+    float s = (m - 1.0f) / (m + 1.0f);
+    float z = s * s;
+    static const float c[4] = {0x1.c71c72p-4f, 0x1.24924ap-3f, 0x1.99999ap-3f, 0x1.555556p-2f};
+    float p = c[0];
+    for (int i = 1; i < 4; i++) p = fmaf(p, z, c[i]);
+    float t = s + s;
+    float lm = fmaf(t * z, p, t);
+    float ef = (float)e;
+    return fmaf(ef, 0x1.62e430p-1f, fmaf(ef, -0x1.05c610p-29f, lm));
+}
+
+double og_exp(double x) {
+    if (isnan(x)) return x;
+    if (x > 709.0) return INFINITY;
+    if (x < -708.0) return 0.0;
+    double k = rint(x * 0x1.71547652b82fep+0);
+    double r = fma(-k, 0x1.62e42fefa39efp-1, x);
+    r = fma(-k, 0x1.abc9e3b39803fp-56, r);
+    static const double c[14] = {
+        0x1.6124613a86d09p-33, 0x1.1eed8eff8d898p-29, 0x1.ae64567f544e4p-26, 0x1.27e4fb7789f5cp-22,
+        0x1.71de3a556c734p-19, 0x1.a01a01a01a01ap-16, 0x1.a01a01a01a01ap-13, 0x1.6c16c16c16c17p-10,
+        0x1.1111111111111p-7,  0x1.5555555555555p-5,  0x1.5555555555555p-3,  0x1.0p-1,
+        1.0,                   1.0};
+    double p = c[0];
+    for (int i = 1; i < 14; i++) p = fma(p, r, c[i]);
+    int64_t ki = (int64_t)k;
+    return p * d_from_bits((uint64_t)(ki + 1023) << 52);
+}
+
+double og_log(double x) {
+    if (!(x > 0.0)) return x == 0.0 ? -INFINITY : NAN;
+    if (isinf(x)) return x;
+    int adj = 0;
+    if (x < 0x1p-1022) {
+        x *= 0x1p52;
+        adj = -52;
+    }
+    uint64_t b = bits_of_d(x);
+    int e = (int)(b >> 52) - 1023 + adj;
+    double m = d_from_bits((b & 0xFFFFFFFFFFFFFull) | 0x3FF0000000000000ull);
+    if (m > 0x1.6a09e667f3bcdp+0) {
+        m *= 0.5;
+        e++;
+    }
+    double s = (m - 1.0) / (m + 1.0);
+    double z = s * s;
+    static const double c[11] = {0x1.642c8590b2164p-5, 0x1.8618618618618p-5, 0x1.af286bca1af28p-5,
+                                 0x1.e1e1e1e1e1e1ep-5, 0x1.1111111111111p-4, 0x1.3b13b13b13b14p-4,
+                                 0x1.745d1745d1746p-4, 0x1.c71c71c71c71cp-4, 0x1.2492492492492p-3,
+                                 0x1.999999999999ap-3, 0x1.5555555555555p-2};
+    double p = c[0];
+    for (int i = 1; i < 11; i++) p = fma(p, z, c[i]);
+    double t = s + s;
+    double lm = fma(t * z, p, t);
+    double ef = (double)e;
+    return fma(ef, 0x1.62e42fefa39efp-1, fma(ef, 0x1.abc9e3b39803fp-56, lm));
+}
+
+#define OG_TABLE 257 /* out-degrees 0..256 */
+
+/* Poisson(lambda) CDF * 2^64, saturating; the out-degree law of the baseline configs. */
+void og_poisson_table(double lambda, uint64_t* table) {
+    double p = og_exp(-lambda), cdf = p;
+    for (int i = 0; i < OG_TABLE; i++) {
+        if (i > 0) {
+            p = p * lambda / (double)i;
+            cdf = cdf + p;
+        }
+        if (cdf >= 1.0 || i == OG_TABLE - 1)
+            table[i] = UINT64_MAX;
+        else
+            table[i] = (uint64_t)(cdf * 0x1p64);
+    }
+}
+
+/* lognormal(0,1) by the Marsaglia polar method */
+float og_fitness(uint64_t seed, uint32_t replica, uint32_t epoch, uint32_t unit) {
+    for (uint32_t i = 0; i < 32; i++) {
+        uint32_t r[4];
+        rng(seed, S_FIT, replica, epoch, unit, i, r);
+        for (int h = 0; h < 2; h++) {
+            float v1 = 2.0f * unif_f(r[2 * h]) - 1.0f;
+            float v2 = 2.0f * unif_f(r[2 * h + 1]) - 1.0f;
+            float s = v1 * v1 + v2 * v2;
+            if (s < 1.0f && s > 0.0f) return og_expf(v1 * sqrtf(-2.0f * og_logf(s) / s));
+        }
+    }
+    return 1.0f;
+}
+
+/* ------------------------------------------------------------------ graph state */
+struct og_graph {
+    uint64_t seed;
+    uint32_t replica;
+    int64_t epoch;
+    /* params */
+    float alpha_f, gamma_f, tau_f;
+    double beta_m1, lambda, growth_rate;
+    int64_t fixed_new;
+    int anchors;
+    uint64_t table[OG_TABLE];
+    /* nodes */
+    int64_t n;
+    int32_t* pub;
+    float* fit;
+    int32_t* indeg;
+    /* CSR */
+    int64_t m;
+    int64_t* fwd_off;
+    int32_t* fwd_col;
+    int64_t* bwd_off;
+    int32_t* bwd_col;
+    /* last epoch */
+    int64_t last_first, last_count;
+    int32_t* arrivals;
+    int64_t stats[5];
+    float* w;
+    uint64_t* cdf;
+    int64_t w_n;
+    int32_t shift;
+};
+
+og_graph* og_create(uint64_t seed, uint32_t replica) {
+    og_graph* g = (og_graph*)calloc(1, sizeof(og_graph));
+    g->seed = seed;
+    g->replica = replica;
+    og_set_params(g, 1.0, 5.0, 1.0, 4.0, 15.0, 0.0, 0, 3);
+    return g;
+}
+
+void og_destroy(og_graph* g) {
+    if (!g) return;
+    free(g->pub);
+    free(g->fit);
+    free(g->indeg);
+    free(g->fwd_off);
+    free(g->fwd_col);
+    free(g->bwd_off);
+    free(g->bwd_col);
+    free(g->arrivals);
+    free(g->w);
+    free(g->cdf);
+    free(g);
+}
+
+int og_set_params(og_graph* g, double alpha, double tau, double gamma, double beta, double lambda,
+                  double growth_rate, int64_t fixed_new, int32_t num_anchors) {
+    if (!(tau > 0) || !(beta >= 1.0) || num_anchors < 1 || num_anchors > 4 || !(lambda >= 0))
+        return 3;
+    g->alpha_f = (float)alpha;
+    g->gamma_f = (float)gamma;
+    g->tau_f = (float)tau;
+    g->beta_m1 = beta - 1.0;
+    g->lambda = lambda;
+    g->growth_rate = growth_rate;
+    g->fixed_new = fixed_new;
+    g->anchors = num_anchors;
+    og_poisson_table(lambda, g->table);
+    return 0;
+}
+
+void og_set_epoch(og_graph* g, int64_t epoch) { g->epoch = epoch; }
+int64_t og_epoch(const og_graph* g) { return g->epoch; }
+
+static int cmp_i32(const void* a, const void* b) {
+    int32_t x = *(const int32_t*)a, y = *(const int32_t*)b;
+    return (x > y) - (x < y);
+}
+
+typedef struct {
+    int32_t a, b;
+} pair32;
+static int cmp_pair(const void* x, const void* y) {
+    const pair32* p = (const pair32*)x;
+    const pair32* q = (const pair32*)y;
+    if (p->a != q->a) return (p->a > q->a) - (p->a < q->a);
+    return (p->b > q->b) - (p->b < q->b);
+}
+
+/* Build CSR (sorted rows, duplicates collapsed) from an edge list. */
+static void build_csr(int64_t n, int64_t m, const int32_t* src, const int32_t* dst, int64_t** off_out,
+                      int32_t** col_out, int64_t* m_out) {
+    pair32* e = (pair32*)malloc(sizeof(pair32) * (size_t)(m > 0 ? m : 1));
+    for (int64_t i = 0; i < m; i++) {
+        e[i].a = src[i];
+        e[i].b = dst[i];
+    }
+    qsort(e, (size_t)m, sizeof(pair32), cmp_pair);
+    int64_t u = 0;
+    for (int64_t i = 0; i < m; i++)
+        if (i == 0 || e[i].a != e[i - 1].a || e[i].b != e[i - 1].b) e[u++] = e[i];
+    int64_t* off = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
+    int32_t* col = (int32_t*)malloc(sizeof(int32_t) * (size_t)(u > 0 ? u : 1));
+    for (int64_t i = 0; i < u; i++) off[e[i].a + 1]++;
+    for (int64_t i = 0; i < n; i++) off[i + 1] += off[i];
+    for (int64_t i = 0; i < u; i++) col[i] = e[i].b;
+    free(e);
+    *off_out = off;
+    *col_out = col;
+    *m_out = u;
+}
+
+int og_load(og_graph* g, int64_t n, const int32_t* pub, const float* fitness, int64_t m,
+            const int32_t* src, const int32_t* dst) {
+    if (n <= 0) return 3;
+    for (int64_t i = 0; i < m; i++)
+        if (src[i] < 0 || src[i] >= n || dst[i] < 0 || dst[i] >= n) return 3;
+    g->n = n;
+    g->pub = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    g->fit = (float*)malloc(sizeof(float) * (size_t)n);
+    g->indeg = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    memcpy(g->pub, pub, sizeof(int32_t) * (size_t)n);
+    memcpy(g->fit, fitness, sizeof(float) * (size_t)n);
+    build_csr(n, m, src, dst, &g->fwd_off, &g->fwd_col, &g->m);
+    int64_t mb;
+    build_csr(n, m, dst, src, &g->bwd_off, &g->bwd_col, &mb);
+    for (int64_t i = 0; i < n; i++) g->indeg[i] = (int32_t)(g->bwd_off[i + 1] - g->bwd_off[i]);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ CSR append */
+/* Appends rows for `delta` new nodes (their forward rows given in agent order, each sorted) and
+ * the matching backward entries; the appended part of every backward row is in agent order, which
+ * is ascending source id.  Restates the host insert of execute() (src/kernel.cu:1766-1815) and
+ * updateNodeInDegreeOutDegree (src/graph.cu:537-618). */
+static void append_rows(og_graph* g, int64_t delta, const int64_t* row_off, const int32_t* rows,
+                        int32_t new_pub, const float* new_fit) {
+    int64_t n = g->n, n2 = n + delta;
+    int64_t e_new = row_off[delta];
+    /* forward */
+    int64_t* fo = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n2 + 1));
+    memcpy(fo, g->fwd_off, sizeof(int64_t) * (size_t)(n + 1));
+    for (int64_t a = 0; a < delta; a++) fo[n + a + 1] = g->m + row_off[a + 1];
+    int32_t* fc = (int32_t*)malloc(sizeof(int32_t) * (size_t)(g->m + e_new + 1));
+    memcpy(fc, g->fwd_col, sizeof(int32_t) * (size_t)g->m);
+    memcpy(fc + g->m, rows, sizeof(int32_t) * (size_t)e_new);
+    /* backward */
+    int64_t* inc = (int64_t*)calloc((size_t)n2, sizeof(int64_t));
+    for (int64_t i = 0; i < e_new; i++) inc[rows[i]]++;
+    int64_t* bo = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n2 + 1));
+    bo[0] = 0;
+    for (int64_t j = 0; j < n2; j++) {
+        int64_t old = j < n ? g->bwd_off[j + 1] - g->bwd_off[j] : 0;
+        bo[j + 1] = bo[j] + old + inc[j];
+    }
+    int32_t* bc = (int32_t*)malloc(sizeof(int32_t) * (size_t)(bo[n2] + 1));
+    int64_t* cur = (int64_t*)malloc(sizeof(int64_t) * (size_t)n2);
+    for (int64_t j = 0; j < n2; j++) {
+        int64_t old = j < n ? g->bwd_off[j + 1] - g->bwd_off[j] : 0;
+        if (old) memcpy(bc + bo[j], g->bwd_col + g->bwd_off[j], sizeof(int32_t) * (size_t)old);
+        cur[j] = bo[j] + old;
+    }
+    for (int64_t a = 0; a < delta; a++)
+        for (int64_t i = row_off[a]; i < row_off[a + 1]; i++) bc[cur[rows[i]]++] = (int32_t)(n + a);
+    /* nodes */
+    g->pub = (int32_t*)realloc(g->pub, sizeof(int32_t) * (size_t)n2);
+    g->fit = (float*)realloc(g->fit, sizeof(float) * (size_t)n2);
+    g->indeg = (int32_t*)realloc(g->indeg, sizeof(int32_t) * (size_t)n2);
+    for (int64_t a = 0; a < delta; a++) {
+        g->pub[n + a] = new_pub;
+        g->fit[n + a] = new_fit[a];
+        g->indeg[n + a] = 0;
+    }
+    for (int64_t j = 0; j < n2; j++) g->indeg[j] += (int32_t)inc[j];
+    free(g->fwd_off);
+    free(g->fwd_col);
+    free(g->bwd_off);
+    free(g->bwd_col);
+    g->fwd_off = fo;
+    g->fwd_col = fc;
+    g->bwd_off = bo;
+    g->bwd_col = bc;
+    g->last_first = g->m;
+    g->last_count = e_new;
+    g->m += e_new;
+    g->n = n2;
+    free(inc);
+    free(cur);
+}
+
+/* ------------------------------------------------------------------ PA epoch */
+typedef struct {
+    float key;
+    int32_t id;
+} keyed;
+static int keyed_less(keyed x, keyed y) { return x.key < y.key || (x.key == y.key && x.id < y.id); }
+static int cmp_keyed(const void* a, const void* b) {
+    keyed x = *(const keyed*)a, y = *(const keyed*)b;
+    return keyed_less(x, y) ? -1 : (keyed_less(y, x) ? 1 : 0);
+}
+
+typedef struct {
+    keyed* v;
+    int64_t n, cap;
+} keyvec;
+static void kv_push(keyvec* kv, keyed x) {
+    if (kv->n == kv->cap) {
+        kv->cap = kv->cap ? kv->cap * 2 : 1024;
+        kv->v = (keyed*)realloc(kv->v, sizeof(keyed) * (size_t)kv->cap);
+    }
+    kv->v[kv->n++] = x;
+}
+
+/* Sample one agent; writes k sorted citations to out_sorted and the arrival order to out_arr.
+ * Returns k.  Counters: cnt[0] rows expanded, cnt[1] elements keyed. */
+static int sample_agent(const og_graph* g, int64_t a, const float* w, const uint64_t* cdf,
+                        int shift, int64_t npos, int32_t* out_sorted, int32_t* out_arr,
+                        int64_t* cnt, keyvec* kv) {
+    const int64_t n = g->n;
+    const uint32_t ep = (uint32_t)g->epoch, rep = g->replica, unit = (uint32_t)a;
+    uint32_t r[4];
+    /* out-degree: Poisson via the CDF table, clipped to [1, min(n, npos)] */
+    rng(g->seed, S_OUTDEG, rep, ep, unit, 0, r);
+    uint64_t u = join64(r[0], r[1]);
+    int kraw = OG_TABLE - 1;
+    for (int i = 0; i < OG_TABLE; i++)
+        if (u < g->table[i]) {
+            kraw = i;
+            break;
+        }
+    int64_t k = kraw < 1 ? 1 : kraw;
+    if (k > n) k = n;
+    if (k > npos) k = npos;
+    /* anchors: uniform over existing nodes (getGeneratorNode, src/abm.cu:567-574) */
+    int32_t anchor[4];
+    rng(g->seed, S_ANCHOR, rep, ep, unit, 0, r);
+    for (int i = 0; i < g->anchors; i++) anchor[i] = (int32_t)(((uint64_t)r[i] * (uint64_t)n) >> 32);
+
+    /* global race: k sequential inverse-CDF draws without replacement */
+    int32_t g_id[256];
+    double g_t[256];
+    int32_t c_id[256];   /* chosen ids, ascending */
+    uint64_t c_q[256];   /* their quantised weights */
+    int nc = 0;
+    uint64_t R = cdf[n - 1];
+    double t = 0.0;
+    const double unit_scale = d_from_bits((uint64_t)(1023 - shift) << 52); /* 2^-shift */
+    for (int64_t i = 0; i < k; i++) {
+        if (R == 0) break;
+        rng(g->seed, S_GLOBAL, rep, ep, unit, (uint32_t)i, r);
+        double E = -og_log(unif_d(r[0], r[1]));
+        double Rd = (double)R * unit_scale;
+        t = t + E / Rd;
+        uint64_t y = hi_mul64(join64(r[2], r[3]), R);
+        /* smallest j with cdf[j] - C(j) > y; C(j) = sum of chosen q with id <= j */
+        int64_t lo = 0, hi = n - 1;
+        while (lo < hi) {
+            int64_t mid = lo + (hi - lo) / 2;
+            uint64_t cm = 0;
+            for (int c = 0; c < nc && c_id[c] <= mid; c++) cm += c_q[c];
+            if (cdf[mid] - cm > y)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        int32_t j = (int32_t)lo;
+        uint64_t qj = cdf[j] - (j > 0 ? cdf[j - 1] : 0);
+        g_id[i] = j;
+        g_t[i] = t;
+        int pos = nc;
+        while (pos > 0 && c_id[pos - 1] > j) {
+            c_id[pos] = c_id[pos - 1];
+            c_q[pos] = c_q[pos - 1];
+            pos--;
+        }
+        c_id[pos] = j;
+        c_q[pos] = qj;
+        nc++;
+        R -= qj;
+    }
+    int ng = nc;
+
+    /* neighbourhood race over the 2-hop undirected ball (multiset; duplicates share a key) */
+    keyed b[256];
+    int nb = 0;
+    if (g->beta_m1 > 0.0) {
+        kv->n = 0;
+#define OG_KEY(node)                                                        \
+    do {                                                                    \
+        int32_t nd_ = (node);                                               \
+        cnt[1]++;                                                           \
+        if (w[nd_] > 0.0f) {                                                \
+            uint32_t rb_[4];                                                \
+            rng(g->seed, S_BOOST, rep, ep, unit, (uint32_t)nd_, rb_);       \
+            keyed kk_ = {-og_logf(unif_f(rb_[0])) / w[nd_], nd_};           \
+            kv_push(kv, kk_);                                               \
+        }                                                                   \
+    } while (0)
+        for (int i = 0; i < g->anchors; i++) OG_KEY(anchor[i]);
+        for (int i = 0; i < g->anchors; i++) {
+            int32_t x = anchor[i];
+            cnt[0]++;
+            for (int dir = 0; dir < 2; dir++) {
+                const int64_t* off = dir ? g->bwd_off : g->fwd_off;
+                const int32_t* col = dir ? g->bwd_col : g->fwd_col;
+                for (int64_t p = off[x]; p < off[x + 1]; p++) {
+                    int32_t y1 = col[p];
+                    OG_KEY(y1);
+                    cnt[0]++;
+                    for (int dir2 = 0; dir2 < 2; dir2++) {
+                        const int64_t* off2 = dir2 ? g->bwd_off : g->fwd_off;
+                        const int32_t* col2 = dir2 ? g->bwd_col : g->fwd_col;
+                        for (int64_t p2 = off2[y1]; p2 < off2[y1 + 1]; p2++) OG_KEY(col2[p2]);
+                    }
+                }
+            }
+        }
+#undef OG_KEY
+        qsort(kv->v, (size_t)kv->n, sizeof(keyed), cmp_keyed);
+        for (int64_t i = 0; i < kv->n && nb < k; i++)
+            if (i == 0 || kv->v[i].id != kv->v[i - 1].id || kv->v[i].key != kv->v[i - 1].key)
+                b[nb++] = kv->v[i];
+    }
+
+    /* merge the two races: first k distinct nodes by (time, id) */
+    int taken = 0, gi = 0, bi = 0;
+    while (taken < k && (gi < ng || bi < nb)) {
+        int32_t id;
+        double tb = bi < nb ? (double)b[bi].key / g->beta_m1 : 0.0;
+        int take_g = bi >= nb || (gi < ng && (g_t[gi] < tb || (g_t[gi] == tb && g_id[gi] <= b[bi].id)));
+        if (take_g)
+            id = g_id[gi++];
+        else
+            id = b[bi++].id;
+        int dup = 0;
+        for (int q = 0; q < taken; q++)
+            if (out_arr[q] == id) {
+                dup = 1;
+                break;
+            }
+        if (!dup) out_arr[taken++] = id;
+    }
+    memcpy(out_sorted, out_arr, sizeof(int32_t) * (size_t)taken);
+    qsort(out_sorted, (size_t)taken, sizeof(int32_t), cmp_i32);
+    return taken;
+}
+
+static void compute_weights(og_graph* g, int64_t* npos_out) {
+    int64_t n = g->n;
+    free(g->w);
+    free(g->cdf);
+    g->w = (float*)malloc(sizeof(float) * (size_t)n);
+    g->cdf = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)n);
+    g->w_n = n;
+    float wmax = 0.0f;
+    for (int64_t j = 0; j < n; j++) {
+        float a = og_logf(g->fit[j]);
+        float b = og_logf((float)(g->indeg[j] + 1));
+        float c = (float)(int32_t)(g->epoch - g->pub[j]) / g->tau_f;
+        float w = og_expf(fmaf(g->gamma_f, a, fmaf(g->alpha_f, b, -c)));
+        g->w[j] = w;
+        if (w > wmax) wmax = w;
+    }
+    /* fixed-point shift: q_j = floor(w_j 2^s) < 2^(62 - ceil(log2 n)) */
+    int ex = (int)((bits_of_f(wmax) >> 23) & 0xFF) - 126;
+    int cl = 0;
+    while (cl < 63 && ((uint64_t)1 << cl) < (uint64_t)n) cl++;
+    int s = 62 - ex - cl;
+    g->shift = s;
+    double scale = d_from_bits((uint64_t)(s + 1023) << 52);
+    uint64_t acc = 0;
+    int64_t npos = 0;
+    for (int64_t j = 0; j < n; j++) {
+        uint64_t q = 0;
+        if (g->w[j] > 0.0f) {
+            q = (uint64_t)((double)g->w[j] * scale);
+            if (q == 0) q = 1;
+            npos++;
+        }
+        acc += q;
+        g->cdf[j] = acc;
+    }
+    *npos_out = npos;
+}
+
+int og_pa_epoch(og_graph* g, int threads) {
+    if (g->n <= 0) return 6;
+    int64_t n = g->n;
+    int64_t delta = g->growth_rate > 0 ? (int64_t)ceil((double)n * g->growth_rate) : g->fixed_new;
+    if (delta <= 0) return 3;
+    int64_t npos;
+    compute_weights(g, &npos);
+    if (npos == 0) return 3;
+    int32_t* rows = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta * 256);
+    int32_t* arr = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta * 256);
+    int32_t* kk = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta);
+    int64_t rows_exp = 0, elems = 0;
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel reduction(+ : rows_exp, elems)
+    {
+        keyvec kv = {0, 0, 0};
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t a = 0; a < delta; a++) {
+            int64_t cnt[2] = {0, 0};
+            kk[a] = sample_agent(g, a, g->w, g->cdf, g->shift, npos, rows + a * 256, arr + a * 256,
+                                 cnt, &kv);
+            rows_exp += cnt[0];
+            elems += cnt[1];
+        }
+        free(kv.v);
+    }
+    int64_t* row_off = (int64_t*)malloc(sizeof(int64_t) * (size_t)(delta + 1));
+    row_off[0] = 0;
+    for (int64_t a = 0; a < delta; a++) row_off[a + 1] = row_off[a] + kk[a];
+    int64_t e_new = row_off[delta];
+    int32_t* flat = (int32_t*)malloc(sizeof(int32_t) * (size_t)(e_new + 1));
+    free(g->arrivals);
+    g->arrivals = (int32_t*)malloc(sizeof(int32_t) * (size_t)(e_new + 1));
+    for (int64_t a = 0; a < delta; a++) {
+        memcpy(flat + row_off[a], rows + a * 256, sizeof(int32_t) * (size_t)kk[a]);
+        memcpy(g->arrivals + row_off[a], arr + a * 256, sizeof(int32_t) * (size_t)kk[a]);
+    }
+    float* nf = (float*)malloc(sizeof(float) * (size_t)delta);
+    for (int64_t a = 0; a < delta; a++)
+        nf[a] = og_fitness(g->seed, g->replica, (uint32_t)g->epoch, (uint32_t)a);
+    append_rows(g, delta, row_off, flat, (int32_t)g->epoch, nf);
+    g->stats[0] = n;
+    g->stats[1] = rows_exp;
+    g->stats[2] = elems;
+    g->stats[3] = e_new;
+    g->stats[4] = e_new;
+    g->epoch++;
+    free(rows);
+    free(arr);
+    free(kk);
+    free(row_off);
+    free(flat);
+    free(nf);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ ER epoch */
+#define OG_ER_CHUNK 65536
+
+/* Geometric-skip walk of one (new node, 2^16-id chunk) task.  Emits into out (may be NULL) and
+ * returns the number of successes. */
+static int64_t er_task(const og_graph* g, int64_t i, int64_t c, int64_t n, double inv_l,
+                       int32_t* out) {
+    int64_t lo = c * OG_ER_CHUNK, hi = lo + OG_ER_CHUNK < n ? lo + OG_ER_CHUNK : n;
+    int64_t pos = lo - 1, cnt = 0;
+    uint32_t r[4];
+    for (uint32_t d = 0;; d++) {
+        if ((d & 1u) == 0) rng(g->seed, S_ER, (uint32_t)c, (uint32_t)g->epoch, (uint32_t)i, d >> 1, r);
+        double u = (d & 1u) ? unif_d(r[2], r[3]) : unif_d(r[0], r[1]);
+        double sk = floor(og_log(u) * inv_l);
+        if (sk >= (double)(hi - pos - 1)) break;
+        pos = pos + 1 + (int64_t)sk;
+        if (out) out[cnt] = (int32_t)pos;
+        cnt++;
+    }
+    return cnt;
+}
+
+int og_er_epoch(og_graph* g, int64_t delta, double p, int threads) {
+    if (g->n <= 0) return 6;
+    if (delta <= 0 || isnan(p)) return 3;
+    if (p > 1.0) p = 1.0;
+    int64_t n = g->n;
+    int64_t chunks = (n + OG_ER_CHUNK - 1) / OG_ER_CHUNK;
+    int64_t tasks = delta * chunks;
+    int64_t* cnt = (int64_t*)calloc((size_t)tasks + 1, sizeof(int64_t));
+    double inv_l = 1.0 / og_log(1.0 - p);
+    if (threads > 0) omp_set_num_threads(threads);
+    if (p > 0.0) {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t t = 0; t < tasks; t++) cnt[t + 1] = er_task(g, t / chunks, t % chunks, n, inv_l, NULL);
+    }
+    for (int64_t t = 0; t < tasks; t++) cnt[t + 1] += cnt[t];
+    int32_t* flat = (int32_t*)malloc(sizeof(int32_t) * (size_t)(cnt[tasks] + 1));
+    if (p > 0.0) {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t t = 0; t < tasks; t++) er_task(g, t / chunks, t % chunks, n, inv_l, flat + cnt[t]);
+    }
+    int64_t* row_off = (int64_t*)malloc(sizeof(int64_t) * (size_t)(delta + 1));
+    for (int64_t a = 0; a <= delta; a++) row_off[a] = cnt[a * chunks];
+    float* nf = (float*)malloc(sizeof(float) * (size_t)delta);
+    for (int64_t a = 0; a < delta; a++)
+        nf[a] = og_fitness(g->seed, g->replica, (uint32_t)g->epoch, (uint32_t)a);
+    free(g->arrivals);
+    g->arrivals = (int32_t*)malloc(sizeof(int32_t) * (size_t)(cnt[tasks] + 1));
+    memcpy(g->arrivals, flat, sizeof(int32_t) * (size_t)cnt[tasks]);
+    append_rows(g, delta, row_off, flat, (int32_t)g->epoch, nf);
+    memset(g->stats, 0, sizeof(g->stats));
+    g->stats[3] = 0;
+    g->stats[4] = cnt[tasks];
+    g->epoch++;
+    free(cnt);
+    free(flat);
+    free(row_off);
+    free(nf);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ readers */
+int64_t og_num_nodes(const og_graph* g) { return g->n; }
+int64_t og_num_edges(const og_graph* g) { return g->m; }
+void og_copy_csr(const og_graph* g, int which, int64_t* off, int32_t* col) {
+    const int64_t* o = which ? g->bwd_off : g->fwd_off;
+    const int32_t* c = which ? g->bwd_col : g->fwd_col;
+    memcpy(off, o, sizeof(int64_t) * (size_t)(g->n + 1));
+    memcpy(col, c, sizeof(int32_t) * (size_t)g->m);
+}
+void og_copy_degrees(const og_graph* g, int32_t* indeg, int32_t* outdeg) {
+    for (int64_t i = 0; i < g->n; i++) {
+        if (indeg) indeg[i] = g->indeg[i];
+        if (outdeg) outdeg[i] = (int32_t)(g->fwd_off[i + 1] - g->fwd_off[i]);
+    }
+}
+void og_copy_nodes(const og_graph* g, int32_t* pub, float* fitness) {
+    memcpy(pub, g->pub, sizeof(int32_t) * (size_t)g->n);
+    memcpy(fitness, g->fit, sizeof(float) * (size_t)g->n);
+}
+void og_epoch_edges(const og_graph* g, int64_t* first, int64_t* count) {
+    *first = g->last_first;
+    *count = g->last_count;
+}
+void og_copy_arrivals(const og_graph* g, int32_t* cited) {
+    if (g->arrivals) memcpy(cited, g->arrivals, sizeof(int32_t) * (size_t)g->last_count);
+}
+void og_stats(const og_graph* g, int64_t* out5) { memcpy(out5, g->stats, sizeof(g->stats)); }
+int64_t og_copy_weights(const og_graph* g, float* w, uint64_t* cdf, int32_t* shift) {
+    if (w) memcpy(w, g->w, sizeof(float) * (size_t)g->w_n);
+    if (cdf) memcpy(cdf, g->cdf, sizeof(uint64_t) * (size_t)g->w_n);
+    if (shift) *shift = g->shift;
+    return g->w_n;
+}

@@ -1,0 +1,58 @@
+/*
+ * oracle.h -- CPU restatement of ParAGraph's per-epoch graph-growth step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU engine and the timed CPU
+ * baseline; the product (paragraph_gb300) never links, loads or calls it.  Only tests/, the
+ * smoke() entry of __graft_entry__.py and bench.py's CPU legs use it.
+ *
+ * Parity status: the reference ships no tests, golden vectors or fixed seeds, and it cannot be
+ * built here (it needs cuCollections, which is absent), so this restatement is pinned by the
+ * published Philox4x32-10 known-answer vectors, by libm error bounds for the elementary functions,
+ * and by distribution-level checks against independent samplers; its choice-level agreement with
+ * the reference itself is unpinned.
+ */
+#ifndef PG_ORACLE_H
+#define PG_ORACLE_H
+#include <stdint.h>
+
+typedef struct og_graph og_graph;
+
+/* elementary building blocks (independent restatements) */
+void og_philox(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);
+float og_logf(float x);
+float og_expf(float x);
+double og_log(double x);
+double og_exp(double x);
+void og_poisson_table(double lambda, uint64_t* table); /* 257 entries */
+float og_fitness(uint64_t seed, uint32_t replica, uint32_t epoch, uint32_t unit);
+
+/* graph state */
+og_graph* og_create(uint64_t seed, uint32_t replica);
+void og_destroy(og_graph* g);
+int og_load(og_graph* g, int64_t n, const int32_t* pub, const float* fitness, int64_t m,
+            const int32_t* src, const int32_t* dst);
+int og_set_params(og_graph* g, double alpha, double tau, double gamma, double beta,
+                  double mean_out_degree, double growth_rate, int64_t fixed_new_nodes,
+                  int32_t num_anchors);
+void og_set_epoch(og_graph* g, int64_t epoch);
+int64_t og_epoch(const og_graph* g);
+
+/* one step; threads <= 0 uses every OpenMP thread.  Returns 0 on success. */
+int og_pa_epoch(og_graph* g, int threads);
+int og_er_epoch(og_graph* g, int64_t delta, double p, int threads);
+
+/* readers */
+int64_t og_num_nodes(const og_graph* g);
+int64_t og_num_edges(const og_graph* g);
+void og_copy_csr(const og_graph* g, int which, int64_t* off, int32_t* col);
+void og_copy_degrees(const og_graph* g, int32_t* indeg, int32_t* outdeg);
+void og_copy_nodes(const og_graph* g, int32_t* pub, float* fitness);
+/* last epoch: first edge index (forward-CSR order) and count; arrivals in arrival order */
+void og_epoch_edges(const og_graph* g, int64_t* first, int64_t* count);
+void og_copy_arrivals(const og_graph* g, int32_t* cited);
+/* last epoch counters: nodes_weighted, rows_expanded, elems_streamed, draws, new_edges */
+void og_stats(const og_graph* g, int64_t* out5);
+/* last epoch weights w0 (float, n_pre entries) and CDF (uint64) for unit tests */
+int64_t og_copy_weights(const og_graph* g, float* w, uint64_t* cdf, int32_t* shift);
+
+#endif

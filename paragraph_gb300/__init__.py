@@ -1,0 +1,329 @@
+"""paragraph_gb300 -- GB300-native per-epoch citation-graph growth (ParAGraph's hot path).
+
+Python mirror of the C ABI in include/paragraph_gb300.h.  The compute path is the in-tree CUDA
+library paragraph_gb300/_lib/libparagraph_gb300.so (sm_103a); there is no CPU fallback: if the
+library is missing, importing the engine raises.
+
+Reference correspondence (paths inside the ParAGraph project):
+  GrowthEngine.load_graph   Graph(edgelist, nodelist) -> ParseNodelist/ParseEdgelist (src/graph.cu:336-447)
+  GrowthEngine.grow_epoch   one iteration of execute()'s epoch loop around buildOneNodeConnections_timed
+                            (src/kernel.cu:1682-1845, 1125-1586)
+  GrowthEngine.er_epoch     the ER G(n,p) step (results/slurm-8634746.out:60-73)
+  GrowthEngine.edges        new_edges_vec / WriteGraph rows (src/graph.cu:909-1003)
+  GrowthEngine.stats        EpochTiming (includes/epoch_profiler.cuh:56-103)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libparagraph_gb300.so"
+
+PG_OK, PG_ERR_CUDA, PG_ERR_CAPACITY, PG_ERR_ARG, PG_ERR_TIMEOUT, PG_ERR_IO, PG_ERR_STATE = range(7)
+PG_WEIGHTS_BASELINE, PG_WEIGHTS_REFCOMPAT = 0, 1
+MAX_OUT_DEGREE = 256
+
+# Every entry point the header declares; tests check the library exports each of them.
+EXPORTED = [
+    "pg_create", "pg_destroy", "pg_last_error", "pg_status_string", "pg_load_graph",
+    "pg_load_replicas", "pg_set_params", "pg_default_params", "pg_set_epoch", "pg_grow_epoch",
+    "pg_run_epochs", "pg_er_epoch", "pg_get_counts", "pg_epoch_edges", "pg_copy_edges",
+    "pg_copy_degrees", "pg_copy_nodes", "pg_copy_csr", "pg_copy_arrivals", "pg_set_timing",
+    "pg_get_stats", "pg_sync", "pg_check_device", "pg_philox4x32_10", "pg_poisson_table",
+    "pg_logf_host", "pg_expf_host", "pg_log_host", "pg_exp_host", "pg_version",
+]
+
+
+class PGError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+class _Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("num_replicas", C.c_int32), ("seed", C.c_uint64),
+                ("weight_model", C.c_int32), ("record_trace", C.c_int32)]
+
+
+class _Params(C.Structure):
+    _fields_ = [("alpha", C.c_double), ("tau", C.c_double), ("gamma", C.c_double),
+                ("beta", C.c_double), ("mean_out_degree", C.c_double), ("growth_rate", C.c_double),
+                ("fixed_new_nodes", C.c_int64), ("num_anchors", C.c_int32), ("reserved", C.c_int32)]
+
+
+class _ReplicaDesc(C.Structure):
+    _fields_ = [("num_nodes", C.c_int64), ("pub_epoch", C.c_void_p), ("fitness", C.c_void_p),
+                ("num_edges", C.c_int64), ("src", C.c_void_p), ("dst", C.c_void_p),
+                ("node_capacity", C.c_int64), ("edge_capacity", C.c_int64),
+                ("planned_epochs", C.c_int32), ("reserved", C.c_int32), ("params", _Params)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "epoch", "new_nodes", "new_edges", "nodes_weighted", "rows_expanded", "elems_streamed",
+        "draws", "bwd_moved", "bytes_alg", "bytes_alg_agents")] + [
+        (n, C.c_double) for n in ("ms_total", "ms_weights", "ms_setup", "ms_agents", "ms_csr", "ms_er")]
+
+
+@dataclass
+class PAParams:
+    """Baseline weight functor w_j = f_j^gamma (indeg_j+1)^alpha exp(-(t-t_j)/tau) beta^[j in N_a]."""
+    alpha: float = 1.0
+    tau: float = 5.0
+    gamma: float = 1.0
+    beta: float = 4.0
+    mean_out_degree: float = 15.0
+    growth_rate: float = 0.0
+    fixed_new_nodes: int = 5000
+    num_anchors: int = 3
+
+    def _c(self) -> _Params:
+        return _Params(self.alpha, self.tau, self.gamma, self.beta, self.mean_out_degree,
+                       self.growth_rate, int(self.fixed_new_nodes), int(self.num_anchors), 0)
+
+
+@dataclass
+class ReplicaInput:
+    pub_epoch: np.ndarray
+    fitness: np.ndarray
+    src: np.ndarray
+    dst: np.ndarray
+    params: PAParams = field(default_factory=PAParams)
+    planned_epochs: int = 1
+    node_capacity: int = 0
+    edge_capacity: int = 0
+
+
+_lib = None
+
+
+def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load the CUDA library; raises if it has not been built (no fallback path exists)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(
+            f"{p} is missing: build it with `python -m paragraph_gb300.build` "
+            "(the growth engine has no CPU fallback)")
+    lib = C.CDLL(str(p))
+    vp, i32, i64, u64 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64
+    P = C.POINTER
+    sig = {
+        "pg_create": (i32, [P(vp), P(_Config)]),
+        "pg_destroy": (None, [vp]),
+        "pg_last_error": (C.c_char_p, [vp]),
+        "pg_status_string": (C.c_char_p, [i32]),
+        "pg_load_graph": (i32, [vp, i64, vp, vp, i64, vp, vp]),
+        "pg_load_replicas": (i32, [vp, P(_ReplicaDesc), i32]),
+        "pg_set_params": (i32, [vp, i32, P(_Params)]),
+        "pg_default_params": (i32, [P(_Params)]),
+        "pg_set_epoch": (i32, [vp, i64]),
+        "pg_grow_epoch": (i32, [vp, P(i64), P(i64)]),
+        "pg_run_epochs": (i32, [vp, i32, i32, P(i64)]),
+        "pg_er_epoch": (i32, [vp, i64, C.c_double, P(i64)]),
+        "pg_get_counts": (i32, [vp, i32, P(i64), P(i64)]),
+        "pg_epoch_edges": (i32, [vp, i32, P(i64), P(i64)]),
+        "pg_copy_edges": (i32, [vp, i32, i64, i64, vp, vp]),
+        "pg_copy_degrees": (i32, [vp, i32, vp, vp]),
+        "pg_copy_nodes": (i32, [vp, i32, vp, vp]),
+        "pg_copy_csr": (i32, [vp, i32, i32, vp, vp]),
+        "pg_copy_arrivals": (i32, [vp, i32, vp]),
+        "pg_set_timing": (i32, [vp, i32]),
+        "pg_get_stats": (i32, [vp, P(_Stats)]),
+        "pg_sync": (i32, [vp]),
+        "pg_check_device": (i32, [vp]),
+        "pg_philox4x32_10": (None, [vp, vp, vp]),
+        "pg_poisson_table": (i32, [C.c_double, vp]),
+        "pg_logf_host": (C.c_float, [C.c_float]),
+        "pg_expf_host": (C.c_float, [C.c_float]),
+        "pg_log_host": (C.c_double, [C.c_double]),
+        "pg_exp_host": (C.c_double, [C.c_double]),
+        "pg_version": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def philox(counter, key) -> np.ndarray:
+    """Philox4x32-10 block of the library (host build of the shared header)."""
+    lib = load_library()
+    c = np.ascontiguousarray(counter, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib.pg_philox4x32_10(_ptr(c), _ptr(k), _ptr(out))
+    return out
+
+
+def poisson_table(lam: float) -> np.ndarray:
+    lib = load_library()
+    t = np.zeros(MAX_OUT_DEGREE + 1, np.uint64)
+    if lib.pg_poisson_table(float(lam), _ptr(t)) != PG_OK:
+        raise PGError(PG_ERR_ARG, "bad lambda")
+    return t
+
+
+class GrowthEngine:
+    """One device context holding R replicas (R == 1: the drop-in growth step)."""
+
+    def __init__(self, seed: int = 42, replicas: int = 1, device: int = 0,
+                 record_trace: bool = False, weight_model: int = PG_WEIGHTS_BASELINE):
+        self._lib = load_library()
+        self._ctx = C.c_void_p()
+        cfg = _Config(device, replicas, seed, weight_model, 1 if record_trace else 0)
+        st = self._lib.pg_create(C.byref(self._ctx), C.byref(cfg))
+        if st != PG_OK:
+            msg = self._lib.pg_last_error(self._ctx).decode() if self._ctx else "pg_create failed"
+            self.close()
+            raise PGError(st, msg)
+        self.replicas = replicas
+        self.record_trace = record_trace
+
+    # ------------------------------------------------------------------ lifecycle
+    def close(self) -> None:
+        if getattr(self, "_ctx", None):
+            self._lib.pg_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int) -> None:
+        if st != PG_OK:
+            raise PGError(st, self._lib.pg_last_error(self._ctx).decode())
+
+    # ------------------------------------------------------------------ input
+    def load_graph(self, pub_epoch, fitness, src, dst, params: PAParams | None = None,
+                   planned_epochs: int = 1) -> None:
+        self.load_replicas([ReplicaInput(pub_epoch, fitness, src, dst, params or PAParams(),
+                                         planned_epochs)])
+
+    def load_replicas(self, reps: list[ReplicaInput]) -> None:
+        keep = []
+        descs = (_ReplicaDesc * len(reps))()
+        for d, r in zip(descs, reps):
+            pub = np.ascontiguousarray(r.pub_epoch, np.int32)
+            fit = np.ascontiguousarray(r.fitness, np.float32)
+            s = np.ascontiguousarray(r.src, np.int32)
+            t = np.ascontiguousarray(r.dst, np.int32)
+            keep += [pub, fit, s, t]
+            d.num_nodes = len(pub)
+            d.pub_epoch = pub.ctypes.data
+            d.fitness = fit.ctypes.data
+            d.num_edges = len(s)
+            d.src = s.ctypes.data if len(s) else None
+            d.dst = t.ctypes.data if len(t) else None
+            d.node_capacity = r.node_capacity
+            d.edge_capacity = r.edge_capacity
+            d.planned_epochs = r.planned_epochs
+            d.params = r.params._c()
+        self._check(self._lib.pg_load_replicas(self._ctx, descs, len(reps)))
+
+    def set_params(self, params: PAParams, replica: int = 0) -> None:
+        p = params._c()
+        self._check(self._lib.pg_set_params(self._ctx, replica, C.byref(p)))
+
+    def set_epoch(self, epoch: int) -> None:
+        self._check(self._lib.pg_set_epoch(self._ctx, epoch))
+
+    # ------------------------------------------------------------------ growth
+    def grow_epoch(self) -> tuple[int, int]:
+        nn, ne = C.c_int64(), C.c_int64()
+        self._check(self._lib.pg_grow_epoch(self._ctx, C.byref(nn), C.byref(ne)))
+        return nn.value, ne.value
+
+    def run_epochs(self, epochs: int, use_graph: bool = True) -> int:
+        ne = C.c_int64()
+        self._check(self._lib.pg_run_epochs(self._ctx, epochs, 1 if use_graph else 0, C.byref(ne)))
+        return ne.value
+
+    def er_epoch(self, delta: int, p: float) -> int:
+        ne = C.c_int64()
+        self._check(self._lib.pg_er_epoch(self._ctx, delta, p, C.byref(ne)))
+        return ne.value
+
+    # ------------------------------------------------------------------ output
+    def counts(self, replica: int = 0) -> tuple[int, int]:
+        n, m = C.c_int64(), C.c_int64()
+        self._check(self._lib.pg_get_counts(self._ctx, replica, C.byref(n), C.byref(m)))
+        return n.value, m.value
+
+    def epoch_edges(self, replica: int = 0) -> tuple[int, int]:
+        f, c = C.c_int64(), C.c_int64()
+        self._check(self._lib.pg_epoch_edges(self._ctx, replica, C.byref(f), C.byref(c)))
+        return f.value, c.value
+
+    def edges(self, first: int, count: int, replica: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        s = np.empty(count, np.int32)
+        d = np.empty(count, np.int32)
+        self._check(self._lib.pg_copy_edges(self._ctx, replica, first, count, _ptr(s), _ptr(d)))
+        return s, d
+
+    def last_epoch_edges(self, replica: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        f, c = self.epoch_edges(replica)
+        return self.edges(f, c, replica)
+
+    def degrees(self, replica: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        n, _ = self.counts(replica)
+        i = np.empty(n, np.int32)
+        o = np.empty(n, np.int32)
+        self._check(self._lib.pg_copy_degrees(self._ctx, replica, _ptr(i), _ptr(o)))
+        return i, o
+
+    def nodes(self, replica: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        n, _ = self.counts(replica)
+        p = np.empty(n, np.int32)
+        f = np.empty(n, np.float32)
+        self._check(self._lib.pg_copy_nodes(self._ctx, replica, _ptr(p), _ptr(f)))
+        return p, f
+
+    def csr(self, which: int = 0, replica: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        n, m = self.counts(replica)
+        off = np.empty(n + 1, np.int64)
+        col = np.empty(max(m, 1), np.int32)
+        self._check(self._lib.pg_copy_csr(self._ctx, replica, which, _ptr(off), _ptr(col)))
+        return off, col[:m]
+
+    def arrivals(self, replica: int = 0) -> np.ndarray:
+        _, c = self.epoch_edges(replica)
+        a = np.empty(max(c, 1), np.int32)
+        self._check(self._lib.pg_copy_arrivals(self._ctx, replica, _ptr(a)))
+        return a[:c]
+
+    def set_timing(self, enable: bool) -> None:
+        self._check(self._lib.pg_set_timing(self._ctx, 1 if enable else 0))
+
+    def stats(self) -> dict:
+        s = _Stats()
+        self._check(self._lib.pg_get_stats(self._ctx, C.byref(s)))
+        return {name: getattr(s, name) for name, _ in _Stats._fields_}
+
+    def sync(self) -> None:
+        self._check(self._lib.pg_sync(self._ctx))
+
+    def check_device(self) -> None:
+        self._check(self._lib.pg_check_device(self._ctx))

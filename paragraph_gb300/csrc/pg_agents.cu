@@ -1,0 +1,444 @@
+// pg_agents.cu -- per-agent citation sampling of the preferential-attachment epoch.
+//
+// Replaces kernelCallStage1/_warped/2/3/4 and the fused ABMKernel (src/kernel.cu:17-402,436-573;
+// device bodies src/abm.cu:376-565,577-994).  One warp owns one agent (new paper) and does:
+//   1. global race: k draws without replacement from the replica's quantised CDF.  Draw i picks the
+//      smallest j with cdf[j] - C(j) > y, where C(j) sums the weights already chosen at ids <= j;
+//      the warp searches 32-ary (32 probes per round, ballot), which gives the same j as any other
+//      search because the function is monotone and integer.  Arrival times are exponential
+//      increments E / R with R the remaining weight.
+//   2. neighbourhood race: the 2-hop undirected ball of the anchors (forward and backward rows,
+//      the reference's GetOneAndTwoHopNeighborhood semantics) is streamed with load-balanced
+//      expansion (32 neighbours' rows at a time, owner found by a shuffle search).  Each element j
+//      gets the key E_j / w_j with E_j drawn from Philox keyed by (agent, j), so duplicates in the
+//      stream share a key and the k smallest distinct keys are found without deduplicating the
+//      ball and without depending on traversal order -- the Efraimidis-Spirakis top-k of the
+//      reference (src/abm.cu:529-564) in exponential-clock form.
+//   3. merge: the first k distinct nodes of the two races by (time, id) are the agent's citations
+//      (weights w_j beta^[j in ball]); they are sorted and appended to the forward CSR, and each
+//      cited node's in-degree counter returns the edge's rank for the backward append.
+// No per-agent O(n) state exists (the reference clears O(n) bitmaps per agent,
+// includes/abm.cuh:178-184, src/abm.cu:722-726).
+#include "pg_engine.cuh"
+
+namespace pg {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ bool key_less(float ka, int ia, float kb, int ib) {
+    return ka < kb || (ka == kb && ia < ib);
+}
+
+template <int KCAP>
+struct AgentSmem {
+    double g_t[KCAP];
+    uint64_t c_cq[KCAP];
+    int32_t g_id[KCAP];
+    int32_t c_id[KCAP];
+    float bk[KCAP];
+    int32_t bi[KCAP];
+    int32_t out[KCAP];
+};
+
+// Offer one candidate per lane to the warp's sorted top-k list (bk, bi)[0..nb).
+template <int KCAP>
+__device__ __forceinline__ void topk_offer(bool valid, float key, int id, int k, int& nb,
+                                           AgentSmem<KCAP>& S) {
+    const int lane = lane_id();
+    bool pass = valid && (nb < k || key_less(key, id, S.bk[k - 1], S.bi[k - 1]));
+    unsigned mask = __ballot_sync(kFull, pass);
+    while (mask) {
+        const int leader = __ffs(mask) - 1;
+        const float ck = __shfl_sync(kFull, key, leader);
+        const int cid = __shfl_sync(kFull, id, leader);
+        int less_cnt = 0;
+        bool dup = false;
+        for (int i = lane; i < nb; i += 32) {
+            const int ii = S.bi[i];
+            if (ii == cid) dup = true;
+            if (key_less(S.bk[i], ii, ck, cid)) ++less_cnt;
+        }
+        if (!__any_sync(kFull, dup)) {
+            const int pos = __reduce_add_sync(kFull, less_cnt);
+            const int last = nb < k ? nb : k - 1;
+            for (int hi = last; hi > pos; hi -= 32) {
+                const int i = hi - 1 - lane;
+                const bool act = i >= pos;
+                float tk = 0.0f;
+                int ti = 0;
+                if (act) {
+                    tk = S.bk[i];
+                    ti = S.bi[i];
+                }
+                __syncwarp();
+                if (act) {
+                    S.bk[i + 1] = tk;
+                    S.bi[i + 1] = ti;
+                }
+                __syncwarp();
+            }
+            if (lane == 0) {
+                S.bk[pos] = ck;
+                S.bi[pos] = cid;
+            }
+            __syncwarp();
+            nb = nb < k ? nb + 1 : k;
+        }
+        pass = pass && lane != leader && (nb < k || key_less(key, id, S.bk[k - 1], S.bi[k - 1]));
+        mask = __ballot_sync(kFull, pass);
+    }
+}
+
+struct AgentCtx {
+    const uint64_t* cdf;
+    const float* w;
+    const int64_t* fwd_off;
+    const int32_t* fwd_col;
+    const int64_t* bwd_off;
+    const int32_t* bwd_col;
+    uint64_t seed;
+    uint32_t rep, ep, unit;
+    double beta_m1;
+};
+
+__device__ __forceinline__ void boost_key(const AgentCtx& C, bool valid, int z, float& key,
+                                          bool& ok) {
+    ok = false;
+    key = 0.0f;
+    if (valid) {
+        const float wz = C.w[z];
+        if (wz > 0.0f) {
+            const u32x4 x = draw(C.seed, kStreamBoost, C.rep, C.ep, C.unit, (uint32_t)z);
+            key = -logf_pg(u01f(x.x[0])) / wz;
+            ok = true;
+        }
+    }
+}
+
+template <int KCAP>
+__device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>& S) {
+    const int lane = lane_id();
+    const int r = replica_of_agent(A.rep, A.R, a);
+    const Replica& rp = A.rep[r];
+    const int64_t n = rp.n;
+    const int64_t al = a - rp.abase;
+    AgentCtx C;
+    C.cdf = A.cdf + rp.nbase;
+    C.w = A.w + rp.nbase;
+    C.fwd_off = A.fwd_off + rp.obase;
+    C.fwd_col = A.fwd_col + rp.ebase;
+    C.bwd_off = A.bwd_off_cur + rp.obase;
+    C.bwd_col = A.bwd_col_cur + rp.ebase;
+    C.seed = A.seed;
+    C.rep = (uint32_t)r;
+    C.ep = (uint32_t)A.st->epoch;
+    C.unit = (uint32_t)al;
+    C.beta_m1 = rp.beta_m1;
+    const int s = cdf_shift(bitsf(rp.wmax_bits), n);
+    const double scale = bitsd((uint64_t)(1023 - s) << 52);
+
+    // ---------------------------------------------------------------- 1. global race
+    uint64_t R = rp.wq_total;
+    double t = 0.0;
+    int nc = 0;
+    for (int i = 0; i < k; ++i) {
+        if (R == 0) break;
+        const u32x4 x = draw(C.seed, kStreamGlobal, C.rep, C.ep, C.unit, (uint32_t)i);
+        const double E = -log_pg(u01d(x.x[0], x.x[1]));
+        t = t + E / ((double)R * scale);
+        const uint64_t y = mulhi64(u64of(x.x[2], x.x[3]), R);
+        // 32-ary search for the smallest j in [0, n) with F(j) = cdf[j] - C(j) > y
+        int64_t lo = 0, hi = n;
+        while (true) {
+            const int64_t span = hi - lo;
+            const int64_t step = span > 32 ? (span + 31) / 32 : 1;
+            int64_t p = lo + (int64_t)(lane + 1) * step - 1;
+            if (p > hi - 1) p = hi - 1;
+            // C(p): chosen weight at ids <= p
+            int cl = 0, ch = nc;
+            while (cl < ch) {
+                const int mid = (cl + ch) >> 1;
+                if (S.c_id[mid] <= p)
+                    cl = mid + 1;
+                else
+                    ch = mid;
+            }
+            const uint64_t cp = cl ? S.c_cq[cl - 1] : 0;
+            const bool pred = (C.cdf[p] - cp) > y;
+            const unsigned m = __ballot_sync(kFull, pred);
+            if (m == 0) {  // F(hi-1) > y is an invariant; report instead of probing out of range
+                if (lane == 0) atomicOr(&A.st->error, kErrArg);
+                lo = 0;
+                break;
+            }
+            const int L = __ffs(m) - 1;  // lane probing hi-1 is always true
+            const int64_t pL = __shfl_sync(kFull, p, L);
+            const int64_t pL1 = __shfl_sync(kFull, p, L > 0 ? L - 1 : 0);
+            if (span <= 32) {
+                lo = pL;
+                break;
+            }
+            hi = pL + 1;
+            lo = L > 0 ? pL1 + 1 : lo;
+        }
+        const int j = (int)lo;
+        const uint64_t qj = C.cdf[j] - (j > 0 ? C.cdf[j - 1] : 0);
+        // insert j into the sorted chosen list
+        int below = 0;
+        for (int q = lane; q < nc; q += 32) below += S.c_id[q] < j ? 1 : 0;
+        const int pos = __reduce_add_sync(kFull, below);
+        for (int top = nc; top > pos; top -= 32) {
+            const int q = top - 1 - lane;
+            const bool act = q >= pos;
+            int tid = 0;
+            uint64_t tq = 0;
+            if (act) {
+                tid = S.c_id[q];
+                tq = S.c_cq[q];
+            }
+            __syncwarp();
+            if (act) {
+                S.c_id[q + 1] = tid;
+                S.c_cq[q + 1] = tq + qj;
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            S.c_id[pos] = j;
+            S.c_cq[pos] = (pos > 0 ? S.c_cq[pos - 1] : 0) + qj;
+            S.g_id[i] = j;
+            S.g_t[i] = t;
+        }
+        __syncwarp();
+        ++nc;
+        R -= qj;
+    }
+    const int ng = nc;
+
+    // ---------------------------------------------------------------- 2. neighbourhood race
+    int nb = 0;
+    long long rows = 0, elems = 0;
+    if (C.beta_m1 > 0.0) {
+        const int na = rp.anchors;
+        const u32x4 xa = draw(C.seed, kStreamAnchor, C.rep, C.ep, C.unit, 0);
+        uint32_t xr = xa.x[0];
+        if (lane == 1) xr = xa.x[1];
+        if (lane == 2) xr = xa.x[2];
+        if (lane == 3) xr = xa.x[3];
+        const int anchor = (int)bounded32(xr, (uint32_t)n);
+        {
+            float key;
+            bool ok;
+            boost_key(C, lane < na, anchor, key, ok);
+            topk_offer<KCAP>(ok, key, anchor, k, nb, S);
+        }
+        rows += na;
+        elems += na;
+        for (int ai = 0; ai < na; ++ai) {
+            const int x = __shfl_sync(kFull, anchor, ai);
+            const int64_t fb = C.fwd_off[x], fe = C.fwd_off[x + 1];
+            const int64_t bb = C.bwd_off[x], be = C.bwd_off[x + 1];
+            const int64_t lf = fe - fb;
+            const int64_t deg1 = lf + (be - bb);
+            rows += deg1;
+            elems += deg1;
+            for (int64_t base = 0; base < deg1; base += 32) {
+                const int64_t idx = base + lane;
+                const bool valid = idx < deg1;
+                int y = 0;
+                if (valid) y = idx < lf ? C.fwd_col[fb + idx] : C.bwd_col[bb + idx - lf];
+                {
+                    float key;
+                    bool ok;
+                    boost_key(C, valid, y, key, ok);
+                    topk_offer<KCAP>(ok, key, y, k, nb, S);
+                }
+                int64_t yf = 0, yb = 0, ylf = 0, ylen = 0;
+                if (valid) {
+                    yf = C.fwd_off[y];
+                    ylf = C.fwd_off[y + 1] - yf;
+                    yb = C.bwd_off[y];
+                    ylen = ylf + (C.bwd_off[y + 1] - yb);
+                }
+                const int64_t incl = warp_incl_scan<int64_t>(ylen);
+                const int64_t total = __shfl_sync(kFull, incl, 31);
+                elems += total;
+                for (int64_t pb = 0; pb < total; pb += 32) {
+                    const int64_t p = pb + lane;
+                    const bool v2 = p < total;
+                    int o = 0;
+#pragma unroll
+                    for (int b = 16; b >= 1; b >>= 1) {
+                        const int64_t iv = __shfl_sync(kFull, incl, o + b - 1);
+                        if (iv <= p) o += b;
+                    }
+                    const int64_t ex_o = __shfl_sync(kFull, incl - ylen, o);
+                    const int64_t yf_o = __shfl_sync(kFull, yf, o);
+                    const int64_t ylf_o = __shfl_sync(kFull, ylf, o);
+                    const int64_t yb_o = __shfl_sync(kFull, yb, o);
+                    int z = 0;
+                    if (v2) {
+                        const int64_t within = p - ex_o;
+                        z = within < ylf_o ? C.fwd_col[yf_o + within]
+                                           : C.bwd_col[yb_o + within - ylf_o];
+                    }
+                    float key;
+                    bool ok;
+                    boost_key(C, v2, z, key, ok);
+                    topk_offer<KCAP>(ok, key, z, k, nb, S);
+                }
+            }
+        }
+    }
+
+    // ---------------------------------------------------------------- 3. merge and emit
+    int taken = 0, gi = 0, bj = 0;
+    while (taken < k && (gi < ng || bj < nb)) {
+        const double tb = bj < nb ? (double)S.bk[bj] / C.beta_m1 : 0.0;
+        const bool take_g =
+            bj >= nb || (gi < ng && (S.g_t[gi] < tb || (S.g_t[gi] == tb && S.g_id[gi] <= S.bi[bj])));
+        const int id = take_g ? S.g_id[gi] : S.bi[bj];
+        if (take_g)
+            ++gi;
+        else
+            ++bj;
+        bool dup = false;
+        for (int q = lane; q < taken; q += 32) dup |= (S.out[q] == id);
+        if (!__any_sync(kFull, dup)) {
+            if (lane == 0) S.out[taken] = id;
+            __syncwarp();
+            ++taken;
+        }
+    }
+    if (taken != k && lane == 0) atomicOr(&A.st->error, kErrArg);
+
+    const int64_t e0 = A.eoff[a];
+    if (A.arrivals)
+        for (int q = lane; q < taken; q += 32) A.arrivals[e0 + q] = S.out[q];
+    // bitonic sort of out[0..P)
+    int P = 1;
+    while (P < taken) P <<= 1;
+    for (int q = lane; q < P; q += 32)
+        if (q >= taken) S.out[q] = 0x7fffffff;
+    __syncwarp();
+    for (int kk = 2; kk <= P; kk <<= 1) {
+        for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+            for (int q = lane; q < P; q += 32) {
+                const int qx = q ^ jj;
+                if (qx > q) {
+                    const int va = S.out[q], vb = S.out[qx];
+                    const bool up = (q & kk) == 0;
+                    if ((va > vb) == up) {
+                        S.out[q] = vb;
+                        S.out[qx] = va;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    const int64_t row0 = rp.m + (e0 - A.eoff[rp.abase]);
+    int32_t* fcol = A.fwd_col + rp.ebase;
+    for (int q = lane; q < taken; q += 32) {
+        const int d = S.out[q];
+        fcol[row0 + q] = d;
+        A.e_dst[e0 + q] = d;
+        A.e_rank[e0 + q] = atomicAdd(&A.inc[rp.nbase + d], 1);
+    }
+    if (lane == 0) {
+        A.fwd_off[rp.obase + n + al + 1] = row0 + taken;
+        atomicAdd(&A.st->rows_expanded, (unsigned long long)rows);
+        atomicAdd(&A.st->elems_streamed, (unsigned long long)elems);
+        atomicAdd(&A.st->draws, (unsigned long long)ng);
+    }
+    __syncwarp();
+}
+
+// ---------------------------------------------------------------- setup: out-degree + new nodes
+__global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
+    if (A.st->error) return;
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= agents) return;
+    const int r = replica_of_agent(A.rep, A.R, a);
+    const Replica& rp = A.rep[r];
+    const int64_t al = a - rp.abase;
+    const uint32_t ep = (uint32_t)A.st->epoch;
+    const u32x4 x = draw(A.seed, kStreamOutDegree, (uint32_t)r, ep, (uint32_t)al, 0);
+    const int kraw = poisson_draw(A.tables + (int64_t)r * kTableEntries, kTableEntries,
+                                  u64of(x.x[0], x.x[1]));
+    int64_t k = kraw < 1 ? 1 : kraw;
+    if (k > rp.n) k = rp.n;
+    if (k > rp.npos) k = rp.npos;
+    A.kk[a] = (int32_t)k;
+    if (k > kKSmall) {
+        const unsigned long long i = atomicAdd(&A.st->big_count, 1ull);
+        A.big_list[i] = (int32_t)a;
+    }
+    const int64_t slot = rp.nbase + rp.n + al;
+    A.pub[slot] = (int32_t)A.st->epoch;
+    A.fit[slot] = lognormal_fitness(A.seed, (uint32_t)r, ep, (uint32_t)al);
+    A.indeg[slot] = 0;
+}
+
+// After the edge-offset scan: totals and capacity checks.
+__global__ void k_edges_check(Arena A, int64_t agents) {
+    if (A.st->error) return;
+    const int64_t E = A.eoff[agents];
+    if (threadIdx.x == 0) {
+        A.st->edges = E;
+        if (E > A.edge_cap) atomicOr(&A.st->error, kErrCapacity);
+    }
+    for (int r = threadIdx.x; r < A.R; r += blockDim.x) {
+        const Replica& rp = A.rep[r];
+        const int64_t er = A.eoff[rp.abase + rp.delta] - A.eoff[rp.abase];
+        if (rp.m + er > rp.m_cap) atomicOr(&A.st->error, kErrCapacity);
+    }
+}
+
+template <int KCAP, bool BIG>
+__global__ void __launch_bounds__(kAgentWarps * 32) k_agents(Arena A, int64_t agents) {
+    __shared__ AgentSmem<KCAP> smem[kAgentWarps];
+    if (A.st->error) return;
+    AgentSmem<KCAP>& S = smem[threadIdx.x >> 5];
+    const int lane = lane_id();
+    const int64_t limit = BIG ? (int64_t)A.st->big_count : agents;
+    while (true) {
+        long long q = 0;
+        if (lane == 0)
+            q = (long long)atomicAdd(BIG ? &A.st->queue_big : &A.st->queue_small, 1ull);
+        q = __shfl_sync(kFull, q, 0);
+        if (q >= limit) break;
+        const int64_t a = BIG ? (int64_t)A.big_list[q] : q;
+        const int k = A.kk[a];
+        if (!BIG && k > KCAP) continue;
+        process_agent<KCAP>(A, a, k, S);
+    }
+}
+
+static int g_blocks_small = 0, g_blocks_big = 0;
+
+void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s) {
+    if (agents <= 0) return;
+    k_agent_setup<<<(unsigned)((agents + 255) / 256), 256, 0, s>>>(A, agents);
+    launch_scan_i32_to_i64(A.kk, A.eoff, agents, A.blocksum, s);
+    k_edges_check<<<1, 256, 0, s>>>(A, agents);
+}
+
+void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) {
+    if (agents <= 0) return;
+    if (!g_blocks_small) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_small, k_agents<kKSmall, false>,
+                                                      kAgentWarps * 32, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_big, k_agents<kKMax, true>,
+                                                      kAgentWarps * 32, 0);
+        if (g_blocks_small < 1) g_blocks_small = 1;
+        if (g_blocks_big < 1) g_blocks_big = 1;
+    }
+    int64_t need = (agents + kAgentWarps - 1) / kAgentWarps;
+    int64_t grid = (int64_t)num_sms * g_blocks_small;
+    if (grid > need) grid = need;
+    k_agents<kKSmall, false><<<(unsigned)grid, kAgentWarps * 32, 0, s>>>(A, agents);
+    k_agents<kKMax, true><<<(unsigned)num_sms * g_blocks_big, kAgentWarps * 32, 0, s>>>(A, agents);
+}
+
+}  // namespace pg

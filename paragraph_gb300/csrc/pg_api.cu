@@ -1,0 +1,1024 @@
+// pg_api.cu -- host side of the C ABI: context, device arena, epoch sequencing.
+//
+// Replaces the host orchestration around buildOneNodeConnections_timed (src/kernel.cu:1125-1586):
+// the reference allocates and frees all device memory per call and per mini-batch, rebuilds the
+// CSR on the host every epoch and copies edges back per agent.  Here the graph stays resident in
+// one arena sized once (capacities planned from the growth rule), an epoch is a fixed sequence of
+// kernels on one stream, and a multi-epoch run can be captured once as a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/paragraph_gb300.h"
+#include "pg_engine.cuh"
+
+using namespace pg;
+
+namespace {
+
+struct HostRep {
+    int64_t nbase, obase, ebase, n_cap, m_cap, n, m;
+    int32_t tbase, ntiles;
+    pg_pa_params prm;
+};
+
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    int64_t n = 0;
+};
+
+struct Checkpoint {
+    bool valid = false;
+    int64_t epoch = 0;
+    int parity = 0;
+    std::vector<HostRep> hrep;
+    DBuf<int32_t> pub, indeg, fwd_col, bwd_col;
+    DBuf<float> fit;
+    DBuf<int64_t> fwd_off, bwd_off;
+    DBuf<Replica> rep;
+};
+
+}  // namespace
+
+struct pg_ctx {
+    pg_config cfg{};
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    int R = 1;
+    bool loaded = false;
+    bool poisoned = false;  // a kernel reported an error mid-epoch; reload before growing again
+    int64_t epoch = 0;
+    int parity = 0;  // which backward buffer is current
+    std::vector<HostRep> hrep;
+    int64_t S = 0, T = 0, M = 0;  // slots, tiles, edge slots
+    int64_t agent_cap = 0, edge_cap = 0, blocks_cap = 0;
+    // device buffers
+    DBuf<Replica> rep;
+    DBuf<EpochState> st;
+    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, e_dst, e_rank, arrivals;
+    DBuf<float> fit, w;
+    DBuf<uint64_t> cdf, tilesum, tileoff, tables;
+    DBuf<int64_t> fwd_off, bwd_off[2], len_tmp, sort_small, sort_large, sort_large_off, eoff,
+        blocksum, er_cnt, er_toff;
+    DBuf<int32_t> fwd_col, bwd_col[2];
+    // host mirror of the last epoch
+    EpochState h_st{};
+    std::vector<Replica> h_rep;
+    pg_stats stats{};
+    int64_t last_first = 0, last_count = 0;  // replica 0 bookkeeping is per replica below
+    std::vector<int64_t> rep_last_first, rep_last_count;
+    bool timing = true;
+    cudaEvent_t ev[6] = {};
+    // CUDA graph of a multi-epoch run
+    cudaGraphExec_t gexec = nullptr;
+    int64_t g_epoch0 = -1;
+    int g_parity0 = -1, g_epochs = 0;
+    Checkpoint ckpt;
+    std::string err;
+};
+
+namespace {
+
+pg_status fail(pg_ctx* c, pg_status s, const std::string& msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+#define PG_CUDA(ctx, call)                                                                        \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(ctx, PG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(DBuf<T>& b, int64_t n) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+    if (n <= 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)&b.p, sizeof(T) * (size_t)n);
+    if (e == cudaSuccess) b.n = n;
+    return e;
+}
+
+template <typename T>
+void dfree(DBuf<T>& b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+}
+
+int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+int64_t delta_of(const pg_pa_params& p, int64_t n) {
+    if (p.growth_rate > 0.0) return (int64_t)std::ceil((double)n * p.growth_rate);
+    return p.fixed_new_nodes > 0 ? p.fixed_new_nodes : 0;
+}
+
+// Upper bound on one epoch's edges for d agents (Poisson(lambda) out-degree clipped to
+// [1, min(256, n)]): mean + 8 standard deviations, never above the hard bound.
+int64_t edge_bound(int64_t d, double lambda, int64_t n) {
+    if (d <= 0) return 0;
+    const double mu = (double)d * (lambda + 1.0);
+    const int64_t stat = (int64_t)std::ceil(mu + 8.0 * std::sqrt(mu) + 64.0);
+    const int64_t hard = d * std::min<int64_t>(kKMax, std::max<int64_t>(n, 1));
+    return std::min(stat, hard);
+}
+
+Arena make_arena(pg_ctx* c) {
+    Arena A{};
+    A.rep = c->rep.p;
+    A.R = c->R;
+    A.ntiles = (int32_t)c->T;
+    A.tile_rep = c->tile_rep.p;
+    A.pub = c->pub.p;
+    A.fit = c->fit.p;
+    A.indeg = c->indeg.p;
+    A.w = c->w.p;
+    A.cdf = c->cdf.p;
+    A.inc = c->inc.p;
+    A.fwd_off = c->fwd_off.p;
+    A.fwd_col = c->fwd_col.p;
+    A.bwd_off_cur = c->bwd_off[c->parity].p;
+    A.bwd_col_cur = c->bwd_col[c->parity].p;
+    A.bwd_off_nxt = c->bwd_off[c->parity ^ 1].p;
+    A.bwd_col_nxt = c->bwd_col[c->parity ^ 1].p;
+    A.tables = c->tables.p;
+    A.kk = c->kk.p;
+    A.eoff = c->eoff.p;
+    A.e_dst = c->e_dst.p;
+    A.e_rank = c->e_rank.p;
+    A.arrivals = c->cfg.record_trace ? c->arrivals.p : nullptr;
+    A.big_list = c->big_list.p;
+    A.len_tmp = c->len_tmp.p;
+    A.tilesum = c->tilesum.p;
+    A.tileoff = c->tileoff.p;
+    A.blocksum = c->blocksum.p;
+    A.sort_small = c->sort_small.p;
+    A.sort_large = c->sort_large.p;
+    A.sort_large_off = c->sort_large_off.p;
+    A.st = c->st.p;
+    A.agent_cap = c->agent_cap;
+    A.edge_cap = c->edge_cap;
+    A.seed = c->cfg.seed;
+    A.record_trace = c->cfg.record_trace;
+    return A;
+}
+
+Replica to_device_rep(const HostRep& h) {
+    Replica r{};
+    r.nbase = h.nbase;
+    r.obase = h.obase;
+    r.ebase = h.ebase;
+    r.n_cap = h.n_cap;
+    r.m_cap = h.m_cap;
+    r.n = h.n;
+    r.m = h.m;
+    r.tbase = h.tbase;
+    r.ntiles = h.ntiles;
+    r.alpha = (float)h.prm.alpha;
+    r.gamma = (float)h.prm.gamma;
+    r.tau = (float)h.prm.tau;
+    r.beta_m1 = h.prm.beta - 1.0;
+    r.growth_rate = h.prm.growth_rate;
+    r.fixed_new = h.prm.fixed_new_nodes;
+    r.anchors = h.prm.num_anchors;
+    return r;
+}
+
+pg_status check_params(pg_ctx* c, const pg_pa_params& p) {
+    if (!(p.tau > 0.0)) return fail(c, PG_ERR_ARG, "tau must be > 0");
+    if (!(p.beta >= 1.0)) return fail(c, PG_ERR_ARG, "beta must be >= 1");
+    if (!(p.mean_out_degree >= 0.0) || p.mean_out_degree > 200.0)
+        return fail(c, PG_ERR_ARG, "mean_out_degree must be in [0, 200]");
+    if (p.num_anchors < 1 || p.num_anchors > PG_MAX_ANCHORS)
+        return fail(c, PG_ERR_ARG, "num_anchors must be in [1, 4]");
+    if (!(p.growth_rate > 0.0) && p.fixed_new_nodes <= 0)
+        return fail(c, PG_ERR_ARG, "need growth_rate > 0 or fixed_new_nodes > 0");
+    if (!std::isfinite(p.alpha) || !std::isfinite(p.gamma))
+        return fail(c, PG_ERR_ARG, "alpha and gamma must be finite");
+    return PG_OK;
+}
+
+// Sorted, duplicate-free CSR from an edge list (Graph::AddEdge set semantics).
+void host_csr(int64_t n, int64_t m, const int32_t* src, const int32_t* dst,
+              std::vector<int64_t>& off, std::vector<int32_t>& col) {
+    off.assign((size_t)n + 1, 0);
+    for (int64_t e = 0; e < m; ++e) off[(size_t)src[e] + 1]++;
+    for (int64_t v = 0; v < n; ++v) off[(size_t)v + 1] += off[(size_t)v];
+    col.resize((size_t)std::max<int64_t>(m, 1));
+    std::vector<int64_t> cur(off.begin(), off.end() - 1);
+    for (int64_t e = 0; e < m; ++e) col[(size_t)cur[(size_t)src[e]]++] = dst[e];
+    int64_t wpos = 0;
+    for (int64_t v = 0; v < n; ++v) {
+        const int64_t b = off[(size_t)v], e = off[(size_t)v + 1];
+        std::sort(col.begin() + b, col.begin() + e);
+        off[(size_t)v] = wpos;
+        for (int64_t i = b; i < e; ++i)
+            if (i == b || col[(size_t)i] != col[(size_t)i - 1]) col[(size_t)wpos++] = col[(size_t)i];
+    }
+    off[(size_t)n] = wpos;
+    col.resize((size_t)std::max<int64_t>(wpos, 1));
+}
+
+// Backward CSR (in-edges) of a forward CSR; rows come out ascending because sources are visited
+// in order.
+void host_transpose(int64_t n, const std::vector<int64_t>& fo, const std::vector<int32_t>& fc,
+                    std::vector<int64_t>& bo, std::vector<int32_t>& bc) {
+    const int64_t m = fo[(size_t)n];
+    bo.assign((size_t)n + 1, 0);
+    for (int64_t i = 0; i < m; ++i) bo[(size_t)fc[(size_t)i] + 1]++;
+    for (int64_t v = 0; v < n; ++v) bo[(size_t)v + 1] += bo[(size_t)v];
+    bc.resize((size_t)std::max<int64_t>(m, 1));
+    std::vector<int64_t> cur(bo.begin(), bo.end() - 1);
+    for (int64_t v = 0; v < n; ++v)
+        for (int64_t i = fo[(size_t)v]; i < fo[(size_t)v + 1]; ++i)
+            bc[(size_t)cur[(size_t)fc[(size_t)i]]++] = (int32_t)v;
+}
+
+void destroy_graph_exec(pg_ctx* c) {
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+    c->g_epoch0 = -1;
+}
+
+pg_status alloc_epoch_buffers(pg_ctx* c, int64_t agent_cap, int64_t edge_cap, int64_t tasks) {
+    const int64_t scan_n = std::max<int64_t>(std::max<int64_t>(agent_cap, tasks), 1);
+    const int64_t blocks = scan_blocks_needed(scan_n) + 2;
+    if (agent_cap > c->agent_cap) {
+        PG_CUDA(c, dalloc(c->kk, agent_cap));
+        PG_CUDA(c, dalloc(c->big_list, agent_cap));
+        PG_CUDA(c, dalloc(c->eoff, agent_cap + 1));
+        c->agent_cap = agent_cap;
+    }
+    if (edge_cap > c->edge_cap) {
+        PG_CUDA(c, dalloc(c->e_dst, edge_cap));
+        PG_CUDA(c, dalloc(c->e_rank, edge_cap));
+        if (c->cfg.record_trace) PG_CUDA(c, dalloc(c->arrivals, edge_cap));
+        c->edge_cap = edge_cap;
+    }
+    if (blocks > c->blocks_cap) {
+        PG_CUDA(c, dalloc(c->blocksum, blocks));
+        c->blocks_cap = blocks;
+    }
+    return PG_OK;
+}
+
+// (Re)build the whole arena from host CSRs.  Used at load and when an R == 1 context grows.
+struct HostGraph {
+    std::vector<int32_t> pub, indeg;
+    std::vector<float> fit;
+    std::vector<int64_t> fo, bo;
+    std::vector<int32_t> fc, bc;
+};
+
+pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<HostGraph>& hg) {
+    const int R = (int)reps.size();
+    int64_t S = 0, T = 0, M = 0;
+    for (int r = 0; r < R; ++r) {
+        HostRep& h = reps[r];
+        h.n_cap = round_up(std::max<int64_t>(h.n_cap, h.n + 1), kTile);
+        h.nbase = S;
+        h.obase = S + r;
+        h.ebase = M;
+        h.tbase = (int32_t)T;
+        h.ntiles = (int32_t)(h.n_cap / kTile);
+        S += h.n_cap;
+        T += h.ntiles;
+        M += std::max<int64_t>(h.m_cap, h.m + 1);
+        h.m_cap = std::max<int64_t>(h.m_cap, h.m + 1);
+    }
+    c->S = S;
+    c->T = T;
+    c->M = M;
+    destroy_graph_exec(c);
+    c->ckpt.valid = false;
+    PG_CUDA(c, dalloc(c->rep, R));
+    PG_CUDA(c, dalloc(c->tile_rep, T));
+    PG_CUDA(c, dalloc(c->tilesum, std::max<int64_t>(T, R) + 1));
+    PG_CUDA(c, dalloc(c->tileoff, T + 1));
+    PG_CUDA(c, dalloc(c->pub, S));
+    PG_CUDA(c, dalloc(c->fit, S));
+    PG_CUDA(c, dalloc(c->indeg, S));
+    PG_CUDA(c, dalloc(c->inc, S));
+    PG_CUDA(c, dalloc(c->w, S));
+    PG_CUDA(c, dalloc(c->cdf, S));
+    PG_CUDA(c, dalloc(c->len_tmp, S));
+    PG_CUDA(c, dalloc(c->sort_small, S));
+    PG_CUDA(c, dalloc(c->sort_large, S));
+    PG_CUDA(c, dalloc(c->sort_large_off, S));
+    PG_CUDA(c, dalloc(c->fwd_off, S + R));
+    PG_CUDA(c, dalloc(c->bwd_off[0], S + R));
+    PG_CUDA(c, dalloc(c->bwd_off[1], S + R));
+    PG_CUDA(c, dalloc(c->fwd_col, M));
+    PG_CUDA(c, dalloc(c->bwd_col[0], M));
+    PG_CUDA(c, dalloc(c->bwd_col[1], M));
+    PG_CUDA(c, dalloc(c->tables, (int64_t)R * kTableEntries));
+    PG_CUDA(c, cudaMemsetAsync(c->inc.p, 0, sizeof(int32_t) * (size_t)S, c->stream));
+    PG_CUDA(c, cudaMemsetAsync(c->w.p, 0, sizeof(float) * (size_t)S, c->stream));
+    c->parity = 0;
+    std::vector<int32_t> trep((size_t)T);
+    std::vector<Replica> drep((size_t)R);
+    std::vector<uint64_t> tabs((size_t)R * kTableEntries);
+    for (int r = 0; r < R; ++r) {
+        const HostRep& h = reps[r];
+        for (int t = 0; t < h.ntiles; ++t) trep[(size_t)h.tbase + t] = r;
+        drep[(size_t)r] = to_device_rep(h);
+        poisson_table(h.prm.mean_out_degree, tabs.data() + (size_t)r * kTableEntries, kTableEntries);
+        const HostGraph& g = hg[(size_t)r];
+        const size_t n = (size_t)h.n, m = (size_t)h.m;
+        PG_CUDA(c, cudaMemcpyAsync(c->pub.p + h.nbase, g.pub.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase, g.fit.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(c->indeg.p + h.nbase, g.indeg.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(c->fwd_off.p + h.obase, g.fo.data(), 8 * (n + 1), cudaMemcpyHostToDevice, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(c->bwd_off[0].p + h.obase, g.bo.data(), 8 * (n + 1), cudaMemcpyHostToDevice, c->stream));
+        if (m) {
+            PG_CUDA(c, cudaMemcpyAsync(c->fwd_col.p + h.ebase, g.fc.data(), 4 * m, cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(c->bwd_col[0].p + h.ebase, g.bc.data(), 4 * m, cudaMemcpyHostToDevice, c->stream));
+        }
+    }
+    PG_CUDA(c, cudaMemcpyAsync(c->tile_rep.p, trep.data(), 4 * (size_t)T, cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(c->rep.p, drep.data(), sizeof(Replica) * (size_t)R, cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(c->tables.p, tabs.data(), 8 * tabs.size(), cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaMemsetAsync(c->st.p, 0, sizeof(EpochState), c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->hrep = reps;
+    c->R = R;
+    c->loaded = true;
+    c->poisoned = false;
+    c->rep_last_first.assign((size_t)R, 0);
+    c->rep_last_count.assign((size_t)R, 0);
+    return PG_OK;
+}
+
+// Host copy of replica r's current graph (used when an R == 1 context grows).
+pg_status download_graph(pg_ctx* c, int r, HostGraph& g) {
+    const HostRep& h = c->hrep[(size_t)r];
+    const size_t n = (size_t)h.n, m = (size_t)h.m;
+    g.pub.resize(n);
+    g.fit.resize(n);
+    g.indeg.resize(n);
+    g.fo.resize(n + 1);
+    g.bo.resize(n + 1);
+    g.fc.resize(std::max<size_t>(m, 1));
+    g.bc.resize(std::max<size_t>(m, 1));
+    PG_CUDA(c, cudaMemcpyAsync(g.pub.data(), c->pub.p + h.nbase, 4 * n, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(g.fit.data(), c->fit.p + h.nbase, 4 * n, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(g.indeg.data(), c->indeg.p + h.nbase, 4 * n, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(g.fo.data(), c->fwd_off.p + h.obase, 8 * (n + 1), cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(g.bo.data(), c->bwd_off[c->parity].p + h.obase, 8 * (n + 1), cudaMemcpyDeviceToHost, c->stream));
+    if (m) {
+        PG_CUDA(c, cudaMemcpyAsync(g.fc.data(), c->fwd_col.p + h.ebase, 4 * m, cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(g.bc.data(), c->bwd_col[c->parity].p + h.ebase, 4 * m, cudaMemcpyDeviceToHost, c->stream));
+    }
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+// Make sure an R == 1 context can hold `need_n` nodes and `need_m` edges.
+pg_status ensure_capacity(pg_ctx* c, int64_t need_n, int64_t need_m) {
+    HostRep& h = c->hrep[0];
+    if (need_n <= h.n_cap && need_m <= h.m_cap) return PG_OK;
+    if (c->R != 1) return fail(c, PG_ERR_CAPACITY, "replica capacity exceeded (plan more epochs)");
+    HostGraph g;
+    pg_status s = download_graph(c, 0, g);
+    if (s != PG_OK) return s;
+    std::vector<HostRep> reps = c->hrep;
+    reps[0].n_cap = std::max<int64_t>(need_n, h.n_cap + h.n_cap / 2);
+    reps[0].m_cap = std::max<int64_t>(need_m, h.m_cap + h.m_cap / 2);
+    std::vector<HostGraph> hg(1);
+    hg[0] = std::move(g);
+    return upload_arena(c, reps, hg);
+}
+
+pg_status read_back(pg_ctx* c) {
+    PG_CUDA(c, cudaMemcpyAsync(&c->h_st, c->st.p, sizeof(EpochState), cudaMemcpyDeviceToHost, c->stream));
+    c->h_rep.resize((size_t)c->R);
+    PG_CUDA(c, cudaMemcpyAsync(c->h_rep.data(), c->rep.p, sizeof(Replica) * (size_t)c->R,
+                               cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status device_error(pg_ctx* c) {
+    const uint32_t e = c->h_st.error;
+    if (!e) return PG_OK;
+    c->poisoned = true;
+    std::string msg = "device reported:";
+    if (e & kErrCapacity) msg += " capacity exceeded;";
+    if (e & kErrBadWeight) msg += " non-finite or all-zero weights;";
+    if (e & kErrArg) msg += " inconsistent agent draw;";
+    return fail(c, (e & kErrCapacity) ? PG_ERR_CAPACITY : PG_ERR_ARG, msg);
+}
+
+float ms_between(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.0f;
+    return ms;
+}
+
+// Enqueue one PA epoch (no synchronisation).  agents = total new nodes of the epoch.
+void enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, bool events) {
+    Arena A = make_arena(c);
+    cudaStream_t s = c->stream;
+    if (events) cudaEventRecord(c->ev[0], s);
+    launch_epoch_begin(A, epoch, 1, s);
+    launch_weights(A, s);
+    if (events) cudaEventRecord(c->ev[1], s);
+    launch_agent_setup(A, agents, s);
+    if (events) cudaEventRecord(c->ev[2], s);
+    launch_agents(A, agents, c->num_sms, s);
+    if (events) cudaEventRecord(c->ev[3], s);
+    launch_bwd_append(A, agents, c->num_sms, s);
+    if (events) cudaEventRecord(c->ev[4], s);
+}
+
+// Planned agents of the next epoch and the node/edge needs of every replica.
+int64_t plan_epoch(pg_ctx* c, std::vector<int64_t>* deltas) {
+    int64_t tot = 0;
+    if (deltas) deltas->assign((size_t)c->R, 0);
+    for (int r = 0; r < c->R; ++r) {
+        const int64_t d = delta_of(c->hrep[(size_t)r].prm, c->hrep[(size_t)r].n);
+        if (deltas) (*deltas)[(size_t)r] = d;
+        tot += d;
+    }
+    return tot;
+}
+
+void fill_stats(pg_ctx* c, int64_t new_nodes, bool er) {
+    pg_stats& S = c->stats;
+    const EpochState& st = c->h_st;
+    S.epoch = st.epoch;
+    S.new_nodes = new_nodes;
+    S.new_edges = st.edges;
+    S.nodes_weighted = (int64_t)st.nodes_weighted;
+    S.rows_expanded = (int64_t)st.rows_expanded;
+    S.elems_streamed = (int64_t)st.elems_streamed;
+    S.draws = (int64_t)st.draws;
+    S.bwd_moved = (int64_t)st.bwd_moved;
+    const int64_t E = st.edges;
+    // byte model: see DESIGN.md ("Algorithmic bytes")
+    const int64_t agents_bytes = 32 * S.rows_expanded + 8 * S.elems_streamed + 32 * S.draws + 16 * E;
+    const int64_t weight_bytes = 44 * S.nodes_weighted;
+    const int64_t csr_bytes = 8 * S.bwd_moved + 12 * E + 24 * (S.nodes_weighted + new_nodes);
+    S.bytes_alg_agents = er ? 0 : agents_bytes;
+    S.bytes_alg = er ? (8 * E + 12 * E + 32 * new_nodes + 8 * S.bwd_moved) : agents_bytes + weight_bytes + csr_bytes;
+}
+
+pg_status finish_epoch(pg_ctx* c, const std::vector<int64_t>& deltas, bool er) {
+    pg_status s = read_back(c);
+    if (s != PG_OK) return s;
+    s = device_error(c);
+    if (s != PG_OK) return s;
+    int64_t nn = 0;
+    for (int r = 0; r < c->R; ++r) {
+        HostRep& h = c->hrep[(size_t)r];
+        c->rep_last_first[(size_t)r] = h.m;
+        h.n = c->h_rep[(size_t)r].n;
+        h.m = c->h_rep[(size_t)r].m;
+        c->rep_last_count[(size_t)r] = h.m - c->rep_last_first[(size_t)r];
+        nn += deltas[(size_t)r];
+    }
+    c->parity ^= 1;
+    c->epoch += 1;
+    fill_stats(c, nn, er);
+    return PG_OK;
+}
+
+pg_status prepare_pa(pg_ctx* c, std::vector<int64_t>& deltas, int64_t& agents) {
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (c->poisoned) return fail(c, PG_ERR_STATE, "an earlier epoch failed on the device; reload the graph");
+    agents = plan_epoch(c, &deltas);
+    if (agents <= 0) return fail(c, PG_ERR_ARG, "epoch adds no nodes");
+    int64_t ebound = 0;
+    for (int r = 0; r < c->R; ++r) {
+        const HostRep& h = c->hrep[(size_t)r];
+        const int64_t eb = edge_bound(deltas[(size_t)r], h.prm.mean_out_degree, h.n);
+        ebound += eb;
+        if (c->R == 1) {
+            pg_status s = ensure_capacity(c, h.n + deltas[(size_t)r], h.m + eb);
+            if (s != PG_OK) return s;
+        }
+    }
+    return alloc_epoch_buffers(c, agents, ebound, 0);
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+const char* pg_version(void) { return "paragraph_gb300 0.1 (sm_103a)"; }
+
+const char* pg_status_string(pg_status s) {
+    switch (s) {
+        case PG_OK: return "ok";
+        case PG_ERR_CUDA: return "CUDA error";
+        case PG_ERR_CAPACITY: return "capacity exceeded";
+        case PG_ERR_ARG: return "invalid argument";
+        case PG_ERR_TIMEOUT: return "device wait timed out";
+        case PG_ERR_IO: return "I/O error";
+        case PG_ERR_STATE: return "invalid state";
+    }
+    return "unknown status";
+}
+
+const char* pg_last_error(const pg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+pg_status pg_default_params(pg_pa_params* out) {
+    if (!out) return PG_ERR_ARG;
+    std::memset(out, 0, sizeof(*out));
+    out->alpha = 1.0;
+    out->tau = 5.0;
+    out->gamma = 1.0;
+    out->beta = 4.0;
+    out->mean_out_degree = 15.0;
+    out->growth_rate = 0.0;
+    out->fixed_new_nodes = 5000;
+    out->num_anchors = 3;
+    return PG_OK;
+}
+
+pg_status pg_create(pg_ctx** out, const pg_config* cfg) {
+    if (!out || !cfg) return PG_ERR_ARG;
+    *out = nullptr;
+    if (cfg->num_replicas < 1) return PG_ERR_ARG;
+    pg_ctx* c = new (std::nothrow) pg_ctx();
+    if (!c) return PG_ERR_CAPACITY;
+    c->cfg = *cfg;
+    c->R = cfg->num_replicas;
+    c->device = cfg->device;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = dalloc(c->st, 1);
+    for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+    if (e != cudaSuccess) {
+        c->err = std::string("CUDA initialisation failed: ") + cudaGetErrorString(e);
+        *out = c;
+        return PG_ERR_CUDA;
+    }
+    *out = c;
+    return PG_OK;
+}
+
+void pg_destroy(pg_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    destroy_graph_exec(c);
+    DBuf<int32_t>* i32[] = {&c->tile_rep, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list,
+                            &c->e_dst, &c->e_rank, &c->arrivals, &c->fwd_col, &c->bwd_col[0],
+                            &c->bwd_col[1], &c->ckpt.pub, &c->ckpt.indeg, &c->ckpt.fwd_col,
+                            &c->ckpt.bwd_col};
+    for (auto* b : i32) dfree(*b);
+    DBuf<int64_t>* i64[] = {&c->fwd_off, &c->bwd_off[0], &c->bwd_off[1], &c->len_tmp,
+                            &c->sort_small, &c->sort_large, &c->sort_large_off, &c->eoff,
+                            &c->blocksum, &c->er_cnt, &c->er_toff, &c->ckpt.fwd_off,
+                            &c->ckpt.bwd_off};
+    for (auto* b : i64) dfree(*b);
+    dfree(c->fit);
+    dfree(c->w);
+    dfree(c->ckpt.fit);
+    dfree(c->cdf);
+    dfree(c->tilesum);
+    dfree(c->tileoff);
+    dfree(c->tables);
+    dfree(c->rep);
+    dfree(c->ckpt.rep);
+    dfree(c->st);
+    for (int i = 0; i < 6; ++i)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+pg_status pg_load_replicas(pg_ctx* c, const pg_replica_desc* descs, int32_t num) {
+    if (!c) return PG_ERR_ARG;
+    if (!descs || num != c->cfg.num_replicas) return fail(c, PG_ERR_ARG, "need one descriptor per replica");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    std::vector<HostRep> reps((size_t)num);
+    std::vector<HostGraph> hg((size_t)num);
+    int64_t max_agents = 0, max_edges = 0;
+    const int max_plan = 1 << 20;
+    std::vector<int64_t> plan_agents, plan_edges;
+    for (int r = 0; r < num; ++r) {
+        const pg_replica_desc& d = descs[r];
+        pg_status s = check_params(c, d.params);
+        if (s != PG_OK) return s;
+        if (d.num_nodes <= 0 || d.num_nodes > (int64_t)INT32_MAX / 2) return fail(c, PG_ERR_ARG, "num_nodes out of range");
+        if (d.num_edges < 0 || (d.num_edges > 0 && (!d.src || !d.dst))) return fail(c, PG_ERR_ARG, "bad edge arrays");
+        if (!d.pub_epoch || !d.fitness) return fail(c, PG_ERR_ARG, "pub_epoch and fitness are required");
+        for (int64_t e = 0; e < d.num_edges; ++e)
+            if (d.src[e] < 0 || d.src[e] >= d.num_nodes || d.dst[e] < 0 || d.dst[e] >= d.num_nodes)
+                return fail(c, PG_ERR_ARG, "edge endpoint out of range at index " + std::to_string(e));
+        HostGraph& g = hg[(size_t)r];
+        host_csr(d.num_nodes, d.num_edges, d.src, d.dst, g.fo, g.fc);
+        host_transpose(d.num_nodes, g.fo, g.fc, g.bo, g.bc);
+        g.pub.assign(d.pub_epoch, d.pub_epoch + d.num_nodes);
+        g.fit.assign(d.fitness, d.fitness + d.num_nodes);
+        g.indeg.resize((size_t)d.num_nodes);
+        for (int64_t v = 0; v < d.num_nodes; ++v) g.indeg[(size_t)v] = (int32_t)(g.bo[(size_t)v + 1] - g.bo[(size_t)v]);
+        HostRep& h = reps[(size_t)r];
+        h.prm = d.params;
+        h.n = d.num_nodes;
+        h.m = g.fo[(size_t)d.num_nodes];
+        // capacity plan
+        int64_t n = h.n, m = h.m;
+        const int epochs = std::max(1, std::min(d.planned_epochs, max_plan));
+        if ((int)plan_agents.size() < epochs) {
+            plan_agents.resize((size_t)epochs, 0);
+            plan_edges.resize((size_t)epochs, 0);
+        }
+        for (int e = 0; e < epochs; ++e) {
+            const int64_t dl = delta_of(h.prm, n);
+            const int64_t eb = edge_bound(dl, h.prm.mean_out_degree, n);
+            plan_agents[(size_t)e] += dl;
+            plan_edges[(size_t)e] += eb;
+            n += dl;
+            m += eb;
+        }
+        h.n_cap = std::max<int64_t>(d.node_capacity, n);
+        h.m_cap = std::max<int64_t>(d.edge_capacity, m);
+    }
+    for (size_t e = 0; e < plan_agents.size(); ++e) {
+        max_agents = std::max(max_agents, plan_agents[e]);
+        max_edges = std::max(max_edges, plan_edges[e]);
+    }
+    pg_status s = upload_arena(c, reps, hg);
+    if (s != PG_OK) return s;
+    c->epoch = 0;
+    return alloc_epoch_buffers(c, max_agents, max_edges, 0);
+}
+
+pg_status pg_load_graph(pg_ctx* c, int64_t n, const int32_t* pub_epoch, const float* fitness,
+                        int64_t m, const int32_t* src, const int32_t* dst) {
+    if (!c) return PG_ERR_ARG;
+    if (c->cfg.num_replicas != 1) return fail(c, PG_ERR_ARG, "pg_load_graph needs num_replicas == 1");
+    pg_replica_desc d{};
+    d.num_nodes = n;
+    d.pub_epoch = pub_epoch;
+    d.fitness = fitness;
+    d.num_edges = m;
+    d.src = src;
+    d.dst = dst;
+    d.planned_epochs = 1;
+    pg_default_params(&d.params);
+    if (c->loaded) d.params = c->hrep[0].prm;
+    return pg_load_replicas(c, &d, 1);
+}
+
+pg_status pg_set_params(pg_ctx* c, int32_t replica, const pg_pa_params* p) {
+    if (!c || !p) return PG_ERR_ARG;
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "load a graph first");
+    if (replica < 0 || replica >= c->R) return fail(c, PG_ERR_ARG, "replica out of range");
+    pg_status s = check_params(c, *p);
+    if (s != PG_OK) return s;
+    HostRep& h = c->hrep[(size_t)replica];
+    h.prm = *p;
+    destroy_graph_exec(c);
+    std::vector<uint64_t> tab(kTableEntries);
+    poisson_table(p->mean_out_degree, tab.data(), kTableEntries);
+    PG_CUDA(c, cudaMemcpyAsync(c->tables.p + (size_t)replica * kTableEntries, tab.data(), 8 * tab.size(),
+                               cudaMemcpyHostToDevice, c->stream));
+    // refresh the parameter fields of the device replica
+    Replica dr;
+    PG_CUDA(c, cudaMemcpyAsync(&dr, c->rep.p + replica, sizeof(Replica), cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    const Replica fresh = to_device_rep(h);
+    dr.alpha = fresh.alpha;
+    dr.gamma = fresh.gamma;
+    dr.tau = fresh.tau;
+    dr.beta_m1 = fresh.beta_m1;
+    dr.growth_rate = fresh.growth_rate;
+    dr.fixed_new = fresh.fixed_new;
+    dr.anchors = fresh.anchors;
+    PG_CUDA(c, cudaMemcpyAsync(c->rep.p + replica, &dr, sizeof(Replica), cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status pg_set_epoch(pg_ctx* c, int64_t epoch) {
+    if (!c) return PG_ERR_ARG;
+    c->epoch = epoch;
+    destroy_graph_exec(c);
+    return PG_OK;
+}
+
+pg_status pg_grow_epoch(pg_ctx* c, int64_t* new_nodes, int64_t* new_edges) {
+    if (!c) return PG_ERR_ARG;
+    PG_CUDA(c, cudaSetDevice(c->device));
+    std::vector<int64_t> deltas;
+    int64_t agents = 0;
+    pg_status s = prepare_pa(c, deltas, agents);
+    if (s != PG_OK) return s;
+    enqueue_pa_epoch(c, c->epoch, agents, c->timing);
+    PG_CUDA(c, cudaGetLastError());
+    s = finish_epoch(c, deltas, false);
+    if (s != PG_OK) return s;
+    if (c->timing) {
+        c->stats.ms_weights = ms_between(c->ev[0], c->ev[1]);
+        c->stats.ms_setup = ms_between(c->ev[1], c->ev[2]);
+        c->stats.ms_agents = ms_between(c->ev[2], c->ev[3]);
+        c->stats.ms_csr = ms_between(c->ev[3], c->ev[4]);
+        c->stats.ms_total = ms_between(c->ev[0], c->ev[4]);
+        c->stats.ms_er = 0.0;
+    }
+    if (new_nodes) *new_nodes = c->stats.new_nodes;
+    if (new_edges) *new_edges = c->stats.new_edges;
+    return PG_OK;
+}
+
+pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_t* new_edges) {
+    if (!c) return PG_ERR_ARG;
+    if (num_epochs < 1) return fail(c, PG_ERR_ARG, "num_epochs must be >= 1");
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (c->poisoned) return fail(c, PG_ERR_STATE, "an earlier epoch failed on the device; reload the graph");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    // plan every epoch on the host mirror; capacities must hold the whole run
+    std::vector<HostRep> saved = c->hrep;
+    std::vector<int64_t> agents((size_t)num_epochs);
+    int64_t max_agents = 0, max_edges = 0;
+    for (int e = 0; e < num_epochs; ++e) {
+        int64_t tot = 0, eb = 0;
+        for (int r = 0; r < c->R; ++r) {
+            HostRep& h = c->hrep[(size_t)r];
+            const int64_t d = delta_of(h.prm, h.n);
+            const int64_t b = edge_bound(d, h.prm.mean_out_degree, h.n);
+            tot += d;
+            eb += b;
+            h.n += d;
+            h.m += b;
+        }
+        agents[(size_t)e] = tot;
+        max_agents = std::max(max_agents, tot);
+        max_edges = std::max(max_edges, eb);
+    }
+    std::vector<HostRep> planned = c->hrep;
+    c->hrep = saved;
+    if (c->R == 1) {
+        pg_status s = ensure_capacity(c, planned[0].n, planned[0].m);
+        if (s != PG_OK) return s;
+    } else {
+        for (int r = 0; r < c->R; ++r)
+            if (planned[(size_t)r].n > c->hrep[(size_t)r].n_cap || planned[(size_t)r].m > c->hrep[(size_t)r].m_cap)
+                return fail(c, PG_ERR_CAPACITY, "run exceeds the planned capacity of replica " + std::to_string(r));
+    }
+    pg_status s = alloc_epoch_buffers(c, max_agents, max_edges, 0);
+    if (s != PG_OK) return s;
+    const int64_t e0 = c->epoch;
+    const int p0 = c->parity;
+    const bool events = c->timing;
+    auto enqueue_all = [&]() {
+        for (int e = 0; e < num_epochs; ++e) {
+            const bool last = e == num_epochs - 1;
+            if (events && e == 0) cudaEventRecord(c->ev[5], c->stream);
+            enqueue_pa_epoch(c, e0 + e, agents[(size_t)e], events && last);
+            c->parity ^= 1;
+        }
+        c->parity = p0;
+    };
+    if (use_graph) {
+        if (!(c->gexec && c->g_epoch0 == e0 && c->g_parity0 == p0 && c->g_epochs == num_epochs)) {
+            destroy_graph_exec(c);
+            // warm one-time initialisation (occupancy queries, attributes) outside capture
+            cudaGraph_t graph;
+            PG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            enqueue_all();
+            cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+            if (ce != cudaSuccess) return fail(c, PG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+            ce = cudaGraphInstantiate(&c->gexec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ce != cudaSuccess) return fail(c, PG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+            c->g_epoch0 = e0;
+            c->g_parity0 = p0;
+            c->g_epochs = num_epochs;
+        }
+        PG_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+    } else {
+        enqueue_all();
+    }
+    PG_CUDA(c, cudaGetLastError());
+    s = read_back(c);
+    if (s != PG_OK) return s;
+    s = device_error(c);
+    if (s != PG_OK) return s;
+    int64_t total = 0, nn = 0;
+    for (int r = 0; r < c->R; ++r) {
+        HostRep& h = c->hrep[(size_t)r];
+        total += c->h_rep[(size_t)r].m - h.m;
+        nn += c->h_rep[(size_t)r].n - h.n;
+        h.n = c->h_rep[(size_t)r].n;
+        h.m = c->h_rep[(size_t)r].m;
+    }
+    if (num_epochs % 2) c->parity ^= 1;
+    c->epoch = e0 + num_epochs;
+    fill_stats(c, nn, false);
+    c->stats.new_edges = total;
+    if (events) {
+        c->stats.ms_total = ms_between(c->ev[5], c->ev[4]);
+        c->stats.ms_weights = ms_between(c->ev[0], c->ev[1]);
+        c->stats.ms_setup = ms_between(c->ev[1], c->ev[2]);
+        c->stats.ms_agents = ms_between(c->ev[2], c->ev[3]);
+        c->stats.ms_csr = ms_between(c->ev[3], c->ev[4]);
+    }
+    if (new_edges) *new_edges = total;
+    return PG_OK;
+}
+
+pg_status pg_er_epoch(pg_ctx* c, int64_t delta, double p, int64_t* new_edges) {
+    if (!c) return PG_ERR_ARG;
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (c->R != 1) return fail(c, PG_ERR_ARG, "ER epochs run on single-replica contexts");
+    if (c->poisoned) return fail(c, PG_ERR_STATE, "an earlier epoch failed on the device; reload the graph");
+    if (delta <= 0 || std::isnan(p)) return fail(c, PG_ERR_ARG, "need delta > 0 and a numeric p");
+    if (p > 1.0) p = 1.0;
+    PG_CUDA(c, cudaSetDevice(c->device));
+    HostRep& h = c->hrep[0];
+    const int64_t n = h.n;
+    const int64_t chunks = (n + kErChunk - 1) / kErChunk;
+    const int64_t tasks = delta * chunks;
+    const double pe = p > 0.0 ? p : 0.0;
+    const double mu = (double)delta * (double)n * pe;
+    int64_t eb = (int64_t)std::ceil(mu + 8.0 * std::sqrt(mu) + 1024.0);
+    eb = std::min<int64_t>(eb, delta * n);
+    pg_status s = ensure_capacity(c, n + delta, h.m + eb);
+    if (s != PG_OK) return s;
+    s = alloc_epoch_buffers(c, delta, eb, tasks);
+    if (s != PG_OK) return s;
+    if (c->er_cnt.n < tasks + 1) PG_CUDA(c, dalloc(c->er_cnt, tasks + 1));
+    if (c->er_toff.n < tasks + 1) PG_CUDA(c, dalloc(c->er_toff, tasks + 1));
+    Arena A = make_arena(c);
+    cudaStream_t st = c->stream;
+    if (c->timing) cudaEventRecord(c->ev[0], st);
+    launch_epoch_begin_delta(A, c->epoch, delta, st);
+    launch_er_epoch(A, delta, p, n, c->er_cnt.p, c->er_toff.p, c->num_sms, st);
+    if (c->timing) cudaEventRecord(c->ev[1], st);
+    launch_bwd_append(A, delta, c->num_sms, st);
+    if (c->timing) cudaEventRecord(c->ev[2], st);
+    PG_CUDA(c, cudaGetLastError());
+    std::vector<int64_t> deltas(1, delta);
+    s = finish_epoch(c, deltas, true);
+    if (s != PG_OK) return s;
+    if (c->timing) {
+        c->stats.ms_er = ms_between(c->ev[0], c->ev[1]);
+        c->stats.ms_csr = ms_between(c->ev[1], c->ev[2]);
+        c->stats.ms_total = ms_between(c->ev[0], c->ev[2]);
+        c->stats.ms_weights = c->stats.ms_setup = c->stats.ms_agents = 0.0;
+    }
+    if (new_edges) *new_edges = c->stats.new_edges;
+    return PG_OK;
+}
+
+pg_status pg_get_counts(const pg_ctx* c, int32_t replica, int64_t* n, int64_t* m) {
+    if (!c || replica < 0 || replica >= c->R || !c->loaded) return PG_ERR_ARG;
+    if (n) *n = c->hrep[(size_t)replica].n;
+    if (m) *m = c->hrep[(size_t)replica].m;
+    return PG_OK;
+}
+
+pg_status pg_epoch_edges(const pg_ctx* c, int32_t replica, int64_t* first, int64_t* count) {
+    if (!c || replica < 0 || replica >= c->R || !c->loaded) return PG_ERR_ARG;
+    if (first) *first = c->rep_last_first[(size_t)replica];
+    if (count) *count = c->rep_last_count[(size_t)replica];
+    return PG_OK;
+}
+
+pg_status pg_copy_edges(pg_ctx* c, int32_t replica, int64_t first, int64_t count, int32_t* src,
+                        int32_t* dst) {
+    if (!c) return PG_ERR_ARG;
+    if (replica < 0 || replica >= c->R || !c->loaded) return fail(c, PG_ERR_ARG, "bad replica");
+    const HostRep& h = c->hrep[(size_t)replica];
+    if (first < 0 || count < 0 || first + count > h.m) return fail(c, PG_ERR_ARG, "edge range out of bounds");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    if (dst && count)
+        PG_CUDA(c, cudaMemcpyAsync(dst, c->fwd_col.p + h.ebase + first, 4 * (size_t)count,
+                                   cudaMemcpyDeviceToHost, c->stream));
+    if (src && count) {
+        // sources from the forward offsets: rows are contiguous in edge order
+        std::vector<int64_t> off((size_t)h.n + 1);
+        PG_CUDA(c, cudaMemcpyAsync(off.data(), c->fwd_off.p + h.obase, 8 * off.size(), cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaStreamSynchronize(c->stream));
+        int64_t v = std::upper_bound(off.begin(), off.end(), first) - off.begin() - 1;
+        for (int64_t i = 0; i < count; ++i) {
+            const int64_t e = first + i;
+            while (off[(size_t)v + 1] <= e) ++v;
+            src[i] = (int32_t)v;
+        }
+    }
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status pg_copy_degrees(pg_ctx* c, int32_t replica, int32_t* indeg, int32_t* outdeg) {
+    if (!c) return PG_ERR_ARG;
+    if (replica < 0 || replica >= c->R || !c->loaded) return fail(c, PG_ERR_ARG, "bad replica");
+    const HostRep& h = c->hrep[(size_t)replica];
+    PG_CUDA(c, cudaSetDevice(c->device));
+    if (indeg)
+        PG_CUDA(c, cudaMemcpyAsync(indeg, c->indeg.p + h.nbase, 4 * (size_t)h.n, cudaMemcpyDeviceToHost, c->stream));
+    if (outdeg) {
+        std::vector<int64_t> off((size_t)h.n + 1);
+        PG_CUDA(c, cudaMemcpyAsync(off.data(), c->fwd_off.p + h.obase, 8 * off.size(), cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaStreamSynchronize(c->stream));
+        for (int64_t v = 0; v < h.n; ++v) outdeg[v] = (int32_t)(off[(size_t)v + 1] - off[(size_t)v]);
+    }
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status pg_copy_nodes(pg_ctx* c, int32_t replica, int32_t* pub_epoch, float* fitness) {
+    if (!c) return PG_ERR_ARG;
+    if (replica < 0 || replica >= c->R || !c->loaded) return fail(c, PG_ERR_ARG, "bad replica");
+    const HostRep& h = c->hrep[(size_t)replica];
+    PG_CUDA(c, cudaSetDevice(c->device));
+    if (pub_epoch)
+        PG_CUDA(c, cudaMemcpyAsync(pub_epoch, c->pub.p + h.nbase, 4 * (size_t)h.n, cudaMemcpyDeviceToHost, c->stream));
+    if (fitness)
+        PG_CUDA(c, cudaMemcpyAsync(fitness, c->fit.p + h.nbase, 4 * (size_t)h.n, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status pg_copy_csr(pg_ctx* c, int32_t replica, int32_t which, int64_t* off, int32_t* col) {
+    if (!c) return PG_ERR_ARG;
+    if (replica < 0 || replica >= c->R || !c->loaded) return fail(c, PG_ERR_ARG, "bad replica");
+    if (which != 0 && which != 1) return fail(c, PG_ERR_ARG, "which must be 0 or 1");
+    const HostRep& h = c->hrep[(size_t)replica];
+    PG_CUDA(c, cudaSetDevice(c->device));
+    const int64_t* o = which ? c->bwd_off[c->parity].p : c->fwd_off.p;
+    const int32_t* cl = which ? c->bwd_col[c->parity].p : c->fwd_col.p;
+    if (off)
+        PG_CUDA(c, cudaMemcpyAsync(off, o + h.obase, 8 * (size_t)(h.n + 1), cudaMemcpyDeviceToHost, c->stream));
+    if (col && h.m)
+        PG_CUDA(c, cudaMemcpyAsync(col, cl + h.ebase, 4 * (size_t)h.m, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status pg_copy_arrivals(pg_ctx* c, int32_t replica, int32_t* cited) {
+    if (!c || !cited) return PG_ERR_ARG;
+    if (!c->cfg.record_trace) return fail(c, PG_ERR_STATE, "context created without record_trace");
+    if (replica < 0 || replica >= c->R || !c->loaded) return fail(c, PG_ERR_ARG, "bad replica");
+    // epoch edge index of the replica's first edge = sum of earlier replicas' counts
+    int64_t base = 0;
+    for (int r = 0; r < replica; ++r) base += c->rep_last_count[(size_t)r];
+    const int64_t cnt = c->rep_last_count[(size_t)replica];
+    if (cnt)
+        PG_CUDA(c, cudaMemcpyAsync(cited, c->arrivals.p + base, 4 * (size_t)cnt, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status pg_set_timing(pg_ctx* c, int32_t enable) {
+    if (!c) return PG_ERR_ARG;
+    c->timing = enable != 0;
+    destroy_graph_exec(c);
+    return PG_OK;
+}
+
+pg_status pg_get_stats(const pg_ctx* c, pg_stats* out) {
+    if (!c || !out) return PG_ERR_ARG;
+    *out = c->stats;
+    return PG_OK;
+}
+
+pg_status pg_sync(pg_ctx* c) {
+    if (!c) return PG_ERR_ARG;
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status pg_check_device(pg_ctx* c) {
+    if (!c) return PG_ERR_ARG;
+    pg_status s = read_back(c);
+    if (s != PG_OK) return s;
+    return device_error(c);
+}
+
+void pg_philox4x32_10(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]) {
+    const u32x4 r = philox(c[0], c[1], c[2], c[3], k[0], k[1]);
+    for (int i = 0; i < 4; ++i) out[i] = r.x[i];
+}
+
+pg_status pg_poisson_table(double lambda, uint64_t* table) {
+    if (!table || !(lambda >= 0.0)) return PG_ERR_ARG;
+    poisson_table(lambda, table, kTableEntries);
+    return PG_OK;
+}
+
+float pg_logf_host(float x) { return logf_pg(x); }
+float pg_expf_host(float x) { return expf_pg(x); }
+double pg_log_host(double x) { return log_pg(x); }
+double pg_exp_host(double x) { return exp_pg(x); }
+
+}  // extern "C"

@@ -1,0 +1,293 @@
+// pg_csr.cu -- device CSR append of one epoch's edges (stage e).
+//
+// Replaces the reference's per-epoch host work: sorting new_edges_vec, inserting into
+// std::map<int, std::set<int>> adjacency (src/kernel.cu:1766-1810), updating in-degrees
+// (src/graph.cu:537-618) and rebuilding int32 CSRs with prepareGraph (src/utils.cu:75-142).
+//
+// Forward rows of new nodes were written by the agent kernel (append-only, sorted).  Backward rows
+// are rebuilt into the other buffer:
+//   len  : new_len = old_len + inc (inc = in-degree histogram of the epoch, filled by atomics in
+//          the agent kernel, which also returned each edge's rank); indeg += inc
+//   scan : per-replica exclusive scan of new_len -> new int64 offsets
+//   copy : old rows moved with one warp per 32 rows (load-balanced over the concatenated rows)
+//   place: each new edge at new_off + old_len + rank
+//   sort : the appended part of a row holds distinct new-node ids in atomic order; rows with up to
+//          32 new entries are sorted by a register bitonic network in one warp, longer ones by a
+//          shared-memory bitmap over the epoch's new-id range.  Rows end up ascending, like the
+//          reference's std::set rows, and bit-identical run to run.
+#include "pg_engine.cuh"
+
+namespace pg {
+
+constexpr unsigned kFullMask = 0xffffffffu;
+
+__global__ void __launch_bounds__(kTileThreads) k_bwd_len(Arena A) {
+    __shared__ uint64_t sw[33];
+    if (A.st->error) return;
+    const int t = blockIdx.x;
+    const int r = A.tile_rep[t];
+    const Replica& rp = A.rep[r];
+    const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
+    const int64_t nact = rp.n + rp.delta;
+    if (v0 >= nact) {
+        if (threadIdx.x == 0) A.tilesum[t] = 0;
+        return;
+    }
+    const int64_t* off = A.bwd_off_cur + rp.obase;
+    int64_t sum = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t v = v0 + (int64_t)threadIdx.x * 4 + i;
+        const int64_t slot = rp.nbase + v;
+        int64_t len = 0;
+        if (v < nact) {
+            const int64_t old = v < rp.n ? off[v + 1] - off[v] : 0;
+            const int ic = A.inc[slot];
+            len = old + ic;
+            if (ic) {
+                A.indeg[slot] += ic;
+                A.inc[slot] = 0;
+                if (ic >= 2) {
+                    if (ic <= kSortSmall) {
+                        const unsigned long long q = atomicAdd(&A.st->sort_small_count, 1ull);
+                        A.sort_small[q] = (slot << 8) | (int64_t)ic;
+                    } else {
+                        const unsigned long long q = atomicAdd(&A.st->sort_large_count, 1ull);
+                        A.sort_large[q] = slot;
+                        A.sort_large_off[q] =
+                            (int64_t)atomicAdd(&A.st->sort_scratch, (unsigned long long)ic);
+                    }
+                }
+            }
+        }
+        A.len_tmp[slot] = len;
+        sum += len;
+    }
+    uint64_t tot;
+    block_excl_scan<uint64_t>((uint64_t)sum, sw, &tot);
+    if (threadIdx.x == 0) A.tilesum[t] = tot;
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_bwd_off(Arena A) {
+    __shared__ int64_t sw[33];
+    if (A.st->error) return;
+    const int t = blockIdx.x;
+    const int r = A.tile_rep[t];
+    const Replica& rp = A.rep[r];
+    const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
+    const int64_t nact = rp.n + rp.delta;
+    if (v0 >= nact) return;
+    int64_t len[4], s = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t v = v0 + (int64_t)threadIdx.x * 4 + i;
+        len[i] = v < nact ? A.len_tmp[rp.nbase + v] : 0;
+        s += len[i];
+    }
+    int64_t tot;
+    int64_t ex = block_excl_scan<int64_t>(s, sw, &tot) + (int64_t)A.tileoff[t];
+    int64_t* off = A.bwd_off_nxt + rp.obase;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t v = v0 + (int64_t)threadIdx.x * 4 + i;
+        if (v < nact) off[v] = ex;
+        ex += len[i];
+        if (v == nact - 1) off[nact] = ex;
+    }
+}
+
+// One warp per 32 consecutive old rows.
+__global__ void __launch_bounds__(256) k_bwd_copy(Arena A, int64_t chunks) {
+    if (A.st->error) return;
+    const int lane = lane_id();
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long moved = 0;
+    for (int64_t c = warp; c < chunks; c += nwarps) {
+        const int t = (int)(c / (kTile / 32));
+        const int r = A.tile_rep[t];
+        const Replica& rp = A.rep[r];
+        const int64_t vbase = (int64_t)(t - rp.tbase) * kTile + (c % (kTile / 32)) * 32;
+        if (vbase >= rp.n) continue;
+        const int64_t v = vbase + lane;
+        const int64_t* oc = A.bwd_off_cur + rp.obase;
+        const int64_t* on = A.bwd_off_nxt + rp.obase;
+        const int32_t* cc = A.bwd_col_cur + rp.ebase;
+        int32_t* cn = A.bwd_col_nxt + rp.ebase;
+        int64_t ob = 0, ol = 0, nb = 0;
+        if (v < rp.n) {
+            ob = oc[v];
+            ol = oc[v + 1] - ob;
+            nb = on[v];
+        }
+        const int64_t incl = warp_incl_scan<int64_t>(ol);
+        const int64_t total = __shfl_sync(kFullMask, incl, 31);
+        moved += (unsigned long long)total;
+        for (int64_t pb = 0; pb < total; pb += 32) {
+            const int64_t p = pb + lane;
+            int o = 0;
+#pragma unroll
+            for (int b = 16; b >= 1; b >>= 1) {
+                const int64_t iv = __shfl_sync(kFullMask, incl, o + b - 1);
+                if (iv <= p) o += b;
+            }
+            const int64_t ex_o = __shfl_sync(kFullMask, incl - ol, o);
+            const int64_t ob_o = __shfl_sync(kFullMask, ob, o);
+            const int64_t nb_o = __shfl_sync(kFullMask, nb, o);
+            if (p < total) cn[nb_o + (p - ex_o)] = cc[ob_o + (p - ex_o)];
+        }
+    }
+    if (lane == 0 && moved) atomicAdd(&A.st->bwd_moved, moved);
+}
+
+// One warp per agent: place its edges at new_off[dst] + old_len(dst) + rank.
+__global__ void __launch_bounds__(256) k_bwd_place(Arena A, int64_t agents) {
+    if (A.st->error) return;
+    const int lane = lane_id();
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t a = warp; a < agents; a += nwarps) {
+        const int r = replica_of_agent(A.rep, A.R, a);
+        const Replica& rp = A.rep[r];
+        const int32_t src = (int32_t)(rp.n + (a - rp.abase));
+        const int64_t e0 = A.eoff[a], e1 = A.eoff[a + 1];
+        const int64_t* oc = A.bwd_off_cur + rp.obase;
+        const int64_t* on = A.bwd_off_nxt + rp.obase;
+        int32_t* cn = A.bwd_col_nxt + rp.ebase;
+        for (int64_t e = e0 + lane; e < e1; e += 32) {
+            const int32_t j = A.e_dst[e];
+            const int64_t old = j < rp.n ? oc[j + 1] - oc[j] : 0;
+            cn[on[j] + old + A.e_rank[e]] = src;
+        }
+    }
+}
+
+__device__ __forceinline__ void seg_bounds(const Arena& A, int64_t slot, const Replica*& rpp,
+                                           int64_t& start, int64_t& len) {
+    const int r = A.tile_rep[slot / kTile];
+    const Replica& rp = A.rep[r];
+    rpp = &rp;
+    const int64_t v = slot - rp.nbase;
+    const int64_t* oc = A.bwd_off_cur + rp.obase;
+    const int64_t* on = A.bwd_off_nxt + rp.obase;
+    const int64_t old = v < rp.n ? oc[v + 1] - oc[v] : 0;
+    start = rp.ebase + on[v] + old;
+    len = on[v + 1] - on[v] - old;
+}
+
+// Rows with 2..32 appended entries: one warp, register bitonic network.
+__global__ void __launch_bounds__(256) k_sort_small(Arena A) {
+    if (A.st->error) return;
+    const int lane = lane_id();
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t cnt = (int64_t)A.st->sort_small_count;
+    for (int64_t i = warp; i < cnt; i += nwarps) {
+        const int64_t slot = A.sort_small[i] >> 8;
+        const Replica* rp;
+        int64_t start, len;
+        seg_bounds(A, slot, rp, start, len);
+        int32_t* seg = A.bwd_col_nxt + start;
+        int v = lane < len ? seg[lane] : 0x7fffffff;
+#pragma unroll
+        for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                const int o = __shfl_xor_sync(kFullMask, v, j);
+                const bool up = (lane & k) == 0;
+                const bool lower = (lane & j) == 0;
+                v = (lower == up) ? min(v, o) : max(v, o);
+            }
+        }
+        if (lane < len) seg[lane] = v;
+    }
+}
+
+// Rows with more than 32 appended entries: one CTA, shared bitmap over [n, n + delta).
+__global__ void __launch_bounds__(1024) k_sort_large(Arena A) {
+    extern __shared__ uint32_t bm[];
+    __shared__ int64_t sw[33];
+    __shared__ int64_t outpos;
+    if (A.st->error) return;
+    const int64_t cnt = (int64_t)A.st->sort_large_count;
+    constexpr int64_t kBits = (int64_t)kBitmapWords * 32;
+    for (int64_t i = blockIdx.x; i < cnt; i += gridDim.x) {
+        const int64_t slot = A.sort_large[i];
+        const Replica* rp;
+        int64_t start, len;
+        seg_bounds(A, slot, rp, start, len);
+        int32_t* seg = A.bwd_col_nxt + start;
+        const int64_t lo = rp->n, range = rp->delta;
+        const int32_t* srcv = seg;
+        if (range > kBits) {  // several chunks: keep the input in the spent rank buffer
+            int32_t* scratch = A.e_rank + A.sort_large_off[i];
+            for (int64_t q = threadIdx.x; q < len; q += blockDim.x) scratch[q] = seg[q];
+            __syncthreads();
+            srcv = scratch;
+        }
+        if (threadIdx.x == 0) outpos = 0;
+        for (int64_t cb = 0; cb < range; cb += kBits) {
+            const int64_t bits = range - cb < kBits ? range - cb : kBits;
+            const int nw = (int)((bits + 31) >> 5);
+            for (int q = threadIdx.x; q < nw; q += blockDim.x) bm[q] = 0;
+            __syncthreads();
+            for (int64_t q = threadIdx.x; q < len; q += blockDim.x) {
+                const int64_t x = (int64_t)srcv[q] - lo - cb;
+                if (x >= 0 && x < bits) atomicOr(&bm[x >> 5], 1u << (x & 31));
+            }
+            __syncthreads();
+            const int per = (nw + (int)blockDim.x - 1) / (int)blockDim.x;
+            const int w0 = threadIdx.x * per;
+            int64_t c = 0;
+            for (int q = w0; q < w0 + per && q < nw; ++q) c += __popc(bm[q]);
+            int64_t tot;
+            int64_t ex = block_excl_scan<int64_t>(c, sw, &tot) + outpos;
+            for (int q = w0; q < w0 + per && q < nw; ++q) {
+                uint32_t word = bm[q];
+                while (word) {
+                    const int b = __ffs(word) - 1;
+                    word &= word - 1;
+                    seg[ex++] = (int32_t)(lo + cb + (int64_t)q * 32 + b);
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) outpos += tot;
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void k_epoch_end(Arena A, int64_t agents) {
+    if (A.st->error) return;
+    for (int r = threadIdx.x; r < A.R; r += blockDim.x) {
+        Replica& rp = A.rep[r];
+        const int64_t er = A.eoff[rp.abase + rp.delta] - A.eoff[rp.abase];
+        rp.m += er;
+        rp.n += rp.delta;
+    }
+}
+
+void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_sort_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kBitmapWords * 4);
+        attr_set = true;
+    }
+    k_bwd_len<<<A.ntiles, kTileThreads, 0, s>>>(A);
+    launch_tile_scan(A, 1, s);
+    k_bwd_off<<<A.ntiles, kTileThreads, 0, s>>>(A);
+    const int64_t chunks = (int64_t)A.ntiles * (kTile / 32);
+    int64_t g = (chunks + 7) / 8;
+    if (g > (int64_t)num_sms * 16) g = (int64_t)num_sms * 16;
+    k_bwd_copy<<<(unsigned)g, 256, 0, s>>>(A, chunks);
+    int64_t ga = (agents + 7) / 8;
+    if (ga > (int64_t)num_sms * 16) ga = (int64_t)num_sms * 16;
+    if (ga < 1) ga = 1;
+    k_bwd_place<<<(unsigned)ga, 256, 0, s>>>(A, agents);
+    k_sort_small<<<(unsigned)num_sms * 8, 256, 0, s>>>(A);
+    k_sort_large<<<(unsigned)num_sms, 1024, kBitmapWords * 4, s>>>(A);
+    k_epoch_end<<<1, 256, 0, s>>>(A, agents);
+}
+
+}  // namespace pg

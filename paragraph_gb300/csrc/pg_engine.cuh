@@ -1,0 +1,191 @@
+// pg_engine.cuh -- device data layout and shared primitives of the growth engine.
+//
+// Layout in HBM (one arena per context, R replicas):
+//   node slot arrays (pub, fitness, indeg, w, cdf, inc) are indexed nbase_r + v, v < n_cap_r; every
+//   nbase_r is a multiple of kTile so a scan tile never spans two replicas;
+//   offset arrays (fwd_off, bwd_off) hold n_cap_r + 1 int64 entries at obase_r = nbase_r + r and
+//   are LOCAL to the replica's edge region;
+//   column arrays (fwd_col, bwd_col) hold replica-local int32 node ids at ebase_r + offset.
+// Backward offsets and columns are double-buffered: each epoch writes the other copy.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pg_core.cuh"
+
+namespace pg {
+
+constexpr int kTile = 1024;          // slots per scan tile
+constexpr int kTileThreads = 256;    // threads per tile CTA (4 slots each)
+constexpr int kKSmall = 64;          // agents with k <= 64 use the small-capacity path
+constexpr int kKMax = 256;           // PG_MAX_OUT_DEGREE
+constexpr int kTableEntries = kKMax + 1;
+constexpr int kAgentWarps = 4;       // warps per CTA in the agent kernel
+constexpr int kErChunk = 65536;      // ids per ER Philox stream
+constexpr int kSortSmall = 32;       // appended segments up to this length sort in one warp
+constexpr int kBitmapWords = 40960;  // 160 KiB of shared bitmap in the large-segment sort
+
+// Device error word bits.
+enum : uint32_t {
+    kErrCapacity = 1u,
+    kErrBadWeight = 2u,
+    kErrArg = 4u,
+};
+
+struct Replica {
+    // static layout
+    int64_t nbase, obase, ebase;
+    int64_t n_cap, m_cap;
+    // state
+    int64_t n, m;
+    // this epoch
+    int64_t delta;
+    int64_t abase;      // first agent (global agent index) of this replica
+    int64_t npos;       // nodes with positive weight
+    uint64_t wq_total;  // quantised total weight
+    uint32_t wmax_bits;
+    int32_t shift;
+    int32_t tbase;      // first slot tile of the replica
+    int32_t ntiles;     // slot tiles of the replica (n_cap / kTile)
+    // parameters
+    float alpha, gamma, tau, pad0;
+    double beta_m1;
+    double growth_rate;
+    int64_t fixed_new;
+    int32_t anchors;
+    int32_t pad1;
+};
+
+// Per-epoch device scalars; reset by the epoch-begin kernel.
+struct EpochState {
+    int64_t epoch;
+    int64_t agents;       // total agents this epoch
+    int64_t edges;        // total new edges this epoch
+    uint32_t error;
+    uint32_t pad;
+    unsigned long long queue_small;
+    unsigned long long queue_big;
+    unsigned long long big_count;
+    unsigned long long sort_small_count;
+    unsigned long long sort_large_count;
+    unsigned long long sort_scratch;
+    // counters of the byte model
+    unsigned long long rows_expanded;
+    unsigned long long elems_streamed;
+    unsigned long long draws;
+    unsigned long long bwd_moved;
+    unsigned long long nodes_weighted;
+};
+
+// Device pointers of the arena (passed by value to kernels).
+struct Arena {
+    Replica* rep;
+    int32_t R;
+    int32_t ntiles;            // total slot tiles
+    const int32_t* tile_rep;   // [ntiles]
+    int32_t* pub;
+    float* fit;
+    int32_t* indeg;
+    float* w;
+    uint64_t* cdf;
+    int32_t* inc;
+    int64_t* fwd_off;
+    int32_t* fwd_col;
+    int64_t* bwd_off_cur;
+    int32_t* bwd_col_cur;
+    int64_t* bwd_off_nxt;
+    int32_t* bwd_col_nxt;
+    const uint64_t* tables;    // [R][kTableEntries]
+    // per-epoch buffers
+    int32_t* kk;               // [agent cap] out-degree per agent
+    int64_t* eoff;             // [agent cap + 1] edge offsets
+    int32_t* e_dst;            // [edge cap]
+    int32_t* e_rank;           // [edge cap]
+    int32_t* arrivals;         // [edge cap] or null
+    int32_t* big_list;         // [agent cap]
+    int64_t* len_tmp;          // [slots]
+    uint64_t* tilesum;         // [ntiles]
+    uint64_t* tileoff;         // [ntiles]
+    int64_t* blocksum;         // [scan blocks]
+    int64_t* sort_small;       // [slots] packed (slot << 8 | len)
+    int64_t* sort_large;       // [slots] slot
+    int64_t* sort_large_off;   // [slots] scratch offset
+    EpochState* st;
+    int64_t agent_cap, edge_cap;
+    uint64_t seed;
+    int32_t record_trace;
+};
+
+// ---------------------------------------------------------------- warp helpers
+#if defined(__CUDACC__)
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
+    const int l = lane_id();
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        T o = __shfl_up_sync(0xffffffffu, v, d);
+        if (l >= d) v += o;
+    }
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    return v;
+}
+
+// Block-wide exclusive scan of one value per thread (blockDim.x <= 1024, multiple of 32).
+template <typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T* smem_warp, T* total) {
+    const int l = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    T incl = warp_incl_scan(v);
+    if (l == 31) smem_warp[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        T x = l < nw ? smem_warp[l] : T(0);
+        T xi = warp_incl_scan(x);
+        if (l < nw) smem_warp[l] = xi - x;
+        if (l == nw - 1) smem_warp[32] = xi;
+    }
+    __syncthreads();
+    T out = smem_warp[wid] + incl - v;
+    if (total) *total = smem_warp[32];
+    __syncthreads();
+    return out;
+}
+
+// Replica of a global agent index: largest r with abase_r <= a.
+__device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64_t a) {
+    int lo = 0, hi = R - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (rep[mid].abase <= a)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+#endif
+
+// ---------------------------------------------------------------- host launchers
+void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s);
+void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cudaStream_t s);
+void launch_weights(const Arena& A, cudaStream_t s);
+void launch_tile_scan(const Arena& A, int mode, cudaStream_t s);
+void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s);
+void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
+void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
+void launch_er_epoch(const Arena& A, int64_t delta, double p, int64_t n, int64_t* cnt,
+                     int64_t* toff, int num_sms, cudaStream_t s);
+// generic exclusive scan of n values; out has n+1 entries (out[n] = total)
+void launch_scan_i64(const int64_t* in, int64_t* out, int64_t n, int64_t* blocksum, cudaStream_t s);
+void launch_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_t* blocksum,
+                            cudaStream_t s);
+int scan_blocks_needed(int64_t n);
+
+}  // namespace pg

@@ -1,0 +1,117 @@
+// pg_er.cu -- Erdos-Renyi G(n,p) growth by geometric skips (stage d).
+//
+// The reference's ER model lives on a branch that is not in the tree; its behaviour is recorded in
+// results/slurm-8634746.out:60-73: every new node links to each pre-epoch node independently with
+// probability p (724,781 edges for 14,746 new x 491,532 existing x 1e-4).
+//
+// Work is O(edges): the gap to the next success is floor(log(u) / log(1-p)).  The id range of each
+// new node is cut into 2^16-id chunks with their own Philox stream, so a (node, chunk) task is
+// independent of how tasks are spread over threads.  A count pass, an exclusive scan and an emit
+// pass that replays the same streams write the edges in (source, target) order with no sort.
+// log is the library's own fp64 log, so the edge list is bit-identical to the CPU oracle.
+#include "pg_engine.cuh"
+
+namespace pg {
+
+__device__ __forceinline__ int64_t er_walk(const Arena& A, int64_t i, int64_t c, int64_t n,
+                                           double inv_l, int32_t* out, int64_t out_base,
+                                           int32_t* col_out, int64_t col_base) {
+    const int64_t lo = c * kErChunk;
+    const int64_t hi = lo + kErChunk < n ? lo + kErChunk : n;
+    int64_t pos = lo - 1, cnt = 0;
+    const uint32_t ep = (uint32_t)A.st->epoch;
+    u32x4 x;
+    x.x[0] = x.x[1] = x.x[2] = x.x[3] = 0;
+    for (uint32_t d = 0;; ++d) {
+        if ((d & 1u) == 0) x = draw(A.seed, kStreamEr, (uint32_t)c, ep, (uint32_t)i, d >> 1);
+        const double u = (d & 1u) ? u01d(x.x[2], x.x[3]) : u01d(x.x[0], x.x[1]);
+        const double sk = floor(log_pg(u) * inv_l);
+        if (sk >= (double)(hi - pos - 1)) break;
+        pos = pos + 1 + (int64_t)sk;
+        if (out) {
+            out[out_base + cnt] = (int32_t)pos;
+            col_out[col_base + cnt] = (int32_t)pos;
+            A.e_rank[out_base + cnt] = atomicAdd(&A.inc[A.rep[0].nbase + pos], 1);
+        }
+        ++cnt;
+    }
+    return cnt;
+}
+
+__global__ void __launch_bounds__(256) k_er_setup(Arena A, int64_t delta) {
+    if (A.st->error) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= delta) return;
+    const Replica& rp = A.rep[0];
+    const int64_t slot = rp.nbase + rp.n + i;
+    const uint32_t ep = (uint32_t)A.st->epoch;
+    A.pub[slot] = (int32_t)A.st->epoch;
+    A.fit[slot] = lognormal_fitness(A.seed, 0u, ep, (uint32_t)i);
+    A.indeg[slot] = 0;
+}
+
+__global__ void __launch_bounds__(256) k_er_count(Arena A, int64_t tasks, int64_t chunks,
+                                                  double inv_l, int64_t* cnt) {
+    if (A.st->error) return;
+    const int64_t n = A.rep[0].n;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tasks;
+         t += (int64_t)gridDim.x * blockDim.x)
+        cnt[t] = er_walk(A, t / chunks, t % chunks, n, inv_l, nullptr, 0, nullptr, 0);
+}
+
+__global__ void k_er_check(Arena A, const int64_t* toff, int64_t tasks) {
+    if (A.st->error) return;
+    const int64_t E = toff[tasks];
+    const Replica& rp = A.rep[0];
+    A.st->edges = E;
+    if (E > A.edge_cap || rp.m + E > rp.m_cap) atomicOr(&A.st->error, kErrCapacity);
+}
+
+__global__ void __launch_bounds__(256) k_er_emit(Arena A, int64_t tasks, int64_t chunks,
+                                                 double inv_l, const int64_t* toff) {
+    if (A.st->error) return;
+    const Replica& rp = A.rep[0];
+    const int64_t n = rp.n;
+    int32_t* fcol = A.fwd_col + rp.ebase;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tasks;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / chunks, c = t % chunks;
+        const int64_t e0 = toff[t];
+        const int64_t cnt = er_walk(A, i, c, n, inv_l, A.e_dst, e0, fcol, rp.m + e0);
+        if (A.arrivals)
+            for (int64_t q = 0; q < cnt; ++q) A.arrivals[e0 + q] = A.e_dst[e0 + q];
+        if (c == chunks - 1) A.fwd_off[rp.obase + n + i + 1] = rp.m + e0 + cnt;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_er_eoff(Arena A, const int64_t* toff, int64_t delta,
+                                                 int64_t chunks) {
+    if (A.st->error) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i <= delta) A.eoff[i] = toff[i * chunks];
+}
+
+// Count, scan and emit; the caller then runs the backward append.
+void launch_er_epoch(const Arena& A, int64_t delta, double p, int64_t n, int64_t* cnt,
+                     int64_t* toff, int num_sms, cudaStream_t s) {
+    const int64_t chunks = (n + kErChunk - 1) / kErChunk;
+    const int64_t tasks = delta * chunks;
+    k_er_setup<<<(unsigned)((delta + 255) / 256), 256, 0, s>>>(A, delta);
+    if (!(p > 0.0)) {  // no edges: zero offsets keep the CSR append consistent
+        cudaMemsetAsync(toff, 0, sizeof(int64_t) * (size_t)(tasks + 1), s);
+        k_er_check<<<1, 32, 0, s>>>(A, toff, tasks);
+        k_er_eoff<<<(unsigned)((delta + 256) / 256), 256, 0, s>>>(A, toff, delta, chunks);
+        return;
+    }
+    const double inv_l = 1.0 / log_pg(1.0 - (p < 1.0 ? p : 1.0));
+    int64_t g = (tasks + 255) / 256;
+    if (g > (int64_t)num_sms * 32) g = (int64_t)num_sms * 32;
+    if (g < 1) g = 1;
+    k_er_count<<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, cnt);
+    launch_scan_i64(cnt, toff, tasks, A.blocksum, s);
+    k_er_check<<<1, 32, 0, s>>>(A, toff, tasks);
+    k_er_emit<<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, toff);
+    k_er_eoff<<<(unsigned)((delta + 256) / 256), 256, 0, s>>>(A, toff, delta, chunks);
+}
+
+}  // namespace pg

@@ -1,0 +1,223 @@
+// pg_weights.cu -- epoch start, per-node weights and the segmented fixed-point CDF.
+//
+// Restates the per-epoch score preparation of execute() (src/kernel.cu:1698-1706;
+// FillInDegreeArr/FillFitnessArr/FillRecencyArr/CalculateScores, src/abm.cu:112-208,324-338),
+// which the reference runs on the host every epoch, with the baseline weight functor
+//   w_j = exp(gamma log f_j + alpha log(indeg_j + 1) - (t - t_j) / tau).
+//
+// The CDF is a per-replica inclusive prefix sum of q_j = floor(w_j 2^s) in uint64 ("segmented":
+// segments are replicas; tiles never span two).  Integer sums are exact and associative, so the CDF
+// is identical for any tile decomposition and any search order -- which is what lets the GPU's
+// 32-ary warp search and the CPU oracle's binary search pick the same node for the same uniform.
+//
+// HBM roofline per node: read fitness, indeg, pub (12 B), write w (4 B); read w (4 B), write cdf
+// (8 B); cdf read+write in the offset pass (16 B).
+#include "pg_engine.cuh"
+
+namespace pg {
+
+__global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, int64_t delta_override) {
+    __shared__ int64_t sw[33];
+    __shared__ int64_t carry;
+    EpochState* st = A.st;
+    if (threadIdx.x == 0) {
+        carry = 0;
+        st->epoch = epoch;
+        st->edges = 0;
+        st->queue_small = 0;
+        st->queue_big = 0;
+        st->big_count = 0;
+        st->sort_small_count = 0;
+        st->sort_large_count = 0;
+        st->sort_scratch = 0;
+        st->rows_expanded = 0;
+        st->elems_streamed = 0;
+        st->draws = 0;
+        st->bwd_moved = 0;
+        st->nodes_weighted = 0;
+    }
+    __syncthreads();
+    for (int base = 0; base < A.R; base += 1024) {
+        const int r = base + threadIdx.x;
+        int64_t d = 0;
+        if (r < A.R) {
+            Replica& rp = A.rep[r];
+            if (delta_override >= 0)
+                d = (r == 0) ? delta_override : 0;
+            else if (rp.growth_rate > 0.0)
+                d = (int64_t)ceil((double)rp.n * rp.growth_rate);
+            else
+                d = rp.fixed_new;
+            if (d < 0) d = 0;
+            if (rp.n + d > rp.n_cap) atomicOr(&st->error, kErrCapacity);
+            rp.delta = d;
+            rp.wmax_bits = 0;
+            rp.npos = 0;
+            rp.wq_total = 0;
+        }
+        int64_t tot;
+        const int64_t ex = block_excl_scan<int64_t>(d, sw, &tot);
+        if (r < A.R) A.rep[r].abase = carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        st->agents = carry;
+        if (carry > A.agent_cap) atomicOr(&st->error, kErrCapacity);
+    }
+}
+
+// w_j for active nodes; per-replica max (as float bits, valid for non-negative floats) and count
+// of positive weights.
+__global__ void __launch_bounds__(kTileThreads) k_weights(Arena A) {
+    if (A.st->error) return;
+    const int t = blockIdx.x;
+    const int r = A.tile_rep[t];
+    const Replica& rp = A.rep[r];
+    const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
+    if (v0 >= rp.n) return;
+    const int64_t n = rp.n;
+    const int32_t ep = (int32_t)A.st->epoch;
+    uint32_t wmax = 0;
+    int cnt = 0, act = 0;
+    bool bad = false;
+#pragma unroll
+    for (int i = 0; i < kTile / kTileThreads; ++i) {
+        const int64_t v = v0 + threadIdx.x + i * kTileThreads;
+        if (v < n) {
+            const int64_t slot = rp.nbase + v;
+            const float w = weight0(A.fit[slot], A.indeg[slot], ep - A.pub[slot], rp.alpha,
+                                    rp.gamma, rp.tau);
+            A.w[slot] = w;
+            ++act;
+            if (!(w <= 3.0e38f)) bad = true;  // inf or NaN
+            if (w > 0.0f) {
+                ++cnt;
+                const uint32_t b = fbits(w);
+                wmax = b > wmax ? b : wmax;
+            }
+        }
+    }
+    wmax = __reduce_max_sync(0xffffffffu, wmax);
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    act = __reduce_add_sync(0xffffffffu, act);
+    if (__any_sync(0xffffffffu, bad) && lane_id() == 0) atomicOr(&A.st->error, kErrBadWeight);
+    if (lane_id() == 0) {
+        if (wmax) atomicMax(&A.rep[r].wmax_bits, wmax);
+        if (cnt) atomicAdd((unsigned long long*)&A.rep[r].npos, (unsigned long long)cnt);
+        if (act) atomicAdd(&A.st->nodes_weighted, (unsigned long long)act);
+    }
+}
+
+// q_j = quantise(w_j, s_r); tile-local inclusive scan into cdf, tile total into tilesum.
+__global__ void __launch_bounds__(kTileThreads) k_cdf_tiles(Arena A) {
+    __shared__ uint64_t sw[33];
+    const int t = blockIdx.x;
+    if (A.st->error) return;
+    const int r = A.tile_rep[t];
+    const Replica& rp = A.rep[r];
+    const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
+    if (v0 >= rp.n) {
+        if (threadIdx.x == 0) A.tilesum[t] = 0;
+        return;
+    }
+    const uint32_t wb = rp.wmax_bits;
+    if (wb == 0) {
+        if (threadIdx.x == 0) atomicOr(&A.st->error, kErrBadWeight);
+        return;
+    }
+    const int s = cdf_shift(bitsf(wb), rp.n);
+    const int64_t n = rp.n;
+    const int64_t vt = v0 + (int64_t)threadIdx.x * 4;
+    const float4 w4 = *reinterpret_cast<const float4*>(A.w + rp.nbase + vt);
+    uint64_t q[4];
+    q[0] = vt + 0 < n ? quantise(w4.x, s) : 0;
+    q[1] = vt + 1 < n ? quantise(w4.y, s) : 0;
+    q[2] = vt + 2 < n ? quantise(w4.z, s) : 0;
+    q[3] = vt + 3 < n ? quantise(w4.w, s) : 0;
+    q[1] += q[0];
+    q[2] += q[1];
+    q[3] += q[2];
+    uint64_t tot;
+    const uint64_t ex = block_excl_scan<uint64_t>(q[3], sw, &tot);
+    ulonglong2* dst = reinterpret_cast<ulonglong2*>(A.cdf + rp.nbase + vt);
+    dst[0] = make_ulonglong2(ex + q[0], ex + q[1]);
+    dst[1] = make_ulonglong2(ex + q[2], ex + q[3]);
+    if (threadIdx.x == 0) A.tilesum[t] = tot;
+}
+
+// One CTA: tileoff[t] = sum of tilesum over the earlier tiles of the same replica (mod 2^64, which
+// is exact because every replica's own total is below 2^63).  mode 0 stores each replica's total in
+// wq_total; mode 1 leaves replicas untouched.
+__global__ void __launch_bounds__(1024) k_tile_scan(Arena A, int mode) {
+    __shared__ uint64_t sw[33];
+    __shared__ uint64_t carry;
+    if (A.st->error) return;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int T = A.ntiles;
+    for (int base = 0; base < T; base += 1024) {
+        const int i = base + threadIdx.x;
+        const uint64_t v = i < T ? A.tilesum[i] : 0;
+        uint64_t tot;
+        const uint64_t ex = block_excl_scan<uint64_t>(v, sw, &tot);
+        if (i < T) A.tileoff[i] = carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    // per-replica base and total; tilesum[] is free now and holds the bases
+    for (int r = threadIdx.x; r < A.R; r += 1024) {
+        const Replica& rp = A.rep[r];
+        const uint64_t b = A.tileoff[rp.tbase];
+        const int e = rp.tbase + rp.ntiles;
+        const uint64_t end = e < T ? A.tileoff[e] : carry;
+        A.tilesum[r] = b;
+        if (mode == 0) A.rep[r].wq_total = end - b;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < T; i += 1024) A.tileoff[i] -= A.tilesum[A.tile_rep[i]];
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_cdf_add(Arena A) {
+    if (A.st->error) return;
+    const int t = blockIdx.x;
+    const int r = A.tile_rep[t];
+    const Replica& rp = A.rep[r];
+    const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
+    if (v0 >= rp.n) return;
+    const uint64_t off = A.tileoff[t];
+    if (off == 0) return;
+    const int64_t vt = v0 + (int64_t)threadIdx.x * 4;
+    ulonglong2* p = reinterpret_cast<ulonglong2*>(A.cdf + rp.nbase + vt);
+    ulonglong2 a = p[0], b = p[1];
+    a.x += off;
+    a.y += off;
+    b.x += off;
+    b.y += off;
+    p[0] = a;
+    p[1] = b;
+}
+
+void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s) {
+    (void)pa_mode;
+    k_epoch_begin<<<1, 1024, 0, s>>>(A, epoch, -1);
+}
+
+void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cudaStream_t s) {
+    k_epoch_begin<<<1, 1024, 0, s>>>(A, epoch, delta);
+}
+
+void launch_tile_scan(const Arena& A, int mode, cudaStream_t s) {
+    k_tile_scan<<<1, 1024, 0, s>>>(A, mode);
+}
+
+void launch_weights(const Arena& A, cudaStream_t s) {
+    k_weights<<<A.ntiles, kTileThreads, 0, s>>>(A);
+    k_cdf_tiles<<<A.ntiles, kTileThreads, 0, s>>>(A);
+    k_tile_scan<<<1, 1024, 0, s>>>(A, 0);
+    k_cdf_add<<<A.ntiles, kTileThreads, 0, s>>>(A);
+}
+
+}  // namespace pg

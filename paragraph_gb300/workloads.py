@@ -1,0 +1,119 @@
+"""Seeded synthetic seed graphs with the shapes of the benchmark configurations.
+
+The reference grows real citation graphs read from edge/node lists (drivers/*.sh pass the "sj"
+graph, which is not distributed with it); these generators stand in for them with the sizes and
+distributions the benchmark configurations name.  All draws come from numpy's PCG64, so a seed
+fixes the graph.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import PAParams, ReplicaInput
+
+
+@dataclass
+class SeedGraph:
+    pub: np.ndarray      # int32 publication epoch
+    fitness: np.ndarray  # float32 > 0
+    src: np.ndarray      # int32 citing node
+    dst: np.ndarray      # int32 cited node
+
+    @property
+    def n(self) -> int:
+        return len(self.pub)
+
+    @property
+    def m(self) -> int:
+        return len(self.src)
+
+
+def _distinct_earlier(rng: np.random.Generator, n: int, k: int) -> tuple[np.ndarray, np.ndarray]:
+    """Node i cites min(k, i) distinct uniformly random earlier nodes."""
+    srcs, dsts = [], []
+    small = min(n, k + 1)
+    for i in range(1, small):  # nodes 1..k cite every earlier node
+        srcs.append(np.full(i, i, np.int32))
+        dsts.append(np.arange(i, dtype=np.int32))
+    if n > k + 1:
+        ids = np.arange(k + 1, n, dtype=np.int64)
+        draws = np.floor(rng.random((len(ids), k)) * ids[:, None]).astype(np.int64)
+        draws.sort(axis=1)
+        dup = np.any(draws[:, 1:] == draws[:, :-1], axis=1)
+        for row in np.nonzero(dup)[0]:  # redraw the few rows with a repeated target
+            i = int(ids[row])
+            draws[row] = np.sort(rng.choice(i, size=k, replace=False))
+        srcs.append(np.repeat(ids, k).astype(np.int32))
+        dsts.append(draws.reshape(-1).astype(np.int32))
+    if not srcs:
+        return np.zeros(0, np.int32), np.zeros(0, np.int32)
+    return np.concatenate(srcs), np.concatenate(dsts)
+
+
+def plain_pa_seed(n: int = 10_000, cites: int = 10, seed: int = 42) -> SeedGraph:
+    """Seed DAG: node i cites min(cites, i) earlier nodes; publication epochs uniform over the five
+    prior epochs (-5..-1); fitness lognormal(0, 1)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    src, dst = _distinct_earlier(rng, n, cites)
+    pub = rng.integers(-5, 0, size=n).astype(np.int32)
+    fit = rng.lognormal(0.0, 1.0, size=n).astype(np.float32)
+    return SeedGraph(pub, fit, src, dst)
+
+
+def pareto_seed(n: int = 1_000_000, shape: float = 2.5, mean_indeg: float = 16.0,
+                seed: int = 42) -> SeedGraph:
+    """Seed with Pareto(shape) target in-degrees wired from later nodes.
+
+    Node i draws a target in-degree floor(x_m U^(-1/shape)) (x_m set for the requested mean) and
+    receives that many citations from uniformly chosen later nodes; repeated pairs collapse when
+    the graph is loaded.  Publication epochs follow id order over the five prior epochs."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    xm = mean_indeg * (shape - 1.0) / shape
+    u = 1.0 - rng.random(n)
+    target = np.floor(xm * u ** (-1.0 / shape)).astype(np.int64)
+    later = (n - 1) - np.arange(n, dtype=np.int64)
+    target = np.minimum(target, later)
+    dst = np.repeat(np.arange(n, dtype=np.int64), target)
+    span = np.repeat(later, target)
+    src = dst + 1 + np.floor(rng.random(len(dst)) * span).astype(np.int64)
+    pub = (-5 + (np.arange(n) * 5) // n).astype(np.int32)
+    fit = rng.lognormal(0.0, 1.0, size=n).astype(np.float32)
+    return SeedGraph(pub, fit, src.astype(np.int32), dst.astype(np.int32))
+
+
+def er_seed(n: int = 100_000) -> SeedGraph:
+    """ER seed: n nodes, no edges."""
+    return SeedGraph(np.full(n, -1, np.int32), np.ones(n, np.float32), np.zeros(0, np.int32),
+                     np.zeros(0, np.int32))
+
+
+# ---------------------------------------------------------------- configuration presets
+def plain_pa_params() -> PAParams:
+    """Plain PA growth: 3 epochs x 5,000 agents, Poisson(15) out-degree, alpha=1, tau=5, gamma=1,
+    beta=4, 3 anchors."""
+    return PAParams(alpha=1.0, tau=5.0, gamma=1.0, beta=4.0, mean_out_degree=15.0,
+                    growth_rate=0.0, fixed_new_nodes=5000, num_anchors=3)
+
+
+def scale_pa_params() -> PAParams:
+    """PA at scale: 3 % growth per epoch, Poisson(30) out-degree."""
+    return PAParams(alpha=1.0, tau=5.0, gamma=1.0, beta=4.0, mean_out_degree=30.0,
+                    growth_rate=0.03, fixed_new_nodes=0, num_anchors=3)
+
+
+def ensemble_inputs(replicas: int = 256, lo: int = 5_000, hi: int = 200_000, epochs: int = 10,
+                    seed: int = 42) -> list[ReplicaInput]:
+    """Batched ensemble: seed sizes log-uniform in [lo, hi]; per-replica alpha~U[0.5,1.5],
+    tau~U[2,10], gamma~U[0.5,2], beta~U[1,8]; Poisson(20) out-degree; 3 % growth."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), replicas)).astype(np.int64)
+    out = []
+    for r in range(replicas):
+        g = plain_pa_seed(int(sizes[r]), 10, seed=seed * 1000 + r)
+        p = PAParams(alpha=float(rng.uniform(0.5, 1.5)), tau=float(rng.uniform(2, 10)),
+                     gamma=float(rng.uniform(0.5, 2.0)), beta=float(rng.uniform(1, 8)),
+                     mean_out_degree=20.0, growth_rate=0.03, fixed_new_nodes=0, num_anchors=3)
+        out.append(ReplicaInput(g.pub, g.fitness, g.src, g.dst, p, planned_epochs=epochs))
+    return out

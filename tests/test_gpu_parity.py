@@ -1,0 +1,126 @@
+"""GPU engine vs CPU oracle, through the C ABI.
+
+Everything here is integer or index work on the same Philox streams and the same fixed-point CDF,
+so the bar is bit-exact: forward/backward CSR, in-degrees, new-node attributes, citation choices
+(sorted rows and arrival order) and the byte-model counters must be identical.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from paragraph_gb300 import GrowthEngine, PAParams, ReplicaInput
+from paragraph_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_for(g, params: PAParams, seed: int, replica: int = 0):
+    og = O.OracleGraph(seed, replica)
+    og.load(g.pub, g.fitness, g.src, g.dst)
+    og.set_params(**params.__dict__)
+    return og
+
+
+def _compare_state(eng: GrowthEngine, og: O.OracleGraph, replica: int = 0):
+    n, m = eng.counts(replica)
+    assert (n, m) == (og.n, og.m)
+    for which in (0, 1):
+        off_g, col_g = eng.csr(which, replica)
+        off_o, col_o = og.csr(which)
+        np.testing.assert_array_equal(off_g, off_o, err_msg=f"offsets which={which}")
+        np.testing.assert_array_equal(col_g, col_o, err_msg=f"columns which={which}")
+    ig, og_ = eng.degrees(replica)
+    io, oo = og.degrees()
+    np.testing.assert_array_equal(ig, io)
+    np.testing.assert_array_equal(og_, oo)
+    pg_, fg = eng.nodes(replica)
+    po, fo = og.nodes()
+    np.testing.assert_array_equal(pg_, po)
+    np.testing.assert_array_equal(fg.view(np.uint32), fo.view(np.uint32))
+
+
+@pytest.mark.parametrize("n0,delta,lam,beta", [(300, 40, 4.0, 4.0), (2000, 500, 15.0, 4.0),
+                                               (2000, 500, 15.0, 1.0), (64, 64, 30.0, 8.0)])
+def test_pa_small_bit_exact(gpu, n0, delta, lam, beta):
+    g = W.plain_pa_seed(n0, 10, seed=7)
+    prm = PAParams(alpha=1.0, tau=5.0, gamma=1.0, beta=beta, mean_out_degree=lam,
+                   growth_rate=0.0, fixed_new_nodes=delta, num_anchors=3)
+    with GrowthEngine(seed=1234, record_trace=True) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=3)
+        og = _oracle_for(g, prm, 1234)
+        for _ in range(3):
+            nn, ne = eng.grow_epoch()
+            og.pa_epoch()
+            assert nn == delta
+            assert ne == og.epoch_edges()[1]
+            np.testing.assert_array_equal(eng.arrivals(), og.arrivals())
+            st, so = eng.stats(), og.stats()
+            for k in ("nodes_weighted", "rows_expanded", "elems_streamed", "draws"):
+                assert st[k] == so[k], k
+            _compare_state(eng, og)
+
+
+def test_plain_pa_config_bit_exact(gpu):
+    """Plain PA growth: 10k seed DAG, 3 epochs x 5,000 agents, Poisson(15), 3 anchors."""
+    g = W.plain_pa_seed(10_000, 10, seed=42)
+    prm = W.plain_pa_params()
+    with GrowthEngine(seed=42) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=3)
+        og = _oracle_for(g, prm, 42)
+        for _ in range(3):
+            eng.grow_epoch()
+            og.pa_epoch()
+            s_g, d_g = eng.last_epoch_edges()
+            s_o, d_o = og.last_epoch_edges()
+            np.testing.assert_array_equal(s_g, s_o)
+            np.testing.assert_array_equal(d_g, d_o)
+        _compare_state(eng, og)
+
+
+@pytest.mark.parametrize("p", [1e-5, 1e-4, 1e-3, 0.0, 1.0])
+def test_er_bit_exact(gpu, p):
+    n0, delta = (20_000, 2000) if p < 1.0 else (3000, 50)
+    s = W.er_seed(n0)
+    with GrowthEngine(seed=99) as eng:
+        eng.load_graph(s.pub, s.fitness, s.src, s.dst)
+        og = O.OracleGraph(99, 0)
+        og.load(s.pub, s.fitness, s.src, s.dst)
+        for _ in range(2):
+            ne = eng.er_epoch(delta, p)
+            og.er_epoch(delta, p)
+            assert ne == og.epoch_edges()[1]
+        _compare_state(eng, og)
+        if p == 1.0:
+            assert og.m == delta * n0 + delta * (n0 + delta)
+
+
+def test_run_epochs_graph_matches_sequential(gpu):
+    g = W.plain_pa_seed(3000, 10, seed=3)
+    prm = PAParams(mean_out_degree=12.0, growth_rate=0.05, fixed_new_nodes=0)
+    with GrowthEngine(seed=5) as a, GrowthEngine(seed=5) as b:
+        a.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=6)
+        b.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=6)
+        for _ in range(6):
+            a.grow_epoch()
+        b.run_epochs(6, use_graph=True)
+        for which in (0, 1):
+            for x, y in zip(a.csr(which), b.csr(which)):
+                np.testing.assert_array_equal(x, y)
+
+
+def test_replicas_match_independent_oracles(gpu):
+    reps = W.ensemble_inputs(replicas=5, lo=500, hi=4000, epochs=3, seed=11)
+    with GrowthEngine(seed=77, replicas=len(reps)) as eng:
+        eng.load_replicas(reps)
+        ogs = []
+        for r, ri in enumerate(reps):
+            og = O.OracleGraph(77, r)
+            og.load(ri.pub_epoch, ri.fitness, ri.src, ri.dst)
+            og.set_params(**ri.params.__dict__)
+            ogs.append(og)
+        for _ in range(3):
+            eng.grow_epoch()
+            for og in ogs:
+                og.pa_epoch()
+        for r, og in enumerate(ogs):
+            _compare_state(eng, og, replica=r)
