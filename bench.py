@@ -1,0 +1,350 @@
+"""Benchmark of the per-epoch graph-growth step (citation edges per second on one GB300).
+
+Default workload -- PA at scale: a 1,000,000-node seed with Pareto(2.5) in-degrees (about 15.4M
+citations), grown 30 epochs at 3 % per epoch (about 2.43M nodes and 44M new citations), Poisson(30)
+out-degree, alpha=1, tau=5, gamma=1, beta=4, 2-hop neighbourhoods of 3 anchors.  One step regrows all
+30 epochs from the device-resident seed (restore + one CUDA-graph replay).  Inputs are synthetic
+(seeded numpy), the working set (CSR arrays, 0.5-0.9 GB) is larger than L2 (129 MB).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value   = new citations of the K timed steps / their device time (CUDA events on the engine's
+          stream, inputs resident in HBM), max over ranks, summed over ranks.
+e2e     = the same metric through the C ABI from host buffers: load the seed (host CSR build +
+          H2D), grow 30 epochs, copy every new citation back (D2H), wall clock.
+roofline: the agent kernel (dominant), algorithmic bytes / its summed CUDA-event time.
+cpu_baseline: the CPU oracle (OpenMP, all host threads) on a bounded sample of the same workload.
+--impl reference times that CPU path alone (the reference itself cannot be built here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = "pa_scale_1M_seed_30_epochs_3pct"
+EPOCHS = 30
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "0x1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def seed_graph(seed: int):
+    from paragraph_gb300 import workloads as W
+
+    return W.pareto_seed(1_000_000, 2.5, 16.0, seed=seed), W.scale_pa_params()
+
+
+def traffic_per_agent_byte() -> float | None:
+    """DRAM bytes per algorithmic byte of the agent kernel, from the committed ncu summary."""
+    p = ROOT / "profiles" / "agents_traffic.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        return float(d["dram_bytes"]) / float(d["bytes_alg"])
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------ CPU legs (oracle)
+def cpu_sample(g, prm, seed: int, max_epochs: int = 3, budget_s: float = 12.0) -> dict:
+    """Time the OpenMP oracle (all host threads) on the first epochs of the workload."""
+    import oracle as O
+
+    og = O.OracleGraph(seed, 0)
+    og.load(g.pub, g.fitness, g.src, g.dst)
+    og.set_params(**prm.__dict__)
+    threads = os.cpu_count() or 1
+    edges, secs, epochs = 0, 0.0, 0
+    while epochs < max_epochs and (epochs == 0 or secs < budget_s):
+        m0 = og.m
+        t0 = time.perf_counter()
+        og.pa_epoch(threads)
+        secs += time.perf_counter() - t0
+        edges += og.m - m0
+        epochs += 1
+    og.close()
+    return {"value": edges / secs, "unit": "citations/s", "cores": threads, "kind": "port",
+            "sample": f"first {epochs} epoch(s) of the workload from the seed ({edges} citations, "
+                      f"{secs:.1f} s), CPU oracle with OpenMP"}
+
+
+def run_reference(args) -> None:
+    world, rank, _, dist = dist_setup()
+    if rank != 0:
+        barrier(dist)
+        return
+    import oracle as O
+
+    g, prm = seed_graph(args.seed)
+    og = O.OracleGraph(args.seed, 0)
+    og.load(g.pub, g.fitness, g.src, g.dst)
+    og.set_params(**prm.__dict__)
+    threads = os.cpu_count() or 1
+    # each step = epoch 0 of the workload from the seed (a bounded sample; the oracle reloads the
+    # seed between steps outside the timed region)
+    def one_step():
+        og2 = O.OracleGraph(args.seed, 0)
+        og2.load(g.pub, g.fitness, g.src, g.dst)
+        og2.set_params(**prm.__dict__)
+        t0 = time.perf_counter()
+        og2.pa_epoch(threads)
+        dt = time.perf_counter() - t0
+        e = og2.epoch_edges()[1]
+        og2.close()
+        return e, dt
+
+    for _ in range(args.warmup):
+        one_step()
+    edges, secs = 0, 0.0
+    for _ in range(args.steps):
+        e, dt = one_step()
+        edges += e
+        secs += dt
+    v = edges / secs
+    line = {"metric": "citation edges/sec (PA growth step)", "value": v, "unit": "citations/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/u64/f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "step": "epoch 0 of the workload from the seed",
+                       "parallelism": "replicas only"},
+            "cpu_baseline": {"value": v, "unit": "citations/s", "cores": threads, "kind": "port",
+                             "sample": "epoch 0 of the workload per step; CPU oracle (the "
+                                       "reference cannot be built: cuCollections is absent)"},
+            "e2e": {"value": v, "unit": "citations/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+
+
+# ------------------------------------------------------------------ GPU leg
+def run_ours(args) -> None:
+    world, rank, local, dist = dist_setup()
+    from paragraph_gb300 import GrowthEngine
+
+    seed = args.seed + rank
+    g, prm = seed_graph(seed)
+    eng = GrowthEngine(seed=seed, device=local)
+    eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=EPOCHS)
+    eng.checkpoint()
+
+    def step():
+        eng.restore()
+        return eng.run_epochs(EPOCHS, use_graph=True)
+
+    for _ in range(args.warmup):
+        step()
+    agents_ms = agents_bytes = 0.0
+    edges = 0
+    launches = 0
+    barrier(dist)
+    eng.sync()
+    with ClockSampler(local) as clocks:
+        t_wall = time.perf_counter()
+        eng.timer_start()
+        for _ in range(args.steps):
+            edges += step()
+            st = eng.stats()
+            agents_ms += st["run_ms_agents"]
+            agents_bytes += st["run_bytes_alg_agents"]
+            launches += st["run_kernel_launches"]
+        ms = eng.timer_stop()
+        wall = time.perf_counter() - t_wall
+    barrier(dist)
+    ms_max = reduce_max(dist, ms)
+    edges_all = reduce_sum(dist, float(edges))
+    value = edges_all / (ms_max / 1000.0)
+
+    # end to end through the C ABI from host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e_edges, e2e_secs = 0, 0.0
+        h2d = d2h = 0
+        for i in range(max(1, args.e2e_steps)):
+            with GrowthEngine(seed=seed, device=local) as e2:
+                t0 = time.perf_counter()
+                e2.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=EPOCHS)
+                n0, m0 = e2.counts()
+                ne = e2.run_epochs(EPOCHS, use_graph=True)
+                n1, m1 = e2.counts()
+                src, dst = e2.edges(m0, m1 - m0)
+                dt = time.perf_counter() - t0
+            e2e_edges += ne
+            e2e_secs += dt
+            h2d = 4 * n0 * 3 + 8 * (n0 + 1) * 2 + 4 * m0 * 2  # pub, fitness, indeg, both CSRs
+            d2h = 4 * (m1 - m0) + 8 * (n1 + 1)  # new targets + forward offsets for the sources
+        e2e = {"value": e2e_edges / e2e_secs, "unit": "citations/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
+
+    if rank != 0:
+        eng.close()
+        return
+    peak, peak_kind = peaks()
+    achieved = agents_bytes / (agents_ms / 1000.0) / 1e9 if agents_ms > 0 else 0.0
+    ratio = traffic_per_agent_byte()
+    per_launch_alg = agents_bytes / max(1, args.steps * EPOCHS * 2)
+    line = {
+        "metric": "citation edges/sec (PA growth step)",
+        "value": value, "unit": "citations/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32/u64/f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "seed_nodes": g.n, "seed_citations": g.m,
+                   "epochs_per_step": EPOCHS, "growth": 0.03, "mean_out_degree": 30,
+                   "alpha": 1.0, "tau": 5.0, "gamma": 1.0, "beta": 4.0, "anchors": 3,
+                   "l2": "inputs larger than L2 (CSR 0.5-0.9 GB)", "parallelism": "replicas only"},
+        "roofline": {"bound": "hbm", "kernel": "k_agents", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None,
+                     "traffic": per_launch_alg * ratio if ratio else None},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "wall_s": wall,
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample(g, prm, seed)
+    eng.close()
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

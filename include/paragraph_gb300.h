@@ -111,6 +111,22 @@ typedef struct {
     double ms_agents;          /* the agent kernel(s) */
     double ms_csr;             /* CSR append */
     double ms_er;              /* ER count + emit (ER epochs) */
+    /* totals of the last pg_run_epochs call (every epoch of the run) */
+    int64_t run_epochs;
+    int64_t run_new_nodes;
+    int64_t run_new_edges;
+    int64_t run_rows_expanded;
+    int64_t run_elems_streamed;
+    int64_t run_draws;
+    int64_t run_bwd_moved;
+    int64_t run_nodes_weighted;
+    int64_t run_bytes_alg;
+    int64_t run_bytes_alg_agents;
+    double run_ms_weights;     /* sums over the run's epochs, CUDA events on the context stream */
+    double run_ms_setup;
+    double run_ms_agents;
+    double run_ms_csr;
+    int64_t run_kernel_launches; /* kernels the run enqueued (graph nodes when captured) */
 } pg_stats;
 
 /* ---- lifecycle ---- */
@@ -164,6 +180,16 @@ pg_status pg_get_stats(const pg_ctx* ctx, pg_stats* out);
 pg_status pg_sync(pg_ctx* ctx);
 /* Reads the device error word; PG_OK when no kernel reported a fault. */
 pg_status pg_check_device(pg_ctx* ctx);
+/* Stream-ordered timer on the context's stream: stop waits for the stream and returns the
+ * milliseconds between the two CUDA events. */
+pg_status pg_timer_start(pg_ctx* ctx);
+pg_status pg_timer_stop(pg_ctx* ctx, double* ms);
+
+/* ---- checkpoint / resume ---- */
+/* Save the whole graph state (nodes, both CSRs, epoch counter) in device memory; pg_restore puts
+ * it back, so a run can be repeated or resumed bit-exactly (the RNG is counter-based). */
+pg_status pg_checkpoint(pg_ctx* ctx);
+pg_status pg_restore(pg_ctx* ctx);
 
 /* ---- host-side building blocks shared with tests ---- */
 /* Philox4x32-10 block (Salmon et al., SC'11) for counter c[4] and key k[2]. */

@@ -36,6 +36,7 @@ EXPORTED = [
     "pg_copy_degrees", "pg_copy_nodes", "pg_copy_csr", "pg_copy_arrivals", "pg_set_timing",
     "pg_get_stats", "pg_sync", "pg_check_device", "pg_philox4x32_10", "pg_poisson_table",
     "pg_logf_host", "pg_expf_host", "pg_log_host", "pg_exp_host", "pg_version",
+    "pg_timer_start", "pg_timer_stop", "pg_checkpoint", "pg_restore",
 ]
 
 
@@ -67,7 +68,12 @@ class _Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "epoch", "new_nodes", "new_edges", "nodes_weighted", "rows_expanded", "elems_streamed",
         "draws", "bwd_moved", "bytes_alg", "bytes_alg_agents")] + [
-        (n, C.c_double) for n in ("ms_total", "ms_weights", "ms_setup", "ms_agents", "ms_csr", "ms_er")]
+        (n, C.c_double) for n in ("ms_total", "ms_weights", "ms_setup", "ms_agents", "ms_csr", "ms_er")] + [
+        (n, C.c_int64) for n in (
+        "run_epochs", "run_new_nodes", "run_new_edges", "run_rows_expanded", "run_elems_streamed",
+        "run_draws", "run_bwd_moved", "run_nodes_weighted", "run_bytes_alg", "run_bytes_alg_agents")] + [
+        (n, C.c_double) for n in ("run_ms_weights", "run_ms_setup", "run_ms_agents", "run_ms_csr")] + [
+        ("run_kernel_launches", C.c_int64)]
 
 
 @dataclass
@@ -146,6 +152,10 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_log_host": (C.c_double, [C.c_double]),
         "pg_exp_host": (C.c_double, [C.c_double]),
         "pg_version": (C.c_char_p, []),
+        "pg_timer_start": (i32, [vp]),
+        "pg_timer_stop": (i32, [vp, P(C.c_double)]),
+        "pg_checkpoint": (i32, [vp]),
+        "pg_restore": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -327,3 +337,18 @@ class GrowthEngine:
 
     def check_device(self) -> None:
         self._check(self._lib.pg_check_device(self._ctx))
+
+    def timer_start(self) -> None:
+        self._check(self._lib.pg_timer_start(self._ctx))
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        self._check(self._lib.pg_timer_stop(self._ctx, C.byref(ms)))
+        return ms.value
+
+    def checkpoint(self) -> None:
+        """Save the graph state in device memory (checkpoint/resume is bit-exact)."""
+        self._check(self._lib.pg_checkpoint(self._ctx))
+
+    def restore(self) -> None:
+        self._check(self._lib.pg_restore(self._ctx))

@@ -424,16 +424,21 @@ void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s) {
     k_edges_check<<<1, 256, 0, s>>>(A, agents);
 }
 
+// Occupancy of the persistent agent kernels; called once per process before any capture.
+cudaError_t init_agent_kernels() {
+    if (g_blocks_small) return cudaSuccess;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &g_blocks_small, k_agents<kKSmall, false>, kAgentWarps * 32, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_big, k_agents<kKMax, true>,
+                                                          kAgentWarps * 32, 0);
+    if (g_blocks_small < 1) g_blocks_small = 1;
+    if (g_blocks_big < 1) g_blocks_big = 1;
+    return e;
+}
+
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) {
     if (agents <= 0) return;
-    if (!g_blocks_small) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_small, k_agents<kKSmall, false>,
-                                                      kAgentWarps * 32, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_big, k_agents<kKMax, true>,
-                                                      kAgentWarps * 32, 0);
-        if (g_blocks_small < 1) g_blocks_small = 1;
-        if (g_blocks_big < 1) g_blocks_big = 1;
-    }
     int64_t need = (agents + kAgentWarps - 1) / kAgentWarps;
     int64_t grid = (int64_t)num_sms * g_blocks_small;
     if (grid > need) grid = need;

@@ -77,6 +77,9 @@ struct pg_ctx {
     std::vector<int64_t> rep_last_first, rep_last_count;
     bool timing = true;
     cudaEvent_t ev[6] = {};
+    std::vector<cudaEvent_t> run_ev;  // 5 per epoch of a pg_run_epochs call
+    cudaEvent_t tev[2] = {};          // pg_timer_start / pg_timer_stop
+    int64_t launches = 0;             // kernels enqueued by the last run
     // CUDA graph of a multi-epoch run
     cudaGraphExec_t gexec = nullptr;
     int64_t g_epoch0 = -1;
@@ -422,24 +425,43 @@ pg_status device_error(pg_ctx* c) {
 
 float ms_between(cudaEvent_t a, cudaEvent_t b) {
     float ms = 0.0f;
-    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.0f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+        cudaGetLastError();  // an unavailable timing must not surface as a later launch error
+        return 0.0f;
+    }
     return ms;
 }
 
-// Enqueue one PA epoch (no synchronisation).  agents = total new nodes of the epoch.
-void enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, bool events) {
+// Enqueue one PA epoch (no synchronisation).  agents = total new nodes of the epoch.  Returns the
+// first launch error with the stage that raised it.
+pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t* ev) {
+    const bool events = ev != nullptr;
     Arena A = make_arena(c);
     cudaStream_t s = c->stream;
-    if (events) cudaEventRecord(c->ev[0], s);
+    cudaError_t e;
+#define PG_STAGE(name)                                                                          \
+    if ((e = cudaPeekAtLastError()) != cudaSuccess) {                                           \
+        cudaGetLastError();                                                                     \
+        return fail(c, PG_ERR_CUDA, std::string("launch error in ") + name + ": " + cudaGetErrorString(e)); \
+    }
+    if (events) cudaEventRecord(ev[0], s);
     launch_epoch_begin(A, epoch, 1, s);
+    PG_STAGE("epoch begin");
     launch_weights(A, s);
-    if (events) cudaEventRecord(c->ev[1], s);
+    PG_STAGE("weights");
+    if (events) cudaEventRecord(ev[1], s);
     launch_agent_setup(A, agents, s);
-    if (events) cudaEventRecord(c->ev[2], s);
+    PG_STAGE("agent setup");
+    if (events) cudaEventRecord(ev[2], s);
     launch_agents(A, agents, c->num_sms, s);
-    if (events) cudaEventRecord(c->ev[3], s);
+    PG_STAGE("agents");
+    if (events) cudaEventRecord(ev[3], s);
     launch_bwd_append(A, agents, c->num_sms, s);
-    if (events) cudaEventRecord(c->ev[4], s);
+    PG_STAGE("backward append");
+    if (events) cudaEventRecord(ev[4], s);
+#undef PG_STAGE
+    c->launches += kPaEpochKernels;
+    return PG_OK;
 }
 
 // Planned agents of the next epoch and the node/edge needs of every replica.
@@ -452,6 +474,23 @@ int64_t plan_epoch(pg_ctx* c, std::vector<int64_t>* deltas) {
         tot += d;
     }
     return tot;
+}
+
+// Algorithmic bytes of the PA epoch (the minimum traffic of the algorithm, not what a given
+// implementation moves):
+//   agents : per adjacency row read 32 B (fwd and bwd begin/end, int64), per streamed neighbour
+//            8 B (its int32 id and its fp32 weight), per draw 32 B (one CDF sector), per edge 16 B
+//            (forward column, in-degree counter, rank, destination)
+//   weights: per node 44 B (fitness, in-degree, publication epoch, weight write, weight read, CDF
+//            write, CDF read+write in the tile-offset pass)
+//   csr    : 8 B per moved backward entry, 12 B per new edge (place + sort), 24 B per node
+//            (old and new backward offsets, length)
+int64_t agent_bytes(int64_t rows, int64_t elems, int64_t draws, int64_t edges) {
+    return 32 * rows + 8 * elems + 32 * draws + 16 * edges;
+}
+int64_t weight_bytes(int64_t nodes) { return 44 * nodes; }
+int64_t csr_bytes(int64_t moved, int64_t edges, int64_t nodes, int64_t new_nodes) {
+    return 8 * moved + 12 * edges + 24 * (nodes + new_nodes);
 }
 
 void fill_stats(pg_ctx* c, int64_t new_nodes, bool er) {
@@ -467,11 +506,12 @@ void fill_stats(pg_ctx* c, int64_t new_nodes, bool er) {
     S.bwd_moved = (int64_t)st.bwd_moved;
     const int64_t E = st.edges;
     // byte model: see DESIGN.md ("Algorithmic bytes")
-    const int64_t agents_bytes = 32 * S.rows_expanded + 8 * S.elems_streamed + 32 * S.draws + 16 * E;
-    const int64_t weight_bytes = 44 * S.nodes_weighted;
-    const int64_t csr_bytes = 8 * S.bwd_moved + 12 * E + 24 * (S.nodes_weighted + new_nodes);
-    S.bytes_alg_agents = er ? 0 : agents_bytes;
-    S.bytes_alg = er ? (8 * E + 12 * E + 32 * new_nodes + 8 * S.bwd_moved) : agents_bytes + weight_bytes + csr_bytes;
+    const int64_t ab = agent_bytes(S.rows_expanded, S.elems_streamed, S.draws, E);
+    S.bytes_alg_agents = er ? 0 : ab;
+    // ER: per edge 8 B edge-list write + 12 B CSR append; per new node 32 B (count + offsets)
+    S.bytes_alg = er ? (8 * E + 12 * E + 32 * new_nodes + 8 * S.bwd_moved)
+                     : ab + weight_bytes(S.nodes_weighted) +
+                           csr_bytes(S.bwd_moved, E, S.nodes_weighted, new_nodes);
 }
 
 pg_status finish_epoch(pg_ctx* c, const std::vector<int64_t>& deltas, bool er) {
@@ -561,7 +601,10 @@ pg_status pg_create(pg_ctx** out, const pg_config* cfg) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = dalloc(c->st, 1);
+    if (e == cudaSuccess) e = init_agent_kernels();
+    if (e == cudaSuccess) e = init_csr_kernels();
     for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->tev[i]);
     if (e != cudaSuccess) {
         c->err = std::string("CUDA initialisation failed: ") + cudaGetErrorString(e);
         *out = c;
@@ -598,6 +641,9 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->st);
     for (int i = 0; i < 6; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (int i = 0; i < 2; ++i)
+        if (c->tev[i]) cudaEventDestroy(c->tev[i]);
+    for (cudaEvent_t e : c->run_ev) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -721,8 +767,13 @@ pg_status pg_grow_epoch(pg_ctx* c, int64_t* new_nodes, int64_t* new_edges) {
     int64_t agents = 0;
     pg_status s = prepare_pa(c, deltas, agents);
     if (s != PG_OK) return s;
-    enqueue_pa_epoch(c, c->epoch, agents, c->timing);
-    PG_CUDA(c, cudaGetLastError());
+    cudaGetLastError();  // errors of earlier, unrelated calls are not this epoch's
+    s = enqueue_pa_epoch(c, c->epoch, agents, c->timing ? c->ev : nullptr);
+    if (s != PG_OK) {
+        cudaStreamSynchronize(c->stream);
+        c->poisoned = true;
+        return s;
+    }
     s = finish_epoch(c, deltas, false);
     if (s != PG_OK) return s;
     if (c->timing) {
@@ -778,23 +829,37 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
     const int64_t e0 = c->epoch;
     const int p0 = c->parity;
     const bool events = c->timing;
-    auto enqueue_all = [&]() {
-        for (int e = 0; e < num_epochs; ++e) {
-            const bool last = e == num_epochs - 1;
-            if (events && e == 0) cudaEventRecord(c->ev[5], c->stream);
-            enqueue_pa_epoch(c, e0 + e, agents[(size_t)e], events && last);
+    if (events && (int64_t)c->run_ev.size() < 5 * (int64_t)num_epochs) {
+        const size_t have = c->run_ev.size();
+        c->run_ev.resize((size_t)num_epochs * 5, nullptr);
+        for (size_t i = have; i < c->run_ev.size(); ++i) PG_CUDA(c, cudaEventCreate(&c->run_ev[i]));
+        destroy_graph_exec(c);
+    }
+    auto enqueue_all = [&]() -> pg_status {
+        pg_status es = PG_OK;
+        c->launches = 0;
+        // clear the run totals (captured as a memset node, so every replay clears them too)
+        const size_t cum0 = offsetof(EpochState, cum_rows_expanded);
+        cudaMemsetAsync(reinterpret_cast<char*>(c->st.p) + cum0, 0, sizeof(EpochState) - cum0, c->stream);
+        for (int e = 0; e < num_epochs && es == PG_OK; ++e) {
+            es = enqueue_pa_epoch(c, e0 + e, agents[(size_t)e], events ? &c->run_ev[(size_t)e * 5] : nullptr);
             c->parity ^= 1;
         }
         c->parity = p0;
+        return es;
     };
+    cudaGetLastError();  // errors of earlier, unrelated calls are not this run's
     if (use_graph) {
         if (!(c->gexec && c->g_epoch0 == e0 && c->g_parity0 == p0 && c->g_epochs == num_epochs)) {
             destroy_graph_exec(c);
-            // warm one-time initialisation (occupancy queries, attributes) outside capture
             cudaGraph_t graph;
             PG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            enqueue_all();
+            const pg_status es = enqueue_all();
             cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+            if (es != PG_OK) {
+                if (ce == cudaSuccess) cudaGraphDestroy(graph);
+                return es;
+            }
             if (ce != cudaSuccess) return fail(c, PG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
             ce = cudaGraphInstantiate(&c->gexec, graph, 0);
             cudaGraphDestroy(graph);
@@ -805,7 +870,12 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
         }
         PG_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
     } else {
-        enqueue_all();
+        const pg_status es = enqueue_all();
+        if (es != PG_OK) {
+            cudaStreamSynchronize(c->stream);
+            c->poisoned = true;
+            return es;
+        }
     }
     PG_CUDA(c, cudaGetLastError());
     s = read_back(c);
@@ -823,14 +893,37 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
     if (num_epochs % 2) c->parity ^= 1;
     c->epoch = e0 + num_epochs;
     fill_stats(c, nn, false);
-    c->stats.new_edges = total;
+    pg_stats& S = c->stats;
+    const EpochState& hs = c->h_st;
+    S.run_epochs = (int64_t)hs.cum_epochs;
+    S.run_new_nodes = (int64_t)hs.cum_new_nodes;
+    S.run_new_edges = (int64_t)hs.cum_edges;
+    S.run_rows_expanded = (int64_t)hs.cum_rows_expanded;
+    S.run_elems_streamed = (int64_t)hs.cum_elems_streamed;
+    S.run_draws = (int64_t)hs.cum_draws;
+    S.run_bwd_moved = (int64_t)hs.cum_bwd_moved;
+    S.run_nodes_weighted = (int64_t)hs.cum_nodes_weighted;
+    S.run_bytes_alg_agents = agent_bytes(S.run_rows_expanded, S.run_elems_streamed, S.run_draws, S.run_new_edges);
+    S.run_bytes_alg = S.run_bytes_alg_agents + weight_bytes(S.run_nodes_weighted) +
+                      csr_bytes(S.run_bwd_moved, S.run_new_edges, S.run_nodes_weighted, S.run_new_nodes);
+    S.run_kernel_launches = c->launches;
+    S.run_ms_weights = S.run_ms_setup = S.run_ms_agents = S.run_ms_csr = 0.0;
     if (events) {
-        c->stats.ms_total = ms_between(c->ev[5], c->ev[4]);
-        c->stats.ms_weights = ms_between(c->ev[0], c->ev[1]);
-        c->stats.ms_setup = ms_between(c->ev[1], c->ev[2]);
-        c->stats.ms_agents = ms_between(c->ev[2], c->ev[3]);
-        c->stats.ms_csr = ms_between(c->ev[3], c->ev[4]);
+        for (int e = 0; e < num_epochs; ++e) {
+            cudaEvent_t* ev = &c->run_ev[(size_t)e * 5];
+            S.run_ms_weights += ms_between(ev[0], ev[1]);
+            S.run_ms_setup += ms_between(ev[1], ev[2]);
+            S.run_ms_agents += ms_between(ev[2], ev[3]);
+            S.run_ms_csr += ms_between(ev[3], ev[4]);
+        }
+        cudaEvent_t* last = &c->run_ev[(size_t)(num_epochs - 1) * 5];
+        S.ms_total = ms_between(c->run_ev[0], last[4]);
+        S.ms_weights = ms_between(last[0], last[1]);
+        S.ms_setup = ms_between(last[1], last[2]);
+        S.ms_agents = ms_between(last[2], last[3]);
+        S.ms_csr = ms_between(last[3], last[4]);
     }
+    S.new_edges = total;
     if (new_edges) *new_edges = total;
     return PG_OK;
 }
@@ -1003,6 +1096,89 @@ pg_status pg_check_device(pg_ctx* c) {
     pg_status s = read_back(c);
     if (s != PG_OK) return s;
     return device_error(c);
+}
+
+pg_status pg_timer_start(pg_ctx* c) {
+    if (!c) return PG_ERR_ARG;
+    PG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
+    return PG_OK;
+}
+
+pg_status pg_timer_stop(pg_ctx* c, double* ms) {
+    if (!c || !ms) return PG_ERR_ARG;
+    PG_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
+    PG_CUDA(c, cudaEventSynchronize(c->tev[1]));
+    float f = 0.0f;
+    PG_CUDA(c, cudaEventElapsedTime(&f, c->tev[0], c->tev[1]));
+    *ms = f;
+    return PG_OK;
+}
+
+pg_status pg_checkpoint(pg_ctx* c) {
+    if (!c) return PG_ERR_ARG;
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (c->poisoned) return fail(c, PG_ERR_STATE, "state is inconsistent after a device error");
+    Checkpoint& k = c->ckpt;
+    cudaStream_t s = c->stream;
+    if (k.pub.n != c->S) {
+        PG_CUDA(c, dalloc(k.pub, c->S));
+        PG_CUDA(c, dalloc(k.indeg, c->S));
+        PG_CUDA(c, dalloc(k.fit, c->S));
+        PG_CUDA(c, dalloc(k.fwd_off, c->S + c->R));
+        PG_CUDA(c, dalloc(k.bwd_off, c->S + c->R));
+        PG_CUDA(c, dalloc(k.rep, c->R));
+    }
+    if (k.fwd_col.n != c->M) {
+        PG_CUDA(c, dalloc(k.fwd_col, c->M));
+        PG_CUDA(c, dalloc(k.bwd_col, c->M));
+    }
+    const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
+    PG_CUDA(c, cudaMemcpyAsync(k.pub.p, c->pub.p, 4 * (size_t)c->S, d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(k.indeg.p, c->indeg.p, 4 * (size_t)c->S, d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(k.fit.p, c->fit.p, 4 * (size_t)c->S, d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(k.fwd_off.p, c->fwd_off.p, 8 * (size_t)(c->S + c->R), d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(k.bwd_off.p, c->bwd_off[c->parity].p, 8 * (size_t)(c->S + c->R), d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(k.rep.p, c->rep.p, sizeof(Replica) * (size_t)c->R, d2d, s));
+    for (const HostRep& h : c->hrep) {
+        if (!h.m) continue;
+        PG_CUDA(c, cudaMemcpyAsync(k.fwd_col.p + h.ebase, c->fwd_col.p + h.ebase, 4 * (size_t)h.m, d2d, s));
+        PG_CUDA(c, cudaMemcpyAsync(k.bwd_col.p + h.ebase, c->bwd_col[c->parity].p + h.ebase, 4 * (size_t)h.m, d2d, s));
+    }
+    PG_CUDA(c, cudaStreamSynchronize(s));
+    k.epoch = c->epoch;
+    k.parity = c->parity;
+    k.hrep = c->hrep;
+    k.valid = true;
+    return PG_OK;
+}
+
+pg_status pg_restore(pg_ctx* c) {
+    if (!c) return PG_ERR_ARG;
+    Checkpoint& k = c->ckpt;
+    if (!k.valid || k.pub.n != c->S || k.fwd_col.n != c->M)
+        return fail(c, PG_ERR_STATE, "no checkpoint matches the current arena");
+    cudaStream_t s = c->stream;
+    const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
+    // the checkpoint's backward copy goes into the buffer that was current when it was taken
+    const int par = k.parity;
+    PG_CUDA(c, cudaMemcpyAsync(c->pub.p, k.pub.p, 4 * (size_t)c->S, d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(c->indeg.p, k.indeg.p, 4 * (size_t)c->S, d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(c->fit.p, k.fit.p, 4 * (size_t)c->S, d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(c->fwd_off.p, k.fwd_off.p, 8 * (size_t)(c->S + c->R), d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(c->bwd_off[par].p, k.bwd_off.p, 8 * (size_t)(c->S + c->R), d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(c->rep.p, k.rep.p, sizeof(Replica) * (size_t)c->R, d2d, s));
+    for (const HostRep& h : k.hrep) {
+        if (!h.m) continue;
+        PG_CUDA(c, cudaMemcpyAsync(c->fwd_col.p + h.ebase, k.fwd_col.p + h.ebase, 4 * (size_t)h.m, d2d, s));
+        PG_CUDA(c, cudaMemcpyAsync(c->bwd_col[par].p + h.ebase, k.bwd_col.p + h.ebase, 4 * (size_t)h.m, d2d, s));
+    }
+    PG_CUDA(c, cudaMemsetAsync(c->inc.p, 0, 4 * (size_t)c->S, s));
+    PG_CUDA(c, cudaStreamSynchronize(s));
+    c->epoch = k.epoch;
+    c->parity = par;
+    c->hrep = k.hrep;
+    c->poisoned = false;
+    return PG_OK;
 }
 
 void pg_philox4x32_10(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]) {

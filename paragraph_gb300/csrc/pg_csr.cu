@@ -258,22 +258,33 @@ __global__ void __launch_bounds__(1024) k_sort_large(Arena A) {
 }
 
 __global__ void k_epoch_end(Arena A, int64_t agents) {
-    if (A.st->error) return;
+    EpochState* st = A.st;
+    if (st->error) return;
     for (int r = threadIdx.x; r < A.R; r += blockDim.x) {
         Replica& rp = A.rep[r];
         const int64_t er = A.eoff[rp.abase + rp.delta] - A.eoff[rp.abase];
         rp.m += er;
         rp.n += rp.delta;
     }
+    if (threadIdx.x == 0) {
+        st->cum_rows_expanded += st->rows_expanded;
+        st->cum_elems_streamed += st->elems_streamed;
+        st->cum_draws += st->draws;
+        st->cum_bwd_moved += st->bwd_moved;
+        st->cum_nodes_weighted += st->nodes_weighted;
+        st->cum_edges += (unsigned long long)A.eoff[agents];
+        st->cum_new_nodes += (unsigned long long)agents;
+        st->cum_epochs += 1;
+    }
+}
+
+// The large-segment sort uses 160 KiB of dynamic shared memory; called once per process.
+cudaError_t init_csr_kernels() {
+    return cudaFuncSetAttribute(k_sort_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                kBitmapWords * 4);
 }
 
 void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_sort_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kBitmapWords * 4);
-        attr_set = true;
-    }
     k_bwd_len<<<A.ntiles, kTileThreads, 0, s>>>(A);
     launch_tile_scan(A, 1, s);
     k_bwd_off<<<A.ntiles, kTileThreads, 0, s>>>(A);

@@ -75,6 +75,15 @@ struct EpochState {
     unsigned long long draws;
     unsigned long long bwd_moved;
     unsigned long long nodes_weighted;
+    // run totals, accumulated by the epoch-end kernel and cleared by the host at run start
+    unsigned long long cum_rows_expanded;
+    unsigned long long cum_elems_streamed;
+    unsigned long long cum_draws;
+    unsigned long long cum_bwd_moved;
+    unsigned long long cum_nodes_weighted;
+    unsigned long long cum_edges;
+    unsigned long long cum_new_nodes;
+    unsigned long long cum_epochs;
 };
 
 // Device pointers of the arena (passed by value to kernels).
@@ -173,6 +182,9 @@ __device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64
 #endif
 
 // ---------------------------------------------------------------- host launchers
+// Kernels one PA epoch enqueues: epoch begin (1), weights + CDF (4), agent setup + offset scan +
+// check (5), agent kernels (2), backward append incl. epoch end (8).
+constexpr int kPaEpochKernels = 20;
 void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s);
 void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cudaStream_t s);
 void launch_weights(const Arena& A, cudaStream_t s);
@@ -187,5 +199,7 @@ void launch_scan_i64(const int64_t* in, int64_t* out, int64_t n, int64_t* blocks
 void launch_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_t* blocksum,
                             cudaStream_t s);
 int scan_blocks_needed(int64_t n);
+cudaError_t init_agent_kernels();
+cudaError_t init_csr_kernels();
 
 }  // namespace pg

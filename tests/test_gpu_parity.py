@@ -124,3 +124,23 @@ def test_replicas_match_independent_oracles(gpu):
                 og.pa_epoch()
         for r, og in enumerate(ogs):
             _compare_state(eng, og, replica=r)
+
+
+def test_checkpoint_restore_regrows_identically(gpu):
+    g = W.plain_pa_seed(4000, 10, seed=9)
+    prm = PAParams(mean_out_degree=20.0, growth_rate=0.03, fixed_new_nodes=0)
+    with GrowthEngine(seed=8) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=8)
+        eng.checkpoint()
+        e1 = eng.run_epochs(8, use_graph=True)
+        a = [eng.csr(w) for w in (0, 1)]
+        eng.restore()
+        assert eng.counts() == (g.n, len(set(zip(g.src.tolist(), g.dst.tolist()))))
+        e2 = eng.run_epochs(8, use_graph=True)  # replays the captured graph
+        assert e1 == e2
+        for (o1, c1), (o2, c2) in zip(a, [eng.csr(w) for w in (0, 1)]):
+            np.testing.assert_array_equal(o1, o2)
+            np.testing.assert_array_equal(c1, c2)
+        st = eng.stats()
+        assert st["run_epochs"] == 8 and st["run_new_edges"] == e2
+        assert st["run_kernel_launches"] == 8 * 20
