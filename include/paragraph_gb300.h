@@ -63,7 +63,18 @@ typedef struct {
     uint64_t seed;         /* Philox key */
     int32_t weight_model;  /* PG_WEIGHTS_* */
     int32_t record_trace;  /* 1: keep each epoch's arrival-ordered citations for pg_loglik_* */
+    int32_t sampler;       /* PG_SAMPLER_* */
+    int32_t reserved;
 } pg_config;
+
+/* How an agent draws its citations; both give the same law (weighted sampling without
+ * replacement with weights w_j beta^[j in 2-hop ball]) from different random streams. */
+enum {
+    PG_SAMPLER_THINNING = 0,  /* Poisson thinning against ball membership; cost independent of the
+                                 ball's size (default) */
+    PG_SAMPLER_ENUMERATE = 1  /* warp-cooperative streaming of the whole 2-hop ball with per-node
+                                 exponential keys */
+};
 
 /* Per-replica model parameters (baseline functor). */
 typedef struct {

@@ -44,6 +44,7 @@ def _load() -> C.CDLL:
         "og_set_params": (i32, [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double, i64, i32]),
         "og_set_epoch": (None, [vp, i64]),
+        "og_set_sampler": (None, [vp, i32]),
         "og_epoch": (i64, [vp]),
         "og_pa_epoch": (i32, [vp, i32]),
         "og_er_epoch": (i32, [vp, i64, C.c_double, i32]),
@@ -140,6 +141,10 @@ class OracleGraph:
 
     def set_epoch(self, e: int) -> None:
         self._lib.og_set_epoch(self._g, e)
+
+    def set_sampler(self, sampler: int) -> None:
+        """0: thinning sampler (default); 1: full 2-hop neighbourhood enumeration."""
+        self._lib.og_set_sampler(self._g, sampler)
 
     def pa_epoch(self, threads: int = 0) -> None:
         st = self._lib.og_pa_epoch(self._g, threads)

@@ -235,9 +235,10 @@ struct og_graph {
     int64_t epoch;
     /* params */
     float alpha_f, gamma_f, tau_f;
-    double beta_m1, lambda, growth_rate;
+    double beta_m1, p_global, lambda, growth_rate;
     int64_t fixed_new;
     int anchors;
+    int sampler; /* 0 thinning, 1 neighbourhood enumeration */
     uint64_t table[OG_TABLE];
     /* nodes */
     int64_t n;
@@ -291,6 +292,7 @@ int og_set_params(og_graph* g, double alpha, double tau, double gamma, double be
     g->gamma_f = (float)gamma;
     g->tau_f = (float)tau;
     g->beta_m1 = beta - 1.0;
+    g->p_global = 1.0 / beta;
     g->lambda = lambda;
     g->growth_rate = growth_rate;
     g->fixed_new = fixed_new;
@@ -300,6 +302,7 @@ int og_set_params(og_graph* g, double alpha, double tau, double gamma, double be
 }
 
 void og_set_epoch(og_graph* g, int64_t epoch) { g->epoch = epoch; }
+void og_set_sampler(og_graph* g, int sampler) { g->sampler = sampler; }
 int64_t og_epoch(const og_graph* g) { return g->epoch; }
 
 static int cmp_i32(const void* a, const void* b) {
@@ -575,6 +578,174 @@ static int sample_agent(const og_graph* g, int64_t a, const float* w, const uint
     return taken;
 }
 
+/* ------------------------------------------------------------------ thinning sampler */
+static int bsearch32(const int32_t* a, int64_t n, int32_t v) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = lo + (hi - lo) / 2;
+        if (a[mid] < v)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo < n && a[lo] == v;
+}
+
+/* j in the 2-hop undirected ball of the anchors <=> j in Z = anchors U adj(anchors), or an
+ * adjacency row of j meets Z.  Pure set membership: any evaluation order gives the same answer. */
+static int in_ball(const og_graph* g, const int32_t* Z, int64_t nz, int32_t j) {
+    if (bsearch32(Z, nz, j)) return 1;
+    for (int dir = 0; dir < 2; dir++) {
+        const int64_t* off = dir ? g->bwd_off : g->fwd_off;
+        const int32_t* col = dir ? g->bwd_col : g->fwd_col;
+        for (int64_t p = off[j]; p < off[j + 1]; p++)
+            if (bsearch32(Z, nz, col[p])) return 1;
+    }
+    return 0;
+}
+
+enum { S_FALLBACK = 9 };
+
+/* Thinning sampler.  One Poisson event stream over all nodes with rate beta*w_j: each event picks
+ * j from the global CDF and is "global" with probability 1/beta (always accepted) or "boost"
+ * (accepted iff j is in the ball).  Node j's accepted events have rate w_j beta^[j in ball], so the
+ * first k distinct accepted nodes are a successive-sampling draw with those weights.  After
+ * 64k+256 events the remaining draws continue without replacement from the CDF minus the chosen
+ * weight (exact by memorylessness), which bounds the work when a few nodes hold most weight. */
+static int sample_agent_thin(const og_graph* g, int64_t a, const uint64_t* cdf, int64_t npos,
+                             int32_t* out_sorted, int32_t* out_arr, int64_t* cnt, int32_t** zbuf,
+                             int64_t* zcap) {
+    const int64_t n = g->n;
+    const uint32_t ep = (uint32_t)g->epoch, rep = g->replica, unit = (uint32_t)a;
+    uint32_t r[4];
+    rng(g->seed, S_OUTDEG, rep, ep, unit, 0, r);
+    uint64_t u = join64(r[0], r[1]);
+    int kraw = OG_TABLE - 1;
+    for (int i = 0; i < OG_TABLE; i++)
+        if (u < g->table[i]) {
+            kraw = i;
+            break;
+        }
+    int64_t k = kraw < 1 ? 1 : kraw;
+    if (k > n) k = n;
+    if (k > npos) k = npos;
+    int32_t anchor[4];
+    rng(g->seed, S_ANCHOR, rep, ep, unit, 0, r);
+    for (int i = 0; i < g->anchors; i++) anchor[i] = (int32_t)(((uint64_t)r[i] * (uint64_t)n) >> 32);
+    /* Z = sorted unique anchors U their forward and backward rows */
+    int64_t nz = g->anchors;
+    for (int i = 0; i < g->anchors; i++)
+        nz += (g->fwd_off[anchor[i] + 1] - g->fwd_off[anchor[i]]) +
+              (g->bwd_off[anchor[i] + 1] - g->bwd_off[anchor[i]]);
+    cnt[0] += nz;
+    if (nz > *zcap) {
+        *zcap = nz;
+        *zbuf = (int32_t*)realloc(*zbuf, sizeof(int32_t) * (size_t)nz);
+    }
+    int32_t* Z = *zbuf;
+    int64_t w = 0;
+    for (int i = 0; i < g->anchors; i++) {
+        Z[w++] = anchor[i];
+        for (int64_t p = g->fwd_off[anchor[i]]; p < g->fwd_off[anchor[i] + 1]; p++) Z[w++] = g->fwd_col[p];
+        for (int64_t p = g->bwd_off[anchor[i]]; p < g->bwd_off[anchor[i] + 1]; p++) Z[w++] = g->bwd_col[p];
+    }
+    qsort(Z, (size_t)nz, sizeof(int32_t), cmp_i32);
+    int64_t uz = 0;
+    for (int64_t i = 0; i < nz; i++)
+        if (i == 0 || Z[i] != Z[i - 1]) Z[uz++] = Z[i];
+    nz = uz;
+
+    const uint64_t Wq = cdf[n - 1];
+    int taken = 0;
+    const int64_t maxev = 64 * k + 256;
+    int64_t events = 0, tests = 0;
+    for (int64_t i = 0; i < maxev && taken < k; i++) {
+        rng(g->seed, S_GLOBAL, rep, ep, unit, (uint32_t)i, r);
+        uint64_t y = hi_mul64(join64(r[0], r[1]), Wq);
+        int64_t lo = 0, hi = n - 1;
+        while (lo < hi) {
+            int64_t mid = lo + (hi - lo) / 2;
+            if (cdf[mid] > y)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        int32_t j = (int32_t)lo;
+        events++;
+        int glob = unif_d(r[2], r[3]) <= g->p_global;
+        if (!glob) {
+            tests++;
+            if (!in_ball(g, Z, nz, j)) continue;
+        }
+        int dup = 0;
+        for (int q = 0; q < taken; q++)
+            if (out_arr[q] == j) {
+                dup = 1;
+                break;
+            }
+        if (!dup) out_arr[taken++] = j;
+    }
+    if (taken < k) {
+        /* exact continuation without replacement over the unchosen nodes */
+        int32_t c_id[256];
+        uint64_t c_q[256];
+        int nc = 0;
+        uint64_t R = Wq;
+        for (int q = 0; q < taken; q++) {
+            int32_t j = out_arr[q];
+            uint64_t qj = cdf[j] - (j > 0 ? cdf[j - 1] : 0);
+            int pos = nc;
+            while (pos > 0 && c_id[pos - 1] > j) {
+                c_id[pos] = c_id[pos - 1];
+                c_q[pos] = c_q[pos - 1];
+                pos--;
+            }
+            c_id[pos] = j;
+            c_q[pos] = qj;
+            nc++;
+            R -= qj;
+        }
+        for (uint32_t f = 0; taken < k && R > 0 && f < (1u << 24); f++) {
+            rng(g->seed, S_FALLBACK, rep, ep, unit, f, r);
+            uint64_t y = hi_mul64(join64(r[0], r[1]), R);
+            int64_t lo = 0, hi = n - 1;
+            while (lo < hi) {
+                int64_t mid = lo + (hi - lo) / 2;
+                uint64_t cm = 0;
+                for (int c = 0; c < nc && c_id[c] <= mid; c++) cm += c_q[c];
+                if (cdf[mid] - cm > y)
+                    hi = mid;
+                else
+                    lo = mid + 1;
+            }
+            int32_t j = (int32_t)lo;
+            events++;
+            int glob = unif_d(r[2], r[3]) <= g->p_global;
+            if (!glob) {
+                tests++;
+                if (!in_ball(g, Z, nz, j)) continue;
+            }
+            uint64_t qj = cdf[j] - (j > 0 ? cdf[j - 1] : 0);
+            int pos = nc;
+            while (pos > 0 && c_id[pos - 1] > j) {
+                c_id[pos] = c_id[pos - 1];
+                c_q[pos] = c_q[pos - 1];
+                pos--;
+            }
+            c_id[pos] = j;
+            c_q[pos] = qj;
+            nc++;
+            R -= qj;
+            out_arr[taken++] = j;
+        }
+    }
+    cnt[1] += tests;
+    cnt[2] += events;
+    memcpy(out_sorted, out_arr, sizeof(int32_t) * (size_t)taken);
+    qsort(out_sorted, (size_t)taken, sizeof(int32_t), cmp_i32);
+    return taken;
+}
+
 static void compute_weights(og_graph* g, int64_t* npos_out) {
     int64_t n = g->n;
     free(g->w);
@@ -624,20 +795,30 @@ int og_pa_epoch(og_graph* g, int threads) {
     int32_t* rows = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta * 256);
     int32_t* arr = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta * 256);
     int32_t* kk = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta);
-    int64_t rows_exp = 0, elems = 0;
+    int64_t rows_exp = 0, elems = 0, draws = 0;
     if (threads > 0) omp_set_num_threads(threads);
-#pragma omp parallel reduction(+ : rows_exp, elems)
+#pragma omp parallel reduction(+ : rows_exp, elems, draws)
     {
         keyvec kv = {0, 0, 0};
+        int32_t* zbuf = NULL;
+        int64_t zcap = 0;
 #pragma omp for schedule(dynamic, 16)
         for (int64_t a = 0; a < delta; a++) {
-            int64_t cnt[2] = {0, 0};
-            kk[a] = sample_agent(g, a, g->w, g->cdf, g->shift, npos, rows + a * 256, arr + a * 256,
-                                 cnt, &kv);
+            int64_t cnt[3] = {0, 0, 0};
+            if (g->sampler == 0) {
+                kk[a] = sample_agent_thin(g, a, g->cdf, npos, rows + a * 256, arr + a * 256, cnt,
+                                          &zbuf, &zcap);
+            } else {
+                kk[a] = sample_agent(g, a, g->w, g->cdf, g->shift, npos, rows + a * 256,
+                                     arr + a * 256, cnt, &kv);
+                cnt[2] = kk[a];
+            }
             rows_exp += cnt[0];
             elems += cnt[1];
+            draws += cnt[2];
         }
         free(kv.v);
+        free(zbuf);
     }
     int64_t* row_off = (int64_t*)malloc(sizeof(int64_t) * (size_t)(delta + 1));
     row_off[0] = 0;
@@ -657,7 +838,7 @@ int og_pa_epoch(og_graph* g, int threads) {
     g->stats[0] = n;
     g->stats[1] = rows_exp;
     g->stats[2] = elems;
-    g->stats[3] = e_new;
+    g->stats[3] = draws;
     g->stats[4] = e_new;
     g->epoch++;
     free(rows);

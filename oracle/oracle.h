@@ -35,6 +35,8 @@ int og_set_params(og_graph* g, double alpha, double tau, double gamma, double be
                   double mean_out_degree, double growth_rate, int64_t fixed_new_nodes,
                   int32_t num_anchors);
 void og_set_epoch(og_graph* g, int64_t epoch);
+/* 0: thinning sampler (default), 1: full 2-hop neighbourhood enumeration */
+void og_set_sampler(og_graph* g, int sampler);
 int64_t og_epoch(const og_graph* g);
 
 /* one step; threads <= 0 uses every OpenMP thread.  Returns 0 on success. */

@@ -26,6 +26,7 @@ LIB_PATH = _PKG / "_lib" / "libparagraph_gb300.so"
 
 PG_OK, PG_ERR_CUDA, PG_ERR_CAPACITY, PG_ERR_ARG, PG_ERR_TIMEOUT, PG_ERR_IO, PG_ERR_STATE = range(7)
 PG_WEIGHTS_BASELINE, PG_WEIGHTS_REFCOMPAT = 0, 1
+PG_SAMPLER_THINNING, PG_SAMPLER_ENUMERATE = 0, 1
 MAX_OUT_DEGREE = 256
 
 # Every entry point the header declares; tests check the library exports each of them.
@@ -48,7 +49,8 @@ class PGError(RuntimeError):
 
 class _Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("num_replicas", C.c_int32), ("seed", C.c_uint64),
-                ("weight_model", C.c_int32), ("record_trace", C.c_int32)]
+                ("weight_model", C.c_int32), ("record_trace", C.c_int32), ("sampler", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class _Params(C.Structure):
@@ -192,10 +194,11 @@ class GrowthEngine:
     """One device context holding R replicas (R == 1: the drop-in growth step)."""
 
     def __init__(self, seed: int = 42, replicas: int = 1, device: int = 0,
-                 record_trace: bool = False, weight_model: int = PG_WEIGHTS_BASELINE):
+                 record_trace: bool = False, weight_model: int = PG_WEIGHTS_BASELINE,
+                 sampler: int = PG_SAMPLER_THINNING):
         self._lib = load_library()
         self._ctx = C.c_void_p()
-        cfg = _Config(device, replicas, seed, weight_model, 1 if record_trace else 0)
+        cfg = _Config(device, replicas, seed, weight_model, 1 if record_trace else 0, sampler, 0)
         st = self._lib.pg_create(C.byref(self._ctx), C.byref(cfg))
         if st != PG_OK:
             msg = self._lib.pg_last_error(self._ctx).decode() if self._ctx else "pg_create failed"

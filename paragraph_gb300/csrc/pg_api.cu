@@ -63,7 +63,9 @@ struct pg_ctx {
     // device buffers
     DBuf<Replica> rep;
     DBuf<EpochState> st;
-    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, e_dst, e_rank, arrivals;
+    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, e_dst, e_rank, arrivals, hlist;
+    DBuf<int8_t> hslot;
+    DBuf<uint64_t> hmask;
     DBuf<float> fit, w;
     DBuf<uint64_t> cdf, tilesum, tileoff, tables;
     DBuf<int64_t> fwd_off, bwd_off[2], len_tmp, sort_small, sort_large, sort_large_off, eoff,
@@ -174,6 +176,10 @@ Arena make_arena(pg_ctx* c) {
     A.edge_cap = c->edge_cap;
     A.seed = c->cfg.seed;
     A.record_trace = c->cfg.record_trace;
+    A.hslot = c->hslot.p;
+    A.hmask = c->hmask.p;
+    A.hlist = c->hlist.p;
+    A.sampler = c->cfg.sampler;
     return A;
 }
 
@@ -195,12 +201,14 @@ Replica to_device_rep(const HostRep& h) {
     r.growth_rate = h.prm.growth_rate;
     r.fixed_new = h.prm.fixed_new_nodes;
     r.anchors = h.prm.num_anchors;
+    r.p_global = 1.0 / h.prm.beta;
+    r.heavy_thr = 0x7fffffff;
     return r;
 }
 
 pg_status check_params(pg_ctx* c, const pg_pa_params& p) {
     if (!(p.tau > 0.0)) return fail(c, PG_ERR_ARG, "tau must be > 0");
-    if (!(p.beta >= 1.0)) return fail(c, PG_ERR_ARG, "beta must be >= 1");
+    if (!(p.beta >= 1.0) || p.beta > 1000.0) return fail(c, PG_ERR_ARG, "beta must be in [1, 1000]");
     if (!(p.mean_out_degree >= 0.0) || p.mean_out_degree > 200.0)
         return fail(c, PG_ERR_ARG, "mean_out_degree must be in [0, 200]");
     if (p.num_anchors < 1 || p.num_anchors > PG_MAX_ANCHORS)
@@ -326,6 +334,10 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->bwd_col[0], M));
     PG_CUDA(c, dalloc(c->bwd_col[1], M));
     PG_CUDA(c, dalloc(c->tables, (int64_t)R * kTableEntries));
+    PG_CUDA(c, dalloc(c->hslot, S));
+    PG_CUDA(c, dalloc(c->hmask, S));
+    PG_CUDA(c, dalloc(c->hlist, (int64_t)R * kHeavyMax));
+    PG_CUDA(c, cudaMemsetAsync(c->hslot.p, 0xFF, (size_t)S, c->stream));
     PG_CUDA(c, cudaMemsetAsync(c->inc.p, 0, sizeof(int32_t) * (size_t)S, c->stream));
     PG_CUDA(c, cudaMemsetAsync(c->w.p, 0, sizeof(float) * (size_t)S, c->stream));
     c->parity = 0;
@@ -449,6 +461,11 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
     PG_STAGE("epoch begin");
     launch_weights(A, s);
     PG_STAGE("weights");
+    if (c->cfg.sampler == PG_SAMPLER_THINNING) {
+        launch_hubs(A, c->num_sms, s);
+        PG_STAGE("hub index");
+        c->launches += kHubKernels;
+    }
     if (events) cudaEventRecord(ev[1], s);
     launch_agent_setup(A, agents, s);
     PG_STAGE("agent setup");
@@ -636,6 +653,9 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->tilesum);
     dfree(c->tileoff);
     dfree(c->tables);
+    dfree(c->hlist);
+    dfree(c->hslot);
+    dfree(c->hmask);
     dfree(c->rep);
     dfree(c->ckpt.rep);
     dfree(c->st);
@@ -745,6 +765,7 @@ pg_status pg_set_params(pg_ctx* c, int32_t replica, const pg_pa_params* p) {
     dr.gamma = fresh.gamma;
     dr.tau = fresh.tau;
     dr.beta_m1 = fresh.beta_m1;
+    dr.p_global = fresh.p_global;
     dr.growth_rate = fresh.growth_rate;
     dr.fixed_new = fresh.fixed_new;
     dr.anchors = fresh.anchors;

@@ -77,6 +77,7 @@ enum Stream : uint32_t {
     kStreamEr = 6,
     kStreamSameYear = 7,
     kStreamUniformFill = 8,
+    kStreamFallback = 9,
 };
 
 // Counter layout: (i, unit, epoch, stream << 24 | aux); key = (seed lo, seed hi).

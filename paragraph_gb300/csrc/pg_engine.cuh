@@ -24,6 +24,16 @@ constexpr int kAgentWarps = 4;       // warps per CTA in the agent kernel
 constexpr int kErChunk = 65536;      // ids per ER Philox stream
 constexpr int kSortSmall = 32;       // appended segments up to this length sort in one warp
 constexpr int kBitmapWords = 40960;  // 160 KiB of shared bitmap in the large-segment sort
+#define PG_MAX_ANCHORS_DEV 4
+constexpr int kZCap = 1024;          // 1-hop frontier entries kept in shared memory per warp
+constexpr int kHeavyMax = 64;        // hubs per replica with a bit in the per-node hub mask
+constexpr int kHeavyMinLog = 10;     // only nodes with degree >= 2^10 can be hubs
+constexpr int kHeavyBins = 24;       // log2-degree histogram bins 10..33
+
+enum Sampler : int32_t {
+    kSamplerThinning = 0,   // Poisson thinning against ball membership (default)
+    kSamplerEnumerate = 1,  // stream the whole 2-hop ball and key every element
+};
 
 // Device error word bits.
 enum : uint32_t {
@@ -50,10 +60,14 @@ struct Replica {
     // parameters
     float alpha, gamma, tau, pad0;
     double beta_m1;
+    double p_global;  // 1 / beta: probability that a thinning event is a global (always kept) one
     double growth_rate;
     int64_t fixed_new;
     int32_t anchors;
-    int32_t pad1;
+    // hub index of the epoch: nodes with degree >= heavy_thr get one of <= 64 mask bits
+    int32_t heavy_thr;
+    int32_t heavy_count;
+    int32_t heavy_hist[kHeavyBins];
 };
 
 // Per-epoch device scalars; reset by the epoch-begin kernel.
@@ -119,10 +133,14 @@ struct Arena {
     int64_t* sort_small;       // [slots] packed (slot << 8 | len)
     int64_t* sort_large;       // [slots] slot
     int64_t* sort_large_off;   // [slots] scratch offset
+    int8_t* hslot;             // [slots] hub bit of the node or -1
+    uint64_t* hmask;           // [slots] bit b set when hub b is adjacent to the node
+    int32_t* hlist;            // [R][kHeavyMax] hub node ids
     EpochState* st;
     int64_t agent_cap, edge_cap;
     uint64_t seed;
     int32_t record_trace;
+    int32_t sampler;
 };
 
 // ---------------------------------------------------------------- warp helpers
@@ -185,9 +203,12 @@ __device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64
 // Kernels one PA epoch enqueues: epoch begin (1), weights + CDF (4), agent setup + offset scan +
 // check (5), agent kernels (2), backward append incl. epoch end (8).
 constexpr int kPaEpochKernels = 20;
+// Extra kernels of the thinning sampler's hub index: histogram, pick, collect, mask.
+constexpr int kHubKernels = 4;
 void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s);
 void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cudaStream_t s);
 void launch_weights(const Arena& A, cudaStream_t s);
+void launch_hubs(const Arena& A, int num_sms, cudaStream_t s);
 void launch_tile_scan(const Arena& A, int mode, cudaStream_t s);
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s);
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);

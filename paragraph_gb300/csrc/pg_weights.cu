@@ -54,6 +54,8 @@ __global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, in
             rp.wmax_bits = 0;
             rp.npos = 0;
             rp.wq_total = 0;
+            for (int b = 0; b < kHeavyBins; ++b) rp.heavy_hist[b] = 0;
+            rp.heavy_count = 0;
         }
         int64_t tot;
         const int64_t ex = block_excl_scan<int64_t>(d, sw, &tot);
@@ -198,6 +200,102 @@ __global__ void __launch_bounds__(kTileThreads) k_cdf_add(Arena A) {
     b.y += off;
     p[0] = a;
     p[1] = b;
+}
+
+// ---------------------------------------------------------------- hub index
+// Ball membership of a high-degree node j needs adj(j) intersected with the agent's 1-hop
+// frontier, which is expensive when j has millions of neighbours.  Each epoch, up to 64 nodes of
+// largest degree per replica become hubs; hmask[v] has bit b set when hub b is adjacent to v, so an
+// agent ORs hmask over its frontier once and answers "hub b in my ball?" with one bit test.  Which
+// nodes are hubs only changes speed, never a result.
+__device__ __forceinline__ int64_t degree_of(const Arena& A, const Replica& rp, int64_t v) {
+    const int64_t* fo = A.fwd_off + rp.obase;
+    const int64_t* bo = A.bwd_off_cur + rp.obase;
+    return (fo[v + 1] - fo[v]) + (bo[v + 1] - bo[v]);
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_hub_hist(Arena A) {
+    if (A.st->error) return;
+    const int t = blockIdx.x;
+    const int r = A.tile_rep[t];
+    Replica& rp = A.rep[r];
+    const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
+    if (v0 >= rp.n) return;
+#pragma unroll
+    for (int i = 0; i < kTile / kTileThreads; ++i) {
+        const int64_t v = v0 + threadIdx.x + i * kTileThreads;
+        if (v >= rp.n) continue;
+        const int64_t slot = rp.nbase + v;
+        A.hslot[slot] = -1;
+        A.hmask[slot] = 0;
+        const int64_t d = degree_of(A, rp, v);
+        if (d >= (1 << kHeavyMinLog)) {
+            int b = 63 - __clzll((unsigned long long)d) - kHeavyMinLog;
+            if (b >= kHeavyBins) b = kHeavyBins - 1;
+            atomicAdd(&rp.heavy_hist[b], 1);
+        }
+    }
+}
+
+__global__ void k_hub_pick(Arena A) {
+    if (A.st->error) return;
+    for (int r = threadIdx.x; r < A.R; r += blockDim.x) {
+        Replica& rp = A.rep[r];
+        int thr = 0x7fffffff, cum = 0;
+        for (int b = kHeavyBins - 1; b >= 0; --b) {
+            cum += rp.heavy_hist[b];
+            if (cum > kHeavyMax) break;
+            if (rp.heavy_hist[b]) thr = 1 << (b + kHeavyMinLog);
+        }
+        rp.heavy_thr = thr;
+        rp.heavy_count = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_hub_collect(Arena A) {
+    if (A.st->error) return;
+    const int t = blockIdx.x;
+    const int r = A.tile_rep[t];
+    Replica& rp = A.rep[r];
+    const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
+    if (v0 >= rp.n) return;
+    const int64_t thr = rp.heavy_thr;
+#pragma unroll
+    for (int i = 0; i < kTile / kTileThreads; ++i) {
+        const int64_t v = v0 + threadIdx.x + i * kTileThreads;
+        if (v >= rp.n) continue;
+        if (degree_of(A, rp, v) >= thr) {
+            const int b = atomicAdd(&rp.heavy_count, 1);
+            if (b < kHeavyMax) {
+                A.hslot[rp.nbase + v] = (int8_t)b;
+                A.hlist[(int64_t)r * kHeavyMax + b] = (int32_t)v;
+            }
+        }
+    }
+}
+
+// One CTA per (replica, hub bit): mark every neighbour of the hub.
+__global__ void __launch_bounds__(256) k_hub_mask(Arena A) {
+    if (A.st->error) return;
+    const int r = blockIdx.x / kHeavyMax, b = blockIdx.x % kHeavyMax;
+    const Replica& rp = A.rep[r];
+    if (b >= rp.heavy_count || b >= kHeavyMax) return;
+    const int64_t h = A.hlist[(int64_t)r * kHeavyMax + b];
+    const unsigned long long bit = 1ull << b;
+    for (int dir = 0; dir < 2; ++dir) {
+        const int64_t* off = (dir ? A.bwd_off_cur : A.fwd_off) + rp.obase;
+        const int32_t* col = (dir ? A.bwd_col_cur : A.fwd_col) + rp.ebase;
+        for (int64_t p = off[h] + threadIdx.x; p < off[h + 1]; p += blockDim.x)
+            atomicOr((unsigned long long*)&A.hmask[rp.nbase + col[p]], bit);
+    }
+}
+
+void launch_hubs(const Arena& A, int num_sms, cudaStream_t s) {
+    (void)num_sms;
+    k_hub_hist<<<A.ntiles, kTileThreads, 0, s>>>(A);
+    k_hub_pick<<<1, 256, 0, s>>>(A);
+    k_hub_collect<<<A.ntiles, kTileThreads, 0, s>>>(A);
+    k_hub_mask<<<(unsigned)A.R * kHeavyMax, 256, 0, s>>>(A);
 }
 
 void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s) {

@@ -103,6 +103,6 @@ def test_create_rejects_bad_config_without_gpu_calls(built):
     import ctypes as C
 
     ctx = C.c_void_p()
-    cfg = pg._Config(0, 0, 1, 0, 0)  # zero replicas
+    cfg = pg._Config(0, 0, 1, 0, 0, 0, 0)  # zero replicas
     assert lib.pg_create(C.byref(ctx), C.byref(cfg)) == pg.PG_ERR_ARG
     assert lib.pg_status_string(pg.PG_ERR_CAPACITY) == b"capacity exceeded"

@@ -8,16 +8,19 @@ import numpy as np
 import pytest
 
 import oracle as O
-from paragraph_gb300 import GrowthEngine, PAParams, ReplicaInput
+from paragraph_gb300 import (PG_SAMPLER_ENUMERATE, PG_SAMPLER_THINNING, GrowthEngine,
+                             PAParams, ReplicaInput)
 from paragraph_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
+SAMPLERS = [PG_SAMPLER_THINNING, PG_SAMPLER_ENUMERATE]
 
 
-def _oracle_for(g, params: PAParams, seed: int, replica: int = 0):
+def _oracle_for(g, params: PAParams, seed: int, replica: int = 0, sampler: int = 0):
     og = O.OracleGraph(seed, replica)
     og.load(g.pub, g.fitness, g.src, g.dst)
     og.set_params(**params.__dict__)
+    og.set_sampler(sampler)
     return og
 
 
@@ -39,15 +42,17 @@ def _compare_state(eng: GrowthEngine, og: O.OracleGraph, replica: int = 0):
     np.testing.assert_array_equal(fg.view(np.uint32), fo.view(np.uint32))
 
 
+@pytest.mark.parametrize("sampler", SAMPLERS)
 @pytest.mark.parametrize("n0,delta,lam,beta", [(300, 40, 4.0, 4.0), (2000, 500, 15.0, 4.0),
-                                               (2000, 500, 15.0, 1.0), (64, 64, 30.0, 8.0)])
-def test_pa_small_bit_exact(gpu, n0, delta, lam, beta):
+                                               (2000, 500, 15.0, 1.0), (64, 64, 30.0, 8.0),
+                                               (12, 30, 60.0, 8.0)])
+def test_pa_small_bit_exact(gpu, sampler, n0, delta, lam, beta):
     g = W.plain_pa_seed(n0, 10, seed=7)
     prm = PAParams(alpha=1.0, tau=5.0, gamma=1.0, beta=beta, mean_out_degree=lam,
                    growth_rate=0.0, fixed_new_nodes=delta, num_anchors=3)
-    with GrowthEngine(seed=1234, record_trace=True) as eng:
+    with GrowthEngine(seed=1234, record_trace=True, sampler=sampler) as eng:
         eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=3)
-        og = _oracle_for(g, prm, 1234)
+        og = _oracle_for(g, prm, 1234, sampler=sampler)
         for _ in range(3):
             nn, ne = eng.grow_epoch()
             og.pa_epoch()
@@ -60,13 +65,14 @@ def test_pa_small_bit_exact(gpu, n0, delta, lam, beta):
             _compare_state(eng, og)
 
 
-def test_plain_pa_config_bit_exact(gpu):
+@pytest.mark.parametrize("sampler", SAMPLERS)
+def test_plain_pa_config_bit_exact(gpu, sampler):
     """Plain PA growth: 10k seed DAG, 3 epochs x 5,000 agents, Poisson(15), 3 anchors."""
     g = W.plain_pa_seed(10_000, 10, seed=42)
     prm = W.plain_pa_params()
-    with GrowthEngine(seed=42) as eng:
+    with GrowthEngine(seed=42, sampler=sampler) as eng:
         eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=3)
-        og = _oracle_for(g, prm, 42)
+        og = _oracle_for(g, prm, 42, sampler=sampler)
         for _ in range(3):
             eng.grow_epoch()
             og.pa_epoch()
@@ -143,4 +149,4 @@ def test_checkpoint_restore_regrows_identically(gpu):
             np.testing.assert_array_equal(c1, c2)
         st = eng.stats()
         assert st["run_epochs"] == 8 and st["run_new_edges"] == e2
-        assert st["run_kernel_launches"] == 8 * 20
+        assert st["run_kernel_launches"] == 8 * (20 + 4)  # thinning adds the hub index
