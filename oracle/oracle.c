@@ -632,19 +632,20 @@ static int sample_agent_thin(const og_graph* g, int64_t a, const uint64_t* cdf, 
     int32_t anchor[4];
     rng(g->seed, S_ANCHOR, rep, ep, unit, 0, r);
     for (int i = 0; i < g->anchors; i++) anchor[i] = (int32_t)(((uint64_t)r[i] * (uint64_t)n) >> 32);
-    /* Z = sorted unique anchors U their forward and backward rows */
-    int64_t nz = g->anchors;
-    for (int i = 0; i < g->anchors; i++)
+    /* Z = sorted unique anchors U their forward and backward rows (only needed when beta > 1) */
+    const int nanch = g->p_global < 1.0 ? g->anchors : 0;
+    int64_t nz = nanch;
+    for (int i = 0; i < nanch; i++)
         nz += (g->fwd_off[anchor[i] + 1] - g->fwd_off[anchor[i]]) +
               (g->bwd_off[anchor[i] + 1] - g->bwd_off[anchor[i]]);
     cnt[0] += nz;
-    if (nz > *zcap) {
-        *zcap = nz;
-        *zbuf = (int32_t*)realloc(*zbuf, sizeof(int32_t) * (size_t)nz);
+    if (nz + 1 > *zcap) {
+        *zcap = nz + 1;
+        *zbuf = (int32_t*)realloc(*zbuf, sizeof(int32_t) * (size_t)(nz + 1));
     }
     int32_t* Z = *zbuf;
     int64_t w = 0;
-    for (int i = 0; i < g->anchors; i++) {
+    for (int i = 0; i < nanch; i++) {
         Z[w++] = anchor[i];
         for (int64_t p = g->fwd_off[anchor[i]]; p < g->fwd_off[anchor[i] + 1]; p++) Z[w++] = g->fwd_col[p];
         for (int64_t p = g->bwd_off[anchor[i]]; p < g->bwd_off[anchor[i] + 1]; p++) Z[w++] = g->bwd_col[p];
