@@ -674,17 +674,18 @@ static int sample_agent_thin(const og_graph* g, int64_t a, const uint64_t* cdf, 
         int32_t j = (int32_t)lo;
         events++;
         int glob = unif_d(r[2], r[3]) <= g->p_global;
-        if (!glob) {
-            tests++;
-            if (!in_ball(g, Z, nz, j)) continue;
-        }
         int dup = 0;
         for (int q = 0; q < taken; q++)
             if (out_arr[q] == j) {
                 dup = 1;
                 break;
             }
-        if (!dup) out_arr[taken++] = j;
+        if (dup) continue; /* an arrived node gains nothing from another event */
+        if (!glob) {
+            tests++;
+            if (!in_ball(g, Z, nz, j)) continue;
+        }
+        out_arr[taken++] = j;
     }
     if (taken < k) {
         /* exact continuation without replacement over the unchosen nodes */

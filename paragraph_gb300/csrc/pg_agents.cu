@@ -365,330 +365,7 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
     emit_row<KCAP>(A, rp, a, al, n, S.out, S.bi, taken, rows, elems, ng);
 }
 
-// ================================================================ thinning sampler
-// One Poisson event stream over all nodes with rate beta * w_j: an event picks j from the global
-// CDF and is global with probability 1/beta (always accepted) or a boost event (accepted iff j is
-// in the agent's 2-hop ball).  Node j's accepted events then have rate w_j beta^[j in ball], so the
-// first k distinct accepted nodes are the successive-sampling draw with those weights -- the same
-// law as the reference's ES top-k over the neighbourhood plus its random fill, with cost
-// independent of the ball's size.  Events are independent, so the 32 lanes of the warp evaluate 32
-// events at once (CDF search + membership) and the acceptances are then taken in event order.
-// Membership: j in ball <=> j in Z = anchors U adj(anchors) (sorted in shared memory, the 1-hop
-// frontier) or adj(j) meets Z; for hubs, one bit of the OR of the hub masks over Z.
-template <int KCAP>
-struct ThinSmem {
-    int32_t Z[kZCap];
-    int32_t arr[KCAP];
-    int32_t out[KCAP];
-    int32_t c_id[KCAP];
-    uint64_t c_cq[KCAP];
-};
-
-struct Ball {
-    const int64_t* fo;
-    const int32_t* fc;
-    const int64_t* bo;
-    const int32_t* bc;
-    const int8_t* hslot;
-    const int32_t* Z;  // shared memory, sorted unique (valid when small)
-    int nz;
-    bool small;
-    int anchors[PG_MAX_ANCHORS_DEV];
-    int na;
-    unsigned long long hm;
-};
-
-__device__ __forceinline__ bool contains(const int32_t* a, int64_t lo, int64_t hi, int32_t v) {
-    int64_t l = lo, h = hi;
-    while (l < h) {
-        const int64_t mid = (l + h) >> 1;
-        if (a[mid] < v)
-            l = mid + 1;
-        else
-            h = mid;
-    }
-    return l < hi && a[l] == v;
-}
-
-__device__ __forceinline__ bool adj_has(const Ball& B, int x, int32_t v) {
-    return contains(B.fc, B.fo[x], B.fo[x + 1], v) || contains(B.bc, B.bo[x], B.bo[x + 1], v);
-}
-
-__device__ __forceinline__ bool in_z(const Ball& B, int32_t v) {
-    if (B.small) return contains(B.Z, 0, B.nz, v);
-    for (int i = 0; i < B.na; ++i)
-        if (v == B.anchors[i] || adj_has(B, B.anchors[i], v)) return true;
-    return false;
-}
-
-// Lane-serial membership test of node j in the 2-hop ball.
-__device__ bool in_ball(const Ball& B, int32_t j) {
-    if (in_z(B, j)) return true;
-    const int hs = B.hslot[j];
-    if (hs >= 0) return (B.hm >> hs) & 1ull;
-    const int64_t f0 = B.fo[j], f1 = B.fo[j + 1], b0 = B.bo[j], b1 = B.bo[j + 1];
-    const int64_t deg = (f1 - f0) + (b1 - b0);
-    if (B.small && deg > 16 * (int64_t)B.nz) {
-        // long row against a short frontier: search each frontier node in j's rows
-        for (int q = 0; q < B.nz; ++q) {
-            const int32_t z = B.Z[q];
-            if (contains(B.fc, f0, f1, z) || contains(B.bc, b0, b1, z)) return true;
-        }
-        return false;
-    }
-    for (int64_t p = f0; p < f1; ++p)
-        if (in_z(B, B.fc[p])) return true;
-    for (int64_t p = b0; p < b1; ++p)
-        if (in_z(B, B.bc[p])) return true;
-    return false;
-}
-
-template <int KCAP>
-__device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KCAP>& S) {
-    const int lane = lane_id();
-    const int r = replica_of_agent(A.rep, A.R, a);
-    const Replica& rp = A.rep[r];
-    const int64_t n = rp.n;
-    const int64_t al = a - rp.abase;
-    const uint32_t ep = (uint32_t)A.st->epoch, unit = (uint32_t)al, rep = (uint32_t)r;
-    const uint64_t* cdf = A.cdf + rp.nbase;
-    Ball B;
-    B.fo = A.fwd_off + rp.obase;
-    B.fc = A.fwd_col + rp.ebase;
-    B.bo = A.bwd_off_cur + rp.obase;
-    B.bc = A.bwd_col_cur + rp.ebase;
-    B.hslot = A.hslot + rp.nbase;
-    B.Z = S.Z;
-    B.na = rp.anchors;
-    B.hm = 0;
-    B.small = true;
-    B.nz = 0;
-    const bool boost = rp.p_global < 1.0;
-    long long rows = 0;
-
-    // ---------------------------------------------------------------- frontier Z
-    if (boost) {
-        const u32x4 xa = draw(A.seed, kStreamAnchor, rep, ep, unit, 0);
-#pragma unroll
-        for (int i = 0; i < PG_MAX_ANCHORS_DEV; ++i) B.anchors[i] = (int)bounded32(xa.x[i], (uint32_t)n);
-        int64_t total = B.na;
-        for (int i = 0; i < B.na; ++i) {
-            const int x = B.anchors[i];
-            total += (B.fo[x + 1] - B.fo[x]) + (B.bo[x + 1] - B.bo[x]);
-        }
-        rows = total;
-        B.small = total <= kZCap;
-        if (B.small) {
-            int w = 0;
-            for (int i = 0; i < B.na; ++i) {
-                const int x = B.anchors[i];
-                if (lane == 0) S.Z[w] = x;
-                ++w;
-                const int64_t lf = B.fo[x + 1] - B.fo[x], lb = B.bo[x + 1] - B.bo[x];
-                for (int64_t q = lane; q < lf; q += 32) S.Z[w + q] = B.fc[B.fo[x] + q];
-                w += (int)lf;
-                for (int64_t q = lane; q < lb; q += 32) S.Z[w + q] = B.bc[B.bo[x] + q];
-                w += (int)lb;
-            }
-            int P = 1;
-            while (P < w) P <<= 1;
-            for (int q = w + lane; q < P; q += 32) S.Z[q] = 0x7fffffff;
-            __syncwarp();
-            for (int kk = 2; kk <= P; kk <<= 1) {
-                for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-                    for (int q = lane; q < P; q += 32) {
-                        const int qx = q ^ jj;
-                        if (qx > q) {
-                            const int va = S.Z[q], vb = S.Z[qx];
-                            if ((va > vb) == ((q & kk) == 0)) {
-                                S.Z[q] = vb;
-                                S.Z[qx] = va;
-                            }
-                        }
-                    }
-                    __syncwarp();
-                }
-            }
-            // in-place unique, chunk by chunk; the predecessor of a chunk's first element is carried
-            // in a register because the previous chunk's writes may have overwritten it
-            int nz = 0, carry = -1;
-            for (int base = 0; base < w; base += 32) {
-                const int q = base + lane;
-                const int v = q < w ? S.Z[q] : 0x7fffffff;
-                int pv = __shfl_up_sync(kFull, v, 1);
-                if (lane == 0) pv = carry;
-                carry = __shfl_sync(kFull, v, 31);
-                const bool keep = q < w && (q == 0 || pv != v);
-                const unsigned m = __ballot_sync(kFull, keep);
-                __syncwarp();
-                if (keep) S.Z[nz + __popc(m & ((1u << lane) - 1))] = v;
-                nz += __popc(m);
-                __syncwarp();
-            }
-            B.nz = nz;
-            unsigned long long hm = 0;
-            for (int q = lane; q < nz; q += 32) hm |= A.hmask[rp.nbase + S.Z[q]];
-            B.hm = hm;
-        } else {
-            B.nz = 0;
-            unsigned long long hm = 0;
-            for (int i = 0; i < B.na; ++i) {
-                const int x = B.anchors[i];
-                if (lane == 0) hm |= A.hmask[rp.nbase + x];
-                for (int64_t p = B.fo[x] + lane; p < B.fo[x + 1]; p += 32) hm |= A.hmask[rp.nbase + B.fc[p]];
-                for (int64_t p = B.bo[x] + lane; p < B.bo[x + 1]; p += 32) hm |= A.hmask[rp.nbase + B.bc[p]];
-            }
-            B.hm = hm;
-        }
-        // OR over lanes
-        unsigned lo = (unsigned)B.hm, hi = (unsigned)(B.hm >> 32);
-        lo = __reduce_or_sync(kFull, lo);
-        hi = __reduce_or_sync(kFull, hi);
-        B.hm = ((unsigned long long)hi << 32) | lo;
-    }
-
-    // ---------------------------------------------------------------- events
-    const uint64_t Wq = rp.wq_total;
-    const double pg = rp.p_global;
-    int nch = 0;
-    long long events = 0, tests = 0;
-    const int maxev = 64 * k + 256;
-    for (int i0 = 0; i0 < maxev && nch < k; i0 += 32) {
-        const u32x4 x = draw(A.seed, kStreamGlobal, rep, ep, unit, (uint32_t)(i0 + lane));
-        const uint64_t y = mulhi64(u64of(x.x[0], x.x[1]), Wq);
-        int64_t lo = 0, hi = n - 1;
-        while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if (cdf[mid] > y)
-                hi = mid;
-            else
-                lo = mid + 1;
-        }
-        const int j = (int)lo;
-        const bool glob = u01d(x.x[2], x.x[3]) <= pg;
-        const bool acc = glob || in_ball(B, j);
-        for (int l = 0; l < 32 && nch < k; ++l) {
-            const int jl = __shfl_sync(kFull, j, l);
-            const bool al_ = __shfl_sync(kFull, acc, l);
-            const bool gl = __shfl_sync(kFull, glob, l);
-            ++events;
-            if (!gl) ++tests;
-            if (!al_) continue;
-            bool dup = false;
-            for (int q = lane; q < nch; q += 32) dup |= (S.arr[q] == jl);
-            if (__any_sync(kFull, dup)) continue;
-            if (lane == 0) S.arr[nch] = jl;
-            __syncwarp();
-            ++nch;
-        }
-    }
-    if (nch < k) {
-        // exact continuation without replacement (memoryless): CDF minus the chosen weight
-        int nc = 0;
-        uint64_t R = Wq;
-        if (lane == 0) {
-            for (int q = 0; q < nch; ++q) {
-                const int j = S.arr[q];
-                const uint64_t qj = cdf[j] - (j > 0 ? cdf[j - 1] : 0);
-                int pos = nc;
-                while (pos > 0 && S.c_id[pos - 1] > j) {
-                    S.c_id[pos] = S.c_id[pos - 1];
-                    S.c_cq[pos] = S.c_cq[pos - 1];
-                    --pos;
-                }
-                S.c_id[pos] = j;
-                S.c_cq[pos] = qj;  // individual weights for now
-                ++nc;
-                R -= qj;
-            }
-            uint64_t acc = 0;
-            for (int q = 0; q < nc; ++q) {
-                acc += S.c_cq[q];
-                S.c_cq[q] = acc;  // cumulative
-            }
-        }
-        __syncwarp();
-        nc = nch;
-        R = __shfl_sync(kFull, R, 0);
-        for (uint32_t f = 0; nch < k && R > 0 && f < (1u << 24); ++f) {
-            const u32x4 x = draw(A.seed, kStreamFallback, rep, ep, unit, f);
-            const uint64_t y = mulhi64(u64of(x.x[0], x.x[1]), R);
-            int64_t lo = 0, hi = n;
-            while (true) {
-                const int64_t span = hi - lo;
-                const int64_t step = span > 32 ? (span + 31) / 32 : 1;
-                int64_t p = lo + (int64_t)(lane + 1) * step - 1;
-                if (p > hi - 1) p = hi - 1;
-                int cl = 0, ch = nc;
-                while (cl < ch) {
-                    const int mid = (cl + ch) >> 1;
-                    if (S.c_id[mid] <= p)
-                        cl = mid + 1;
-                    else
-                        ch = mid;
-                }
-                const uint64_t cp = cl ? S.c_cq[cl - 1] : 0;
-                const unsigned m = __ballot_sync(kFull, (cdf[p] - cp) > y);
-                if (m == 0) {
-                    if (lane == 0) atomicOr(&A.st->error, kErrArg);
-                    lo = 0;
-                    break;
-                }
-                const int L = __ffs(m) - 1;
-                const int64_t pL = __shfl_sync(kFull, p, L);
-                const int64_t pL1 = __shfl_sync(kFull, p, L > 0 ? L - 1 : 0);
-                if (span <= 32) {
-                    lo = pL;
-                    break;
-                }
-                hi = pL + 1;
-                lo = L > 0 ? pL1 + 1 : lo;
-            }
-            const int j = (int)lo;
-            const bool glob = u01d(x.x[2], x.x[3]) <= pg;
-            ++events;
-            bool accept = glob;
-            if (!glob) {
-                ++tests;
-                int mem = 0;
-                if (lane == 0) mem = in_ball(B, j) ? 1 : 0;
-                accept = __shfl_sync(kFull, mem, 0) != 0;
-            }
-            if (!accept) continue;
-            const uint64_t qj = cdf[j] - (j > 0 ? cdf[j - 1] : 0);
-            int below = 0;
-            for (int q = lane; q < nc; q += 32) below += S.c_id[q] < j ? 1 : 0;
-            const int pos = __reduce_add_sync(kFull, below);
-            for (int top = nc; top > pos; top -= 32) {
-                const int q = top - 1 - lane;
-                const bool act = q >= pos;
-                int tid = 0;
-                uint64_t tq = 0;
-                if (act) {
-                    tid = S.c_id[q];
-                    tq = S.c_cq[q];
-                }
-                __syncwarp();
-                if (act) {
-                    S.c_id[q + 1] = tid;
-                    S.c_cq[q + 1] = tq + qj;
-                }
-                __syncwarp();
-            }
-            if (lane == 0) {
-                S.c_id[pos] = j;
-                S.c_cq[pos] = (pos > 0 ? S.c_cq[pos - 1] : 0) + qj;
-                S.arr[nch] = j;
-            }
-            __syncwarp();
-            ++nc;
-            ++nch;
-            R -= qj;
-        }
-    }
-    if (nch != k && lane == 0) atomicOr(&A.st->error, kErrArg);
-    emit_row<KCAP>(A, rp, a, al, n, S.arr, S.out, nch, rows, tests, events);
-}
+#include "pg_thin.cuh"
 
 // ---------------------------------------------------------------- setup: out-degree + new nodes
 __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
@@ -733,7 +410,10 @@ __global__ void k_edges_check(Arena A, int64_t agents) {
 
 template <int KCAP, bool BIG, bool THIN>
 __global__ void __launch_bounds__(kAgentWarps * 32) k_agents(Arena A, int64_t agents) {
-    using Smem = typename std::conditional<THIN, ThinSmem<KCAP>, AgentSmem<KCAP>>::type;
+    // frontier capacity: 2048 entries for the common small-k kernel, 1024 for the k <= 256 one so
+    // that four warps stay within 48 KiB of static shared memory
+    constexpr int ZCAP = KCAP <= kKSmall ? 2 * kZCap : kZCap;
+    using Smem = typename std::conditional<THIN, ThinSmem<KCAP, ZCAP>, AgentSmem<KCAP>>::type;
     __shared__ Smem smem[kAgentWarps];
     if (A.st->error) return;
     Smem& S = smem[threadIdx.x >> 5];
@@ -749,7 +429,7 @@ __global__ void __launch_bounds__(kAgentWarps * 32) k_agents(Arena A, int64_t ag
         const int k = A.kk[a];
         if (!BIG && k > KCAP) continue;
         if constexpr (THIN)
-            process_agent_thin<KCAP>(A, a, k, S);
+            process_agent_thin<KCAP, ZCAP>(A, a, k, S);
         else
             process_agent<KCAP>(A, a, k, S);
     }

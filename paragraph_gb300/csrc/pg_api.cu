@@ -64,7 +64,8 @@ struct pg_ctx {
     DBuf<Replica> rep;
     DBuf<EpochState> st;
     DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, e_dst, e_rank, arrivals, hlist;
-    DBuf<int8_t> hslot;
+    DBuf<int16_t> hslot;
+    DBuf<uint64_t> hub2;
     DBuf<uint64_t> hmask;
     DBuf<float> fit, w;
     DBuf<uint64_t> cdf, tilesum, tileoff, tables;
@@ -178,6 +179,7 @@ Arena make_arena(pg_ctx* c) {
     A.record_trace = c->cfg.record_trace;
     A.hslot = c->hslot.p;
     A.hmask = c->hmask.p;
+    A.hub2 = c->hub2.p;
     A.hlist = c->hlist.p;
     A.sampler = c->cfg.sampler;
     return A;
@@ -335,9 +337,10 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->bwd_col[1], M));
     PG_CUDA(c, dalloc(c->tables, (int64_t)R * kTableEntries));
     PG_CUDA(c, dalloc(c->hslot, S));
-    PG_CUDA(c, dalloc(c->hmask, S));
+    PG_CUDA(c, dalloc(c->hmask, S * kMaskWords));
+    PG_CUDA(c, dalloc(c->hub2, (int64_t)R * kHeavyMax * kMaskWords));
     PG_CUDA(c, dalloc(c->hlist, (int64_t)R * kHeavyMax));
-    PG_CUDA(c, cudaMemsetAsync(c->hslot.p, 0xFF, (size_t)S, c->stream));
+    PG_CUDA(c, cudaMemsetAsync(c->hslot.p, 0xFF, 2 * (size_t)S, c->stream));
     PG_CUDA(c, cudaMemsetAsync(c->inc.p, 0, sizeof(int32_t) * (size_t)S, c->stream));
     PG_CUDA(c, cudaMemsetAsync(c->w.p, 0, sizeof(float) * (size_t)S, c->stream));
     c->parity = 0;
@@ -656,6 +659,7 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->hlist);
     dfree(c->hslot);
     dfree(c->hmask);
+    dfree(c->hub2);
     dfree(c->rep);
     dfree(c->ckpt.rep);
     dfree(c->st);

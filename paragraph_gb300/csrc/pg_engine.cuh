@@ -26,7 +26,8 @@ constexpr int kSortSmall = 32;       // appended segments up to this length sort
 constexpr int kBitmapWords = 40960;  // 160 KiB of shared bitmap in the large-segment sort
 #define PG_MAX_ANCHORS_DEV 4
 constexpr int kZCap = 1024;          // 1-hop frontier entries kept in shared memory per warp
-constexpr int kHeavyMax = 64;        // hubs per replica with a bit in the per-node hub mask
+constexpr int kHeavyMax = 256;       // hubs per replica with a bit in the per-node hub mask
+constexpr int kMaskWords = kHeavyMax / 64;
 constexpr int kHeavyMinLog = 10;     // only nodes with degree >= 2^10 can be hubs
 constexpr int kHeavyBins = 24;       // log2-degree histogram bins 10..33
 
@@ -64,7 +65,7 @@ struct Replica {
     double growth_rate;
     int64_t fixed_new;
     int32_t anchors;
-    // hub index of the epoch: nodes with degree >= heavy_thr get one of <= 64 mask bits
+    // hub index of the epoch: nodes with degree >= heavy_thr get one of <= kHeavyMax mask bits
     int32_t heavy_thr;
     int32_t heavy_count;
     int32_t heavy_hist[kHeavyBins];
@@ -133,8 +134,9 @@ struct Arena {
     int64_t* sort_small;       // [slots] packed (slot << 8 | len)
     int64_t* sort_large;       // [slots] slot
     int64_t* sort_large_off;   // [slots] scratch offset
-    int8_t* hslot;             // [slots] hub bit of the node or -1
-    uint64_t* hmask;           // [slots] bit b set when hub b is adjacent to the node
+    int16_t* hslot;            // [slots] hub bit of the node or -1
+    uint64_t* hmask;           // [slots][kMaskWords] bit b set when hub b is adjacent to the node
+    uint64_t* hub2;            // [R][kHeavyMax][kMaskWords] hubs sharing a neighbour with hub b
     int32_t* hlist;            // [R][kHeavyMax] hub node ids
     EpochState* st;
     int64_t agent_cap, edge_cap;
@@ -203,8 +205,8 @@ __device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64
 // Kernels one PA epoch enqueues: epoch begin (1), weights + CDF (4), agent setup + offset scan +
 // check (5), agent kernels (2), backward append incl. epoch end (8).
 constexpr int kPaEpochKernels = 20;
-// Extra kernels of the thinning sampler's hub index: histogram, pick, collect, mask.
-constexpr int kHubKernels = 4;
+// Extra kernels of the thinning sampler's hub index: histogram, pick, collect, mask, hub pairs.
+constexpr int kHubKernels = 5;
 void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s);
 void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cudaStream_t s);
 void launch_weights(const Arena& A, cudaStream_t s);

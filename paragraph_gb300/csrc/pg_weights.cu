@@ -227,7 +227,8 @@ __global__ void __launch_bounds__(kTileThreads) k_hub_hist(Arena A) {
         if (v >= rp.n) continue;
         const int64_t slot = rp.nbase + v;
         A.hslot[slot] = -1;
-        A.hmask[slot] = 0;
+#pragma unroll
+        for (int w = 0; w < kMaskWords; ++w) A.hmask[slot * kMaskWords + w] = 0;
         const int64_t d = degree_of(A, rp, v);
         if (d >= (1 << kHeavyMinLog)) {
             int b = 63 - __clzll((unsigned long long)d) - kHeavyMinLog;
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(kTileThreads) k_hub_collect(Arena A) {
         if (degree_of(A, rp, v) >= thr) {
             const int b = atomicAdd(&rp.heavy_count, 1);
             if (b < kHeavyMax) {
-                A.hslot[rp.nbase + v] = (int8_t)b;
+                A.hslot[rp.nbase + v] = (int16_t)b;
                 A.hlist[(int64_t)r * kHeavyMax + b] = (int32_t)v;
             }
         }
@@ -281,13 +282,47 @@ __global__ void __launch_bounds__(256) k_hub_mask(Arena A) {
     const Replica& rp = A.rep[r];
     if (b >= rp.heavy_count || b >= kHeavyMax) return;
     const int64_t h = A.hlist[(int64_t)r * kHeavyMax + b];
-    const unsigned long long bit = 1ull << b;
+    const unsigned long long bit = 1ull << (b & 63);
     for (int dir = 0; dir < 2; ++dir) {
         const int64_t* off = (dir ? A.bwd_off_cur : A.fwd_off) + rp.obase;
         const int32_t* col = (dir ? A.bwd_col_cur : A.fwd_col) + rp.ebase;
         for (int64_t p = off[h] + threadIdx.x; p < off[h + 1]; p += blockDim.x)
-            atomicOr((unsigned long long*)&A.hmask[rp.nbase + col[p]], bit);
+            atomicOr((unsigned long long*)&A.hmask[(rp.nbase + col[p]) * kMaskWords + (b >> 6)], bit);
     }
+}
+
+// One CTA per (replica, hub bit): hub2[b] = OR of hmask over the hub's neighbours, i.e. the hubs
+// that share at least one neighbour with hub b.
+__global__ void __launch_bounds__(256) k_hub_pairs(Arena A) {
+    __shared__ unsigned long long acc[kMaskWords];
+    if (A.st->error) return;
+    const int r = blockIdx.x / kHeavyMax, b = blockIdx.x % kHeavyMax;
+    const Replica& rp = A.rep[r];
+    if (b >= rp.heavy_count || b >= kHeavyMax) return;
+    if (threadIdx.x < kMaskWords) acc[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t h = A.hlist[(int64_t)r * kHeavyMax + b];
+    unsigned long long m[kMaskWords];
+#pragma unroll
+    for (int w = 0; w < kMaskWords; ++w) m[w] = 0;
+    for (int dir = 0; dir < 2; ++dir) {
+        const int64_t* off = (dir ? A.bwd_off_cur : A.fwd_off) + rp.obase;
+        const int32_t* col = (dir ? A.bwd_col_cur : A.fwd_col) + rp.ebase;
+        for (int64_t p = off[h] + threadIdx.x; p < off[h + 1]; p += blockDim.x) {
+            const uint64_t* hm = A.hmask + (rp.nbase + col[p]) * kMaskWords;
+#pragma unroll
+            for (int w = 0; w < kMaskWords; ++w) m[w] |= hm[w];
+        }
+    }
+#pragma unroll
+    for (int w = 0; w < kMaskWords; ++w) {
+        unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)m[w]);
+        unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(m[w] >> 32));
+        if (lane_id() == 0 && (lo | hi)) atomicOr(&acc[w], ((unsigned long long)hi << 32) | lo);
+    }
+    __syncthreads();
+    if (threadIdx.x < kMaskWords)
+        A.hub2[((int64_t)r * kHeavyMax + b) * kMaskWords + threadIdx.x] = acc[threadIdx.x];
 }
 
 void launch_hubs(const Arena& A, int num_sms, cudaStream_t s) {
@@ -296,6 +331,7 @@ void launch_hubs(const Arena& A, int num_sms, cudaStream_t s) {
     k_hub_pick<<<1, 256, 0, s>>>(A);
     k_hub_collect<<<A.ntiles, kTileThreads, 0, s>>>(A);
     k_hub_mask<<<(unsigned)A.R * kHeavyMax, 256, 0, s>>>(A);
+    k_hub_pairs<<<(unsigned)A.R * kHeavyMax, 256, 0, s>>>(A);
 }
 
 void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s) {
