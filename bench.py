@@ -165,13 +165,19 @@ def traffic_per_agent_byte() -> float | None:
 
 
 # ------------------------------------------------------------------ CPU legs (oracle)
-def cpu_sample(g, prm, seed: int, max_epochs: int = 3, budget_s: float = 12.0) -> dict:
-    """Time the OpenMP oracle (all host threads) on the first epochs of the workload."""
+def cpu_sample(g, prm, seed: int, max_epochs: int = 3, budget_s: float = 12.0,
+               sampler: int = 1) -> dict:
+    """Time the OpenMP oracle (all host threads) on the first epochs of the workload.
+
+    sampler 1 (default) is the reference's algorithm -- enumerate each agent's 2-hop neighbourhood
+    and key every candidate (src/abm.cu:461-565,577-682); sampler 0 is this project's thinning
+    sampler run on the CPU."""
     import oracle as O
 
     og = O.OracleGraph(seed, 0)
     og.load(g.pub, g.fitness, g.src, g.dst)
     og.set_params(**prm.__dict__)
+    og.set_sampler(sampler)
     threads = os.cpu_count() or 1
     edges, secs, epochs = 0, 0.0, 0
     while epochs < max_epochs and (epochs == 0 or secs < budget_s):
@@ -182,9 +188,10 @@ def cpu_sample(g, prm, seed: int, max_epochs: int = 3, budget_s: float = 12.0) -
         edges += og.m - m0
         epochs += 1
     og.close()
+    algo = "neighbourhood enumeration (the reference's algorithm)" if sampler else "thinning sampler"
     return {"value": edges / secs, "unit": "citations/s", "cores": threads, "kind": "port",
             "sample": f"first {epochs} epoch(s) of the workload from the seed ({edges} citations, "
-                      f"{secs:.1f} s), CPU oracle with OpenMP"}
+                      f"{secs:.1f} s), CPU oracle with OpenMP, {algo}"}
 
 
 def run_reference(args) -> None:
@@ -195,9 +202,6 @@ def run_reference(args) -> None:
     import oracle as O
 
     g, prm = seed_graph(args.seed)
-    og = O.OracleGraph(args.seed, 0)
-    og.load(g.pub, g.fitness, g.src, g.dst)
-    og.set_params(**prm.__dict__)
     threads = os.cpu_count() or 1
     # each step = epoch 0 of the workload from the seed (a bounded sample; the oracle reloads the
     # seed between steps outside the timed region)
@@ -205,6 +209,7 @@ def run_reference(args) -> None:
         og2 = O.OracleGraph(args.seed, 0)
         og2.load(g.pub, g.fitness, g.src, g.dst)
         og2.set_params(**prm.__dict__)
+        og2.set_sampler(1)  # the reference's algorithm: enumerate the 2-hop neighbourhood
         t0 = time.perf_counter()
         og2.pa_epoch(threads)
         dt = time.perf_counter() - t0
@@ -322,7 +327,8 @@ def run_ours(args) -> None:
         "clocks": clocks.summary(),
     }
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_sample(g, prm, seed)
+        line["cpu_baseline"] = cpu_sample(g, prm, seed, sampler=1)
+        line["cpu_thinning"] = cpu_sample(g, prm, seed, sampler=0, max_epochs=2, budget_s=5.0)
     eng.close()
     print(json.dumps(line), flush=True)
 

@@ -96,48 +96,56 @@ __global__ void __launch_bounds__(kTileThreads) k_bwd_off(Arena A) {
     }
 }
 
-// One warp per 32 consecutive old rows.
-__global__ void __launch_bounds__(256) k_bwd_copy(Arena A, int64_t chunks) {
+// Largest v in [lo, hi] with off[v] <= p (the row holding position p).
+__device__ __forceinline__ int64_t row_of(const int64_t* off, int64_t lo, int64_t hi, int64_t p) {
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= p)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Old backward entries moved to their new positions, in tiles of kCopyTile consecutive positions
+// (not rows), so a hub row with millions of entries is spread over many CTAs.  Reads and writes are
+// coalesced; each position finds its row by a binary search inside the tile's row range.
+__global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
+    __shared__ int64_t s_rows[2];
     if (A.st->error) return;
-    const int lane = lane_id();
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t total = (int64_t)A.st->copy_tiles;
     unsigned long long moved = 0;
-    for (int64_t c = warp; c < chunks; c += nwarps) {
-        const int t = (int)(c / (kTile / 32));
-        const int r = A.tile_rep[t];
-        const Replica& rp = A.rep[r];
-        const int64_t vbase = (int64_t)(t - rp.tbase) * kTile + (c % (kTile / 32)) * 32;
-        if (vbase >= rp.n) continue;
-        const int64_t v = vbase + lane;
+    for (int64_t t = blockIdx.x; t < total; t += gridDim.x) {
+        int lo = 0, hi = A.R - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (A.rep[mid].ctbase <= t)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const Replica& rp = A.rep[lo];
+        const int64_t p0 = (t - rp.ctbase) * kCopyTile;
+        const int64_t p1 = p0 + kCopyTile < rp.m ? p0 + kCopyTile : rp.m;
         const int64_t* oc = A.bwd_off_cur + rp.obase;
         const int64_t* on = A.bwd_off_nxt + rp.obase;
         const int32_t* cc = A.bwd_col_cur + rp.ebase;
         int32_t* cn = A.bwd_col_nxt + rp.ebase;
-        int64_t ob = 0, ol = 0, nb = 0;
-        if (v < rp.n) {
-            ob = oc[v];
-            ol = oc[v + 1] - ob;
-            nb = on[v];
+        if (threadIdx.x == 0) {
+            s_rows[0] = row_of(oc, 0, rp.n - 1, p0);
+            s_rows[1] = row_of(oc, s_rows[0], rp.n - 1, p1 - 1);
+            moved += (unsigned long long)(p1 - p0);
         }
-        const int64_t incl = warp_incl_scan<int64_t>(ol);
-        const int64_t total = __shfl_sync(kFullMask, incl, 31);
-        moved += (unsigned long long)total;
-        for (int64_t pb = 0; pb < total; pb += 32) {
-            const int64_t p = pb + lane;
-            int o = 0;
-#pragma unroll
-            for (int b = 16; b >= 1; b >>= 1) {
-                const int64_t iv = __shfl_sync(kFullMask, incl, o + b - 1);
-                if (iv <= p) o += b;
-            }
-            const int64_t ex_o = __shfl_sync(kFullMask, incl - ol, o);
-            const int64_t ob_o = __shfl_sync(kFullMask, ob, o);
-            const int64_t nb_o = __shfl_sync(kFullMask, nb, o);
-            if (p < total) cn[nb_o + (p - ex_o)] = cc[ob_o + (p - ex_o)];
+        __syncthreads();
+        const int64_t r0 = s_rows[0], r1 = s_rows[1];
+        for (int64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+            const int64_t v = row_of(oc, r0, r1, p);
+            cn[on[v] + (p - oc[v])] = cc[p];
         }
+        __syncthreads();
     }
-    if (lane == 0 && moved) atomicAdd(&A.st->bwd_moved, moved);
+    if (threadIdx.x == 0 && moved) atomicAdd(&A.st->bwd_moved, moved);
 }
 
 // One warp per agent: place its edges at new_off[dst] + old_len(dst) + rank.
@@ -288,10 +296,7 @@ void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t
     k_bwd_len<<<A.ntiles, kTileThreads, 0, s>>>(A);
     launch_tile_scan(A, 1, s);
     k_bwd_off<<<A.ntiles, kTileThreads, 0, s>>>(A);
-    const int64_t chunks = (int64_t)A.ntiles * (kTile / 32);
-    int64_t g = (chunks + 7) / 8;
-    if (g > (int64_t)num_sms * 16) g = (int64_t)num_sms * 16;
-    k_bwd_copy<<<(unsigned)g, 256, 0, s>>>(A, chunks);
+    k_bwd_copy<<<(unsigned)num_sms * 8, 256, 0, s>>>(A);
     int64_t ga = (agents + 7) / 8;
     if (ga > (int64_t)num_sms * 16) ga = (int64_t)num_sms * 16;
     if (ga < 1) ga = 1;

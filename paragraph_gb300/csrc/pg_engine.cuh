@@ -26,6 +26,7 @@ constexpr int kSortSmall = 32;       // appended segments up to this length sort
 constexpr int kBitmapWords = 40960;  // 160 KiB of shared bitmap in the large-segment sort
 #define PG_MAX_ANCHORS_DEV 4
 constexpr int kZCap = 1024;          // 1-hop frontier entries kept in shared memory per warp
+constexpr int kCopyTile = 4096;      // backward entries per copy tile
 constexpr int kHeavyMax = 256;       // hubs per replica with a bit in the per-node hub mask
 constexpr int kMaskWords = kHeavyMax / 64;
 constexpr int kHeavyMinLog = 10;     // only nodes with degree >= 2^10 can be hubs
@@ -69,6 +70,7 @@ struct Replica {
     int32_t heavy_thr;
     int32_t heavy_count;
     int32_t heavy_hist[kHeavyBins];
+    int64_t ctbase;  // first backward-copy tile of the replica this epoch
 };
 
 // Per-epoch device scalars; reset by the epoch-begin kernel.
@@ -90,6 +92,7 @@ struct EpochState {
     unsigned long long draws;
     unsigned long long bwd_moved;
     unsigned long long nodes_weighted;
+    unsigned long long copy_tiles;  // backward-copy tiles of the epoch (all replicas)
     // run totals, accumulated by the epoch-end kernel and cleared by the host at run start
     unsigned long long cum_rows_expanded;
     unsigned long long cum_elems_streamed;

@@ -18,10 +18,11 @@ namespace pg {
 
 __global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, int64_t delta_override) {
     __shared__ int64_t sw[33];
-    __shared__ int64_t carry;
+    __shared__ int64_t carry, ccarry;
     EpochState* st = A.st;
     if (threadIdx.x == 0) {
         carry = 0;
+        ccarry = 0;
         st->epoch = epoch;
         st->edges = 0;
         st->queue_small = 0;
@@ -63,8 +64,16 @@ __global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, in
         __syncthreads();
         if (threadIdx.x == 0) carry += tot;
         __syncthreads();
+        const int64_t ct = r < A.R ? (A.rep[r].m + kCopyTile - 1) / kCopyTile : 0;
+        int64_t ctot;
+        const int64_t cex = block_excl_scan<int64_t>(ct, sw, &ctot);
+        if (r < A.R) A.rep[r].ctbase = ccarry + cex;
+        __syncthreads();
+        if (threadIdx.x == 0) ccarry += ctot;
+        __syncthreads();
     }
     if (threadIdx.x == 0) {
+        st->copy_tiles = (unsigned long long)ccarry;
         st->agents = carry;
         if (carry > A.agent_cap) atomicOr(&st->error, kErrCapacity);
     }
@@ -251,6 +260,9 @@ __global__ void k_hub_pick(Arena A) {
         rp.heavy_thr = thr;
         rp.heavy_count = 0;
     }
+    // hub-pair masks are OR-accumulated by k_hub_pairs
+    const int64_t words = (int64_t)A.R * kHeavyMax * kMaskWords;
+    for (int64_t i = threadIdx.x; i < words; i += blockDim.x) A.hub2[i] = 0;
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_hub_collect(Arena A) {
@@ -275,40 +287,43 @@ __global__ void __launch_bounds__(kTileThreads) k_hub_collect(Arena A) {
     }
 }
 
-// One CTA per (replica, hub bit): mark every neighbour of the hub.
-__global__ void __launch_bounds__(256) k_hub_mask(Arena A) {
+// G CTAs per (replica, hub bit) split the hub's neighbours: mark every neighbour of the hub.
+__global__ void __launch_bounds__(256) k_hub_mask(Arena A, int G) {
     if (A.st->error) return;
-    const int r = blockIdx.x / kHeavyMax, b = blockIdx.x % kHeavyMax;
+    const int item = blockIdx.x / G, g = blockIdx.x % G;
+    const int r = item / kHeavyMax, b = item % kHeavyMax;
     const Replica& rp = A.rep[r];
     if (b >= rp.heavy_count || b >= kHeavyMax) return;
     const int64_t h = A.hlist[(int64_t)r * kHeavyMax + b];
     const unsigned long long bit = 1ull << (b & 63);
+    const int64_t stride = (int64_t)G * blockDim.x;
     for (int dir = 0; dir < 2; ++dir) {
         const int64_t* off = (dir ? A.bwd_off_cur : A.fwd_off) + rp.obase;
         const int32_t* col = (dir ? A.bwd_col_cur : A.fwd_col) + rp.ebase;
-        for (int64_t p = off[h] + threadIdx.x; p < off[h + 1]; p += blockDim.x)
+        for (int64_t p = off[h] + (int64_t)g * blockDim.x + threadIdx.x; p < off[h + 1]; p += stride)
             atomicOr((unsigned long long*)&A.hmask[(rp.nbase + col[p]) * kMaskWords + (b >> 6)], bit);
     }
 }
 
-// One CTA per (replica, hub bit): hub2[b] = OR of hmask over the hub's neighbours, i.e. the hubs
-// that share at least one neighbour with hub b.
-__global__ void __launch_bounds__(256) k_hub_pairs(Arena A) {
+// hub2[b] = OR of hmask over the hub's neighbours: the hubs sharing a neighbour with hub b.
+__global__ void __launch_bounds__(256) k_hub_pairs(Arena A, int G) {
     __shared__ unsigned long long acc[kMaskWords];
     if (A.st->error) return;
-    const int r = blockIdx.x / kHeavyMax, b = blockIdx.x % kHeavyMax;
+    const int item = blockIdx.x / G, g = blockIdx.x % G;
+    const int r = item / kHeavyMax, b = item % kHeavyMax;
     const Replica& rp = A.rep[r];
     if (b >= rp.heavy_count || b >= kHeavyMax) return;
     if (threadIdx.x < kMaskWords) acc[threadIdx.x] = 0;
     __syncthreads();
     const int64_t h = A.hlist[(int64_t)r * kHeavyMax + b];
+    const int64_t stride = (int64_t)G * blockDim.x;
     unsigned long long m[kMaskWords];
 #pragma unroll
     for (int w = 0; w < kMaskWords; ++w) m[w] = 0;
     for (int dir = 0; dir < 2; ++dir) {
         const int64_t* off = (dir ? A.bwd_off_cur : A.fwd_off) + rp.obase;
         const int32_t* col = (dir ? A.bwd_col_cur : A.fwd_col) + rp.ebase;
-        for (int64_t p = off[h] + threadIdx.x; p < off[h + 1]; p += blockDim.x) {
+        for (int64_t p = off[h] + (int64_t)g * blockDim.x + threadIdx.x; p < off[h + 1]; p += stride) {
             const uint64_t* hm = A.hmask + (rp.nbase + col[p]) * kMaskWords;
 #pragma unroll
             for (int w = 0; w < kMaskWords; ++w) m[w] |= hm[w];
@@ -321,17 +336,19 @@ __global__ void __launch_bounds__(256) k_hub_pairs(Arena A) {
         if (lane_id() == 0 && (lo | hi)) atomicOr(&acc[w], ((unsigned long long)hi << 32) | lo);
     }
     __syncthreads();
-    if (threadIdx.x < kMaskWords)
-        A.hub2[((int64_t)r * kHeavyMax + b) * kMaskWords + threadIdx.x] = acc[threadIdx.x];
+    if (threadIdx.x < kMaskWords && acc[threadIdx.x])
+        atomicOr((unsigned long long*)&A.hub2[((int64_t)r * kHeavyMax + b) * kMaskWords + threadIdx.x],
+                 acc[threadIdx.x]);
 }
 
 void launch_hubs(const Arena& A, int num_sms, cudaStream_t s) {
     (void)num_sms;
+    const int G = A.R >= 64 ? 1 : 64 / A.R;  // CTAs per hub
     k_hub_hist<<<A.ntiles, kTileThreads, 0, s>>>(A);
     k_hub_pick<<<1, 256, 0, s>>>(A);
     k_hub_collect<<<A.ntiles, kTileThreads, 0, s>>>(A);
-    k_hub_mask<<<(unsigned)A.R * kHeavyMax, 256, 0, s>>>(A);
-    k_hub_pairs<<<(unsigned)A.R * kHeavyMax, 256, 0, s>>>(A);
+    k_hub_mask<<<(unsigned)(A.R * kHeavyMax * G), 256, 0, s>>>(A, G);
+    k_hub_pairs<<<(unsigned)(A.R * kHeavyMax * G), 256, 0, s>>>(A, G);
 }
 
 void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s) {
