@@ -447,6 +447,17 @@ float ms_between(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
+// Record a timing event.  Inside a stream capture a plain record only expresses a dependency; the
+// external flag turns it into an event-record node, so captured runs are timed as well.
+void record_event(cudaEvent_t e, cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cs);
+    if (cs == cudaStreamCaptureStatusActive)
+        cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    else
+        cudaEventRecord(e, s);
+}
+
 // Enqueue one PA epoch (no synchronisation).  agents = total new nodes of the epoch.  Returns the
 // first launch error with the stage that raised it.
 pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t* ev) {
@@ -459,7 +470,7 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
         cudaGetLastError();                                                                     \
         return fail(c, PG_ERR_CUDA, std::string("launch error in ") + name + ": " + cudaGetErrorString(e)); \
     }
-    if (events) cudaEventRecord(ev[0], s);
+    if (events) record_event(ev[0], s);
     launch_epoch_begin(A, epoch, 1, s);
     PG_STAGE("epoch begin");
     launch_weights(A, s);
@@ -469,16 +480,16 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
         PG_STAGE("hub index");
         c->launches += kHubKernels;
     }
-    if (events) cudaEventRecord(ev[1], s);
+    if (events) record_event(ev[1], s);
     launch_agent_setup(A, agents, s);
     PG_STAGE("agent setup");
-    if (events) cudaEventRecord(ev[2], s);
+    if (events) record_event(ev[2], s);
     launch_agents(A, agents, c->num_sms, s);
     PG_STAGE("agents");
-    if (events) cudaEventRecord(ev[3], s);
+    if (events) record_event(ev[3], s);
     launch_bwd_append(A, agents, c->num_sms, s);
     PG_STAGE("backward append");
-    if (events) cudaEventRecord(ev[4], s);
+    if (events) record_event(ev[4], s);
 #undef PG_STAGE
     c->launches += kPaEpochKernels;
     return PG_OK;
