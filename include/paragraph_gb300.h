@@ -202,6 +202,26 @@ pg_status pg_timer_stop(pg_ctx* ctx, double* ms);
 pg_status pg_checkpoint(pg_ctx* ctx);
 pg_status pg_restore(pg_ctx* ctx);
 
+/* ---- allocation-free generation ---- */
+/* Largest delta * ceil(n_existing / 65536) that pg_er_generate_noalloc accepts. */
+#define PG_NOALLOC_MAX_TASKS (1 << 18)
+/* No counterpart in the reference: an Erdos-Renyi epoch's edge list written into device buffers
+ * the caller owns, without allocating device memory.  It is for callers that must not call
+ * cudaMalloc/cudaFree at this point -- e.g. a program timing or capturing other device work, or a
+ * runtime that only hands out pre-sized buffers.  The edges equal those pg_er_epoch appends for
+ * the same seed, epoch, n_existing (pre-epoch nodes), delta and p: sources n_existing + i, targets
+ * in [0, n_existing), ordered by (source, target).  Scratch is a fixed 2 MiB device array inside
+ * the library (held by every GPU that loads it until the process exits); delta *
+ * ceil(n_existing/65536) above PG_NOALLOC_MAX_TASKS is rejected with PG_ERR_CAPACITY.  The first
+ * call on a device looks up that array's device address, so make it before any stream capture.
+ * Calls share the array: calls that overlap on the GPU (other streams or threads) race.  The call
+ * synchronises `stream` (a cudaStream_t, NULL for the legacy default stream); *num_edges receives
+ * the edge count, and when it exceeds `capacity` nothing is written and PG_ERR_CAPACITY is
+ * returned. */
+pg_status pg_er_generate_noalloc(uint64_t seed, int64_t epoch, int64_t n_existing, int64_t delta,
+                                 double p, int32_t* d_src, int32_t* d_dst, int64_t capacity,
+                                 int64_t* num_edges, void* stream);
+
 /* ---- host-side building blocks shared with tests ---- */
 /* Philox4x32-10 block (Salmon et al., SC'11) for counter c[4] and key k[2]. */
 void pg_philox4x32_10(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);

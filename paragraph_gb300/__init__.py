@@ -37,7 +37,7 @@ EXPORTED = [
     "pg_copy_degrees", "pg_copy_nodes", "pg_copy_csr", "pg_copy_arrivals", "pg_set_timing",
     "pg_get_stats", "pg_sync", "pg_check_device", "pg_philox4x32_10", "pg_poisson_table",
     "pg_logf_host", "pg_expf_host", "pg_log_host", "pg_exp_host", "pg_version",
-    "pg_timer_start", "pg_timer_stop", "pg_checkpoint", "pg_restore",
+    "pg_timer_start", "pg_timer_stop", "pg_checkpoint", "pg_restore", "pg_er_generate_noalloc",
 ]
 
 
@@ -158,6 +158,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_timer_stop": (i32, [vp, P(C.c_double)]),
         "pg_checkpoint": (i32, [vp]),
         "pg_restore": (i32, [vp]),
+        "pg_er_generate_noalloc": (i32, [u64, i64, i64, i64, C.c_double, vp, vp, i64, P(i64), vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
