@@ -333,6 +333,45 @@ def run_ours(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def epoch_report(args) -> None:
+    """One JSON line per epoch of the workload: stage times (CUDA events) and byte-model counters.
+    Stops early when an epoch exceeds --epoch-cap-s (the enumeration sampler slows down as hubs
+    grow)."""
+    from paragraph_gb300 import GrowthEngine
+
+    g, prm = seed_graph(args.seed)
+    with GrowthEngine(seed=args.seed, sampler=args.sampler) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=EPOCHS)
+        for e in range(args.report_epochs):
+            t0 = time.perf_counter()
+            nn, ne = eng.grow_epoch()
+            wall = time.perf_counter() - t0
+            s = eng.stats()
+            keep = ("new_edges", "rows_expanded", "elems_streamed", "draws", "bwd_moved",
+                    "bytes_alg", "bytes_alg_agents", "ms_total", "ms_weights", "ms_setup",
+                    "ms_agents", "ms_csr")
+            rec = {"epoch": e, "sampler": args.sampler, "nodes": eng.counts()[0], "new_nodes": nn}
+            rec.update({k: (round(s[k], 4) if isinstance(s[k], float) else s[k]) for k in keep})
+            print(json.dumps(rec), flush=True)
+            if wall > args.epoch_cap_s:
+                break
+
+
+def profile_case(args) -> None:
+    """Small bounded case for ncu: load the workload's seed and run two PA epochs."""
+    from paragraph_gb300 import GrowthEngine
+
+    g, prm = seed_graph(args.seed)
+    with GrowthEngine(seed=args.seed, sampler=args.sampler) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=2)
+        for e in range(2):
+            eng.grow_epoch()
+            s = eng.stats()
+            print(json.dumps({"epoch": e, "bytes_alg_agents": s["bytes_alg_agents"],
+                              "bytes_alg": s["bytes_alg"], "ms_agents": s["ms_agents"],
+                              "new_edges": s["new_edges"]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -343,7 +382,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--sampler", type=int, default=0, help="0 thinning, 1 neighbourhood enumeration")
+    ap.add_argument("--epoch-report", action="store_true", help="per-epoch stage report instead")
+    ap.add_argument("--report-epochs", type=int, default=EPOCHS)
+    ap.add_argument("--epoch-cap-s", type=float, default=10.0)
+    ap.add_argument("--profile-case", action="store_true", help="two epochs for ncu, then exit")
     args = ap.parse_args()
+    if args.epoch_report:
+        return epoch_report(args)
+    if args.profile_case:
+        return profile_case(args)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
