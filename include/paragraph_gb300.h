@@ -138,6 +138,8 @@ typedef struct {
     double run_ms_agents;
     double run_ms_csr;
     int64_t run_kernel_launches; /* kernels the run enqueued (graph nodes when captured) */
+    int64_t adj_scanned;       /* adjacency entries examined by ball-membership tests (thinning) */
+    int64_t run_adj_scanned;
 } pg_stats;
 
 /* ---- lifecycle ---- */

@@ -200,10 +200,10 @@ class OracleGraph:
         return a[:c]
 
     def stats(self) -> dict:
-        s = np.zeros(5, np.int64)
+        s = np.zeros(6, np.int64)
         self._lib.og_stats(self._g, _p(s))
         return dict(nodes_weighted=int(s[0]), rows_expanded=int(s[1]), elems_streamed=int(s[2]),
-                    draws=int(s[3]), new_edges=int(s[4]))
+                    draws=int(s[3]), new_edges=int(s[4]), adj_scanned=int(s[5]))
 
     def weights(self):
         n = self._lib.og_copy_weights(self._g, None, None, None)

@@ -17,14 +17,16 @@
  *   neighbourhood     the 2-hop undirected ball of GetOneAndTwoHopNeighborhood
  *                     (src/abm.cu:577-682): forward and backward rows of the anchors and of their
  *                     neighbours.
- *   sampling          weighted sampling without replacement.  The reference draws
- *                     Efraimidis-Spirakis keys log(u)/score and keeps a top-k heap
- *                     (src/abm.cu:461-565, gpu-std/device_min_heap.cuh:71-145).  Here the same
- *                     exponential-clock idea is split into two independent races: a global race
- *                     over all nodes (sequential inverse-CDF draws, without replacement) and a
- *                     neighbourhood race over the ball with rate (beta-1) w_j (keys E/w_j, k
- *                     smallest).  The first k distinct arrivals of the merged race are a
- *                     successive-sampling draw with weights w_j beta^[j in N_a].
+ *   sampling          weighted sampling without replacement with weights w_j beta^[j in N_a].
+ *                     The reference draws Efraimidis-Spirakis keys log(u)/score and keeps a top-k
+ *                     heap (src/abm.cu:461-565, gpu-std/device_min_heap.cuh:71-145).  Two
+ *                     restatements of that law, each consuming its own Philox streams:
+ *                     sample_agent_thin (default): one Poisson event stream with rate beta w_j,
+ *                       each event global (kept) with probability 1/beta or boost (kept iff the
+ *                       node is in the ball); the first k distinct kept nodes are the sample;
+ *                     sample_agent (enumeration): a global race of sequential inverse-CDF draws
+ *                       without replacement merged with a neighbourhood race over the enumerated
+ *                       ball (keys E/w_j, k smallest).
  *   edge emit         ABMKernelStage4 (src/abm.cu:958-994): one (agent, cited) edge per choice.
  *   CSR append        the host edge insert and updateNodeInDegreeOutDegree
  *                     (src/kernel.cu:1766-1815, src/graph.cu:537-618).
@@ -239,6 +241,7 @@ struct og_graph {
     int64_t fixed_new;
     int anchors;
     int sampler; /* 0 thinning, 1 neighbourhood enumeration */
+    int64_t hub_thr; /* degree from which a node is a hub this epoch (thinning counters) */
     uint64_t table[OG_TABLE];
     /* nodes */
     int64_t n;
@@ -254,7 +257,7 @@ struct og_graph {
     /* last epoch */
     int64_t last_first, last_count;
     int32_t* arrivals;
-    int64_t stats[5];
+    int64_t stats[6];
     float* w;
     uint64_t* cdf;
     int64_t w_n;
@@ -592,16 +595,49 @@ static int bsearch32(const int32_t* a, int64_t n, int32_t v) {
 }
 
 /* j in the 2-hop undirected ball of the anchors <=> j in Z = anchors U adj(anchors), or an
- * adjacency row of j meets Z.  Pure set membership: any evaluation order gives the same answer. */
-static int in_ball(const og_graph* g, const int32_t* Z, int64_t nz, int32_t j) {
+ * adjacency row of j meets Z.  Pure set membership: any evaluation order gives the same answer.
+ * *examined counts the adjacency entries of j looked at in order (forward row, then backward row)
+ * up to and including the first hit; it is 0 when j is in Z or is a hub (degree >= hub_thr), whose
+ * membership the engine answers from a bit mask. */
+static int in_ball(const og_graph* g, const int32_t* Z, int64_t nz, int32_t j, int64_t* examined) {
+    *examined = 0;
     if (bsearch32(Z, nz, j)) return 1;
+    const int64_t deg = (g->fwd_off[j + 1] - g->fwd_off[j]) + (g->bwd_off[j + 1] - g->bwd_off[j]);
+    const int hub = deg >= g->hub_thr;
+    int64_t seen = 0;
     for (int dir = 0; dir < 2; dir++) {
         const int64_t* off = dir ? g->bwd_off : g->fwd_off;
         const int32_t* col = dir ? g->bwd_col : g->fwd_col;
-        for (int64_t p = off[j]; p < off[j + 1]; p++)
-            if (bsearch32(Z, nz, col[p])) return 1;
+        for (int64_t p = off[j]; p < off[j + 1]; p++) {
+            seen++;
+            if (bsearch32(Z, nz, col[p])) {
+                if (!hub) *examined = seen;
+                return 1;
+            }
+        }
     }
+    if (!hub) *examined = seen;
     return 0;
+}
+
+/* Hub threshold of the epoch: at most 256 nodes, those in the highest log2-degree bins (>= 2^10). */
+static int64_t hub_threshold(const og_graph* g) {
+    int64_t hist[24] = {0};
+    for (int64_t v = 0; v < g->n; v++) {
+        int64_t d = (g->fwd_off[v + 1] - g->fwd_off[v]) + (g->bwd_off[v + 1] - g->bwd_off[v]);
+        if (d >= 1024) {
+            int b = 63 - __builtin_clzll((unsigned long long)d) - 10;
+            if (b > 23) b = 23;
+            hist[b]++;
+        }
+    }
+    int64_t thr = INT64_MAX, cum = 0;
+    for (int b = 23; b >= 0; b--) {
+        cum += hist[b];
+        if (cum > 256) break;
+        if (hist[b]) thr = (int64_t)1 << (b + 10);
+    }
+    return thr;
 }
 
 enum { S_FALLBACK = 9 };
@@ -659,7 +695,7 @@ static int sample_agent_thin(const og_graph* g, int64_t a, const uint64_t* cdf, 
     const uint64_t Wq = cdf[n - 1];
     int taken = 0;
     const int64_t maxev = 64 * k + 256;
-    int64_t events = 0, tests = 0;
+    int64_t events = 0, tests = 0, scanned = 0;
     for (int64_t i = 0; i < maxev && taken < k; i++) {
         rng(g->seed, S_GLOBAL, rep, ep, unit, (uint32_t)i, r);
         uint64_t y = hi_mul64(join64(r[0], r[1]), Wq);
@@ -682,8 +718,11 @@ static int sample_agent_thin(const og_graph* g, int64_t a, const uint64_t* cdf, 
             }
         if (dup) continue; /* an arrived node gains nothing from another event */
         if (!glob) {
+            int64_t ex;
             tests++;
-            if (!in_ball(g, Z, nz, j)) continue;
+            int mem = in_ball(g, Z, nz, j, &ex);
+            scanned += ex;
+            if (!mem) continue;
         }
         out_arr[taken++] = j;
     }
@@ -724,8 +763,11 @@ static int sample_agent_thin(const og_graph* g, int64_t a, const uint64_t* cdf, 
             events++;
             int glob = unif_d(r[2], r[3]) <= g->p_global;
             if (!glob) {
+                int64_t ex;
                 tests++;
-                if (!in_ball(g, Z, nz, j)) continue;
+                int mem = in_ball(g, Z, nz, j, &ex);
+                scanned += ex;
+                if (!mem) continue;
             }
             uint64_t qj = cdf[j] - (j > 0 ? cdf[j - 1] : 0);
             int pos = nc;
@@ -743,6 +785,7 @@ static int sample_agent_thin(const og_graph* g, int64_t a, const uint64_t* cdf, 
     }
     cnt[1] += tests;
     cnt[2] += events;
+    cnt[3] += scanned;
     memcpy(out_sorted, out_arr, sizeof(int32_t) * (size_t)taken);
     qsort(out_sorted, (size_t)taken, sizeof(int32_t), cmp_i32);
     return taken;
@@ -797,16 +840,17 @@ int og_pa_epoch(og_graph* g, int threads) {
     int32_t* rows = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta * 256);
     int32_t* arr = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta * 256);
     int32_t* kk = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta);
-    int64_t rows_exp = 0, elems = 0, draws = 0;
+    int64_t rows_exp = 0, elems = 0, draws = 0, scanned = 0;
+    g->hub_thr = g->sampler == 0 ? hub_threshold(g) : INT64_MAX;
     if (threads > 0) omp_set_num_threads(threads);
-#pragma omp parallel reduction(+ : rows_exp, elems, draws)
+#pragma omp parallel reduction(+ : rows_exp, elems, draws, scanned)
     {
         keyvec kv = {0, 0, 0};
         int32_t* zbuf = NULL;
         int64_t zcap = 0;
 #pragma omp for schedule(dynamic, 16)
         for (int64_t a = 0; a < delta; a++) {
-            int64_t cnt[3] = {0, 0, 0};
+            int64_t cnt[4] = {0, 0, 0, 0};
             if (g->sampler == 0) {
                 kk[a] = sample_agent_thin(g, a, g->cdf, npos, rows + a * 256, arr + a * 256, cnt,
                                           &zbuf, &zcap);
@@ -818,6 +862,7 @@ int og_pa_epoch(og_graph* g, int threads) {
             rows_exp += cnt[0];
             elems += cnt[1];
             draws += cnt[2];
+            scanned += cnt[3];
         }
         free(kv.v);
         free(zbuf);
@@ -842,6 +887,7 @@ int og_pa_epoch(og_graph* g, int threads) {
     g->stats[2] = elems;
     g->stats[3] = draws;
     g->stats[4] = e_new;
+    g->stats[5] = scanned;
     g->epoch++;
     free(rows);
     free(arr);
@@ -940,7 +986,7 @@ void og_epoch_edges(const og_graph* g, int64_t* first, int64_t* count) {
 void og_copy_arrivals(const og_graph* g, int32_t* cited) {
     if (g->arrivals) memcpy(cited, g->arrivals, sizeof(int32_t) * (size_t)g->last_count);
 }
-void og_stats(const og_graph* g, int64_t* out5) { memcpy(out5, g->stats, sizeof(g->stats)); }
+void og_stats(const og_graph* g, int64_t* out6) { memcpy(out6, g->stats, sizeof(g->stats)); }
 int64_t og_copy_weights(const og_graph* g, float* w, uint64_t* cdf, int32_t* shift) {
     if (w) memcpy(w, g->w, sizeof(float) * (size_t)g->w_n);
     if (cdf) memcpy(cdf, g->cdf, sizeof(uint64_t) * (size_t)g->w_n);

@@ -52,8 +52,8 @@ void og_copy_nodes(const og_graph* g, int32_t* pub, float* fitness);
 /* last epoch: first edge index (forward-CSR order) and count; arrivals in arrival order */
 void og_epoch_edges(const og_graph* g, int64_t* first, int64_t* count);
 void og_copy_arrivals(const og_graph* g, int32_t* cited);
-/* last epoch counters: nodes_weighted, rows_expanded, elems_streamed, draws, new_edges */
-void og_stats(const og_graph* g, int64_t* out5);
+/* last epoch counters: nodes_weighted, rows_expanded, elems_streamed, draws, new_edges, adj_scanned */
+void og_stats(const og_graph* g, int64_t* out6);
 /* last epoch weights w0 (float, n_pre entries) and CDF (uint64) for unit tests */
 int64_t og_copy_weights(const og_graph* g, float* w, uint64_t* cdf, int32_t* shift);
 

@@ -75,7 +75,8 @@ class _Stats(C.Structure):
         "run_epochs", "run_new_nodes", "run_new_edges", "run_rows_expanded", "run_elems_streamed",
         "run_draws", "run_bwd_moved", "run_nodes_weighted", "run_bytes_alg", "run_bytes_alg_agents")] + [
         (n, C.c_double) for n in ("run_ms_weights", "run_ms_setup", "run_ms_agents", "run_ms_csr")] + [
-        ("run_kernel_launches", C.c_int64)]
+        ("run_kernel_launches", C.c_int64), ("adj_scanned", C.c_int64),
+        ("run_adj_scanned", C.c_int64)]
 
 
 @dataclass

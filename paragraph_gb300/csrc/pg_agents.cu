@@ -410,10 +410,10 @@ __global__ void k_edges_check(Arena A, int64_t agents) {
 
 template <int KCAP, bool BIG, bool THIN>
 __global__ void __launch_bounds__(kAgentWarps * 32) k_agents(Arena A, int64_t agents) {
-    // frontier capacity: 2048 entries for the common small-k kernel, 1024 for the k <= 256 one so
-    // that four warps stay within 48 KiB of static shared memory
-    constexpr int ZCAP = KCAP <= kKSmall ? 2 * kZCap : kZCap;
-    using Smem = typename std::conditional<THIN, ThinSmem<KCAP, ZCAP>, AgentSmem<KCAP>>::type;
+    // frontier hash capacity: 2048 slots for the common small-k kernel, 1024 for the k <= 256 one
+    // so that four warps stay within 48 KiB of static shared memory
+    constexpr int HCAP = KCAP <= kKSmall ? 2 * kZCap : kZCap;
+    using Smem = typename std::conditional<THIN, ThinSmem<KCAP, HCAP>, AgentSmem<KCAP>>::type;
     __shared__ Smem smem[kAgentWarps];
     if (A.st->error) return;
     Smem& S = smem[threadIdx.x >> 5];
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(kAgentWarps * 32) k_agents(Arena A, int64_t ag
         const int k = A.kk[a];
         if (!BIG && k > KCAP) continue;
         if constexpr (THIN)
-            process_agent_thin<KCAP, ZCAP>(A, a, k, S);
+            process_agent_thin<KCAP, HCAP>(A, a, k, S);
         else
             process_agent<KCAP>(A, a, k, S);
     }

@@ -509,14 +509,19 @@ int64_t plan_epoch(pg_ctx* c, std::vector<int64_t>* deltas) {
 
 // Algorithmic bytes of the PA epoch (the minimum traffic of the algorithm, not what a given
 // implementation moves):
-//   agents : per adjacency row read 32 B (fwd and bwd begin/end, int64), per streamed neighbour
-//            8 B (its int32 id and its fp32 weight), per draw 32 B (one CDF sector), per edge 16 B
-//            (forward column, in-degree counter, rank, destination)
+//   agents, thinning sampler: per frontier entry gathered 36 B (its int32 id and its 256-bit hub
+//            mask), per membership test 16 B (the candidate's row offsets), per adjacency entry the
+//            test examined 4 B, per event 32 B (one CDF sector), per edge 16 B (forward column,
+//            in-degree counter, rank, destination)
+//   agents, enumeration sampler: per adjacency row read 32 B (fwd and bwd begin/end, int64), per
+//            streamed neighbour 8 B (its int32 id and its fp32 weight), per draw 32 B, per edge 16 B
 //   weights: per node 44 B (fitness, in-degree, publication epoch, weight write, weight read, CDF
 //            write, CDF read+write in the tile-offset pass)
 //   csr    : 8 B per moved backward entry, 12 B per new edge (place + sort), 24 B per node
 //            (old and new backward offsets, length)
-int64_t agent_bytes(int64_t rows, int64_t elems, int64_t draws, int64_t edges) {
+int64_t agent_bytes(bool thin, int64_t rows, int64_t elems, int64_t draws, int64_t edges,
+                    int64_t scanned) {
+    if (thin) return 36 * rows + 16 * elems + 4 * scanned + 32 * draws + 16 * edges;
     return 32 * rows + 8 * elems + 32 * draws + 16 * edges;
 }
 int64_t weight_bytes(int64_t nodes) { return 44 * nodes; }
@@ -535,9 +540,10 @@ void fill_stats(pg_ctx* c, int64_t new_nodes, bool er) {
     S.elems_streamed = (int64_t)st.elems_streamed;
     S.draws = (int64_t)st.draws;
     S.bwd_moved = (int64_t)st.bwd_moved;
+    S.adj_scanned = (int64_t)st.adj_scanned;
     const int64_t E = st.edges;
-    // byte model: see DESIGN.md ("Algorithmic bytes")
-    const int64_t ab = agent_bytes(S.rows_expanded, S.elems_streamed, S.draws, E);
+    const int64_t ab = agent_bytes(c->cfg.sampler == PG_SAMPLER_THINNING, S.rows_expanded,
+                                   S.elems_streamed, S.draws, E, S.adj_scanned);
     S.bytes_alg_agents = er ? 0 : ab;
     // ER: per edge 8 B edge-list write + 12 B CSR append; per new node 32 B (count + offsets)
     S.bytes_alg = er ? (8 * E + 12 * E + 32 * new_nodes + 8 * S.bwd_moved)
@@ -939,7 +945,10 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
     S.run_draws = (int64_t)hs.cum_draws;
     S.run_bwd_moved = (int64_t)hs.cum_bwd_moved;
     S.run_nodes_weighted = (int64_t)hs.cum_nodes_weighted;
-    S.run_bytes_alg_agents = agent_bytes(S.run_rows_expanded, S.run_elems_streamed, S.run_draws, S.run_new_edges);
+    S.run_adj_scanned = (int64_t)hs.cum_adj_scanned;
+    S.run_bytes_alg_agents = agent_bytes(c->cfg.sampler == PG_SAMPLER_THINNING, S.run_rows_expanded,
+                                         S.run_elems_streamed, S.run_draws, S.run_new_edges,
+                                         S.run_adj_scanned);
     S.run_bytes_alg = S.run_bytes_alg_agents + weight_bytes(S.run_nodes_weighted) +
                       csr_bytes(S.run_bwd_moved, S.run_new_edges, S.run_nodes_weighted, S.run_new_nodes);
     S.run_kernel_launches = c->launches;

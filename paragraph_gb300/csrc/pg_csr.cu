@@ -283,6 +283,7 @@ __global__ void k_epoch_end(Arena A, int64_t agents) {
         st->cum_edges += (unsigned long long)A.eoff[agents];
         st->cum_new_nodes += (unsigned long long)agents;
         st->cum_epochs += 1;
+        st->cum_adj_scanned += st->adj_scanned;
     }
 }
 

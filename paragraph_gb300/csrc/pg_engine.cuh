@@ -93,6 +93,7 @@ struct EpochState {
     unsigned long long bwd_moved;
     unsigned long long nodes_weighted;
     unsigned long long copy_tiles;  // backward-copy tiles of the epoch (all replicas)
+    unsigned long long adj_scanned; // adjacency entries examined by membership tests
     // run totals, accumulated by the epoch-end kernel and cleared by the host at run start
     unsigned long long cum_rows_expanded;
     unsigned long long cum_elems_streamed;
@@ -102,6 +103,7 @@ struct EpochState {
     unsigned long long cum_edges;
     unsigned long long cum_new_nodes;
     unsigned long long cum_epochs;
+    unsigned long long cum_adj_scanned;
 };
 
 // Device pointers of the arena (passed by value to kernels).

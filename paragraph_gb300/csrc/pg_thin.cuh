@@ -10,16 +10,19 @@
 //
 // Ball membership, the 2-hop BFS of GetOneAndTwoHopNeighborhood (src/abm.cu:577-682) answered on
 // demand instead of materialised:
-//   Z  = anchors U adj(x) for every non-hub anchor x   -- the 1-hop frontier, sorted in shared mem.
+//   Z  = anchors U adj(x) for every non-hub anchor x   -- the 1-hop frontier, a hash set in shared
+//                                                          memory (open addressing, load <= 1/2).
 //   HA = hub bits of the anchors that are hubs          -- their (huge) rows stay implicit.
 //   in_z(v)   <=> v in Z  or  hmask[v] & HA != 0        (v adjacent to a hub anchor)
 //   member(j) <=> in_z(j)  or  some z in adj(j) has in_z(z)
 // For a hub j, the second clause is one bit of HM = OR of hmask over Z | OR of hub2[b] over b in HA,
-// where hub2[b] marks the hubs that share a neighbour with hub b.
+// where hub2[b] marks the hubs that share a neighbour with hub b.  A test of a non-hub j scans
+// adj(j) (forward row, then backward row) 32 entries at a time and stops at the first hit; the
+// number of entries it examined feeds the byte model.
 
-template <int KCAP, int ZCAP>
+template <int KCAP, int HCAP>
 struct ThinSmem {
-    int32_t Z[ZCAP];
+    int32_t H[HCAP];  // frontier hash set, -1 = empty
     int32_t arr[KCAP];
     int32_t out[KCAP];
     int32_t c_id[KCAP];
@@ -35,17 +38,17 @@ struct Ball {
     const int32_t* fc;
     const int64_t* bo;
     const int32_t* bc;
-    const int16_t* hslot;       // hub bit of the node or -1
+    const int16_t* hslot;             // hub bit of the node or -1
     const unsigned long long* hmask;  // [node][kMaskWords]
-    const int32_t* Z;           // sorted unique (shared memory) when small
-    int nz;
-    bool small;
+    const int32_t* H;                 // frontier hash set (shared memory)
+    int hbits;                        // log2 of the hash capacity
+    bool small;                       // every non-hub anchor's rows are in H
     int na;
     int anchors[PG_MAX_ANCHORS_DEV];
-    bool big_anchor[PG_MAX_ANCHORS_DEV];  // non-hub anchor whose rows did not fit in Z
-    Mask ha;                    // hub bits of hub anchors
+    bool big_anchor[PG_MAX_ANCHORS_DEV];  // non-hub anchor whose rows did not fit in H
+    Mask ha;                          // hub bits of hub anchors
     bool any_ha;
-    Mask hm;                    // hubs in the ball through Z or a hub anchor
+    Mask hm;                          // hubs in the ball through Z or a hub anchor
 };
 
 __device__ __forceinline__ bool contains(const int32_t* a, int64_t lo, int64_t hi, int32_t v) {
@@ -60,23 +63,47 @@ __device__ __forceinline__ bool contains(const int32_t* a, int64_t lo, int64_t h
     return l < hi && a[l] == v;
 }
 
+__device__ __forceinline__ uint32_t hslot_of(int32_t v, int bits) {
+    return ((uint32_t)v * 0x9E3779B1u) >> (32 - bits);
+}
+
+// Insert v into the shared hash set (any lane, concurrently).
+__device__ __forceinline__ void hash_insert(int32_t* H, int bits, int32_t v) {
+    const uint32_t mask = (1u << bits) - 1u;
+    uint32_t s = hslot_of(v, bits);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const int prev = atomicCAS(&H[s], -1, v);
+        if (prev == -1 || prev == v) return;
+        s = (s + 1u) & mask;
+    }
+}
+
+__device__ __forceinline__ bool hash_contains(const int32_t* H, int bits, int32_t v) {
+    const uint32_t mask = (1u << bits) - 1u;
+    uint32_t s = hslot_of(v, bits);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const int k = H[s];
+        if (k == v) return true;
+        if (k == -1) return false;
+        s = (s + 1u) & mask;
+    }
+    return false;
+}
+
 __device__ __forceinline__ int hub_slot(const Ball& B, int32_t v) { return B.hslot[v]; }
 
 __device__ __forceinline__ bool mask_bit(const Mask& m, int b) { return (m.w[b >> 6] >> (b & 63)) & 1ull; }
 
 // v in Z (frontier) -- lane-level, any lane may call it with its own v
 __device__ __forceinline__ bool in_z(const Ball& B, int32_t v) {
-    if (B.small) {
-        if (contains(B.Z, 0, B.nz, v)) return true;
-    } else {
+    if (hash_contains(B.H, B.hbits, v)) return true;
+    if (!B.small) {
         for (int i = 0; i < B.na; ++i) {
+            if (!B.big_anchor[i]) continue;
             const int x = B.anchors[i];
-            if (v == x) return true;
-            if (B.big_anchor[i] &&
-                (contains(B.fc, B.fo[x], B.fo[x + 1], v) || contains(B.bc, B.bo[x], B.bo[x + 1], v)))
+            if (contains(B.fc, B.fo[x], B.fo[x + 1], v) || contains(B.bc, B.bo[x], B.bo[x + 1], v))
                 return true;
         }
-        if (contains(B.Z, 0, B.nz, v)) return true;
     }
     if (B.any_ha) {
         const unsigned long long* m = B.hmask + (int64_t)v * kMaskWords;
@@ -87,9 +114,11 @@ __device__ __forceinline__ bool in_z(const Ball& B, int32_t v) {
     return false;
 }
 
-// Warp-cooperative membership of one node j (warp-uniform argument and result).
-__device__ bool member_warp(const Ball& B, int32_t j) {
+// Warp-cooperative membership of one node j (warp-uniform argument and result); `examined` gets the
+// adjacency entries looked at, in order, up to and including the first hit.
+__device__ bool member_warp(const Ball& B, int32_t j, long long& examined) {
     const int lane = lane_id();
+    examined = 0;
     if (in_z(B, j)) return true;  // every lane evaluates the same thing
     const int hs = hub_slot(B, j);
     if (hs >= 0) return mask_bit(B.hm, hs);
@@ -99,14 +128,22 @@ __device__ bool member_warp(const Ball& B, int32_t j) {
         const int64_t p0 = off[j], p1 = off[j + 1];
         for (int64_t p = p0; p < p1; p += 32) {
             const bool hit = (p + lane < p1) && in_z(B, col[p + lane]);
-            if (__any_sync(kFull, hit)) return true;
+            const unsigned m = __ballot_sync(kFull, hit);
+            if (m) {
+                examined += (p - p0) + __ffs(m);
+                return true;
+            }
         }
+        examined += p1 - p0;
     }
     return false;
 }
 
-template <int KCAP, int ZCAP>
-__device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KCAP, ZCAP>& S) {
+template <int KCAP, int HCAP>
+__device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KCAP, HCAP>& S) {
+    constexpr int kHBits = HCAP == 4096 ? 12 : (HCAP == 2048 ? 11 : 10);
+    static_assert(HCAP == (1 << kHBits), "hash capacity must be 1024, 2048 or 4096");
+    constexpr int ZCAP = HCAP / 2;  // entries gathered into the frontier (with repeats)
     const int lane = lane_id();
     const int r = replica_of_agent(A.rep, A.R, a);
     const Replica& rp = A.rep[r];
@@ -121,8 +158,8 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     B.bc = A.bwd_col_cur + rp.ebase;
     B.hslot = A.hslot + rp.nbase;
     B.hmask = reinterpret_cast<const unsigned long long*>(A.hmask) + rp.nbase * kMaskWords;
-    B.Z = S.Z;
-    B.nz = 0;
+    B.H = S.H;
+    B.hbits = kHBits;
     B.small = true;
     B.na = 0;
     B.any_ha = false;
@@ -133,9 +170,10 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
 
     // ---------------------------------------------------------------- frontier
     if (boost) {
+        for (int q = lane; q < HCAP; q += 32) S.H[q] = -1;
         B.na = rp.anchors;
         const u32x4 xa = draw(A.seed, kStreamAnchor, rep, ep, unit, 0);
-        int64_t zsize = B.na;
+        int64_t zsize = 0;
 #pragma unroll
         for (int i = 0; i < PG_MAX_ANCHORS_DEV; ++i) {
             B.anchors[i] = (int)bounded32(xa.x[i], (uint32_t)n);
@@ -144,7 +182,7 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
         for (int i = 0; i < B.na; ++i) {
             const int x = B.anchors[i];
             const int64_t d = (B.fo[x + 1] - B.fo[x]) + (B.bo[x + 1] - B.bo[x]);
-            rows += d;
+            rows += d + 1;
             const int hs = hub_slot(B, x);
             if (hs >= 0) {
                 B.ha.w[hs >> 6] |= 1ull << (hs & 63);
@@ -153,9 +191,8 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                 zsize += d;
             }
         }
-        rows += B.na;
         // non-hub anchors whose rows would overflow the shared frontier stay implicit
-        if (zsize > ZCAP) {
+        if (zsize + B.na > ZCAP) {
             B.small = false;
             zsize = B.na;
             for (int i = 0; i < B.na; ++i) {
@@ -168,72 +205,27 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                     B.big_anchor[i] = true;
             }
         }
-        int w = 0;
-        for (int i = 0; i < B.na; ++i) {
-            const int x = B.anchors[i];
-            if (lane == 0) S.Z[w] = x;
-            ++w;
-            if (hub_slot(B, x) >= 0 || B.big_anchor[i]) continue;
-            const int64_t lf = B.fo[x + 1] - B.fo[x], lb = B.bo[x + 1] - B.bo[x];
-            for (int64_t q = lane; q < lf; q += 32) S.Z[w + q] = B.fc[B.fo[x] + q];
-            w += (int)lf;
-            for (int64_t q = lane; q < lb; q += 32) S.Z[w + q] = B.bc[B.bo[x] + q];
-            w += (int)lb;
-        }
-        int P = 1;
-        while (P < w) P <<= 1;
-        for (int q = w + lane; q < P; q += 32) S.Z[q] = 0x7fffffff;
         __syncwarp();
-        for (int kk = 2; kk <= P; kk <<= 1) {
-            for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-                for (int q = lane; q < P; q += 32) {
-                    const int qx = q ^ jj;
-                    if (qx > q) {
-                        const int va = S.Z[q], vb = S.Z[qx];
-                        if ((va > vb) == ((q & kk) == 0)) {
-                            S.Z[q] = vb;
-                            S.Z[qx] = va;
-                        }
-                    }
-                }
-                __syncwarp();
-            }
-        }
-        // in-place unique; a chunk's predecessor is carried in a register because the previous
-        // chunk's writes may have overwritten it
-        int nz = 0, carry = -1;
-        for (int base = 0; base < w; base += 32) {
-            const int q = base + lane;
-            const int v = q < w ? S.Z[q] : 0x7fffffff;
-            int pv = __shfl_up_sync(kFull, v, 1);
-            if (lane == 0) pv = carry;
-            carry = __shfl_sync(kFull, v, 31);
-            const bool keep = q < w && (q == 0 || pv != v);
-            const unsigned m = __ballot_sync(kFull, keep);
-            __syncwarp();
-            if (keep) S.Z[nz + __popc(m & ((1u << lane) - 1))] = v;
-            nz += __popc(m);
-            __syncwarp();
-        }
-        B.nz = nz;
-        // HM: hubs adjacent to the frontier, to a big anchor's rows, or sharing a neighbour with a
-        // hub anchor
         Mask hm;
 #pragma unroll
         for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] = 0ull;
-        for (int q = lane; q < nz; q += 32) {
-            const unsigned long long* m = B.hmask + (int64_t)S.Z[q] * kMaskWords;
-#pragma unroll
-            for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] |= m[ww];
-        }
         for (int i = 0; i < B.na; ++i) {
             const int x = B.anchors[i];
-            if (!B.big_anchor[i]) continue;
+            if (lane == 0) {
+                hash_insert(S.H, kHBits, x);
+                const unsigned long long* m = B.hmask + (int64_t)x * kMaskWords;
+#pragma unroll
+                for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] |= m[ww];
+            }
+            if (hub_slot(B, x) >= 0) continue;
+            const bool into_hash = !B.big_anchor[i];
             for (int dir = 0; dir < 2; ++dir) {
                 const int64_t* off = dir ? B.bo : B.fo;
                 const int32_t* col = dir ? B.bc : B.fc;
                 for (int64_t p = off[x] + lane; p < off[x + 1]; p += 32) {
-                    const unsigned long long* m = B.hmask + (int64_t)col[p] * kMaskWords;
+                    const int32_t v = col[p];
+                    if (into_hash) hash_insert(S.H, kHBits, v);
+                    const unsigned long long* m = B.hmask + (int64_t)v * kMaskWords;
 #pragma unroll
                     for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] |= m[ww];
                 }
@@ -255,13 +247,14 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             hi = __reduce_or_sync(kFull, hi);
             B.hm.w[ww] = ((unsigned long long)hi << 32) | lo;
         }
+        __syncwarp();
     }
 
     // ---------------------------------------------------------------- events
     const uint64_t Wq = rp.wq_total;
     const double pg = rp.p_global;
     int nch = 0;
-    long long events = 0, tests = 0;
+    long long events = 0, tests = 0, scanned = 0;
     const int maxev = 64 * k + 256;
     for (int i0 = 0; i0 < maxev && nch < k; i0 += 32) {
         const u32x4 x = draw(A.seed, kStreamGlobal, rep, ep, unit, (uint32_t)(i0 + lane));
@@ -285,7 +278,10 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             if (__any_sync(kFull, dup)) continue;
             if (!gl) {
                 ++tests;
-                if (!member_warp(B, jl)) continue;
+                long long ex;
+                const bool mem = member_warp(B, jl, ex);
+                scanned += ex;
+                if (!mem) continue;
             }
             if (lane == 0) S.arr[nch] = jl;
             __syncwarp();
@@ -359,7 +355,10 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             ++events;
             if (!glob) {
                 ++tests;
-                if (!member_warp(B, j)) continue;
+                long long ex;
+                const bool mem = member_warp(B, j, ex);
+                scanned += ex;
+                if (!mem) continue;
             }
             const uint64_t qj = cdf[j] - (j > 0 ? cdf[j - 1] : 0);
             int below = 0;
@@ -393,5 +392,6 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
         }
     }
     if (nch != k && lane == 0) atomicOr(&A.st->error, kErrArg);
+    if (lane == 0 && scanned) atomicAdd(&A.st->adj_scanned, (unsigned long long)scanned);
     emit_row<KCAP>(A, rp, a, al, n, S.arr, S.out, nch, rows, tests, events);
 }

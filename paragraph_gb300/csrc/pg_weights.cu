@@ -36,6 +36,7 @@ __global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, in
         st->draws = 0;
         st->bwd_moved = 0;
         st->nodes_weighted = 0;
+        st->adj_scanned = 0;
     }
     __syncthreads();
     for (int base = 0; base < A.R; base += 1024) {

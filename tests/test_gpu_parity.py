@@ -62,6 +62,8 @@ def test_pa_small_bit_exact(gpu, sampler, n0, delta, lam, beta):
             st, so = eng.stats(), og.stats()
             for k in ("nodes_weighted", "rows_expanded", "elems_streamed", "draws"):
                 assert st[k] == so[k], k
+            if sampler == PG_SAMPLER_THINNING:
+                assert st["adj_scanned"] == so["adj_scanned"]
             _compare_state(eng, og)
 
 
