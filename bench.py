@@ -333,6 +333,152 @@ def run_ours(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+ENS_REPLICAS, ENS_EPOCHS = 256, 10
+ENS_WORKLOAD = "ensemble_256_replicas_5k_200k_10_epochs_3pct"
+
+
+def run_ensemble(args) -> None:
+    """Batched ensemble: 256 replicas (seed sizes log-uniform in [5k, 200k], per-replica alpha,
+    tau, gamma, beta, Poisson(20), 3 % growth) grown 10 epochs in ONE context -- one launch of each
+    epoch kernel over all replicas, the 10 epochs captured as one CUDA graph, launch shape picked by
+    the engine's autotuner.  The same replicas grown serially, one single-replica context each
+    (the plain per-replica method), give the serial time.  An eval is one replica grown 10 epochs.
+    Under torchrun the replicas are split across ranks (no exchange)."""
+    world, rank, local, dist = dist_setup()
+    from paragraph_gb300 import GrowthEngine
+    from paragraph_gb300 import workloads as W
+
+    reps_all = W.ensemble_inputs(replicas=ENS_REPLICAS, lo=5_000, hi=200_000, epochs=ENS_EPOCHS,
+                                 seed=args.seed)
+    idx = list(range(rank, ENS_REPLICAS, world))
+    reps = [reps_all[i] for i in idx]
+    eng = GrowthEngine(seed=args.seed, replicas=len(reps), device=local)
+    eng.load_replicas(reps)
+    tuned, tune_ms = eng.autotune(ENS_EPOCHS)
+    eng.checkpoint()
+
+    def step():
+        eng.restore()
+        return eng.run_epochs(ENS_EPOCHS, use_graph=True)
+
+    for _ in range(args.warmup):
+        step()
+    barrier(dist)
+    edges, dev_ms, wall = 0, 0.0, 0.0
+    launches = 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            eng.restore()
+            t0 = time.perf_counter()
+            edges += eng.run_epochs(ENS_EPOCHS, use_graph=True)
+            wall += time.perf_counter() - t0
+            st = eng.stats()
+            dev_ms += st["ms_total"]
+            launches += st["run_kernel_launches"]
+    barrier(dist)
+    dev_ms_max = reduce_max(dist, dev_ms)
+    wall_max = reduce_max(dist, wall)
+    evals = reduce_sum(dist, float(len(reps) * args.steps))
+    edges_all = reduce_sum(dist, float(edges))
+    eng.close()
+
+    # serial: the plain per-replica method, one context and one 10-epoch graph run per replica
+    ser_dev_ms, ser_wall = 0.0, 0.0
+    ser_steps = max(1, min(args.steps, 2))
+    engines = []
+    for i, ri in zip(idx, reps):
+        e1 = GrowthEngine(seed=args.seed, device=local, replica_base=i)
+        e1.load_replicas([ri])
+        e1.checkpoint()
+        e1.run_epochs(ENS_EPOCHS, use_graph=True)  # warm: capture the graph
+        engines.append(e1)
+    barrier(dist)
+    for _ in range(ser_steps):
+        for e1 in engines:
+            e1.restore()
+            t0 = time.perf_counter()
+            e1.run_epochs(ENS_EPOCHS, use_graph=True)
+            ser_wall += time.perf_counter() - t0
+            ser_dev_ms += e1.stats()["ms_total"]
+    for e1 in engines:
+        e1.close()
+    barrier(dist)
+    ser_wall = reduce_max(dist, ser_wall) / ser_steps
+    ser_dev_ms = reduce_max(dist, ser_dev_ms) / ser_steps
+
+    # end to end: host inputs -> load -> 10 epochs -> every new citation back on the host
+    e2e = None
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        h2d = d2h = 0
+        with GrowthEngine(seed=args.seed, replicas=len(reps), device=local) as e2:
+            e2.set_tuning(**tuned)
+            e2.load_replicas(reps)
+            m0 = [e2.counts(r) for r in range(len(reps))]
+            ne = e2.run_epochs(ENS_EPOCHS, use_graph=True)
+            for r in range(len(reps)):
+                n0_, mm0 = m0[r]
+                n1, m1 = e2.counts(r)
+                e2.edges(mm0, m1 - mm0, r)
+                h2d += 4 * n0_ * 3 + 8 * (n0_ + 1) * 2 + 4 * mm0 * 2
+                d2h += 4 * (m1 - mm0) + 8 * (n1 + 1)
+        dt = reduce_max(dist, time.perf_counter() - t0)
+        e2e = {"value": reduce_sum(dist, float(len(reps))) / dt, "unit": "evals/s",
+               "h2d_bytes_per_step": int(reduce_sum(dist, float(h2d))),
+               "d2h_bytes_per_step": int(reduce_sum(dist, float(d2h))),
+               "citations_per_s": reduce_sum(dist, float(ne)) / dt}
+    if rank != 0:
+        return
+    value = evals / (dev_ms_max / 1000.0)
+    line = {
+        "metric": "ensemble evals/sec (replica grown 10 epochs)",
+        "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32/u64/f32", "data": "synthetic",
+        "config": {"workload": ENS_WORKLOAD, "replicas": ENS_REPLICAS, "epochs": ENS_EPOCHS,
+                   "mean_out_degree": 20, "growth": 0.03, "tuning": tuned,
+                   "autotune_best_ms": tune_ms, "parallelism": "replicas only",
+                   "l2": "inputs larger than L2 (all replicas' CSRs, several GB)"},
+        "citations_per_s": edges_all / (dev_ms_max / 1000.0),
+        "wall_evals_per_s": evals / wall_max,
+        "serial": {"device_ms_per_step": ser_dev_ms, "wall_ms_per_step": 1000.0 * ser_wall,
+                   "evals_per_s_device": len(idx) * world / (ser_dev_ms / 1000.0),
+                   "speedup_device": (ser_dev_ms / 1000.0) / (dev_ms_max / 1000.0 / args.steps),
+                   "speedup_wall": ser_wall / (wall_max / args.steps)},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = ensemble_cpu_sample(reps_all, args.seed)
+    print(json.dumps(line), flush=True)
+
+
+def ensemble_cpu_sample(reps, seed: int, budget_s: float = 12.0) -> dict:
+    """The CPU oracle (OpenMP, neighbourhood enumeration) growing replicas of the ensemble for
+    all 10 epochs, in order, until the time budget is spent."""
+    import oracle as O
+
+    threads = os.cpu_count() or 1
+    secs, done = 0.0, 0
+    for r, ri in enumerate(reps):
+        og = O.OracleGraph(seed, r)
+        og.load(ri.pub_epoch, ri.fitness, ri.src, ri.dst)
+        og.set_params(**ri.params.__dict__)
+        og.set_sampler(1)
+        t0 = time.perf_counter()
+        for _ in range(ENS_EPOCHS):
+            og.pa_epoch(threads)
+        secs += time.perf_counter() - t0
+        og.close()
+        done += 1
+        if secs > budget_s:
+            break
+    return {"value": done / secs, "unit": "evals/s", "cores": threads, "kind": "port",
+            "sample": f"first {done} replicas of the ensemble, 10 epochs each ({secs:.1f} s), CPU "
+                      f"oracle with OpenMP, neighbourhood enumeration"}
+
+
 def epoch_report(args) -> None:
     """One JSON line per epoch of the workload: stage times (CUDA events) and byte-model counters.
     Stops early when an epoch exceeds --epoch-cap-s (the enumeration sampler slows down as hubs
@@ -387,7 +533,13 @@ def main():
     ap.add_argument("--report-epochs", type=int, default=EPOCHS)
     ap.add_argument("--epoch-cap-s", type=float, default=10.0)
     ap.add_argument("--profile-case", action="store_true", help="two epochs for ncu, then exit")
+    ap.add_argument("--ensemble", action="store_true",
+                    help="batched ensemble (256 replicas x 10 epochs) against the serial loop")
     args = ap.parse_args()
+    if args.ensemble:
+        if args.warmup < 3:
+            args.warmup = 3
+        return run_ensemble(args)
     if args.epoch_report:
         return epoch_report(args)
     if args.profile_case:

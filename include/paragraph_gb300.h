@@ -7,7 +7,7 @@
  * No C++ exception crosses this boundary and no entry point takes a torch or CUDA type.
  *
  * Reference interfaces replaced (paths are inside the ParAGraph project):
- *   pg_load_graph / pg_load_replica  <- Graph::ParseNodelist / ParseEdgelist / AddEdge and the
+ *   pg_load_graph / pg_load_replicas <- Graph::ParseNodelist / ParseEdgelist / AddEdge and the
  *                                       per-epoch host CSR rebuild prepareGraph
  *                                       (src/graph.cu:336-447, src/graph.cu:820-826,
  *                                        src/utils.cu:75-142)
@@ -64,7 +64,8 @@ typedef struct {
     int32_t weight_model;  /* PG_WEIGHTS_* */
     int32_t record_trace;  /* 1: keep each epoch's arrival-ordered citations for pg_loglik_* */
     int32_t sampler;       /* PG_SAMPLER_* */
-    int32_t reserved;
+    int32_t replica_base;  /* RNG index of replica 0 (replica r draws as replica_base + r), so a
+                              single-replica context can reproduce replica i of a batched one */
 } pg_config;
 
 /* How an agent draws its citations; both give the same law (weighted sampling without
@@ -114,7 +115,7 @@ typedef struct {
     int64_t elems_streamed;    /* neighbourhood elements keyed (with multiplicity) */
     int64_t draws;             /* global-race draws */
     int64_t bwd_moved;         /* old backward-CSR entries moved by the append */
-    int64_t bytes_alg;         /* algorithmic bytes of the epoch (byte model in the design doc) */
+    int64_t bytes_alg;         /* algorithmic bytes of the epoch (per-stage byte model of the engine) */
     int64_t bytes_alg_agents;  /* algorithmic bytes of the agent kernel alone */
     double ms_total;           /* device time of the whole epoch, CUDA events */
     double ms_weights;         /* weights + quantise + CDF scan */
@@ -203,6 +204,22 @@ pg_status pg_timer_stop(pg_ctx* ctx, double* ms);
  * it back, so a run can be repeated or resumed bit-exactly (the RNG is counter-based). */
 pg_status pg_checkpoint(pg_ctx* ctx);
 pg_status pg_restore(pg_ctx* ctx);
+
+/* ---- launch tuning (no counterpart in the reference; results never depend on it) ---- */
+typedef struct {
+    int32_t agent_ctas_per_sm; /* CTAs per SM of the k <= 64 agent kernel; 0 = occupancy limit */
+    int32_t small_hash;        /* 1: 1024-slot frontier hash per warp in that kernel, 0: 2048 */
+    int32_t copy_ctas_per_sm;  /* CTAs per SM of the backward-CSR copy; 0 = default (8) */
+    int32_t reserved;
+} pg_tuning;
+pg_status pg_set_tuning(pg_ctx* ctx, const pg_tuning* tuning);
+pg_status pg_get_tuning(const pg_ctx* ctx, pg_tuning* tuning);
+/* Times every candidate tuning on the next num_epochs epochs of the loaded replicas and keeps the
+ * fastest (written to best, its time in milliseconds to best_ms; either may be NULL).  The graph is
+ * saved before and put back after every candidate, so the context is left exactly as it was; a
+ * checkpoint taken earlier with pg_checkpoint is kept.  Every candidate must produce the same edge
+ * count, else PG_ERR_STATE. */
+pg_status pg_autotune(pg_ctx* ctx, int32_t num_epochs, pg_tuning* best, double* best_ms);
 
 /* ---- allocation-free generation ---- */
 /* Largest delta * ceil(n_existing / 65536) that pg_er_generate_noalloc accepts. */

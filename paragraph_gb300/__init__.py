@@ -38,6 +38,7 @@ EXPORTED = [
     "pg_get_stats", "pg_sync", "pg_check_device", "pg_philox4x32_10", "pg_poisson_table",
     "pg_logf_host", "pg_expf_host", "pg_log_host", "pg_exp_host", "pg_version",
     "pg_timer_start", "pg_timer_stop", "pg_checkpoint", "pg_restore", "pg_er_generate_noalloc",
+    "pg_set_tuning", "pg_get_tuning", "pg_autotune",
 ]
 
 
@@ -50,7 +51,7 @@ class PGError(RuntimeError):
 class _Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("num_replicas", C.c_int32), ("seed", C.c_uint64),
                 ("weight_model", C.c_int32), ("record_trace", C.c_int32), ("sampler", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("replica_base", C.c_int32)]
 
 
 class _Params(C.Structure):
@@ -77,6 +78,11 @@ class _Stats(C.Structure):
         (n, C.c_double) for n in ("run_ms_weights", "run_ms_setup", "run_ms_agents", "run_ms_csr")] + [
         ("run_kernel_launches", C.c_int64), ("adj_scanned", C.c_int64),
         ("run_adj_scanned", C.c_int64)]
+
+
+class _Tuning(C.Structure):
+    _fields_ = [("agent_ctas_per_sm", C.c_int32), ("small_hash", C.c_int32),
+                ("copy_ctas_per_sm", C.c_int32), ("reserved", C.c_int32)]
 
 
 @dataclass
@@ -160,6 +166,9 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_checkpoint": (i32, [vp]),
         "pg_restore": (i32, [vp]),
         "pg_er_generate_noalloc": (i32, [u64, i64, i64, i64, C.c_double, vp, vp, i64, P(i64), vp]),
+        "pg_set_tuning": (i32, [vp, P(_Tuning)]),
+        "pg_get_tuning": (i32, [vp, P(_Tuning)]),
+        "pg_autotune": (i32, [vp, i32, P(_Tuning), P(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -197,10 +206,11 @@ class GrowthEngine:
 
     def __init__(self, seed: int = 42, replicas: int = 1, device: int = 0,
                  record_trace: bool = False, weight_model: int = PG_WEIGHTS_BASELINE,
-                 sampler: int = PG_SAMPLER_THINNING):
+                 sampler: int = PG_SAMPLER_THINNING, replica_base: int = 0):
         self._lib = load_library()
         self._ctx = C.c_void_p()
-        cfg = _Config(device, replicas, seed, weight_model, 1 if record_trace else 0, sampler, 0)
+        cfg = _Config(device, replicas, seed, weight_model, 1 if record_trace else 0, sampler,
+                      replica_base)
         st = self._lib.pg_create(C.byref(self._ctx), C.byref(cfg))
         if st != PG_OK:
             msg = self._lib.pg_last_error(self._ctx).decode() if self._ctx else "pg_create failed"
@@ -357,3 +367,22 @@ class GrowthEngine:
 
     def restore(self) -> None:
         self._check(self._lib.pg_restore(self._ctx))
+
+    def set_tuning(self, agent_ctas_per_sm: int = 0, small_hash: int = 0,
+                   copy_ctas_per_sm: int = 0) -> None:
+        """Launch shape of the agent and backward-copy kernels (results never depend on it)."""
+        t = _Tuning(agent_ctas_per_sm, small_hash, copy_ctas_per_sm, 0)
+        self._check(self._lib.pg_set_tuning(self._ctx, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = _Tuning()
+        self._check(self._lib.pg_get_tuning(self._ctx, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in _Tuning._fields_ if k != "reserved"}
+
+    def autotune(self, epochs: int) -> tuple[dict, float]:
+        """Time the candidate tunings on the next `epochs` epochs, keep the fastest; the graph is
+        left as it was.  Returns (tuning, milliseconds of the best candidate)."""
+        t = _Tuning()
+        ms = C.c_double()
+        self._check(self._lib.pg_autotune(self._ctx, int(epochs), C.byref(t), C.byref(ms)))
+        return {k: getattr(t, k) for k, _ in _Tuning._fields_ if k != "reserved"}, ms.value

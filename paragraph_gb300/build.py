@@ -64,7 +64,7 @@ def build_library(force: bool = False, verbose_ptxas: bool = False) -> Path:
         for s, log in zip(srcs, logs):
             print(f"== {s.name}\n{log}")
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

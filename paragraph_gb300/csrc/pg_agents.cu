@@ -181,7 +181,7 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
     C.bwd_off = A.bwd_off_cur + rp.obase;
     C.bwd_col = A.bwd_col_cur + rp.ebase;
     C.seed = A.seed;
-    C.rep = (uint32_t)r;
+    C.rep = (uint32_t)(r + A.rep_base);
     C.ep = (uint32_t)A.st->epoch;
     C.unit = (uint32_t)al;
     C.beta_m1 = rp.beta_m1;
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
     const Replica& rp = A.rep[r];
     const int64_t al = a - rp.abase;
     const uint32_t ep = (uint32_t)A.st->epoch;
-    const u32x4 x = draw(A.seed, kStreamOutDegree, (uint32_t)r, ep, (uint32_t)al, 0);
+    const u32x4 x = draw(A.seed, kStreamOutDegree, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, 0);
     const int kraw = poisson_draw(A.tables + (int64_t)r * kTableEntries, kTableEntries,
                                   u64of(x.x[0], x.x[1]));
     int64_t k = kraw < 1 ? 1 : kraw;
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
     }
     const int64_t slot = rp.nbase + rp.n + al;
     A.pub[slot] = (int32_t)A.st->epoch;
-    A.fit[slot] = lognormal_fitness(A.seed, (uint32_t)r, ep, (uint32_t)al);
+    A.fit[slot] = lognormal_fitness(A.seed, (uint32_t)(r + A.rep_base), ep, (uint32_t)al);
     A.indeg[slot] = 0;
 }
 
@@ -408,11 +408,12 @@ __global__ void k_edges_check(Arena A, int64_t agents) {
     }
 }
 
-template <int KCAP, bool BIG, bool THIN>
+template <int KCAP, bool BIG, bool THIN, bool HSMALL = false>
 __global__ void __launch_bounds__(kAgentWarps * 32) k_agents(Arena A, int64_t agents) {
-    // frontier hash capacity: 2048 slots for the common small-k kernel, 1024 for the k <= 256 one
-    // so that four warps stay within 48 KiB of static shared memory
-    constexpr int HCAP = KCAP <= kKSmall ? 2 * kZCap : kZCap;
+    // frontier hash capacity: 2048 slots for the common small-k kernel (1024 in the HSMALL variant,
+    // which fits more CTAs per SM), 1024 for the k <= 256 one so that four warps stay within 48 KiB
+    // of static shared memory
+    constexpr int HCAP = (KCAP <= kKSmall && !HSMALL) ? 2 * kZCap : kZCap;
     using Smem = typename std::conditional<THIN, ThinSmem<KCAP, HCAP>, AgentSmem<KCAP>>::type;
     __shared__ Smem smem[kAgentWarps];
     if (A.st->error) return;
@@ -436,6 +437,7 @@ __global__ void __launch_bounds__(kAgentWarps * 32) k_agents(Arena A, int64_t ag
 }
 
 static int g_blocks[2][2] = {{0, 0}, {0, 0}};  // [thin][big]
+static int g_blocks_hsmall = 0;                 // thinning, k <= 64, 1024-slot frontier
 
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s) {
     if (agents <= 0) return;
@@ -453,22 +455,34 @@ cudaError_t init_agent_kernels() {
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[0][1], k_agents<kKMax, true, false>, th, 0);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[1][0], k_agents<kKSmall, false, true>, th, 0);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[1][1], k_agents<kKMax, true, true>, th, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_hsmall, k_agents<kKSmall, false, true, true>, th, 0);
     for (auto& row : g_blocks)
         for (int& b : row)
             if (b < 1) b = 1;
+    if (g_blocks_hsmall < 1) g_blocks_hsmall = 1;
     return e;
+}
+
+int agent_occupancy(int thin, int small_hash) {
+    return thin ? (small_hash ? g_blocks_hsmall : g_blocks[1][0]) : g_blocks[0][0];
 }
 
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) {
     if (agents <= 0) return;
     const int t = A.sampler == kSamplerThinning ? 1 : 0;
+    const bool hs = t && A.tune_small_hash;
+    int per_sm = t ? (hs ? g_blocks_hsmall : g_blocks[1][0]) : g_blocks[0][0];
+    if (A.tune_agent_ctas > 0 && A.tune_agent_ctas < per_sm) per_sm = A.tune_agent_ctas;
     int64_t need = (agents + kAgentWarps - 1) / kAgentWarps;
-    int64_t grid = (int64_t)num_sms * g_blocks[t][0];
+    int64_t grid = (int64_t)num_sms * per_sm;
     if (grid > need) grid = need;
     const unsigned gbig = (unsigned)num_sms * g_blocks[t][1];
     const int th = kAgentWarps * 32;
     if (t) {
-        k_agents<kKSmall, false, true><<<(unsigned)grid, th, 0, s>>>(A, agents);
+        if (hs)
+            k_agents<kKSmall, false, true, true><<<(unsigned)grid, th, 0, s>>>(A, agents);
+        else
+            k_agents<kKSmall, false, true><<<(unsigned)grid, th, 0, s>>>(A, agents);
         k_agents<kKMax, true, true><<<gbig, th, 0, s>>>(A, agents);
     } else {
         k_agents<kKSmall, false, false><<<(unsigned)grid, th, 0, s>>>(A, agents);

@@ -8,11 +8,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/paragraph_gb300.h"
@@ -88,6 +90,7 @@ struct pg_ctx {
     int64_t g_epoch0 = -1;
     int g_parity0 = -1, g_epochs = 0;
     Checkpoint ckpt;
+    pg_tuning tune{};
     std::string err;
 };
 
@@ -182,6 +185,10 @@ Arena make_arena(pg_ctx* c) {
     A.hub2 = c->hub2.p;
     A.hlist = c->hlist.p;
     A.sampler = c->cfg.sampler;
+    A.tune_agent_ctas = c->tune.agent_ctas_per_sm;
+    A.tune_small_hash = c->tune.small_hash;
+    A.tune_copy_ctas = c->tune.copy_ctas_per_sm;
+    A.rep_base = c->cfg.replica_base;
     return A;
 }
 
@@ -256,6 +263,18 @@ void host_transpose(int64_t n, const std::vector<int64_t>& fo, const std::vector
     for (int64_t v = 0; v < n; ++v)
         for (int64_t i = fo[(size_t)v]; i < fo[(size_t)v + 1]; ++i)
             bc[(size_t)cur[(size_t)fc[(size_t)i]]++] = (int32_t)v;
+}
+
+void free_checkpoint(Checkpoint& k) {
+    dfree(k.pub);
+    dfree(k.indeg);
+    dfree(k.fwd_col);
+    dfree(k.bwd_col);
+    dfree(k.fit);
+    dfree(k.fwd_off);
+    dfree(k.bwd_off);
+    dfree(k.rep);
+    k.valid = false;
 }
 
 void destroy_graph_exec(pg_ctx* c) {
@@ -628,7 +647,7 @@ pg_status pg_default_params(pg_pa_params* out) {
 pg_status pg_create(pg_ctx** out, const pg_config* cfg) {
     if (!out || !cfg) return PG_ERR_ARG;
     *out = nullptr;
-    if (cfg->num_replicas < 1) return PG_ERR_ARG;
+    if (cfg->num_replicas < 1 || cfg->replica_base < 0) return PG_ERR_ARG;
     pg_ctx* c = new (std::nothrow) pg_ctx();
     if (!c) return PG_ERR_CAPACITY;
     c->cfg = *cfg;
@@ -658,17 +677,15 @@ void pg_destroy(pg_ctx* c) {
     destroy_graph_exec(c);
     DBuf<int32_t>* i32[] = {&c->tile_rep, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list,
                             &c->e_dst, &c->e_rank, &c->arrivals, &c->fwd_col, &c->bwd_col[0],
-                            &c->bwd_col[1], &c->ckpt.pub, &c->ckpt.indeg, &c->ckpt.fwd_col,
-                            &c->ckpt.bwd_col};
+                            &c->bwd_col[1]};
     for (auto* b : i32) dfree(*b);
     DBuf<int64_t>* i64[] = {&c->fwd_off, &c->bwd_off[0], &c->bwd_off[1], &c->len_tmp,
                             &c->sort_small, &c->sort_large, &c->sort_large_off, &c->eoff,
-                            &c->blocksum, &c->er_cnt, &c->er_toff, &c->ckpt.fwd_off,
-                            &c->ckpt.bwd_off};
+                            &c->blocksum, &c->er_cnt, &c->er_toff};
     for (auto* b : i64) dfree(*b);
+    free_checkpoint(c->ckpt);
     dfree(c->fit);
     dfree(c->w);
-    dfree(c->ckpt.fit);
     dfree(c->cdf);
     dfree(c->tilesum);
     dfree(c->tileoff);
@@ -678,7 +695,6 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->hmask);
     dfree(c->hub2);
     dfree(c->rep);
-    dfree(c->ckpt.rep);
     dfree(c->st);
     for (int i = 0; i < 6; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
@@ -708,13 +724,32 @@ pg_status pg_load_replicas(pg_ctx* c, const pg_replica_desc* descs, int32_t num)
         for (int64_t e = 0; e < d.num_edges; ++e)
             if (d.src[e] < 0 || d.src[e] >= d.num_nodes || d.dst[e] < 0 || d.dst[e] >= d.num_nodes)
                 return fail(c, PG_ERR_ARG, "edge endpoint out of range at index " + std::to_string(e));
-        HostGraph& g = hg[(size_t)r];
-        host_csr(d.num_nodes, d.num_edges, d.src, d.dst, g.fo, g.fc);
-        host_transpose(d.num_nodes, g.fo, g.fc, g.bo, g.bc);
-        g.pub.assign(d.pub_epoch, d.pub_epoch + d.num_nodes);
-        g.fit.assign(d.fitness, d.fitness + d.num_nodes);
-        g.indeg.resize((size_t)d.num_nodes);
-        for (int64_t v = 0; v < d.num_nodes; ++v) g.indeg[(size_t)v] = (int32_t)(g.bo[(size_t)v + 1] - g.bo[(size_t)v]);
+    }
+    // host CSRs of the replicas, built on all host threads (replicas are independent)
+    {
+        std::atomic<int> next{0};
+        auto worker = [&]() {
+            for (int r = next++; r < num; r = next++) {
+                const pg_replica_desc& d = descs[r];
+                HostGraph& g = hg[(size_t)r];
+                host_csr(d.num_nodes, d.num_edges, d.src, d.dst, g.fo, g.fc);
+                host_transpose(d.num_nodes, g.fo, g.fc, g.bo, g.bc);
+                g.pub.assign(d.pub_epoch, d.pub_epoch + d.num_nodes);
+                g.fit.assign(d.fitness, d.fitness + d.num_nodes);
+                g.indeg.resize((size_t)d.num_nodes);
+                for (int64_t v = 0; v < d.num_nodes; ++v)
+                    g.indeg[(size_t)v] = (int32_t)(g.bo[(size_t)v + 1] - g.bo[(size_t)v]);
+            }
+        };
+        const int nt = std::max(1, std::min<int>(num, (int)std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+        worker();
+        for (auto& th : pool) th.join();
+    }
+    for (int r = 0; r < num; ++r) {
+        const pg_replica_desc& d = descs[r];
+        const HostGraph& g = hg[(size_t)r];
         HostRep& h = reps[(size_t)r];
         h.prm = d.params;
         h.n = d.num_nodes;
@@ -831,20 +866,20 @@ pg_status pg_grow_epoch(pg_ctx* c, int64_t* new_nodes, int64_t* new_edges) {
     return PG_OK;
 }
 
-pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_t* new_edges) {
-    if (!c) return PG_ERR_ARG;
-    if (num_epochs < 1) return fail(c, PG_ERR_ARG, "num_epochs must be >= 1");
-    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
-    if (c->poisoned) return fail(c, PG_ERR_STATE, "an earlier epoch failed on the device; reload the graph");
-    PG_CUDA(c, cudaSetDevice(c->device));
-    // plan every epoch on the host mirror; capacities must hold the whole run
-    std::vector<HostRep> saved = c->hrep;
-    std::vector<int64_t> agents((size_t)num_epochs);
-    int64_t max_agents = 0, max_edges = 0;
+namespace {
+
+// Plans num_epochs PA epochs on the host mirror (agents per epoch, largest agent and edge counts)
+// and makes sure the arena and per-epoch buffers hold the whole run: a single-replica arena grows,
+// a multi-replica one must already be large enough.
+pg_status plan_run(pg_ctx* c, int num_epochs, std::vector<int64_t>& agents, int64_t& max_agents,
+                   int64_t& max_edges) {
+    std::vector<HostRep> planned = c->hrep;
+    agents.assign((size_t)num_epochs, 0);
+    max_agents = max_edges = 0;
     for (int e = 0; e < num_epochs; ++e) {
         int64_t tot = 0, eb = 0;
         for (int r = 0; r < c->R; ++r) {
-            HostRep& h = c->hrep[(size_t)r];
+            HostRep& h = planned[(size_t)r];
             const int64_t d = delta_of(h.prm, h.n);
             const int64_t b = edge_bound(d, h.prm.mean_out_degree, h.n);
             tot += d;
@@ -856,17 +891,28 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
         max_agents = std::max(max_agents, tot);
         max_edges = std::max(max_edges, eb);
     }
-    std::vector<HostRep> planned = c->hrep;
-    c->hrep = saved;
     if (c->R == 1) {
-        pg_status s = ensure_capacity(c, planned[0].n, planned[0].m);
+        const pg_status s = ensure_capacity(c, planned[0].n, planned[0].m);
         if (s != PG_OK) return s;
     } else {
         for (int r = 0; r < c->R; ++r)
             if (planned[(size_t)r].n > c->hrep[(size_t)r].n_cap || planned[(size_t)r].m > c->hrep[(size_t)r].m_cap)
                 return fail(c, PG_ERR_CAPACITY, "run exceeds the planned capacity of replica " + std::to_string(r));
     }
-    pg_status s = alloc_epoch_buffers(c, max_agents, max_edges, 0);
+    return alloc_epoch_buffers(c, max_agents, max_edges, 0);
+}
+
+}  // namespace
+
+pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_t* new_edges) {
+    if (!c) return PG_ERR_ARG;
+    if (num_epochs < 1) return fail(c, PG_ERR_ARG, "num_epochs must be >= 1");
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (c->poisoned) return fail(c, PG_ERR_STATE, "an earlier epoch failed on the device; reload the graph");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    std::vector<int64_t> agents;
+    int64_t max_agents = 0, max_edges = 0;
+    pg_status s = plan_run(c, num_epochs, agents, max_agents, max_edges);
     if (s != PG_OK) return s;
     const int64_t e0 = c->epoch;
     const int p0 = c->parity;
@@ -1224,6 +1270,111 @@ pg_status pg_restore(pg_ctx* c) {
     c->hrep = k.hrep;
     c->poisoned = false;
     return PG_OK;
+}
+
+pg_status pg_set_tuning(pg_ctx* c, const pg_tuning* t) {
+    if (!c) return PG_ERR_ARG;
+    if (!t || t->agent_ctas_per_sm < 0 || t->agent_ctas_per_sm > 32 || t->copy_ctas_per_sm < 0 ||
+        t->copy_ctas_per_sm > 64 || (t->small_hash != 0 && t->small_hash != 1))
+        return fail(c, PG_ERR_ARG, "tuning out of range");
+    if (std::memcmp(&c->tune, t, sizeof(pg_tuning)) != 0) {
+        c->tune = *t;
+        c->tune.reserved = 0;
+        destroy_graph_exec(c);  // captured launches carry the old grid sizes
+    }
+    return PG_OK;
+}
+
+pg_status pg_get_tuning(const pg_ctx* c, pg_tuning* t) {
+    if (!c || !t) return PG_ERR_ARG;
+    *t = c->tune;
+    return PG_OK;
+}
+
+// Coordinate search: agent-kernel shape (frontier hash capacity x CTAs per SM) first, then the
+// backward-copy grid.  Each candidate runs the same epochs from the same saved state twice, as a
+// captured graph (the second run, a replay, is the one timed).
+pg_status pg_autotune(pg_ctx* c, int32_t num_epochs, pg_tuning* best, double* best_ms) {
+    if (!c) return PG_ERR_ARG;
+    if (num_epochs < 1) return fail(c, PG_ERR_ARG, "num_epochs must be >= 1");
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (c->poisoned) return fail(c, PG_ERR_STATE, "an earlier epoch failed on the device; reload the graph");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    {
+        // size the arena for the run first: a single-replica arena that grew afterwards would no
+        // longer match the saved state
+        std::vector<int64_t> agents;
+        int64_t ma = 0, me = 0;
+        const pg_status ps = plan_run(c, num_epochs, agents, ma, me);
+        if (ps != PG_OK) return ps;
+    }
+    Checkpoint user = c->ckpt;  // the caller's checkpoint stays aside, untouched
+    c->ckpt = Checkpoint{};
+    const pg_tuning start = c->tune;
+    pg_status s = PG_OK;
+    int64_t ref_edges = -1;
+    double best_t = 1e300;
+    pg_tuning best_cfg = start;
+    auto trial = [&](const pg_tuning& t) -> pg_status {
+        pg_status ts = pg_set_tuning(c, &t);
+        double ms = 0.0;
+        int64_t e1 = 0, e2 = 0;
+        if (ts == PG_OK) ts = pg_restore(c);
+        if (ts == PG_OK) ts = pg_run_epochs(c, num_epochs, 1, &e1);
+        if (ts == PG_OK) ts = pg_restore(c);
+        if (ts == PG_OK) ts = pg_timer_start(c);
+        if (ts == PG_OK) ts = pg_run_epochs(c, num_epochs, 1, &e2);
+        if (ts == PG_OK) ts = pg_timer_stop(c, &ms);
+        if (ts != PG_OK) return ts;
+        if (ref_edges < 0) ref_edges = e1;
+        if (e1 != ref_edges || e2 != ref_edges)
+            return fail(c, PG_ERR_STATE, "tuning candidates disagree on the edge count");
+        if (ms < best_t) {
+            best_t = ms;
+            best_cfg = c->tune;
+        }
+        return PG_OK;
+    };
+    s = pg_checkpoint(c);
+    const int thin = c->cfg.sampler == PG_SAMPLER_THINNING ? 1 : 0;
+    for (int hs = 0; hs <= thin && s == PG_OK; ++hs) {
+        const int occ = agent_occupancy(thin, hs);
+        std::vector<int> vals;
+        for (int v : {0, std::max(1, (occ * 3) / 4), std::max(1, occ / 2)}) {
+            if (v >= occ) v = 0;
+            if (std::find(vals.begin(), vals.end(), v) == vals.end()) vals.push_back(v);
+        }
+        for (int v : vals) {
+            if (s != PG_OK) break;
+            pg_tuning t = start;
+            t.agent_ctas_per_sm = v;
+            t.small_hash = hs;
+            s = trial(t);
+        }
+    }
+    const int copies[3] = {4, 8, 16};
+    const pg_tuning agent_best = best_cfg;
+    for (int i = 0; i < 3 && s == PG_OK; ++i) {
+        pg_tuning t = agent_best;
+        t.copy_ctas_per_sm = copies[i];
+        if (t.copy_ctas_per_sm == (agent_best.copy_ctas_per_sm ? agent_best.copy_ctas_per_sm : 8)) continue;
+        s = trial(t);
+    }
+    // leave the graph as it was and the best tuning in force
+    if (c->ckpt.valid) {
+        const pg_status rs = pg_restore(c);
+        if (s == PG_OK) s = rs;
+    }
+    free_checkpoint(c->ckpt);
+    c->ckpt = user;
+    if (s != PG_OK) {
+        pg_set_tuning(c, &start);
+        return s;
+    }
+    s = pg_set_tuning(c, &best_cfg);
+    if (best) *best = best_cfg;
+    if (best_ms) *best_ms = best_t;
+    return s;
 }
 
 void pg_philox4x32_10(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]) {

@@ -297,7 +297,8 @@ void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t
     k_bwd_len<<<A.ntiles, kTileThreads, 0, s>>>(A);
     launch_tile_scan(A, 1, s);
     k_bwd_off<<<A.ntiles, kTileThreads, 0, s>>>(A);
-    k_bwd_copy<<<(unsigned)num_sms * 8, 256, 0, s>>>(A);
+    const int copy_per_sm = A.tune_copy_ctas > 0 ? A.tune_copy_ctas : 8;
+    k_bwd_copy<<<(unsigned)(num_sms * copy_per_sm), 256, 0, s>>>(A);
     int64_t ga = (agents + 7) / 8;
     if (ga > (int64_t)num_sms * 16) ga = (int64_t)num_sms * 16;
     if (ga < 1) ga = 1;

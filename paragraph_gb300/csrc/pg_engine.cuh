@@ -148,6 +148,11 @@ struct Arena {
     uint64_t seed;
     int32_t record_trace;
     int32_t sampler;
+    // launch tuning (results do not depend on it)
+    int32_t tune_agent_ctas;   // agent-kernel CTAs per SM, 0 = occupancy limit
+    int32_t tune_small_hash;   // 1: 1024-slot frontier hash in the k <= 64 kernel, 0: 2048
+    int32_t tune_copy_ctas;    // backward-copy CTAs per SM
+    int32_t rep_base;          // RNG replica index of replica 0 (pg_config.replica_base)
 };
 
 // ---------------------------------------------------------------- warp helpers
@@ -228,6 +233,8 @@ void launch_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_t*
                             cudaStream_t s);
 int scan_blocks_needed(int64_t n);
 cudaError_t init_agent_kernels();
+// resident CTAs per SM of the k <= 64 agent kernel (after init_agent_kernels)
+int agent_occupancy(int thin, int small_hash);
 cudaError_t init_csr_kernels();
 
 }  // namespace pg

@@ -149,7 +149,7 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     const Replica& rp = A.rep[r];
     const int64_t n = rp.n;
     const int64_t al = a - rp.abase;
-    const uint32_t ep = (uint32_t)A.st->epoch, unit = (uint32_t)al, rep = (uint32_t)r;
+    const uint32_t ep = (uint32_t)A.st->epoch, unit = (uint32_t)al, rep = (uint32_t)(r + A.rep_base);
     const uint64_t* cdf = A.cdf + rp.nbase;
     Ball B;
     B.fo = A.fwd_off + rp.obase;

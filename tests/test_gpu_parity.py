@@ -152,3 +152,57 @@ def test_checkpoint_restore_regrows_identically(gpu):
         st = eng.stats()
         assert st["run_epochs"] == 8 and st["run_new_edges"] == e2
         assert st["run_kernel_launches"] == 8 * (20 + 5)  # thinning adds the hub index
+
+
+def test_tuning_never_changes_results(gpu):
+    """Every launch shape the tuner may pick gives the same graph, and autotune leaves the graph
+    exactly as it found it."""
+    reps = W.ensemble_inputs(replicas=6, lo=2000, hi=20000, epochs=4, seed=21)
+    tunings = [dict(), dict(agent_ctas_per_sm=2), dict(small_hash=1),
+               dict(small_hash=1, agent_ctas_per_sm=3, copy_ctas_per_sm=4),
+               dict(copy_ctas_per_sm=16)]
+    ref = None
+    with GrowthEngine(seed=31, replicas=len(reps)) as eng:
+        eng.load_replicas(reps)
+        eng.checkpoint()
+        for t in tunings:
+            eng.restore()
+            eng.set_tuning(**t)
+            eng.run_epochs(4, use_graph=True)
+            got = [eng.csr(w, r) for r in range(len(reps)) for w in (0, 1)]
+            if ref is None:
+                ref = got
+                continue
+            for (o1, c1), (o2, c2) in zip(ref, got):
+                np.testing.assert_array_equal(o1, o2)
+                np.testing.assert_array_equal(c1, c2)
+        eng.restore()
+        before = [eng.csr(0, r) for r in range(len(reps))]
+        best, ms = eng.autotune(2)
+        assert ms > 0 and best["small_hash"] in (0, 1)
+        assert eng.tuning() == best
+        for r, (o1, c1) in enumerate(before):
+            o2, c2 = eng.csr(0, r)
+            np.testing.assert_array_equal(o1, o2)
+            np.testing.assert_array_equal(c1, c2)
+        # the caller's checkpoint survives the tuner
+        eng.run_epochs(4, use_graph=True)
+        eng.restore()
+        for r, (o1, c1) in enumerate(before):
+            np.testing.assert_array_equal(eng.csr(0, r)[1], c1)
+
+
+def test_single_replica_context_reproduces_batched_replica(gpu):
+    """replica_base lets a one-replica context draw as replica i of a batched one, so the serial
+    loop and the batched ensemble grow identical graphs."""
+    reps = W.ensemble_inputs(replicas=4, lo=1000, hi=8000, epochs=3, seed=5)
+    with GrowthEngine(seed=13, replicas=len(reps)) as batched:
+        batched.load_replicas(reps)
+        batched.run_epochs(3, use_graph=True)
+        for i, ri in enumerate(reps):
+            with GrowthEngine(seed=13, replica_base=i) as one:
+                one.load_replicas([ri])
+                one.run_epochs(3, use_graph=True)
+                for w in (0, 1):
+                    for x, y in zip(batched.csr(w, i), one.csr(w, 0)):
+                        np.testing.assert_array_equal(x, y)
