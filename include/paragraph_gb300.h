@@ -141,6 +141,13 @@ typedef struct {
     int64_t run_kernel_launches; /* kernels the run enqueued (graph nodes when captured) */
     int64_t adj_scanned;       /* adjacency entries examined by ball-membership tests (thinning) */
     int64_t run_adj_scanned;
+    /* last pg_loglik_fwd: ball elements summed over agents, adjacency entries read to build the
+     * balls, citations; device milliseconds of the last pg_loglik_fwd and pg_loglik_bwd calls */
+    int64_t lik_ball_elems;
+    int64_t lik_adj_entries;
+    int64_t lik_citations;
+    double lik_ms_fwd;
+    double lik_ms_bwd;
 } pg_stats;
 
 /* ---- lifecycle ---- */
@@ -186,6 +193,9 @@ pg_status pg_copy_csr(pg_ctx* ctx, int32_t replica, int32_t which, int64_t* off,
 /* Citations of the last epoch in arrival order ([count] as from pg_epoch_edges); needs
  * record_trace. */
 pg_status pg_copy_arrivals(pg_ctx* ctx, int32_t replica, int32_t* cited);
+/* Anchors of the last PA epoch's agents, [new_nodes][4] with unused slots -1; needs record_trace.
+ * (The reference draws one generator node per paper, getGeneratorNode, src/abm.cu:567-574.) */
+pg_status pg_copy_anchors(pg_ctx* ctx, int32_t replica, int32_t* anchors);
 
 /* ---- measurement ---- */
 /* enable != 0 records CUDA events around every kernel group of each epoch (default on). */
@@ -220,6 +230,41 @@ pg_status pg_get_tuning(const pg_ctx* ctx, pg_tuning* tuning);
  * checkpoint taken earlier with pg_checkpoint is kept.  Every candidate must produce the same edge
  * count, else PG_ERR_STATE. */
 pg_status pg_autotune(pg_ctx* ctx, int32_t num_epochs, pg_tuning* best, double* best_ms);
+
+/* ---- log-likelihood of a growth trace and its adjoint (no counterpart in the reference) ----
+ * A trace is a seed graph followed by epochs of agents; agent a (node epoch_nodes[0] + a, in the
+ * epoch whose node range holds it) drew its citations c_1..c_k in the recorded order by
+ * successive sampling without replacement over the nodes j < n_e that existed when the epoch
+ * began, with weights
+ *   W_j = fitness_j^gamma (indeg_e(j)+1)^alpha exp(-(t_e - t_j)/tau) beta^[j in N_a],
+ * indeg_e the in-degree in the epoch-start graph and N_a the undirected 2-hop ball of the agent's
+ * anchors in that graph.  log L(theta) = sum_a sum_i [log W_{c_i} - log(Z_a - sum_{l<i} W_{c_l})],
+ * Z_a = sum_{j < n_e} W_j, theta = (alpha, tau, gamma, beta).  Weights are fp32; Z_a, the prefix
+ * sums and the log-sums are FP64. */
+typedef struct {
+    int64_t num_nodes;          /* nodes at the end of the trace */
+    const int32_t* pub_epoch;   /* [num_nodes] */
+    const float* fitness;       /* [num_nodes] > 0 */
+    int64_t num_seed_edges;     /* edges among the seed nodes (set semantics) */
+    const int32_t* seed_src;
+    const int32_t* seed_dst;
+    int32_t num_epochs;
+    int32_t num_anchors;        /* anchors per agent, 1..PG_MAX_ANCHORS */
+    const int64_t* epoch_nodes; /* [num_epochs + 1] nodes when each epoch began; last = num_nodes */
+    const int32_t* epoch_t;     /* [num_epochs] epoch index t_e (recency origin) */
+    const int32_t* anchors;     /* [agents][4], unused slots -1 */
+    const int64_t* cite_off;    /* [agents + 1], at most PG_MAX_OUT_DEGREE citations per agent */
+    const int32_t* cites;       /* citations of every agent in draw order */
+} pg_trace_desc;
+/* Copies the trace to the device (a trace and the growth state coexist in one context). */
+pg_status pg_trace_load(pg_ctx* ctx, const pg_trace_desc* trace);
+/* log L at each of batch points theta[b] = (alpha, tau, gamma, beta) (row-major [batch][4]).  Saves
+ * the per-agent normalisers Z_a for pg_loglik_bwd. */
+pg_status pg_loglik_fwd(pg_ctx* ctx, int32_t batch, const double* theta, double* loglik);
+/* Adjoint: grad[b][k] = dloglik[b] * d log L / d theta_k at the points of the last pg_loglik_fwd
+ * (theta must be the same; dloglik NULL means all ones).  Weights are recomputed, not stored. */
+pg_status pg_loglik_bwd(pg_ctx* ctx, int32_t batch, const double* theta, const double* dloglik,
+                        double* grad);
 
 /* ---- allocation-free generation ---- */
 /* Largest delta * ceil(n_existing / 65536) that pg_er_generate_noalloc accepts. */

@@ -17,6 +17,14 @@ LIB = _DIR / "_build" / "liboracle.so"
 _lib = None
 
 
+class _Trace(C.Structure):
+    _fields_ = [("num_nodes", C.c_int64), ("pub", C.c_void_p), ("fitness", C.c_void_p),
+                ("num_seed_edges", C.c_int64), ("seed_src", C.c_void_p), ("seed_dst", C.c_void_p),
+                ("num_epochs", C.c_int32), ("num_anchors", C.c_int32), ("epoch_nodes", C.c_void_p),
+                ("epoch_t", C.c_void_p), ("anchors", C.c_void_p), ("cite_off", C.c_void_p),
+                ("cites", C.c_void_p)]
+
+
 def _load() -> C.CDLL:
     global _lib
     if _lib is not None:
@@ -57,6 +65,8 @@ def _load() -> C.CDLL:
         "og_copy_arrivals": (None, [vp, vp]),
         "og_stats": (None, [vp, vp]),
         "og_copy_weights": (i64, [vp, vp, vp, C.POINTER(i32)]),
+        "og_agent_anchors": (None, [u64, u32, u32, i64, i64, i32, vp]),
+        "og_loglik": (i32, [C.POINTER(_Trace), i32, vp, vp, vp, i32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -212,3 +222,81 @@ class OracleGraph:
         sh = C.c_int32()
         self._lib.og_copy_weights(self._g, _p(w), _p(cdf), C.byref(sh))
         return w, cdf, sh.value
+
+
+# ---------------------------------------------------------------- growth traces and their likelihood
+class Trace:
+    """A growth trace: seed graph, then epochs of agents (agent a is node epoch_nodes[0] + a) with
+    anchors ([agents, 4], -1 unused) and citations in draw order (cites[cite_off[a]:cite_off[a+1]])."""
+
+    FIELDS = ("pub", "fitness", "seed_src", "seed_dst", "epoch_nodes", "epoch_t", "anchors",
+              "cite_off", "cites")
+    DTYPES = (np.int32, np.float32, np.int32, np.int32, np.int64, np.int32, np.int32, np.int64,
+              np.int32)
+
+    def __init__(self, num_anchors: int, **arrays):
+        self.num_anchors = int(num_anchors)
+        for f, dt in zip(self.FIELDS, self.DTYPES):
+            setattr(self, f, np.ascontiguousarray(arrays[f], dt))
+
+    @property
+    def num_nodes(self) -> int:
+        return len(self.pub)
+
+    @property
+    def num_epochs(self) -> int:
+        return len(self.epoch_t)
+
+    @property
+    def agents(self) -> int:
+        return len(self.cite_off) - 1
+
+
+def agent_anchors(seed: int, replica: int, epoch: int, n: int, agents: int, num_anchors: int):
+    out = np.empty((agents, 4), np.int32)
+    _load().og_agent_anchors(seed, replica, epoch & 0xFFFFFFFF, n, agents, num_anchors, _p(out))
+    return out
+
+
+def grow_trace(g, params, epochs: int, seed: int, sampler: int = 0, replica: int = 0,
+               threads: int = 0) -> Trace:
+    """Grow `epochs` PA epochs on the CPU from seed graph g and record the trace."""
+    og = OracleGraph(seed, replica)
+    og.load(g.pub, g.fitness, g.src, g.dst)
+    og.set_params(**params.__dict__)
+    og.set_sampler(sampler)
+    ep_nodes, ep_t, anchors, cites, counts = [og.n], [], [], [], []
+    for _ in range(epochs):
+        n_e, t = og.n, og._lib.og_epoch(og._g)
+        og.pa_epoch(threads)
+        d = og.n - n_e
+        ep_t.append(t)
+        anchors.append(agent_anchors(seed, replica, t, n_e, d, params.num_anchors))
+        off, _ = og.csr(0)
+        counts.append(np.diff(off[n_e:n_e + d + 1]))
+        cites.append(og.arrivals())
+        ep_nodes.append(og.n)
+    pub, fit = og.nodes()
+    og.close()
+    cnt = np.concatenate(counts)
+    return Trace(params.num_anchors, pub=pub, fitness=fit, seed_src=g.src, seed_dst=g.dst,
+                 epoch_nodes=np.array(ep_nodes), epoch_t=np.array(ep_t),
+                 anchors=np.concatenate(anchors), cite_off=np.concatenate([[0], np.cumsum(cnt)]),
+                 cites=np.concatenate(cites))
+
+
+def loglik(trace, theta, grad: bool = True, threads: int = 0):
+    """FP64 log-likelihood (and gradient) of a trace at each row (alpha, tau, gamma, beta) of
+    theta.  Returns ll[B] or (ll[B], grad[B, 4])."""
+    th = np.ascontiguousarray(np.atleast_2d(theta), np.float64)
+    B = th.shape[0]
+    ll = np.zeros(B)
+    gr = np.zeros((B, 4)) if grad else None
+    T = _Trace(trace.num_nodes, _p(trace.pub), _p(trace.fitness), len(trace.seed_src),
+               _p(trace.seed_src), _p(trace.seed_dst), trace.num_epochs, trace.num_anchors,
+               _p(trace.epoch_nodes), _p(trace.epoch_t), _p(trace.anchors), _p(trace.cite_off),
+               _p(trace.cites))
+    st = _load().og_loglik(C.byref(T), B, _p(th), _p(ll), _p(gr), threads)
+    if st:
+        raise ValueError(f"og_loglik failed ({st})")
+    return (ll, gr) if grad else ll

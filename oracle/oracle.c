@@ -993,3 +993,214 @@ int64_t og_copy_weights(const og_graph* g, float* w, uint64_t* cdf, int32_t* shi
     if (shift) *shift = g->shift;
     return g->w_n;
 }
+
+/* ------------------------------------------------------------------ anchors of an epoch's agents */
+void og_agent_anchors(uint64_t seed, uint32_t replica, uint32_t epoch, int64_t n, int64_t agents,
+                      int num_anchors, int32_t* out) {
+    for (int64_t a = 0; a < agents; a++) {
+        uint32_t r[4];
+        rng(seed, S_ANCHOR, replica, epoch, (uint32_t)a, 0, r);
+        for (int i = 0; i < 4; i++)
+            out[a * 4 + i] = i < num_anchors ? (int32_t)(((uint64_t)r[i] * (uint64_t)n) >> 32) : -1;
+    }
+}
+
+/* ------------------------------------------------------------------ log-likelihood of a trace
+ *
+ * No counterpart in the reference: the model the samplers above draw from, written as a density.
+ * Agent a of trace epoch e is node n_0 + a; it drew c_1..c_k in this order by successive sampling
+ * without replacement over the nodes j < n_e that existed when the epoch began, with weights
+ *   W_j = f_j^gamma (indeg_e(j)+1)^alpha exp(-(t_e - t_j)/tau) beta^[j in N_a],
+ * indeg_e the in-degree in the epoch-start graph and N_a the undirected 2-hop ball of the agent's
+ * anchors in that graph.  Then
+ *   log L = sum_a sum_i [ log W_{c_i} - log(Z_a - sum_{l<i} W_{c_l}) ],  Z_a = sum_{j<n_e} W_j.
+ * The out-degree and the anchors do not depend on theta = (alpha, tau, gamma, beta).  The gradient
+ * is the direct derivative:  d/dtheta log W_j = g_j = (log(indeg+1), (t_e-t_j)/tau^2, log f_j,
+ * [j in N_a]/beta),  dZ_a = sum_j W_j g_j.  All arithmetic is FP64 with libm exp and log.
+ */
+static int64_t upper_bound64(const int32_t* a, int64_t lo, int64_t hi, int32_t v) {
+    /* first index in [lo, hi) with a[i] > v */
+    while (lo < hi) {
+        int64_t mid = lo + ((hi - lo) >> 1);
+        if (a[mid] <= v)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+int og_loglik(const og_trace* T, int batch, const double* theta, double* ll, double* grad,
+              int threads) {
+    const int64_t n = T->num_nodes;
+    const int E = T->num_epochs;
+    if (n <= 0 || E < 1 || batch < 1) return 3;
+    const int64_t n0 = T->epoch_nodes[0];
+    const int64_t agents = n - n0;
+    if (T->epoch_nodes[E] != n) return 3;
+    const int64_t mc = T->cite_off[agents];
+    /* final graph: seed edges plus every agent's citations */
+    const int64_t m = T->num_seed_edges + mc;
+    int32_t* src = (int32_t*)malloc(sizeof(int32_t) * (size_t)(m > 0 ? m : 1));
+    int32_t* dst = (int32_t*)malloc(sizeof(int32_t) * (size_t)(m > 0 ? m : 1));
+    memcpy(src, T->seed_src, sizeof(int32_t) * (size_t)T->num_seed_edges);
+    memcpy(dst, T->seed_dst, sizeof(int32_t) * (size_t)T->num_seed_edges);
+    for (int64_t a = 0; a < agents; a++)
+        for (int64_t p = T->cite_off[a]; p < T->cite_off[a + 1]; p++) {
+            src[T->num_seed_edges + p] = (int32_t)(n0 + a);
+            dst[T->num_seed_edges + p] = T->cites[p];
+        }
+    int64_t *fo, *bo, mf, mb;
+    int32_t *fc, *bc;
+    build_csr(n, m, src, dst, &fo, &fc, &mf);
+    build_csr(n, m, dst, src, &bo, &bc, &mb);
+    free(src);
+    free(dst);
+    /* theta-independent node features of every epoch */
+    double* lf = (double*)malloc(sizeof(double) * (size_t)n);
+    double* ld = (double*)malloc(sizeof(double) * (size_t)n * (size_t)E);
+    for (int64_t j = 0; j < n; j++) lf[j] = log((double)T->fitness[j]);
+    for (int e = 0; e < E; e++) {
+        const int64_t ne = T->epoch_nodes[e];
+        for (int64_t j = 0; j < ne; j++) {
+            const int64_t d = upper_bound64(bc, bo[j], bo[j + 1], (int32_t)(ne - 1)) - bo[j];
+            ld[(size_t)e * (size_t)n + (size_t)j] = log((double)d + 1.0);
+        }
+    }
+    /* per epoch and theta: Z_glob = sum_j w_j and G_glob = sum_j w_j g_j (alpha, tau, gamma) */
+    double* zg = (double*)calloc((size_t)E * (size_t)batch * 4, sizeof(double));
+    for (int e = 0; e < E; e++) {
+        const int64_t ne = T->epoch_nodes[e];
+        const double te = (double)T->epoch_t[e];
+        for (int b = 0; b < batch; b++) {
+            const double al = theta[b * 4], tau = theta[b * 4 + 1], ga = theta[b * 4 + 2];
+            double z = 0, g0 = 0, g1 = 0, g2 = 0;
+            for (int64_t j = 0; j < ne; j++) {
+                const double dl = ld[(size_t)e * (size_t)n + (size_t)j], dt = te - (double)T->pub[j];
+                const double w = exp(ga * lf[j] + al * dl - dt / tau);
+                z += w;
+                g0 += w * dl;
+                g1 += w * dt;
+                g2 += w * lf[j];
+            }
+            double* o = zg + ((size_t)e * (size_t)batch + (size_t)b) * 4;
+            o[0] = z;
+            o[1] = g0;
+            o[2] = g1 / (tau * tau);
+            o[3] = g2;
+        }
+    }
+    for (int b = 0; b < batch; b++) {
+        ll[b] = 0;
+        if (grad)
+            for (int k = 0; k < 4; k++) grad[b * 4 + k] = 0;
+    }
+    if (threads > 0) omp_set_num_threads(threads);
+    int bad = 0;
+#pragma omp parallel
+    {
+        int32_t* stamp = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+        int32_t* ball = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+        double* acc = (double*)calloc((size_t)batch * 5, sizeof(double));
+        for (int64_t j = 0; j < n; j++) stamp[j] = -1;
+#pragma omp for schedule(dynamic, 32)
+        for (int64_t a = 0; a < agents; a++) {
+            const int64_t v = n0 + a;
+            int e = 0;
+            while (e + 1 < E && T->epoch_nodes[e + 1] <= v) e++;
+            const int64_t ne = T->epoch_nodes[e];
+            const double te = (double)T->epoch_t[e];
+            const double* lde = ld + (size_t)e * (size_t)n;
+            /* the 2-hop ball in the epoch-start graph (rows restricted to nodes j < n_e) */
+            int64_t nb = 0;
+            const int32_t mark = (int32_t)a;
+#define OG_BALL_ADD(x)                       \
+    do {                                     \
+        const int32_t x_ = (x);              \
+        if (stamp[x_] != mark) {             \
+            stamp[x_] = mark;                \
+            ball[nb++] = x_;                 \
+        }                                    \
+    } while (0)
+            for (int i = 0; i < T->num_anchors; i++) {
+                const int32_t x = T->anchors[a * 4 + i];
+                if (x < 0) continue;
+                OG_BALL_ADD(x);
+            }
+            const int64_t n1 = nb;
+            /* 1-hop: neighbours of the anchors */
+            int64_t h1 = nb;
+            for (int64_t q = 0; q < n1; q++) {
+                const int32_t x = ball[q];
+                for (int64_t p = fo[x]; p < fo[x + 1]; p++) OG_BALL_ADD(fc[p]);
+                const int64_t be = upper_bound64(bc, bo[x], bo[x + 1], (int32_t)(ne - 1));
+                for (int64_t p = bo[x]; p < be; p++) OG_BALL_ADD(bc[p]);
+            }
+            h1 = nb;
+            /* 2-hop: neighbours of the 1-hop nodes */
+            for (int64_t q = n1; q < h1; q++) {
+                const int32_t x = ball[q];
+                for (int64_t p = fo[x]; p < fo[x + 1]; p++) OG_BALL_ADD(fc[p]);
+                const int64_t be = upper_bound64(bc, bo[x], bo[x + 1], (int32_t)(ne - 1));
+                for (int64_t p = bo[x]; p < be; p++) OG_BALL_ADD(bc[p]);
+            }
+#undef OG_BALL_ADD
+            const int64_t c0 = T->cite_off[a], c1 = T->cite_off[a + 1];
+            for (int b = 0; b < batch; b++) {
+                const double al = theta[b * 4], tau = theta[b * 4 + 1], ga = theta[b * 4 + 2],
+                             be = theta[b * 4 + 3];
+                const double itau2 = 1.0 / (tau * tau), lbe = log(be);
+                double s = 0, t0 = 0, t1 = 0, t2 = 0;
+                for (int64_t q = 0; q < nb; q++) {
+                    const int32_t j = ball[q];
+                    const double dl = lde[j], dt = te - (double)T->pub[j];
+                    const double w = exp(ga * lf[j] + al * dl - dt / tau);
+                    s += w;
+                    t0 += w * dl;
+                    t1 += w * dt;
+                    t2 += w * lf[j];
+                }
+                const double* gg = zg + ((size_t)e * (size_t)batch + (size_t)b) * 4;
+                const double z = gg[0] + (be - 1.0) * s;
+                const double dz[4] = {gg[1] + (be - 1.0) * t0, gg[2] + (be - 1.0) * t1 * itau2,
+                                      gg[3] + (be - 1.0) * t2, s};
+                double p = 0, dp[4] = {0, 0, 0, 0}, l = 0, gsum[4] = {0, 0, 0, 0};
+                for (int64_t i = c0; i < c1; i++) {
+                    const int32_t c = T->cites[i];
+                    const int in = stamp[c] == mark;
+                    const double dl = lde[c], dt = te - (double)T->pub[c];
+                    const double x = ga * lf[c] + al * dl - dt / tau + (in ? lbe : 0.0);
+                    const double W = exp(x);
+                    const double D = z - p;
+                    if (!(D > 0)) bad = 1;
+                    l += x - log(D);
+                    const double g[4] = {dl, dt * itau2, lf[c], in ? 1.0 / be : 0.0};
+                    for (int k = 0; k < 4; k++) {
+                        gsum[k] += g[k] - (dz[k] - dp[k]) / D;
+                        dp[k] += W * g[k];
+                    }
+                    p += W;
+                }
+                acc[b * 5] += l;
+                for (int k = 0; k < 4; k++) acc[b * 5 + 1 + k] += gsum[k];
+            }
+        }
+#pragma omp critical
+        for (int b = 0; b < batch; b++) {
+            ll[b] += acc[b * 5];
+            if (grad)
+                for (int k = 0; k < 4; k++) grad[b * 4 + k] += acc[b * 5 + 1 + k];
+        }
+        free(stamp);
+        free(ball);
+        free(acc);
+    }
+    free(fo);
+    free(fc);
+    free(bo);
+    free(bc);
+    free(lf);
+    free(ld);
+    free(zg);
+    return bad ? 4 : 0;
+}

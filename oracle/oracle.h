@@ -57,4 +57,31 @@ void og_stats(const og_graph* g, int64_t* out6);
 /* last epoch weights w0 (float, n_pre entries) and CDF (uint64) for unit tests */
 int64_t og_copy_weights(const og_graph* g, float* w, uint64_t* cdf, int32_t* shift);
 
+/* anchors of an epoch's agents: [agents][4], unused slots -1 (uniform over the n existing nodes) */
+void og_agent_anchors(uint64_t seed, uint32_t replica, uint32_t epoch, int64_t n, int64_t agents,
+                      int num_anchors, int32_t* out);
+
+/* A growth trace: the seed graph, then epochs of agents (agent a is node epoch_nodes[0] + a) with
+ * their anchors and their citations in draw order. */
+typedef struct {
+    int64_t num_nodes;          /* nodes at the end of the trace */
+    const int32_t* pub;         /* [num_nodes] publication epoch */
+    const float* fitness;       /* [num_nodes] */
+    int64_t num_seed_edges;
+    const int32_t* seed_src;
+    const int32_t* seed_dst;
+    int32_t num_epochs;
+    int32_t num_anchors;
+    const int64_t* epoch_nodes; /* [num_epochs + 1] nodes when each epoch began; last = num_nodes */
+    const int32_t* epoch_t;     /* [num_epochs] epoch index t of each trace epoch */
+    const int32_t* anchors;     /* [agents][4] */
+    const int64_t* cite_off;    /* [agents + 1] */
+    const int32_t* cites;       /* citations of each agent in draw order */
+} og_trace;
+
+/* FP64 log-likelihood of the trace at each theta[b] = (alpha, tau, gamma, beta); grad ([batch][4])
+ * may be NULL.  Returns 0, or 4 when a normaliser was not positive. */
+int og_loglik(const og_trace* trace, int batch, const double* theta, double* ll, double* grad,
+              int threads);
+
 #endif

@@ -38,7 +38,8 @@ EXPORTED = [
     "pg_get_stats", "pg_sync", "pg_check_device", "pg_philox4x32_10", "pg_poisson_table",
     "pg_logf_host", "pg_expf_host", "pg_log_host", "pg_exp_host", "pg_version",
     "pg_timer_start", "pg_timer_stop", "pg_checkpoint", "pg_restore", "pg_er_generate_noalloc",
-    "pg_set_tuning", "pg_get_tuning", "pg_autotune",
+    "pg_set_tuning", "pg_get_tuning", "pg_autotune", "pg_copy_anchors", "pg_trace_load",
+    "pg_loglik_fwd", "pg_loglik_bwd",
 ]
 
 
@@ -77,12 +78,22 @@ class _Stats(C.Structure):
         "run_draws", "run_bwd_moved", "run_nodes_weighted", "run_bytes_alg", "run_bytes_alg_agents")] + [
         (n, C.c_double) for n in ("run_ms_weights", "run_ms_setup", "run_ms_agents", "run_ms_csr")] + [
         ("run_kernel_launches", C.c_int64), ("adj_scanned", C.c_int64),
-        ("run_adj_scanned", C.c_int64)]
+        ("run_adj_scanned", C.c_int64), ("lik_ball_elems", C.c_int64),
+        ("lik_adj_entries", C.c_int64), ("lik_citations", C.c_int64), ("lik_ms_fwd", C.c_double),
+        ("lik_ms_bwd", C.c_double)]
 
 
 class _Tuning(C.Structure):
     _fields_ = [("agent_ctas_per_sm", C.c_int32), ("small_hash", C.c_int32),
                 ("copy_ctas_per_sm", C.c_int32), ("reserved", C.c_int32)]
+
+
+class _TraceDesc(C.Structure):
+    _fields_ = [("num_nodes", C.c_int64), ("pub_epoch", C.c_void_p), ("fitness", C.c_void_p),
+                ("num_seed_edges", C.c_int64), ("seed_src", C.c_void_p), ("seed_dst", C.c_void_p),
+                ("num_epochs", C.c_int32), ("num_anchors", C.c_int32), ("epoch_nodes", C.c_void_p),
+                ("epoch_t", C.c_void_p), ("anchors", C.c_void_p), ("cite_off", C.c_void_p),
+                ("cites", C.c_void_p)]
 
 
 @dataclass
@@ -112,6 +123,40 @@ class ReplicaInput:
     planned_epochs: int = 1
     node_capacity: int = 0
     edge_capacity: int = 0
+
+
+@dataclass
+class TraceInput:
+    """A growth trace: seed graph, then epochs of agents (agent a is node epoch_nodes[0] + a) with
+    anchors ([agents, 4], unused -1) and citations in draw order (cites[cite_off[a]:cite_off[a+1]])."""
+    pub: np.ndarray
+    fitness: np.ndarray
+    seed_src: np.ndarray
+    seed_dst: np.ndarray
+    epoch_nodes: np.ndarray
+    epoch_t: np.ndarray
+    anchors: np.ndarray
+    cite_off: np.ndarray
+    cites: np.ndarray
+    num_anchors: int = 3
+
+    def __post_init__(self):
+        for f, dt in (("pub", np.int32), ("fitness", np.float32), ("seed_src", np.int32),
+                      ("seed_dst", np.int32), ("epoch_nodes", np.int64), ("epoch_t", np.int32),
+                      ("anchors", np.int32), ("cite_off", np.int64), ("cites", np.int32)):
+            setattr(self, f, np.ascontiguousarray(getattr(self, f), dt))
+
+    @property
+    def num_nodes(self) -> int:
+        return len(self.pub)
+
+    @property
+    def num_epochs(self) -> int:
+        return len(self.epoch_t)
+
+    @property
+    def agents(self) -> int:
+        return len(self.cite_off) - 1
 
 
 _lib = None
@@ -169,6 +214,10 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_set_tuning": (i32, [vp, P(_Tuning)]),
         "pg_get_tuning": (i32, [vp, P(_Tuning)]),
         "pg_autotune": (i32, [vp, i32, P(_Tuning), P(C.c_double)]),
+        "pg_copy_anchors": (i32, [vp, i32, vp]),
+        "pg_trace_load": (i32, [vp, P(_TraceDesc)]),
+        "pg_loglik_fwd": (i32, [vp, i32, vp, vp]),
+        "pg_loglik_bwd": (i32, [vp, i32, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -339,6 +388,14 @@ class GrowthEngine:
         self._check(self._lib.pg_copy_arrivals(self._ctx, replica, _ptr(a)))
         return a[:c]
 
+    def anchors(self, count: int | None = None, replica: int = 0) -> np.ndarray:
+        """Anchors of the last PA epoch's agents, [count, 4] (needs record_trace); count defaults
+        to the epoch's new nodes of a single-replica context."""
+        d = int(self.stats()["new_nodes"]) if count is None else int(count)
+        a = np.empty((max(d, 1), 4), np.int32)
+        self._check(self._lib.pg_copy_anchors(self._ctx, replica, _ptr(a)))
+        return a[:d]
+
     def set_timing(self, enable: bool) -> None:
         self._check(self._lib.pg_set_timing(self._ctx, 1 if enable else 0))
 
@@ -386,3 +443,27 @@ class GrowthEngine:
         ms = C.c_double()
         self._check(self._lib.pg_autotune(self._ctx, int(epochs), C.byref(t), C.byref(ms)))
         return {k: getattr(t, k) for k, _ in _Tuning._fields_ if k != "reserved"}, ms.value
+
+    # ---------------------------------------------------------------- trace log-likelihood
+    def load_trace(self, t: TraceInput) -> None:
+        """Copy a growth trace to the device for loglik / loglik_grad."""
+        self._trace = t  # keeps the arrays alive while the descriptor points at them
+        d = _TraceDesc(t.num_nodes, _ptr(t.pub), _ptr(t.fitness), len(t.seed_src), _ptr(t.seed_src),
+                       _ptr(t.seed_dst), t.num_epochs, t.num_anchors, _ptr(t.epoch_nodes),
+                       _ptr(t.epoch_t), _ptr(t.anchors), _ptr(t.cite_off), _ptr(t.cites))
+        self._check(self._lib.pg_trace_load(self._ctx, C.byref(d)))
+
+    def loglik(self, theta) -> np.ndarray:
+        """log L at each row (alpha, tau, gamma, beta) of theta (forward pass)."""
+        th = np.ascontiguousarray(np.atleast_2d(theta), np.float64)
+        out = np.empty(th.shape[0])
+        self._check(self._lib.pg_loglik_fwd(self._ctx, th.shape[0], _ptr(th), _ptr(out)))
+        return out
+
+    def loglik_grad(self, theta, dloglik=None) -> np.ndarray:
+        """Adjoint pass at the points of the last loglik call: [B, 4] gradient (times dloglik)."""
+        th = np.ascontiguousarray(np.atleast_2d(theta), np.float64)
+        g = np.empty((th.shape[0], 4))
+        dl = None if dloglik is None else np.ascontiguousarray(dloglik, np.float64)
+        self._check(self._lib.pg_loglik_bwd(self._ctx, th.shape[0], _ptr(th), _ptr(dl), _ptr(g)))
+        return g

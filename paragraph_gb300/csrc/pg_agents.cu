@@ -391,6 +391,13 @@ __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
     A.pub[slot] = (int32_t)A.st->epoch;
     A.fit[slot] = lognormal_fitness(A.seed, (uint32_t)(r + A.rep_base), ep, (uint32_t)al);
     A.indeg[slot] = 0;
+    if (A.anchors_out) {
+        // the same draw the agent kernels make for the neighbourhood (recorded for traces)
+        const u32x4 xa = draw(A.seed, kStreamAnchor, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, 0);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            A.anchors_out[a * 4 + i] = i < rp.anchors ? (int32_t)bounded32(xa.x[i], (uint32_t)rp.n) : -1;
+    }
 }
 
 // After the edge-offset scan: totals and capacity checks.

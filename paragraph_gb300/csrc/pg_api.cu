@@ -19,6 +19,7 @@
 
 #include "../../include/paragraph_gb300.h"
 #include "pg_engine.cuh"
+#include "pg_lik.cuh"
 
 using namespace pg;
 
@@ -34,6 +35,21 @@ template <typename T>
 struct DBuf {
     T* p = nullptr;
     int64_t n = 0;
+};
+
+// A loaded growth trace and the buffers of the likelihood passes.
+struct LikState {
+    bool loaded = false;
+    int64_t n = 0, n0 = 0, agents = 0;
+    int epochs = 0, num_anchors = 0, words = 0, chunks = 0, grid = 0;
+    DBuf<int64_t> epoch_nodes, fo, bo, coff;
+    DBuf<int32_t> epoch_t, fc, bc, pub, anchors, cites, agent_epoch;
+    DBuf<float> fit;
+    DBuf<float4> feat;
+    DBuf<double> theta, zglob, gglob, gpart, zagent, out, res;
+    DBuf<uint32_t> err;
+    DBuf<unsigned long long> counters;  // ball elements, adjacency entries, citations
+    std::vector<double> fwd_theta;  // points of the last forward pass
 };
 
 struct Checkpoint {
@@ -65,7 +81,7 @@ struct pg_ctx {
     // device buffers
     DBuf<Replica> rep;
     DBuf<EpochState> st;
-    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, e_dst, e_rank, arrivals, hlist;
+    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, e_dst, e_rank, arrivals, hlist, anchors;
     DBuf<int16_t> hslot;
     DBuf<uint64_t> hub2;
     DBuf<uint64_t> hmask;
@@ -84,12 +100,14 @@ struct pg_ctx {
     cudaEvent_t ev[6] = {};
     std::vector<cudaEvent_t> run_ev;  // 5 per epoch of a pg_run_epochs call
     cudaEvent_t tev[2] = {};          // pg_timer_start / pg_timer_stop
+    cudaEvent_t lev[2] = {};          // around each likelihood pass
     int64_t launches = 0;             // kernels enqueued by the last run
     // CUDA graph of a multi-epoch run
     cudaGraphExec_t gexec = nullptr;
     int64_t g_epoch0 = -1;
     int g_parity0 = -1, g_epochs = 0;
     Checkpoint ckpt;
+    LikState lik;
     pg_tuning tune{};
     std::string err;
 };
@@ -167,6 +185,7 @@ Arena make_arena(pg_ctx* c) {
     A.e_dst = c->e_dst.p;
     A.e_rank = c->e_rank.p;
     A.arrivals = c->cfg.record_trace ? c->arrivals.p : nullptr;
+    A.anchors_out = c->cfg.record_trace ? c->anchors.p : nullptr;
     A.big_list = c->big_list.p;
     A.len_tmp = c->len_tmp.p;
     A.tilesum = c->tilesum.p;
@@ -277,6 +296,21 @@ void free_checkpoint(Checkpoint& k) {
     k.valid = false;
 }
 
+void free_lik(LikState& L) {
+    DBuf<int64_t>* i64[] = {&L.epoch_nodes, &L.fo, &L.bo, &L.coff};
+    for (auto* b : i64) dfree(*b);
+    DBuf<int32_t>* i32[] = {&L.epoch_t, &L.fc, &L.bc, &L.pub, &L.anchors, &L.cites, &L.agent_epoch};
+    for (auto* b : i32) dfree(*b);
+    DBuf<double>* f64[] = {&L.theta, &L.zglob, &L.gglob, &L.gpart, &L.zagent, &L.out, &L.res};
+    for (auto* b : f64) dfree(*b);
+    dfree(L.fit);
+    dfree(L.feat);
+    dfree(L.err);
+    dfree(L.counters);
+    L.loaded = false;
+    L.fwd_theta.clear();
+}
+
 void destroy_graph_exec(pg_ctx* c) {
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     c->gexec = nullptr;
@@ -290,6 +324,7 @@ pg_status alloc_epoch_buffers(pg_ctx* c, int64_t agent_cap, int64_t edge_cap, in
         PG_CUDA(c, dalloc(c->kk, agent_cap));
         PG_CUDA(c, dalloc(c->big_list, agent_cap));
         PG_CUDA(c, dalloc(c->eoff, agent_cap + 1));
+        if (c->cfg.record_trace) PG_CUDA(c, dalloc(c->anchors, 4 * agent_cap));
         c->agent_cap = agent_cap;
     }
     if (edge_cap > c->edge_cap) {
@@ -661,6 +696,7 @@ pg_status pg_create(pg_ctx** out, const pg_config* cfg) {
     if (e == cudaSuccess) e = init_csr_kernels();
     for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->tev[i]);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->lev[i]);
     if (e != cudaSuccess) {
         c->err = std::string("CUDA initialisation failed: ") + cudaGetErrorString(e);
         *out = c;
@@ -676,7 +712,7 @@ void pg_destroy(pg_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     destroy_graph_exec(c);
     DBuf<int32_t>* i32[] = {&c->tile_rep, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list,
-                            &c->e_dst, &c->e_rank, &c->arrivals, &c->fwd_col, &c->bwd_col[0],
+                            &c->e_dst, &c->e_rank, &c->arrivals, &c->anchors, &c->fwd_col, &c->bwd_col[0],
                             &c->bwd_col[1]};
     for (auto* b : i32) dfree(*b);
     DBuf<int64_t>* i64[] = {&c->fwd_off, &c->bwd_off[0], &c->bwd_off[1], &c->len_tmp,
@@ -684,6 +720,7 @@ void pg_destroy(pg_ctx* c) {
                             &c->blocksum, &c->er_cnt, &c->er_toff};
     for (auto* b : i64) dfree(*b);
     free_checkpoint(c->ckpt);
+    free_lik(c->lik);
     dfree(c->fit);
     dfree(c->w);
     dfree(c->cdf);
@@ -698,8 +735,10 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->st);
     for (int i = 0; i < 6; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < 2; ++i) {
         if (c->tev[i]) cudaEventDestroy(c->tev[i]);
+        if (c->lev[i]) cudaEventDestroy(c->lev[i]);
+    }
     for (cudaEvent_t e : c->run_ev) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1163,6 +1202,20 @@ pg_status pg_copy_arrivals(pg_ctx* c, int32_t replica, int32_t* cited) {
     return PG_OK;
 }
 
+pg_status pg_copy_anchors(pg_ctx* c, int32_t replica, int32_t* anchors) {
+    if (!c || !anchors) return PG_ERR_ARG;
+    if (!c->cfg.record_trace) return fail(c, PG_ERR_STATE, "context created without record_trace");
+    if (replica < 0 || replica >= c->R || !c->loaded) return fail(c, PG_ERR_ARG, "bad replica");
+    if (c->h_rep.size() != (size_t)c->R || c->stats.epoch < 0 || c->rep_last_count.empty())
+        return fail(c, PG_ERR_STATE, "no PA epoch has run");
+    const Replica& h = c->h_rep[(size_t)replica];
+    if (h.delta > 0)
+        PG_CUDA(c, cudaMemcpyAsync(anchors, c->anchors.p + 4 * h.abase, 16 * (size_t)h.delta,
+                                   cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
 pg_status pg_set_timing(pg_ctx* c, int32_t enable) {
     if (!c) return PG_ERR_ARG;
     c->timing = enable != 0;
@@ -1394,3 +1447,246 @@ double pg_log_host(double x) { return log_pg(x); }
 double pg_exp_host(double x) { return exp_pg(x); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- trace log-likelihood
+namespace {
+
+template <typename T>
+pg_status upload(pg_ctx* c, DBuf<T>& d, const T* h, int64_t n) {
+    PG_CUDA(c, dalloc(d, n));
+    if (n > 0) PG_CUDA(c, cudaMemcpyAsync(d.p, h, sizeof(T) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    return PG_OK;
+}
+
+LikTrace make_trace(const pg_ctx* c) {
+    const LikState& L = c->lik;
+    LikTrace T{};
+    T.n = L.n;
+    T.agents = L.agents;
+    T.epochs = L.epochs;
+    T.num_anchors = L.num_anchors;
+    T.bitmap_words = L.words;
+    T.chunks = L.chunks;
+    T.epoch_nodes = L.epoch_nodes.p;
+    T.epoch_t = L.epoch_t.p;
+    T.fo = L.fo.p;
+    T.fc = L.fc.p;
+    T.bo = L.bo.p;
+    T.bc = L.bc.p;
+    T.fit = L.fit.p;
+    T.pub = L.pub.p;
+    T.feat = L.feat.p;
+    T.anchors = L.anchors.p;
+    T.coff = L.coff.p;
+    T.cites = L.cites.p;
+    T.agent_epoch = L.agent_epoch.p;
+    return T;
+}
+
+pg_status check_theta(pg_ctx* c, int32_t batch, const double* theta) {
+    if (batch < 1 || !theta) return fail(c, PG_ERR_ARG, "need batch >= 1 parameter points");
+    for (int b = 0; b < batch; ++b) {
+        const double* t = theta + 4 * b;
+        if (!std::isfinite(t[0]) || !std::isfinite(t[2]) || !(t[1] > 0.0) || !std::isfinite(t[1]) ||
+            !(t[3] > 0.0) || !std::isfinite(t[3]))
+            return fail(c, PG_ERR_ARG, "theta " + std::to_string(b) + ": need finite alpha, gamma and tau, beta > 0");
+    }
+    return PG_OK;
+}
+
+// One pass (forward or adjoint) over every group of <= 64 points; results[b * K + k].
+pg_status run_lik(pg_ctx* c, int32_t batch, const double* theta, int adjoint, double* results) {
+    LikState& L = c->lik;
+    const int groups = (batch + kLikMaxB - 1) / kLikMaxB;
+    const int K = adjoint ? 4 : 1;
+    const int64_t zneed = (int64_t)groups * L.agents * kLikMaxB;
+    if (L.theta.n < 4 * (int64_t)groups * kLikMaxB) PG_CUDA(c, dalloc(L.theta, 4 * (int64_t)groups * kLikMaxB));
+    if (L.zagent.n < zneed) {
+        if (adjoint) return fail(c, PG_ERR_STATE, "run pg_loglik_fwd first");
+        PG_CUDA(c, dalloc(L.zagent, zneed));
+    }
+    if (L.zglob.n < (int64_t)groups * L.epochs * kLikMaxB) {
+        if (adjoint) return fail(c, PG_ERR_STATE, "run pg_loglik_fwd first");
+        PG_CUDA(c, dalloc(L.zglob, (int64_t)groups * L.epochs * kLikMaxB));
+    }
+    if (L.gglob.n < (int64_t)L.epochs * kLikMaxB * 3) PG_CUDA(c, dalloc(L.gglob, (int64_t)L.epochs * kLikMaxB * 3));
+    if (L.gpart.n < (int64_t)L.epochs * L.chunks * kLikMaxB * 4)
+        PG_CUDA(c, dalloc(L.gpart, (int64_t)L.epochs * L.chunks * kLikMaxB * 4));
+    if (L.out.n < L.agents * kLikMaxB * 4) PG_CUDA(c, dalloc(L.out, std::max<int64_t>(1, L.agents) * kLikMaxB * 4));
+    if (L.res.n < kLikMaxB * 4) PG_CUDA(c, dalloc(L.res, kLikMaxB * 4));
+    PG_CUDA(c, cudaMemcpyAsync(L.theta.p, theta, sizeof(double) * 4 * (size_t)batch, cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaMemsetAsync(L.err.p, 0, sizeof(uint32_t), c->stream));
+    if (!adjoint) PG_CUDA(c, cudaMemsetAsync(L.counters.p, 0, 3 * sizeof(unsigned long long), c->stream));
+    const LikTrace T = make_trace(c);
+    if (c->timing) record_event(c->lev[0], c->stream);
+    std::vector<double> h((size_t)kLikMaxB * 4);
+    cudaGetLastError();
+    for (int g = 0; g < groups; ++g) {
+        LikBatch P{};
+        P.B = std::min(kLikMaxB, batch - g * kLikMaxB);
+        P.BE = 1;
+        while (P.BE < P.B) P.BE <<= 1;
+        P.theta = L.theta.p + 4 * (int64_t)g * kLikMaxB;
+        P.zglob = L.zglob.p + (int64_t)g * L.epochs * kLikMaxB;
+        P.gglob = L.gglob.p;
+        P.gpart = L.gpart.p;
+        P.zagent = L.zagent.p + (int64_t)g * L.agents * kLikMaxB;
+        P.out = L.out.p;
+        P.res = L.res.p;
+        P.error = L.err.p;
+        P.counters = (!adjoint && g == 0) ? L.counters.p : nullptr;
+        launch_lik(T, P, adjoint, L.grid, c->stream);
+        PG_CUDA(c, cudaGetLastError());
+        PG_CUDA(c, cudaMemcpyAsync(h.data(), L.res.p, sizeof(double) * (size_t)P.B * K, cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaStreamSynchronize(c->stream));
+        std::memcpy(results + (int64_t)g * kLikMaxB * K, h.data(), sizeof(double) * (size_t)P.B * K);
+    }
+    if (c->timing) {
+        record_event(c->lev[1], c->stream);
+        PG_CUDA(c, cudaStreamSynchronize(c->stream));
+        (adjoint ? c->stats.lik_ms_bwd : c->stats.lik_ms_fwd) = ms_between(c->lev[0], c->lev[1]);
+    }
+    if (!adjoint) {
+        unsigned long long cnt[3];
+        PG_CUDA(c, cudaMemcpy(cnt, L.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
+        c->stats.lik_ball_elems = (int64_t)cnt[0];
+        c->stats.lik_adj_entries = (int64_t)cnt[1];
+        c->stats.lik_citations = (int64_t)cnt[2];
+    }
+    uint32_t err = 0;
+    PG_CUDA(c, cudaMemcpy(&err, L.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (err) return fail(c, PG_ERR_ARG, "a per-agent normaliser was not positive (weights underflow at this theta)");
+    return PG_OK;
+}
+
+}  // namespace
+
+pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
+    if (!c) return PG_ERR_ARG;
+    if (!t || !t->pub_epoch || !t->fitness || !t->epoch_nodes || !t->epoch_t || !t->cite_off)
+        return fail(c, PG_ERR_ARG, "incomplete trace descriptor");
+    const int64_t n = t->num_nodes;
+    const int E = t->num_epochs;
+    if (n <= 0 || n > (int64_t)INT32_MAX / 2 || E < 1) return fail(c, PG_ERR_ARG, "trace size out of range");
+    if (t->num_anchors < 1 || t->num_anchors > PG_MAX_ANCHORS) return fail(c, PG_ERR_ARG, "num_anchors must be in [1, 4]");
+    const int64_t n0 = t->epoch_nodes[0];
+    if (n0 < 1 || t->epoch_nodes[E] != n) return fail(c, PG_ERR_ARG, "epoch_nodes must run from the seed size to num_nodes");
+    for (int e = 0; e < E; ++e)
+        if (t->epoch_nodes[e + 1] < t->epoch_nodes[e]) return fail(c, PG_ERR_ARG, "epoch_nodes must not decrease");
+    const int64_t agents = n - n0;
+    if (agents > 0 && (!t->anchors || !t->cites)) return fail(c, PG_ERR_ARG, "anchors and cites are required");
+    if (t->num_seed_edges < 0 || (t->num_seed_edges > 0 && (!t->seed_src || !t->seed_dst)))
+        return fail(c, PG_ERR_ARG, "bad seed edge arrays");
+    for (int64_t i = 0; i < t->num_seed_edges; ++i)
+        if (t->seed_src[i] < 0 || t->seed_src[i] >= n0 || t->seed_dst[i] < 0 || t->seed_dst[i] >= n0)
+            return fail(c, PG_ERR_ARG, "seed edge " + std::to_string(i) + " leaves the seed");
+    if (t->cite_off[0] != 0) return fail(c, PG_ERR_ARG, "cite_off[0] must be 0");
+    std::vector<int32_t> aep((size_t)std::max<int64_t>(agents, 1));
+    {
+        int e = 0;
+        for (int64_t a = 0; a < agents; ++a) {
+            const int64_t v = n0 + a;
+            while (t->epoch_nodes[e + 1] <= v) ++e;
+            aep[(size_t)a] = e;
+            const int64_t ne = t->epoch_nodes[e];
+            const int64_t k = t->cite_off[a + 1] - t->cite_off[a];
+            if (k < 0 || k > PG_MAX_OUT_DEGREE)
+                return fail(c, PG_ERR_ARG, "agent " + std::to_string(a) + ": 0..256 citations");
+            for (int64_t p = t->cite_off[a]; p < t->cite_off[a + 1]; ++p)
+                if (t->cites[p] < 0 || t->cites[p] >= ne)
+                    return fail(c, PG_ERR_ARG, "agent " + std::to_string(a) + " cites a node that did not exist yet");
+            for (int i = 0; i < 4; ++i) {
+                const int32_t x = t->anchors[a * 4 + i];
+                if (x < -1 || x >= ne || (i < t->num_anchors && x < 0) || (i >= t->num_anchors && x != -1))
+                    return fail(c, PG_ERR_ARG, "agent " + std::to_string(a) + ": bad anchor");
+            }
+        }
+    }
+    PG_CUDA(c, cudaSetDevice(c->device));
+    // final graph = seed edges + every agent's citations
+    const int64_t mc = t->cite_off[agents];
+    const int64_t m = t->num_seed_edges + mc;
+    std::vector<int32_t> src((size_t)std::max<int64_t>(m, 1)), dst((size_t)std::max<int64_t>(m, 1));
+    if (t->num_seed_edges) {
+        std::memcpy(src.data(), t->seed_src, 4 * (size_t)t->num_seed_edges);
+        std::memcpy(dst.data(), t->seed_dst, 4 * (size_t)t->num_seed_edges);
+    }
+    for (int64_t a = 0; a < agents; ++a)
+        for (int64_t p = t->cite_off[a]; p < t->cite_off[a + 1]; ++p) {
+            src[(size_t)(t->num_seed_edges + p)] = (int32_t)(n0 + a);
+            dst[(size_t)(t->num_seed_edges + p)] = t->cites[p];
+        }
+    std::vector<int64_t> fo, bo;
+    std::vector<int32_t> fc, bc;
+    host_csr(n, m, src.data(), dst.data(), fo, fc);
+    host_transpose(n, fo, fc, bo, bc);
+    LikState& L = c->lik;
+    free_lik(L);
+    L.n = n;
+    L.n0 = n0;
+    L.agents = agents;
+    L.epochs = E;
+    L.num_anchors = t->num_anchors;
+    int64_t nmax = 1;
+    for (int e = 0; e < E; ++e) nmax = std::max(nmax, t->epoch_nodes[e]);
+    L.words = (int)std::min<int64_t>((nmax + 31) / 32, kLikMaxWords);
+    L.words = (L.words + 3) / 4 * 4;
+    L.chunks = (int)((nmax + kLikChunk - 1) / kLikChunk);
+    pg_status s = PG_OK;
+    if ((s = upload(c, L.epoch_nodes, t->epoch_nodes, (int64_t)E + 1)) != PG_OK) return s;
+    if ((s = upload(c, L.epoch_t, t->epoch_t, (int64_t)E)) != PG_OK) return s;
+    if ((s = upload(c, L.fo, fo.data(), n + 1)) != PG_OK) return s;
+    if ((s = upload(c, L.fc, fc.data(), (int64_t)fc.size())) != PG_OK) return s;
+    if ((s = upload(c, L.bo, bo.data(), n + 1)) != PG_OK) return s;
+    if ((s = upload(c, L.bc, bc.data(), (int64_t)bc.size())) != PG_OK) return s;
+    if ((s = upload(c, L.fit, t->fitness, n)) != PG_OK) return s;
+    if ((s = upload(c, L.pub, t->pub_epoch, n)) != PG_OK) return s;
+    if ((s = upload(c, L.anchors, t->anchors, 4 * std::max<int64_t>(agents, 1) * (agents > 0))) != PG_OK) return s;
+    if ((s = upload(c, L.coff, t->cite_off, agents + 1)) != PG_OK) return s;
+    if ((s = upload(c, L.cites, t->cites, mc)) != PG_OK) return s;
+    if ((s = upload(c, L.agent_epoch, aep.data(), agents)) != PG_OK) return s;
+    PG_CUDA(c, dalloc(L.feat, (int64_t)E * n));
+    PG_CUDA(c, dalloc(L.err, 1));
+    PG_CUDA(c, dalloc(L.counters, 3));
+    int per_sm = 1;
+    PG_CUDA(c, init_lik_kernels(L.words, &per_sm));
+    L.grid = c->num_sms * per_sm;
+    cudaGetLastError();
+    launch_lik_features(make_trace(c), c->num_sms, c->stream);
+    PG_CUDA(c, cudaGetLastError());
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    L.loaded = true;
+    return PG_OK;
+}
+
+pg_status pg_loglik_fwd(pg_ctx* c, int32_t batch, const double* theta, double* loglik) {
+    if (!c) return PG_ERR_ARG;
+    if (!c->lik.loaded) return fail(c, PG_ERR_STATE, "no trace loaded");
+    if (!loglik) return fail(c, PG_ERR_ARG, "loglik is NULL");
+    pg_status s = check_theta(c, batch, theta);
+    if (s != PG_OK) return s;
+    PG_CUDA(c, cudaSetDevice(c->device));
+    c->lik.fwd_theta.clear();
+    s = run_lik(c, batch, theta, 0, loglik);
+    if (s == PG_OK) c->lik.fwd_theta.assign(theta, theta + 4 * (size_t)batch);
+    return s;
+}
+
+pg_status pg_loglik_bwd(pg_ctx* c, int32_t batch, const double* theta, const double* dloglik,
+                        double* grad) {
+    if (!c) return PG_ERR_ARG;
+    if (!c->lik.loaded) return fail(c, PG_ERR_STATE, "no trace loaded");
+    if (!grad) return fail(c, PG_ERR_ARG, "grad is NULL");
+    pg_status s = check_theta(c, batch, theta);
+    if (s != PG_OK) return s;
+    if (c->lik.fwd_theta.size() != 4 * (size_t)batch ||
+        std::memcmp(c->lik.fwd_theta.data(), theta, sizeof(double) * 4 * (size_t)batch) != 0)
+        return fail(c, PG_ERR_STATE, "pg_loglik_bwd needs the points of the last pg_loglik_fwd");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    s = run_lik(c, batch, theta, 1, grad);
+    if (s != PG_OK) return s;
+    if (dloglik)
+        for (int b = 0; b < batch; ++b)
+            for (int k = 0; k < 4; ++k) grad[4 * b + k] *= dloglik[b];
+    return PG_OK;
+}

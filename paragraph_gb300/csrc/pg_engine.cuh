@@ -131,6 +131,7 @@ struct Arena {
     int32_t* e_dst;            // [edge cap]
     int32_t* e_rank;           // [edge cap]
     int32_t* arrivals;         // [edge cap] or null
+    int32_t* anchors_out;      // [agent cap][4] anchors of each agent, or null (record_trace)
     int32_t* big_list;         // [agent cap]
     int64_t* len_tmp;          // [slots]
     uint64_t* tilesum;         // [ntiles]

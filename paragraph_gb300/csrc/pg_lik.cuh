@@ -1,0 +1,65 @@
+// pg_lik.cuh -- device layout of a growth trace and of one batch of parameter points for the
+// log-likelihood forward pass and its adjoint.
+//
+// The trace lives in its own buffers beside the growth arena:
+//   final graph as forward and backward CSR (rows sorted ascending), int64 offsets;
+//   feat[e][j] = (log f_j, log(indeg_e(j)+1), t_e - t_j, 0) for every trace epoch e and node j < n_e,
+//   one float4 per (epoch, node) so a weight is one 16-byte gather and one exp;
+//   per agent: its epoch, anchors [4] and citations in draw order (cite offsets int64).
+// indeg_e(j) is the number of in-edges of j from nodes < n_e: the prefix of j's backward row below
+// n_e, because rows are sorted and node ids grow with time.
+#pragma once
+#include "pg_engine.cuh"
+
+namespace pg {
+
+constexpr int kLikMaxB = 64;         // parameter points per launch
+constexpr int kLikThreads = 256;
+constexpr int kLikList = 4096;       // ball ids staged in shared memory per window
+constexpr int kLikChunk = 4096;      // nodes per CTA in the per-epoch global sums
+constexpr int kLikMaxWords = 24576;  // ball bitmap words per pass (96 KiB, 786,432 ids)
+
+struct LikTrace {
+    int64_t n;                   // nodes at the end of the trace
+    int64_t agents;
+    int32_t epochs;
+    int32_t num_anchors;
+    int32_t bitmap_words;        // words of the shared ball bitmap per pass (multiple of 4)
+    int32_t chunks;              // node chunks per epoch in the global pass
+    const int64_t* epoch_nodes;  // [epochs + 1]
+    const int32_t* epoch_t;      // [epochs]
+    const int64_t* fo;
+    const int32_t* fc;
+    const int64_t* bo;
+    const int32_t* bc;
+    const float* fit;            // [n]
+    const int32_t* pub;          // [n]
+    float4* feat;                // [epochs][n]
+    const int32_t* anchors;      // [agents][4]
+    const int64_t* coff;         // [agents + 1]
+    const int32_t* cites;
+    const int32_t* agent_epoch;  // [agents]
+};
+
+struct LikBatch {
+    int32_t B;           // points in this launch (<= kLikMaxB)
+    int32_t BE;          // B rounded up to a power of two: threads per point group
+    const double* theta; // [B][4] alpha, tau, gamma, beta
+    double* zglob;       // [epochs][B]      sum_{j<n_e} w_j          (forward writes)
+    double* gglob;       // [epochs][B][3]   sum_j w_j dlog w_j/dtheta (adjoint writes)
+    double* gpart;       // [epochs][chunks][B][4] partial sums of the global pass
+    double* zagent;      // [agents][B]      per-agent normaliser Z_a (forward writes, adjoint reads)
+    double* out;         // [agents][B][1|4] per-agent log-likelihood or gradient
+    double* res;         // [B][1|4]         totals
+    uint32_t* error;     // bit 2: a normaliser was not positive
+    unsigned long long* counters;  // forward, first group only (else null): ball elements,
+                                   // adjacency entries read, citations
+};
+
+size_t lik_agent_smem(int bitmap_words);
+cudaError_t init_lik_kernels(int bitmap_words, int* blocks_per_sm);
+void launch_lik_features(const LikTrace& T, int num_sms, cudaStream_t s);
+// adjoint = 0: forward (Z_glob, per-agent Z_a and log-likelihood); 1: adjoint (gradient)
+void launch_lik(const LikTrace& T, const LikBatch& P, int adjoint, int agent_grid, cudaStream_t s);
+
+}  // namespace pg

@@ -117,3 +117,45 @@ def ensemble_inputs(replicas: int = 256, lo: int = 5_000, hi: int = 200_000, epo
                      mean_out_degree=20.0, growth_rate=0.03, fixed_new_nodes=0, num_anchors=3)
         out.append(ReplicaInput(g.pub, g.fitness, g.src, g.dst, p, planned_epochs=epochs))
     return out
+
+
+def grow_trace(g: SeedGraph, params: PAParams, epochs: int, seed: int = 42,
+               device: int = 0) -> "TraceInput":
+    """Grow `epochs` PA epochs from seed graph g on the GPU and record the trace (each agent's
+    anchors and its citations in draw order)."""
+    from . import GrowthEngine, TraceInput
+
+    ep_nodes, ep_t, anchors, cites, counts = [g.n], [], [], [], []
+    with GrowthEngine(seed=seed, device=device, record_trace=True) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, params, planned_epochs=epochs)
+        for e in range(epochs):
+            n_e = eng.counts()[0]
+            nn, _ = eng.grow_epoch()
+            ep_t.append(e)
+            anchors.append(eng.anchors(nn))
+            first, cnt = eng.epoch_edges()
+            off, _ = eng.csr(0)
+            counts.append(np.diff(off[n_e:n_e + nn + 1]))
+            cites.append(eng.arrivals())
+            ep_nodes.append(n_e + nn)
+        pub, fit = eng.nodes()
+    cnt = np.concatenate(counts)
+    return TraceInput(pub=pub, fitness=fit, seed_src=g.src, seed_dst=g.dst,
+                      epoch_nodes=np.array(ep_nodes), epoch_t=np.array(ep_t),
+                      anchors=np.concatenate(anchors), cite_off=np.concatenate([[0], np.cumsum(cnt)]),
+                      cites=np.concatenate(cites), num_anchors=params.num_anchors)
+
+
+def calibration_params() -> PAParams:
+    """Trace for calibration: theta* = (alpha, tau, gamma, beta) = (1, 5, 1, 4), Poisson(20)
+    out-degree, 3 % growth, 3 anchors."""
+    return PAParams(alpha=1.0, tau=5.0, gamma=1.0, beta=4.0, mean_out_degree=20.0,
+                    growth_rate=0.03, fixed_new_nodes=0, num_anchors=3)
+
+
+def theta_batch(points: int = 64, seed: int = 7) -> np.ndarray:
+    """Parameter points from the ensemble ranges: alpha~U[0.5,1.5], tau~U[2,10], gamma~U[0.5,2],
+    beta~U[1,8]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return np.stack([rng.uniform(0.5, 1.5, points), rng.uniform(2, 10, points),
+                     rng.uniform(0.5, 2.0, points), rng.uniform(1, 8, points)], axis=1)

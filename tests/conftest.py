@@ -39,7 +39,7 @@ def has_gpu():
         return False
 
 
-@pytest.fixture()
+@pytest.fixture(scope="session")
 def gpu(built, has_gpu):
     if not has_gpu:
         pytest.fail("GPU test collected on a machine without a GPU (run with -m 'not gpu')")

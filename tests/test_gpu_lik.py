@@ -1,0 +1,120 @@
+"""GPU log-likelihood forward pass and adjoint against the FP64 oracle.
+
+The GPU computes each weight in fp32 (one exp of an fp32 exponent) and every normaliser, prefix
+sum and log-sum in FP64; the oracle is FP64 throughout.  Tolerances: log-likelihood relative
+error <= 1e-7 (fp32 exponents carry about 1e-7 relative error into each of the ~1e5 terms);
+gradient relative error (2-norm over the four components) <= 1e-6 at the 64 points drawn from the
+parameter ranges.  At the generating point theta* the gradient is close to zero -- the trace was
+drawn there -- so the same absolute error is a larger share of it: there the bound is 1e-5."""
+import numpy as np
+import pytest
+
+import oracle as O
+from paragraph_gb300 import GrowthEngine, PGError
+from paragraph_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+THETA_STAR = np.array([1.0, 5.0, 1.0, 4.0])
+
+
+@pytest.fixture(scope="module")
+def trace_mid(gpu):
+    g = W.plain_pa_seed(20_000, 10, seed=3)
+    return W.grow_trace(g, W.calibration_params(), 10, seed=5)
+
+
+def test_gpu_trace_equals_oracle_trace(gpu):
+    """Anchors and draw-order citations recorded by the GPU growth step match the oracle's."""
+    g = W.plain_pa_seed(4000, 10, seed=4)
+    prm = W.calibration_params()
+    tg = W.grow_trace(g, prm, 4, seed=9)
+    to = O.grow_trace(g, prm, 4, seed=9)
+    for f in ("epoch_nodes", "epoch_t", "anchors", "cite_off", "cites", "pub"):
+        np.testing.assert_array_equal(getattr(tg, f), getattr(to, f), err_msg=f)
+    np.testing.assert_array_equal(tg.fitness.view(np.uint32), to.fitness.view(np.uint32))
+
+
+def test_loglik_and_gradient_match_fp64_oracle(trace_mid):
+    pts = np.vstack([THETA_STAR, W.theta_batch(64, seed=1)])
+    with GrowthEngine(seed=1) as eng:
+        eng.load_trace(trace_mid)
+        ll = eng.loglik(pts)
+        gr = eng.loglik_grad(pts)
+    llo, gro = O.loglik(trace_mid, pts)
+    rel_ll = np.abs(ll - llo) / np.abs(llo)
+    rel_g = np.linalg.norm(gr - gro, axis=1) / np.linalg.norm(gro, axis=1)
+    msg = f"loglik {rel_ll.max():.3g}, grad (64 points) {rel_g[1:].max():.3g}, grad (theta*) {rel_g[0]:.3g}"
+    assert rel_ll.max() <= 1e-7, msg
+    assert rel_g[1:].max() <= 1e-6, msg
+    assert rel_g[0] <= 1e-5, msg
+
+
+def test_batch_groups_and_single_points_agree(trace_mid):
+    """70 points run as two launches of <= 64; every point alone gives the same values.  A single
+    point splits the ball sums over more threads than a batch, so the compensated fp32 partial
+    sums differ in order: agreement is to 1e-9 (log-likelihood) and 1e-7 (gradient), not bitwise."""
+    pts = W.theta_batch(70, seed=2)
+    with GrowthEngine(seed=1) as eng:
+        eng.load_trace(trace_mid)
+        ll = eng.loglik(pts)
+        gr = eng.loglik_grad(pts, dloglik=np.full(70, 2.0))
+        for b in (0, 33, 64, 69):
+            l1 = eng.loglik(pts[b:b + 1])
+            g1 = eng.loglik_grad(pts[b:b + 1])
+            assert abs(l1[0] - ll[b]) <= 1e-9 * abs(ll[b])
+            assert np.linalg.norm(2.0 * g1[0] - gr[b]) <= 1e-7 * np.linalg.norm(gr[b])
+
+
+def test_adjoint_matches_gpu_central_differences(trace_mid):
+    """Central differences of the GPU's own log-likelihood (h = 1e-4).  The fp32 weights make the
+    log-likelihood accurate to about 1e-8 relative, about 1e-2 absolute here, and that rounding
+    changes from one point to the next, so the differences carry up to 1e-2 / 2e-4 = 50 units of
+    noise on gradients of 1e4: the check is at 1e-3 relative.  The FP64 gradient of the oracle
+    meets central differences at 1e-6 (tests/test_lik_oracle.py) and the GPU adjoint meets that
+    FP64 gradient at 1e-6 (above)."""
+    pts = W.theta_batch(4, seed=5)
+    h = 1e-4
+    with GrowthEngine(seed=1) as eng:
+        eng.load_trace(trace_mid)
+        eng.loglik(pts)
+        gr = eng.loglik_grad(pts)
+        for b in range(len(pts)):
+            shifted = []
+            for k in range(4):
+                for s in (1.0, -1.0):
+                    t = pts[b].copy()
+                    t[k] += s * h
+                    shifted.append(t)
+            l = eng.loglik(np.array(shifted))
+            fd = (l[0::2] - l[1::2]) / (2 * h)
+            assert np.linalg.norm(fd - gr[b]) / np.linalg.norm(gr[b]) <= 1e-3
+
+
+def test_adjoint_needs_the_forward_points(trace_mid):
+    pts = W.theta_batch(3, seed=8)
+    with GrowthEngine(seed=1) as eng:
+        eng.load_trace(trace_mid)
+        with pytest.raises(PGError):
+            eng.loglik_grad(pts)
+        eng.loglik(pts)
+        with pytest.raises(PGError):
+            eng.loglik_grad(pts[:2])
+        eng.loglik_grad(pts)
+
+
+def test_ball_bitmap_in_several_passes(gpu):
+    """A seed of 900k nodes needs two shared-memory bitmap passes (786,432 ids each)."""
+    g = W.plain_pa_seed(900_000, 10, seed=6)
+    prm = W.calibration_params()
+    prm.growth_rate = 0.0
+    prm.fixed_new_nodes = 3000
+    tr = W.grow_trace(g, prm, 1, seed=2)
+    pts = np.vstack([THETA_STAR, [0.7, 3.0, 1.5, 6.0]])
+    with GrowthEngine(seed=1) as eng:
+        eng.load_trace(tr)
+        ll = eng.loglik(pts)
+        gr = eng.loglik_grad(pts)
+    llo, gro = O.loglik(tr, pts)
+    assert (np.abs(ll - llo) / np.abs(llo)).max() <= 1e-7
+    rel = np.linalg.norm(gr - gro, axis=1) / np.linalg.norm(gro, axis=1)
+    assert rel[0] <= 1e-5 and rel[1] <= 1e-6, rel
