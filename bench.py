@@ -503,7 +503,7 @@ def run_loglik(args) -> None:
     from paragraph_gb300 import GrowthEngine
     from paragraph_gb300 import workloads as W
 
-    g = W.plain_pa_seed(200_000, 10, seed=args.seed)
+    g = W.plain_pa_seed(args.lik_seed_nodes, 10, seed=args.seed)
     trace = W.grow_trace(g, W.calibration_params(), LIK_EPOCHS, seed=args.seed, device=local)
     pts_all = W.theta_batch(LIK_POINTS, seed=args.seed)
     pts = np.ascontiguousarray(pts_all[rank::world])
@@ -665,6 +665,8 @@ def main():
                     help="batched ensemble (256 replicas x 10 epochs) against the serial loop")
     ap.add_argument("--loglik", action="store_true",
                     help="log-likelihood + adjoint at 64 points against the per-point loop")
+    ap.add_argument("--lik-seed-nodes", type=int, default=200_000,
+                    help="seed size of the calibration trace (smaller cases for profiling)")
     args = ap.parse_args()
     if args.ensemble or args.loglik:
         if args.warmup < 3:

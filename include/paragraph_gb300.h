@@ -220,7 +220,10 @@ typedef struct {
     int32_t agent_ctas_per_sm; /* CTAs per SM of the k <= 64 agent kernel; 0 = occupancy limit */
     int32_t small_hash;        /* 1: 1024-slot frontier hash per warp in that kernel, 0: 2048 */
     int32_t copy_ctas_per_sm;  /* CTAs per SM of the backward-CSR copy; 0 = default (8) */
-    int32_t reserved;
+    int32_t lik_chunk_agents;  /* > 0: pg_trace_load keeps at most this many agents' neighbourhood
+                                  balls per chunk, so every likelihood pass rebuilds them chunk by
+                                  chunk; 0: as many as fit in a quarter of free device memory (one
+                                  chunk = built once and reused by every pass) */
 } pg_tuning;
 pg_status pg_set_tuning(pg_ctx* ctx, const pg_tuning* tuning);
 pg_status pg_get_tuning(const pg_ctx* ctx, pg_tuning* tuning);

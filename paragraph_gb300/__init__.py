@@ -85,7 +85,7 @@ class _Stats(C.Structure):
 
 class _Tuning(C.Structure):
     _fields_ = [("agent_ctas_per_sm", C.c_int32), ("small_hash", C.c_int32),
-                ("copy_ctas_per_sm", C.c_int32), ("reserved", C.c_int32)]
+                ("copy_ctas_per_sm", C.c_int32), ("lik_chunk_agents", C.c_int32)]
 
 
 class _TraceDesc(C.Structure):
@@ -426,15 +426,16 @@ class GrowthEngine:
         self._check(self._lib.pg_restore(self._ctx))
 
     def set_tuning(self, agent_ctas_per_sm: int = 0, small_hash: int = 0,
-                   copy_ctas_per_sm: int = 0) -> None:
-        """Launch shape of the agent and backward-copy kernels (results never depend on it)."""
-        t = _Tuning(agent_ctas_per_sm, small_hash, copy_ctas_per_sm, 0)
+                   copy_ctas_per_sm: int = 0, lik_chunk_agents: int = 0) -> None:
+        """Launch shape of the agent and backward-copy kernels, and the likelihood's ball chunking
+        (results never depend on them)."""
+        t = _Tuning(agent_ctas_per_sm, small_hash, copy_ctas_per_sm, lik_chunk_agents)
         self._check(self._lib.pg_set_tuning(self._ctx, C.byref(t)))
 
     def tuning(self) -> dict:
         t = _Tuning()
         self._check(self._lib.pg_get_tuning(self._ctx, C.byref(t)))
-        return {k: getattr(t, k) for k, _ in _Tuning._fields_ if k != "reserved"}
+        return {k: getattr(t, k) for k, _ in _Tuning._fields_}
 
     def autotune(self, epochs: int) -> tuple[dict, float]:
         """Time the candidate tunings on the next `epochs` epochs, keep the fastest; the graph is
@@ -442,7 +443,7 @@ class GrowthEngine:
         t = _Tuning()
         ms = C.c_double()
         self._check(self._lib.pg_autotune(self._ctx, int(epochs), C.byref(t), C.byref(ms)))
-        return {k: getattr(t, k) for k, _ in _Tuning._fields_ if k != "reserved"}, ms.value
+        return {k: getattr(t, k) for k, _ in _Tuning._fields_}, ms.value
 
     # ---------------------------------------------------------------- trace log-likelihood
     def load_trace(self, t: TraceInput) -> None:

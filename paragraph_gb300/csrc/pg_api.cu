@@ -41,14 +41,19 @@ struct DBuf {
 struct LikState {
     bool loaded = false;
     int64_t n = 0, n0 = 0, agents = 0;
-    int epochs = 0, num_anchors = 0, words = 0, chunks = 0, grid = 0;
-    DBuf<int64_t> epoch_nodes, fo, bo, coff;
-    DBuf<int32_t> epoch_t, fc, bc, pub, anchors, cites, agent_epoch;
+    int epochs = 0, num_anchors = 0, words = 0, chunks = 0, ball_grid = 0, eval_grid[2] = {0, 0};
+    int64_t chunk_agents = 0;  // > 0: at most this many agents' balls per chunk (pg_tuning)
+    DBuf<int64_t> epoch_nodes, fo, bo, coff, boff, bcnt, badj;
+    DBuf<int32_t> epoch_t, fc, bc, pub, anchors, cites, agent_epoch, bids;
+    DBuf<uint8_t> cflag;
     DBuf<float> fit;
     DBuf<float4> feat;
-    DBuf<double> theta, zglob, gglob, gpart, zagent, out, res;
+    DBuf<double> theta, pp, zglob, gglob, gpart, zagent, out, res;
     DBuf<uint32_t> err;
-    DBuf<unsigned long long> counters;  // ball elements, adjacency entries, citations
+    std::vector<int64_t> hboff;              // ball offsets on the host
+    std::vector<std::pair<int64_t, int64_t>> ball_chunks;  // agent ranges whose balls fit in bids
+    bool balls_cached = false;               // one chunk: built at load, reused by every pass
+    int64_t ball_elems = 0, adj_entries = 0, citations = 0;
     std::vector<double> fwd_theta;  // points of the last forward pass
 };
 
@@ -297,16 +302,19 @@ void free_checkpoint(Checkpoint& k) {
 }
 
 void free_lik(LikState& L) {
-    DBuf<int64_t>* i64[] = {&L.epoch_nodes, &L.fo, &L.bo, &L.coff};
+    DBuf<int64_t>* i64[] = {&L.epoch_nodes, &L.fo, &L.bo, &L.coff, &L.boff, &L.bcnt, &L.badj};
     for (auto* b : i64) dfree(*b);
-    DBuf<int32_t>* i32[] = {&L.epoch_t, &L.fc, &L.bc, &L.pub, &L.anchors, &L.cites, &L.agent_epoch};
+    DBuf<int32_t>* i32[] = {&L.epoch_t, &L.fc, &L.bc, &L.pub, &L.anchors, &L.cites, &L.agent_epoch, &L.bids};
     for (auto* b : i32) dfree(*b);
-    DBuf<double>* f64[] = {&L.theta, &L.zglob, &L.gglob, &L.gpart, &L.zagent, &L.out, &L.res};
+    DBuf<double>* f64[] = {&L.theta, &L.pp, &L.zglob, &L.gglob, &L.gpart, &L.zagent, &L.out, &L.res};
     for (auto* b : f64) dfree(*b);
+    dfree(L.cflag);
     dfree(L.fit);
     dfree(L.feat);
     dfree(L.err);
-    dfree(L.counters);
+    L.hboff.clear();
+    L.ball_chunks.clear();
+    L.balls_cached = false;
     L.loaded = false;
     L.fwd_theta.clear();
 }
@@ -1328,11 +1336,10 @@ pg_status pg_restore(pg_ctx* c) {
 pg_status pg_set_tuning(pg_ctx* c, const pg_tuning* t) {
     if (!c) return PG_ERR_ARG;
     if (!t || t->agent_ctas_per_sm < 0 || t->agent_ctas_per_sm > 32 || t->copy_ctas_per_sm < 0 ||
-        t->copy_ctas_per_sm > 64 || (t->small_hash != 0 && t->small_hash != 1))
+        t->copy_ctas_per_sm > 64 || (t->small_hash != 0 && t->small_hash != 1) || t->lik_chunk_agents < 0)
         return fail(c, PG_ERR_ARG, "tuning out of range");
     if (std::memcmp(&c->tune, t, sizeof(pg_tuning)) != 0) {
         c->tune = *t;
-        c->tune.reserved = 0;
         destroy_graph_exec(c);  // captured launches carry the old grid sizes
     }
     return PG_OK;
@@ -1494,13 +1501,25 @@ pg_status check_theta(pg_ctx* c, int32_t batch, const double* theta) {
     return PG_OK;
 }
 
+LikBalls make_balls(const LikState& L, int64_t a0) {
+    LikBalls Bl{};
+    Bl.boff = L.boff.p;
+    Bl.base = L.hboff.empty() ? 0 : L.hboff[(size_t)a0];
+    Bl.ids = L.bids.p;
+    Bl.cflag = L.cflag.p;
+    Bl.cnt = L.bcnt.p;
+    Bl.adj = L.badj.p;
+    return Bl;
+}
+
 // One pass (forward or adjoint) over every group of <= 64 points; results[b * K + k].
 pg_status run_lik(pg_ctx* c, int32_t batch, const double* theta, int adjoint, double* results) {
     LikState& L = c->lik;
     const int groups = (batch + kLikMaxB - 1) / kLikMaxB;
     const int K = adjoint ? 4 : 1;
-    const int64_t zneed = (int64_t)groups * L.agents * kLikMaxB;
+    const int64_t zneed = (int64_t)groups * std::max<int64_t>(L.agents, 1) * kLikMaxB;
     if (L.theta.n < 4 * (int64_t)groups * kLikMaxB) PG_CUDA(c, dalloc(L.theta, 4 * (int64_t)groups * kLikMaxB));
+    if (L.pp.n < 8 * (int64_t)groups * kLikMaxB) PG_CUDA(c, dalloc(L.pp, 8 * (int64_t)groups * kLikMaxB));
     if (L.zagent.n < zneed) {
         if (adjoint) return fail(c, PG_ERR_STATE, "run pg_loglik_fwd first");
         PG_CUDA(c, dalloc(L.zagent, zneed));
@@ -1512,11 +1531,26 @@ pg_status run_lik(pg_ctx* c, int32_t batch, const double* theta, int adjoint, do
     if (L.gglob.n < (int64_t)L.epochs * kLikMaxB * 3) PG_CUDA(c, dalloc(L.gglob, (int64_t)L.epochs * kLikMaxB * 3));
     if (L.gpart.n < (int64_t)L.epochs * L.chunks * kLikMaxB * 4)
         PG_CUDA(c, dalloc(L.gpart, (int64_t)L.epochs * L.chunks * kLikMaxB * 4));
-    if (L.out.n < L.agents * kLikMaxB * 4) PG_CUDA(c, dalloc(L.out, std::max<int64_t>(1, L.agents) * kLikMaxB * 4));
+    if (L.out.n < std::max<int64_t>(1, L.agents) * kLikMaxB * 4)
+        PG_CUDA(c, dalloc(L.out, std::max<int64_t>(1, L.agents) * kLikMaxB * 4));
     if (L.res.n < kLikMaxB * 4) PG_CUDA(c, dalloc(L.res, kLikMaxB * 4));
+    // per point: alpha, 1/tau, gamma, beta, log beta, 1/beta, 1/tau^2, tau
+    std::vector<double> pp((size_t)batch * 8);
+    for (int b = 0; b < batch; ++b) {
+        const double* t = theta + 4 * b;
+        double* q = pp.data() + 8 * b;
+        q[0] = t[0];
+        q[1] = 1.0 / t[1];
+        q[2] = t[2];
+        q[3] = t[3];
+        q[4] = log_pg(t[3]);
+        q[5] = 1.0 / t[3];
+        q[6] = 1.0 / (t[1] * t[1]);
+        q[7] = t[1];
+    }
     PG_CUDA(c, cudaMemcpyAsync(L.theta.p, theta, sizeof(double) * 4 * (size_t)batch, cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(L.pp.p, pp.data(), sizeof(double) * 8 * (size_t)batch, cudaMemcpyHostToDevice, c->stream));
     PG_CUDA(c, cudaMemsetAsync(L.err.p, 0, sizeof(uint32_t), c->stream));
-    if (!adjoint) PG_CUDA(c, cudaMemsetAsync(L.counters.p, 0, 3 * sizeof(unsigned long long), c->stream));
     const LikTrace T = make_trace(c);
     if (c->timing) record_event(c->lev[0], c->stream);
     std::vector<double> h((size_t)kLikMaxB * 4);
@@ -1526,7 +1560,9 @@ pg_status run_lik(pg_ctx* c, int32_t batch, const double* theta, int adjoint, do
         P.B = std::min(kLikMaxB, batch - g * kLikMaxB);
         P.BE = 1;
         while (P.BE < P.B) P.BE <<= 1;
+        P.BW = std::min(P.BE, 32);
         P.theta = L.theta.p + 4 * (int64_t)g * kLikMaxB;
+        P.pp = L.pp.p + 8 * (int64_t)g * kLikMaxB;
         P.zglob = L.zglob.p + (int64_t)g * L.epochs * kLikMaxB;
         P.gglob = L.gglob.p;
         P.gpart = L.gpart.p;
@@ -1534,8 +1570,13 @@ pg_status run_lik(pg_ctx* c, int32_t batch, const double* theta, int adjoint, do
         P.out = L.out.p;
         P.res = L.res.p;
         P.error = L.err.p;
-        P.counters = (!adjoint && g == 0) ? L.counters.p : nullptr;
-        launch_lik(T, P, adjoint, L.grid, c->stream);
+        launch_lik_global(T, P, adjoint, c->stream);
+        for (const auto& ch : L.ball_chunks) {
+            const LikBalls Bl = make_balls(L, ch.first);
+            if (!L.balls_cached) launch_lik_ball(T, Bl, 1, ch.first, ch.second, L.ball_grid, c->stream);
+            launch_lik_eval(T, P, Bl, adjoint, ch.first, ch.second, L.eval_grid[adjoint], c->stream);
+        }
+        launch_lik_sum(T, P, adjoint, c->stream);
         PG_CUDA(c, cudaGetLastError());
         PG_CUDA(c, cudaMemcpyAsync(h.data(), L.res.p, sizeof(double) * (size_t)P.B * K, cudaMemcpyDeviceToHost, c->stream));
         PG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1545,13 +1586,6 @@ pg_status run_lik(pg_ctx* c, int32_t batch, const double* theta, int adjoint, do
         record_event(c->lev[1], c->stream);
         PG_CUDA(c, cudaStreamSynchronize(c->stream));
         (adjoint ? c->stats.lik_ms_bwd : c->stats.lik_ms_fwd) = ms_between(c->lev[0], c->lev[1]);
-    }
-    if (!adjoint) {
-        unsigned long long cnt[3];
-        PG_CUDA(c, cudaMemcpy(cnt, L.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
-        c->stats.lik_ball_elems = (int64_t)cnt[0];
-        c->stats.lik_adj_entries = (int64_t)cnt[1];
-        c->stats.lik_citations = (int64_t)cnt[2];
     }
     uint32_t err = 0;
     PG_CUDA(c, cudaMemcpy(&err, L.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
@@ -1647,14 +1681,64 @@ pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
     if ((s = upload(c, L.agent_epoch, aep.data(), agents)) != PG_OK) return s;
     PG_CUDA(c, dalloc(L.feat, (int64_t)E * n));
     PG_CUDA(c, dalloc(L.err, 1));
-    PG_CUDA(c, dalloc(L.counters, 3));
-    int per_sm = 1;
-    PG_CUDA(c, init_lik_kernels(L.words, &per_sm));
-    L.grid = c->num_sms * per_sm;
+    int ball_sm = 1, eval_sm[2] = {1, 1};
+    PG_CUDA(c, init_lik_kernels(L.words, &ball_sm, eval_sm));
+    L.ball_grid = c->num_sms * ball_sm;
+    L.eval_grid[0] = c->num_sms * eval_sm[0];
+    L.eval_grid[1] = c->num_sms * eval_sm[1];
     cudaGetLastError();
     launch_lik_features(make_trace(c), c->num_sms, c->stream);
     PG_CUDA(c, cudaGetLastError());
+    // balls: sizes first, then as many agents' balls per chunk as memory allows
+    const int64_t na = std::max<int64_t>(agents, 1);
+    PG_CUDA(c, dalloc(L.bcnt, na));
+    PG_CUDA(c, dalloc(L.badj, na));
+    PG_CUDA(c, dalloc(L.cflag, std::max<int64_t>(mc, 1)));
+    launch_lik_ball(make_trace(c), make_balls(L, 0), 0, 0, agents, L.ball_grid, c->stream);
+    PG_CUDA(c, cudaGetLastError());
+    std::vector<int64_t> cnt((size_t)na, 0), adj((size_t)na, 0);
+    if (agents > 0) {
+        PG_CUDA(c, cudaMemcpyAsync(cnt.data(), L.bcnt.p, 8 * (size_t)agents, cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(adj.data(), L.badj.p, 8 * (size_t)agents, cudaMemcpyDeviceToHost, c->stream));
+    }
     PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    L.hboff.assign((size_t)agents + 1, 0);
+    int64_t biggest = 1;
+    L.adj_entries = 0;
+    for (int64_t a = 0; a < agents; ++a) {
+        L.hboff[(size_t)a + 1] = L.hboff[(size_t)a] + cnt[(size_t)a];
+        biggest = std::max(biggest, cnt[(size_t)a]);
+        L.adj_entries += adj[(size_t)a];
+    }
+    L.ball_elems = L.hboff[(size_t)agents];
+    L.citations = mc;
+    if ((s = upload(c, L.boff, L.hboff.data(), agents + 1)) != PG_OK) return s;
+    size_t free_b = 0, total_b = 0;
+    PG_CUDA(c, cudaMemGetInfo(&free_b, &total_b));
+    const int64_t budget = std::max<int64_t>(biggest, (int64_t)(free_b / 4) / 4);  // ids in a quarter of free memory
+    int64_t a = 0;
+    while (a < agents) {
+        int64_t b = a;
+        while (b < agents && L.hboff[(size_t)b + 1] - L.hboff[(size_t)a] <= budget &&
+               (c->tune.lik_chunk_agents <= 0 || b - a < c->tune.lik_chunk_agents))
+            ++b;
+        if (b == a) b = a + 1;
+        L.ball_chunks.emplace_back(a, b);
+        a = b;
+    }
+    int64_t chunk_max = 1;
+    for (const auto& ch : L.ball_chunks)
+        chunk_max = std::max(chunk_max, L.hboff[(size_t)ch.second] - L.hboff[(size_t)ch.first]);
+    PG_CUDA(c, dalloc(L.bids, chunk_max));
+    L.balls_cached = L.ball_chunks.size() == 1;
+    if (L.balls_cached) {
+        launch_lik_ball(make_trace(c), make_balls(L, 0), 1, 0, agents, L.ball_grid, c->stream);
+        PG_CUDA(c, cudaGetLastError());
+    }
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->stats.lik_ball_elems = L.ball_elems;
+    c->stats.lik_adj_entries = L.adj_entries;
+    c->stats.lik_citations = L.citations;
     L.loaded = true;
     return PG_OK;
 }

@@ -53,6 +53,23 @@ __device__ __forceinline__ float lik_x(const float4 f, float al, float ga, float
     return ga * f.x + al * f.y - f.z * itau;
 }
 
+// log(1 - u) for u in [0, 0.5): -2 atanh(t), t = u / (2 - u) in [0, 1/3), by the odd Taylor series
+// of atanh, t + t^3/3 + ... + t^17/17 (truncation below 1e-9 relative at t = 1/3).
+__device__ __forceinline__ float log1m_pg(float u) {
+    const float t = u / (2.0f - u);
+    const float s = t * t;
+    float p = 1.0f / 17.0f;
+    p = p * s + 1.0f / 15.0f;
+    p = p * s + 1.0f / 13.0f;
+    p = p * s + 1.0f / 11.0f;
+    p = p * s + 1.0f / 9.0f;
+    p = p * s + 1.0f / 7.0f;
+    p = p * s + 1.0f / 5.0f;
+    p = p * s + 1.0f / 3.0f;
+    p = p * s + 1.0f;
+    return -2.0f * t * p;
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(256) k_lik_features(LikTrace T) {
@@ -135,41 +152,27 @@ __global__ void k_lik_global_sum(LikTrace T, LikBatch P) {
     }
 }
 
-template <bool ADJ>
-__global__ void __launch_bounds__(kLikThreads) k_lik_agents(LikTrace T, LikBatch P) {
+// The 2-hop ball of agents [a0, a1) in the epoch-start graph, one CTA per agent, as a bitmap over
+// [0, n_e) in shared memory (passes of bitmap_words * 32 ids).  EMIT = false: ball sizes (and the
+// adjacency entries read) into Bl.cnt; EMIT = true: the ids, ascending, at Bl.ids[boff[a] - base]
+// and the ball membership of each citation into Bl.cflag.
+template <bool EMIT>
+__global__ void __launch_bounds__(kLikThreads) k_lik_ball(LikTrace T, LikBalls Bl, int64_t a0, int64_t a1) {
     extern __shared__ __align__(16) unsigned char lik_smem[];
-    double* red = reinterpret_cast<double*>(lik_smem);     // [256][4]
-    double* sums = red + kLikThreads * 4;                  // [64][4]
-    int32_t* list = reinterpret_cast<int32_t*>(sums + kLikMaxB * 4);  // [kLikList]
-    int32_t* cid = list + kLikList;                        // [kKMax]
-    uint32_t* bits = reinterpret_cast<uint32_t*>(cid + kKMax);        // [bitmap_words]
-    uint8_t* flag = reinterpret_cast<uint8_t*>(bits + T.bitmap_words);  // [kKMax]
-    __shared__ int64_t seg[2 * PG_MAX_ANCHORS_DEV + 1];  // prefix of the anchors' row lengths
-    __shared__ int64_t rowb[2 * PG_MAX_ANCHORS_DEV];     // first entry of each anchor row
+    uint32_t* bits = reinterpret_cast<uint32_t*>(lik_smem);  // [bitmap_words]
+    __shared__ int64_t seg[2 * PG_MAX_ANCHORS_DEV + 1];       // prefix of the anchors' row lengths
+    __shared__ int64_t rowb[2 * PG_MAX_ANCHORS_DEV];          // first entry of each anchor row
     __shared__ int32_t anc[PG_MAX_ANCHORS_DEV];
     __shared__ int32_t nanc;
     __shared__ int32_t scan_ws[33];
     __shared__ unsigned long long adj_read;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int BE = P.BE, B = P.B;
-    const int b = tid & (BE - 1), sub = tid / BE, nsub = kLikThreads / BE;
-    float al = 0.f, ga = 0.f, itau = 0.f;
-    if (b < B) {
-        al = (float)P.theta[b * 4];
-        itau = (float)(1.0 / P.theta[b * 4 + 1]);
-        ga = (float)P.theta[b * 4 + 2];
-    }
     const int64_t pass_ids = (int64_t)T.bitmap_words * 32;
-    for (int64_t a = blockIdx.x; a < T.agents; a += gridDim.x) {
+    for (int64_t a = a0 + blockIdx.x; a < a1; a += gridDim.x) {
         const int e = T.agent_epoch[a];
         const int64_t ne = T.epoch_nodes[e];
-        const float4* F = T.feat + (int64_t)e * T.n;
         const int64_t c0 = T.coff[a];
         const int k = (int)(T.coff[a + 1] - c0);
-        for (int i = tid; i < k; i += kLikThreads) {
-            cid[i] = T.cites[c0 + i];
-            flag[i] = 0;
-        }
         if (tid == 0) {
             int na = 0;
             for (int i = 0; i < T.num_anchors; ++i) {
@@ -190,11 +193,11 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_agents(LikTrace T, LikBatch
             seg[2 * na] = acc;
             adj_read = (unsigned long long)acc;
         }
-        unsigned long long ball_elems = 0;
-        Kahan s, t0, t1, t2;
         __syncthreads();
         const int na = nanc;
         const int64_t L1 = seg[2 * na];
+        int64_t written = EMIT ? Bl.boff[a] - Bl.base : 0;
+        unsigned long long ball = 0;
         for (int64_t lo = 0; lo < ne; lo += pass_ids) {
             const int64_t hi = ne < lo + pass_ids ? ne : lo + pass_ids;
             const int nw = (int)((hi - lo + 31) >> 5);
@@ -218,18 +221,21 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_agents(LikTrace T, LikBatch
                 for (int64_t p = T.fo[y] + lane; p < f1; p += 32) mark(T.fc[p]);
                 const int64_t b1 = bwd_cut(T, y, ne);
                 for (int64_t p = T.bo[y] + lane; p < b1; p += 32) mark(T.bc[p]);
-                if (!ADJ && P.counters && lane == 0 && lo == 0)
+                if (!EMIT && lane == 0 && lo == 0)
                     atomicAdd(&adj_read, (unsigned long long)((f1 - T.fo[y]) + (b1 - T.bo[y])));
             }
             __syncthreads();
-            for (int i = tid; i < k; i += kLikThreads) {
-                const int64_t c = cid[i];
-                if (c >= lo && c < hi) {
-                    const int64_t o = c - lo;
-                    if ((bits[o >> 5] >> (o & 31)) & 1u) flag[i] = 1;
+            if (EMIT) {
+                for (int i = tid; i < k; i += kLikThreads) {
+                    const int64_t c = T.cites[c0 + i];
+                    if (c >= lo && c < hi) {
+                        const int64_t o = c - lo;
+                        Bl.cflag[c0 + i] = (uint8_t)((bits[o >> 5] >> (o & 31)) & 1u);
+                    }
                 }
             }
-            // compact the set bits into windows of ids; every point sums the window's weights
+            // each thread owns a contiguous run of words; a block scan of their popcounts places
+            // its ids so the ball comes out ascending
             const int wpt = (nw + kLikThreads - 1) / kLikThreads;
             const int w0 = tid * wpt < nw ? tid * wpt : nw;
             const int w1 = w0 + wpt < nw ? w0 + wpt : nw;
@@ -237,130 +243,161 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_agents(LikTrace T, LikBatch
             for (int w = w0; w < w1; ++w) cnt += __popc(bits[w]);
             int total = 0;
             const int off = block_excl_scan<int>(cnt, scan_ws, &total);
-            ball_elems += (unsigned long long)total;
-            for (int base = 0; base < total; base += kLikList) {
-                if (cnt > 0 && off + cnt > base && off < base + kLikList) {
-                    int r = off;
-                    for (int w = w0; w < w1 && r < base + kLikList; ++w) {
-                        uint32_t m = bits[w];
-                        while (m) {
-                            const int bit = __ffs(m) - 1;
-                            m &= m - 1u;
-                            if (r >= base && r < base + kLikList)
-                                list[r - base] = (int32_t)(lo + ((int64_t)w << 5) + bit);
-                            ++r;
-                        }
+            if (EMIT && cnt > 0) {
+                int32_t* out = Bl.ids + written + off;
+                int r = 0;
+                for (int w = w0; w < w1; ++w) {
+                    uint32_t m = bits[w];
+                    while (m) {
+                        const int bit = __ffs(m) - 1;
+                        m &= m - 1u;
+                        out[r++] = (int32_t)(lo + ((int64_t)w << 5) + bit);
                     }
                 }
-                __syncthreads();
-                const int cw = total - base < kLikList ? total - base : kLikList;
-                if (b < B) {
-                    for (int i = sub; i < cw; i += nsub) {
-                        const float4 f = F[list[i]];
-                        const float w = expf_pg(lik_x(f, al, ga, itau));
-                        kadd(s, w);
-                        if (ADJ) {
-                            kadd(t0, w * f.y);
-                            kadd(t1, w * f.z);
-                            kadd(t2, w * f.x);
-                        }
-                    }
-                }
-                __syncthreads();
             }
+            written += total;
+            ball += (unsigned long long)total;
+            __syncthreads();  // the bitmap is cleared by the next pass
         }
-        red[tid * 4 + 0] = kval(s);
-        red[tid * 4 + 1] = kval(t0);
-        red[tid * 4 + 2] = kval(t1);
-        red[tid * 4 + 3] = kval(t2);
-        __syncthreads();
-        if (!ADJ && P.counters && tid == 0) {
-            atomicAdd(&P.counters[0], ball_elems);
-            atomicAdd(&P.counters[1], adj_read);
-            atomicAdd(&P.counters[2], (unsigned long long)k);
-        }
-        if (tid < B) {
-            double acc[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int q = 0; q < nsub; ++q)
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) acc[kk] += red[(q * BE + tid) * 4 + kk];
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk) sums[tid * 4 + kk] = acc[kk];
+        if (!EMIT && tid == 0) {
+            Bl.cnt[a] = (int64_t)ball;
+            Bl.adj[a] = (int64_t)adj_read;
         }
         __syncthreads();
-        // citations in draw order, one warp per point
-        for (int bb = warp; bb < B; bb += kLikThreads / 32) {
-            const double beta = P.theta[bb * 4 + 3], tau = P.theta[bb * 4 + 1];
-            const float alb = (float)P.theta[bb * 4], gab = (float)P.theta[bb * 4 + 2],
-                        itb = (float)(1.0 / tau);
-            const double lbe = log_pg(beta), ibe = 1.0 / beta, itau2 = 1.0 / (tau * tau);
-            const double S = sums[bb * 4];
-            double Z;
-            double dz[4] = {0.0, 0.0, 0.0, 0.0};
-            if (!ADJ) {
-                Z = P.zglob[e * B + bb] + (beta - 1.0) * S;
-                if (lane == 0) P.zagent[a * B + bb] = Z;
-            } else {
-                Z = P.zagent[a * B + bb];
-                const double* gg = P.gglob + ((int64_t)e * B + bb) * 3;
-                dz[0] = gg[0] + (beta - 1.0) * sums[bb * 4 + 1];
-                dz[1] = gg[1] + (beta - 1.0) * (sums[bb * 4 + 2] * itau2);
-                dz[2] = gg[2] + (beta - 1.0) * sums[bb * 4 + 3];
-                dz[3] = S;
-            }
-            double carry = 0.0, l = 0.0;
-            double dcarry[4] = {0.0, 0.0, 0.0, 0.0}, g[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int i0 = 0; i0 < k; i0 += 32) {
-                const int i = i0 + lane;
-                const bool v = i < k;
-                double W = 0.0, x64 = 0.0;
-                double gk[4] = {0.0, 0.0, 0.0, 0.0};
-                if (v) {
-                    const float4 f = F[cid[i]];
-                    const float x = lik_x(f, alb, gab, itb);
-                    const float w = expf_pg(x);
-                    const bool in = flag[i] != 0;
-                    W = in ? (double)w * beta : (double)w;
-                    x64 = in ? (double)x + lbe : (double)x;
-                    gk[0] = f.y;
-                    gk[1] = (double)f.z * itau2;
-                    gk[2] = f.x;
-                    gk[3] = in ? ibe : 0.0;
-                }
-                const double incl = warp_incl_scan(W);
-                double excl = __shfl_up_sync(0xffffffffu, incl, 1);
-                if (lane == 0) excl = 0.0;
-                double D = Z - (carry + excl);
-                if (D < W) D = W;
-                if (v && !(D > 0.0)) {
-                    atomicOr(P.error, 2u);
-                    D = 1.0;
-                }
-                if (v) l += x64 - log_pg(D);
+    }
+}
+
+// Forward (ADJ = false) or adjoint pass over agents [a0, a1) whose balls are in Bl.  One warp per
+// (agent, group of up to 32 points): lane = point p + BW * slice; the slices split the ball, so a
+// batch of 32+ points keeps every lane on its own point and a single point spreads its ball over
+// the whole warp.  Ball sums: fp32 weights, compensated fp32 per lane, FP64 across slices.  The
+// citations are then walked in draw order by the slice-0 lane of each point with FP64 running
+// sums:  D_i = Z_a - P_i,  log D_i = log Z_a + log(1 - P_i / Z_a),  and in the adjoint
+// g_i - (dZ_a - dP_i) / D_i.
+template <bool ADJ>
+__global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P, LikBalls Bl,
+                                                          int64_t a0, int64_t a1) {
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int BW = P.BW, SL = 32 / BW;
+    const int groups = (P.B + BW - 1) / BW;
+    const int pl = lane & (BW - 1), sl = lane / BW;
+    const int64_t items = (a1 - a0) * groups;
+    for (int64_t it = wid; it < items; it += nwarps) {
+        const int64_t a = a0 + it / groups;
+        const int b = (int)(it % groups) * BW + pl;
+        const bool active = b < P.B;
+        const double* pp = P.pp + (active ? b : 0) * 8;
+        const float al = (float)pp[0], itau = (float)pp[1], ga = (float)pp[2];
+        const int e = T.agent_epoch[a];
+        const float4* F = T.feat + (int64_t)e * T.n;
+        const int64_t j0 = Bl.boff[a] - Bl.base, j1 = Bl.boff[a + 1] - Bl.base;
+        Kahan s, t0, t1, t2;
+        if (active) {
+            int64_t q = j0 + sl;
+            for (; q + 3 * SL < j1; q += 4 * SL) {
+                const int32_t i0 = Bl.ids[q], i1 = Bl.ids[q + SL], i2 = Bl.ids[q + 2 * SL],
+                              i3 = Bl.ids[q + 3 * SL];
+                const float4 f0 = F[i0], f1 = F[i1], f2 = F[i2], f3 = F[i3];
+                const float w0 = expf_pg(lik_x(f0, al, ga, itau)), w1 = expf_pg(lik_x(f1, al, ga, itau)),
+                            w2 = expf_pg(lik_x(f2, al, ga, itau)), w3 = expf_pg(lik_x(f3, al, ga, itau));
+                kadd(s, w0);
+                kadd(s, w1);
+                kadd(s, w2);
+                kadd(s, w3);
                 if (ADJ) {
-#pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) {
-                        const double ik = warp_incl_scan(W * gk[kk]);
-                        double ek = __shfl_up_sync(0xffffffffu, ik, 1);
-                        if (lane == 0) ek = 0.0;
-                        if (v) g[kk] += gk[kk] - (dz[kk] - (dcarry[kk] + ek)) / D;
-                        dcarry[kk] += __shfl_sync(0xffffffffu, ik, 31);
-                    }
+                    kadd(t0, w0 * f0.y);
+                    kadd(t0, w1 * f1.y);
+                    kadd(t0, w2 * f2.y);
+                    kadd(t0, w3 * f3.y);
+                    kadd(t1, w0 * f0.z);
+                    kadd(t1, w1 * f1.z);
+                    kadd(t1, w2 * f2.z);
+                    kadd(t1, w3 * f3.z);
+                    kadd(t2, w0 * f0.x);
+                    kadd(t2, w1 * f1.x);
+                    kadd(t2, w2 * f2.x);
+                    kadd(t2, w3 * f3.x);
                 }
-                carry += __shfl_sync(0xffffffffu, incl, 31);
             }
-            if (!ADJ) {
-                l = warp_sum(l);
-                if (lane == 0) P.out[a * B + bb] = l;
-            } else {
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) g[kk] = warp_sum(g[kk]);
-                if (lane == 0)
-#pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) P.out[(a * B + bb) * 4 + kk] = g[kk];
+            for (; q < j1; q += SL) {
+                const float4 f = F[Bl.ids[q]];
+                const float w = expf_pg(lik_x(f, al, ga, itau));
+                kadd(s, w);
+                if (ADJ) {
+                    kadd(t0, w * f.y);
+                    kadd(t1, w * f.z);
+                    kadd(t2, w * f.x);
+                }
             }
         }
-        __syncthreads();  // shared buffers are reused by the next agent
+        double S = kval(s), T0 = kval(t0), T1 = kval(t1), T2 = kval(t2);
+        for (int o = BW; o < 32; o <<= 1) {
+            S += __shfl_xor_sync(0xffffffffu, S, o);
+            if (ADJ) {
+                T0 += __shfl_xor_sync(0xffffffffu, T0, o);
+                T1 += __shfl_xor_sync(0xffffffffu, T1, o);
+                T2 += __shfl_xor_sync(0xffffffffu, T2, o);
+            }
+        }
+        if (!active || sl != 0) continue;
+        const double beta = pp[3], lbe = pp[4], ibe = pp[5], itau2 = pp[6];
+        const int64_t c0 = T.coff[a];
+        const int k = (int)(T.coff[a + 1] - c0);
+        double Z;
+        double dz[4] = {0.0, 0.0, 0.0, 0.0};
+        if (!ADJ) {
+            Z = P.zglob[e * P.B + b] + (beta - 1.0) * S;
+            P.zagent[a * P.B + b] = Z;
+        } else {
+            Z = P.zagent[a * P.B + b];
+            const double* gg = P.gglob + ((int64_t)e * P.B + b) * 3;
+            dz[0] = gg[0] + (beta - 1.0) * T0;
+            dz[1] = gg[1] + (beta - 1.0) * (T1 * itau2);
+            dz[2] = gg[2] + (beta - 1.0) * T2;
+            dz[3] = S;
+        }
+        if (!(Z > 0.0)) {
+            atomicOr(P.error, 2u);
+            continue;
+        }
+        const double logZ = ADJ ? 0.0 : log_pg(Z), invZ = 1.0 / Z;
+        double Pc = 0.0, l = 0.0;
+        double dP[4] = {0.0, 0.0, 0.0, 0.0}, g[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int i = 0; i < k; ++i) {
+            const bool in = Bl.cflag[c0 + i] != 0;
+            const float4 f = F[T.cites[c0 + i]];
+            const float x = lik_x(f, al, ga, itau);
+            const float w = expf_pg(x);
+            const double W = in ? (double)w * beta : (double)w;
+            if (!ADJ) {
+                // log D_i - log Z_a = log(1 - u), u = P_i / Z_a in [0, 1)
+                const double u = Pc * invZ;
+                double lr;
+                if (u < 0.5)
+                    lr = (double)log1m_pg((float)u);
+                else
+                    lr = log_pg(Z - Pc) - logZ;
+                l += (in ? (double)x + lbe : (double)x) - (logZ + lr);
+            } else {
+                const double D = Z - Pc;
+                const double id = 1.0 / (D > W ? D : W);
+                const double gk[4] = {(double)f.y, (double)f.z * itau2, (double)f.x, in ? ibe : 0.0};
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    g[kk] += gk[kk] - (dz[kk] - dP[kk]) * id;
+                    dP[kk] += W * gk[kk];
+                }
+            }
+            Pc += W;
+        }
+        if (!ADJ) {
+            P.out[a * P.B + b] = l;
+        } else {
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) P.out[(a * P.B + b) * 4 + kk] = g[kk];
+        }
     }
 }
 
@@ -380,24 +417,64 @@ __global__ void __launch_bounds__(256) k_lik_sum(const double* out, int64_t agen
     if (threadIdx.x == 0) res[b * K + kk] = r[0];
 }
 
-size_t lik_agent_smem(int bitmap_words) {
-    return sizeof(double) * (kLikThreads * 4 + kLikMaxB * 4) + sizeof(int32_t) * (kLikList + kKMax) +
-           sizeof(uint32_t) * (size_t)bitmap_words + kKMax;
+size_t lik_ball_smem(int bitmap_words) { return sizeof(uint32_t) * (size_t)bitmap_words; }
+
+cudaError_t init_lik_kernels(int bitmap_words, int* ball_per_sm, int* eval_per_sm) {
+    // eval_per_sm[0]: forward, [1]: adjoint
+    const int smem = (int)lik_ball_smem(bitmap_words);
+    cudaError_t e = cudaFuncSetAttribute(k_lik_ball<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_lik_ball<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int b0 = 1, b1 = 1, v0 = 1, v1 = 1;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_lik_ball<false>, kLikThreads, smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_lik_ball<true>, kLikThreads, smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v0, k_lik_eval<false>, kLikThreads, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v1, k_lik_eval<true>, kLikThreads, 0);
+    *ball_per_sm = b0 < b1 ? (b0 < 1 ? 1 : b0) : (b1 < 1 ? 1 : b1);
+    eval_per_sm[0] = v0 < 1 ? 1 : v0;
+    eval_per_sm[1] = v1 < 1 ? 1 : v1;
+    return e;
 }
 
-cudaError_t init_lik_kernels(int bitmap_words, int* blocks_per_sm) {
-    const int smem = (int)lik_agent_smem(bitmap_words);
-    cudaError_t e = cudaFuncSetAttribute(k_lik_agents<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_lik_agents<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    int b0 = 1, b1 = 1;
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_lik_agents<false>, kLikThreads, smem);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_lik_agents<true>, kLikThreads, smem);
-    const int b = b0 < b1 ? b0 : b1;
-    *blocks_per_sm = b < 1 ? 1 : b;
-    return e;
+void launch_lik_ball(const LikTrace& T, const LikBalls& Bl, int emit, int64_t a0, int64_t a1, int grid,
+                     cudaStream_t s) {
+    if (a1 <= a0) return;
+    int64_t g = a1 - a0 < grid ? a1 - a0 : grid;
+    const size_t smem = lik_ball_smem(T.bitmap_words);
+    if (emit)
+        k_lik_ball<true><<<(unsigned)g, kLikThreads, smem, s>>>(T, Bl, a0, a1);
+    else
+        k_lik_ball<false><<<(unsigned)g, kLikThreads, smem, s>>>(T, Bl, a0, a1);
+}
+
+void launch_lik_global(const LikTrace& T, const LikBatch& P, int adjoint, cudaStream_t s) {
+    const dim3 gg((unsigned)T.chunks, (unsigned)T.epochs);
+    const unsigned gs = (unsigned)((T.epochs * P.B + 127) / 128);
+    if (adjoint) {
+        k_lik_global<true><<<gg, kLikThreads, 0, s>>>(T, P);
+        k_lik_global_sum<true><<<gs, 128, 0, s>>>(T, P);
+    } else {
+        k_lik_global<false><<<gg, kLikThreads, 0, s>>>(T, P);
+        k_lik_global_sum<false><<<gs, 128, 0, s>>>(T, P);
+    }
+}
+
+void launch_lik_eval(const LikTrace& T, const LikBatch& P, const LikBalls& Bl, int adjoint, int64_t a0,
+                     int64_t a1, int grid, cudaStream_t s) {
+    if (a1 <= a0) return;
+    const int groups = (P.B + P.BW - 1) / P.BW;
+    const int64_t warps = (a1 - a0) * groups;
+    int64_t g = (warps + kLikThreads / 32 - 1) / (kLikThreads / 32);
+    if (g > grid) g = grid;
+    if (adjoint)
+        k_lik_eval<true><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+    else
+        k_lik_eval<false><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+}
+
+void launch_lik_sum(const LikTrace& T, const LikBatch& P, int adjoint, cudaStream_t s) {
+    const int K = adjoint ? 4 : 1;
+    k_lik_sum<<<(unsigned)(P.B * K), 256, 0, s>>>(P.out, T.agents, P.B, K, P.res);
 }
 
 void launch_lik_features(const LikTrace& T, int num_sms, cudaStream_t s) {
@@ -405,25 +482,6 @@ void launch_lik_features(const LikTrace& T, int num_sms, cudaStream_t s) {
     if (gx > (int64_t)num_sms * 8) gx = (int64_t)num_sms * 8;
     if (gx < 1) gx = 1;
     k_lik_features<<<dim3((unsigned)gx, (unsigned)T.epochs), 256, 0, s>>>(T);
-}
-
-void launch_lik(const LikTrace& T, const LikBatch& P, int adjoint, int agent_grid, cudaStream_t s) {
-    const dim3 gg((unsigned)T.chunks, (unsigned)T.epochs);
-    const unsigned gs = (unsigned)((T.epochs * P.B + 127) / 128);
-    const size_t smem = lik_agent_smem(T.bitmap_words);
-    int64_t ga = T.agents < agent_grid ? T.agents : agent_grid;
-    if (ga < 1) ga = 1;
-    const int K = adjoint ? 4 : 1;
-    if (adjoint) {
-        k_lik_global<true><<<gg, kLikThreads, 0, s>>>(T, P);
-        k_lik_global_sum<true><<<gs, 128, 0, s>>>(T, P);
-        k_lik_agents<true><<<(unsigned)ga, kLikThreads, smem, s>>>(T, P);
-    } else {
-        k_lik_global<false><<<gg, kLikThreads, 0, s>>>(T, P);
-        k_lik_global_sum<false><<<gs, 128, 0, s>>>(T, P);
-        k_lik_agents<false><<<(unsigned)ga, kLikThreads, smem, s>>>(T, P);
-    }
-    k_lik_sum<<<(unsigned)(P.B * K), 256, 0, s>>>(P.out, T.agents, P.B, K, P.res);
 }
 
 }  // namespace pg

@@ -43,8 +43,11 @@ struct LikTrace {
 
 struct LikBatch {
     int32_t B;           // points in this launch (<= kLikMaxB)
-    int32_t BE;          // B rounded up to a power of two: threads per point group
+    int32_t BE;          // global pass: B rounded up to a power of two (threads per node slice)
+    int32_t BW;          // agent pass: points per warp, min(32, B) rounded up to a power of two
+    int32_t pad;
     const double* theta; // [B][4] alpha, tau, gamma, beta
+    const double* pp;    // [B][8] alpha, 1/tau, gamma, beta, log beta, 1/beta, 1/tau^2, tau
     double* zglob;       // [epochs][B]      sum_{j<n_e} w_j          (forward writes)
     double* gglob;       // [epochs][B][3]   sum_j w_j dlog w_j/dtheta (adjoint writes)
     double* gpart;       // [epochs][chunks][B][4] partial sums of the global pass
@@ -52,14 +55,31 @@ struct LikBatch {
     double* out;         // [agents][B][1|4] per-agent log-likelihood or gradient
     double* res;         // [B][1|4]         totals
     uint32_t* error;     // bit 2: a normaliser was not positive
-    unsigned long long* counters;  // forward, first group only (else null): ball elements,
-                                   // adjacency entries read, citations
 };
 
-size_t lik_agent_smem(int bitmap_words);
-cudaError_t init_lik_kernels(int bitmap_words, int* blocks_per_sm);
+// Agents' 2-hop balls, built once per trace when they fit in memory (else per chunk of agents and
+// pass).  Ids of a ball are ascending.
+struct LikBalls {
+    const int64_t* boff;  // [agents + 1] offsets into the concatenation of all balls
+    int64_t base;         // boff of the first agent whose ball is in ids
+    int32_t* ids;         // ball ids of agents [a0, a1) at boff[a] - base
+    uint8_t* cflag;       // [citations] 1 when the cited node is in the citing agent's ball
+    int64_t* cnt;         // [agents] ball sizes (count pass)
+    int64_t* adj;         // [agents] adjacency entries read to build each ball (count pass)
+};
+
+size_t lik_ball_smem(int bitmap_words);
+// resident CTAs per SM: ball kernels (*ball_per_sm), forward and adjoint pass (eval_per_sm[2])
+cudaError_t init_lik_kernels(int bitmap_words, int* ball_per_sm, int* eval_per_sm);
 void launch_lik_features(const LikTrace& T, int num_sms, cudaStream_t s);
-// adjoint = 0: forward (Z_glob, per-agent Z_a and log-likelihood); 1: adjoint (gradient)
-void launch_lik(const LikTrace& T, const LikBatch& P, int adjoint, int agent_grid, cudaStream_t s);
+// emit = 0: ball sizes into Bl.cnt / Bl.adj; 1: ball ids and citation flags
+void launch_lik_ball(const LikTrace& T, const LikBalls& Bl, int emit, int64_t a0, int64_t a1, int grid,
+                     cudaStream_t s);
+// per-epoch sums: forward Z_glob, adjoint dZ_glob
+void launch_lik_global(const LikTrace& T, const LikBatch& P, int adjoint, cudaStream_t s);
+// per-agent pass over agents [a0, a1) (their balls in Bl)
+void launch_lik_eval(const LikTrace& T, const LikBatch& P, const LikBalls& Bl, int adjoint, int64_t a0,
+                     int64_t a1, int grid, cudaStream_t s);
+void launch_lik_sum(const LikTrace& T, const LikBatch& P, int adjoint, cudaStream_t s);
 
 }  // namespace pg

@@ -118,3 +118,17 @@ def test_ball_bitmap_in_several_passes(gpu):
     assert (np.abs(ll - llo) / np.abs(llo)).max() <= 1e-7
     rel = np.linalg.norm(gr - gro, axis=1) / np.linalg.norm(gro, axis=1)
     assert rel[0] <= 1e-5 and rel[1] <= 1e-6, rel
+
+
+def test_ball_chunks_rebuilt_per_pass_give_identical_results(trace_mid):
+    """Balls kept for all agents at once, or rebuilt chunk by chunk in every pass (what a trace too
+    large for memory does): the per-agent arithmetic is the same, so the results are bitwise equal."""
+    pts = W.theta_batch(5, seed=4)
+    with GrowthEngine(seed=1) as a, GrowthEngine(seed=1) as b:
+        a.load_trace(trace_mid)
+        b.set_tuning(lik_chunk_agents=700)
+        b.load_trace(trace_mid)
+        la, lb = a.loglik(pts), b.loglik(pts)
+        ga, gb = a.loglik_grad(pts), b.loglik_grad(pts)
+    np.testing.assert_array_equal(la, lb)
+    np.testing.assert_array_equal(ga, gb)
