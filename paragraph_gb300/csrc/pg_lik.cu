@@ -3,25 +3,32 @@
 // this is the density of the sampling law the growth step draws from
 // (w_j beta^[j in N_a], successive sampling without replacement).
 //
+// Weights: w_j = 2^(x2_j), x2_j = log2(e) (gamma log f_j + alpha log(indeg_j+1) - (t-t_j)/tau) in
+// fp32 (per-point constants pre-multiplied by log2 e), evaluated by the special-function unit
+// (PTX ex2.approx.ftz.f32, relative error < 2^-22; results below 2^-126 flush to zero).  The same
+// weight function feeds every sum below, so the normalisers and the citations' prefix sums agree.
+//
 // Per launch (forward or adjoint):
 //   k_lik_global      per epoch: sum_{j<n_e} w_j (forward) or sum_j w_j g_j (adjoint), one CTA per
-//                     4096-node chunk; fp32 weights, compensated fp32 sums per thread, FP64 across
-//                     threads and chunks (fixed order, so results are reproducible).
+//                     4096-node chunk; compensated fp32 sums per thread, FP64 across threads and
+//                     chunks (fixed order, so results are reproducible).
 //   k_lik_global_sum  chunks -> one FP64 value per (epoch, point).
-//   k_lik_agents      one CTA per agent (static assignment): builds the agent's 2-hop ball as a
-//                     bitmap over [0, n_e) in shared memory (passes of 786,432 ids), compacts it
-//                     into windows of ids, and every point sums its ball weights S_a (adjoint: also
-//                     sum w g) -- the ball is built once for all points of the batch.  Then one
-//                     warp per point walks the agent's citations in draw order with FP64 prefix
-//                     scans: D_i = Z_a - sum_{l<i} W_{c_l}, log-likelihood sum x_i - log D_i, and
-//                     in the adjoint g_i - (dZ_a - dP_i) / D_i.  The adjoint recomputes every
-//                     weight and reads only the forward's per-agent Z_a.
+//   k_lik_ball        (once per trace, or per chunk of agents and pass) the agent's 2-hop ball as
+//                     a bitmap over [0, n_e) in shared memory, compacted to ascending ids.
+//   k_lik_eval        one warp per agent and group of points: every point sums its ball weights
+//                     S_a (adjoint: also sum w g), reading each ball element once for all the
+//                     warp's points.  Then the citations are walked in draw order with FP64 running
+//                     sums: D_i = Z_a - sum_{l<i} W_{c_l}, log-likelihood sum x_i - log D_i, and in
+//                     the adjoint g_i - (dZ_a - dP_i) / D_i.  The adjoint recomputes every weight and
+//                     reads only the forward's per-agent Z_a.
 //   k_lik_sum         agents -> totals per point (fixed order).
 #include "pg_lik.cuh"
 
 namespace pg {
 
 namespace {
+
+constexpr double kLn2d = 0x1.62e42fefa39efp-1;
 
 struct Kahan {
     float s = 0.f, c = 0.f;
@@ -49,8 +56,39 @@ __device__ __forceinline__ int64_t bwd_cut(const LikTrace& T, int64_t x, int64_t
     return lo;
 }
 
-__device__ __forceinline__ float lik_x(const float4 f, float al, float ga, float itau) {
-    return ga * f.x + al * f.y - f.z * itau;
+// 2^x on the special-function unit (PTX ex2.approx.ftz.f32).
+__device__ __forceinline__ float ex2_sfu(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Per-point constants of the weight exponent in base 2.
+struct LikC {
+    float al2, ga2, it2;  // alpha log2 e, gamma log2 e, log2 e / tau
+};
+__device__ __forceinline__ LikC lik_c(const double* pp) {
+    LikC c;
+    c.al2 = (float)(pp[0] * kLog2e);
+    c.ga2 = (float)(pp[2] * kLog2e);
+    c.it2 = (float)(pp[1] * kLog2e);
+    return c;
+}
+// x2 = log2 of the weight: ga2 log f + al2 log(d+1) - it2 (t - t_j)
+__device__ __forceinline__ float lik_x2(const float4 f, const LikC& c) {
+    return __fmaf_rn(c.ga2, f.x, __fmaf_rn(c.al2, f.y, -(f.z * c.it2)));
+}
+
+// 1/D for D > 0 in FP64: Newton's iteration for the reciprocal, r' = r + r (1 - D r), started from
+// the fp32 reciprocal of the special-function unit (relative error < 2^-22); one step squares the
+// error (< 2^-44).  Outside the fp32 normal range the plain FP64 division is used.
+__device__ __forceinline__ double recip_nr(double D) {
+    if (!(D > 1e-30 && D < 1e30)) return 1.0 / D;
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"((float)D));
+    const double r = (double)rf;
+    const double e = __fma_rn(-D, r, 1.0);
+    return __fma_rn(r, e, r);
 }
 
 // log(1 - u) for u in [0, 0.5): -2 atanh(t), t = u / (2 - u) in [0, 1/3), by the odd Taylor series
@@ -99,13 +137,12 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_global(LikTrace T, LikBatch
     const int b = tid & (BE - 1), sub = tid / BE, nsub = kLikThreads / BE;
     Kahan s, t0, t1, t2;
     if (b < B && lo < ne) {
-        const float al = (float)P.theta[b * 4], itau = (float)(1.0 / P.theta[b * 4 + 1]),
-                    ga = (float)P.theta[b * 4 + 2];
+        const LikC c = lik_c(P.pp + b * 8);
         const int64_t hi = ne < lo + kLikChunk ? ne : lo + kLikChunk;
         const float4* F = T.feat + (int64_t)e * T.n;
         for (int64_t j = lo + sub; j < hi; j += nsub) {
             const float4 f = F[j];
-            const float w = expf_pg(lik_x(f, al, ga, itau));
+            const float w = ex2_sfu(lik_x2(f, c));
             kadd(s, w);
             if (ADJ) {
                 kadd(t0, w * f.y);
@@ -268,135 +305,139 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_ball(LikTrace T, LikBalls B
 }
 
 // Forward (ADJ = false) or adjoint pass over agents [a0, a1) whose balls are in Bl.  One warp per
-// (agent, group of up to 32 points): lane = point p + BW * slice; the slices split the ball, so a
-// batch of 32+ points keeps every lane on its own point and a single point spreads its ball over
-// the whole warp.  Ball sums: fp32 weights, compensated fp32 per lane, FP64 across slices.  The
-// citations are then walked in draw order by the slice-0 lane of each point with FP64 running
-// sums:  D_i = Z_a - P_i,  log D_i = log Z_a + log(1 - P_i / Z_a),  and in the adjoint
-// g_i - (dZ_a - dP_i) / D_i.
-template <bool ADJ>
+// (agent, group of points).  NP = 2 (33..64 points): lane l holds points l and l + 32, and every lane
+// walks the whole ball, so each ball element is read once for all points.  NP = 1 (<= 32 points):
+// lane = point p + BW * slice; the slices split the ball, so a single point spreads its ball over
+// the whole warp.  Ball sums: fp32 weights, four elements summed pairwise, then compensated fp32
+// per lane, FP64 across slices.  The citations are then walked in draw order by the slice-0 lane
+// of each point with FP64 running sums:  D_i = Z_a - P_i,  log D_i = log Z_a + log(1 - P_i / Z_a),
+// and in the adjoint g_i - (dZ_a - dP_i) / D_i.
+template <bool ADJ, int NP>
 __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P, LikBalls Bl,
                                                           int64_t a0, int64_t a1) {
     const int lane = threadIdx.x & 31;
     const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int BW = P.BW, SL = 32 / BW;
-    const int groups = (P.B + BW - 1) / BW;
+    const int BW = NP == 2 ? 32 : P.BW, SL = 32 / BW;
+    const int groups = NP == 2 ? 1 : (P.B + BW - 1) / BW;
     const int pl = lane & (BW - 1), sl = lane / BW;
     const int64_t items = (a1 - a0) * groups;
     for (int64_t it = wid; it < items; it += nwarps) {
         const int64_t a = a0 + it / groups;
-        const int b = (int)(it % groups) * BW + pl;
-        const bool active = b < P.B;
-        const double* pp = P.pp + (active ? b : 0) * 8;
-        const float al = (float)pp[0], itau = (float)pp[1], ga = (float)pp[2];
+        int bq[NP];
+        bool act[NP];
+        LikC cq[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            bq[p] = NP == 2 ? lane + 32 * p : (int)(it % groups) * BW + pl;
+            act[p] = bq[p] < P.B;
+            cq[p] = lik_c(P.pp + (act[p] ? bq[p] : 0) * 8);
+        }
         const int e = T.agent_epoch[a];
         const float4* F = T.feat + (int64_t)e * T.n;
         const int64_t j0 = Bl.boff[a] - Bl.base, j1 = Bl.boff[a + 1] - Bl.base;
-        Kahan s, t0, t1, t2;
-        if (active) {
-            int64_t q = j0 + sl;
-            for (; q + 3 * SL < j1; q += 4 * SL) {
-                const int32_t i0 = Bl.ids[q], i1 = Bl.ids[q + SL], i2 = Bl.ids[q + 2 * SL],
-                              i3 = Bl.ids[q + 3 * SL];
-                const float4 f0 = F[i0], f1 = F[i1], f2 = F[i2], f3 = F[i3];
-                const float w0 = expf_pg(lik_x(f0, al, ga, itau)), w1 = expf_pg(lik_x(f1, al, ga, itau)),
-                            w2 = expf_pg(lik_x(f2, al, ga, itau)), w3 = expf_pg(lik_x(f3, al, ga, itau));
-                kadd(s, w0);
-                kadd(s, w1);
-                kadd(s, w2);
-                kadd(s, w3);
+        Kahan s[NP], t0[NP], t1[NP], t2[NP];
+        int64_t q = j0 + sl;
+        for (; q + 3 * SL < j1; q += 4 * SL) {
+            const int32_t i0 = Bl.ids[q], i1 = Bl.ids[q + SL], i2 = Bl.ids[q + 2 * SL], i3 = Bl.ids[q + 3 * SL];
+            const float4 f0 = F[i0], f1 = F[i1], f2 = F[i2], f3 = F[i3];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const float w0 = ex2_sfu(lik_x2(f0, cq[p])), w1 = ex2_sfu(lik_x2(f1, cq[p])),
+                            w2 = ex2_sfu(lik_x2(f2, cq[p])), w3 = ex2_sfu(lik_x2(f3, cq[p]));
+                kadd(s[p], (w0 + w1) + (w2 + w3));
                 if (ADJ) {
-                    kadd(t0, w0 * f0.y);
-                    kadd(t0, w1 * f1.y);
-                    kadd(t0, w2 * f2.y);
-                    kadd(t0, w3 * f3.y);
-                    kadd(t1, w0 * f0.z);
-                    kadd(t1, w1 * f1.z);
-                    kadd(t1, w2 * f2.z);
-                    kadd(t1, w3 * f3.z);
-                    kadd(t2, w0 * f0.x);
-                    kadd(t2, w1 * f1.x);
-                    kadd(t2, w2 * f2.x);
-                    kadd(t2, w3 * f3.x);
-                }
-            }
-            for (; q < j1; q += SL) {
-                const float4 f = F[Bl.ids[q]];
-                const float w = expf_pg(lik_x(f, al, ga, itau));
-                kadd(s, w);
-                if (ADJ) {
-                    kadd(t0, w * f.y);
-                    kadd(t1, w * f.z);
-                    kadd(t2, w * f.x);
+                    kadd(t0[p], __fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
+                    kadd(t1[p], __fmaf_rn(w3, f3.z, __fmaf_rn(w2, f2.z, __fmaf_rn(w1, f1.z, w0 * f0.z))));
+                    kadd(t2[p], __fmaf_rn(w3, f3.x, __fmaf_rn(w2, f2.x, __fmaf_rn(w1, f1.x, w0 * f0.x))));
                 }
             }
         }
-        double S = kval(s), T0 = kval(t0), T1 = kval(t1), T2 = kval(t2);
-        for (int o = BW; o < 32; o <<= 1) {
-            S += __shfl_xor_sync(0xffffffffu, S, o);
-            if (ADJ) {
-                T0 += __shfl_xor_sync(0xffffffffu, T0, o);
-                T1 += __shfl_xor_sync(0xffffffffu, T1, o);
-                T2 += __shfl_xor_sync(0xffffffffu, T2, o);
+        for (; q < j1; q += SL) {
+            const float4 f = F[Bl.ids[q]];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const float w = ex2_sfu(lik_x2(f, cq[p]));
+                kadd(s[p], w);
+                if (ADJ) {
+                    kadd(t0[p], w * f.y);
+                    kadd(t1[p], w * f.z);
+                    kadd(t2[p], w * f.x);
+                }
             }
         }
-        if (!active || sl != 0) continue;
-        const double beta = pp[3], lbe = pp[4], ibe = pp[5], itau2 = pp[6];
-        const int64_t c0 = T.coff[a];
-        const int k = (int)(T.coff[a + 1] - c0);
-        double Z;
-        double dz[4] = {0.0, 0.0, 0.0, 0.0};
-        if (!ADJ) {
-            Z = P.zglob[e * P.B + b] + (beta - 1.0) * S;
-            P.zagent[a * P.B + b] = Z;
-        } else {
-            Z = P.zagent[a * P.B + b];
-            const double* gg = P.gglob + ((int64_t)e * P.B + b) * 3;
-            dz[0] = gg[0] + (beta - 1.0) * T0;
-            dz[1] = gg[1] + (beta - 1.0) * (T1 * itau2);
-            dz[2] = gg[2] + (beta - 1.0) * T2;
-            dz[3] = S;
-        }
-        if (!(Z > 0.0)) {
-            atomicOr(P.error, 2u);
-            continue;
-        }
-        const double logZ = ADJ ? 0.0 : log_pg(Z), invZ = 1.0 / Z;
-        double Pc = 0.0, l = 0.0;
-        double dP[4] = {0.0, 0.0, 0.0, 0.0}, g[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int i = 0; i < k; ++i) {
-            const bool in = Bl.cflag[c0 + i] != 0;
-            const float4 f = F[T.cites[c0 + i]];
-            const float x = lik_x(f, al, ga, itau);
-            const float w = expf_pg(x);
-            const double W = in ? (double)w * beta : (double)w;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            double S = kval(s[p]), T0 = kval(t0[p]), T1 = kval(t1[p]), T2 = kval(t2[p]);
+            for (int o = BW; o < 32; o <<= 1) {
+                S += __shfl_xor_sync(0xffffffffu, S, o);
+                if (ADJ) {
+                    T0 += __shfl_xor_sync(0xffffffffu, T0, o);
+                    T1 += __shfl_xor_sync(0xffffffffu, T1, o);
+                    T2 += __shfl_xor_sync(0xffffffffu, T2, o);
+                }
+            }
+            if (!act[p] || sl != 0) continue;
+            const int b = bq[p];
+            const LikC c = cq[p];
+            const double* pp = P.pp + b * 8;
+            const double beta = pp[3], lbe = pp[4], ibe = pp[5], itau2 = pp[6];
+            const int64_t c0 = T.coff[a];
+            const int k = (int)(T.coff[a + 1] - c0);
+            double Z;
+            double dz[4] = {0.0, 0.0, 0.0, 0.0};
             if (!ADJ) {
-                // log D_i - log Z_a = log(1 - u), u = P_i / Z_a in [0, 1)
-                const double u = Pc * invZ;
-                double lr;
-                if (u < 0.5)
-                    lr = (double)log1m_pg((float)u);
-                else
-                    lr = log_pg(Z - Pc) - logZ;
-                l += (in ? (double)x + lbe : (double)x) - (logZ + lr);
+                Z = P.zglob[e * P.B + b] + (beta - 1.0) * S;
+                P.zagent[a * P.B + b] = Z;
             } else {
-                const double D = Z - Pc;
-                const double id = 1.0 / (D > W ? D : W);
-                const double gk[4] = {(double)f.y, (double)f.z * itau2, (double)f.x, in ? ibe : 0.0};
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) {
-                    g[kk] += gk[kk] - (dz[kk] - dP[kk]) * id;
-                    dP[kk] += W * gk[kk];
-                }
+                Z = P.zagent[a * P.B + b];
+                const double* gg = P.gglob + ((int64_t)e * P.B + b) * 3;
+                dz[0] = gg[0] + (beta - 1.0) * T0;
+                dz[1] = gg[1] + (beta - 1.0) * (T1 * itau2);
+                dz[2] = gg[2] + (beta - 1.0) * T2;
+                dz[3] = S;
             }
-            Pc += W;
-        }
-        if (!ADJ) {
-            P.out[a * P.B + b] = l;
-        } else {
+            if (!(Z > 0.0)) {
+                atomicOr(P.error, 2u);
+                continue;
+            }
+            const double logZ = ADJ ? 0.0 : log_pg(Z), invZ = ADJ ? 0.0 : 1.0 / Z;
+            double Pc = 0.0, l = 0.0;
+            double dP[4] = {0.0, 0.0, 0.0, 0.0}, g[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int i = 0; i < k; ++i) {
+                const bool in = Bl.cflag[c0 + i] != 0;
+                const float4 f = F[T.cites[c0 + i]];
+                const float x2 = lik_x2(f, c);
+                const float w = ex2_sfu(x2);
+                const double W = in ? (double)w * beta : (double)w;
+                if (!ADJ) {
+                    // log D_i - log Z_a = log(1 - u), u = P_i / Z_a in [0, 1)
+                    const double u = Pc * invZ;
+                    double lr;
+                    if (u < 0.5)
+                        lr = (double)log1m_pg((float)u);
+                    else
+                        lr = log_pg(Z - Pc) - logZ;
+                    const double x = (double)x2 * kLn2d;
+                    l += (in ? x + lbe : x) - (logZ + lr);
+                } else {
+                    const double D = Z - Pc;
+                    const double id = recip_nr(D > W ? D : W);
+                    const double gk[4] = {(double)f.y, (double)f.z * itau2, (double)f.x, in ? ibe : 0.0};
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) P.out[(a * P.B + b) * 4 + kk] = g[kk];
+                    for (int kk = 0; kk < 4; ++kk) {
+                        g[kk] += gk[kk] - (dz[kk] - dP[kk]) * id;
+                        dP[kk] += W * gk[kk];
+                    }
+                }
+                Pc += W;
+            }
+            if (!ADJ) {
+                P.out[a * P.B + b] = l;
+            } else {
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) P.out[(a * P.B + b) * 4 + kk] = g[kk];
+            }
         }
     }
 }
@@ -428,8 +469,8 @@ cudaError_t init_lik_kernels(int bitmap_words, int* ball_per_sm, int* eval_per_s
     int b0 = 1, b1 = 1, v0 = 1, v1 = 1;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_lik_ball<false>, kLikThreads, smem);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_lik_ball<true>, kLikThreads, smem);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v0, k_lik_eval<false>, kLikThreads, 0);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v1, k_lik_eval<true>, kLikThreads, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v0, k_lik_eval<false, 2>, kLikThreads, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v1, k_lik_eval<true, 2>, kLikThreads, 0);
     *ball_per_sm = b0 < b1 ? (b0 < 1 ? 1 : b0) : (b1 < 1 ? 1 : b1);
     eval_per_sm[0] = v0 < 1 ? 1 : v0;
     eval_per_sm[1] = v1 < 1 ? 1 : v1;
@@ -462,14 +503,22 @@ void launch_lik_global(const LikTrace& T, const LikBatch& P, int adjoint, cudaSt
 void launch_lik_eval(const LikTrace& T, const LikBatch& P, const LikBalls& Bl, int adjoint, int64_t a0,
                      int64_t a1, int grid, cudaStream_t s) {
     if (a1 <= a0) return;
-    const int groups = (P.B + P.BW - 1) / P.BW;
+    const bool two = P.B > 32;
+    const int groups = two ? 1 : (P.B + P.BW - 1) / P.BW;
     const int64_t warps = (a1 - a0) * groups;
     int64_t g = (warps + kLikThreads / 32 - 1) / (kLikThreads / 32);
     if (g > grid) g = grid;
-    if (adjoint)
-        k_lik_eval<true><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
-    else
-        k_lik_eval<false><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+    if (adjoint) {
+        if (two)
+            k_lik_eval<true, 2><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+        else
+            k_lik_eval<true, 1><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+    } else {
+        if (two)
+            k_lik_eval<false, 2><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+        else
+            k_lik_eval<false, 1><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+    }
 }
 
 void launch_lik_sum(const LikTrace& T, const LikBatch& P, int adjoint, cudaStream_t s) {
