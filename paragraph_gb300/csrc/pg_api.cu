@@ -92,6 +92,7 @@ struct pg_ctx {
     DBuf<uint64_t> hmask;
     DBuf<float> fit, w;
     DBuf<uint64_t> cdf, tilesum, tileoff, tables;
+    DBuf<int32_t> guide;
     DBuf<int64_t> fwd_off, bwd_off[2], len_tmp, sort_small, sort_large, sort_large_off, eoff,
         blocksum, er_cnt, er_toff;
     DBuf<int32_t> fwd_col, bwd_col[2];
@@ -177,6 +178,7 @@ Arena make_arena(pg_ctx* c) {
     A.indeg = c->indeg.p;
     A.w = c->w.p;
     A.cdf = c->cdf.p;
+    A.guide = c->guide.p;
     A.inc = c->inc.p;
     A.fwd_off = c->fwd_off.p;
     A.fwd_col = c->fwd_col.p;
@@ -387,6 +389,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->inc, S));
     PG_CUDA(c, dalloc(c->w, S));
     PG_CUDA(c, dalloc(c->cdf, S));
+    PG_CUDA(c, dalloc(c->guide, S));
     PG_CUDA(c, dalloc(c->len_tmp, S));
     PG_CUDA(c, dalloc(c->sort_small, S));
     PG_CUDA(c, dalloc(c->sort_large, S));
@@ -538,9 +541,10 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
     launch_weights(A, s);
     PG_STAGE("weights");
     if (c->cfg.sampler == PG_SAMPLER_THINNING) {
+        launch_guide(A, s);
         launch_hubs(A, c->num_sms, s);
-        PG_STAGE("hub index");
-        c->launches += kHubKernels;
+        PG_STAGE("guide table and hub index");
+        c->launches += kThinKernels;
     }
     if (events) record_event(ev[1], s);
     launch_agent_setup(A, agents, s);
@@ -732,6 +736,7 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->fit);
     dfree(c->w);
     dfree(c->cdf);
+    dfree(c->guide);
     dfree(c->tilesum);
     dfree(c->tileoff);
     dfree(c->tables);

@@ -117,6 +117,7 @@ struct Arena {
     int32_t* indeg;
     float* w;
     uint64_t* cdf;
+    int32_t* guide;            // [slots] guide table of the CDF (thinning sampler)
     int32_t* inc;
     int64_t* fwd_off;
     int32_t* fwd_col;
@@ -155,6 +156,30 @@ struct Arena {
     int32_t tune_copy_ctas;    // backward-copy CTAs per SM
     int32_t rep_base;          // RNG replica index of replica 0 (pg_config.replica_base)
 };
+
+// Guide table of a replica's CDF (total Wq over n nodes): bucket g covers [g 2^gs, (g+1) 2^gs),
+// with gs the smallest shift that leaves at most n buckets, so there are more than n/2 of them and
+// a draw's answer lies between two adjacent guide entries a few CDF entries apart on average.
+PG_HD int bitlen_u64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+    return x ? 64 - __clzll((long long)x) : 0;
+#else
+    int b = 0;
+    while (x) {
+        ++b;
+        x >>= 1;
+    }
+    return b;
+#endif
+}
+PG_HD int guide_shift(uint64_t Wq, int64_t n) {
+    if (Wq <= 1) return 0;
+    const uint64_t top = Wq - 1, lim = (uint64_t)(n > 1 ? n - 1 : 0);
+    const int bt = bitlen_u64(top), bl = bitlen_u64(lim);
+    int s = bt > bl ? bt - bl : 0;
+    if ((top >> s) > lim) ++s;
+    return s;
+}
 
 // ---------------------------------------------------------------- warp helpers
 #if defined(__CUDACC__)
@@ -216,12 +241,14 @@ __device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64
 // Kernels one PA epoch enqueues: epoch begin (1), weights + CDF (4), agent setup + offset scan +
 // check (5), agent kernels (2), backward append incl. epoch end (8).
 constexpr int kPaEpochKernels = 20;
-// Extra kernels of the thinning sampler's hub index: histogram, pick, collect, mask, hub pairs.
-constexpr int kHubKernels = 5;
+// Extra kernels of the thinning sampler: the CDF's guide table (1) and the hub index (histogram,
+// pick, collect, mask, hub pairs).
+constexpr int kThinKernels = 6;
 void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s);
 void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cudaStream_t s);
 void launch_weights(const Arena& A, cudaStream_t s);
 void launch_hubs(const Arena& A, int num_sms, cudaStream_t s);
+void launch_guide(const Arena& A, cudaStream_t s);
 void launch_tile_scan(const Arena& A, int mode, cudaStream_t s);
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s);
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);

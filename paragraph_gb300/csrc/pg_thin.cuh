@@ -114,29 +114,82 @@ __device__ __forceinline__ bool in_z(const Ball& B, int32_t v) {
     return false;
 }
 
-// Warp-cooperative membership of one node j (warp-uniform argument and result); `examined` gets the
-// adjacency entries looked at, in order, up to and including the first hit.
-__device__ bool member_warp(const Ball& B, int32_t j, long long& examined) {
-    const int lane = lane_id();
+// Rows of at most this many entries (forward + backward) are tested by one lane; longer ones by
+// the whole warp.
+constexpr int kLaneRows = 32;
+
+// Membership of the lane's own candidate j, every lane at once.  `examined` gets the adjacency
+// entries looked at, in order (forward row, then backward row), up to and including the first hit.
+// When j is not in Z, not a hub and its rows are longer than kLaneRows, `decided` is false and the
+// answer comes from member_rows_warp.
+__device__ bool member_lane(const Ball& B, int32_t j, long long& examined, bool& decided) {
     examined = 0;
-    if (in_z(B, j)) return true;  // every lane evaluates the same thing
+    decided = true;
+    if (in_z(B, j)) return true;
     const int hs = hub_slot(B, j);
     if (hs >= 0) return mask_bit(B.hm, hs);
+    const int64_t f0 = B.fo[j], f1 = B.fo[j + 1], b0 = B.bo[j], b1 = B.bo[j + 1];
+    const int64_t nf = f1 - f0, d = nf + (b1 - b0);
+    if (d > kLaneRows) {
+        decided = false;
+        return false;
+    }
+    // four entries in flight per step; position q of the concatenated rows
+    for (int64_t q = 0; q < d; q += 4) {
+        int32_t v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t x = q + u;
+            v[u] = x < d ? (x < nf ? B.fc[f0 + x] : B.bc[b0 + (x - nf)]) : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (v[u] >= 0 && in_z(B, v[u])) {
+                examined = q + u + 1;
+                return true;
+            }
+    }
+    examined = d;
+    return false;
+}
+
+// Warp-cooperative row scan of a non-hub j outside Z (warp-uniform argument and result), 128
+// entries per step; `examined` as in member_lane.
+__device__ bool member_rows_warp(const Ball& B, int32_t j, long long& examined) {
+    const int lane = lane_id();
+    examined = 0;
     for (int dir = 0; dir < 2; ++dir) {
         const int64_t* off = dir ? B.bo : B.fo;
         const int32_t* col = dir ? B.bc : B.fc;
         const int64_t p0 = off[j], p1 = off[j + 1];
-        for (int64_t p = p0; p < p1; p += 32) {
-            const bool hit = (p + lane < p1) && in_z(B, col[p + lane]);
-            const unsigned m = __ballot_sync(kFull, hit);
-            if (m) {
-                examined += (p - p0) + __ffs(m);
-                return true;
+        for (int64_t p = p0; p < p1; p += 128) {
+            int32_t v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t x = p + 32 * u + lane;
+                v[u] = x < p1 ? col[x] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const unsigned m = __ballot_sync(kFull, v[u] >= 0 && in_z(B, v[u]));
+                if (m) {
+                    examined += (p + 32 * u - p0) + __ffs(m);
+                    return true;
+                }
             }
         }
         examined += p1 - p0;
     }
     return false;
+}
+
+// Warp-cooperative membership of one node j (warp-uniform argument and result).
+__device__ bool member_warp(const Ball& B, int32_t j, long long& examined) {
+    examined = 0;
+    if (in_z(B, j)) return true;  // every lane evaluates the same thing
+    const int hs = hub_slot(B, j);
+    if (hs >= 0) return mask_bit(B.hm, hs);
+    return member_rows_warp(B, j, examined);
 }
 
 template <int KCAP, int HCAP>
@@ -256,10 +309,15 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     int nch = 0;
     long long events = 0, tests = 0, scanned = 0;
     const int maxev = 64 * k + 256;
+    // guide table: the answer for y lies in [guide[g], guide[g + 1]], g = y >> gs
+    const int32_t* guide = A.guide + rp.nbase;
+    const int gs = guide_shift(Wq, n);
+    const int64_t used = Wq ? (int64_t)((Wq - 1) >> gs) + 1 : 0;
     for (int i0 = 0; i0 < maxev && nch < k; i0 += 32) {
         const u32x4 x = draw(A.seed, kStreamGlobal, rep, ep, unit, (uint32_t)(i0 + lane));
         const uint64_t y = mulhi64(u64of(x.x[0], x.x[1]), Wq);
-        int64_t lo = 0, hi = n - 1;
+        const int64_t g = (int64_t)(y >> gs);
+        int64_t lo = guide[g], hi = g + 1 < used ? guide[g + 1] : n - 1;
         while (lo < hi) {
             const int64_t mid = (lo + hi) >> 1;
             if (cdf[mid] > y)
@@ -269,6 +327,11 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
         }
         const int j = (int)lo;
         const bool glob = u01d(x.x[2], x.x[3]) <= pg;
+        // every boost candidate of the batch tested at once (a pure function of j, so testing
+        // events that end up unused changes nothing); long rows wait for the warp below
+        long long ex_l = 0;
+        bool dec_l = true, mem_l = true;
+        if (!glob) mem_l = member_lane(B, j, ex_l, dec_l);
         for (int l = 0; l < 32 && nch < k; ++l) {
             const int jl = __shfl_sync(kFull, j, l);
             const bool gl = __shfl_sync(kFull, glob, l);
@@ -278,8 +341,9 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             if (__any_sync(kFull, dup)) continue;
             if (!gl) {
                 ++tests;
-                long long ex;
-                const bool mem = member_warp(B, jl, ex);
+                long long ex = __shfl_sync(kFull, ex_l, l);
+                bool mem = __shfl_sync(kFull, mem_l, l);
+                if (!__shfl_sync(kFull, dec_l, l)) mem = member_rows_warp(B, jl, ex);
                 scanned += ex;
                 if (!mem) continue;
             }

@@ -156,6 +156,7 @@ __global__ void __launch_bounds__(kTileThreads) k_cdf_tiles(Arena A) {
     ulonglong2* dst = reinterpret_cast<ulonglong2*>(A.cdf + rp.nbase + vt);
     dst[0] = make_ulonglong2(ex + q[0], ex + q[1]);
     dst[1] = make_ulonglong2(ex + q[2], ex + q[3]);
+    *reinterpret_cast<int4*>(A.guide + rp.nbase + vt) = make_int4(0, 0, 0, 0);  // marks start at 0
     if (threadIdx.x == 0) A.tilesum[t] = tot;
 }
 
@@ -192,6 +193,8 @@ __global__ void __launch_bounds__(1024) k_tile_scan(Arena A, int mode) {
     for (int i = threadIdx.x; i < T; i += 1024) A.tileoff[i] -= A.tilesum[A.tile_rep[i]];
 }
 
+// Tile offsets into the CDF, and the guide table's marks: node v whose CDF interval
+// [cdf[v-1], cdf[v]) contains bucket starts g 2^gs marks the first of them, guide[g] = v.
 __global__ void __launch_bounds__(kTileThreads) k_cdf_add(Arena A) {
     if (A.st->error) return;
     const int t = blockIdx.x;
@@ -200,16 +203,91 @@ __global__ void __launch_bounds__(kTileThreads) k_cdf_add(Arena A) {
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
     if (v0 >= rp.n) return;
     const uint64_t off = A.tileoff[t];
-    if (off == 0) return;
     const int64_t vt = v0 + (int64_t)threadIdx.x * 4;
     ulonglong2* p = reinterpret_cast<ulonglong2*>(A.cdf + rp.nbase + vt);
     ulonglong2 a = p[0], b = p[1];
+    // the tile-local value before this thread's first slot (written by k_cdf_tiles, read before
+    // any thread of the tile adds the offset)
+    const uint64_t before = threadIdx.x == 0 ? 0 : A.cdf[rp.nbase + vt - 1];
+    __syncthreads();
     a.x += off;
     a.y += off;
     b.x += off;
     b.y += off;
-    p[0] = a;
-    p[1] = b;
+    if (off) {
+        p[0] = a;
+        p[1] = b;
+    }
+    const int gs = guide_shift(rp.wq_total, rp.n);
+    const uint64_t c[5] = {before + off, a.x, a.y, b.x, b.y};
+    int32_t* guide = A.guide + rp.nbase;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const uint64_t lo = c[i], hi = c[i + 1];
+        if (vt + i < rp.n && hi > lo) {
+            const uint64_t g0 = (lo + ((1ull << gs) - 1)) >> gs, g1 = (hi - 1) >> gs;
+            if (g0 <= g1) guide[g0] = (int32_t)(vt + i);
+        }
+    }
+}
+
+// Guide table fill: guide[g] = smallest v with cdf[v] > g 2^gs, for g < used(Wq, n).  Each tile of
+// buckets takes the running maximum of its marks, starting from the node that owns its first
+// bucket (one binary search per tile), so no tile waits for another.
+__global__ void __launch_bounds__(kTileThreads) k_guide_fill(Arena A) {
+    __shared__ int32_t wmax[kTileThreads / 32];
+    __shared__ int32_t carry;
+    if (A.st->error) return;
+    const int t = blockIdx.x;
+    const int r = A.tile_rep[t];
+    const Replica& rp = A.rep[r];
+    const uint64_t Wq = rp.wq_total;
+    if (Wq == 0 || rp.n <= 0) return;
+    const int gs = guide_shift(Wq, rp.n);
+    const int64_t used = (int64_t)((Wq - 1) >> gs) + 1;
+    const int64_t g0 = (int64_t)(t - rp.tbase) * kTile;
+    if (g0 >= used) return;
+    const uint64_t* cdf = A.cdf + rp.nbase;
+    if (threadIdx.x == 0) {
+        int32_t v = 0;
+        if (g0 > 0) {
+            const uint64_t y = (uint64_t)g0 << gs;
+            int64_t lo = 0, hi = rp.n - 1;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (cdf[mid] > y)
+                    hi = mid;
+                else
+                    lo = mid + 1;
+            }
+            v = (int32_t)lo;
+        }
+        carry = v;
+    }
+    int4* gp = reinterpret_cast<int4*>(A.guide + rp.nbase + g0) + threadIdx.x;
+    int4 m = *gp;
+    m.y = max(m.y, m.x);
+    m.z = max(m.z, m.y);
+    m.w = max(m.w, m.z);
+    // block-wide inclusive running maximum of the threads' last values
+    int32_t x = m.w;
+    const int lane = lane_id(), wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int32_t o = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x = max(x, o);
+    }
+    if (lane == 31) wmax[wid] = x;
+    __syncthreads();
+    int32_t pre = carry;
+    for (int w = 0; w < wid; ++w) pre = max(pre, wmax[w]);
+    const int32_t prev = __shfl_up_sync(0xffffffffu, x, 1);
+    if (lane > 0) pre = max(pre, prev);
+    m.x = max(m.x, pre);
+    m.y = max(m.y, pre);
+    m.z = max(m.z, pre);
+    m.w = max(m.w, pre);
+    *gp = m;
 }
 
 // ---------------------------------------------------------------- hub index
@@ -371,5 +449,7 @@ void launch_weights(const Arena& A, cudaStream_t s) {
     k_tile_scan<<<1, 1024, 0, s>>>(A, 0);
     k_cdf_add<<<A.ntiles, kTileThreads, 0, s>>>(A);
 }
+
+void launch_guide(const Arena& A, cudaStream_t s) { k_guide_fill<<<A.ntiles, kTileThreads, 0, s>>>(A); }
 
 }  // namespace pg
