@@ -14,8 +14,10 @@
  *   pg_grow_epoch                    <- buildOneNodeConnections_timed (src/kernel.cu:1125-1586) plus
  *                                       the host edge insert and in-degree update that follow it in
  *                                       execute() (src/kernel.cu:1766-1815, src/graph.cu:537-618)
- *   pg_grow_epoch_refcompat          <- the same step with the reference's linear score mix, budget
- *                                       split and uniform fill (src/kernel.cu:196-402,
+ *   pg_rc_configure + pg_grow_epoch  <- the same step with the reference's own model (context
+ *     (weight_model REFCOMPAT)          created with PG_WEIGHTS_REFCOMPAT): its linear score mix
+ *                                       (src/abm.cu:112-208,324-338), budget split, same-year,
+ *                                       1-hop / 2-hop picks and uniform fill (src/kernel.cu:196-402,
  *                                       src/abm.cu:376-565)
  *   pg_er_epoch                      <- the G(n,p) growth step of the reference's ER model, whose
  *                                       semantics are recorded in results/slurm-8634746.out:60-73
@@ -178,6 +180,39 @@ pg_status pg_run_epochs(pg_ctx* ctx, int32_t num_epochs, int32_t use_graph, int6
 /* One Erdos-Renyi G(n,p) epoch on replica 0: delta new nodes, each linking to every pre-epoch node
  * with probability p, by geometric skips. */
 pg_status pg_er_epoch(pg_ctx* ctx, int64_t delta, double p, int64_t* new_edges);
+
+/* ---- refcompat functor: ParAGraph's own per-paper model (the abm driver's options) ---- */
+typedef struct {
+    double pa_weight;     /* --preferential-weight; all three >= 0: fixed (normalised to sum 1), */
+    double rec_weight;    /* --recency-weight        else each agent draws three U(0,1) weights   */
+    double fit_weight;    /* --fitness-weight        and normalises them (ABM::PopulateWeightArrs) */
+    double alpha;         /* --alpha: share of the neighbourhood budget taken from the 1-hop set;
+                             < 0: U(0,1) per agent (ABM::PopulateAlphaArr) */
+    double fully_random;  /* --fully-random-citations: out-degree fraction reserved for uniform picks */
+    double same_year;     /* --same-year-proportion: fraction of each epoch's agents citing a paper
+                             of their own epoch */
+    double growth_rate;   /* --growth-rate: new papers per epoch = ceil(n * growth_rate) */
+    int32_t gamma;        /* exponent of the in-degree and fitness scores, 1..4 (reference: 3) */
+    int32_t decay;        /* fitness decay exponent after the peak window, 0..8 (reference: 3) */
+} pg_rc_params;
+/* Configures replica `replica` of a PG_WEIGHTS_REFCOMPAT context after pg_load_graph (whose
+ * fitness values are the seed papers' peak fitness; lag 0, duration 1000): the parameters, the
+ * out-degree bag (ABM::ReadOutDegreeBag, src/abm.cu:70-89; values clipped to [0, 256], out-degrees
+ * to [1, min(256, n-1)]) and the recency probabilities rec[age] for age 0..rec_len-1, rec_len <= 1024
+ * (ABM::ReadRecencyProbabilities, src/abm.cu:91-110).  pg_grow_epoch / pg_run_epochs then run the
+ * reference's per-paper rule on the device. */
+pg_status pg_rc_configure(pg_ctx* ctx, int32_t replica, const pg_rc_params* params, const int32_t* bag,
+                          int64_t bag_len, const double* rec, int32_t rec_len);
+/* Fitness windows of papers [first, first+count): lag, peak value (>= 1), peak duration -- the
+ * planted papers of ABM::PlantNodes (includes/abm.cuh:486-504). */
+pg_status pg_rc_set_nodes(pg_ctx* ctx, int32_t replica, int64_t first, int64_t count, const int32_t* lag,
+                          const int32_t* peak, const int32_t* dur);
+/* Per-paper draws of the last refcompat epoch, [new_nodes][6]: pa, rec and fit weights, alpha,
+ * generator node, out-degree (the agent columns of Graph::WriteAttributes, src/graph.cu:1057-1211). */
+pg_status pg_rc_copy_agents(pg_ctx* ctx, int32_t replica, double* out);
+/* Host tables shared with tests: the bag's 257-entry CDF and the 1000-entry peak-fitness CDF (2^64). */
+pg_status pg_rc_bag_table(const int32_t* bag, int64_t len, uint64_t* table);
+pg_status pg_rc_fitness_table(uint64_t* table);
 
 /* ---- output ---- */
 pg_status pg_get_counts(const pg_ctx* ctx, int32_t replica, int64_t* n, int64_t* m);

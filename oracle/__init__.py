@@ -67,6 +67,12 @@ def _load() -> C.CDLL:
         "og_copy_weights": (i64, [vp, vp, vp, C.POINTER(i32)]),
         "og_agent_anchors": (None, [u64, u32, u32, i64, i64, i32, vp]),
         "og_loglik": (i32, [C.POINTER(_Trace), i32, vp, vp, vp, i32]),
+        "og_rc_configure": (i32, [vp, vp, vp, i64, vp, i32]),
+        "og_rc_bag_table": (None, [vp, i64, vp]),
+        "og_rc_fitness_table": (None, [vp]),
+        "og_rc_set_nodes": (None, [vp, i64, i64, vp, vp, vp]),
+        "og_rc_epoch": (i32, [vp, i32]),
+        "og_rc_copy_agents": (None, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -111,6 +117,19 @@ def poisson_table(lam: float) -> np.ndarray:
     return t
 
 
+def rc_bag_table(bag) -> np.ndarray:
+    b = np.ascontiguousarray(bag, np.int32)
+    t = np.zeros(257, np.uint64)
+    _load().og_rc_bag_table(_p(b), len(b), _p(t))
+    return t
+
+
+def rc_fitness_table() -> np.ndarray:
+    t = np.zeros(1000, np.uint64)
+    _load().og_rc_fitness_table(_p(t))
+    return t
+
+
 def fitness(seed: int, replica: int, epoch: int, unit: int) -> float:
     return _load().og_fitness(seed, replica, epoch & 0xFFFFFFFF, unit)
 
@@ -151,6 +170,36 @@ class OracleGraph:
 
     def set_epoch(self, e: int) -> None:
         self._lib.og_set_epoch(self._g, e)
+
+    # ---- refcompat functor (ParAGraph's own per-paper model)
+    def rc_configure(self, rc, bag, recency) -> None:
+        """rc: an object with the fields of paragraph_gb300.RCParams; bag: out-degree bag;
+        recency[dy]: recency probability of age dy."""
+        prm = np.array([rc.pa_weight, rc.rec_weight, rc.fit_weight, rc.alpha, rc.fully_random,
+                        rc.same_year, rc.growth_rate, rc.gamma, rc.decay], np.float64)
+        bag = np.ascontiguousarray(bag, np.int32)
+        rec = np.ascontiguousarray(recency, np.float64)
+        st = self._lib.og_rc_configure(self._g, _p(prm), _p(bag), len(bag), _p(rec), len(rec))
+        if st:
+            raise ValueError(f"og_rc_configure failed ({st})")
+
+    def rc_set_nodes(self, first: int, lag, peak, dur) -> None:
+        lag = np.ascontiguousarray(lag, np.int32)
+        peak = np.ascontiguousarray(peak, np.int32)
+        dur = np.ascontiguousarray(dur, np.int32)
+        self._lib.og_rc_set_nodes(self._g, first, len(lag), _p(lag), _p(peak), _p(dur))
+
+    def rc_epoch(self, threads: int = 0) -> None:
+        st = self._lib.og_rc_epoch(self._g, threads)
+        if st:
+            raise ValueError(f"og_rc_epoch failed ({st})")
+
+    def rc_agents(self) -> np.ndarray:
+        """Last refcompat epoch, per agent: pa, rec, fit weights, alpha, generator, out-degree."""
+        k = self.n - self.stats()["nodes_weighted"]
+        out = np.zeros((k, 6), np.float64)
+        self._lib.og_rc_copy_agents(self._g, _p(out))
+        return out
 
     def set_sampler(self, sampler: int) -> None:
         """0: thinning sampler (default); 1: full 2-hop neighbourhood enumeration."""

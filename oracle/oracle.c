@@ -199,6 +199,7 @@ double og_log(double x) {
 }
 
 #define OG_TABLE 257 /* out-degrees 0..256 */
+#define OG_RC_FIT_MAX 1000 /* peak fitness values 1..1000 */
 
 /* Poisson(lambda) CDF * 2^64, saturating; the out-degree law of the baseline configs. */
 void og_poisson_table(double lambda, uint64_t* table) {
@@ -262,6 +263,17 @@ struct og_graph {
     uint64_t* cdf;
     int64_t w_n;
     int32_t shift;
+    /* refcompat functor (og_rc_configure) */
+    int rc;
+    double rc_w[3], rc_alpha, rc_frc, rc_sy, rc_growth;
+    int rc_gamma, rc_decay;
+    uint64_t rc_bag[OG_TABLE];
+    uint64_t rc_fit_table[OG_RC_FIT_MAX];
+    double* rc_rec;
+    int rc_rec_len;
+    int32_t* rc_lag; /* per node: fitness lag and peak duration (the peak value is fit[]) */
+    int32_t* rc_dur;
+    double* rc_agents; /* last epoch, per agent: pa, rec, fit weights, alpha, generator, out-degree */
 };
 
 og_graph* og_create(uint64_t seed, uint32_t replica) {
@@ -284,6 +296,10 @@ void og_destroy(og_graph* g) {
     free(g->arrivals);
     free(g->w);
     free(g->cdf);
+    free(g->rc_rec);
+    free(g->rc_lag);
+    free(g->rc_dur);
+    free(g->rc_agents);
     free(g);
 }
 
@@ -1203,4 +1219,424 @@ int og_loglik(const og_trace* T, int batch, const double* theta, double* ll, dou
     free(ld);
     free(zg);
     return bad ? 4 : 0;
+}
+
+/* ------------------------------------------------------------------ refcompat functor
+ *
+ * ParAGraph's own per-paper model (the drop-in semantics of its abm driver), on the same graph
+ * state.  Per epoch t with n nodes and delta = ceil(n * growth_rate) new papers:
+ *   scores (ABM::FillInDegreeArr / FillFitnessArr / FillRecencyArr / CalculateScores,
+ *   src/abm.cu:112-208,324-338):
+ *     f_j   = 1 before pub+lag, the peak value up to pub+lag+dur, then (int)(peak/(t-pub-lag-dur+1)^decay)
+ *     pa_j  = (indeg_j^gamma + 1) / sum,  fit_j = (f_j^gamma + 1) / sum   (integer sums, exact)
+ *     rec_j = P(t-pub_j) / (count(t-pub_j) * sum of P over the distinct ages present)
+ *     score_aj = w_pa pa_j + w_rec rec_j + w_fit fit_j (per-agent weights, normalised)
+ *   agent a (budget split src/kernel.cu:230-402; citations src/abm.cu:376-565):
+ *     d from the out-degree bag, clipped to [1, min(256, n-1)]; generator g uniform over [0, n);
+ *     sy = 1 for exactly floor(delta * same_year) agents, citing paper n + U[0, delta);
+ *     rsv = floor(fully_random d);  in = min(ceil((d-1-sy-rsv) alpha), |N1|) from the 1-hop set
+ *     of g;  out = min(d-1-sy-rsv-in, |N2|) from the 2-hop set (minus the 1-hop set and g), both
+ *     by Efraimidis-Spirakis keys (k smallest E_j/score_j, E_j exponential, keyed by (agent, j));
+ *     the remaining d-1-sy-in-out uniformly from [0, n-1) without g and earlier choices.
+ * Arrival order: g, the same-year paper, 1-hop picks, 2-hop picks (key order), uniform picks.
+ */
+enum { S_SAMEYEAR = 7, S_FILL = 8, S_RCAGENT = 10, S_RCKEY = 11, S_RCFIT = 12 };
+#define OG_RC_FILL_BLOCKS (1u << 20) /* Philox blocks a uniform fill may use (then an error) */
+
+static double u128_to_d(unsigned __int128 v) {
+    return (double)(uint64_t)(v >> 64) * 0x1p64 + (double)(uint64_t)v;
+}
+
+void og_rc_bag_table(const int32_t* bag, int64_t len, uint64_t* table) {
+    int64_t cnt[OG_TABLE];
+    memset(cnt, 0, sizeof(cnt));
+    for (int64_t i = 0; i < len; i++) {
+        int32_t v = bag[i] < 0 ? 0 : (bag[i] > OG_TABLE - 1 ? OG_TABLE - 1 : bag[i]);
+        cnt[v]++;
+    }
+    int64_t cum = 0;
+    for (int v = 0; v < OG_TABLE; v++) {
+        cum += cnt[v];
+        table[v] = (cum >= len || v == OG_TABLE - 1)
+                       ? ~(uint64_t)0
+                       : (uint64_t)((((unsigned __int128)cum) << 64) / (unsigned __int128)len);
+    }
+}
+
+/* Peak-fitness distribution of ABM::AssignPeakFitnessValues (includes/abm.cuh:469-484):
+ * P(v) proportional to v^-1.634 for v in 1..1000, as 2^64-scaled CDF thresholds. */
+void og_rc_fitness_table(uint64_t* table) {
+    double p[OG_RC_FIT_MAX], tot = 0.0;
+    for (int i = 0; i < OG_RC_FIT_MAX; i++) {
+        p[i] = og_exp(-1.634 * og_log((double)(i + 1)));
+        tot += p[i];
+    }
+    double cum = 0.0;
+    for (int i = 0; i < OG_RC_FIT_MAX; i++) {
+        cum += p[i];
+        double q = cum / tot;
+        table[i] = (q >= 1.0 || i == OG_RC_FIT_MAX - 1) ? ~(uint64_t)0 : (uint64_t)(q * 0x1p64);
+    }
+}
+
+int og_rc_configure(og_graph* g, const double* prm, const int32_t* bag, int64_t bag_len,
+                    const double* rec, int32_t rec_len) {
+    /* prm: pa, rec, fit weights, alpha, fully_random, same_year, growth_rate, gamma, decay */
+    if (bag_len <= 0 || rec_len < 0 || !(prm[6] > 0.0)) return 3;
+    int fixed = prm[0] >= 0.0 && prm[1] >= 0.0 && prm[2] >= 0.0;
+    if (fixed && !(prm[0] + prm[1] + prm[2] > 0.0)) return 3;
+    g->rc = 1;
+    for (int i = 0; i < 3; i++) g->rc_w[i] = fixed ? prm[i] : -1.0;
+    g->rc_alpha = prm[3] > 1.0 ? 1.0 : prm[3];
+    g->rc_frc = prm[4];
+    g->rc_sy = prm[5];
+    g->rc_growth = prm[6];
+    g->rc_gamma = (int)prm[7];
+    g->rc_decay = (int)prm[8];
+    og_rc_bag_table(bag, bag_len, g->rc_bag);
+    og_rc_fitness_table(g->rc_fit_table);
+    free(g->rc_rec);
+    g->rc_rec_len = rec_len;
+    g->rc_rec = (double*)malloc(sizeof(double) * (size_t)(rec_len > 0 ? rec_len : 1));
+    if (rec_len) memcpy(g->rc_rec, rec, sizeof(double) * (size_t)rec_len);
+    free(g->rc_lag);
+    free(g->rc_dur);
+    g->rc_lag = (int32_t*)malloc(sizeof(int32_t) * (size_t)(g->n > 0 ? g->n : 1));
+    g->rc_dur = (int32_t*)malloc(sizeof(int32_t) * (size_t)(g->n > 0 ? g->n : 1));
+    for (int64_t j = 0; j < g->n; j++) {
+        g->rc_lag[j] = 0;
+        g->rc_dur[j] = 1000;
+    }
+    return 0;
+}
+
+void og_rc_set_nodes(og_graph* g, int64_t first, int64_t count, const int32_t* lag,
+                     const int32_t* peak, const int32_t* dur) {
+    for (int64_t i = 0; i < count; i++) {
+        g->rc_lag[first + i] = lag[i];
+        g->fit[first + i] = (float)peak[i];
+        g->rc_dur[first + i] = dur[i];
+    }
+}
+
+static int64_t ipow_i64(int64_t x, int e) {
+    int64_t r = 1;
+    for (int i = 0; i < e; i++) r *= x;
+    return r;
+}
+
+/* fitness of node j at epoch t (ABM::FillFitnessArr, src/abm.cu:152-176) */
+static int32_t rc_fitness_at(const og_graph* g, int64_t j, int64_t t) {
+    int64_t pub = g->pub[j], lag = g->rc_lag[j], dur = g->rc_dur[j];
+    int64_t peak = (int64_t)g->fit[j];
+    if (pub + lag > t) return 1;
+    if (pub + lag + dur >= t) return (int32_t)peak;
+    double den = (double)ipow_i64(t - pub - lag - dur + 1, g->rc_decay);
+    return (int32_t)((double)peak / den);
+}
+
+static void rc_scores(const og_graph* g, double* pa, double* rec, double* fit) {
+    int64_t n = g->n, t = g->epoch;
+    unsigned __int128 spa = 0, sfit = 0;
+    int64_t* cnt = (int64_t*)calloc((size_t)(g->rc_rec_len > 0 ? g->rc_rec_len : 1), sizeof(int64_t));
+    for (int64_t j = 0; j < n; j++) {
+        unsigned __int128 a = 1, f = 1, x = (unsigned __int128)(uint32_t)g->indeg[j];
+        unsigned __int128 y = (unsigned __int128)(uint32_t)rc_fitness_at(g, j, t);
+        for (int e = 0; e < g->rc_gamma; e++) {
+            a *= x;
+            f *= y;
+        }
+        spa += a + 1;
+        sfit += f + 1;
+        pa[j] = u128_to_d(a + 1);
+        fit[j] = u128_to_d(f + 1);
+        int64_t dy = t - g->pub[j];
+        if (dy >= 0 && dy < g->rc_rec_len) cnt[dy]++;
+    }
+    double U = 0.0;
+    for (int i = 0; i < g->rc_rec_len; i++)
+        if (cnt[i]) U += g->rc_rec[i];
+    double dpa = u128_to_d(spa), dfit = u128_to_d(sfit);
+    for (int64_t j = 0; j < n; j++) {
+        pa[j] = pa[j] / dpa;
+        fit[j] = fit[j] / dfit;
+        int64_t dy = t - g->pub[j];
+        rec[j] = (dy >= 0 && dy < g->rc_rec_len && U > 0.0) ? g->rc_rec[dy] / ((double)cnt[dy] * U) : 0.0;
+    }
+    free(cnt);
+}
+
+/* bijection of [0, 2^bits): three rounds of xor-key, odd multiply, xorshift */
+static uint32_t rc_perm(uint32_t x, int bits, const uint32_t key[4]) {
+    uint32_t mask = bits >= 32 ? 0xFFFFFFFFu : ((1u << bits) - 1u);
+    int h = bits / 2 + 1;
+    for (int r = 0; r < 3; r++) {
+        x = (x ^ key[r]) & mask;
+        x = (x * (key[(r + 1) & 3] | 1u)) & mask;
+        if (h < bits) x ^= x >> h;
+    }
+    return x;
+}
+
+/* 1 when agent a is one of the floor(delta * same_year) same-year citers; its target in *tgt */
+static int rc_same_year(const og_graph* g, int64_t a, int64_t delta, int32_t* tgt) {
+    int64_t S = (int64_t)floor((double)delta * g->rc_sy);
+    if (S <= 0) return 0;
+    int bits = 1;
+    while (bits < 31 && ((int64_t)1 << bits) < delta) bits++;
+    uint32_t key[4];
+    rng(g->seed, S_SAMEYEAR, g->replica, (uint32_t)g->epoch, 0xFFFFFFFFu, 0, key);
+    uint32_t x = (uint32_t)a;
+    do {
+        x = rc_perm(x, bits, key);
+    } while ((int64_t)x >= delta);
+    if ((int64_t)x >= S) return 0;
+    uint32_t r[4];
+    rng(g->seed, S_SAMEYEAR, g->replica, (uint32_t)g->epoch, (uint32_t)a, 0, r);
+    *tgt = (int32_t)(g->n + (int64_t)(((uint64_t)r[0] * (uint64_t)delta) >> 32));
+    return 1;
+}
+
+static float rc_key(const og_graph* g, int64_t a, int32_t j, double score) {
+    if (!(score > 0.0)) return INFINITY;
+    uint32_t r[4];
+    rng(g->seed, S_RCKEY, g->replica, (uint32_t)g->epoch, (uint32_t)a, (uint32_t)j, r);
+    double E = -og_log(unif_d(r[0], r[1]));
+    return (float)(E / score);
+}
+
+/* k smallest distinct (key, id) of a keyed multiset (duplicates share a key) */
+static int rc_topk(keyvec* kv, int k, int32_t* out) {
+    qsort(kv->v, (size_t)kv->n, sizeof(keyed), cmp_keyed);
+    int c = 0;
+    for (int64_t i = 0; i < kv->n && c < k; i++)
+        if (i == 0 || kv->v[i].id != kv->v[i - 1].id) out[c++] = kv->v[i].id;
+    return c;
+}
+
+static int rc_in_row(const og_graph* g, int32_t x, int32_t v) {
+    return bsearch32(g->fwd_col + g->fwd_off[x], g->fwd_off[x + 1] - g->fwd_off[x], v) ||
+           bsearch32(g->bwd_col + g->bwd_off[x], g->bwd_off[x + 1] - g->bwd_off[x], v);
+}
+
+/* Per-agent parameters: weights (normalised), alpha, generator. */
+static void rc_agent_params(const og_graph* g, int64_t a, double* w3, double* alpha, int32_t* gen) {
+    uint32_t r0[4], r1[4], r2[4];
+    rng(g->seed, S_RCAGENT, g->replica, (uint32_t)g->epoch, (uint32_t)a, 0, r0);
+    rng(g->seed, S_RCAGENT, g->replica, (uint32_t)g->epoch, (uint32_t)a, 1, r1);
+    rng(g->seed, S_RCAGENT, g->replica, (uint32_t)g->epoch, (uint32_t)a, 2, r2);
+    double wp = g->rc_w[0] >= 0.0 ? g->rc_w[0] : unif_d(r0[0], r0[1]);
+    double wr = g->rc_w[1] >= 0.0 ? g->rc_w[1] : unif_d(r0[2], r0[3]);
+    double wf = g->rc_w[2] >= 0.0 ? g->rc_w[2] : unif_d(r1[0], r1[1]);
+    double sum = wp + wr + wf;
+    w3[0] = wp / sum;
+    w3[1] = wr / sum;
+    w3[2] = wf / sum;
+    *alpha = g->rc_alpha >= 0.0 ? g->rc_alpha : unif_d(r1[2], r1[3]);
+    *gen = (int32_t)(((uint64_t)r2[0] * (uint64_t)g->n) >> 32);
+}
+
+static int rc_agent(const og_graph* g, int64_t a, int64_t delta, int d, const double* pa,
+                    const double* rec, const double* fit, int32_t* out_sorted, int32_t* out_arr,
+                    int64_t* cnt, keyvec* kv, double* info) {
+    const int64_t n = g->n;
+    double w3[3], alpha;
+    int32_t gen;
+    rc_agent_params(g, a, w3, &alpha, &gen);
+#define RC_SCORE(j) (w3[0] * pa[j] + w3[1] * rec[j] + w3[2] * fit[j])
+    int c = 0;
+    out_arr[c++] = gen;
+    int32_t tgt;
+    int sy = d >= 2 ? rc_same_year(g, a, delta, &tgt) : 0; /* an agent of out-degree 1 cites g only */
+    if (sy) out_arr[c++] = tgt;
+    int rsv = (int)floor(g->rc_frc * (double)d);
+    int rem1 = d - 1 - sy - rsv;
+    int in_t = rem1 > 0 ? (int)ceil((double)rem1 * alpha) : 0;
+    if (in_t > rem1) in_t = rem1 > 0 ? rem1 : 0;
+    /* 1-hop set of the generator (streamed when it has a budget) */
+    kv->n = 0;
+    cnt[0]++;
+    for (int dir = 0; dir < 2 && in_t > 0; dir++) {
+        const int64_t* off = dir ? g->bwd_off : g->fwd_off;
+        const int32_t* col = dir ? g->bwd_col : g->fwd_col;
+        for (int64_t p = off[gen]; p < off[gen + 1]; p++) {
+            int32_t y = col[p];
+            if (y == gen) continue;
+            cnt[1]++;
+            keyed kk = {rc_key(g, a, y, RC_SCORE(y)), y};
+            kv_push(kv, kk);
+        }
+    }
+    int in = in_t > 0 ? rc_topk(kv, in_t, out_arr + c) : 0;
+    c += in;
+    int rem2 = d - 1 - sy - rsv - in;
+    int out = 0;
+    if (rem2 > 0) {
+        kv->n = 0;
+        for (int dir = 0; dir < 2; dir++) {
+            const int64_t* off = dir ? g->bwd_off : g->fwd_off;
+            const int32_t* col = dir ? g->bwd_col : g->fwd_col;
+            for (int64_t p = off[gen]; p < off[gen + 1]; p++) {
+                int32_t y = col[p];
+                if (y == gen) continue;
+                cnt[0]++;
+                for (int dir2 = 0; dir2 < 2; dir2++) {
+                    const int64_t* off2 = dir2 ? g->bwd_off : g->fwd_off;
+                    const int32_t* col2 = dir2 ? g->bwd_col : g->fwd_col;
+                    for (int64_t p2 = off2[y]; p2 < off2[y + 1]; p2++) {
+                        int32_t z = col2[p2];
+                        if (z == gen || rc_in_row(g, gen, z)) continue;
+                        cnt[1]++;
+                        keyed kk = {rc_key(g, a, z, RC_SCORE(z)), z};
+                        kv_push(kv, kk);
+                    }
+                }
+            }
+        }
+        out = rc_topk(kv, rem2, out_arr + c);
+        c += out;
+    }
+    int rnd = d - 1 - sy - in - out;
+    /* uniform fill over [0, n-1) without the generator and earlier choices */
+    for (uint32_t i = 0; rnd > 0; i++) {
+        uint32_t r[4];
+        if (i >= OG_RC_FILL_BLOCKS) return -1;
+        rng(g->seed, S_FILL, g->replica, (uint32_t)g->epoch, (uint32_t)a, i, r);
+        for (int q = 0; q < 4 && rnd > 0; q++) {
+            int32_t v = (int32_t)(((uint64_t)r[q] * (uint64_t)(n - 1)) >> 32);
+            cnt[2]++;
+            int dup = 0;
+            for (int z = 0; z < c; z++)
+                if (out_arr[z] == v) {
+                    dup = 1;
+                    break;
+                }
+            if (dup) continue;
+            out_arr[c++] = v;
+            rnd--;
+        }
+    }
+#undef RC_SCORE
+    info[0] = w3[0];
+    info[1] = w3[1];
+    info[2] = w3[2];
+    info[3] = alpha;
+    info[4] = (double)gen;
+    info[5] = (double)d;
+    memcpy(out_sorted, out_arr, sizeof(int32_t) * (size_t)c);
+    qsort(out_sorted, (size_t)c, sizeof(int32_t), cmp_i32);
+    return c;
+}
+
+int og_rc_epoch(og_graph* g, int threads) {
+    if (!g->rc || g->n < 2) return 6;
+    const int64_t n = g->n;
+    const int64_t delta = (int64_t)ceil((double)n * g->rc_growth);
+    if (delta <= 0) return 3;
+    double* pa = (double*)malloc(sizeof(double) * (size_t)n);
+    double* rec = (double*)malloc(sizeof(double) * (size_t)n);
+    double* fit = (double*)malloc(sizeof(double) * (size_t)n);
+    rc_scores(g, pa, rec, fit);
+    int32_t* rows = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta * 256);
+    int32_t* arr = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta * 256);
+    int32_t* kk = (int32_t*)malloc(sizeof(int32_t) * (size_t)delta);
+    free(g->rc_agents);
+    g->rc_agents = (double*)malloc(sizeof(double) * 6 * (size_t)delta);
+    int64_t rows_exp = 0, elems = 0, draws = 0;
+    int failed = 0;
+    int dmax = n - 1 < OG_TABLE - 1 ? (int)(n - 1) : OG_TABLE - 1;
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel reduction(+ : rows_exp, elems, draws) reduction(| : failed)
+    {
+        keyvec kv = {0, 0, 0};
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t a = 0; a < delta; a++) {
+            uint32_t r[4];
+            rng(g->seed, S_OUTDEG, g->replica, (uint32_t)g->epoch, (uint32_t)a, 0, r);
+            uint64_t u = join64(r[0], r[1]);
+            int d = OG_TABLE - 1;
+            for (int i = 0; i < OG_TABLE; i++)
+                if (u < g->rc_bag[i]) {
+                    d = i;
+                    break;
+                }
+            if (d < 1) d = 1;
+            if (d > dmax) d = dmax;
+            int64_t cnt[3] = {0, 0, 0};
+            int c = rc_agent(g, a, delta, d, pa, rec, fit, rows + a * 256, arr + a * 256, cnt, &kv,
+                             g->rc_agents + 6 * a);
+            if (c < 0) {
+                failed = 1;
+                c = 0;
+            }
+            kk[a] = c;
+            rows_exp += cnt[0];
+            elems += cnt[1];
+            draws += cnt[2];
+        }
+        free(kv.v);
+    }
+    if (failed) {
+        free(pa);
+        free(rec);
+        free(fit);
+        free(rows);
+        free(arr);
+        free(kk);
+        return 4;
+    }
+    int64_t* row_off = (int64_t*)malloc(sizeof(int64_t) * (size_t)(delta + 1));
+    row_off[0] = 0;
+    for (int64_t a = 0; a < delta; a++) row_off[a + 1] = row_off[a] + kk[a];
+    int64_t e_new = row_off[delta];
+    int32_t* flat = (int32_t*)malloc(sizeof(int32_t) * (size_t)(e_new + 1));
+    free(g->arrivals);
+    g->arrivals = (int32_t*)malloc(sizeof(int32_t) * (size_t)(e_new + 1));
+    for (int64_t a = 0; a < delta; a++) {
+        memcpy(flat + row_off[a], rows + a * 256, sizeof(int32_t) * (size_t)kk[a]);
+        memcpy(g->arrivals + row_off[a], arr + a * 256, sizeof(int32_t) * (size_t)kk[a]);
+    }
+    /* new papers: peak fitness from the power-law table, static window (lag 0, duration 1000) */
+    float* nf = (float*)malloc(sizeof(float) * (size_t)delta);
+    for (int64_t a = 0; a < delta; a++) {
+        uint32_t r[4];
+        rng(g->seed, S_RCFIT, g->replica, (uint32_t)g->epoch, (uint32_t)a, 0, r);
+        uint64_t u = join64(r[0], r[1]);
+        int v = OG_RC_FIT_MAX;
+        for (int i = 0; i < OG_RC_FIT_MAX; i++)
+            if (u < g->rc_fit_table[i]) {
+                v = i + 1;
+                break;
+            }
+        nf[a] = (float)v;
+    }
+    append_rows(g, delta, row_off, flat, (int32_t)g->epoch, nf);
+    g->rc_lag = (int32_t*)realloc(g->rc_lag, sizeof(int32_t) * (size_t)g->n);
+    g->rc_dur = (int32_t*)realloc(g->rc_dur, sizeof(int32_t) * (size_t)g->n);
+    for (int64_t j = n; j < g->n; j++) {
+        g->rc_lag[j] = 0;
+        g->rc_dur[j] = 1000;
+    }
+    g->stats[0] = n;
+    g->stats[1] = rows_exp;
+    g->stats[2] = elems;
+    g->stats[3] = draws;
+    g->stats[4] = e_new;
+    g->stats[5] = 0;
+    g->epoch++;
+    free(pa);
+    free(rec);
+    free(fit);
+    free(rows);
+    free(arr);
+    free(kk);
+    free(row_off);
+    free(flat);
+    free(nf);
+    return 0;
+}
+
+void og_rc_copy_agents(const og_graph* g, double* out6) {
+    /* agents of the last epoch = nodes added by it */
+    if (g->rc_agents) memcpy(out6, g->rc_agents, sizeof(double) * 6 * (size_t)(g->n - g->stats[0]));
 }

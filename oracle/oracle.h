@@ -84,4 +84,19 @@ typedef struct {
 int og_loglik(const og_trace* trace, int batch, const double* theta, double* ll, double* grad,
               int threads);
 
+/* ---- refcompat functor: ParAGraph's own per-paper model ----
+ * prm: pa, rec, fit weights (all >= 0: fixed, normalised; else drawn per agent), alpha (< 0: per
+ * agent), fully_random, same_year, growth_rate, gamma, decay.  bag: out-degree bag; rec[dy]:
+ * recency probability of age dy in [0, rec_len).  Returns 0 or 3. */
+int og_rc_configure(og_graph* g, const double* prm, const int32_t* bag, int64_t bag_len,
+                    const double* rec, int32_t rec_len);
+void og_rc_bag_table(const int32_t* bag, int64_t len, uint64_t* table);    /* 257 entries */
+void og_rc_fitness_table(uint64_t* table);                                  /* 1000 entries */
+/* fitness window of nodes [first, first+count): lag, peak value, duration */
+void og_rc_set_nodes(og_graph* g, int64_t first, int64_t count, const int32_t* lag,
+                     const int32_t* peak, const int32_t* dur);
+int og_rc_epoch(og_graph* g, int threads);
+/* last refcompat epoch, per agent: pa, rec, fit weights, alpha, generator, out-degree */
+void og_rc_copy_agents(const og_graph* g, double* out6);
+
 #endif

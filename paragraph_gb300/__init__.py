@@ -39,7 +39,8 @@ EXPORTED = [
     "pg_logf_host", "pg_expf_host", "pg_log_host", "pg_exp_host", "pg_version",
     "pg_timer_start", "pg_timer_stop", "pg_checkpoint", "pg_restore", "pg_er_generate_noalloc",
     "pg_set_tuning", "pg_get_tuning", "pg_autotune", "pg_copy_anchors", "pg_trace_load",
-    "pg_loglik_fwd", "pg_loglik_bwd",
+    "pg_loglik_fwd", "pg_loglik_bwd", "pg_rc_configure", "pg_rc_set_nodes", "pg_rc_copy_agents",
+    "pg_rc_bag_table", "pg_rc_fitness_table",
 ]
 
 
@@ -59,6 +60,28 @@ class _Params(C.Structure):
     _fields_ = [("alpha", C.c_double), ("tau", C.c_double), ("gamma", C.c_double),
                 ("beta", C.c_double), ("mean_out_degree", C.c_double), ("growth_rate", C.c_double),
                 ("fixed_new_nodes", C.c_int64), ("num_anchors", C.c_int32), ("reserved", C.c_int32)]
+
+
+class _RcParams(C.Structure):
+    _fields_ = [("pa_weight", C.c_double), ("rec_weight", C.c_double), ("fit_weight", C.c_double),
+                ("alpha", C.c_double), ("fully_random", C.c_double), ("same_year", C.c_double),
+                ("growth_rate", C.c_double), ("gamma", C.c_int32), ("decay", C.c_int32)]
+
+
+@dataclass
+class RCParams:
+    """Parameters of the refcompat functor -- ParAGraph's own model, with the abm driver's
+    defaults (src/main.cu:29-114; gamma and decay are constants of the reference,
+    includes/abm.cuh:543-553).  A weight or alpha below 0 is drawn per agent."""
+    pa_weight: float = -1.0
+    rec_weight: float = -1.0
+    fit_weight: float = -1.0
+    alpha: float = -1.0
+    fully_random: float = 0.05
+    same_year: float = 0.0
+    growth_rate: float = 0.03
+    gamma: int = 3
+    decay: int = 3
 
 
 class _ReplicaDesc(C.Structure):
@@ -218,6 +241,11 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_trace_load": (i32, [vp, P(_TraceDesc)]),
         "pg_loglik_fwd": (i32, [vp, i32, vp, vp]),
         "pg_loglik_bwd": (i32, [vp, i32, vp, vp, vp]),
+        "pg_rc_configure": (i32, [vp, i32, P(_RcParams), vp, i64, vp, i32]),
+        "pg_rc_set_nodes": (i32, [vp, i32, i64, i64, vp, vp, vp]),
+        "pg_rc_copy_agents": (i32, [vp, i32, vp]),
+        "pg_rc_bag_table": (i32, [vp, i64, vp]),
+        "pg_rc_fitness_table": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -240,6 +268,20 @@ def philox(counter, key) -> np.ndarray:
     out = np.zeros(4, np.uint32)
     lib.pg_philox4x32_10(_ptr(c), _ptr(k), _ptr(out))
     return out
+
+
+def rc_bag_table(bag) -> np.ndarray:
+    b = np.ascontiguousarray(bag, np.int32)
+    t = np.zeros(MAX_OUT_DEGREE + 1, np.uint64)
+    if load_library().pg_rc_bag_table(_ptr(b), len(b), _ptr(t)) != PG_OK:
+        raise PGError(PG_ERR_ARG, "empty bag")
+    return t
+
+
+def rc_fitness_table() -> np.ndarray:
+    t = np.zeros(1000, np.uint64)
+    load_library().pg_rc_fitness_table(_ptr(t))
+    return t
 
 
 def poisson_table(lam: float) -> np.ndarray:
@@ -320,6 +362,34 @@ class GrowthEngine:
     def set_params(self, params: PAParams, replica: int = 0) -> None:
         p = params._c()
         self._check(self._lib.pg_set_params(self._ctx, replica, C.byref(p)))
+
+    # ---------------------------------------------------------------- refcompat functor
+    def rc_configure(self, rc: "RCParams", bag, recency, replica: int = 0) -> None:
+        """ParAGraph's own model for `replica` (context created with PG_WEIGHTS_REFCOMPAT):
+        parameters, out-degree bag and recency probabilities recency[age]."""
+        prm = _RcParams(rc.pa_weight, rc.rec_weight, rc.fit_weight, rc.alpha, rc.fully_random,
+                        rc.same_year, rc.growth_rate, int(rc.gamma), int(rc.decay))
+        b = np.ascontiguousarray(bag, np.int32)
+        r = np.ascontiguousarray(recency, np.float64)
+        self._check(self._lib.pg_rc_configure(self._ctx, replica, C.byref(prm), _ptr(b), len(b),
+                                              _ptr(r) if len(r) else None, len(r)))
+
+    def rc_set_nodes(self, first: int, lag, peak, dur, replica: int = 0) -> None:
+        """Fitness windows (lag, peak value, duration) of papers [first, first + len(lag))."""
+        lag = np.ascontiguousarray(lag, np.int32)
+        peak = np.ascontiguousarray(peak, np.int32)
+        dur = np.ascontiguousarray(dur, np.int32)
+        self._check(self._lib.pg_rc_set_nodes(self._ctx, replica, first, len(lag), _ptr(lag),
+                                              _ptr(peak), _ptr(dur)))
+
+    def rc_agents(self, replica: int = 0) -> np.ndarray:
+        """Last refcompat epoch, per new paper: pa, rec, fit weights, alpha, generator, out-degree."""
+        k = self.stats()["new_nodes"] if self.replicas == 1 else None
+        if k is None:
+            raise PGError(PG_ERR_ARG, "rc_agents of a multi-replica context: use the C ABI")
+        out = np.zeros((k, 6), np.float64)
+        self._check(self._lib.pg_rc_copy_agents(self._ctx, replica, _ptr(out)))
+        return out
 
     def set_epoch(self, epoch: int) -> None:
         self._check(self._lib.pg_set_epoch(self._ctx, epoch))

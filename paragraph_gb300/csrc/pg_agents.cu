@@ -22,6 +22,7 @@
 #include <type_traits>
 
 #include "pg_engine.cuh"
+#include "pg_rc.cuh"
 
 namespace pg {
 
@@ -42,10 +43,9 @@ struct AgentSmem {
     int32_t out[KCAP];
 };
 
-// Offer one candidate per lane to the warp's sorted top-k list (bk, bi)[0..nb).
-template <int KCAP>
-__device__ __forceinline__ void topk_offer(bool valid, float key, int id, int k, int& nb,
-                                           AgentSmem<KCAP>& S) {
+// Offer one candidate per lane to the warp's sorted top-k list (bk, bi)[0..nb) of S.
+template <typename SM>
+__device__ __forceinline__ void topk_offer(bool valid, float key, int id, int k, int& nb, SM& S) {
     const int lane = lane_id();
     bool pass = valid && (nb < k || key_less(key, id, S.bk[k - 1], S.bi[k - 1]));
     unsigned mask = __ballot_sync(kFull, pass);
@@ -281,7 +281,7 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
             float key;
             bool ok;
             boost_key(C, lane < na, anchor, key, ok);
-            topk_offer<KCAP>(ok, key, anchor, k, nb, S);
+            topk_offer(ok, key, anchor, k, nb, S);
         }
         rows += na;
         elems += na;
@@ -302,7 +302,7 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
                     float key;
                     bool ok;
                     boost_key(C, valid, y, key, ok);
-                    topk_offer<KCAP>(ok, key, y, k, nb, S);
+                    topk_offer(ok, key, y, k, nb, S);
                 }
                 int64_t yf = 0, yb = 0, ylf = 0, ylen = 0;
                 if (valid) {
@@ -336,7 +336,7 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
                     float key;
                     bool ok;
                     boost_key(C, v2, z, key, ok);
-                    topk_offer<KCAP>(ok, key, z, k, nb, S);
+                    topk_offer(ok, key, z, k, nb, S);
                 }
             }
         }
@@ -366,6 +366,7 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
 }
 
 #include "pg_thin.cuh"
+#include "pg_rc_agent.cuh"
 
 // ---------------------------------------------------------------- setup: out-degree + new nodes
 __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
@@ -376,20 +377,36 @@ __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
     const Replica& rp = A.rep[r];
     const int64_t al = a - rp.abase;
     const uint32_t ep = (uint32_t)A.st->epoch;
+    const bool rc = A.weight_model == 1;
+    // out-degree: Poisson (baseline) or the out-degree bag (refcompat), both as a 257-entry CDF
     const u32x4 x = draw(A.seed, kStreamOutDegree, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, 0);
     const int kraw = poisson_draw(A.tables + (int64_t)r * kTableEntries, kTableEntries,
                                   u64of(x.x[0], x.x[1]));
     int64_t k = kraw < 1 ? 1 : kraw;
-    if (k > rp.n) k = rp.n;
-    if (k > rp.npos) k = rp.npos;
+    if (rc) {
+        const int64_t kmax = rp.n - 1 < kKMax ? rp.n - 1 : kKMax;
+        if (k > kmax) k = kmax;
+    } else {
+        if (k > rp.n) k = rp.n;
+        if (k > rp.npos) k = rp.npos;
+    }
     A.kk[a] = (int32_t)k;
-    if (k > kKSmall) {
+    if (!rc && k > kKSmall) {
         const unsigned long long i = atomicAdd(&A.st->big_count, 1ull);
         A.big_list[i] = (int32_t)a;
     }
     const int64_t slot = rp.nbase + rp.n + al;
     A.pub[slot] = (int32_t)A.st->epoch;
-    A.fit[slot] = lognormal_fitness(A.seed, (uint32_t)(r + A.rep_base), ep, (uint32_t)al);
+    if (rc) {
+        // peak fitness from the power-law table, static window (ABM::AssignPeakFitnessValues,
+        // AssignFitnessLagDuration, AssignFitnessPeakDuration; includes/abm.cuh:447-484)
+        const u32x4 xf = draw(A.seed, kStreamRcFitness, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, 0);
+        A.fit[slot] = (float)rc_peak_draw(A.rc_ftab, u64of(xf.x[0], xf.x[1]));
+        A.rc_lag[slot] = 0;
+        A.rc_dur[slot] = 1000;
+    } else {
+        A.fit[slot] = lognormal_fitness(A.seed, (uint32_t)(r + A.rep_base), ep, (uint32_t)al);
+    }
     A.indeg[slot] = 0;
     if (A.anchors_out) {
         // the same draw the agent kernels make for the neighbourhood (recorded for traces)
@@ -421,12 +438,19 @@ __global__ void __launch_bounds__(kAgentWarps * 32) k_agents(Arena A, int64_t ag
     // which fits more CTAs per SM), 1024 for the k <= 256 one so that four warps stay within 48 KiB
     // of static shared memory
     constexpr int HCAP = (KCAP <= kKSmall && !HSMALL) ? 2 * kZCap : kZCap;
-    using Smem = typename std::conditional<THIN, ThinSmem<KCAP, HCAP>, AgentSmem<KCAP>>::type;
+    constexpr int STAGE = (KCAP <= kKSmall && HSMALL) ? 1024 : 512;
+    using Smem = typename std::conditional<THIN, ThinSmem<KCAP, HCAP, STAGE>, AgentSmem<KCAP>>::type;
     __shared__ Smem smem[kAgentWarps];
     if (A.st->error) return;
     Smem& S = smem[threadIdx.x >> 5];
     const int lane = lane_id();
     const int64_t limit = BIG ? (int64_t)A.st->big_count : agents;
+    uint32_t phase = 0;
+    if constexpr (THIN) {
+        if (lane == 0) mbar_init(&S.bar, 1);
+        fence_proxy_async();
+        __syncwarp();
+    }
     while (true) {
         long long q = 0;
         if (lane == 0)
@@ -436,11 +460,43 @@ __global__ void __launch_bounds__(kAgentWarps * 32) k_agents(Arena A, int64_t ag
         const int64_t a = BIG ? (int64_t)A.big_list[q] : q;
         const int k = A.kk[a];
         if (!BIG && k > KCAP) continue;
-        if constexpr (THIN)
-            process_agent_thin<KCAP, HCAP>(A, a, k, S);
-        else
+        if constexpr (THIN) {
+            if (!process_agent_thin<KCAP, HCAP, STAGE>(A, a, k, S, phase)) break;
+        } else
             process_agent<KCAP>(A, a, k, S);
     }
+}
+
+__global__ void __launch_bounds__(kAgentWarps * 32) k_agents_rc(Arena A, int64_t agents) {
+    __shared__ RcSmem smem[kAgentWarps];
+    if (A.st->error) return;
+    RcSmem& S = smem[threadIdx.x >> 5];
+    const int lane = lane_id();
+    while (true) {
+        long long q = 0;
+        if (lane == 0) q = (long long)atomicAdd(&A.st->queue_small, 1ull);
+        q = __shfl_sync(kFull, q, 0);
+        if (q >= agents) break;
+        process_agent_rc(A, q, A.kk[q], S);
+    }
+}
+
+static int g_blocks_rc = 0;
+
+cudaError_t init_rc_kernels() {
+    if (g_blocks_rc) return cudaSuccess;
+    const cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_rc, k_agents_rc, kAgentWarps * 32, 0);
+    if (g_blocks_rc < 1) g_blocks_rc = 1;
+    return e;
+}
+
+void launch_rc_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) {
+    if (agents <= 0) return;
+    int64_t grid = (int64_t)num_sms * (g_blocks_rc ? g_blocks_rc : 1);
+    const int64_t need = (agents + kAgentWarps - 1) / kAgentWarps;
+    if (grid > need) grid = need;
+    k_agents_rc<<<(unsigned)grid, kAgentWarps * 32, 0, s>>>(A, agents);
 }
 
 static int g_blocks[2][2] = {{0, 0}, {0, 0}};  // [thin][big]

@@ -20,6 +20,7 @@
 #include "../../include/paragraph_gb300.h"
 #include "pg_engine.cuh"
 #include "pg_lik.cuh"
+#include "pg_rc.cuh"
 
 using namespace pg;
 
@@ -29,6 +30,12 @@ struct HostRep {
     int64_t nbase, obase, ebase, n_cap, m_cap, n, m;
     int32_t tbase, ntiles;
     pg_pa_params prm;
+    // refcompat functor (pg_rc_configure)
+    bool rc = false;
+    pg_rc_params rcp{};
+    int32_t kmax = 0;                  // largest out-degree of the bag (clipped to [1, 256])
+    std::vector<uint64_t> bag_table;   // [kTableEntries]
+    std::vector<double> rtab;          // [kRcAgeMax]
 };
 
 template <typename T>
@@ -62,7 +69,7 @@ struct Checkpoint {
     int64_t epoch = 0;
     int parity = 0;
     std::vector<HostRep> hrep;
-    DBuf<int32_t> pub, indeg, fwd_col, bwd_col;
+    DBuf<int32_t> pub, indeg, fwd_col, bwd_col, rc_lag, rc_dur;
     DBuf<float> fit;
     DBuf<int64_t> fwd_off, bwd_off;
     DBuf<Replica> rep;
@@ -96,6 +103,11 @@ struct pg_ctx {
     DBuf<int64_t> fwd_off, bwd_off[2], len_tmp, sort_small, sort_large, sort_large_off, eoff,
         blocksum, er_cnt, er_toff;
     DBuf<int32_t> fwd_col, bwd_col[2];
+    // refcompat functor
+    DBuf<double> rc_pa, rc_rec, rc_fit, rc_rtab, rc_agent;
+    DBuf<int32_t> rc_lag, rc_dur, rc_cnt;
+    DBuf<uint64_t> rc_ftab;
+    DBuf<unsigned long long> rc_acc;
     // host mirror of the last epoch
     EpochState h_st{};
     std::vector<Replica> h_rep;
@@ -159,8 +171,9 @@ int64_t delta_of(const pg_pa_params& p, int64_t n) {
 
 // Upper bound on one epoch's edges for d agents (Poisson(lambda) out-degree clipped to
 // [1, min(256, n)]): mean + 8 standard deviations, never above the hard bound.
-int64_t edge_bound(int64_t d, double lambda, int64_t n) {
+int64_t edge_bound(int64_t d, double lambda, int64_t n, int32_t kmax = 0) {
     if (d <= 0) return 0;
+    if (kmax > 0) return d * std::min<int64_t>(std::min<int64_t>(kmax, kKMax), std::max<int64_t>(n - 1, 1));
     const double mu = (double)d * (lambda + 1.0);
     const int64_t stat = (int64_t)std::ceil(mu + 8.0 * std::sqrt(mu) + 64.0);
     const int64_t hard = d * std::min<int64_t>(kKMax, std::max<int64_t>(n, 1));
@@ -215,6 +228,17 @@ Arena make_arena(pg_ctx* c) {
     A.tune_small_hash = c->tune.small_hash;
     A.tune_copy_ctas = c->tune.copy_ctas_per_sm;
     A.rep_base = c->cfg.replica_base;
+    A.weight_model = c->cfg.weight_model;
+    A.rc_pa = c->rc_pa.p;
+    A.rc_rec = c->rc_rec.p;
+    A.rc_fit = c->rc_fit.p;
+    A.rc_lag = c->rc_lag.p;
+    A.rc_dur = c->rc_dur.p;
+    A.rc_rtab = c->rc_rtab.p;
+    A.rc_ftab = c->rc_ftab.p;
+    A.rc_acc = c->rc_acc.p;
+    A.rc_cnt = c->rc_cnt.p;
+    A.rc_agent = c->rc_agent.p;
     return A;
 }
 
@@ -238,6 +262,18 @@ Replica to_device_rep(const HostRep& h) {
     r.anchors = h.prm.num_anchors;
     r.p_global = 1.0 / h.prm.beta;
     r.heavy_thr = 0x7fffffff;
+    if (h.rc) {
+        const bool fixed = h.rcp.pa_weight >= 0.0 && h.rcp.rec_weight >= 0.0 && h.rcp.fit_weight >= 0.0;
+        r.rc_w[0] = fixed ? h.rcp.pa_weight : -1.0;
+        r.rc_w[1] = fixed ? h.rcp.rec_weight : -1.0;
+        r.rc_w[2] = fixed ? h.rcp.fit_weight : -1.0;
+        r.rc_alpha = h.rcp.alpha > 1.0 ? 1.0 : h.rcp.alpha;
+        r.rc_frc = h.rcp.fully_random;
+        r.rc_sy = h.rcp.same_year;
+        r.rc_gamma = h.rcp.gamma;
+        r.rc_decay = h.rcp.decay;
+        r.rc_rec_len = (int32_t)h.rtab.size();
+    }
     return r;
 }
 
@@ -300,6 +336,8 @@ void free_checkpoint(Checkpoint& k) {
     dfree(k.fwd_off);
     dfree(k.bwd_off);
     dfree(k.rep);
+    dfree(k.rc_lag);
+    dfree(k.rc_dur);
     k.valid = false;
 }
 
@@ -335,6 +373,7 @@ pg_status alloc_epoch_buffers(pg_ctx* c, int64_t agent_cap, int64_t edge_cap, in
         PG_CUDA(c, dalloc(c->big_list, agent_cap));
         PG_CUDA(c, dalloc(c->eoff, agent_cap + 1));
         if (c->cfg.record_trace) PG_CUDA(c, dalloc(c->anchors, 4 * agent_cap));
+        if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) PG_CUDA(c, dalloc(c->rc_agent, 6 * agent_cap));
         c->agent_cap = agent_cap;
     }
     if (edge_cap > c->edge_cap) {
@@ -356,6 +395,7 @@ struct HostGraph {
     std::vector<float> fit;
     std::vector<int64_t> fo, bo;
     std::vector<int32_t> fc, bc;
+    std::vector<int32_t> lag, dur;  // refcompat fitness windows (empty: lag 0, duration 1000)
 };
 
 pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<HostGraph>& hg) {
@@ -371,8 +411,10 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         h.ntiles = (int32_t)(h.n_cap / kTile);
         S += h.n_cap;
         T += h.ntiles;
-        M += std::max<int64_t>(h.m_cap, h.m + 1);
-        h.m_cap = std::max<int64_t>(h.m_cap, h.m + 1);
+        // edge regions are multiples of 4 entries, so every 16-byte-aligned window around a row
+        // (the agent kernel's bulk copies) starts and ends inside its replica's region
+        h.m_cap = round_up(std::max<int64_t>(h.m_cap, h.m + 1), 4);
+        M += h.m_cap;
     }
     c->S = S;
     c->T = T;
@@ -405,6 +447,28 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->hmask, S * kMaskWords));
     PG_CUDA(c, dalloc(c->hub2, (int64_t)R * kHeavyMax * kMaskWords));
     PG_CUDA(c, dalloc(c->hlist, (int64_t)R * kHeavyMax));
+    if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
+        PG_CUDA(c, dalloc(c->rc_pa, S));
+        PG_CUDA(c, dalloc(c->rc_rec, S));
+        PG_CUDA(c, dalloc(c->rc_fit, S));
+        PG_CUDA(c, dalloc(c->rc_lag, S));
+        PG_CUDA(c, dalloc(c->rc_dur, S));
+        PG_CUDA(c, dalloc(c->rc_acc, 4 * (int64_t)R));
+        PG_CUDA(c, dalloc(c->rc_cnt, (int64_t)R * kRcAgeMax));
+        PG_CUDA(c, dalloc(c->rc_rtab, (int64_t)R * kRcAgeMax));
+        if (!c->rc_ftab.p) {
+            std::vector<uint64_t> ft(kRcFitMax);
+            rc_fitness_table_host(ft.data());
+            PG_CUDA(c, dalloc(c->rc_ftab, kRcFitMax));
+            PG_CUDA(c, cudaMemcpyAsync(c->rc_ftab.p, ft.data(), 8 * ft.size(), cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaStreamSynchronize(c->stream));
+        }
+        std::vector<double> rt((size_t)R * kRcAgeMax, 0.0);
+        for (int r = 0; r < R; ++r)
+            std::copy(reps[r].rtab.begin(), reps[r].rtab.end(), rt.begin() + (size_t)r * kRcAgeMax);
+        PG_CUDA(c, cudaMemcpyAsync(c->rc_rtab.p, rt.data(), 8 * rt.size(), cudaMemcpyHostToDevice, c->stream));
+        PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
     PG_CUDA(c, cudaMemsetAsync(c->hslot.p, 0xFF, 2 * (size_t)S, c->stream));
     PG_CUDA(c, cudaMemsetAsync(c->inc.p, 0, sizeof(int32_t) * (size_t)S, c->stream));
     PG_CUDA(c, cudaMemsetAsync(c->w.p, 0, sizeof(float) * (size_t)S, c->stream));
@@ -416,9 +480,20 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         const HostRep& h = reps[r];
         for (int t = 0; t < h.ntiles; ++t) trep[(size_t)h.tbase + t] = r;
         drep[(size_t)r] = to_device_rep(h);
-        poisson_table(h.prm.mean_out_degree, tabs.data() + (size_t)r * kTableEntries, kTableEntries);
+        if (h.rc)
+            std::copy(h.bag_table.begin(), h.bag_table.end(), tabs.begin() + (size_t)r * kTableEntries);
+        else
+            poisson_table(h.prm.mean_out_degree, tabs.data() + (size_t)r * kTableEntries, kTableEntries);
         const HostGraph& g = hg[(size_t)r];
         const size_t n = (size_t)h.n, m = (size_t)h.m;
+        if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
+            std::vector<int32_t> lag(n, 0), dur(n, 1000);
+            const std::vector<int32_t>& L = g.lag.size() == n ? g.lag : lag;
+            const std::vector<int32_t>& D = g.dur.size() == n ? g.dur : dur;
+            PG_CUDA(c, cudaMemcpyAsync(c->rc_lag.p + h.nbase, L.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(c->rc_dur.p + h.nbase, D.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaStreamSynchronize(c->stream));
+        }
         PG_CUDA(c, cudaMemcpyAsync(c->pub.p + h.nbase, g.pub.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
         PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase, g.fit.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
         PG_CUDA(c, cudaMemcpyAsync(c->indeg.p + h.nbase, g.indeg.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
@@ -463,6 +538,12 @@ pg_status download_graph(pg_ctx* c, int r, HostGraph& g) {
         PG_CUDA(c, cudaMemcpyAsync(g.fc.data(), c->fwd_col.p + h.ebase, 4 * m, cudaMemcpyDeviceToHost, c->stream));
         PG_CUDA(c, cudaMemcpyAsync(g.bc.data(), c->bwd_col[c->parity].p + h.ebase, 4 * m, cudaMemcpyDeviceToHost, c->stream));
     }
+    if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
+        g.lag.resize(n);
+        g.dur.resize(n);
+        PG_CUDA(c, cudaMemcpyAsync(g.lag.data(), c->rc_lag.p + h.nbase, 4 * n, cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(g.dur.data(), c->rc_dur.p + h.nbase, 4 * n, cudaMemcpyDeviceToHost, c->stream));
+    }
     PG_CUDA(c, cudaStreamSynchronize(c->stream));
     return PG_OK;
 }
@@ -500,7 +581,8 @@ pg_status device_error(pg_ctx* c) {
     if (e & kErrCapacity) msg += " capacity exceeded;";
     if (e & kErrBadWeight) msg += " non-finite or all-zero weights;";
     if (e & kErrArg) msg += " inconsistent agent draw;";
-    return fail(c, (e & kErrCapacity) ? PG_ERR_CAPACITY : PG_ERR_ARG, msg);
+    if (e & kErrTimeout) msg += " bounded wait on an asynchronous copy ran out;";
+    return fail(c, (e & kErrCapacity) ? PG_ERR_CAPACITY : ((e & kErrTimeout) ? PG_ERR_TIMEOUT : PG_ERR_ARG), msg);
 }
 
 float ms_between(cudaEvent_t a, cudaEvent_t b) {
@@ -538,6 +620,23 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
     if (events) record_event(ev[0], s);
     launch_epoch_begin(A, epoch, 1, s);
     PG_STAGE("epoch begin");
+    if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
+        // ParAGraph's own model: score components, out-degrees, the per-paper rule, CSR append
+        launch_rc_scores(A, s);
+        PG_STAGE("refcompat scores");
+        if (events) record_event(ev[1], s);
+        launch_agent_setup(A, agents, s);
+        PG_STAGE("agent setup");
+        if (events) record_event(ev[2], s);
+        launch_rc_agents(A, agents, c->num_sms, s);
+        PG_STAGE("refcompat agents");
+        if (events) record_event(ev[3], s);
+        launch_bwd_append(A, agents, c->num_sms, s);
+        PG_STAGE("backward append");
+        if (events) record_event(ev[4], s);
+        c->launches += kPaEpochKernels - 4 - 2 + kRcScoreKernels + 1;
+        return PG_OK;
+    }
     launch_weights(A, s);
     PG_STAGE("weights");
     if (c->cfg.sampler == PG_SAMPLER_THINNING) {
@@ -637,15 +736,26 @@ pg_status finish_epoch(pg_ctx* c, const std::vector<int64_t>& deltas, bool er) {
     return PG_OK;
 }
 
+pg_status check_rc_ready(pg_ctx* c) {
+    if (c->cfg.weight_model != PG_WEIGHTS_REFCOMPAT) return PG_OK;
+    for (int r = 0; r < c->R; ++r) {
+        if (!c->hrep[(size_t)r].rc)
+            return fail(c, PG_ERR_STATE, "refcompat context: call pg_rc_configure for every replica first");
+        if (c->hrep[(size_t)r].n < 2) return fail(c, PG_ERR_STATE, "refcompat growth needs at least 2 nodes");
+    }
+    return PG_OK;
+}
+
 pg_status prepare_pa(pg_ctx* c, std::vector<int64_t>& deltas, int64_t& agents) {
     if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (check_rc_ready(c) != PG_OK) return PG_ERR_STATE;
     if (c->poisoned) return fail(c, PG_ERR_STATE, "an earlier epoch failed on the device; reload the graph");
     agents = plan_epoch(c, &deltas);
     if (agents <= 0) return fail(c, PG_ERR_ARG, "epoch adds no nodes");
     int64_t ebound = 0;
     for (int r = 0; r < c->R; ++r) {
         const HostRep& h = c->hrep[(size_t)r];
-        const int64_t eb = edge_bound(deltas[(size_t)r], h.prm.mean_out_degree, h.n);
+        const int64_t eb = edge_bound(deltas[(size_t)r], h.prm.mean_out_degree, h.n, h.rc ? h.kmax : 0);
         ebound += eb;
         if (c->R == 1) {
             pg_status s = ensure_capacity(c, h.n + deltas[(size_t)r], h.m + eb);
@@ -695,6 +805,7 @@ pg_status pg_create(pg_ctx** out, const pg_config* cfg) {
     if (!out || !cfg) return PG_ERR_ARG;
     *out = nullptr;
     if (cfg->num_replicas < 1 || cfg->replica_base < 0) return PG_ERR_ARG;
+    if (cfg->weight_model != PG_WEIGHTS_BASELINE && cfg->weight_model != PG_WEIGHTS_REFCOMPAT) return PG_ERR_ARG;
     pg_ctx* c = new (std::nothrow) pg_ctx();
     if (!c) return PG_ERR_CAPACITY;
     c->cfg = *cfg;
@@ -706,6 +817,7 @@ pg_status pg_create(pg_ctx** out, const pg_config* cfg) {
     if (e == cudaSuccess) e = dalloc(c->st, 1);
     if (e == cudaSuccess) e = init_agent_kernels();
     if (e == cudaSuccess) e = init_csr_kernels();
+    if (e == cudaSuccess && cfg->weight_model == PG_WEIGHTS_REFCOMPAT) e = init_rc_kernels();
     for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->tev[i]);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->lev[i]);
@@ -737,6 +849,16 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->w);
     dfree(c->cdf);
     dfree(c->guide);
+    dfree(c->rc_pa);
+    dfree(c->rc_rec);
+    dfree(c->rc_fit);
+    dfree(c->rc_rtab);
+    dfree(c->rc_agent);
+    dfree(c->rc_lag);
+    dfree(c->rc_dur);
+    dfree(c->rc_cnt);
+    dfree(c->rc_ftab);
+    dfree(c->rc_acc);
     dfree(c->tilesum);
     dfree(c->tileoff);
     dfree(c->tables);
@@ -815,7 +937,7 @@ pg_status pg_load_replicas(pg_ctx* c, const pg_replica_desc* descs, int32_t num)
         }
         for (int e = 0; e < epochs; ++e) {
             const int64_t dl = delta_of(h.prm, n);
-            const int64_t eb = edge_bound(dl, h.prm.mean_out_degree, n);
+            const int64_t eb = edge_bound(dl, h.prm.mean_out_degree, n, h.rc ? h.kmax : 0);
             plan_agents[(size_t)e] += dl;
             plan_edges[(size_t)e] += eb;
             n += dl;
@@ -859,9 +981,13 @@ pg_status pg_set_params(pg_ctx* c, int32_t replica, const pg_pa_params* p) {
     if (s != PG_OK) return s;
     HostRep& h = c->hrep[(size_t)replica];
     h.prm = *p;
+    if (h.rc) h.prm.growth_rate = h.rcp.growth_rate;  // the refcompat growth rate stays in force
     destroy_graph_exec(c);
     std::vector<uint64_t> tab(kTableEntries);
-    poisson_table(p->mean_out_degree, tab.data(), kTableEntries);
+    if (h.rc)
+        tab = h.bag_table;
+    else
+        poisson_table(p->mean_out_degree, tab.data(), kTableEntries);
     PG_CUDA(c, cudaMemcpyAsync(c->tables.p + (size_t)replica * kTableEntries, tab.data(), 8 * tab.size(),
                                cudaMemcpyHostToDevice, c->stream));
     // refresh the parameter fields of the device replica
@@ -933,7 +1059,7 @@ pg_status plan_run(pg_ctx* c, int num_epochs, std::vector<int64_t>& agents, int6
         for (int r = 0; r < c->R; ++r) {
             HostRep& h = planned[(size_t)r];
             const int64_t d = delta_of(h.prm, h.n);
-            const int64_t b = edge_bound(d, h.prm.mean_out_degree, h.n);
+            const int64_t b = edge_bound(d, h.prm.mean_out_degree, h.n, h.rc ? h.kmax : 0);
             tot += d;
             eb += b;
             h.n += d;
@@ -961,6 +1087,7 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
     if (num_epochs < 1) return fail(c, PG_ERR_ARG, "num_epochs must be >= 1");
     if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
     if (c->poisoned) return fail(c, PG_ERR_STATE, "an earlier epoch failed on the device; reload the graph");
+    if (check_rc_ready(c) != PG_OK) return PG_ERR_STATE;
     PG_CUDA(c, cudaSetDevice(c->device));
     std::vector<int64_t> agents;
     int64_t max_agents = 0, max_edges = 0;
@@ -1290,6 +1417,14 @@ pg_status pg_checkpoint(pg_ctx* c) {
         PG_CUDA(c, dalloc(k.bwd_col, c->M));
     }
     const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
+    if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
+        if (k.rc_lag.n != c->S) {
+            PG_CUDA(c, dalloc(k.rc_lag, c->S));
+            PG_CUDA(c, dalloc(k.rc_dur, c->S));
+        }
+        PG_CUDA(c, cudaMemcpyAsync(k.rc_lag.p, c->rc_lag.p, 4 * (size_t)c->S, d2d, s));
+        PG_CUDA(c, cudaMemcpyAsync(k.rc_dur.p, c->rc_dur.p, 4 * (size_t)c->S, d2d, s));
+    }
     PG_CUDA(c, cudaMemcpyAsync(k.pub.p, c->pub.p, 4 * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(k.indeg.p, c->indeg.p, 4 * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(k.fit.p, c->fit.p, 4 * (size_t)c->S, d2d, s));
@@ -1318,6 +1453,10 @@ pg_status pg_restore(pg_ctx* c) {
     const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
     // the checkpoint's backward copy goes into the buffer that was current when it was taken
     const int par = k.parity;
+    if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT && k.rc_lag.n == c->S) {
+        PG_CUDA(c, cudaMemcpyAsync(c->rc_lag.p, k.rc_lag.p, 4 * (size_t)c->S, d2d, s));
+        PG_CUDA(c, cudaMemcpyAsync(c->rc_dur.p, k.rc_dur.p, 4 * (size_t)c->S, d2d, s));
+    }
     PG_CUDA(c, cudaMemcpyAsync(c->pub.p, k.pub.p, 4 * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(c->indeg.p, k.indeg.p, 4 * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(c->fit.p, k.fit.p, 4 * (size_t)c->S, d2d, s));
@@ -1457,6 +1596,113 @@ float pg_logf_host(float x) { return logf_pg(x); }
 float pg_expf_host(float x) { return expf_pg(x); }
 double pg_log_host(double x) { return log_pg(x); }
 double pg_exp_host(double x) { return exp_pg(x); }
+
+
+// ---------------------------------------------------------------- refcompat functor
+pg_status pg_rc_bag_table(const int32_t* bag, int64_t len, uint64_t* table) {
+    if (!bag || len <= 0 || !table) return PG_ERR_ARG;
+    rc_bag_table_host(bag, len, table);
+    return PG_OK;
+}
+
+pg_status pg_rc_fitness_table(uint64_t* table) {
+    if (!table) return PG_ERR_ARG;
+    rc_fitness_table_host(table);
+    return PG_OK;
+}
+
+pg_status pg_rc_configure(pg_ctx* c, int32_t replica, const pg_rc_params* p, const int32_t* bag,
+                          int64_t bag_len, const double* rec, int32_t rec_len) {
+    if (!c || !p) return PG_ERR_ARG;
+    if (c->cfg.weight_model != PG_WEIGHTS_REFCOMPAT)
+        return fail(c, PG_ERR_STATE, "the context was not created with PG_WEIGHTS_REFCOMPAT");
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "load a graph first");
+    if (replica < 0 || replica >= c->R) return fail(c, PG_ERR_ARG, "replica out of range");
+    if (!bag || bag_len <= 0) return fail(c, PG_ERR_ARG, "the out-degree bag is empty");
+    if (rec_len < 0 || rec_len > kRcAgeMax || (rec_len > 0 && !rec))
+        return fail(c, PG_ERR_ARG, "recency table must have 0..1024 entries");
+    if (!(p->growth_rate > 0.0)) return fail(c, PG_ERR_ARG, "growth_rate must be > 0");
+    if (!(p->fully_random >= 0.0 && p->fully_random <= 1.0)) return fail(c, PG_ERR_ARG, "fully_random must be in [0, 1]");
+    if (!(p->same_year >= 0.0 && p->same_year <= 1.0)) return fail(c, PG_ERR_ARG, "same_year must be in [0, 1]");
+    if (p->gamma < 1 || p->gamma > 4 || p->decay < 0 || p->decay > 8)
+        return fail(c, PG_ERR_ARG, "gamma must be in [1, 4] and decay in [0, 8]");
+    const bool fixed = p->pa_weight >= 0.0 && p->rec_weight >= 0.0 && p->fit_weight >= 0.0;
+    if (fixed && !(p->pa_weight + p->rec_weight + p->fit_weight > 0.0))
+        return fail(c, PG_ERR_ARG, "the three score weights sum to zero");
+    for (int i = 0; i < rec_len; ++i)
+        if (!(rec[i] >= 0.0) || !std::isfinite(rec[i])) return fail(c, PG_ERR_ARG, "recency probabilities must be finite and >= 0");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    HostRep& h = c->hrep[(size_t)replica];
+    h.rc = true;
+    h.rcp = *p;
+    h.prm.growth_rate = p->growth_rate;
+    h.prm.fixed_new_nodes = 0;
+    h.bag_table.assign(kTableEntries, 0);
+    rc_bag_table_host(bag, bag_len, h.bag_table.data());
+    int32_t kmax = 1;
+    for (int64_t i = 0; i < bag_len; ++i) kmax = std::max(kmax, std::min<int32_t>(bag[i], kKMax));
+    h.kmax = kmax;
+    h.rtab.assign(rec, rec + rec_len);
+    destroy_graph_exec(c);
+    std::vector<double> rt(kRcAgeMax, 0.0);
+    std::copy(h.rtab.begin(), h.rtab.end(), rt.begin());
+    PG_CUDA(c, cudaMemcpyAsync(c->rc_rtab.p + (size_t)replica * kRcAgeMax, rt.data(), 8 * rt.size(),
+                               cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(c->tables.p + (size_t)replica * kTableEntries, h.bag_table.data(),
+                               8 * h.bag_table.size(), cudaMemcpyHostToDevice, c->stream));
+    Replica dr;
+    PG_CUDA(c, cudaMemcpyAsync(&dr, c->rep.p + replica, sizeof(Replica), cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    const Replica fresh = to_device_rep(h);
+    for (int i = 0; i < 3; ++i) dr.rc_w[i] = fresh.rc_w[i];
+    dr.rc_alpha = fresh.rc_alpha;
+    dr.rc_frc = fresh.rc_frc;
+    dr.rc_sy = fresh.rc_sy;
+    dr.rc_gamma = fresh.rc_gamma;
+    dr.rc_decay = fresh.rc_decay;
+    dr.rc_rec_len = fresh.rc_rec_len;
+    dr.growth_rate = fresh.growth_rate;
+    dr.fixed_new = fresh.fixed_new;
+    PG_CUDA(c, cudaMemcpyAsync(c->rep.p + replica, &dr, sizeof(Replica), cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status pg_rc_set_nodes(pg_ctx* c, int32_t replica, int64_t first, int64_t count, const int32_t* lag,
+                          const int32_t* peak, const int32_t* dur) {
+    if (!c || !lag || !peak || !dur) return PG_ERR_ARG;
+    if (c->cfg.weight_model != PG_WEIGHTS_REFCOMPAT)
+        return fail(c, PG_ERR_STATE, "the context was not created with PG_WEIGHTS_REFCOMPAT");
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "load a graph first");
+    if (replica < 0 || replica >= c->R) return fail(c, PG_ERR_ARG, "replica out of range");
+    const HostRep& h = c->hrep[(size_t)replica];
+    if (first < 0 || count < 0 || first + count > h.n) return fail(c, PG_ERR_ARG, "node range out of bounds");
+    if (count == 0) return PG_OK;
+    std::vector<float> pk((size_t)count);
+    for (int64_t i = 0; i < count; ++i) {
+        if (peak[i] < 1 || lag[i] < 0 || dur[i] < 0) return fail(c, PG_ERR_ARG, "peak must be >= 1, lag and duration >= 0");
+        pk[(size_t)i] = (float)peak[i];
+    }
+    PG_CUDA(c, cudaSetDevice(c->device));
+    PG_CUDA(c, cudaMemcpyAsync(c->rc_lag.p + h.nbase + first, lag, 4 * (size_t)count, cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(c->rc_dur.p + h.nbase + first, dur, 4 * (size_t)count, cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase + first, pk.data(), 4 * (size_t)count, cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status pg_rc_copy_agents(pg_ctx* c, int32_t replica, double* out) {
+    if (!c || !out) return PG_ERR_ARG;
+    if (c->cfg.weight_model != PG_WEIGHTS_REFCOMPAT)
+        return fail(c, PG_ERR_STATE, "the context was not created with PG_WEIGHTS_REFCOMPAT");
+    if (replica < 0 || replica >= c->R) return fail(c, PG_ERR_ARG, "replica out of range");
+    if (c->h_rep.size() != (size_t)c->R || !c->rc_agent.p) return fail(c, PG_ERR_STATE, "no refcompat epoch has run");
+    const Replica& r = c->h_rep[(size_t)replica];
+    PG_CUDA(c, cudaSetDevice(c->device));
+    PG_CUDA(c, cudaMemcpyAsync(out, c->rc_agent.p + 6 * r.abase, 8 * 6 * (size_t)r.delta, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
 
 }  // extern "C"
 

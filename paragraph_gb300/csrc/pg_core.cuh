@@ -78,6 +78,9 @@ enum Stream : uint32_t {
     kStreamSameYear = 7,
     kStreamUniformFill = 8,
     kStreamFallback = 9,
+    kStreamRcAgent = 10,
+    kStreamRcKey = 11,
+    kStreamRcFitness = 12,
 };
 
 // Counter layout: (i, unit, epoch, stream << 24 | aux); key = (seed lo, seed hi).

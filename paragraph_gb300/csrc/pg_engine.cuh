@@ -31,6 +31,9 @@ constexpr int kHeavyMax = 256;       // hubs per replica with a bit in the per-n
 constexpr int kMaskWords = kHeavyMax / 64;
 constexpr int kHeavyMinLog = 10;     // only nodes with degree >= 2^10 can be hubs
 constexpr int kHeavyBins = 24;       // log2-degree histogram bins 10..33
+constexpr int kRcAgeMax = 1024;      // recency probabilities by age 0..1023 (refcompat)
+constexpr int kRcFitMax = 1000;      // peak fitness values 1..1000 (refcompat)
+constexpr uint32_t kRcFillBlocks = 1u << 20;  // Philox blocks a uniform fill may use
 
 enum Sampler : int32_t {
     kSamplerThinning = 0,   // Poisson thinning against ball membership (default)
@@ -42,6 +45,7 @@ enum : uint32_t {
     kErrCapacity = 1u,
     kErrBadWeight = 2u,
     kErrArg = 4u,
+    kErrTimeout = 8u,  // a bounded wait on an asynchronous copy ran out
 };
 
 struct Replica {
@@ -71,6 +75,13 @@ struct Replica {
     int32_t heavy_count;
     int32_t heavy_hist[kHeavyBins];
     int64_t ctbase;  // first backward-copy tile of the replica this epoch
+    // refcompat functor (weight model PG_WEIGHTS_REFCOMPAT)
+    double rc_w[3];   // pa, rec, fit weights, normalised; rc_w[0] < 0: drawn per agent
+    double rc_alpha;  // share of the neighbourhood budget from the 1-hop set; < 0: per agent
+    double rc_frc;    // fraction of the out-degree reserved for uniform citations
+    double rc_sy;     // fraction of agents citing a paper of their own epoch
+    double rc_dpa, rc_dfit, rc_U;  // this epoch: score normalisers and the recency denominator
+    int32_t rc_gamma, rc_decay, rc_rec_len, rc_pad;
 };
 
 // Per-epoch device scalars; reset by the epoch-begin kernel.
@@ -145,6 +156,19 @@ struct Arena {
     uint64_t* hmask;           // [slots][kMaskWords] bit b set when hub b is adjacent to the node
     uint64_t* hub2;            // [R][kHeavyMax][kMaskWords] hubs sharing a neighbour with hub b
     int32_t* hlist;            // [R][kHeavyMax] hub node ids
+    // refcompat functor (null unless the context uses PG_WEIGHTS_REFCOMPAT)
+    double* rc_pa;             // [slots] score components of the epoch
+    double* rc_rec;
+    double* rc_fit;
+    int32_t* rc_lag;           // [slots] fitness window: lag and peak duration (peak = fit)
+    int32_t* rc_dur;
+    const double* rc_rtab;     // [R][kRcAgeMax] recency probability by age
+    const uint64_t* rc_ftab;   // [kRcFitMax] peak-fitness CDF thresholds (2^64 scale)
+    unsigned long long* rc_acc;  // [R][4] 128-bit sums of the pa and fit numerators (lo, hi)
+    int32_t* rc_cnt;           // [R][kRcAgeMax] nodes per age
+    double* rc_agent;          // [agent cap][6] pa, rec, fit weights, alpha, generator, out-degree
+    int32_t weight_model;      // PG_WEIGHTS_*
+    int32_t pad_wm;
     EpochState* st;
     int64_t agent_cap, edge_cap;
     uint64_t seed;
@@ -253,6 +277,11 @@ void launch_tile_scan(const Arena& A, int mode, cudaStream_t s);
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s);
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
 void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
+// refcompat functor: score components of the epoch (4 kernels) and the agent kernel
+constexpr int kRcScoreKernels = 4;
+void launch_rc_scores(const Arena& A, cudaStream_t s);
+void launch_rc_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
+cudaError_t init_rc_kernels();
 void launch_er_epoch(const Arena& A, int64_t delta, double p, int64_t n, int64_t* cnt,
                      int64_t* toff, int num_sms, cudaStream_t s);
 // generic exclusive scan of n values; out has n+1 entries (out[n] = total)

@@ -20,14 +20,61 @@
 // adj(j) (forward row, then backward row) 32 entries at a time and stops at the first hit; the
 // number of entries it examined feeds the byte model.
 
-template <int KCAP, int HCAP>
+constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a bulk-copy barrier before giving up
+
+// STAGE: adjacency entries staged per chunk and warp (1024 in the small-hash k <= 64 kernel, 512
+// where the frontier hash or k is larger, so four warps stay within 48 KiB of static shared memory)
+template <int KCAP, int HCAP, int STAGE>
 struct ThinSmem {
+    __align__(16) int32_t stage[STAGE];  // candidate rows, filled by bulk asynchronous copies
     int32_t H[HCAP];  // frontier hash set, -1 = empty
     int32_t arr[KCAP];
     int32_t out[KCAP];
     int32_t c_id[KCAP];
     uint64_t c_cq[KCAP];
+    unsigned long long bar;  // mbarrier of the warp's bulk copies
 };
+
+// ---- bulk asynchronous copies (the TMA engine's cp.async.bulk) into shared memory
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the phase with the given parity; false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// bytes (a multiple of 16, both addresses 16-byte aligned) from global to shared memory, counted
+// on the barrier's transaction bytes
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
 
 struct Mask {
     unsigned long long w[kMaskWords];
@@ -114,47 +161,9 @@ __device__ __forceinline__ bool in_z(const Ball& B, int32_t v) {
     return false;
 }
 
-// Rows of at most this many entries (forward + backward) are tested by one lane; longer ones by
-// the whole warp.
-constexpr int kLaneRows = 32;
-
-// Membership of the lane's own candidate j, every lane at once.  `examined` gets the adjacency
-// entries looked at, in order (forward row, then backward row), up to and including the first hit.
-// When j is not in Z, not a hub and its rows are longer than kLaneRows, `decided` is false and the
-// answer comes from member_rows_warp.
-__device__ bool member_lane(const Ball& B, int32_t j, long long& examined, bool& decided) {
-    examined = 0;
-    decided = true;
-    if (in_z(B, j)) return true;
-    const int hs = hub_slot(B, j);
-    if (hs >= 0) return mask_bit(B.hm, hs);
-    const int64_t f0 = B.fo[j], f1 = B.fo[j + 1], b0 = B.bo[j], b1 = B.bo[j + 1];
-    const int64_t nf = f1 - f0, d = nf + (b1 - b0);
-    if (d > kLaneRows) {
-        decided = false;
-        return false;
-    }
-    // four entries in flight per step; position q of the concatenated rows
-    for (int64_t q = 0; q < d; q += 4) {
-        int32_t v[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int64_t x = q + u;
-            v[u] = x < d ? (x < nf ? B.fc[f0 + x] : B.bc[b0 + (x - nf)]) : -1;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (v[u] >= 0 && in_z(B, v[u])) {
-                examined = q + u + 1;
-                return true;
-            }
-    }
-    examined = d;
-    return false;
-}
-
 // Warp-cooperative row scan of a non-hub j outside Z (warp-uniform argument and result), 128
-// entries per step; `examined` as in member_lane.
+// entries per step.  `examined` gets the adjacency entries looked at, in order (forward row, then
+// backward row), up to and including the first hit.
 __device__ bool member_rows_warp(const Ball& B, int32_t j, long long& examined) {
     const int lane = lane_id();
     examined = 0;
@@ -192,8 +201,11 @@ __device__ bool member_warp(const Ball& B, int32_t j, long long& examined) {
     return member_rows_warp(B, j, examined);
 }
 
-template <int KCAP, int HCAP>
-__device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KCAP, HCAP>& S) {
+// Returns false when a bounded wait ran out (the error word is set and the warp must stop).
+template <int KCAP, int HCAP, int STAGE>
+__device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KCAP, HCAP, STAGE>& S,
+                                   uint32_t& phase) {
+    constexpr int kStage = STAGE;
     constexpr int kHBits = HCAP == 4096 ? 12 : (HCAP == 2048 ? 11 : 10);
     static_assert(HCAP == (1 << kHBits), "hash capacity must be 1024, 2048 or 4096");
     constexpr int ZCAP = HCAP / 2;  // entries gathered into the frontier (with repeats)
@@ -313,6 +325,7 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     const int32_t* guide = A.guide + rp.nbase;
     const int gs = guide_shift(Wq, n);
     const int64_t used = Wq ? (int64_t)((Wq - 1) >> gs) + 1 : 0;
+    const unsigned below = (1u << lane) - 1u;
     for (int i0 = 0; i0 < maxev && nch < k; i0 += 32) {
         const u32x4 x = draw(A.seed, kStreamGlobal, rep, ep, unit, (uint32_t)(i0 + lane));
         const uint64_t y = mulhi64(u64of(x.x[0], x.x[1]), Wq);
@@ -327,30 +340,140 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
         }
         const int j = (int)lo;
         const bool glob = u01d(x.x[2], x.x[3]) <= pg;
-        // every boost candidate of the batch tested at once (a pure function of j, so testing
-        // events that end up unused changes nothing); long rows wait for the warp below
-        long long ex_l = 0;
-        bool dec_l = true, mem_l = true;
-        if (!glob) mem_l = member_lane(B, j, ex_l, dec_l);
-        for (int l = 0; l < 32 && nch < k; ++l) {
-            const int jl = __shfl_sync(kFull, j, l);
-            const bool gl = __shfl_sync(kFull, glob, l);
-            ++events;
-            bool dup = false;
-            for (int q = lane; q < nch; q += 32) dup |= (S.arr[q] == jl);
-            if (__any_sync(kFull, dup)) continue;
-            if (!gl) {
-                ++tests;
-                long long ex = __shfl_sync(kFull, ex_l, l);
-                bool mem = __shfl_sync(kFull, mem_l, l);
-                if (!__shfl_sync(kFull, dec_l, l)) mem = member_rows_warp(B, jl, ex);
-                scanned += ex;
-                if (!mem) continue;
+        // The 32 events of the batch are decided together, with the result of taking them one
+        // at a time in event order: an event whose node was already chosen is skipped, a boost
+        // event is tested for membership, and the first k acceptances end the draw.
+        bool pre = false;  // node chosen by an earlier batch
+        for (int q = 0; q < nch; ++q) pre |= S.arr[q] == j;
+        // one membership test per distinct boost node, by the lowest lane holding it
+        const unsigned grp = __match_any_sync(kFull, j);
+        const unsigned bm = __ballot_sync(kFull, !glob);
+        bool mem = false, scan = false;
+        long long ex = 0;
+        int64_t d = 0, f0 = 0, lf = 0, b0 = 0;
+        if (lane == __ffs(grp) - 1 && !pre && (grp & bm)) {
+            if (in_z(B, j)) {
+                mem = true;
+            } else {
+                const int hs = hub_slot(B, j);
+                if (hs >= 0) {
+                    mem = mask_bit(B.hm, hs);
+                } else {
+                    f0 = B.fo[j];
+                    lf = B.fo[j + 1] - f0;
+                    b0 = B.bo[j];
+                    d = lf + (B.bo[j + 1] - b0);
+                    scan = d > 0;
+                    ex = d;  // a miss examines both rows
+                }
             }
-            if (lane == 0) S.arr[nch] = jl;
-            __syncwarp();
-            ++nch;
         }
+        // The rows of every node under test are staged into shared memory by bulk asynchronous
+        // copies of 16-byte-aligned windows around them (forward window, then backward window,
+        // lane after lane), kStage entries per chunk, and tested against the frontier owner by
+        // owner; a row stops at its first hit, and a row with a hit copies nothing more.
+        const int64_t lb = d - lf;
+        const int64_t fa0 = f0 & ~3ll, fw = lf > 0 ? (((f0 + lf + 3) & ~3ll) - fa0) : 0;
+        const int64_t ba0 = b0 & ~3ll, bw = lb > 0 ? (((b0 + lb + 3) & ~3ll) - ba0) : 0;
+        const int64_t W = scan ? fw + bw : 0;
+        const int64_t wincl = warp_incl_scan(W);
+        const int64_t wx = wincl - W;
+        const int64_t DW = __shfl_sync(kFull, wincl, 31);
+        int64_t mp = d;  // first-hit position of this lane's node (d: none yet)
+        for (int64_t c0 = 0; c0 < DW; c0 += kStage) {
+            const int64_t c1 = c0 + kStage < DW ? c0 + kStage : DW;
+            int64_t s0 = wx > c0 ? wx : c0, s1 = wx + W < c1 ? wx + W : c1;
+            if (mp < d || s1 < s0) s1 = s0;
+            const uint32_t total = __reduce_add_sync(kFull, (uint32_t)(s1 - s0) * 4u);
+            if (total == 0) continue;
+            __syncwarp();  // the previous chunk's reads of the stage are done
+            fence_proxy_async();
+            if (lane == 0) mbar_expect_tx(&S.bar, total);
+            __syncwarp();
+            if (s1 > s0) {
+                const int64_t fe = wx + fw;
+                if (s0 < fe) {
+                    const int64_t e1 = s1 < fe ? s1 : fe;
+                    bulk_g2s(&S.stage[s0 - c0], B.fc + fa0 + (s0 - wx), (uint32_t)(e1 - s0) * 4u, &S.bar);
+                }
+                if (s1 > fe) {
+                    const int64_t e0 = s0 > fe ? s0 : fe;
+                    bulk_g2s(&S.stage[e0 - c0], B.bc + ba0 + (e0 - fe), (uint32_t)(s1 - e0) * 4u, &S.bar);
+                }
+            }
+            const bool ok = mbar_wait(&S.bar, phase);
+            phase ^= 1u;
+            if (!__all_sync(kFull, ok)) {
+                // give the copies in flight a second bounded wait, then abandon the warp
+                if (lane == 0) atomicOr(&A.st->error, kErrTimeout);
+                mbar_wait(&S.bar, phase ^ 1u);
+                return false;
+            }
+            unsigned om = __ballot_sync(kFull, s1 > s0);
+            while (om) {
+                const int o = __ffs(om) - 1;
+                om &= om - 1u;
+                const int64_t os0 = __shfl_sync(kFull, s0, o), os1 = __shfl_sync(kFull, s1, o);
+                const int64_t owx = __shfl_sync(kFull, wx, o), ofw = __shfl_sync(kFull, fw, o);
+                const int64_t ofa0 = __shfl_sync(kFull, fa0, o), of0 = __shfl_sync(kFull, f0, o);
+                const int64_t olf = __shfl_sync(kFull, lf, o), oba0 = __shfl_sync(kFull, ba0, o);
+                const int64_t ob0 = __shfl_sync(kFull, b0, o), olb = __shfl_sync(kFull, lb, o);
+                for (int64_t q0 = os0; q0 < os1; q0 += 32) {
+                    const int64_t q = q0 + lane;
+                    bool hit = false;
+                    int64_t x = 0;
+                    if (q < os1) {
+                        const int64_t off = q - owx;
+                        bool valid;
+                        if (off < ofw) {
+                            const int64_t idx = ofa0 + off;
+                            valid = idx >= of0 && idx < of0 + olf;
+                            x = idx - of0;
+                        } else {
+                            const int64_t idx = oba0 + (off - ofw);
+                            valid = idx >= ob0 && idx < ob0 + olb;
+                            x = olf + (idx - ob0);
+                        }
+                        if (valid) hit = in_z(B, S.stage[q - c0]);
+                    }
+                    const unsigned hm = __ballot_sync(kFull, hit);
+                    if (hm) {
+                        const int64_t xh = __shfl_sync(kFull, x, __ffs(hm) - 1);
+                        if (lane == o) mp = xh;
+                        break;
+                    }
+                }
+            }
+        }
+        if (scan && mp < d) {
+            mem = true;
+            ex = mp + 1;
+        }
+        const int leader = __ffs(grp) - 1;
+        mem = __shfl_sync(kFull, mem, leader);
+        ex = __shfl_sync(kFull, ex, leader);
+        // acceptance: the first candidate lane of each node's group; the batch ends at the
+        // acceptance that completes k
+        const bool cand = !pre && (glob || mem);
+        const unsigned gc = grp & __ballot_sync(kFull, cand);
+        const int first = gc ? __ffs(gc) - 1 : 32;
+        const unsigned am = __ballot_sync(kFull, cand && lane == first);
+        const int R = k - nch;
+        unsigned consumed = kFull;
+        if (__popc(am) >= R) {
+            unsigned m = am;
+            for (int q = 1; q < R; ++q) m &= m - 1u;
+            const int L = __ffs(m) - 1;
+            consumed = L == 31 ? kFull : ((1u << (L + 1)) - 1u);
+        }
+        const bool tested = !glob && !pre && lane <= first && ((consumed >> lane) & 1u);
+        events += __popc(consumed);
+        tests += __popc(__ballot_sync(kFull, tested));
+        scanned += warp_sum<long long>(tested ? ex : 0ll);
+        const unsigned took = am & consumed;
+        if ((took >> lane) & 1u) S.arr[nch + __popc(took & below)] = j;
+        __syncwarp();
+        nch += __popc(took);
     }
     if (nch < k) {
         // exact continuation without replacement (memoryless): CDF minus the chosen weight
@@ -458,4 +581,5 @@ __device__ void process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     if (nch != k && lane == 0) atomicOr(&A.st->error, kErrArg);
     if (lane == 0 && scanned) atomicAdd(&A.st->adj_scanned, (unsigned long long)scanned);
     emit_row<KCAP>(A, rp, a, al, n, S.arr, S.out, nch, rows, tests, events);
+    return true;
 }

@@ -159,3 +159,27 @@ def theta_batch(points: int = 64, seed: int = 7) -> np.ndarray:
     rng = np.random.Generator(np.random.PCG64(seed))
     return np.stack([rng.uniform(0.5, 1.5, points), rng.uniform(2, 10, points),
                      rng.uniform(0.5, 2.0, points), rng.uniform(1, 8, points)], axis=1)
+
+
+# ---------------------------------------------------------------- refcompat inputs
+def rc_seed(n: int = 10_000, cites: int = 10, seed: int = 42, years: int = 10) -> SeedGraph:
+    """Seed for ParAGraph's own model: node i cites min(cites, i) earlier nodes, publication years
+    spread over the `years` prior epochs, integer peak fitness drawn from P(v) ~ v^-1.634 over
+    1..1000 (the reference's InitializeFitness, src/abm.cu:124-150)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    src, dst = _distinct_earlier(rng, n, cites)
+    pub = np.sort(rng.integers(-years, 0, size=n)).astype(np.int32)
+    v = np.arange(1, 1001, dtype=np.float64)
+    p = v ** -1.634
+    fit = rng.choice(v, size=n, p=p / p.sum()).astype(np.float32)
+    return SeedGraph(pub, fit, src, dst)
+
+
+def rc_tables(seed: int = 42, bag_mean: float = 15.0, bag_len: int = 1000,
+              ages: int = 40) -> tuple[np.ndarray, np.ndarray]:
+    """An out-degree bag (Poisson-like counts, as a list of observed out-degrees) and recency
+    probabilities by age (geometric decay), the two input files of the reference's abm driver."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    bag = np.clip(rng.poisson(bag_mean, size=bag_len), 0, 300).astype(np.int32)
+    rec = 0.8 ** np.arange(ages, dtype=np.float64)
+    return bag, rec / rec.sum()
