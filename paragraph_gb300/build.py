@@ -52,6 +52,9 @@ def build_library(force: bool = False, verbose_ptxas: bool = False) -> Path:
     headers = list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
     newest = max(p.stat().st_mtime for p in srcs + headers)
     if LIB.exists() and not force and LIB.stat().st_mtime >= newest:
+        drv_src = PKG / "abm" / "abm_main.cpp"
+        if not DRIVER.exists() or DRIVER.stat().st_mtime < max(drv_src.stat().st_mtime, LIB.stat().st_mtime):
+            build_driver()
         return LIB
     objdir = PKG / "_build"
     objdir.mkdir(exist_ok=True)
@@ -69,7 +72,25 @@ def build_library(force: bool = False, verbose_ptxas: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver()
     return LIB
+
+
+DRIVER = LIBDIR / "abm"
+
+
+def build_driver() -> Path:
+    """The `abm` command-line driver (C++17), linked against the library with an $ORIGIN rpath."""
+    src = PKG / "abm" / "abm_main.cpp"
+    cxx = os.environ.get("CXX", "g++")
+    tmp = DRIVER.with_suffix(".tmp")
+    cmd = [cxx, "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(src), "-L", str(LIBDIR),
+           "-lparagraph_gb300", "-Wl,-rpath,$ORIGIN", "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"abm driver build failed:\n{r.stderr}")
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 def build_oracle(force: bool = False) -> Path:
