@@ -10,8 +10,9 @@ out-degree, alpha=1, tau=5, gamma=1, beta=4, 2-hop neighbourhoods of 3 anchors. 
 
 value   = new citations of the K timed steps / their device time (CUDA events on the engine's
           stream, inputs resident in HBM), max over ranks, summed over ranks.
-e2e     = the same metric through the C ABI from host buffers: load the seed (host CSR build +
-          H2D), grow 30 epochs, copy every new citation back (D2H), wall clock.
+e2e     = the same metric through the C ABI from page-locked host buffers: load the seed (raw edge
+          arrays H2D, CSR built on the device), grow 30 epochs, copy every new citation back (D2H),
+          wall clock.
 roofline: the agent kernel (dominant), algorithmic bytes / its summed CUDA-event time.
 cpu_baseline: the CPU oracle (OpenMP, all host threads) on a bounded sample of the same workload.
 --impl reference times that CPU path alone (the reference itself cannot be built here).
@@ -283,23 +284,34 @@ def run_ours(args) -> None:
     # end to end through the C ABI from host buffers
     e2e = None
     if not args.no_e2e:
+        import torch
+
+        # page-locked host buffers, filled before the timed region: the seed's raw arrays in,
+        # every new citation (source, target) out
+        def pinned(a):
+            return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+        hp, hf, hs, hd = pinned(g.pub), pinned(g.fitness), pinned(g.src), pinned(g.dst)
+        cap = int(edges // max(1, args.steps)) + 1
+        out = (torch.empty(cap, dtype=torch.int32).pin_memory().numpy(),
+               torch.empty(cap, dtype=torch.int32).pin_memory().numpy())
         e2e_edges, e2e_secs = 0, 0.0
         h2d = d2h = 0
         for i in range(max(1, args.e2e_steps)):
             with GrowthEngine(seed=seed, device=local) as e2:
                 t0 = time.perf_counter()
-                e2.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=EPOCHS)
+                e2.load_graph(hp, hf, hs, hd, prm, planned_epochs=EPOCHS)
                 n0, m0 = e2.counts()
-                ne = e2.run_epochs(EPOCHS, use_graph=True)
+                ne = e2.run_epochs(EPOCHS, use_graph=False)
                 n1, m1 = e2.counts()
-                src, dst = e2.edges(m0, m1 - m0)
+                src, dst = e2.edges(m0, m1 - m0, out=out)
                 dt = time.perf_counter() - t0
             e2e_edges += ne
             e2e_secs += dt
-            h2d = 4 * n0 * 3 + 8 * (n0 + 1) * 2 + 4 * m0 * 2  # pub, fitness, indeg, both CSRs
-            d2h = 4 * (m1 - m0) + 8 * (n1 + 1)  # new targets + forward offsets for the sources
+            h2d = 4 * g.n * 2 + 4 * g.m * 2  # publication epochs, fitness, raw sources and targets
+            d2h = 8 * (m1 - m0)  # every new citation: source and target
         e2e = {"value": e2e_edges / e2e_secs, "unit": "citations/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h}
+               "d2h_bytes_per_step": d2h, "inputs": "page-locked host buffers; seed CSR built on the device"}
 
     if rank != 0:
         eng.close()

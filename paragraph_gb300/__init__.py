@@ -421,11 +421,20 @@ class GrowthEngine:
         self._check(self._lib.pg_epoch_edges(self._ctx, replica, C.byref(f), C.byref(c)))
         return f.value, c.value
 
-    def edges(self, first: int, count: int, replica: int = 0) -> tuple[np.ndarray, np.ndarray]:
-        s = np.empty(count, np.int32)
-        d = np.empty(count, np.int32)
+    def edges(self, first: int, count: int, replica: int = 0,
+              out: tuple[np.ndarray, np.ndarray] | None = None) -> tuple[np.ndarray, np.ndarray]:
+        """Edges [first, first + count) in forward-CSR order; `out` may hold caller-owned int32
+        buffers of at least `count` entries (e.g. page-locked memory for a faster copy)."""
+        if out is None:
+            s = np.empty(count, np.int32)
+            d = np.empty(count, np.int32)
+        else:
+            s, d = out
+            if (s.dtype != np.int32 or d.dtype != np.int32 or len(s) < count or len(d) < count
+                    or not s.flags.c_contiguous or not d.flags.c_contiguous):
+                raise PGError(PG_ERR_ARG, "out buffers must be contiguous int32 of >= count entries")
         self._check(self._lib.pg_copy_edges(self._ctx, replica, first, count, _ptr(s), _ptr(d)))
-        return s, d
+        return s[:count], d[:count]
 
     def last_epoch_edges(self, replica: int = 0) -> tuple[np.ndarray, np.ndarray]:
         f, c = self.epoch_edges(replica)

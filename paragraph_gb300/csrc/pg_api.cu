@@ -291,6 +291,29 @@ pg_status check_params(pg_ctx* c, const pg_pa_params& p) {
     return PG_OK;
 }
 
+// Index of the first edge with an endpoint outside [0, n), or -1; chunks on all host threads.
+int64_t first_bad_edge(const int32_t* src, const int32_t* dst, int64_t m, int64_t n) {
+    if (m <= 0) return -1;
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::thread::hardware_concurrency(),
+                                                               (m + (1 << 20) - 1) >> 20));
+    std::vector<int64_t> first((size_t)nt, -1);
+    auto work = [&](int t) {
+        const int64_t a = m * t / nt, b = m * (t + 1) / nt;
+        for (int64_t e = a; e < b; ++e)
+            if (src[e] < 0 || src[e] >= n || dst[e] < 0 || dst[e] >= n) {
+                first[(size_t)t] = e;
+                return;
+            }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto& th : pool) th.join();
+    for (int64_t f : first)
+        if (f >= 0) return f;
+    return -1;
+}
+
 // Sorted, duplicate-free CSR from an edge list (Graph::AddEdge set semantics).
 void host_csr(int64_t n, int64_t m, const int32_t* src, const int32_t* dst,
               std::vector<int64_t>& off, std::vector<int32_t>& col) {
@@ -398,7 +421,10 @@ struct HostGraph {
     std::vector<int32_t> lag, dur;  // refcompat fitness windows (empty: lag 0, duration 1000)
 };
 
-pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<HostGraph>& hg) {
+// raw != nullptr: the replicas' CSRs are built on the device from raw[r].src / raw[r].dst (h.m is
+// an upper bound on entry and the unique edge count on return); else hg holds host CSRs.
+pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<HostGraph>& hg,
+                       const pg_replica_desc* raw = nullptr) {
     const int R = (int)reps.size();
     int64_t S = 0, T = 0, M = 0;
     for (int r = 0; r < R; ++r) {
@@ -476,10 +502,25 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     std::vector<int32_t> trep((size_t)T);
     std::vector<Replica> drep((size_t)R);
     std::vector<uint64_t> tabs((size_t)R * kTableEntries);
+    // scratch of the device CSR build: raw edges of one replica and the sort buffers
+    DBuf<char> scratch;
+    DBuf<int32_t> raw_src, raw_dst;
+    DBuf<uint32_t> berr;
+    if (raw) {
+        int64_t mm = 1, nn = 1;
+        for (int r = 0; r < R; ++r) {
+            mm = std::max<int64_t>(mm, raw[r].num_edges);
+            nn = std::max<int64_t>(nn, raw[r].num_nodes);
+        }
+        PG_CUDA(c, dalloc(scratch, (int64_t)build_scratch_bytes(mm, nn)));
+        PG_CUDA(c, dalloc(raw_src, mm));
+        PG_CUDA(c, dalloc(raw_dst, mm));
+        PG_CUDA(c, dalloc(berr, 1));
+        PG_CUDA(c, cudaMemsetAsync(berr.p, 0, 4, c->stream));
+    }
     for (int r = 0; r < R; ++r) {
-        const HostRep& h = reps[r];
+        HostRep& h = reps[r];
         for (int t = 0; t < h.ntiles; ++t) trep[(size_t)h.tbase + t] = r;
-        drep[(size_t)r] = to_device_rep(h);
         if (h.rc)
             std::copy(h.bag_table.begin(), h.bag_table.end(), tabs.begin() + (size_t)r * kTableEntries);
         else
@@ -494,15 +535,44 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             PG_CUDA(c, cudaMemcpyAsync(c->rc_dur.p + h.nbase, D.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
             PG_CUDA(c, cudaStreamSynchronize(c->stream));
         }
-        PG_CUDA(c, cudaMemcpyAsync(c->pub.p + h.nbase, g.pub.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
-        PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase, g.fit.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
-        PG_CUDA(c, cudaMemcpyAsync(c->indeg.p + h.nbase, g.indeg.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
-        PG_CUDA(c, cudaMemcpyAsync(c->fwd_off.p + h.obase, g.fo.data(), 8 * (n + 1), cudaMemcpyHostToDevice, c->stream));
-        PG_CUDA(c, cudaMemcpyAsync(c->bwd_off[0].p + h.obase, g.bo.data(), 8 * (n + 1), cudaMemcpyHostToDevice, c->stream));
-        if (m) {
-            PG_CUDA(c, cudaMemcpyAsync(c->fwd_col.p + h.ebase, g.fc.data(), 4 * m, cudaMemcpyHostToDevice, c->stream));
-            PG_CUDA(c, cudaMemcpyAsync(c->bwd_col[0].p + h.ebase, g.bc.data(), 4 * m, cudaMemcpyHostToDevice, c->stream));
+        if (raw) {
+            const pg_replica_desc& d = raw[r];
+            PG_CUDA(c, cudaMemcpyAsync(c->pub.p + h.nbase, d.pub_epoch, 4 * n, cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase, d.fitness, 4 * n, cudaMemcpyHostToDevice, c->stream));
+            if (d.num_edges > 0) {
+                PG_CUDA(c, cudaMemcpyAsync(raw_src.p, d.src, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream));
+                PG_CUDA(c, cudaMemcpyAsync(raw_dst.p, d.dst, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream));
+            }
+            int64_t u = 0;
+            cudaGetLastError();
+            launch_build_csr(raw_src.p, raw_dst.p, d.num_edges, (int64_t)n, scratch.p, c->fwd_off.p + h.obase,
+                             c->fwd_col.p + h.ebase, c->bwd_off[0].p + h.obase, c->bwd_col[0].p + h.ebase,
+                             c->indeg.p + h.nbase, &u, berr.p, c->stream);
+            PG_CUDA(c, cudaGetLastError());
+            PG_CUDA(c, cudaStreamSynchronize(c->stream));
+            uint32_t be = 0;
+            PG_CUDA(c, cudaMemcpy(&be, berr.p, 4, cudaMemcpyDeviceToHost));
+            if (be) return fail(c, PG_ERR_ARG, "edge endpoint out of range in replica " + std::to_string(r));
+            h.m = u;
+        } else {
+            PG_CUDA(c, cudaMemcpyAsync(c->pub.p + h.nbase, g.pub.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase, g.fit.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(c->indeg.p + h.nbase, g.indeg.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(c->fwd_off.p + h.obase, g.fo.data(), 8 * (n + 1), cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(c->bwd_off[0].p + h.obase, g.bo.data(), 8 * (n + 1), cudaMemcpyHostToDevice, c->stream));
+            if (m) {
+                PG_CUDA(c, cudaMemcpyAsync(c->fwd_col.p + h.ebase, g.fc.data(), 4 * m, cudaMemcpyHostToDevice, c->stream));
+                PG_CUDA(c, cudaMemcpyAsync(c->bwd_col[0].p + h.ebase, g.bc.data(), 4 * m, cudaMemcpyHostToDevice, c->stream));
+            }
         }
+        drep[(size_t)r] = to_device_rep(h);
+    }
+    if (raw) {
+        PG_CUDA(c, cudaStreamSynchronize(c->stream));
+        dfree(scratch);
+        dfree(raw_src);
+        dfree(raw_dst);
+        dfree(berr);
     }
     PG_CUDA(c, cudaMemcpyAsync(c->tile_rep.p, trep.data(), 4 * (size_t)T, cudaMemcpyHostToDevice, c->stream));
     PG_CUDA(c, cudaMemcpyAsync(c->rep.p, drep.data(), sizeof(Replica) * (size_t)R, cudaMemcpyHostToDevice, c->stream));
@@ -895,39 +965,19 @@ pg_status pg_load_replicas(pg_ctx* c, const pg_replica_desc* descs, int32_t num)
         if (d.num_nodes <= 0 || d.num_nodes > (int64_t)INT32_MAX / 2) return fail(c, PG_ERR_ARG, "num_nodes out of range");
         if (d.num_edges < 0 || (d.num_edges > 0 && (!d.src || !d.dst))) return fail(c, PG_ERR_ARG, "bad edge arrays");
         if (!d.pub_epoch || !d.fitness) return fail(c, PG_ERR_ARG, "pub_epoch and fitness are required");
-        for (int64_t e = 0; e < d.num_edges; ++e)
-            if (d.src[e] < 0 || d.src[e] >= d.num_nodes || d.dst[e] < 0 || d.dst[e] >= d.num_nodes)
-                return fail(c, PG_ERR_ARG, "edge endpoint out of range at index " + std::to_string(e));
+        // endpoints checked on all host threads before the arena is touched, so a bad edge list
+        // leaves the loaded graph intact
+        const int64_t bad = first_bad_edge(d.src, d.dst, d.num_edges, d.num_nodes);
+        if (bad >= 0) return fail(c, PG_ERR_ARG, "edge endpoint out of range at index " + std::to_string(bad));
     }
-    // host CSRs of the replicas, built on all host threads (replicas are independent)
-    {
-        std::atomic<int> next{0};
-        auto worker = [&]() {
-            for (int r = next++; r < num; r = next++) {
-                const pg_replica_desc& d = descs[r];
-                HostGraph& g = hg[(size_t)r];
-                host_csr(d.num_nodes, d.num_edges, d.src, d.dst, g.fo, g.fc);
-                host_transpose(d.num_nodes, g.fo, g.fc, g.bo, g.bc);
-                g.pub.assign(d.pub_epoch, d.pub_epoch + d.num_nodes);
-                g.fit.assign(d.fitness, d.fitness + d.num_nodes);
-                g.indeg.resize((size_t)d.num_nodes);
-                for (int64_t v = 0; v < d.num_nodes; ++v)
-                    g.indeg[(size_t)v] = (int32_t)(g.bo[(size_t)v + 1] - g.bo[(size_t)v]);
-            }
-        };
-        const int nt = std::max(1, std::min<int>(num, (int)std::thread::hardware_concurrency()));
-        std::vector<std::thread> pool;
-        for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
-        worker();
-        for (auto& th : pool) th.join();
-    }
+    // the CSRs are built on the device from the raw edges (upload_arena); the plan below uses the
+    // raw edge count, an upper bound on the unique edges
     for (int r = 0; r < num; ++r) {
         const pg_replica_desc& d = descs[r];
-        const HostGraph& g = hg[(size_t)r];
         HostRep& h = reps[(size_t)r];
         h.prm = d.params;
         h.n = d.num_nodes;
-        h.m = g.fo[(size_t)d.num_nodes];
+        h.m = d.num_edges;
         // capacity plan
         int64_t n = h.n, m = h.m;
         const int epochs = std::max(1, std::min(d.planned_epochs, max_plan));
@@ -950,7 +1000,7 @@ pg_status pg_load_replicas(pg_ctx* c, const pg_replica_desc* descs, int32_t num)
         max_agents = std::max(max_agents, plan_agents[e]);
         max_edges = std::max(max_edges, plan_edges[e]);
     }
-    pg_status s = upload_arena(c, reps, hg);
+    pg_status s = upload_arena(c, reps, hg, descs);
     if (s != PG_OK) return s;
     c->epoch = 0;
     return alloc_epoch_buffers(c, max_agents, max_edges, 0);

@@ -1,0 +1,220 @@
+// pg_build.cu -- device construction of a replica's forward and backward CSR from a raw edge list.
+//
+// Replaces the reference's seed load (Graph::ParseEdgelist / AddEdge into std::map<int,
+// std::set<int>>, src/graph.cu:376-447,820-826, then prepareGraph's int32 CSR, src/utils.cu:75-142)
+// with a device pipeline, so a load costs one upload of the raw (source, target) arrays:
+//   k_edge_keys     key = source << b | target (b = bits of n - 1), ids checked against [0, n)
+//   radix passes    stable LSD radix sort of the keys, 8-bit digits over the 2b key bits
+//                   (per pass: tile histograms, one scan over [digit][tile], stable scatter)
+//   k_unique_*      duplicates collapse (Graph::AddEdge set semantics), forward columns and
+//                   per-source counts; counts -> int64 offsets by the engine's scan
+//   radix passes    the unique keys stably re-sorted on the target field only, which orders them
+//                   by (target, source): backward columns and in-degrees.
+// Rows come out ascending, as the reference's std::set rows.  Every step is integer work, so the
+// result equals the host construction bit for bit.
+#include <algorithm>
+
+#include "pg_engine.cuh"
+
+namespace pg {
+
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kSortThreads = 256;
+constexpr int kSortTile = kSortThreads * 16;  // keys per CTA
+
+__global__ void __launch_bounds__(256) k_edge_keys(const int32_t* src, const int32_t* dst, int64_t m,
+                                                   int64_t n, int bits, unsigned long long* keys,
+                                                   uint32_t* err) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t s = src[i], d = dst[i];
+        if (s < 0 || s >= n || d < 0 || d >= n) {
+            atomicOr(err, kErrArg);
+            keys[i] = 0ull;
+            continue;
+        }
+        keys[i] = ((unsigned long long)s << bits) | (unsigned long long)d;
+    }
+}
+
+// Digit histogram of each tile, written digit-major: hist[d * tiles + t].
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long long* keys, int64_t m, int shift,
+                                                             int dmask, int64_t tiles, int64_t* hist) {
+    __shared__ int h[kRadix];
+    for (int i = threadIdx.x; i < kRadix; i += kSortThreads) h[i] = 0;
+    __syncthreads();
+    const int64_t t = blockIdx.x;
+    const int64_t base = t * kSortTile;
+    for (int i = threadIdx.x; i < kSortTile; i += kSortThreads) {
+        const int64_t k = base + i;
+        if (k < m) atomicAdd(&h[(int)((keys[k] >> shift) & dmask)], 1);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadix; d += kSortThreads) hist[(int64_t)d * tiles + t] = h[d];
+}
+
+// Stable scatter: key k of tile t with digit d goes to off[d * tiles + t] + (number of earlier keys
+// of the tile with digit d).  The tile is walked in chunks of 256 keys in order; inside a chunk a key
+// is ranked among its warp's equal digits (match), warps are ordered by a per-chunk table.
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned long long* keys, int64_t m,
+                                                                int shift, int dmask, int64_t tiles,
+                                                                const int64_t* off, unsigned long long* out) {
+    constexpr int W = kSortThreads / 32;
+    __shared__ int64_t run[kRadix];        // keys of each digit placed by earlier chunks
+    __shared__ int wcnt[W][kRadix];        // this chunk: keys of each digit per warp
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t t = blockIdx.x;
+    for (int d = threadIdx.x; d < kRadix; d += kSortThreads) run[d] = off[(int64_t)d * tiles + t];
+    const int64_t base = t * kSortTile;
+    for (int c = 0; c < kSortTile; c += kSortThreads) {
+        for (int i = threadIdx.x; i < W * kRadix; i += kSortThreads) (&wcnt[0][0])[i] = 0;
+        __syncthreads();
+        const int64_t k = base + c + threadIdx.x;
+        const bool valid = k < m;
+        const unsigned long long key = valid ? keys[k] : 0ull;
+        const int d = valid ? (int)((key >> shift) & dmask) : kRadix;  // kRadix: no digit
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            int before = 0;
+            for (int w = 0; w < warp; ++w) before += wcnt[w][d];
+            out[run[d] + before + rank] = key;
+        }
+        __syncthreads();
+        for (int dd = threadIdx.x; dd < kRadix; dd += kSortThreads) {
+            int s = 0;
+            for (int w = 0; w < W; ++w) s += wcnt[w][dd];
+            run[dd] += s;
+        }
+        __syncthreads();
+    }
+}
+
+// flag[i] = 1 when key i differs from key i-1 (the first of a run of duplicates)
+__global__ void __launch_bounds__(256) k_unique_flags(const unsigned long long* keys, int64_t m, int32_t* flag) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+// Compact the unique keys (sorted by source, then target) and count the edges of every source.
+__global__ void __launch_bounds__(256) k_unique_compact(const unsigned long long* keys, int64_t m, const int32_t* flag,
+                                                        const int64_t* pos, int bits, unsigned long long* ukeys,
+                                                        int32_t* fcol, int32_t* fcnt) {
+    const unsigned long long mask = (1ull << bits) - 1ull;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!flag[i]) continue;
+        const unsigned long long k = keys[i];
+        const int64_t p = pos[i];
+        ukeys[p] = k;
+        fcol[p] = (int32_t)(k & mask);
+        atomicAdd(&fcnt[(int64_t)(k >> bits)], 1);
+    }
+}
+
+// Keys sorted by (target, source): backward columns (sources) and per-target counts.
+__global__ void __launch_bounds__(256) k_backward_cols(const unsigned long long* keys, int64_t u, int bits,
+                                                       int32_t* bcol, int32_t* bcnt) {
+    const unsigned long long mask = (1ull << bits) - 1ull;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < u; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long k = keys[i];
+        bcol[i] = (int32_t)(k >> bits);
+        atomicAdd(&bcnt[(int64_t)(k & mask)], 1);
+    }
+}
+
+int64_t build_radix_tiles(int64_t m) { return (m + kSortTile - 1) / kSortTile; }
+int64_t build_scan_entries(int64_t m) { return build_radix_tiles(m) * kRadix; }
+
+// One stable pass on the `width` (<= 8) key bits from `shift`; `hist`/`off` hold kRadix * tiles
+// (+1) entries.
+static void radix_pass(const unsigned long long* in, unsigned long long* out, int64_t m, int shift, int width,
+                       int64_t* hist, int64_t* off, int64_t* blocksum, cudaStream_t s) {
+    const int64_t tiles = build_radix_tiles(m);
+    const int dmask = (1 << width) - 1;
+    k_radix_hist<<<(unsigned)tiles, kSortThreads, 0, s>>>(in, m, shift, dmask, tiles, hist);
+    launch_scan_i64(hist, off, tiles * kRadix, blocksum, s);
+    k_radix_scatter<<<(unsigned)tiles, kSortThreads, 0, s>>>(in, m, shift, dmask, tiles, off, out);
+}
+
+// Sorts keys[0..m) stably on bits [lo, hi) (8-bit digits from lo); tmp is a second buffer of m keys.
+// Returns the buffer holding the result (keys or tmp).
+static unsigned long long* radix_sort(unsigned long long* keys, unsigned long long* tmp, int64_t m, int lo, int hi,
+                                      int64_t* hist, int64_t* off, int64_t* blocksum, cudaStream_t s) {
+    unsigned long long* a = keys;
+    unsigned long long* b = tmp;
+    for (int sh = lo; sh < hi; sh += kRadixBits) {
+        // the last digit stops at bit hi: the bits above it belong to another field of the key
+        radix_pass(a, b, m, sh, hi - sh < kRadixBits ? hi - sh : kRadixBits, hist, off, blocksum, s);
+        unsigned long long* t = a;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+// The scratch the build needs for m raw edges (bytes), for the caller's allocation.
+size_t build_scratch_bytes(int64_t m, int64_t n) {
+    const int64_t e = m > 0 ? m : 1;
+    const int64_t scan = build_scan_entries(e) + 1;
+    return (size_t)(3 * e) * 8 + (size_t)e * 4 + (size_t)(e + 1) * 8 + (size_t)(2 * scan) * 8 +
+           (size_t)(n + 1) * 4 * 2 + (size_t)(scan_blocks_needed(std::max<int64_t>(std::max<int64_t>(scan, e + 1), n + 1)) + 2) * 8 +
+           16 * 256;
+}
+
+// Builds replica CSRs on the device.  src/dst: m raw device edges; outputs: fo/fc/bo/bc (the
+// replica's regions), indeg (n entries).  Returns the number of unique edges through *u_out (read
+// back by the caller after a sync).  Scratch layout is carved from `scratch`.
+void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,
+                      int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_out,
+                      uint32_t* err, cudaStream_t s) {
+    const int64_t e = m > 0 ? m : 1;
+    const int64_t scan = build_scan_entries(e) + 1;
+    char* p = reinterpret_cast<char*>(scratch);
+    auto take = [&](size_t bytes) {
+        char* q = p;
+        p += (bytes + 255) & ~(size_t)255;
+        return q;
+    };
+    unsigned long long* k0 = reinterpret_cast<unsigned long long*>(take((size_t)e * 8));
+    unsigned long long* k1 = reinterpret_cast<unsigned long long*>(take((size_t)e * 8));
+    unsigned long long* uk = reinterpret_cast<unsigned long long*>(take((size_t)e * 8));
+    int32_t* flag = reinterpret_cast<int32_t*>(take((size_t)e * 4));
+    int64_t* pos = reinterpret_cast<int64_t*>(take((size_t)(e + 1) * 8));
+    int64_t* hist = reinterpret_cast<int64_t*>(take((size_t)scan * 8));
+    int64_t* off = reinterpret_cast<int64_t*>(take((size_t)scan * 8));
+    int32_t* fcnt = reinterpret_cast<int32_t*>(take((size_t)(n + 1) * 4));
+    int32_t* bcnt = reinterpret_cast<int32_t*>(take((size_t)(n + 1) * 4));
+    int64_t* blocksum = reinterpret_cast<int64_t*>(
+        take((size_t)(scan_blocks_needed(std::max<int64_t>(std::max<int64_t>(scan, e + 1), n + 1)) + 2) * 8));
+    int bits = 1;
+    while (bits < 31 && ((int64_t)1 << bits) < n) ++bits;
+    cudaMemsetAsync(fcnt, 0, (size_t)(n + 1) * 4, s);
+    cudaMemsetAsync(bcnt, 0, (size_t)(n + 1) * 4, s);
+    const unsigned grid = (unsigned)std::min<int64_t>((e + 255) / 256, 152 * 16);
+    int64_t u = 0;
+    if (m > 0) {
+        k_edge_keys<<<grid, 256, 0, s>>>(src, dst, m, n, bits, k0, err);
+        unsigned long long* sorted = radix_sort(k0, k1, m, 0, 2 * bits, hist, off, blocksum, s);
+        k_unique_flags<<<grid, 256, 0, s>>>(sorted, m, flag);
+        launch_scan_i32_to_i64(flag, pos, m, blocksum, s);
+        k_unique_compact<<<grid, 256, 0, s>>>(sorted, m, flag, pos, bits, uk, fc, fcnt);
+        // number of unique edges
+        cudaMemcpyAsync(u_out, pos + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        u = *u_out;
+        if (u > 0) {
+            unsigned long long* other = sorted == k0 ? k1 : k0;
+            unsigned long long* bsorted = radix_sort(uk, other, u, 0, bits, hist, off, blocksum, s);
+            k_backward_cols<<<grid, 256, 0, s>>>(bsorted, u, bits, bc, bcnt);
+        }
+    } else {
+        *u_out = 0;
+    }
+    launch_scan_i32_to_i64(fcnt, fo, n, blocksum, s);
+    launch_scan_i32_to_i64(bcnt, bo, n, blocksum, s);
+    cudaMemcpyAsync(indeg, bcnt, (size_t)n * 4, cudaMemcpyDeviceToDevice, s);
+}
+
+}  // namespace pg

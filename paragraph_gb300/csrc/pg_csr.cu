@@ -110,9 +110,15 @@ __device__ __forceinline__ int64_t row_of(const int64_t* off, int64_t lo, int64_
 
 // Old backward entries moved to their new positions, in tiles of kCopyTile consecutive positions
 // (not rows), so a hub row with millions of entries is spread over many CTAs.  Reads and writes are
-// coalesced; each position finds its row by a binary search inside the tile's row range.
+// coalesced.  The tile's row offsets and per-row shifts (new - old start) are staged in shared
+// memory once, so each position finds its row by a shared-memory binary search; a tile spanning
+// more than kCopyRows rows (long runs of empty rows) searches the global offsets instead.
+constexpr int kCopyRows = 2048;
+
 __global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
     __shared__ int64_t s_rows[2];
+    __shared__ int64_t s_oc[kCopyRows + 1];  // old offsets of the tile's rows, and the next one
+    __shared__ int64_t s_sh[kCopyRows];      // new minus old offset of the tile's rows
     if (A.st->error) return;
     const int64_t total = (int64_t)A.st->copy_tiles;
     unsigned long long moved = 0;
@@ -139,9 +145,32 @@ __global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
         }
         __syncthreads();
         const int64_t r0 = s_rows[0], r1 = s_rows[1];
-        for (int64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-            const int64_t v = row_of(oc, r0, r1, p);
-            cn[on[v] + (p - oc[v])] = cc[p];
+        const int64_t nr = r1 - r0 + 1;
+        if (nr <= kCopyRows) {
+            for (int64_t i = threadIdx.x; i < nr; i += blockDim.x) {
+                const int64_t o = oc[r0 + i];
+                s_oc[i] = o;
+                s_sh[i] = on[r0 + i] - o;
+            }
+            if (threadIdx.x == 0) s_oc[nr] = oc[r1 + 1];
+            __syncthreads();
+            const int last = (int)nr - 1;
+            for (int64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+                int l = 0, h = last;
+                while (l < h) {
+                    const int mid = (l + h + 1) >> 1;
+                    if (s_oc[mid] <= p)
+                        l = mid;
+                    else
+                        h = mid - 1;
+                }
+                cn[p + s_sh[l]] = cc[p];
+            }
+        } else {
+            for (int64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+                const int64_t v = row_of(oc, r0, r1, p);
+                cn[on[v] + (p - oc[v])] = cc[p];
+            }
         }
         __syncthreads();
     }

@@ -290,6 +290,11 @@ void launch_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_t*
                             cudaStream_t s);
 int scan_blocks_needed(int64_t n);
 cudaError_t init_agent_kernels();
+// device CSR construction from a raw edge list (pg_build.cu)
+size_t build_scratch_bytes(int64_t m, int64_t n);
+void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,
+                      int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_out,
+                      uint32_t* err, cudaStream_t s);
 // resident CTAs per SM of the k <= 64 agent kernel (after init_agent_kernels)
 int agent_occupancy(int thin, int small_hash);
 cudaError_t init_csr_kernels();

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from paragraph_gb300 import (PG_SAMPLER_ENUMERATE, PG_SAMPLER_THINNING, GrowthEngine,
+from paragraph_gb300 import (PG_SAMPLER_ENUMERATE, PG_SAMPLER_THINNING, GrowthEngine, PGError,
                              PAParams, ReplicaInput)
 from paragraph_gb300 import workloads as W
 
@@ -206,3 +206,43 @@ def test_single_replica_context_reproduces_batched_replica(gpu):
                 for w in (0, 1):
                     for x, y in zip(batched.csr(w, i), one.csr(w, 0)):
                         np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.parametrize("n", [1500, 50_000, 300_001])
+def test_device_seed_load_matches_host_construction(gpu, n):
+    """The seed CSRs are built on the device (radix sort, duplicate removal, transpose); they equal
+    the oracle's host construction, including duplicate edges, self-loops and isolated nodes, node
+    counts whose id width is not a multiple of the 8-bit digit, and graphs larger than one sort
+    tile per pass."""
+    rng = np.random.default_rng(5)
+    src = rng.integers(0, n, 6 * n).astype(np.int32)
+    dst = rng.integers(0, n, 6 * n).astype(np.int32)
+    src = np.concatenate([src, src[:1000], np.arange(10, dtype=np.int32)])   # duplicates, self-loops
+    dst = np.concatenate([dst, dst[:1000], np.arange(10, dtype=np.int32)])
+    pub = rng.integers(-5, 0, n).astype(np.int32)
+    fit = rng.lognormal(0, 1, n).astype(np.float32)
+    with GrowthEngine(seed=1) as eng:
+        eng.load_graph(pub, fit, src, dst, PAParams(fixed_new_nodes=100), planned_epochs=1)
+        og = O.OracleGraph(1, 0)
+        og.load(pub, fit, src, dst)
+        _compare_state(eng, og)
+        tiny = GrowthEngine(seed=1)
+        tiny.load_graph(pub[:3], fit[:3], np.zeros(0, np.int32), np.zeros(0, np.int32),
+                        PAParams(fixed_new_nodes=2), planned_epochs=1)
+        assert tiny.counts() == (3, 0)
+        tiny.close()
+        with pytest.raises(PGError):
+            eng.load_graph(pub, fit, np.array([0, n], np.int32), np.array([1, 2], np.int32))
+
+
+def test_edges_into_caller_buffers(gpu):
+    g = W.plain_pa_seed(2000, 5, seed=2)
+    with GrowthEngine(seed=3) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, PAParams(fixed_new_nodes=300), planned_epochs=1)
+        eng.grow_epoch()
+        f, c = eng.epoch_edges()
+        a = eng.edges(f, c)
+        buf = (np.empty(c + 7, np.int32), np.empty(c + 7, np.int32))
+        b = eng.edges(f, c, out=buf)
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[1], b[1])
