@@ -619,6 +619,97 @@ def loglik_cpu_sample(trace, pts, ll_gpu, gr_gpu, budget_points: int = 2) -> dic
             "loglik_rel_err_vs_fp64": rel_ll, "grad_rel_err_vs_fp64": rel_g}
 
 
+def run_small_configs(args) -> None:
+    """The two small configurations as separate lines (not the headline): plain PA growth (10k
+    seed, 3 epochs of 5,000, Poisson(15), 3 anchors) and ER G(n,p) growth (100k seed without edges,
+    10 epochs of 10,000 at p in {1e-5, 1e-4, 1e-3}).  Each step regrows all epochs from the
+    device-resident seed; the CPU oracle times the same work on all host threads."""
+    import oracle as O
+    from paragraph_gb300 import GrowthEngine, PAParams
+    from paragraph_gb300 import workloads as W
+
+    peak, peak_kind = peaks()
+    threads = os.cpu_count() or 1
+    # plain PA
+    g = W.plain_pa_seed(10_000, 10, seed=args.seed)
+    prm = W.plain_pa_params()
+    with GrowthEngine(seed=args.seed) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=3)
+        eng.checkpoint()
+        for _ in range(args.warmup):
+            eng.restore()
+            eng.run_epochs(3, use_graph=True)
+        eng.sync()
+        edges = 0
+        eng.timer_start()
+        for _ in range(args.steps):
+            eng.restore()
+            edges += eng.run_epochs(3, use_graph=True)
+        ms = eng.timer_stop()
+        st = eng.stats()
+    og = O.OracleGraph(args.seed, 0)
+    og.load(g.pub, g.fitness, g.src, g.dst)
+    og.set_params(**prm.__dict__)
+    og.set_sampler(1)
+    t0 = time.perf_counter()
+    cpu_edges = 0
+    for _ in range(3):
+        m0 = og.m
+        og.pa_epoch(threads)
+        cpu_edges += og.m - m0
+    cpu_s = time.perf_counter() - t0
+    og.close()
+    gbs = st["run_bytes_alg"] / (ms / args.steps / 1000.0) / 1e9 if ms > 0 else 0.0
+    print(json.dumps({
+        "metric": "citation edges/sec (plain PA growth)", "value": edges / (ms / 1000.0),
+        "unit": "citations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "dtype": "int32/u64/f32",
+        "data": "synthetic", "config": {"workload": "plain_pa_10k_seed_3x5000", "seed_nodes": 10_000,
+                                        "epochs": 3, "agents_per_epoch": 5000, "mean_out_degree": 15},
+        "epoch_bytes_roofline": {"achieved": gbs, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                                 "frac": gbs / peak if peak else None,
+                                 "note": "whole-epoch algorithmic bytes / epoch time; launch-bound at this size"},
+        "cpu_baseline": {"value": cpu_edges / cpu_s, "unit": "citations/s", "cores": threads, "kind": "port",
+                         "sample": "the 3 epochs, CPU oracle, neighbourhood enumeration"}}), flush=True)
+    # ER
+    g = W.er_seed(100_000)
+    for p in (1e-5, 1e-4, 1e-3):
+        with GrowthEngine(seed=args.seed) as eng:
+            def er_step(timed: bool):
+                # reload the seed (untimed), then the 10 epochs between device events
+                eng.load_graph(g.pub, g.fitness, g.src, g.dst, PAParams(fixed_new_nodes=10_000),
+                               planned_epochs=1)
+                eng.sync()
+                eng.timer_start()
+                e = sum(eng.er_epoch(10_000, p) for _ in range(10))
+                return e, eng.timer_stop()
+
+            for _ in range(args.warmup):
+                er_step(False)
+            edges, ms = 0, 0.0
+            for _ in range(args.steps):
+                e, t = er_step(True)
+                edges += e
+                ms += t
+        og = O.OracleGraph(args.seed, 0)
+        og.load(g.pub, g.fitness, g.src, g.dst)
+        t0 = time.perf_counter()
+        m0 = og.m
+        for _ in range(10):
+            og.er_epoch(10_000, p, threads)
+        cpu_s = time.perf_counter() - t0
+        cpu_edges = og.m - m0
+        og.close()
+        print(json.dumps({
+            "metric": "citation edges/sec (ER G(n,p) growth)", "value": edges / (ms / 1000.0),
+            "unit": "citations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "dtype": "int32/f64 skips",
+            "data": "synthetic", "config": {"workload": "er_100k_seed_10x10000", "p": p},
+            "timing": "host-synchronised epochs (pg_er_epoch), device events around the step",
+            "cpu_baseline": {"value": cpu_edges / cpu_s, "unit": "citations/s", "cores": threads,
+                             "kind": "port", "sample": "the 10 epochs, CPU oracle"}}), flush=True)
+
+
 def epoch_report(args) -> None:
     """One JSON line per epoch of the workload: stage times (CUDA events) and byte-model counters.
     Stops early when an epoch exceeds --epoch-cap-s (the enumeration sampler slows down as hubs
@@ -644,8 +735,11 @@ def epoch_report(args) -> None:
 
 
 def profile_case(args) -> None:
-    """Small bounded case for ncu: load the workload's seed and run two PA epochs."""
-    from paragraph_gb300 import GrowthEngine
+    """Small bounded case for ncu: load the workload's seed and run two PA epochs; with
+    --profile-stages also one ER epoch (100k seed, 10,000 new nodes, p = 1e-3) and one refcompat
+    epoch (200k seed), so every stage kernel launches at least once."""
+    from paragraph_gb300 import PG_WEIGHTS_REFCOMPAT, GrowthEngine, PAParams, RCParams
+    from paragraph_gb300 import workloads as W
 
     g, prm = seed_graph(args.seed)
     with GrowthEngine(seed=args.seed, sampler=args.sampler) as eng:
@@ -655,7 +749,26 @@ def profile_case(args) -> None:
             s = eng.stats()
             print(json.dumps({"epoch": e, "bytes_alg_agents": s["bytes_alg_agents"],
                               "bytes_alg": s["bytes_alg"], "ms_agents": s["ms_agents"],
-                              "new_edges": s["new_edges"]}), flush=True)
+                              "ms_csr": s["ms_csr"], "ms_weights": s["ms_weights"],
+                              "new_edges": s["new_edges"], "bwd_moved": s["bwd_moved"],
+                              "nodes": s["nodes_weighted"]}), flush=True)
+    if not args.profile_stages:
+        return
+    ge = W.er_seed(100_000)
+    with GrowthEngine(seed=args.seed) as eng:
+        eng.load_graph(ge.pub, ge.fitness, ge.src, ge.dst, PAParams(fixed_new_nodes=10_000), planned_epochs=1)
+        ne = eng.er_epoch(10_000, 1e-3)
+        s = eng.stats()
+        print(json.dumps({"er_edges": ne, "ms_er": s["ms_er"], "bytes_alg": s["bytes_alg"]}), flush=True)
+    gr = W.rc_seed(200_000, 10, seed=args.seed)
+    bag, rec = W.rc_tables(seed=args.seed)
+    with GrowthEngine(seed=args.seed, weight_model=PG_WEIGHTS_REFCOMPAT) as eng:
+        eng.load_graph(gr.pub, gr.fitness, gr.src, gr.dst, PAParams(growth_rate=0.03), planned_epochs=1)
+        eng.rc_configure(RCParams(growth_rate=0.03, same_year=0.1), bag, rec)
+        nn, ne = eng.grow_epoch()
+        s = eng.stats()
+        print(json.dumps({"rc_new_nodes": nn, "rc_edges": ne, "ms_agents": s["ms_agents"],
+                          "ms_weights": s["ms_weights"], "elems": s["elems_streamed"]}), flush=True)
 
 
 def main():
@@ -673,13 +786,21 @@ def main():
     ap.add_argument("--report-epochs", type=int, default=EPOCHS)
     ap.add_argument("--epoch-cap-s", type=float, default=10.0)
     ap.add_argument("--profile-case", action="store_true", help="two epochs for ncu, then exit")
+    ap.add_argument("--profile-stages", action="store_true",
+                    help="with --profile-case: also one ER and one refcompat epoch")
     ap.add_argument("--ensemble", action="store_true",
                     help="batched ensemble (256 replicas x 10 epochs) against the serial loop")
     ap.add_argument("--loglik", action="store_true",
                     help="log-likelihood + adjoint at 64 points against the per-point loop")
     ap.add_argument("--lik-seed-nodes", type=int, default=200_000,
                     help="seed size of the calibration trace (smaller cases for profiling)")
+    ap.add_argument("--small-configs", action="store_true",
+                    help="plain PA (10k seed) and ER G(n,p) lines with their CPU baselines")
     args = ap.parse_args()
+    if args.small_configs:
+        if args.warmup < 3:
+            args.warmup = 3
+        return run_small_configs(args)
     if args.ensemble or args.loglik:
         if args.warmup < 3:
             args.warmup = 3

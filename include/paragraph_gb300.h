@@ -232,6 +232,13 @@ pg_status pg_copy_arrivals(pg_ctx* ctx, int32_t replica, int32_t* cited);
  * (The reference draws one generator node per paper, getGeneratorNode, src/abm.cu:567-574.) */
 pg_status pg_copy_anchors(pg_ctx* ctx, int32_t replica, int32_t* anchors);
 
+/* The replica's edge list as text, one "source,target\n" line per edge in forward-CSR order (the
+ * rows of Graph::WriteGraph, src/graph.cu:909-1003, without its "#source,target" header), node v
+ * printed as ids[v] (n_ids = the replica's node count); formatted on the device.  out == NULL only
+ * reports the size in *bytes; a buffer smaller than the text gives PG_ERR_CAPACITY. */
+pg_status pg_format_edges(pg_ctx* ctx, int32_t replica, const int64_t* ids, int64_t n_ids, char* out,
+                          int64_t cap, int64_t* bytes);
+
 /* ---- measurement ---- */
 /* enable != 0 records CUDA events around every kernel group of each epoch (default on). */
 pg_status pg_set_timing(pg_ctx* ctx, int32_t enable);

@@ -40,7 +40,7 @@ EXPORTED = [
     "pg_timer_start", "pg_timer_stop", "pg_checkpoint", "pg_restore", "pg_er_generate_noalloc",
     "pg_set_tuning", "pg_get_tuning", "pg_autotune", "pg_copy_anchors", "pg_trace_load",
     "pg_loglik_fwd", "pg_loglik_bwd", "pg_rc_configure", "pg_rc_set_nodes", "pg_rc_copy_agents",
-    "pg_rc_bag_table", "pg_rc_fitness_table",
+    "pg_rc_bag_table", "pg_rc_fitness_table", "pg_format_edges",
 ]
 
 
@@ -246,6 +246,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_rc_copy_agents": (i32, [vp, i32, vp]),
         "pg_rc_bag_table": (i32, [vp, i64, vp]),
         "pg_rc_fitness_table": (i32, [vp]),
+        "pg_format_edges": (i32, [vp, i32, vp, i64, vp, i64, P(i64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -435,6 +436,18 @@ class GrowthEngine:
                 raise PGError(PG_ERR_ARG, "out buffers must be contiguous int32 of >= count entries")
         self._check(self._lib.pg_copy_edges(self._ctx, replica, first, count, _ptr(s), _ptr(d)))
         return s[:count], d[:count]
+
+    def format_edges(self, ids, replica: int = 0) -> bytes:
+        """The edge list as "source,target\\n" text with node v printed as ids[v], formatted on the
+        device (the rows of the reference's WriteGraph)."""
+        ids = np.ascontiguousarray(ids, np.int64)
+        size = C.c_int64()
+        self._check(self._lib.pg_format_edges(self._ctx, replica, _ptr(ids), len(ids), None, 0,
+                                              C.byref(size)))
+        buf = C.create_string_buffer(max(size.value, 1))
+        self._check(self._lib.pg_format_edges(self._ctx, replica, _ptr(ids), len(ids), buf,
+                                              size.value, C.byref(size)))
+        return buf.raw[:size.value]
 
     def last_epoch_edges(self, replica: int = 0) -> tuple[np.ndarray, np.ndarray]:
         f, c = self.epoch_edges(replica)

@@ -488,23 +488,15 @@ int run(int argc, char** argv) {
     PG_TRY(ctx, pg_copy_degrees(ctx, 0, indeg.data(), outdeg.data()));
     PG_TRY(ctx, pg_copy_nodes(ctx, 0, pubs.data(), fits.data()));
     {
+        // the edge rows are formatted on the device (pg_format_edges) and written in one block
         FILE* f = std::fopen(o.str("--output-file").c_str(), "wb");
         if (!f) return die(log, "cannot write " + o.str("--output-file"));
         std::fputs("#source,target\n", f);
-        std::string buf;
-        buf.reserve(1 << 20);
-        char tmp[48];
-        for (int64_t u = 0; u < n; ++u)
-            for (int64_t p = off[(size_t)u]; p < off[(size_t)u + 1]; ++p) {
-                const int len = std::snprintf(tmp, sizeof(tmp), "%lld,%lld\n", (long long)orig[(size_t)u],
-                                              (long long)orig[(size_t)col[(size_t)p]]);
-                buf.append(tmp, (size_t)len);
-                if (buf.size() > (1u << 20)) {
-                    std::fwrite(buf.data(), 1, buf.size(), f);
-                    buf.clear();
-                }
-            }
-        std::fwrite(buf.data(), 1, buf.size(), f);
+        int64_t bytes = 0;
+        PG_TRY(ctx, pg_format_edges(ctx, 0, orig.data(), n, nullptr, 0, &bytes));
+        std::vector<char> txt((size_t)std::max<int64_t>(bytes, 1));
+        PG_TRY(ctx, pg_format_edges(ctx, 0, orig.data(), n, txt.data(), bytes, &bytes));
+        std::fwrite(txt.data(), 1, (size_t)bytes, f);
         std::fclose(f);
     }
     {

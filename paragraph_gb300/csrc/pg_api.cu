@@ -93,7 +93,7 @@ struct pg_ctx {
     // device buffers
     DBuf<Replica> rep;
     DBuf<EpochState> st;
-    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, e_dst, e_rank, arrivals, hlist, anchors;
+    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, e_dst, e_rank, arrivals, hlist, anchors, tile_row;
     DBuf<int16_t> hslot;
     DBuf<uint64_t> hub2;
     DBuf<uint64_t> hmask;
@@ -207,6 +207,7 @@ Arena make_arena(pg_ctx* c) {
     A.arrivals = c->cfg.record_trace ? c->arrivals.p : nullptr;
     A.anchors_out = c->cfg.record_trace ? c->anchors.p : nullptr;
     A.big_list = c->big_list.p;
+    A.tile_row = c->tile_row.p;
     A.len_tmp = c->len_tmp.p;
     A.tilesum = c->tilesum.p;
     A.tileoff = c->tileoff.p;
@@ -458,6 +459,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->w, S));
     PG_CUDA(c, dalloc(c->cdf, S));
     PG_CUDA(c, dalloc(c->guide, S));
+    PG_CUDA(c, dalloc(c->tile_row, M / kCopyTile + 2 * (int64_t)R + 2));
     PG_CUDA(c, dalloc(c->len_tmp, S));
     PG_CUDA(c, dalloc(c->sort_small, S));
     PG_CUDA(c, dalloc(c->sort_large, S));
@@ -905,7 +907,7 @@ void pg_destroy(pg_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     destroy_graph_exec(c);
-    DBuf<int32_t>* i32[] = {&c->tile_rep, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list,
+    DBuf<int32_t>* i32[] = {&c->tile_rep, &c->tile_row, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list,
                             &c->e_dst, &c->e_rank, &c->arrivals, &c->anchors, &c->fwd_col, &c->bwd_col[0],
                             &c->bwd_col[1]};
     for (auto* b : i32) dfree(*b);
@@ -1750,6 +1752,56 @@ pg_status pg_rc_copy_agents(pg_ctx* c, int32_t replica, double* out) {
     const Replica& r = c->h_rep[(size_t)replica];
     PG_CUDA(c, cudaSetDevice(c->device));
     PG_CUDA(c, cudaMemcpyAsync(out, c->rc_agent.p + 6 * r.abase, 8 * 6 * (size_t)r.delta, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+
+// ---------------------------------------------------------------- text output
+pg_status pg_format_edges(pg_ctx* c, int32_t replica, const int64_t* ids, int64_t n_ids, char* out,
+                          int64_t cap, int64_t* bytes) {
+    if (!c || !ids || !bytes) return PG_ERR_ARG;
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (replica < 0 || replica >= c->R) return fail(c, PG_ERR_ARG, "replica out of range");
+    const HostRep& h = c->hrep[(size_t)replica];
+    if (n_ids != h.n) return fail(c, PG_ERR_ARG, "ids must hold one id per node");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    const int64_t n = h.n, m = h.m;
+    struct Tmp {
+        DBuf<int64_t> did, off, bs;
+        DBuf<int32_t> len;
+        DBuf<char> txt;
+        ~Tmp() {
+            dfree(did);
+            dfree(off);
+            dfree(bs);
+            dfree(len);
+            dfree(txt);
+        }
+    } t;
+    PG_CUDA(c, dalloc(t.did, n));
+    PG_CUDA(c, dalloc(t.len, std::max<int64_t>(m, 1)));
+    PG_CUDA(c, dalloc(t.off, m + 1));
+    PG_CUDA(c, dalloc(t.bs, scan_blocks_needed(std::max<int64_t>(m, 1)) + 2));
+    PG_CUDA(c, cudaMemcpyAsync(t.did.p, ids, 8 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    const int64_t* fo = c->fwd_off.p + h.obase;
+    const int32_t* fc = c->fwd_col.p + h.ebase;
+    cudaGetLastError();
+    launch_text_len(fo, fc, n, m, t.did.p, t.len.p, c->num_sms, c->stream);
+    launch_scan_i32_to_i64(t.len.p, t.off.p, m, t.bs.p, c->stream);
+    PG_CUDA(c, cudaGetLastError());
+    int64_t total = 0;
+    PG_CUDA(c, cudaMemcpyAsync(&total, t.off.p + m, 8, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    *bytes = total;
+    if (!out) return PG_OK;
+    if (cap < total)
+        return fail(c, PG_ERR_CAPACITY, "the output buffer holds " + std::to_string(cap) + " bytes, the text needs " +
+                                            std::to_string(total));
+    PG_CUDA(c, dalloc(t.txt, std::max<int64_t>(total, 1)));
+    launch_text_write(fo, fc, n, m, t.did.p, t.off.p, t.txt.p, c->num_sms, c->stream);
+    PG_CUDA(c, cudaGetLastError());
+    PG_CUDA(c, cudaMemcpyAsync(out, t.txt.p, (size_t)total, cudaMemcpyDeviceToHost, c->stream));
     PG_CUDA(c, cudaStreamSynchronize(c->stream));
     return PG_OK;
 }

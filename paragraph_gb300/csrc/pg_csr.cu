@@ -42,6 +42,11 @@ __global__ void __launch_bounds__(kTileThreads) k_bwd_len(Arena A) {
         int64_t len = 0;
         if (v < nact) {
             const int64_t old = v < rp.n ? off[v + 1] - off[v] : 0;
+            if (old > 0) {
+                // the copy tiles whose first position lies in this row start their row search here
+                for (int64_t ct = (off[v] + kCopyTile - 1) / kCopyTile; ct * kCopyTile < off[v + 1]; ++ct)
+                    A.tile_row[rp.ctbase + ct] = (int32_t)v;
+            }
             const int ic = A.inc[slot];
             len = old + ic;
             if (ic) {
@@ -116,7 +121,6 @@ __device__ __forceinline__ int64_t row_of(const int64_t* off, int64_t lo, int64_
 constexpr int kCopyRows = 2048;
 
 __global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
-    __shared__ int64_t s_rows[2];
     __shared__ int64_t s_oc[kCopyRows + 1];  // old offsets of the tile's rows, and the next one
     __shared__ int64_t s_sh[kCopyRows];      // new minus old offset of the tile's rows
     if (A.st->error) return;
@@ -138,13 +142,12 @@ __global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
         const int64_t* on = A.bwd_off_nxt + rp.obase;
         const int32_t* cc = A.bwd_col_cur + rp.ebase;
         int32_t* cn = A.bwd_col_nxt + rp.ebase;
-        if (threadIdx.x == 0) {
-            s_rows[0] = row_of(oc, 0, rp.n - 1, p0);
-            s_rows[1] = row_of(oc, s_rows[0], rp.n - 1, p1 - 1);
-            moved += (unsigned long long)(p1 - p0);
-        }
-        __syncthreads();
-        const int64_t r0 = s_rows[0], r1 = s_rows[1];
+        // rows holding the tile's first position and the next tile's first position (recorded by
+        // k_bwd_len); the tile's last position lies in a row between them
+        const int64_t tl = t - rp.ctbase;
+        const int64_t r0 = A.tile_row[t];
+        const int64_t r1 = (tl + 1) * kCopyTile < rp.m ? (int64_t)A.tile_row[t + 1] : rp.n - 1;
+        if (threadIdx.x == 0) moved += (unsigned long long)(p1 - p0);
         const int64_t nr = r1 - r0 + 1;
         if (nr <= kCopyRows) {
             for (int64_t i = threadIdx.x; i < nr; i += blockDim.x) {

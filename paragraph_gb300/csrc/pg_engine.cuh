@@ -145,6 +145,7 @@ struct Arena {
     int32_t* arrivals;         // [edge cap] or null
     int32_t* anchors_out;      // [agent cap][4] anchors of each agent, or null (record_trace)
     int32_t* big_list;         // [agent cap]
+    int32_t* tile_row;         // [copy tiles] row holding the first position of each copy tile
     int64_t* len_tmp;          // [slots]
     uint64_t* tilesum;         // [ntiles]
     uint64_t* tileoff;         // [ntiles]
@@ -290,6 +291,11 @@ void launch_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_t*
                             cudaStream_t s);
 int scan_blocks_needed(int64_t n);
 cudaError_t init_agent_kernels();
+// the edge list as text on the device (pg_text.cu)
+void launch_text_len(const int64_t* fo, const int32_t* fc, int64_t n, int64_t m, const int64_t* ids, int32_t* len,
+                     int num_sms, cudaStream_t s);
+void launch_text_write(const int64_t* fo, const int32_t* fc, int64_t n, int64_t m, const int64_t* ids,
+                       const int64_t* off, char* out, int num_sms, cudaStream_t s);
 // device CSR construction from a raw edge list (pg_build.cu)
 size_t build_scratch_bytes(int64_t m, int64_t n);
 void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,

@@ -20,6 +20,16 @@
 // adj(j) (forward row, then backward row) 32 entries at a time and stops at the first hit; the
 // number of entries it examined feeds the byte model.
 
+// Per-warp shared-memory part of an agent's ball (kept out of registers: read only on the rare
+// paths of hub anchors, oversized anchors and hub candidates).
+struct BallAux {
+    unsigned long long ha[kMaskWords];     // hub bits of hub anchors
+    unsigned long long hm[kMaskWords];     // hubs in the ball through Z or a hub anchor
+    int32_t anchors[PG_MAX_ANCHORS_DEV];
+    int32_t big[PG_MAX_ANCHORS_DEV];       // non-hub anchor whose rows did not fit in H
+    int32_t na;
+};
+
 constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a bulk-copy barrier before giving up
 
 // STAGE: adjacency entries staged per chunk and warp (1024 in the small-hash k <= 64 kernel, 512
@@ -32,6 +42,7 @@ struct ThinSmem {
     int32_t out[KCAP];
     int32_t c_id[KCAP];
     uint64_t c_cq[KCAP];
+    BallAux aux;
     unsigned long long bar;  // mbarrier of the warp's bulk copies
 };
 
@@ -88,14 +99,10 @@ struct Ball {
     const int16_t* hslot;             // hub bit of the node or -1
     const unsigned long long* hmask;  // [node][kMaskWords]
     const int32_t* H;                 // frontier hash set (shared memory)
+    const BallAux* X;                 // anchors and hub masks (shared memory)
     int hbits;                        // log2 of the hash capacity
     bool small;                       // every non-hub anchor's rows are in H
-    int na;
-    int anchors[PG_MAX_ANCHORS_DEV];
-    bool big_anchor[PG_MAX_ANCHORS_DEV];  // non-hub anchor whose rows did not fit in H
-    Mask ha;                          // hub bits of hub anchors
-    bool any_ha;
-    Mask hm;                          // hubs in the ball through Z or a hub anchor
+    bool any_ha;                      // some anchor is a hub
 };
 
 __device__ __forceinline__ bool contains(const int32_t* a, int64_t lo, int64_t hi, int32_t v) {
@@ -145,9 +152,10 @@ __device__ __forceinline__ bool mask_bit(const Mask& m, int b) { return (m.w[b >
 __device__ __forceinline__ bool in_z(const Ball& B, int32_t v) {
     if (hash_contains(B.H, B.hbits, v)) return true;
     if (!B.small) {
-        for (int i = 0; i < B.na; ++i) {
-            if (!B.big_anchor[i]) continue;
-            const int x = B.anchors[i];
+        const BallAux& X = *B.X;
+        for (int i = 0; i < X.na; ++i) {
+            if (!X.big[i]) continue;
+            const int x = X.anchors[i];
             if (contains(B.fc, B.fo[x], B.fo[x + 1], v) || contains(B.bc, B.bo[x], B.bo[x + 1], v))
                 return true;
         }
@@ -156,7 +164,7 @@ __device__ __forceinline__ bool in_z(const Ball& B, int32_t v) {
         const unsigned long long* m = B.hmask + (int64_t)v * kMaskWords;
 #pragma unroll
         for (int w = 0; w < kMaskWords; ++w)
-            if (m[w] & B.ha.w[w]) return true;
+            if (m[w] & B.X->ha[w]) return true;
     }
     return false;
 }
@@ -197,7 +205,7 @@ __device__ bool member_warp(const Ball& B, int32_t j, long long& examined) {
     examined = 0;
     if (in_z(B, j)) return true;  // every lane evaluates the same thing
     const int hs = hub_slot(B, j);
-    if (hs >= 0) return mask_bit(B.hm, hs);
+    if (hs >= 0) return (B.X->hm[hs >> 6] >> (hs & 63)) & 1ull;
     return member_rows_warp(B, j, examined);
 }
 
@@ -224,58 +232,72 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     B.hslot = A.hslot + rp.nbase;
     B.hmask = reinterpret_cast<const unsigned long long*>(A.hmask) + rp.nbase * kMaskWords;
     B.H = S.H;
+    B.X = &S.aux;
     B.hbits = kHBits;
     B.small = true;
-    B.na = 0;
     B.any_ha = false;
-#pragma unroll
-    for (int w = 0; w < kMaskWords; ++w) B.ha.w[w] = B.hm.w[w] = 0ull;
     const bool boost = rp.p_global < 1.0;
     long long rows = 0;
 
     // ---------------------------------------------------------------- frontier
+    // (every lane computes the same anchor facts; lane 0 stores them in the warp's BallAux)
+    Mask ha;
+#pragma unroll
+    for (int w = 0; w < kMaskWords; ++w) ha.w[w] = 0ull;
+    int anc[PG_MAX_ANCHORS_DEV];
+    bool big[PG_MAX_ANCHORS_DEV];
+    const int na = boost ? rp.anchors : 0;
     if (boost) {
         for (int q = lane; q < HCAP; q += 32) S.H[q] = -1;
-        B.na = rp.anchors;
         const u32x4 xa = draw(A.seed, kStreamAnchor, rep, ep, unit, 0);
         int64_t zsize = 0;
 #pragma unroll
         for (int i = 0; i < PG_MAX_ANCHORS_DEV; ++i) {
-            B.anchors[i] = (int)bounded32(xa.x[i], (uint32_t)n);
-            B.big_anchor[i] = false;
+            anc[i] = (int)bounded32(xa.x[i], (uint32_t)n);
+            big[i] = false;
         }
-        for (int i = 0; i < B.na; ++i) {
-            const int x = B.anchors[i];
+        for (int i = 0; i < na; ++i) {
+            const int x = anc[i];
             const int64_t d = (B.fo[x + 1] - B.fo[x]) + (B.bo[x + 1] - B.bo[x]);
             rows += d + 1;
             const int hs = hub_slot(B, x);
             if (hs >= 0) {
-                B.ha.w[hs >> 6] |= 1ull << (hs & 63);
+                ha.w[hs >> 6] |= 1ull << (hs & 63);
                 B.any_ha = true;
             } else {
                 zsize += d;
             }
         }
         // non-hub anchors whose rows would overflow the shared frontier stay implicit
-        if (zsize + B.na > ZCAP) {
+        if (zsize + na > ZCAP) {
             B.small = false;
-            zsize = B.na;
-            for (int i = 0; i < B.na; ++i) {
-                const int x = B.anchors[i];
+            zsize = na;
+            for (int i = 0; i < na; ++i) {
+                const int x = anc[i];
                 if (hub_slot(B, x) >= 0) continue;
                 const int64_t d = (B.fo[x + 1] - B.fo[x]) + (B.bo[x + 1] - B.bo[x]);
                 if (zsize + d <= ZCAP)
                     zsize += d;
                 else
-                    B.big_anchor[i] = true;
+                    big[i] = true;
             }
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int i = 0; i < PG_MAX_ANCHORS_DEV; ++i) {
+                S.aux.anchors[i] = anc[i];
+                S.aux.big[i] = big[i] ? 1 : 0;
+            }
+            S.aux.na = na;
+#pragma unroll
+            for (int w = 0; w < kMaskWords; ++w) S.aux.ha[w] = ha.w[w];
         }
         __syncwarp();
         Mask hm;
 #pragma unroll
         for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] = 0ull;
-        for (int i = 0; i < B.na; ++i) {
-            const int x = B.anchors[i];
+        for (int i = 0; i < na; ++i) {
+            const int x = anc[i];
             if (lane == 0) {
                 hash_insert(S.H, kHBits, x);
                 const unsigned long long* m = B.hmask + (int64_t)x * kMaskWords;
@@ -283,7 +305,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                 for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] |= m[ww];
             }
             if (hub_slot(B, x) >= 0) continue;
-            const bool into_hash = !B.big_anchor[i];
+            const bool into_hash = !big[i];
             for (int dir = 0; dir < 2; ++dir) {
                 const int64_t* off = dir ? B.bo : B.fo;
                 const int32_t* col = dir ? B.bc : B.fc;
@@ -300,7 +322,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             const unsigned long long* hh = reinterpret_cast<const unsigned long long*>(A.hub2) +
                                            (int64_t)r * kHeavyMax * kMaskWords;
             for (int b = lane; b < kHeavyMax; b += 32)
-                if (mask_bit(B.ha, b)) {
+                if (mask_bit(ha, b)) {
 #pragma unroll
                     for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] |= hh[(int64_t)b * kMaskWords + ww];
                 }
@@ -310,7 +332,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             unsigned lo = (unsigned)hm.w[ww], hi = (unsigned)(hm.w[ww] >> 32);
             lo = __reduce_or_sync(kFull, lo);
             hi = __reduce_or_sync(kFull, hi);
-            B.hm.w[ww] = ((unsigned long long)hi << 32) | lo;
+            if (lane == 0) S.aux.hm[ww] = ((unsigned long long)hi << 32) | lo;
         }
         __syncwarp();
     }
@@ -357,7 +379,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             } else {
                 const int hs = hub_slot(B, j);
                 if (hs >= 0) {
-                    mem = mask_bit(B.hm, hs);
+                    mem = (B.X->hm[hs >> 6] >> (hs & 63)) & 1ull;
                 } else {
                     f0 = B.fo[j];
                     lf = B.fo[j + 1] - f0;
@@ -409,36 +431,36 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                 mbar_wait(&S.bar, phase ^ 1u);
                 return false;
             }
+            // owner by owner, in 32-bit chunk coordinates: chunk position q maps to row position
+            // q + fx0 (forward window, q < qf) or q + bx0 (backward window); valid entries are the
+            // row's own (forward: [0, lf), backward: [lf, d)), the rest is window padding
+            const int64_t qf64 = wx + fw - c0;
+            const int qs = (int)(s0 - c0), qe = (int)(s1 - c0);
+            const int qf = (int)(qf64 < -1 ? -1 : (qf64 > kStage ? kStage : qf64));
+            const int fx0 = (int)((c0 - wx) + (fa0 - f0));
+            const int bx0 = (int)(lf + (c0 - wx - fw) + (ba0 - b0));
+            const int lf32 = (int)lf, d32 = (int)d;
             unsigned om = __ballot_sync(kFull, s1 > s0);
             while (om) {
                 const int o = __ffs(om) - 1;
                 om &= om - 1u;
-                const int64_t os0 = __shfl_sync(kFull, s0, o), os1 = __shfl_sync(kFull, s1, o);
-                const int64_t owx = __shfl_sync(kFull, wx, o), ofw = __shfl_sync(kFull, fw, o);
-                const int64_t ofa0 = __shfl_sync(kFull, fa0, o), of0 = __shfl_sync(kFull, f0, o);
-                const int64_t olf = __shfl_sync(kFull, lf, o), oba0 = __shfl_sync(kFull, ba0, o);
-                const int64_t ob0 = __shfl_sync(kFull, b0, o), olb = __shfl_sync(kFull, lb, o);
-                for (int64_t q0 = os0; q0 < os1; q0 += 32) {
-                    const int64_t q = q0 + lane;
+                const int oqs = __shfl_sync(kFull, qs, o), oqe = __shfl_sync(kFull, qe, o);
+                const int oqf = __shfl_sync(kFull, qf, o), ofx0 = __shfl_sync(kFull, fx0, o);
+                const int obx0 = __shfl_sync(kFull, bx0, o), olf = __shfl_sync(kFull, lf32, o);
+                const int od = __shfl_sync(kFull, d32, o);
+                for (int q0 = oqs; q0 < oqe; q0 += 32) {
+                    const int q = q0 + lane;
                     bool hit = false;
-                    int64_t x = 0;
-                    if (q < os1) {
-                        const int64_t off = q - owx;
-                        bool valid;
-                        if (off < ofw) {
-                            const int64_t idx = ofa0 + off;
-                            valid = idx >= of0 && idx < of0 + olf;
-                            x = idx - of0;
-                        } else {
-                            const int64_t idx = oba0 + (off - ofw);
-                            valid = idx >= ob0 && idx < ob0 + olb;
-                            x = olf + (idx - ob0);
-                        }
-                        if (valid) hit = in_z(B, S.stage[q - c0]);
+                    int x = 0;
+                    if (q < oqe) {
+                        const bool fwd = q < oqf;
+                        x = q + (fwd ? ofx0 : obx0);
+                        const bool valid = fwd ? (x >= 0 && x < olf) : (x >= olf && x < od);
+                        if (valid) hit = in_z(B, S.stage[q]);
                     }
                     const unsigned hm = __ballot_sync(kFull, hit);
                     if (hm) {
-                        const int64_t xh = __shfl_sync(kFull, x, __ffs(hm) - 1);
+                        const int xh = __shfl_sync(kFull, x, __ffs(hm) - 1);
                         if (lane == o) mp = xh;
                         break;
                     }

@@ -246,3 +246,22 @@ def test_edges_into_caller_buffers(gpu):
         b = eng.edges(f, c, out=buf)
         np.testing.assert_array_equal(a[0], b[0])
         np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_format_edges_text(gpu):
+    """The device text writer prints every edge as "ids[source],ids[target]\\n" in forward-CSR
+    order, for large, small and negative ids."""
+    g = W.plain_pa_seed(3000, 5, seed=8)
+    with GrowthEngine(seed=4) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, PAParams(fixed_new_nodes=500), planned_epochs=1)
+        eng.grow_epoch()
+        n, m = eng.counts()
+        ids = 10**12 + 7 * np.arange(n, dtype=np.int64) - 5
+        ids[0], ids[3], ids[7] = 0, -42, 9
+        txt = eng.format_edges(ids)
+        off, col = eng.csr(0)
+        src = np.repeat(np.arange(n), np.diff(off))
+        expect = "".join(f"{ids[s]},{ids[d]}\n" for s, d in zip(src, col)).encode()
+        assert txt == expect
+        with pytest.raises(PGError):
+            eng.format_edges(ids[:-1])
