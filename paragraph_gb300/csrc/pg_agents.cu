@@ -432,22 +432,45 @@ __global__ void k_edges_check(Arena A, int64_t agents) {
     }
 }
 
+// entries per stage buffer of the thinning sampler (two buffers per warp)
+template <int KCAP, bool HSMALL>
+struct ThinStage {
+    static constexpr int value = (KCAP <= kKSmall && HSMALL) ? 1024 : 512;
+};
+
+template <int KCAP, bool HSMALL>
+constexpr size_t thin_smem_bytes() {
+    constexpr int HCAP = (KCAP <= kKSmall && !HSMALL) ? 2 * kZCap : kZCap;
+    return sizeof(ThinSmem<KCAP, HCAP, ThinStage<KCAP, HSMALL>::value>) * kAgentWarps;
+}
+
 template <int KCAP, bool BIG, bool THIN, bool HSMALL = false>
-__global__ void __launch_bounds__(kAgentWarps * 32) k_agents(Arena A, int64_t agents) {
+__global__ void __launch_bounds__(kAgentWarps * 32, 4) k_agents(Arena A, int64_t agents) {
     // frontier hash capacity: 2048 slots for the common small-k kernel (1024 in the HSMALL variant,
     // which fits more CTAs per SM), 1024 for the k <= 256 one so that four warps stay within 48 KiB
     // of static shared memory
     constexpr int HCAP = (KCAP <= kKSmall && !HSMALL) ? 2 * kZCap : kZCap;
-    constexpr int STAGE = (KCAP <= kKSmall && HSMALL) ? 1024 : 512;
+    constexpr int STAGE = ThinStage<KCAP, HSMALL>::value;
     using Smem = typename std::conditional<THIN, ThinSmem<KCAP, HCAP, STAGE>, AgentSmem<KCAP>>::type;
-    __shared__ Smem smem[kAgentWarps];
+    Smem* smem;
+    if constexpr (THIN) {
+        // the thinning variants hold two stage buffers per warp and go past 48 KiB: dynamic
+        extern __shared__ __align__(16) unsigned char agent_dsm[];
+        smem = reinterpret_cast<Smem*>(agent_dsm);
+    } else {
+        __shared__ Smem agent_ssm[kAgentWarps];
+        smem = agent_ssm;
+    }
     if (A.st->error) return;
     Smem& S = smem[threadIdx.x >> 5];
     const int lane = lane_id();
     const int64_t limit = BIG ? (int64_t)A.st->big_count : agents;
     uint32_t phase = 0;
     if constexpr (THIN) {
-        if (lane == 0) mbar_init(&S.bar, 1);
+        if (lane == 0) {
+            mbar_init(&S.bar[0], 1);
+            mbar_init(&S.bar[1], 1);
+        }
         fence_proxy_async();
         __syncwarp();
     }
@@ -516,9 +539,14 @@ cudaError_t init_agent_kernels() {
     const int th = kAgentWarps * 32;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[0][0], k_agents<kKSmall, false, false>, th, 0);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[0][1], k_agents<kKMax, true, false>, th, 0);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[1][0], k_agents<kKSmall, false, true>, th, 0);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[1][1], k_agents<kKMax, true, true>, th, 0);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_hsmall, k_agents<kKSmall, false, true, true>, th, 0);
+    constexpr size_t ds = thin_smem_bytes<kKSmall, false>(), db = thin_smem_bytes<kKMax, false>(),
+                     dh = thin_smem_bytes<kKSmall, true>();
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents<kKSmall, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ds);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents<kKMax, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)db);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents<kKSmall, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dh);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[1][0], k_agents<kKSmall, false, true>, th, ds);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[1][1], k_agents<kKMax, true, true>, th, db);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_hsmall, k_agents<kKSmall, false, true, true>, th, dh);
     for (auto& row : g_blocks)
         for (int& b : row)
             if (b < 1) b = 1;
@@ -543,10 +571,10 @@ void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) 
     const int th = kAgentWarps * 32;
     if (t) {
         if (hs)
-            k_agents<kKSmall, false, true, true><<<(unsigned)grid, th, 0, s>>>(A, agents);
+            k_agents<kKSmall, false, true, true><<<(unsigned)grid, th, thin_smem_bytes<kKSmall, true>(), s>>>(A, agents);
         else
-            k_agents<kKSmall, false, true><<<(unsigned)grid, th, 0, s>>>(A, agents);
-        k_agents<kKMax, true, true><<<gbig, th, 0, s>>>(A, agents);
+            k_agents<kKSmall, false, true><<<(unsigned)grid, th, thin_smem_bytes<kKSmall, false>(), s>>>(A, agents);
+        k_agents<kKMax, true, true><<<gbig, th, thin_smem_bytes<kKMax, false>(), s>>>(A, agents);
     } else {
         k_agents<kKSmall, false, false><<<(unsigned)grid, th, 0, s>>>(A, agents);
         k_agents<kKMax, true, false><<<gbig, th, 0, s>>>(A, agents);

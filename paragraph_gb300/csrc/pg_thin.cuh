@@ -36,14 +36,14 @@ constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a bulk-copy barrier befor
 // where the frontier hash or k is larger, so four warps stay within 48 KiB of static shared memory)
 template <int KCAP, int HCAP, int STAGE>
 struct ThinSmem {
-    __align__(16) int32_t stage[STAGE];  // candidate rows, filled by bulk asynchronous copies
+    __align__(16) int32_t stage[2][STAGE];  // candidate rows, two buffers filled by bulk copies
     int32_t H[HCAP];  // frontier hash set, -1 = empty
     int32_t arr[KCAP];
     int32_t out[KCAP];
     int32_t c_id[KCAP];
     uint64_t c_cq[KCAP];
     BallAux aux;
-    unsigned long long bar;  // mbarrier of the warp's bulk copies
+    unsigned long long bar[2];  // mbarriers of the two stage buffers
 };
 
 // ---- bulk asynchronous copies (the TMA engine's cp.async.bulk) into shared memory
@@ -117,8 +117,11 @@ __device__ __forceinline__ bool contains(const int32_t* a, int64_t lo, int64_t h
     return l < hi && a[l] == v;
 }
 
+// The frontier set is an open-addressing table probed linearly from the first slot of a 4-slot
+// bucket.  With no deletions a bucket always fills as a prefix, so a lookup reads a whole bucket
+// with one 16-byte load and stops at the first bucket whose last slot is free.
 __device__ __forceinline__ uint32_t hslot_of(int32_t v, int bits) {
-    return ((uint32_t)v * 0x9E3779B1u) >> (32 - bits);
+    return (((uint32_t)v * 0x9E3779B1u) >> (34 - bits)) << 2;
 }
 
 // Insert v into the shared hash set (any lane, concurrently).
@@ -132,14 +135,18 @@ __device__ __forceinline__ void hash_insert(int32_t* H, int bits, int32_t v) {
     }
 }
 
+__device__ __forceinline__ bool bucket_has(const int4& b, int32_t v) {
+    return b.x == v || b.y == v || b.z == v || b.w == v;
+}
+
 __device__ __forceinline__ bool hash_contains(const int32_t* H, int bits, int32_t v) {
     const uint32_t mask = (1u << bits) - 1u;
     uint32_t s = hslot_of(v, bits);
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-        const int k = H[s];
-        if (k == v) return true;
-        if (k == -1) return false;
-        s = (s + 1u) & mask;
+    for (uint32_t probe = 0; probe <= mask; probe += 4) {
+        const int4 b = *reinterpret_cast<const int4*>(H + s);
+        if (bucket_has(b, v)) return true;
+        if (b.w == -1) return false;
+        s = (s + 4u) & mask;
     }
     return false;
 }
@@ -374,26 +381,27 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
         long long ex = 0;
         int64_t d = 0, f0 = 0, lf = 0, b0 = 0;
         if (lane == __ffs(grp) - 1 && !pre && (grp & bm)) {
+            // the node's hub slot and row bounds are loaded before the frontier probe, so the
+            // global loads overlap the shared-memory hash lookups
+            const int hs = hub_slot(B, j);
+            const int64_t jf0 = B.fo[j], jf1 = B.fo[j + 1], jb0 = B.bo[j], jb1 = B.bo[j + 1];
             if (in_z(B, j)) {
                 mem = true;
+            } else if (hs >= 0) {
+                mem = (B.X->hm[hs >> 6] >> (hs & 63)) & 1ull;
             } else {
-                const int hs = hub_slot(B, j);
-                if (hs >= 0) {
-                    mem = (B.X->hm[hs >> 6] >> (hs & 63)) & 1ull;
-                } else {
-                    f0 = B.fo[j];
-                    lf = B.fo[j + 1] - f0;
-                    b0 = B.bo[j];
-                    d = lf + (B.bo[j + 1] - b0);
-                    scan = d > 0;
-                    ex = d;  // a miss examines both rows
-                }
+                f0 = jf0;
+                lf = jf1 - jf0;
+                b0 = jb0;
+                d = lf + (jb1 - jb0);
+                scan = d > 0;
+                ex = d;  // a miss examines both rows
             }
         }
         // The rows of every node under test are staged into shared memory by bulk asynchronous
         // copies of 16-byte-aligned windows around them (forward window, then backward window,
-        // lane after lane), kStage entries per chunk, and tested against the frontier owner by
-        // owner; a row stops at its first hit, and a row with a hit copies nothing more.
+        // lane after lane), kStage entries per chunk; each row keeps its first hit, and a row with
+        // a hit copies nothing more.
         const int64_t lb = d - lf;
         const int64_t fa0 = f0 & ~3ll, fw = lf > 0 ? (((f0 + lf + 3) & ~3ll) - fa0) : 0;
         const int64_t ba0 = b0 & ~3ll, bw = lb > 0 ? (((b0 + lb + 3) & ~3ll) - ba0) : 0;
@@ -402,67 +410,115 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
         const int64_t wx = wincl - W;
         const int64_t DW = __shfl_sync(kFull, wincl, 31);
         int64_t mp = d;  // first-hit position of this lane's node (d: none yet)
-        for (int64_t c0 = 0; c0 < DW; c0 += kStage) {
+        // this lane's part of chunk c0 (empty once its row has a hit)
+        auto part = [&](int64_t c0, int64_t& s0, int64_t& s1) {
             const int64_t c1 = c0 + kStage < DW ? c0 + kStage : DW;
-            int64_t s0 = wx > c0 ? wx : c0, s1 = wx + W < c1 ? wx + W : c1;
+            s0 = wx > c0 ? wx : c0;
+            s1 = wx + W < c1 ? wx + W : c1;
             if (mp < d || s1 < s0) s1 = s0;
+        };
+        // issue the bulk copies of chunk c0 into buffer `buf`; false when nothing is copied
+        auto issue = [&](int64_t c0, int buf) -> bool {
+            int64_t s0, s1;
+            part(c0, s0, s1);
             const uint32_t total = __reduce_add_sync(kFull, (uint32_t)(s1 - s0) * 4u);
-            if (total == 0) continue;
-            __syncwarp();  // the previous chunk's reads of the stage are done
+            if (total == 0) return false;
+            __syncwarp();  // earlier reads of this buffer are done
             fence_proxy_async();
-            if (lane == 0) mbar_expect_tx(&S.bar, total);
+            if (lane == 0) mbar_expect_tx(&S.bar[buf], total);
             __syncwarp();
             if (s1 > s0) {
                 const int64_t fe = wx + fw;
                 if (s0 < fe) {
                     const int64_t e1 = s1 < fe ? s1 : fe;
-                    bulk_g2s(&S.stage[s0 - c0], B.fc + fa0 + (s0 - wx), (uint32_t)(e1 - s0) * 4u, &S.bar);
+                    bulk_g2s(&S.stage[buf][s0 - c0], B.fc + fa0 + (s0 - wx), (uint32_t)(e1 - s0) * 4u,
+                             &S.bar[buf]);
                 }
                 if (s1 > fe) {
                     const int64_t e0 = s0 > fe ? s0 : fe;
-                    bulk_g2s(&S.stage[e0 - c0], B.bc + ba0 + (e0 - fe), (uint32_t)(s1 - e0) * 4u, &S.bar);
+                    bulk_g2s(&S.stage[buf][e0 - c0], B.bc + ba0 + (e0 - fe), (uint32_t)(s1 - e0) * 4u,
+                             &S.bar[buf]);
                 }
             }
-            const bool ok = mbar_wait(&S.bar, phase);
-            phase ^= 1u;
+            return true;
+        };
+        // chunks are double-buffered: chunk c+1 is in flight while chunk c is tested
+        const bool simple = B.small && !B.any_ha;  // membership in Z is the frontier hash alone
+        const int64_t nchunk = (DW + kStage - 1) / kStage;
+        uint32_t armed = 0;  // bit b: buffer b has copies in flight
+        if (nchunk > 0 && issue(0, 0)) armed = 1u;
+        for (int64_t c = 0; c < nchunk; ++c) {
+            const int buf = (int)(c & 1);
+            const int64_t c0 = c * kStage;
+            if (c + 1 < nchunk && issue(c0 + kStage, buf ^ 1)) armed |= 2u >> buf;
+            if (!((armed >> buf) & 1u)) continue;
+            armed &= ~(1u << buf);
+            const bool ok = mbar_wait(&S.bar[buf], (phase >> buf) & 1u);
+            phase ^= 1u << buf;
             if (!__all_sync(kFull, ok)) {
                 // give the copies in flight a second bounded wait, then abandon the warp
                 if (lane == 0) atomicOr(&A.st->error, kErrTimeout);
-                mbar_wait(&S.bar, phase ^ 1u);
+                mbar_wait(&S.bar[buf], ((phase >> buf) & 1u) ^ 1u);
+                if (armed) mbar_wait(&S.bar[buf ^ 1], (phase >> (buf ^ 1)) & 1u);
                 return false;
             }
-            // owner by owner, in 32-bit chunk coordinates: chunk position q maps to row position
-            // q + fx0 (forward window, q < qf) or q + bx0 (backward window); valid entries are the
-            // row's own (forward: [0, lf), backward: [lf, d)), the rest is window padding
-            const int64_t qf64 = wx + fw - c0;
-            const int qs = (int)(s0 - c0), qe = (int)(s1 - c0);
+            const int32_t* stg = S.stage[buf];
+            // The chunk is tested flat, four entries per lane and step, whatever row they belong
+            // to; a hit is then given to the lane whose window holds it, which keeps it when its
+            // row has no hit yet and the entry is the row's own (not window padding).  Entries of
+            // a row whose hit came in an earlier chunk (copied before the hit was known) or of a
+            // row not copied at all (stale) are tested too and their hits dropped.  Chunk
+            // position q maps to row position q + fx0 in the forward window (q < qf), q + bx0 in
+            // the backward one.
+            const int nq = (int)(DW - c0 < kStage ? DW - c0 : kStage);
+            const int64_t wlo64 = wx - c0, whi64 = wx + W - c0, qf64 = wx + fw - c0;
+            const int wlo = (int)(wlo64 < -1 ? -1 : (wlo64 > kStage ? kStage : wlo64));
+            const int whi = (int)(whi64 < -1 ? -1 : (whi64 > kStage ? kStage : whi64));
             const int qf = (int)(qf64 < -1 ? -1 : (qf64 > kStage ? kStage : qf64));
             const int fx0 = (int)((c0 - wx) + (fa0 - f0));
             const int bx0 = (int)(lf + (c0 - wx - fw) + (ba0 - b0));
             const int lf32 = (int)lf, d32 = (int)d;
-            unsigned om = __ballot_sync(kFull, s1 > s0);
-            while (om) {
-                const int o = __ffs(om) - 1;
-                om &= om - 1u;
-                const int oqs = __shfl_sync(kFull, qs, o), oqe = __shfl_sync(kFull, qe, o);
-                const int oqf = __shfl_sync(kFull, qf, o), ofx0 = __shfl_sync(kFull, fx0, o);
-                const int obx0 = __shfl_sync(kFull, bx0, o), olf = __shfl_sync(kFull, lf32, o);
-                const int od = __shfl_sync(kFull, d32, o);
-                for (int q0 = oqs; q0 < oqe; q0 += 32) {
-                    const int q = q0 + lane;
-                    bool hit = false;
-                    int x = 0;
-                    if (q < oqe) {
-                        const bool fwd = q < oqf;
-                        x = q + (fwd ? ofx0 : obx0);
-                        const bool valid = fwd ? (x >= 0 && x < olf) : (x >= olf && x < od);
-                        if (valid) hit = in_z(B, S.stage[q]);
+            for (int i0 = 0; i0 < nq; i0 += 128) {
+                bool hit[4];
+                if (simple) {
+                    // the four entries' first buckets are read together; a full bucket without
+                    // the entry (rare at the frontier's load) continues the probe
+                    int32_t v[4];
+                    int4 hb[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int q = i0 + 32 * u + lane;
+                        v[u] = stg[q < nq ? q : 0];
+                        hb[u] = *reinterpret_cast<const int4*>(B.H + hslot_of(v[u], B.hbits));
                     }
-                    const unsigned hm = __ballot_sync(kFull, hit);
-                    if (hm) {
-                        const int xh = __shfl_sync(kFull, x, __ffs(hm) - 1);
-                        if (lane == o) mp = xh;
-                        break;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const bool in = i0 + 32 * u + lane < nq;
+                        hit[u] = in && bucket_has(hb[u], v[u]);
+                        if (in && !hit[u] && hb[u].w != -1) hit[u] = hash_contains(B.H, B.hbits, v[u]);
+                    }
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int q = i0 + 32 * u + lane;
+                        hit[u] = false;
+                        if (q < nq) {  // stale entries may hold any value: only node ids reach the masks
+                            const int32_t v = stg[q];
+                            hit[u] = (uint32_t)v < (uint32_t)n && in_z(B, v);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    unsigned hm = __ballot_sync(kFull, hit[u]);
+                    while (hm) {
+                        const int qh = i0 + 32 * u + __ffs(hm) - 1;
+                        hm &= hm - 1u;
+                        if (qh >= wlo && qh < whi && mp == d) {
+                            const bool fwd = qh < qf;
+                            const int x = qh + (fwd ? fx0 : bx0);
+                            if (fwd ? (x >= 0 && x < lf32) : (x >= lf32 && x < d32)) mp = x;
+                        }
                     }
                 }
             }
