@@ -31,6 +31,7 @@ struct BallAux {
 };
 
 constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a bulk-copy barrier before giving up
+constexpr int kTestU = 4;                  // entries per lane and step of the membership scan
 
 // STAGE: adjacency entries staged per chunk and warp (1024 in the small-hash k <= 64 kernel, 512
 // where the frontier hash or k is larger, so four warps stay within 48 KiB of static shared memory)
@@ -247,91 +248,130 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     long long rows = 0;
 
     // ---------------------------------------------------------------- frontier
-    // (every lane computes the same anchor facts; lane 0 stores them in the warp's BallAux)
+    // Lane l < 2na owns one anchor row (anchor l >> 1; forward row for even l, backward for odd),
+    // so the anchors' row bounds and hub slots load together; every lane then derives the same
+    // anchor facts with shuffles, lane 0 stores them in the warp's BallAux, and the rows of the
+    // non-hub anchors are gathered flat, each entry loaded and inserted independently.
+    static_assert(kMaskWords == 4 && PG_MAX_ANCHORS_DEV == 4, "frontier layout");
     Mask ha;
 #pragma unroll
     for (int w = 0; w < kMaskWords; ++w) ha.w[w] = 0ull;
-    int anc[PG_MAX_ANCHORS_DEV];
-    bool big[PG_MAX_ANCHORS_DEV];
     const int na = boost ? rp.anchors : 0;
     if (boost) {
         for (int q = lane; q < HCAP; q += 32) S.H[q] = -1;
         const u32x4 xa = draw(A.seed, kStreamAnchor, rep, ep, unit, 0);
+        auto anchor = [&](int i) -> int {
+            const uint32_t w = i == 0 ? xa.x[0] : (i == 1 ? xa.x[1] : (i == 2 ? xa.x[2] : xa.x[3]));
+            return (int)bounded32(w, (uint32_t)n);
+        };
+        const int rl = (lane >> 1) & 3;
+        const bool has_row = lane < 2 * na;
+        const int xrow = anchor(rl);
+        int64_t r_st = 0, r_len = 0;
+        int r_hs = -1;
+        if (has_row) {
+            const int64_t* off = (lane & 1) ? B.bo : B.fo;
+            r_st = off[xrow];
+            r_len = off[xrow + 1] - r_st;
+            r_hs = hub_slot(B, xrow);
+        }
+        int64_t dd[PG_MAX_ANCHORS_DEV];
+        int hh[PG_MAX_ANCHORS_DEV];
         int64_t zsize = 0;
 #pragma unroll
         for (int i = 0; i < PG_MAX_ANCHORS_DEV; ++i) {
-            anc[i] = (int)bounded32(xa.x[i], (uint32_t)n);
-            big[i] = false;
-        }
-        for (int i = 0; i < na; ++i) {
-            const int x = anc[i];
-            const int64_t d = (B.fo[x + 1] - B.fo[x]) + (B.bo[x + 1] - B.bo[x]);
-            rows += d + 1;
-            const int hs = hub_slot(B, x);
-            if (hs >= 0) {
-                ha.w[hs >> 6] |= 1ull << (hs & 63);
-                B.any_ha = true;
-            } else {
-                zsize += d;
+            dd[i] = __shfl_sync(kFull, r_len, 2 * i) + __shfl_sync(kFull, r_len, 2 * i + 1);
+            hh[i] = __shfl_sync(kFull, r_hs, 2 * i);
+            if (i < na) {
+                rows += dd[i] + 1;
+                if (hh[i] >= 0) {
+#pragma unroll
+                    for (int w = 0; w < kMaskWords; ++w)
+                        if ((hh[i] >> 6) == w) ha.w[w] |= 1ull << (hh[i] & 63);
+                    B.any_ha = true;
+                } else {
+                    zsize += dd[i];
+                }
             }
         }
         // non-hub anchors whose rows would overflow the shared frontier stay implicit
+        unsigned bigm = 0u;  // bit i: anchor i's rows are not in H
         if (zsize + na > ZCAP) {
             B.small = false;
             zsize = na;
-            for (int i = 0; i < na; ++i) {
-                const int x = anc[i];
-                if (hub_slot(B, x) >= 0) continue;
-                const int64_t d = (B.fo[x + 1] - B.fo[x]) + (B.bo[x + 1] - B.bo[x]);
-                if (zsize + d <= ZCAP)
-                    zsize += d;
+#pragma unroll
+            for (int i = 0; i < PG_MAX_ANCHORS_DEV; ++i) {
+                if (i >= na || hh[i] >= 0) continue;
+                if (zsize + dd[i] <= ZCAP)
+                    zsize += dd[i];
                 else
-                    big[i] = true;
+                    bigm |= 1u << i;
             }
         }
         if (lane == 0) {
 #pragma unroll
             for (int i = 0; i < PG_MAX_ANCHORS_DEV; ++i) {
-                S.aux.anchors[i] = anc[i];
-                S.aux.big[i] = big[i] ? 1 : 0;
+                S.aux.anchors[i] = anchor(i);
+                S.aux.big[i] = (int)((bigm >> i) & 1u);
             }
             S.aux.na = na;
 #pragma unroll
             for (int w = 0; w < kMaskWords; ++w) S.aux.ha[w] = ha.w[w];
         }
-        __syncwarp();
         Mask hm;
 #pragma unroll
         for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] = 0ull;
-        for (int i = 0; i < na; ++i) {
-            const int x = anc[i];
-            if (lane == 0) {
-                hash_insert(S.H, kHBits, x);
-                const unsigned long long* m = B.hmask + (int64_t)x * kMaskWords;
+        auto add_mask = [&](int32_t v) {
+            const ulonglong2* m = reinterpret_cast<const ulonglong2*>(B.hmask + (int64_t)v * kMaskWords);
+            const ulonglong2 m0 = m[0], m1 = m[1];
+            hm.w[0] |= m0.x;
+            hm.w[1] |= m0.y;
+            hm.w[2] |= m1.x;
+            hm.w[3] |= m1.y;
+        };
+        if (lane < na) {
+            const int x = anchor(lane & 3);
+            hash_insert(S.H, kHBits, x);
+            add_mask(x);
+        }
+        // the non-hub anchors' rows, flat: entry p belongs to the last row lane whose exclusive
+        // offset is at or below p (the rows are laid out in lane order)
+        const bool row_in = has_row && r_hs < 0;
+        const int64_t len_in = row_in ? r_len : 0;
+        const int64_t incl = warp_incl_scan(len_in);
+        const int64_t excl = incl - len_in;
+        const int64_t T = __shfl_sync(kFull, incl, 31);
+        const int into = (row_in && !((bigm >> rl) & 1u)) ? 1 : 0;
+        for (int64_t p0 = 0; p0 < T; p0 += 64) {
+            int32_t v[2];
+            int ih[2];
+            bool ok[2];
 #pragma unroll
-                for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] |= m[ww];
+            for (int u = 0; u < 2; ++u) {
+                const int64_t p = p0 + 32 * u + lane;
+                int L = 0;
+#pragma unroll
+                for (int bb = 4; bb >= 1; bb >>= 1)
+                    if (__shfl_sync(kFull, excl, L + bb) <= p) L += bb;
+                const int64_t st = __shfl_sync(kFull, r_st, L), e0 = __shfl_sync(kFull, excl, L);
+                ih[u] = __shfl_sync(kFull, into, L);
+                ok[u] = p < T;
+                v[u] = ok[u] ? ((L & 1) ? B.bc : B.fc)[st + (p - e0)] : 0;
             }
-            if (hub_slot(B, x) >= 0) continue;
-            const bool into_hash = !big[i];
-            for (int dir = 0; dir < 2; ++dir) {
-                const int64_t* off = dir ? B.bo : B.fo;
-                const int32_t* col = dir ? B.bc : B.fc;
-                for (int64_t p = off[x] + lane; p < off[x + 1]; p += 32) {
-                    const int32_t v = col[p];
-                    if (into_hash) hash_insert(S.H, kHBits, v);
-                    const unsigned long long* m = B.hmask + (int64_t)v * kMaskWords;
 #pragma unroll
-                    for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] |= m[ww];
-                }
+            for (int u = 0; u < 2; ++u) {
+                if (!ok[u]) continue;
+                if (ih[u]) hash_insert(S.H, kHBits, v[u]);
+                add_mask(v[u]);
             }
         }
         if (B.any_ha) {
-            const unsigned long long* hh = reinterpret_cast<const unsigned long long*>(A.hub2) +
-                                           (int64_t)r * kHeavyMax * kMaskWords;
-            for (int b = lane; b < kHeavyMax; b += 32)
-                if (mask_bit(ha, b)) {
+            const unsigned long long* hh2 = reinterpret_cast<const unsigned long long*>(A.hub2) +
+                                            (int64_t)r * kHeavyMax * kMaskWords;
+            for (int bb = lane; bb < kHeavyMax; bb += 32)
+                if (mask_bit(ha, bb)) {
 #pragma unroll
-                    for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] |= hh[(int64_t)b * kMaskWords + ww];
+                    for (int ww = 0; ww < kMaskWords; ++ww) hm.w[ww] |= hh2[(int64_t)bb * kMaskWords + ww];
                 }
         }
 #pragma unroll
@@ -423,8 +463,8 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             part(c0, s0, s1);
             const uint32_t total = __reduce_add_sync(kFull, (uint32_t)(s1 - s0) * 4u);
             if (total == 0) return false;
-            __syncwarp();  // earlier reads of this buffer are done
-            fence_proxy_async();
+            // the warp's reads of this buffer have completed (their values fed its ballots)
+            __syncwarp();
             if (lane == 0) mbar_expect_tx(&S.bar[buf], total);
             __syncwarp();
             if (s1 > s0) {
@@ -463,7 +503,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                 return false;
             }
             const int32_t* stg = S.stage[buf];
-            // The chunk is tested flat, four entries per lane and step, whatever row they belong
+            // The chunk is tested flat, kTestU entries per lane and step, whatever row they belong
             // to; a hit is then given to the lane whose window holds it, which keeps it when its
             // row has no hit yet and the entry is the row's own (not window padding).  Entries of
             // a row whose hit came in an earlier chunk (copied before the hit was known) or of a
@@ -478,28 +518,28 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             const int fx0 = (int)((c0 - wx) + (fa0 - f0));
             const int bx0 = (int)(lf + (c0 - wx - fw) + (ba0 - b0));
             const int lf32 = (int)lf, d32 = (int)d;
-            for (int i0 = 0; i0 < nq; i0 += 128) {
-                bool hit[4];
+            for (int i0 = 0; i0 < nq; i0 += 32 * kTestU) {
+                bool hit[kTestU];
                 if (simple) {
-                    // the four entries' first buckets are read together; a full bucket without
+                    // the entries' first buckets are read together; a full bucket without
                     // the entry (rare at the frontier's load) continues the probe
-                    int32_t v[4];
-                    int4 hb[4];
+                    int32_t v[kTestU];
+                    int4 hb[kTestU];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
+                    for (int u = 0; u < kTestU; ++u) {
                         const int q = i0 + 32 * u + lane;
                         v[u] = stg[q < nq ? q : 0];
                         hb[u] = *reinterpret_cast<const int4*>(B.H + hslot_of(v[u], B.hbits));
                     }
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
+                    for (int u = 0; u < kTestU; ++u) {
                         const bool in = i0 + 32 * u + lane < nq;
                         hit[u] = in && bucket_has(hb[u], v[u]);
                         if (in && !hit[u] && hb[u].w != -1) hit[u] = hash_contains(B.H, B.hbits, v[u]);
                     }
                 } else {
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
+                    for (int u = 0; u < kTestU; ++u) {
                         const int q = i0 + 32 * u + lane;
                         hit[u] = false;
                         if (q < nq) {  // stale entries may hold any value: only node ids reach the masks
@@ -509,7 +549,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                     }
                 }
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
+                for (int u = 0; u < kTestU; ++u) {
                     unsigned hm = __ballot_sync(kFull, hit[u]);
                     while (hm) {
                         const int qh = i0 + 32 * u + __ffs(hm) - 1;
