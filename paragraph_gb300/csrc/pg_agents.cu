@@ -408,6 +408,17 @@ __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
         A.fit[slot] = lognormal_fitness(A.seed, (uint32_t)(r + A.rep_base), ep, (uint32_t)al);
     }
     A.indeg[slot] = 0;
+    if (!rc && A.sampler == kSamplerThinning && rp.p_global < 1.0) {
+        // flag the hubs among this agent's anchors (the same draw the agent kernel makes): their
+        // hub-pair rows are the only ones read
+        const u32x4 xa = draw(A.seed, kStreamAnchor, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, 0);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (i >= rp.anchors) break;
+            const int hs = A.hslot[rp.nbase + bounded32(xa.x[i], (uint32_t)rp.n)];
+            if (hs >= 0) atomicOr(&A.hub_need[(int64_t)r * (kHeavyMax / 32) + (hs >> 5)], 1u << (hs & 31));
+        }
+    }
     if (A.anchors_out) {
         // the same draw the agent kernels make for the neighbourhood (recorded for traces)
         const u32x4 xa = draw(A.seed, kStreamAnchor, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, 0);

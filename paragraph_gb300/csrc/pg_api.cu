@@ -96,6 +96,7 @@ struct pg_ctx {
     DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, e_dst, e_rank, arrivals, hlist, anchors, tile_row;
     DBuf<int16_t> hslot;
     DBuf<uint64_t> hub2;
+    DBuf<uint32_t> hub_need;
     DBuf<uint64_t> hmask;
     DBuf<float> fit, w;
     DBuf<uint64_t> cdf, tilesum, tileoff, tables;
@@ -223,6 +224,7 @@ Arena make_arena(pg_ctx* c) {
     A.hslot = c->hslot.p;
     A.hmask = c->hmask.p;
     A.hub2 = c->hub2.p;
+    A.hub_need = c->hub_need.p;
     A.hlist = c->hlist.p;
     A.sampler = c->cfg.sampler;
     A.tune_agent_ctas = c->tune.agent_ctas_per_sm;
@@ -474,6 +476,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->hslot, S));
     PG_CUDA(c, dalloc(c->hmask, S * kMaskWords));
     PG_CUDA(c, dalloc(c->hub2, (int64_t)R * kHeavyMax * kMaskWords));
+    PG_CUDA(c, dalloc(c->hub_need, (int64_t)R * (kHeavyMax / 32)));
     PG_CUDA(c, dalloc(c->hlist, (int64_t)R * kHeavyMax));
     if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
         PG_CUDA(c, dalloc(c->rc_pa, S));
@@ -720,6 +723,10 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
     if (events) record_event(ev[1], s);
     launch_agent_setup(A, agents, s);
     PG_STAGE("agent setup");
+    if (c->cfg.sampler == PG_SAMPLER_THINNING) {
+        launch_hub_pairs(A, s);  // for the hubs the setup found among the anchors
+        PG_STAGE("hub pairs");
+    }
     if (events) record_event(ev[2], s);
     launch_agents(A, agents, c->num_sms, s);
     PG_STAGE("agents");
@@ -938,6 +945,7 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->hslot);
     dfree(c->hmask);
     dfree(c->hub2);
+    dfree(c->hub_need);
     dfree(c->rep);
     dfree(c->st);
     for (int i = 0; i < 6; ++i)

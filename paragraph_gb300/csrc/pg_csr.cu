@@ -53,9 +53,9 @@ __global__ void __launch_bounds__(kTileThreads) k_bwd_len(Arena A) {
                 A.indeg[slot] += ic;
                 A.inc[slot] = 0;
                 if (ic >= 2) {
-                    if (ic <= kSortSmall) {
+                    if (ic <= kSortMid) {
                         const unsigned long long q = atomicAdd(&A.st->sort_small_count, 1ull);
-                        A.sort_small[q] = (slot << 8) | (int64_t)ic;
+                        A.sort_small[q] = (slot << 9) | (int64_t)ic;
                     } else {
                         const unsigned long long q = atomicAdd(&A.st->sort_large_count, 1ull);
                         A.sort_large[q] = slot;
@@ -215,7 +215,52 @@ __device__ __forceinline__ void seg_bounds(const Arena& A, int64_t slot, const R
     len = on[v + 1] - on[v] - old;
 }
 
-// Rows with 2..32 appended entries: one warp, register bitonic network.
+// Bitonic network over R registers per lane: element i of lane l has index 32 i + l; partners
+// 32 or more apart sit in the same lane (register compare), nearer ones in another lane (shuffle).
+template <int R>
+__device__ __forceinline__ void warp_bitonic(int (&v)[R], int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    const int ip = i ^ (j >> 5);
+                    if (ip > i) {
+                        const bool up = ((i * 32 + lane) & k) == 0;
+                        const int a = v[i], b = v[ip];
+                        const bool sw = (a > b) == up;
+                        v[i] = sw ? b : a;
+                        v[ip] = sw ? a : b;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    const int o = __shfl_xor_sync(kFullMask, v[i], j);
+                    const bool up = ((i * 32 + lane) & k) == 0;
+                    const bool lower = (lane & j) == 0;
+                    v[i] = (lower == up) ? min(v[i], o) : max(v[i], o);
+                }
+            }
+        }
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void warp_sort_segment(int32_t* seg, int64_t len, int lane) {
+    int v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = i * 32 + lane < len ? seg[i * 32 + lane] : 0x7fffffff;
+    warp_bitonic<R>(v, lane);
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+        if (i * 32 + lane < len) seg[i * 32 + lane] = v[i];
+}
+
+// Rows with 2..kSortMid appended entries: one warp, bitonic network in registers (1, 2, 4 or 8
+// entries per lane).
 __global__ void __launch_bounds__(256) k_sort_small(Arena A) {
     if (A.st->error) return;
     const int lane = lane_id();
@@ -223,27 +268,23 @@ __global__ void __launch_bounds__(256) k_sort_small(Arena A) {
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t cnt = (int64_t)A.st->sort_small_count;
     for (int64_t i = warp; i < cnt; i += nwarps) {
-        const int64_t slot = A.sort_small[i] >> 8;
+        const int64_t slot = A.sort_small[i] >> 9;
         const Replica* rp;
         int64_t start, len;
         seg_bounds(A, slot, rp, start, len);
         int32_t* seg = A.bwd_col_nxt + start;
-        int v = lane < len ? seg[lane] : 0x7fffffff;
-#pragma unroll
-        for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                const int o = __shfl_xor_sync(kFullMask, v, j);
-                const bool up = (lane & k) == 0;
-                const bool lower = (lane & j) == 0;
-                v = (lower == up) ? min(v, o) : max(v, o);
-            }
-        }
-        if (lane < len) seg[lane] = v;
+        if (len <= 32)
+            warp_sort_segment<1>(seg, len, lane);
+        else if (len <= 64)
+            warp_sort_segment<2>(seg, len, lane);
+        else if (len <= 128)
+            warp_sort_segment<4>(seg, len, lane);
+        else
+            warp_sort_segment<8>(seg, len, lane);
     }
 }
 
-// Rows with more than 32 appended entries: one CTA, shared bitmap over [n, n + delta).
+// Rows with more than kSortMid appended entries: one CTA, shared bitmap over [n, n + delta).
 __global__ void __launch_bounds__(1024) k_sort_large(Arena A) {
     extern __shared__ uint32_t bm[];
     __shared__ int64_t sw[33];

@@ -22,7 +22,7 @@ constexpr int kKMax = 256;           // PG_MAX_OUT_DEGREE
 constexpr int kTableEntries = kKMax + 1;
 constexpr int kAgentWarps = 4;       // warps per CTA in the agent kernel
 constexpr int kErChunk = 65536;      // ids per ER Philox stream
-constexpr int kSortSmall = 32;       // appended segments up to this length sort in one warp
+constexpr int kSortMid = 256;        // appended segments up to this length sort in one warp's registers
 constexpr int kBitmapWords = 40960;  // 160 KiB of shared bitmap in the large-segment sort
 #define PG_MAX_ANCHORS_DEV 4
 constexpr int kZCap = 1024;          // 1-hop frontier entries kept in shared memory per warp
@@ -156,6 +156,7 @@ struct Arena {
     int16_t* hslot;            // [slots] hub bit of the node or -1
     uint64_t* hmask;           // [slots][kMaskWords] bit b set when hub b is adjacent to the node
     uint64_t* hub2;            // [R][kHeavyMax][kMaskWords] hubs sharing a neighbour with hub b
+    uint32_t* hub_need;        // [R][kHeavyMax / 32] hubs some agent of the epoch has as anchor
     int32_t* hlist;            // [R][kHeavyMax] hub node ids
     // refcompat functor (null unless the context uses PG_WEIGHTS_REFCOMPAT)
     double* rc_pa;             // [slots] score components of the epoch
@@ -273,6 +274,7 @@ void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t
 void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cudaStream_t s);
 void launch_weights(const Arena& A, cudaStream_t s);
 void launch_hubs(const Arena& A, int num_sms, cudaStream_t s);
+void launch_hub_pairs(const Arena& A, cudaStream_t s);
 void launch_guide(const Arena& A, cudaStream_t s);
 void launch_tile_scan(const Arena& A, int mode, cudaStream_t s);
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s);

@@ -339,9 +339,10 @@ __global__ void k_hub_pick(Arena A) {
         rp.heavy_thr = thr;
         rp.heavy_count = 0;
     }
-    // hub-pair masks are OR-accumulated by k_hub_pairs
+    // hub-pair masks are OR-accumulated by k_hub_pairs, for the hubs the agent setup flags
     const int64_t words = (int64_t)A.R * kHeavyMax * kMaskWords;
     for (int64_t i = threadIdx.x; i < words; i += blockDim.x) A.hub2[i] = 0;
+    for (int64_t i = threadIdx.x; i < (int64_t)A.R * (kHeavyMax / 32); i += blockDim.x) A.hub_need[i] = 0u;
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_hub_collect(Arena A) {
@@ -392,6 +393,8 @@ __global__ void __launch_bounds__(256) k_hub_pairs(Arena A, int G) {
     const int r = item / kHeavyMax, b = item % kHeavyMax;
     const Replica& rp = A.rep[r];
     if (b >= rp.heavy_count || b >= kHeavyMax) return;
+    // only an agent whose anchor is hub b reads its row
+    if (!((A.hub_need[(int64_t)r * (kHeavyMax / 32) + (b >> 5)] >> (b & 31)) & 1u)) return;
     if (threadIdx.x < kMaskWords) acc[threadIdx.x] = 0;
     __syncthreads();
     const int64_t h = A.hlist[(int64_t)r * kHeavyMax + b];
@@ -427,6 +430,10 @@ void launch_hubs(const Arena& A, int num_sms, cudaStream_t s) {
     k_hub_pick<<<1, 256, 0, s>>>(A);
     k_hub_collect<<<A.ntiles, kTileThreads, 0, s>>>(A);
     k_hub_mask<<<(unsigned)(A.R * kHeavyMax * G), 256, 0, s>>>(A, G);
+}
+
+void launch_hub_pairs(const Arena& A, cudaStream_t s) {
+    const int G = A.R >= 64 ? 1 : 64 / A.R;
     k_hub_pairs<<<(unsigned)(A.R * kHeavyMax * G), 256, 0, s>>>(A, G);
 }
 
