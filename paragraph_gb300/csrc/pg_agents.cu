@@ -117,46 +117,47 @@ __device__ __forceinline__ void boost_key(const AgentCtx& C, bool valid, int z, 
     }
 }
 
+// The agent's targets sorted (bitonic network in registers, R entries per lane), written to its
+// forward row and the edge list, and counted into the in-degree increments.
+template <int R>
+__device__ __forceinline__ void emit_sorted(const Arena& A, const Replica& rp, int64_t e0, int64_t row0,
+                                            const int32_t* arr, int taken, int lane) {
+    int v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = i * 32 + lane < taken ? arr[i * 32 + lane] : 0x7fffffff;
+    warp_bitonic<R>(v, lane);
+    int32_t* fcol = A.fwd_col + rp.ebase;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int q = i * 32 + lane;
+        if (q < taken) {
+            const int d = v[i];
+            fcol[row0 + q] = d;
+            A.e_dst[e0 + q] = d;
+            A.e_rank[e0 + q] = atomicAdd(&A.inc[rp.nbase + d], 1);
+        }
+    }
+}
+
 // Append one agent's citations: arrival order to the trace, the sorted row to the forward CSR and
 // the epoch edge list, one in-degree increment (whose old value is the edge's rank in the cited
 // node's new backward entries) per citation, and the byte-model counters.
 template <int KCAP>
 __device__ void emit_row(const Arena& A, const Replica& rp, int64_t a, int64_t al, int64_t n,
-                         const int32_t* arr, int32_t* out, int taken, long long rows,
-                         long long elems, long long draws) {
+                         const int32_t* arr, int taken, long long rows, long long elems, long long draws) {
     const int lane = lane_id();
     const int64_t e0 = A.eoff[a];
-    int P = 1;
-    while (P < taken) P <<= 1;
-    for (int q = lane; q < P; q += 32) {
-        const int v = q < taken ? arr[q] : 0x7fffffff;
-        if (A.arrivals && q < taken) A.arrivals[e0 + q] = v;
-        out[q] = v;
-    }
-    __syncwarp();
-    for (int kk = 2; kk <= P; kk <<= 1) {
-        for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-            for (int q = lane; q < P; q += 32) {
-                const int qx = q ^ jj;
-                if (qx > q) {
-                    const int va = out[q], vb = out[qx];
-                    if ((va > vb) == ((q & kk) == 0)) {
-                        out[q] = vb;
-                        out[qx] = va;
-                    }
-                }
-            }
-            __syncwarp();
-        }
-    }
+    if (A.arrivals)
+        for (int q = lane; q < taken; q += 32) A.arrivals[e0 + q] = arr[q];
     const int64_t row0 = rp.m + (e0 - A.eoff[rp.abase]);
-    int32_t* fcol = A.fwd_col + rp.ebase;
-    for (int q = lane; q < taken; q += 32) {
-        const int d = out[q];
-        fcol[row0 + q] = d;
-        A.e_dst[e0 + q] = d;
-        A.e_rank[e0 + q] = atomicAdd(&A.inc[rp.nbase + d], 1);
-    }
+    if (taken <= 32)
+        emit_sorted<1>(A, rp, e0, row0, arr, taken, lane);
+    else if (KCAP <= 64 || taken <= 64)
+        emit_sorted<2>(A, rp, e0, row0, arr, taken, lane);
+    else if (KCAP <= 128 || taken <= 128)
+        emit_sorted<4>(A, rp, e0, row0, arr, taken, lane);
+    else
+        emit_sorted<8>(A, rp, e0, row0, arr, taken, lane);
     if (lane == 0) {
         A.fwd_off[rp.obase + n + al + 1] = row0 + taken;
         atomicAdd(&A.st->rows_expanded, (unsigned long long)rows);
@@ -362,7 +363,7 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
         }
     }
     if (taken != k && lane == 0) atomicOr(&A.st->error, kErrArg);
-    emit_row<KCAP>(A, rp, a, al, n, S.out, S.bi, taken, rows, elems, ng);
+    emit_row<KCAP>(A, rp, a, al, n, S.out, taken, rows, elems, ng);
 }
 
 #include "pg_thin.cuh"

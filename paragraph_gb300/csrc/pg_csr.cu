@@ -116,13 +116,17 @@ __device__ __forceinline__ int64_t row_of(const int64_t* off, int64_t lo, int64_
 // Old backward entries moved to their new positions, in tiles of kCopyTile consecutive positions
 // (not rows), so a hub row with millions of entries is spread over many CTAs.  Reads and writes are
 // coalesced.  The tile's row offsets and per-row shifts (new - old start) are staged in shared
-// memory once, so each position finds its row by a shared-memory binary search; a tile spanning
-// more than kCopyRows rows (long runs of empty rows) searches the global offsets instead.
+// memory once, with the row holding the first position of every 32-position block, so each
+// position searches only the rows between its block's row and the next block's (usually one or
+// two); a tile spanning more than kCopyRows rows (long runs of empty rows) searches the global
+// offsets instead.
 constexpr int kCopyRows = 2048;
+constexpr int kCopyBlocks = kCopyTile / 32;
 
 __global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
     __shared__ int64_t s_oc[kCopyRows + 1];  // old offsets of the tile's rows, and the next one
     __shared__ int64_t s_sh[kCopyRows];      // new minus old offset of the tile's rows
+    __shared__ int16_t s_blk[kCopyBlocks];   // row (tile-relative) holding each block's first position
     if (A.st->error) return;
     const int64_t total = (int64_t)A.st->copy_tiles;
     unsigned long long moved = 0;
@@ -157,9 +161,19 @@ __global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
             }
             if (threadIdx.x == 0) s_oc[nr] = oc[r1 + 1];
             __syncthreads();
+            // block b starts at p0 + 32 b; the non-empty row holding it marks it
+            for (int64_t i = threadIdx.x; i < nr; i += blockDim.x) {
+                const int64_t a = s_oc[i] - p0, e = s_oc[i + 1] - p0;
+                int64_t b0 = a > 0 ? (a + 31) >> 5 : 0;
+                const int64_t b1 = e > 0 ? ((e - 1) >> 5) : -1;
+                for (; b0 <= b1 && b0 < kCopyBlocks; ++b0) s_blk[b0] = (int16_t)i;
+            }
+            __syncthreads();
             const int last = (int)nr - 1;
+            const int nblk = (int)((p1 - p0 + 31) >> 5);
             for (int64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-                int l = 0, h = last;
+                const int b = (int)((p - p0) >> 5);
+                int l = s_blk[b], h = b + 1 < nblk ? s_blk[b + 1] : last;
                 while (l < h) {
                     const int mid = (l + h + 1) >> 1;
                     if (s_oc[mid] <= p)
@@ -213,39 +227,6 @@ __device__ __forceinline__ void seg_bounds(const Arena& A, int64_t slot, const R
     const int64_t old = v < rp.n ? oc[v + 1] - oc[v] : 0;
     start = rp.ebase + on[v] + old;
     len = on[v + 1] - on[v] - old;
-}
-
-// Bitonic network over R registers per lane: element i of lane l has index 32 i + l; partners
-// 32 or more apart sit in the same lane (register compare), nearer ones in another lane (shuffle).
-template <int R>
-__device__ __forceinline__ void warp_bitonic(int (&v)[R], int lane) {
-#pragma unroll
-    for (int k = 2; k <= 32 * R; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            if (j >= 32) {
-#pragma unroll
-                for (int i = 0; i < R; ++i) {
-                    const int ip = i ^ (j >> 5);
-                    if (ip > i) {
-                        const bool up = ((i * 32 + lane) & k) == 0;
-                        const int a = v[i], b = v[ip];
-                        const bool sw = (a > b) == up;
-                        v[i] = sw ? b : a;
-                        v[ip] = sw ? a : b;
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < R; ++i) {
-                    const int o = __shfl_xor_sync(kFullMask, v[i], j);
-                    const bool up = ((i * 32 + lane) & k) == 0;
-                    const bool lower = (lane & j) == 0;
-                    v[i] = (lower == up) ? min(v[i], o) : max(v[i], o);
-                }
-            }
-        }
-    }
 }
 
 template <int R>

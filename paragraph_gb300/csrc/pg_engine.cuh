@@ -229,6 +229,39 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// Bitonic network over R registers per lane: element i of lane l has index 32 i + l; partners
+// 32 or more apart sit in the same lane (register compare), nearer ones in another lane (shuffle).
+template <int R>
+__device__ __forceinline__ void warp_bitonic(int (&v)[R], int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    const int ip = i ^ (j >> 5);
+                    if (ip > i) {
+                        const bool up = ((i * 32 + lane) & k) == 0;
+                        const int a = v[i], b = v[ip];
+                        const bool sw = (a > b) == up;
+                        v[i] = sw ? b : a;
+                        v[ip] = sw ? a : b;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    const int o = __shfl_xor_sync(0xffffffffu, v[i], j);
+                    const bool up = ((i * 32 + lane) & k) == 0;
+                    const bool lower = (lane & j) == 0;
+                    v[i] = (lower == up) ? min(v[i], o) : max(v[i], o);
+                }
+            }
+        }
+    }
+}
+
 // Block-wide exclusive scan of one value per thread (blockDim.x <= 1024, multiple of 32).
 template <typename T>
 __device__ __forceinline__ T block_excl_scan(T v, T* smem_warp, T* total) {

@@ -186,5 +186,5 @@ __device__ void process_agent_rc(const Arena& A, int64_t a, int k, RcSmem& S) {
         o[4] = (double)gen;
         o[5] = (double)k;
     }
-    emit_row<kKMax>(A, rp, a, al, n, S.arr, S.out, c < k ? c : k, rows, elems, draws);
+    emit_row<kKMax>(A, rp, a, al, n, S.arr, c < k ? c : k, rows, elems, draws);
 }

@@ -40,7 +40,6 @@ struct ThinSmem {
     __align__(16) int32_t stage[2][STAGE];  // candidate rows, two buffers filled by bulk copies
     int32_t H[HCAP];  // frontier hash set, -1 = empty
     int32_t arr[KCAP];
-    int32_t out[KCAP];
     int32_t c_id[KCAP];
     uint64_t c_cq[KCAP];
     BallAux aux;
@@ -698,6 +697,6 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     }
     if (nch != k && lane == 0) atomicOr(&A.st->error, kErrArg);
     if (lane == 0 && scanned) atomicAdd(&A.st->adj_scanned, (unsigned long long)scanned);
-    emit_row<KCAP>(A, rp, a, al, n, S.arr, S.out, nch, rows, tests, events);
+    emit_row<KCAP>(A, rp, a, al, n, S.arr, nch, rows, tests, events);
     return true;
 }
