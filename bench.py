@@ -679,6 +679,10 @@ def run_small_configs(args) -> None:
                 # reload the seed (untimed), then the 10 epochs between device events
                 eng.load_graph(g.pub, g.fitness, g.src, g.dst, PAParams(fixed_new_nodes=10_000),
                                planned_epochs=1)
+                # room for the 10 epochs' expected edges (1.45e10 p in all) with an 8-sigma margin
+                n0, m0 = eng.counts()
+                mu = [10_000 * (n0 + 10_000 * t) * p for t in range(10)]
+                eng.reserve(n0 + 100_000, int(m0 + sum(x + 8 * x ** 0.5 + 1024 for x in mu)))
                 eng.sync()
                 eng.timer_start()
                 e = sum(eng.er_epoch(10_000, p) for _ in range(10))

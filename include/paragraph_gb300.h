@@ -180,6 +180,10 @@ pg_status pg_run_epochs(pg_ctx* ctx, int32_t num_epochs, int32_t use_graph, int6
 /* One Erdos-Renyi G(n,p) epoch on replica 0: delta new nodes, each linking to every pre-epoch node
  * with probability p, by geometric skips. */
 pg_status pg_er_epoch(pg_ctx* ctx, int64_t delta, double p, int64_t* new_edges);
+/* Grow a single-replica context to hold at least n_cap nodes and m_cap citations before its
+ * epochs run (ER epochs, whose edge count a PA plan does not cover, otherwise grow the arena
+ * through the host when they outrun it).  No-op when the capacity suffices. */
+pg_status pg_reserve(pg_ctx* ctx, int64_t n_cap, int64_t m_cap);
 
 /* ---- refcompat functor: ParAGraph's own per-paper model (the abm driver's options) ---- */
 typedef struct {

@@ -33,7 +33,7 @@ MAX_OUT_DEGREE = 256
 EXPORTED = [
     "pg_create", "pg_destroy", "pg_last_error", "pg_status_string", "pg_load_graph",
     "pg_load_replicas", "pg_set_params", "pg_default_params", "pg_set_epoch", "pg_grow_epoch",
-    "pg_run_epochs", "pg_er_epoch", "pg_get_counts", "pg_epoch_edges", "pg_copy_edges",
+    "pg_run_epochs", "pg_er_epoch", "pg_reserve", "pg_get_counts", "pg_epoch_edges", "pg_copy_edges",
     "pg_copy_degrees", "pg_copy_nodes", "pg_copy_csr", "pg_copy_arrivals", "pg_set_timing",
     "pg_get_stats", "pg_sync", "pg_check_device", "pg_philox4x32_10", "pg_poisson_table",
     "pg_logf_host", "pg_expf_host", "pg_log_host", "pg_exp_host", "pg_version",
@@ -211,6 +211,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_grow_epoch": (i32, [vp, P(i64), P(i64)]),
         "pg_run_epochs": (i32, [vp, i32, i32, P(i64)]),
         "pg_er_epoch": (i32, [vp, i64, C.c_double, P(i64)]),
+        "pg_reserve": (i32, [vp, i64, i64]),
         "pg_get_counts": (i32, [vp, i32, P(i64), P(i64)]),
         "pg_epoch_edges": (i32, [vp, i32, P(i64), P(i64)]),
         "pg_copy_edges": (i32, [vp, i32, i64, i64, vp, vp]),
@@ -410,6 +411,10 @@ class GrowthEngine:
         ne = C.c_int64()
         self._check(self._lib.pg_er_epoch(self._ctx, delta, p, C.byref(ne)))
         return ne.value
+
+    def reserve(self, n_cap: int, m_cap: int) -> None:
+        """Grow a single-replica context to n_cap nodes and m_cap citations ahead of its epochs."""
+        self._check(self._lib.pg_reserve(self._ctx, int(n_cap), int(m_cap)))
 
     # ------------------------------------------------------------------ output
     def counts(self, replica: int = 0) -> tuple[int, int]:

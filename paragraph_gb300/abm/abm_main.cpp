@@ -389,6 +389,23 @@ int run(int argc, char** argv) {
     if (o.has("--epoch-log")) elog.open(o.str("--epoch-log"));
     log.info("start year " + std::to_string(start_year) + ", " + std::to_string(cycles) + " cycles, model " +
              (er ? std::string("er-gnp") : wm));
+    if (er) {
+        // size the arena for every cycle up front: a PA plan does not cover ER edge counts, and an
+        // arena outgrown mid-run is rebuilt through the host
+        int64_t n = 0, m = 0;
+        pg_get_counts(ctx, 0, &n, &m);
+        double nf = (double)n, mf = (double)m;
+        for (int cyc = 0; cyc < cycles; ++cyc) {
+            const double nn = std::ceil(nf * growth);
+            double p = o.num("--er-probability", -1.0);
+            if (o.has("--er-edges-per-node")) p = o.num("--er-edges-per-node", 0.0) / nf;
+            p = std::min(std::max(p, 0.0), 1.0);
+            const double mu = nn * nf * p;
+            mf += mu + 8.0 * std::sqrt(mu) + 1024.0;
+            nf += nn;
+        }
+        PG_TRY(ctx, pg_reserve(ctx, (int64_t)nf, (int64_t)mf));
+    }
     const auto t_run = std::chrono::steady_clock::now();
     int64_t total_edges = 0;
     for (int cyc = 0; cyc < cycles; ++cyc) {

@@ -394,6 +394,9 @@ void destroy_graph_exec(pg_ctx* c) {
 pg_status alloc_epoch_buffers(pg_ctx* c, int64_t agent_cap, int64_t edge_cap, int64_t tasks) {
     const int64_t scan_n = std::max<int64_t>(std::max<int64_t>(agent_cap, tasks), 1);
     const int64_t blocks = scan_blocks_needed(scan_n) + 2;
+    // buffers that must grow grow by half again, so a run of growing epochs reallocates rarely
+    if (agent_cap > c->agent_cap) agent_cap = std::max<int64_t>(agent_cap, c->agent_cap + c->agent_cap / 2);
+    if (edge_cap > c->edge_cap) edge_cap = std::max<int64_t>(edge_cap, c->edge_cap + c->edge_cap / 2);
     if (agent_cap > c->agent_cap) {
         PG_CUDA(c, dalloc(c->kk, agent_cap));
         PG_CUDA(c, dalloc(c->big_list, agent_cap));
@@ -1300,6 +1303,16 @@ pg_status pg_er_epoch(pg_ctx* c, int64_t delta, double p, int64_t* new_edges) {
     }
     if (new_edges) *new_edges = c->stats.new_edges;
     return PG_OK;
+}
+
+pg_status pg_reserve(pg_ctx* c, int64_t n_cap, int64_t m_cap) {
+    if (!c) return PG_ERR_ARG;
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (c->R != 1) return fail(c, PG_ERR_ARG, "capacity reservations apply to single-replica contexts");
+    if (c->poisoned) return fail(c, PG_ERR_STATE, "an earlier epoch failed on the device; reload the graph");
+    if (n_cap < 0 || m_cap < 0) return fail(c, PG_ERR_ARG, "negative capacity");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    return ensure_capacity(c, n_cap, m_cap);
 }
 
 pg_status pg_get_counts(const pg_ctx* c, int32_t replica, int64_t* n, int64_t* m) {

@@ -85,7 +85,9 @@ def test_plain_pa_config_bit_exact(gpu, sampler):
         _compare_state(eng, og)
 
 
-@pytest.mark.parametrize("p", [1e-5, 1e-4, 1e-3, 0.0, 1.0])
+# at n0 = 20,000 these p give 0.2 .. 20 expected successes per chunk: every lane-group width of
+# the walk (1, 2, 4, 8, 16, 32 lanes per task) is exercised
+@pytest.mark.parametrize("p", [1e-5, 1e-4, 2e-4, 4e-4, 7e-4, 1e-3, 0.0, 1.0])
 def test_er_bit_exact(gpu, p):
     n0, delta = (20_000, 2000) if p < 1.0 else (3000, 50)
     s = W.er_seed(n0)
@@ -100,6 +102,24 @@ def test_er_bit_exact(gpu, p):
         _compare_state(eng, og)
         if p == 1.0:
             assert og.m == delta * n0 + delta * (n0 + delta)
+
+
+def test_er_reserve_keeps_results(gpu):
+    """Capacity reserved up front (no arena growth between epochs) changes no edge."""
+    s = W.er_seed(20_000)
+    runs = []
+    for reserve in (False, True):
+        with GrowthEngine(seed=7) as eng:
+            eng.load_graph(s.pub, s.fitness, s.src, s.dst)
+            n0, m0 = eng.counts()
+            if reserve:
+                eng.reserve(n0 + 3 * 2000, m0 + 3 * 2000 * 26_000)
+                eng.reserve(10, 10)  # already large enough: no-op
+            for _ in range(3):
+                eng.er_epoch(2000, 1e-3)
+            runs.append(eng.csr(0))
+    np.testing.assert_array_equal(runs[0][0], runs[1][0])
+    np.testing.assert_array_equal(runs[0][1], runs[1][1])
 
 
 def test_run_epochs_graph_matches_sequential(gpu):
