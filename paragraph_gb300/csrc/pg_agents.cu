@@ -409,17 +409,33 @@ __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
         A.fit[slot] = lognormal_fitness(A.seed, (uint32_t)(r + A.rep_base), ep, (uint32_t)al);
     }
     A.indeg[slot] = 0;
+    int heavy = 0;
     if (!rc && A.sampler == kSamplerThinning && rp.p_global < 1.0) {
-        // flag the hubs among this agent's anchors (the same draw the agent kernel makes): their
-        // hub-pair rows are the only ones read
+        // the anchors (the same draw the agent kernel makes): flag the hubs among them, whose
+        // hub-pair rows are the only ones read, and mark the agent heavy when an anchor is a hub or
+        // the anchors' rows would not all fit the smaller shared frontier (the agent then tests
+        // memberships against global rows); heavy agents are taken first, so none starts late
         const u32x4 xa = draw(A.seed, kStreamAnchor, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, 0);
+        const int64_t* fo = A.fwd_off + rp.obase;
+        const int64_t* bo = A.bwd_off_cur + rp.obase;
+        int64_t zsize = rp.anchors;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             if (i >= rp.anchors) break;
-            const int hs = A.hslot[rp.nbase + bounded32(xa.x[i], (uint32_t)rp.n)];
-            if (hs >= 0) atomicOr(&A.hub_need[(int64_t)r * (kHeavyMax / 32) + (hs >> 5)], 1u << (hs & 31));
+            const int64_t x = bounded32(xa.x[i], (uint32_t)rp.n);
+            const int hs = A.hslot[rp.nbase + x];
+            if (hs >= 0) {
+                atomicOr(&A.hub_need[(int64_t)r * (kHeavyMax / 32) + (hs >> 5)], 1u << (hs & 31));
+                heavy = 1;
+            } else {
+                zsize += (fo[x + 1] - fo[x]) + (bo[x + 1] - bo[x]);
+            }
         }
+        if (zsize > kZCap / 2) heavy = 1;
+        if (k > kKSmall) heavy = 0;  // the k <= 256 kernel has its own list
+        if (heavy) A.heavy_list[atomicAdd(&A.st->heavy_count, 1ull)] = (int32_t)a;
     }
+    A.heavy_mark[a] = heavy;
     if (A.anchors_out) {
         // the same draw the agent kernels make for the neighbourhood (recorded for traces)
         const u32x4 xa = draw(A.seed, kStreamAnchor, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, 0);
@@ -476,7 +492,10 @@ __global__ void __launch_bounds__(kAgentWarps * 32, 4) k_agents(Arena A, int64_t
     if (A.st->error) return;
     Smem& S = smem[threadIdx.x >> 5];
     const int lane = lane_id();
-    const int64_t limit = BIG ? (int64_t)A.st->big_count : agents;
+    // the small thinning kernel walks the heavy list, then every agent not on it
+    constexpr bool kHeavyFirst = THIN && !BIG;
+    const int64_t hc = kHeavyFirst ? (int64_t)A.st->heavy_count : 0;
+    const int64_t limit = BIG ? (int64_t)A.st->big_count : agents + hc;
     uint32_t phase = 0;
     if constexpr (THIN) {
         if (lane == 0) {
@@ -492,7 +511,15 @@ __global__ void __launch_bounds__(kAgentWarps * 32, 4) k_agents(Arena A, int64_t
             q = (long long)atomicAdd(BIG ? &A.st->queue_big : &A.st->queue_small, 1ull);
         q = __shfl_sync(kFull, q, 0);
         if (q >= limit) break;
-        const int64_t a = BIG ? (int64_t)A.big_list[q] : q;
+        int64_t a;
+        if (BIG)
+            a = (int64_t)A.big_list[q];
+        else if (q < hc)
+            a = (int64_t)A.heavy_list[q];
+        else {
+            a = q - hc;
+            if (kHeavyFirst && A.heavy_mark[a]) continue;
+        }
         const int k = A.kk[a];
         if (!BIG && k > KCAP) continue;
         if constexpr (THIN) {

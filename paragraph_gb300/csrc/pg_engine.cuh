@@ -94,6 +94,7 @@ struct EpochState {
     unsigned long long queue_small;
     unsigned long long queue_big;
     unsigned long long big_count;
+    unsigned long long heavy_count;  // agents the small thinning kernel takes first
     unsigned long long sort_small_count;
     unsigned long long sort_large_count;
     unsigned long long sort_scratch;
@@ -145,6 +146,8 @@ struct Arena {
     int32_t* arrivals;         // [edge cap] or null
     int32_t* anchors_out;      // [agent cap][4] anchors of each agent, or null (record_trace)
     int32_t* big_list;         // [agent cap]
+    int32_t* heavy_list;       // [agent cap] agents with a hub or a large frontier (k <= kKSmall)
+    int32_t* heavy_mark;       // [agent cap] 1 when the agent is on heavy_list
     int32_t* tile_row;         // [copy tiles] row holding the first position of each copy tile
     int64_t* len_tmp;          // [slots]
     uint64_t* tilesum;         // [ntiles]
