@@ -104,6 +104,50 @@ def test_er_bit_exact(gpu, p):
             assert og.m == delta * n0 + delta * (n0 + delta)
 
 
+def _popular_seed(n: int, popular: int, lo: int, hi: int, seed: int) -> W.SeedGraph:
+    """Sparse background (4 random citations per node) plus `popular` nodes cited by lo..hi
+    random others: more than 256 nodes with rows longer than the shared frontier, so many are
+    not hubs."""
+    rng = np.random.default_rng(seed)
+    src = [rng.integers(0, n, size=4 * n)]
+    dst = [rng.integers(0, n, size=4 * n)]
+    for v, d in zip(rng.choice(n, popular, replace=False), rng.integers(lo, hi, size=popular)):
+        src.append(rng.integers(0, n, size=d))
+        dst.append(np.full(d, v))
+    src, dst = np.concatenate(src), np.concatenate(dst)
+    keep = src != dst
+    return W.SeedGraph(rng.integers(-5, 0, size=n).astype(np.int32),
+                       rng.lognormal(0.0, 1.0, size=n).astype(np.float32),
+                       src[keep].astype(np.int32), dst[keep].astype(np.int32))
+
+
+@pytest.mark.parametrize("small_hash", [0, 1])
+def test_large_anchor_rows_bit_exact(gpu, small_hash):
+    """Agents whose anchors' rows overflow the shared frontier (1,024 entries, 512 with the small
+    hash): membership in those rows is a binary search of the CSR rows; such agents are also the
+    ones the setup lists first."""
+    g = _popular_seed(6000, 2000, 1000, 3000, seed=5)
+    prm = PAParams(alpha=1.0, tau=5.0, gamma=1.0, beta=4.0, mean_out_degree=20.0,
+                   growth_rate=0.0, fixed_new_nodes=300, num_anchors=3)
+    with GrowthEngine(seed=77, record_trace=True) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=2)
+        eng.set_tuning(small_hash=small_hash)
+        og = _oracle_for(g, prm, 77, sampler=PG_SAMPLER_THINNING)
+        over = 0
+        for _ in range(2):
+            ind, outd = eng.degrees()
+            deg = ind.astype(np.int64) + outd
+            eng.grow_epoch()
+            og.pa_epoch()
+            anc = eng.anchors()[:, :3]
+            over += int((deg[anc].sum(axis=1) > 1024).sum())
+            st, so = eng.stats(), og.stats()
+            assert st["adj_scanned"] == so["adj_scanned"]
+            np.testing.assert_array_equal(eng.arrivals(), og.arrivals())
+            _compare_state(eng, og)
+        assert over > 0  # some agents' anchor rows exceed the shared frontier
+
+
 def test_er_reserve_keeps_results(gpu):
     """Capacity reserved up front (no arena growth between epochs) changes no edge."""
     s = W.er_seed(20_000)
