@@ -182,7 +182,8 @@ pg_status pg_run_epochs(pg_ctx* ctx, int32_t num_epochs, int32_t use_graph, int6
 pg_status pg_er_epoch(pg_ctx* ctx, int64_t delta, double p, int64_t* new_edges);
 /* Grow a single-replica context to hold at least n_cap nodes and m_cap citations before its
  * epochs run (ER epochs, whose edge count a PA plan does not cover, otherwise grow the arena
- * through the host when they outrun it).  No-op when the capacity suffices. */
+ * through the host when they outrun it).  No-op when the capacity suffices; growing the arena
+ * drops a checkpoint and a captured run graph (both refer to the old buffers). */
 pg_status pg_reserve(pg_ctx* ctx, int64_t n_cap, int64_t m_cap);
 
 /* ---- refcompat functor: ParAGraph's own per-paper model (the abm driver's options) ---- */
