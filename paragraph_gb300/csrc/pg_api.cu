@@ -104,6 +104,7 @@ struct pg_ctx {
     DBuf<int64_t> fwd_off, bwd_off[2], len_tmp, sort_small, sort_large, sort_large_off, eoff,
         blocksum, er_cnt, er_toff;
     DBuf<int32_t> fwd_col, bwd_col[2];
+    DBuf<int32_t> src_tmp;  // sources of an edge range being copied out
     // refcompat functor
     DBuf<double> rc_pa, rc_rec, rc_fit, rc_rtab, rc_agent;
     DBuf<int32_t> rc_lag, rc_dur, rc_cnt;
@@ -953,6 +954,7 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->hmask);
     dfree(c->hub2);
     dfree(c->hub_need);
+    dfree(c->src_tmp);
     dfree(c->rep);
     dfree(c->st);
     for (int i = 0; i < 6; ++i)
@@ -1344,16 +1346,12 @@ pg_status pg_copy_edges(pg_ctx* c, int32_t replica, int64_t first, int64_t count
         PG_CUDA(c, cudaMemcpyAsync(dst, c->fwd_col.p + h.ebase + first, 4 * (size_t)count,
                                    cudaMemcpyDeviceToHost, c->stream));
     if (src && count) {
-        // sources from the forward offsets: rows are contiguous in edge order
-        std::vector<int64_t> off((size_t)h.n + 1);
-        PG_CUDA(c, cudaMemcpyAsync(off.data(), c->fwd_off.p + h.obase, 8 * off.size(), cudaMemcpyDeviceToHost, c->stream));
-        PG_CUDA(c, cudaStreamSynchronize(c->stream));
-        int64_t v = std::upper_bound(off.begin(), off.end(), first) - off.begin() - 1;
-        for (int64_t i = 0; i < count; ++i) {
-            const int64_t e = first + i;
-            while (off[(size_t)v + 1] <= e) ++v;
-            src[i] = (int32_t)v;
-        }
+        // sources expanded from the forward offsets on the device (rows are contiguous in edge
+        // order), then one copy
+        if (c->src_tmp.n < count) PG_CUDA(c, dalloc(c->src_tmp, count));
+        launch_edge_sources(c->fwd_off.p + h.obase, h.n, first, count, c->src_tmp.p, c->num_sms, c->stream);
+        PG_CUDA(c, cudaGetLastError());
+        PG_CUDA(c, cudaMemcpyAsync(src, c->src_tmp.p, 4 * (size_t)count, cudaMemcpyDeviceToHost, c->stream));
     }
     PG_CUDA(c, cudaStreamSynchronize(c->stream));
     return PG_OK;

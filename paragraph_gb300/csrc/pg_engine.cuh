@@ -334,6 +334,9 @@ void launch_text_len(const int64_t* fo, const int32_t* fc, int64_t n, int64_t m,
                      int num_sms, cudaStream_t s);
 void launch_text_write(const int64_t* fo, const int32_t* fc, int64_t n, int64_t m, const int64_t* ids,
                        const int64_t* off, char* out, int num_sms, cudaStream_t s);
+// the source of every edge in [first, first + count) of a forward CSR, from its offsets
+void launch_edge_sources(const int64_t* fo, int64_t n, int64_t first, int64_t count, int32_t* out,
+                         int num_sms, cudaStream_t s);
 // device CSR construction from a raw edge list (pg_build.cu)
 size_t build_scratch_bytes(int64_t m, int64_t n);
 void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,

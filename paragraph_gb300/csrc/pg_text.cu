@@ -67,6 +67,28 @@ __global__ void __launch_bounds__(256) k_text_write(const int64_t* fo, const int
     }
 }
 
+// Sources of the edges [first, first + count): one thread per row writes the row's part of the
+// range (rows are contiguous in edge order, so the writes of neighbouring rows are adjacent).
+__global__ void __launch_bounds__(256) k_edge_sources(const int64_t* fo, int64_t n, int64_t first, int64_t count,
+                                                      int32_t* out) {
+    const int64_t last = first + count;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        int64_t p0 = fo[v], p1 = fo[v + 1];
+        if (p1 <= first || p0 >= last) continue;
+        p0 = p0 > first ? p0 : first;
+        p1 = p1 < last ? p1 : last;
+        for (int64_t p = p0; p < p1; ++p) out[p - first] = (int32_t)v;
+    }
+}
+
+void launch_edge_sources(const int64_t* fo, int64_t n, int64_t first, int64_t count, int32_t* out,
+                         int num_sms, cudaStream_t s) {
+    if (count <= 0 || n <= 0) return;
+    int64_t g = (n + 255) / 256;
+    if (g > (int64_t)num_sms * 16) g = (int64_t)num_sms * 16;
+    k_edge_sources<<<(unsigned)g, 256, 0, s>>>(fo, n, first, count, out);
+}
+
 void launch_text_len(const int64_t* fo, const int32_t* fc, int64_t n, int64_t m, const int64_t* ids, int32_t* len,
                      int num_sms, cudaStream_t s) {
     if (m <= 0) return;
