@@ -433,7 +433,7 @@ def run_ensemble(args) -> None:
                 n1, m1 = e2.counts(r)
                 e2.edges(mm0, m1 - mm0, r)
                 h2d += 4 * n0_ * 3 + 8 * (n0_ + 1) * 2 + 4 * mm0 * 2
-                d2h += 4 * (m1 - mm0) + 8 * (n1 + 1)
+                d2h += 8 * (m1 - mm0)  # sources (expanded on the device) and targets
         dt = reduce_max(dist, time.perf_counter() - t0)
         e2e = {"value": reduce_sum(dist, float(len(reps))) / dt, "unit": "evals/s",
                "h2d_bytes_per_step": int(reduce_sum(dist, float(h2d))),
