@@ -153,7 +153,11 @@ __device__ __forceinline__ bool hash_contains(const int32_t* H, int bits, int32_
 
 __device__ __forceinline__ int hub_slot(const Ball& B, int32_t v) { return B.hslot[v]; }
 
-__device__ __forceinline__ bool mask_bit(const Mask& m, int b) { return (m.w[b >> 6] >> (b & 63)) & 1ull; }
+__device__ __forceinline__ bool mask_bit(const Mask& m, int b) {
+    const int w = b >> 6;  // a select, not an indexed load: the mask stays in registers
+    const unsigned long long x = w == 0 ? m.w[0] : (w == 1 ? m.w[1] : (w == 2 ? m.w[2] : m.w[3]));
+    return (x >> (b & 63)) & 1ull;
+}
 
 // v in Z (frontier) -- lane-level, any lane may call it with its own v
 __device__ __forceinline__ bool in_z(const Ball& B, int32_t v) {
@@ -528,13 +532,13 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                     for (int u = 0; u < kTestU; ++u) {
                         const int q = i0 + 32 * u + lane;
                         v[u] = stg[q < nq ? q : 0];
-                        hb[u] = *reinterpret_cast<const int4*>(B.H + hslot_of(v[u], B.hbits));
+                        hb[u] = *reinterpret_cast<const int4*>(S.H + hslot_of(v[u], kHBits));
                     }
 #pragma unroll
                     for (int u = 0; u < kTestU; ++u) {
                         const bool in = i0 + 32 * u + lane < nq;
                         hit[u] = in && bucket_has(hb[u], v[u]);
-                        if (in && !hit[u] && hb[u].w != -1) hit[u] = hash_contains(B.H, B.hbits, v[u]);
+                        if (in && !hit[u] && hb[u].w != -1) hit[u] = hash_contains(S.H, kHBits, v[u]);
                     }
                 } else {
 #pragma unroll
