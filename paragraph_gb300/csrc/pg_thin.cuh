@@ -551,6 +551,11 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                         }
                     }
                 }
+                // hits are rare: one vote skips the per-entry ballots of a step without any
+                bool anyhit = false;
+#pragma unroll
+                for (int u = 0; u < kTestU; ++u) anyhit |= hit[u];
+                if (!__any_sync(kFull, anyhit)) continue;
 #pragma unroll
                 for (int u = 0; u < kTestU; ++u) {
                     unsigned hm = __ballot_sync(kFull, hit[u]);
