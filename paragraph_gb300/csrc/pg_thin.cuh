@@ -534,11 +534,18 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                         v[u] = stg[q < nq ? q : 0];
                         hb[u] = *reinterpret_cast<const int4*>(S.H + hslot_of(v[u], kHBits));
                     }
+                    bool more[kTestU], anymore = false;
 #pragma unroll
                     for (int u = 0; u < kTestU; ++u) {
                         const bool in = i0 + 32 * u + lane < nq;
                         hit[u] = in && bucket_has(hb[u], v[u]);
-                        if (in && !hit[u] && hb[u].w != -1) hit[u] = hash_contains(S.H, kHBits, v[u]);
+                        more[u] = in && !hit[u] && hb[u].w != -1;
+                        anymore |= more[u];
+                    }
+                    if (__any_sync(kFull, anymore)) {
+#pragma unroll
+                        for (int u = 0; u < kTestU; ++u)
+                            if (more[u]) hit[u] = hash_contains(S.H, kHBits, v[u]);
                     }
                 } else {
 #pragma unroll
