@@ -512,6 +512,7 @@ __global__ void __launch_bounds__(kAgentWarps * 32, 4) k_agents(Arena A, int64_t
         q = __shfl_sync(kFull, q, 0);
         if (q >= limit) break;
         int64_t a;
+        bool general = true;  // heavy-listed (or k > 64) agents take the general instance
         if (BIG)
             a = (int64_t)A.big_list[q];
         else if (q < hc)
@@ -519,11 +520,14 @@ __global__ void __launch_bounds__(kAgentWarps * 32, 4) k_agents(Arena A, int64_t
         else {
             a = q - hc;
             if (kHeavyFirst && A.heavy_mark[a]) continue;
+            general = !kHeavyFirst;
         }
         const int k = A.kk[a];
         if (!BIG && k > KCAP) continue;
         if constexpr (THIN) {
-            if (!process_agent_thin<KCAP, HCAP, STAGE>(A, a, k, S, phase)) break;
+            const bool ok = general ? process_agent_thin<KCAP, HCAP, STAGE, true>(A, a, k, S, phase)
+                                    : process_agent_thin<KCAP, HCAP, STAGE, false>(A, a, k, S, phase);
+            if (!ok) break;
         } else
             process_agent<KCAP>(A, a, k, S);
     }
@@ -591,6 +595,14 @@ cudaError_t init_agent_kernels() {
             if (b < 1) b = 1;
     if (g_blocks_hsmall < 1) g_blocks_hsmall = 1;
     return e;
+}
+
+// Warps of the agent kernels that can be resident at once (the rows of the global anchor table).
+int64_t agent_warp_slots(int num_sms) {
+    int mb = g_blocks_hsmall;
+    for (auto& row : g_blocks)
+        for (int b : row) mb = b > mb ? b : mb;
+    return (int64_t)num_sms * mb * kAgentWarps;
 }
 
 int agent_occupancy(int thin, int small_hash) {

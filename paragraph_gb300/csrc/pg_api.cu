@@ -97,6 +97,7 @@ struct pg_ctx {
     DBuf<int16_t> hslot;
     DBuf<uint64_t> hub2;
     DBuf<uint32_t> hub_need;
+    DBuf<int32_t> zbig;
     DBuf<uint64_t> hmask;
     DBuf<float> fit, w;
     DBuf<uint64_t> cdf, tilesum, tileoff, tables;
@@ -228,6 +229,7 @@ Arena make_arena(pg_ctx* c) {
     A.hmask = c->hmask.p;
     A.hub2 = c->hub2.p;
     A.hub_need = c->hub_need.p;
+    A.zbig = c->zbig.p;
     A.hlist = c->hlist.p;
     A.sampler = c->cfg.sampler;
     A.tune_agent_ctas = c->tune.agent_ctas_per_sm;
@@ -905,6 +907,9 @@ pg_status pg_create(pg_ctx** out, const pg_config* cfg) {
     if (e == cudaSuccess) e = init_agent_kernels();
     if (e == cudaSuccess) e = init_csr_kernels();
     if (e == cudaSuccess && cfg->weight_model == PG_WEIGHTS_REFCOMPAT) e = init_rc_kernels();
+    // one global hash per resident agent warp, for anchors whose rows overflow the shared one
+    if (e == cudaSuccess && cfg->weight_model == PG_WEIGHTS_BASELINE && cfg->sampler == PG_SAMPLER_THINNING)
+        e = dalloc(c->zbig, agent_warp_slots(c->num_sms) << kGBits);
     for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->tev[i]);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->lev[i]);
@@ -954,6 +959,7 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->hmask);
     dfree(c->hub2);
     dfree(c->hub_need);
+    dfree(c->zbig);
     dfree(c->src_tmp);
     dfree(c->rep);
     dfree(c->st);

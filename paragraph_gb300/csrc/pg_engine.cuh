@@ -25,6 +25,7 @@ constexpr int kErChunk = 65536;      // ids per ER Philox stream
 constexpr int kSortMid = 256;        // appended segments up to this length sort in one warp's registers
 constexpr int kBitmapWords = 40960;  // 160 KiB of shared bitmap in the large-segment sort
 #define PG_MAX_ANCHORS_DEV 4
+constexpr int kGBits = 13;           // per-warp global hash for anchor rows too large for shared memory
 constexpr int kZCap = 1024;          // 1-hop frontier entries kept in shared memory per warp
 constexpr int kCopyTile = 4096;      // backward entries per copy tile
 constexpr int kHeavyMax = 256;       // hubs per replica with a bit in the per-node hub mask
@@ -148,6 +149,7 @@ struct Arena {
     int32_t* big_list;         // [agent cap]
     int32_t* heavy_list;       // [agent cap] agents with a hub or a large frontier (k <= kKSmall)
     int32_t* heavy_mark;       // [agent cap] 1 when the agent is on heavy_list
+    int32_t* zbig;             // [agent-kernel warp slots][1 << kGBits] rows of anchors too large for H
     int32_t* tile_row;         // [copy tiles] row holding the first position of each copy tile
     int64_t* len_tmp;          // [slots]
     uint64_t* tilesum;         // [ntiles]
@@ -344,6 +346,7 @@ void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t
                       uint32_t* err, cudaStream_t s);
 // resident CTAs per SM of the k <= 64 agent kernel (after init_agent_kernels)
 int agent_occupancy(int thin, int small_hash);
+int64_t agent_warp_slots(int num_sms);
 cudaError_t init_csr_kernels();
 
 }  // namespace pg

@@ -99,6 +99,7 @@ struct Ball {
     const int16_t* hslot;             // hub bit of the node or -1
     const unsigned long long* hmask;  // [node][kMaskWords]
     const int32_t* H;                 // frontier hash set (shared memory)
+    const int32_t* G;                 // rows of the anchors too large for H (global), or null
     const BallAux* X;                 // anchors and hub masks (shared memory)
     int hbits;                        // log2 of the hash capacity
     bool small;                       // every non-hub anchor's rows are in H
@@ -151,6 +152,32 @@ __device__ __forceinline__ bool hash_contains(const int32_t* H, int bits, int32_
     return false;
 }
 
+// The same set in global memory (the warp's own table of 1 << kGBits slots), for the rows of
+// anchors that do not fit the shared one.  Lookups read through L2 (ld.global.cg): the table is
+// cleared with stores and filled with L2 atomics in the same agent, so an L1 copy from an earlier
+// agent must not answer.
+__device__ __forceinline__ void ghash_insert(int32_t* G, int32_t v) {
+    const uint32_t mask = (1u << kGBits) - 1u;
+    uint32_t s = hslot_of(v, kGBits);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const int prev = atomicCAS(&G[s], -1, v);
+        if (prev == -1 || prev == v) return;
+        s = (s + 1u) & mask;
+    }
+}
+
+__device__ __forceinline__ bool ghash_contains(const int32_t* G, int32_t v) {
+    const uint32_t mask = (1u << kGBits) - 1u;
+    uint32_t s = hslot_of(v, kGBits);
+    for (uint32_t probe = 0; probe <= mask; probe += 4) {
+        const int4 b = __ldcg(reinterpret_cast<const int4*>(G + s));
+        if (bucket_has(b, v)) return true;
+        if (b.w == -1) return false;
+        s = (s + 4u) & mask;
+    }
+    return false;
+}
+
 __device__ __forceinline__ int hub_slot(const Ball& B, int32_t v) { return B.hslot[v]; }
 
 __device__ __forceinline__ bool mask_bit(const Mask& m, int b) {
@@ -162,7 +189,9 @@ __device__ __forceinline__ bool mask_bit(const Mask& m, int b) {
 // v in Z (frontier) -- lane-level, any lane may call it with its own v
 __device__ __forceinline__ bool in_z(const Ball& B, int32_t v) {
     if (hash_contains(B.H, B.hbits, v)) return true;
-    if (!B.small) {
+    if (B.G) {
+        if (ghash_contains(B.G, v)) return true;
+    } else if (!B.small) {
         const BallAux& X = *B.X;
         for (int i = 0; i < X.na; ++i) {
             if (!X.big[i]) continue;
@@ -221,7 +250,9 @@ __device__ bool member_warp(const Ball& B, int32_t j, long long& examined) {
 }
 
 // Returns false when a bounded wait ran out (the error word is set and the warp must stop).
-template <int KCAP, int HCAP, int STAGE>
+// GENERAL = false is the lean instance for the agents the setup did not list as heavy: no hub
+// anchor and anchor rows within the shared frontier, so membership in Z is the frontier hash alone.
+template <int KCAP, int HCAP, int STAGE, bool GENERAL>
 __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KCAP, HCAP, STAGE>& S,
                                    uint32_t& phase) {
     constexpr int kStage = STAGE;
@@ -243,6 +274,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     B.hslot = A.hslot + rp.nbase;
     B.hmask = reinterpret_cast<const unsigned long long*>(A.hmask) + rp.nbase * kMaskWords;
     B.H = S.H;
+    B.G = nullptr;
     B.X = &S.aux;
     B.hbits = kHBits;
     B.small = true;
@@ -311,6 +343,22 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                     bigm |= 1u << i;
             }
         }
+        // the general instance puts the rows of the anchors left out of H into the warp's global
+        // table when they fit it at three-quarters load (otherwise membership in them is a binary
+        // search of the rows)
+        int32_t* G = nullptr;
+        if (GENERAL && bigm && A.zbig) {
+            int64_t tb = 0;
+#pragma unroll
+            for (int i = 0; i < PG_MAX_ANCHORS_DEV; ++i)
+                if ((bigm >> i) & 1u) tb += dd[i];
+            if (tb <= (3 << kGBits) / 4) {
+                G = A.zbig + (((int64_t)blockIdx.x * kAgentWarps + (threadIdx.x >> 5)) << kGBits);
+                int4* g4 = reinterpret_cast<int4*>(G);
+                for (int q = lane; q < (1 << kGBits) / 4; q += 32) g4[q] = make_int4(-1, -1, -1, -1);
+                __syncwarp();
+            }
+        }
         if (lane == 0) {
 #pragma unroll
             for (int i = 0; i < PG_MAX_ANCHORS_DEV; ++i) {
@@ -344,7 +392,8 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
         const int64_t incl = warp_incl_scan(len_in);
         const int64_t excl = incl - len_in;
         const int64_t T = __shfl_sync(kFull, incl, 31);
-        const int into = (row_in && !((bigm >> rl) & 1u)) ? 1 : 0;
+        // 1: into H; 2: into the global table; 0: neither (hub masks only)
+        const int into = row_in ? (!((bigm >> rl) & 1u) ? 1 : (G ? 2 : 0)) : 0;
         for (int64_t p0 = 0; p0 < T; p0 += 64) {
             int32_t v[2];
             int ih[2];
@@ -364,7 +413,10 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
                 if (!ok[u]) continue;
-                if (ih[u]) hash_insert(S.H, kHBits, v[u]);
+                if (ih[u] == 1)
+                    hash_insert(S.H, kHBits, v[u]);
+                else if (GENERAL && ih[u] == 2)
+                    ghash_insert(G, v[u]);
                 add_mask(v[u]);
             }
         }
@@ -385,6 +437,14 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             if (lane == 0) S.aux.hm[ww] = ((unsigned long long)hi << 32) | lo;
         }
         __syncwarp();
+        B.G = G;
+    }
+
+    if (!GENERAL && !(B.small && !B.any_ha)) {
+        // the setup lists every agent with a hub anchor or anchor rows beyond 512 entries as
+        // heavy, so the lean instance never gets one; a mismatch is reported, not guessed around
+        if (lane == 0) atomicOr(&A.st->error, kErrArg);
+        return false;
     }
 
     // ---------------------------------------------------------------- events
@@ -428,7 +488,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             // global loads overlap the shared-memory hash lookups
             const int hs = hub_slot(B, j);
             const int64_t jf0 = B.fo[j], jf1 = B.fo[j + 1], jb0 = B.bo[j], jb1 = B.bo[j + 1];
-            if (in_z(B, j)) {
+            if (GENERAL ? in_z(B, j) : hash_contains(S.H, kHBits, j)) {
                 mem = true;
             } else if (hs >= 0) {
                 mem = (B.X->hm[hs >> 6] >> (hs & 63)) & 1ull;
@@ -486,7 +546,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             return true;
         };
         // chunks are double-buffered: chunk c+1 is in flight while chunk c is tested
-        const bool simple = B.small && !B.any_ha;  // membership in Z is the frontier hash alone
+        const bool simple = !GENERAL || (B.small && !B.any_ha);  // membership in Z: the hash alone
         const int64_t nchunk = (DW + kStage - 1) / kStage;
         uint32_t armed = 0;  // bit b: buffer b has copies in flight
         if (nchunk > 0 && issue(0, 0)) armed = 1u;
