@@ -171,17 +171,30 @@ __global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
             __syncthreads();
             const int last = (int)nr - 1;
             const int nblk = (int)((p1 - p0 + 31) >> 5);
-            for (int64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-                const int b = (int)((p - p0) >> 5);
-                int l = s_blk[b], h = b + 1 < nblk ? s_blk[b + 1] : last;
-                while (l < h) {
-                    const int mid = (l + h + 1) >> 1;
-                    if (s_oc[mid] <= p)
-                        l = mid;
-                    else
-                        h = mid - 1;
+            // four positions per thread in flight: their loads are issued before any is placed
+            constexpr int kU = 4;
+            for (int64_t pb = p0 + threadIdx.x; pb < p1; pb += kU * (int64_t)blockDim.x) {
+                int32_t val[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int64_t p = pb + u * (int64_t)blockDim.x;
+                    val[u] = p < p1 ? cc[p] : 0;
                 }
-                cn[p + s_sh[l]] = cc[p];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int64_t p = pb + u * (int64_t)blockDim.x;
+                    if (p >= p1) break;
+                    const int b = (int)((p - p0) >> 5);
+                    int l = s_blk[b], h = b + 1 < nblk ? s_blk[b + 1] : last;
+                    while (l < h) {
+                        const int mid = (l + h + 1) >> 1;
+                        if (s_oc[mid] <= p)
+                            l = mid;
+                        else
+                            h = mid - 1;
+                    }
+                    cn[p + s_sh[l]] = val[u];
+                }
             }
         } else {
             for (int64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
