@@ -171,8 +171,8 @@ __global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
             __syncthreads();
             const int last = (int)nr - 1;
             const int nblk = (int)((p1 - p0 + 31) >> 5);
-            // four positions per thread in flight: their loads are issued before any is placed
-            constexpr int kU = 4;
+            // eight positions per thread in flight: their loads are issued before any is placed
+            constexpr int kU = 8;
             for (int64_t pb = p0 + threadIdx.x; pb < p1; pb += kU * (int64_t)blockDim.x) {
                 int32_t val[kU];
 #pragma unroll
