@@ -84,6 +84,8 @@ __global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, in
 // w_j for active nodes; per-replica max (as float bits, valid for non-negative floats) and count
 // of positive weights.
 __global__ void __launch_bounds__(kTileThreads) k_weights(Arena A) {
+    __shared__ uint32_t s_max[kTileThreads / 32];
+    __shared__ int s_cnt[kTileThreads / 32], s_act[kTileThreads / 32];
     if (A.st->error) return;
     const int t = blockIdx.x;
     const int r = A.tile_rep[t];
@@ -92,17 +94,28 @@ __global__ void __launch_bounds__(kTileThreads) k_weights(Arena A) {
     if (v0 >= rp.n) return;
     const int64_t n = rp.n;
     const int32_t ep = (int32_t)A.st->epoch;
+    constexpr int kPer = kTile / kTileThreads;
+    // every input of the thread's nodes is loaded before any weight is stored (the stores could
+    // otherwise alias the later loads and serialise them)
+    float fv[kPer];
+    int32_t iv[kPer], pv[kPer];
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+        const int64_t v = v0 + threadIdx.x + i * kTileThreads;
+        const int64_t slot = rp.nbase + (v < n ? v : 0);
+        fv[i] = A.fit[slot];
+        iv[i] = A.indeg[slot];
+        pv[i] = A.pub[slot];
+    }
     uint32_t wmax = 0;
     int cnt = 0, act = 0;
     bool bad = false;
 #pragma unroll
-    for (int i = 0; i < kTile / kTileThreads; ++i) {
+    for (int i = 0; i < kPer; ++i) {
         const int64_t v = v0 + threadIdx.x + i * kTileThreads;
         if (v < n) {
-            const int64_t slot = rp.nbase + v;
-            const float w = weight0(A.fit[slot], A.indeg[slot], ep - A.pub[slot], rp.alpha,
-                                    rp.gamma, rp.tau);
-            A.w[slot] = w;
+            const float w = weight0(fv[i], iv[i], ep - pv[i], rp.alpha, rp.gamma, rp.tau);
+            A.w[rp.nbase + v] = w;
             ++act;
             if (!(w <= 3.0e38f)) bad = true;  // inf or NaN
             if (w > 0.0f) {
@@ -112,11 +125,24 @@ __global__ void __launch_bounds__(kTileThreads) k_weights(Arena A) {
             }
         }
     }
+    // one set of replica atomics per CTA
     wmax = __reduce_max_sync(0xffffffffu, wmax);
     cnt = __reduce_add_sync(0xffffffffu, cnt);
     act = __reduce_add_sync(0xffffffffu, act);
     if (__any_sync(0xffffffffu, bad) && lane_id() == 0) atomicOr(&A.st->error, kErrBadWeight);
+    const int wid = threadIdx.x >> 5;
     if (lane_id() == 0) {
+        s_max[wid] = wmax;
+        s_cnt[wid] = cnt;
+        s_act[wid] = act;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kTileThreads / 32; ++w) {
+            wmax = s_max[w] > wmax ? s_max[w] : wmax;
+            cnt += s_cnt[w];
+            act += s_act[w];
+        }
         if (wmax) atomicMax(&A.rep[r].wmax_bits, wmax);
         if (cnt) atomicAdd((unsigned long long*)&A.rep[r].npos, (unsigned long long)cnt);
         if (act) atomicAdd(&A.st->nodes_weighted, (unsigned long long)act);
