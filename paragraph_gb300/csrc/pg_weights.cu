@@ -336,15 +336,26 @@ __global__ void __launch_bounds__(kTileThreads) k_hub_hist(Arena A) {
     Replica& rp = A.rep[r];
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
     if (v0 >= rp.n) return;
+    // the degrees of the thread's nodes are loaded before the resets are stored (the stores could
+    // otherwise alias the later loads and serialise them)
+    constexpr int kPer = kTile / kTileThreads;
+    int64_t dg[kPer];
 #pragma unroll
-    for (int i = 0; i < kTile / kTileThreads; ++i) {
+    for (int i = 0; i < kPer; ++i) {
+        const int64_t v = v0 + threadIdx.x + i * kTileThreads;
+        dg[i] = v < rp.n ? degree_of(A, rp, v) : 0;
+    }
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
         const int64_t v = v0 + threadIdx.x + i * kTileThreads;
         if (v >= rp.n) continue;
         const int64_t slot = rp.nbase + v;
         A.hslot[slot] = -1;
-#pragma unroll
-        for (int w = 0; w < kMaskWords; ++w) A.hmask[slot * kMaskWords + w] = 0;
-        const int64_t d = degree_of(A, rp, v);
+        static_assert(kMaskWords == 4, "hub mask row of 32 bytes");
+        ulonglong2* hm = reinterpret_cast<ulonglong2*>(A.hmask + slot * kMaskWords);
+        hm[0] = make_ulonglong2(0ull, 0ull);
+        hm[1] = make_ulonglong2(0ull, 0ull);
+        const int64_t d = dg[i];
         if (d >= (1 << kHeavyMinLog)) {
             int b = 63 - __clzll((unsigned long long)d) - kHeavyMinLog;
             if (b >= kHeavyBins) b = kHeavyBins - 1;
@@ -380,11 +391,18 @@ __global__ void __launch_bounds__(kTileThreads) k_hub_collect(Arena A) {
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
     if (v0 >= rp.n) return;
     const int64_t thr = rp.heavy_thr;
+    constexpr int kPer = kTile / kTileThreads;
+    int64_t dg[kPer];
 #pragma unroll
-    for (int i = 0; i < kTile / kTileThreads; ++i) {
+    for (int i = 0; i < kPer; ++i) {
+        const int64_t v = v0 + threadIdx.x + i * kTileThreads;
+        dg[i] = v < rp.n ? degree_of(A, rp, v) : 0;
+    }
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
         const int64_t v = v0 + threadIdx.x + i * kTileThreads;
         if (v >= rp.n) continue;
-        if (degree_of(A, rp, v) >= thr) {
+        if (dg[i] >= thr) {
             const int b = atomicAdd(&rp.heavy_count, 1);
             if (b < kHeavyMax) {
                 A.hslot[rp.nbase + v] = (int16_t)b;
