@@ -714,6 +714,70 @@ def run_small_configs(args) -> None:
                              "kind": "port", "sample": "the 10 epochs, CPU oracle"}}), flush=True)
 
 
+def run_refcompat(args) -> None:
+    """The reference's own per-paper model (refcompat weights: preferential, recency and fitness
+    scores, 1-hop/2-hop split, same-year and uniform citations) on a 200k-paper seed, 10 epochs at
+    3 % growth with 10 % same-year citations, regrown from a device checkpoint each step; the CPU
+    oracle of the same model (all host threads) on the same 10 epochs beside it."""
+    import oracle as O
+    from paragraph_gb300 import PG_WEIGHTS_REFCOMPAT, GrowthEngine, PAParams, RCParams
+    from paragraph_gb300 import workloads as W
+
+    threads = os.cpu_count() or 1
+    g = W.rc_seed(200_000, 10, seed=args.seed)
+    bag, rec = W.rc_tables(seed=args.seed)
+    rc = RCParams(growth_rate=0.03, same_year=0.1)
+    epochs = 10
+    with GrowthEngine(seed=args.seed, weight_model=PG_WEIGHTS_REFCOMPAT) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, PAParams(growth_rate=0.03), planned_epochs=epochs)
+        eng.rc_configure(rc, bag, rec)
+        # the bag, not the PA plan, bounds the out-degrees: room for every epoch before the
+        # checkpoint (an arena regrown mid-run drops it)
+        n0, m0 = eng.counts()
+        n1 = n0
+        for _ in range(epochs):
+            n1 += int(np.ceil(n1 * 0.03))
+        eng.reserve(n1, m0 + (n1 - n0) * int(min(max(bag), 256)))
+        eng.checkpoint()
+
+        def step():
+            eng.restore()
+            eng.sync()
+            eng.timer_start()
+            ne = eng.run_epochs(epochs, use_graph=True)
+            return ne, eng.timer_stop()
+
+        for _ in range(args.warmup):
+            step()
+        edges, ms = 0, 0.0
+        for _ in range(args.steps):
+            e, t = step()
+            edges += e
+            ms += t
+        launches = eng.stats()["run_kernel_launches"]
+    og = O.OracleGraph(args.seed, 0)
+    og.load(g.pub, g.fitness, g.src, g.dst)
+    og.rc_configure(rc, bag, rec)
+    t0 = time.perf_counter()
+    m0 = og.m
+    for _ in range(epochs):
+        og.rc_epoch(threads)
+    cpu_s = time.perf_counter() - t0
+    cpu_edges = og.m - m0
+    og.close()
+    print(json.dumps({
+        "metric": "citation edges/sec (refcompat growth step)", "value": edges / (ms / 1000.0),
+        "unit": "citations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32/u128 scores/f64", "data": "synthetic",
+        "config": {"workload": "refcompat_200k_seed_10_epochs_3pct", "same_year": 0.1,
+                   "parallelism": "replicas only"},
+        "gpu_launches": launches,
+        "cpu_baseline": {"value": cpu_edges / cpu_s, "unit": "citations/s", "cores": threads, "kind": "port",
+                         "sample": "the 10 epochs, CPU oracle of the refcompat model (all threads)"}}),
+        flush=True)
+
+
 def epoch_report(args) -> None:
     """One JSON line per epoch of the workload: stage times (CUDA events) and byte-model counters.
     Stops early when an epoch exceeds --epoch-cap-s (the enumeration sampler slows down as hubs
@@ -800,7 +864,13 @@ def main():
                     help="seed size of the calibration trace (smaller cases for profiling)")
     ap.add_argument("--small-configs", action="store_true",
                     help="plain PA (10k seed) and ER G(n,p) lines with their CPU baselines")
+    ap.add_argument("--refcompat", action="store_true",
+                    help="the reference's own per-paper model (refcompat) with its CPU baseline")
     args = ap.parse_args()
+    if args.refcompat:
+        if args.warmup < 3:
+            args.warmup = 3
+        return run_refcompat(args)
     if args.small_configs:
         if args.warmup < 3:
             args.warmup = 3
