@@ -574,13 +574,6 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             // position q maps to row position q + fx0 in the forward window (q < qf), q + bx0 in
             // the backward one.
             const int nq = (int)(DW - c0 < kStage ? DW - c0 : kStage);
-            const int64_t wlo64 = wx - c0, whi64 = wx + W - c0, qf64 = wx + fw - c0;
-            const int wlo = (int)(wlo64 < -1 ? -1 : (wlo64 > kStage ? kStage : wlo64));
-            const int whi = (int)(whi64 < -1 ? -1 : (whi64 > kStage ? kStage : whi64));
-            const int qf = (int)(qf64 < -1 ? -1 : (qf64 > kStage ? kStage : qf64));
-            const int fx0 = (int)((c0 - wx) + (fa0 - f0));
-            const int bx0 = (int)(lf + (c0 - wx - fw) + (ba0 - b0));
-            const int lf32 = (int)lf, d32 = (int)d;
             for (int i0 = 0; i0 < nq; i0 += 32 * kTestU) {
                 bool hit[kTestU];
                 if (simple) {
@@ -591,7 +584,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
 #pragma unroll
                     for (int u = 0; u < kTestU; ++u) {
                         const int q = i0 + 32 * u + lane;
-                        v[u] = stg[q < nq ? q : 0];
+                        v[u] = stg[q];  // q < kStage: past nq the entry is stale and masked below
                         hb[u] = *reinterpret_cast<const int4*>(S.H + hslot_of(v[u], kHBits));
                     }
                     bool more[kTestU], anymore = false;
@@ -623,6 +616,14 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
 #pragma unroll
                 for (int u = 0; u < kTestU; ++u) anyhit |= hit[u];
                 if (!__any_sync(kFull, anyhit)) continue;
+                // a step with hits: this lane's window in chunk coordinates (computed only here)
+                const int64_t wlo64 = wx - c0, whi64 = wx + W - c0, qf64 = wx + fw - c0;
+                const int wlo = (int)(wlo64 < -1 ? -1 : (wlo64 > kStage ? kStage : wlo64));
+                const int whi = (int)(whi64 < -1 ? -1 : (whi64 > kStage ? kStage : whi64));
+                const int qf = (int)(qf64 < -1 ? -1 : (qf64 > kStage ? kStage : qf64));
+                const int fx0 = (int)((c0 - wx) + (fa0 - f0));
+                const int bx0 = (int)(lf + (c0 - wx - fw) + (ba0 - b0));
+                const int lf32 = (int)lf, d32 = (int)d;
 #pragma unroll
                 for (int u = 0; u < kTestU; ++u) {
                     unsigned hm = __ballot_sync(kFull, hit[u]);
