@@ -5,20 +5,23 @@
 // in the agent's 2-hop ball).  Node j's accepted events then have rate w_j beta^[j in ball], so the
 // first k distinct accepted nodes are the successive-sampling draw with those weights -- the law of
 // the reference's ES top-k over the neighbourhood (src/abm.cu:461-565) -- at a cost that does not
-// depend on the ball's size.  The 32 lanes evaluate 32 events at once (Philox + CDF search); the
-// acceptances are then taken in event order, each boost candidate tested by the whole warp.
+// depend on the ball's size.  The 32 lanes evaluate 32 events at once (Philox + guide-table CDF
+// search); the acceptances are then taken in event order.  The rows of all boost candidates of a
+// batch are staged into shared memory by bulk copies and tested together.
 //
 // Ball membership, the 2-hop BFS of GetOneAndTwoHopNeighborhood (src/abm.cu:577-682) answered on
 // demand instead of materialised:
 //   Z  = anchors U adj(x) for every non-hub anchor x   -- the 1-hop frontier, a hash set in shared
-//                                                          memory (open addressing, load <= 1/2).
+//                                                          memory (4-slot buckets, load <= 1/2);
+//                                                          rows too large for it go to a per-warp
+//                                                          global table or stay in the CSR.
 //   HA = hub bits of the anchors that are hubs          -- their (huge) rows stay implicit.
 //   in_z(v)   <=> v in Z  or  hmask[v] & HA != 0        (v adjacent to a hub anchor)
 //   member(j) <=> in_z(j)  or  some z in adj(j) has in_z(z)
 // For a hub j, the second clause is one bit of HM = OR of hmask over Z | OR of hub2[b] over b in HA,
 // where hub2[b] marks the hubs that share a neighbour with hub b.  A test of a non-hub j scans
-// adj(j) (forward row, then backward row) 32 entries at a time and stops at the first hit; the
-// number of entries it examined feeds the byte model.
+// adj(j) (forward row, then backward row) and keeps its first hit; the number of entries it
+// examined (up to that hit) feeds the byte model.
 
 // Per-warp shared-memory part of an agent's ball (kept out of registers: read only on the rare
 // paths of hub anchors, oversized anchors and hub candidates).
@@ -33,8 +36,8 @@ struct BallAux {
 constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a bulk-copy barrier before giving up
 constexpr int kTestU = 4;                  // entries per lane and step of the membership scan
 
-// STAGE: adjacency entries staged per chunk and warp (1024 in the small-hash k <= 64 kernel, 512
-// where the frontier hash or k is larger, so four warps stay within 48 KiB of static shared memory)
+// STAGE: adjacency entries per stage buffer (two per warp; 1024 in the small-hash k <= 64 kernel,
+// 512 in the others); the struct lives in dynamic shared memory, one per warp
 template <int KCAP, int HCAP, int STAGE>
 struct ThinSmem {
     __align__(16) int32_t stage[2][STAGE];  // candidate rows, two buffers filled by bulk copies
