@@ -455,6 +455,42 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         h.m_cap = round_up(std::max<int64_t>(h.m_cap, h.m + 1), 4);
         M += h.m_cap;
     }
+    // a single replica's raw edges are uploaded and checked before the arena is touched (a bad
+    // edge list leaves the loaded graph intact); the build below reuses the upload
+    DBuf<int32_t> raw_src, raw_dst;
+    bool raw_up = false;
+    if (raw && R == 1 && raw[0].num_edges > 0) {
+        const pg_replica_desc& d = raw[0];
+        DBuf<unsigned long long> first;
+        auto drop = [&]() {
+            dfree(raw_src);
+            dfree(raw_dst);
+            dfree(first);
+        };
+        cudaError_t e = dalloc(raw_src, d.num_edges);
+        if (e == cudaSuccess) e = dalloc(raw_dst, d.num_edges);
+        if (e == cudaSuccess) e = dalloc(first, 1);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(raw_src.p, d.src, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(raw_dst.p, d.dst, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream);
+        unsigned long long bad = ~0ull;
+        if (e == cudaSuccess) {
+            launch_first_bad_edge(raw_src.p, raw_dst.p, d.num_edges, d.num_nodes, first.p, c->stream);
+            e = cudaMemcpyAsync(&bad, first.p, sizeof(bad), cudaMemcpyDeviceToHost, c->stream);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        dfree(first);
+        if (e != cudaSuccess) {
+            drop();
+            return fail(c, PG_ERR_CUDA, std::string("edge upload: ") + cudaGetErrorString(e));
+        }
+        if (bad != ~0ull) {
+            drop();
+            return fail(c, PG_ERR_ARG, "edge endpoint out of range at index " + std::to_string(bad));
+        }
+        raw_up = true;
+    }
     c->S = S;
     c->T = T;
     c->M = M;
@@ -519,7 +555,6 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     std::vector<uint64_t> tabs((size_t)R * kTableEntries);
     // scratch of the device CSR build: raw edges of one replica and the sort buffers
     DBuf<char> scratch;
-    DBuf<int32_t> raw_src, raw_dst;
     DBuf<uint32_t> berr;
     if (raw) {
         int64_t mm = 1, nn = 1;
@@ -528,8 +563,10 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             nn = std::max<int64_t>(nn, raw[r].num_nodes);
         }
         PG_CUDA(c, dalloc(scratch, (int64_t)build_scratch_bytes(mm, nn)));
-        PG_CUDA(c, dalloc(raw_src, mm));
-        PG_CUDA(c, dalloc(raw_dst, mm));
+        if (!raw_up) {
+            PG_CUDA(c, dalloc(raw_src, mm));
+            PG_CUDA(c, dalloc(raw_dst, mm));
+        }
         PG_CUDA(c, dalloc(berr, 1));
         PG_CUDA(c, cudaMemsetAsync(berr.p, 0, 4, c->stream));
     }
@@ -554,7 +591,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             const pg_replica_desc& d = raw[r];
             PG_CUDA(c, cudaMemcpyAsync(c->pub.p + h.nbase, d.pub_epoch, 4 * n, cudaMemcpyHostToDevice, c->stream));
             PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase, d.fitness, 4 * n, cudaMemcpyHostToDevice, c->stream));
-            if (d.num_edges > 0) {
+            if (d.num_edges > 0 && !raw_up) {
                 PG_CUDA(c, cudaMemcpyAsync(raw_src.p, d.src, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream));
                 PG_CUDA(c, cudaMemcpyAsync(raw_dst.p, d.dst, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream));
             }
@@ -990,10 +1027,13 @@ pg_status pg_load_replicas(pg_ctx* c, const pg_replica_desc* descs, int32_t num)
         if (d.num_nodes <= 0 || d.num_nodes > (int64_t)INT32_MAX / 2) return fail(c, PG_ERR_ARG, "num_nodes out of range");
         if (d.num_edges < 0 || (d.num_edges > 0 && (!d.src || !d.dst))) return fail(c, PG_ERR_ARG, "bad edge arrays");
         if (!d.pub_epoch || !d.fitness) return fail(c, PG_ERR_ARG, "pub_epoch and fitness are required");
-        // endpoints checked on all host threads before the arena is touched, so a bad edge list
-        // leaves the loaded graph intact
-        const int64_t bad = first_bad_edge(d.src, d.dst, d.num_edges, d.num_nodes);
-        if (bad >= 0) return fail(c, PG_ERR_ARG, "edge endpoint out of range at index " + std::to_string(bad));
+        // endpoints checked before the arena is touched, so a bad edge list leaves the loaded graph
+        // intact: on all host threads here for several replicas, on the device (after the upload
+        // the build needs anyway) for one
+        if (num > 1) {
+            const int64_t bad = first_bad_edge(d.src, d.dst, d.num_edges, d.num_nodes);
+            if (bad >= 0) return fail(c, PG_ERR_ARG, "edge endpoint out of range at index " + std::to_string(bad));
+        }
     }
     // the CSRs are built on the device from the raw edges (upload_arena); the plan below uses the
     // raw edge count, an upper bound on the unique edges

@@ -124,6 +124,21 @@ __global__ void __launch_bounds__(256) k_backward_cols(const unsigned long long*
     }
 }
 
+// Index of the first edge with an endpoint outside [0, n) (atomic minimum; ~0 when none).
+__global__ void __launch_bounds__(256) k_first_bad_edge(const int32_t* src, const int32_t* dst, int64_t m, int64_t n,
+                                                        unsigned long long* first) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        if ((uint32_t)src[i] >= (uint32_t)n || (uint32_t)dst[i] >= (uint32_t)n) atomicMin(first, (unsigned long long)i);
+}
+
+void launch_first_bad_edge(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, unsigned long long* first,
+                           cudaStream_t s) {
+    cudaMemsetAsync(first, 0xFF, sizeof(unsigned long long), s);
+    if (m <= 0) return;
+    const unsigned grid = (unsigned)std::min<int64_t>((m + 255) / 256, 152 * 16);
+    k_first_bad_edge<<<grid, 256, 0, s>>>(src, dst, m, n, first);
+}
+
 int64_t build_radix_tiles(int64_t m) { return (m + kSortTile - 1) / kSortTile; }
 int64_t build_scan_entries(int64_t m) { return build_radix_tiles(m) * kRadix; }
 

@@ -340,6 +340,8 @@ void launch_text_write(const int64_t* fo, const int32_t* fc, int64_t n, int64_t 
 void launch_edge_sources(const int64_t* fo, int64_t n, int64_t first, int64_t count, int32_t* out,
                          int num_sms, cudaStream_t s);
 // device CSR construction from a raw edge list (pg_build.cu)
+void launch_first_bad_edge(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, unsigned long long* first,
+                           cudaStream_t s);
 size_t build_scratch_bytes(int64_t m, int64_t n);
 void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,
                       int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_out,

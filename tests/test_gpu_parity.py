@@ -295,8 +295,12 @@ def test_device_seed_load_matches_host_construction(gpu, n):
                         PAParams(fixed_new_nodes=2), planned_epochs=1)
         assert tiny.counts() == (3, 0)
         tiny.close()
-        with pytest.raises(PGError):
+        before = eng.counts()
+        with pytest.raises(PGError, match="out of range at index 1"):
             eng.load_graph(pub, fit, np.array([0, n], np.int32), np.array([1, 2], np.int32))
+        # the rejected edge list left the loaded graph as it was
+        assert eng.counts() == before
+        _compare_state(eng, og)
 
 
 def test_edges_into_caller_buffers(gpu):
