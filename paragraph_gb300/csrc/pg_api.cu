@@ -82,6 +82,8 @@ struct pg_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;        // the hub index of an epoch, beside the weights
+    cudaEvent_t fork = nullptr, join = nullptr;
     int R = 1;
     bool loaded = false;
     bool poisoned = false;  // a kernel reported an error mid-epoch; reload before growing again
@@ -759,12 +761,23 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
         c->launches += kPaEpochKernels - 4 - 2 + kRcScoreKernels + 1;
         return PG_OK;
     }
+    // the hub index reads only the CSR and the weights and guide table only node attributes: the
+    // hub kernels run on a side stream forked here and joined before the agent setup (the same
+    // dependencies inside a captured graph)
+    const bool thin = c->cfg.sampler == PG_SAMPLER_THINNING;
+    if (thin) {
+        PG_CUDA(c, cudaEventRecord(c->fork, s));
+        PG_CUDA(c, cudaStreamWaitEvent(c->side, c->fork, 0));
+        launch_hubs(A, c->num_sms, c->side);
+        PG_STAGE("hub index");
+        PG_CUDA(c, cudaEventRecord(c->join, c->side));
+    }
     launch_weights(A, s);
     PG_STAGE("weights");
-    if (c->cfg.sampler == PG_SAMPLER_THINNING) {
+    if (thin) {
         launch_guide(A, s);
-        launch_hubs(A, c->num_sms, s);
-        PG_STAGE("guide table and hub index");
+        PG_STAGE("guide table");
+        PG_CUDA(c, cudaStreamWaitEvent(s, c->join, 0));
         c->launches += kThinKernels;
     }
     if (events) record_event(ev[1], s);
@@ -950,6 +963,9 @@ pg_status pg_create(pg_ctx** out, const pg_config* cfg) {
     for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->tev[i]);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->lev[i]);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         c->err = std::string("CUDA initialisation failed: ") + cudaGetErrorString(e);
         *out = c;
@@ -1007,6 +1023,9 @@ void pg_destroy(pg_ctx* c) {
         if (c->lev[i]) cudaEventDestroy(c->lev[i]);
     }
     for (cudaEvent_t e : c->run_ev) cudaEventDestroy(e);
+    if (c->fork) cudaEventDestroy(c->fork);
+    if (c->join) cudaEventDestroy(c->join);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
