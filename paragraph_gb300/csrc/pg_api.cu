@@ -755,7 +755,7 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
         launch_rc_agents(A, agents, c->num_sms, s);
         PG_STAGE("refcompat agents");
         if (events) record_event(ev[3], s);
-        launch_bwd_append(A, agents, c->num_sms, s);
+        launch_bwd_append(A, agents, c->num_sms, s, c->side, c->fork, c->join);
         PG_STAGE("backward append");
         if (events) record_event(ev[4], s);
         c->launches += kPaEpochKernels - 4 - 2 + kRcScoreKernels + 1;
@@ -791,7 +791,7 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
     launch_agents(A, agents, c->num_sms, s);
     PG_STAGE("agents");
     if (events) record_event(ev[3], s);
-    launch_bwd_append(A, agents, c->num_sms, s);
+    launch_bwd_append(A, agents, c->num_sms, s, c->side, c->fork, c->join);
     PG_STAGE("backward append");
     if (events) record_event(ev[4], s);
 #undef PG_STAGE
@@ -1360,7 +1360,7 @@ pg_status pg_er_epoch(pg_ctx* c, int64_t delta, double p, int64_t* new_edges) {
     launch_epoch_begin_delta(A, c->epoch, delta, st);
     launch_er_epoch(A, delta, p, n, c->er_cnt.p, c->er_toff.p, c->num_sms, st);
     if (c->timing) cudaEventRecord(c->ev[1], st);
-    launch_bwd_append(A, delta, c->num_sms, st);
+    launch_bwd_append(A, delta, c->num_sms, st, c->side, c->fork, c->join);
     if (c->timing) cudaEventRecord(c->ev[2], st);
     PG_CUDA(c, cudaGetLastError());
     std::vector<int64_t> deltas(1, delta);

@@ -360,18 +360,28 @@ cudaError_t init_csr_kernels() {
                                 kBitmapWords * 4);
 }
 
-void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) {
+void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s, cudaStream_t side,
+                       cudaEvent_t fork, cudaEvent_t join) {
     k_bwd_len<<<A.ntiles, kTileThreads, 0, s>>>(A);
     launch_tile_scan(A, 1, s);
     k_bwd_off<<<A.ntiles, kTileThreads, 0, s>>>(A);
     const int copy_per_sm = A.tune_copy_ctas > 0 ? A.tune_copy_ctas : 8;
-    k_bwd_copy<<<(unsigned)(num_sms * copy_per_sm), 256, 0, s>>>(A);
+    // the old entries' copy and the new entries' placement and sorts write disjoint positions of
+    // the next backward CSR: with a side stream they overlap
+    const bool two = side && fork && join;
+    if (two) {
+        cudaEventRecord(fork, s);
+        cudaStreamWaitEvent(side, fork, 0);
+    }
+    k_bwd_copy<<<(unsigned)(num_sms * copy_per_sm), 256, 0, two ? side : s>>>(A);
+    if (two) cudaEventRecord(join, side);
     int64_t ga = (agents + 7) / 8;
     if (ga > (int64_t)num_sms * 16) ga = (int64_t)num_sms * 16;
     if (ga < 1) ga = 1;
     k_bwd_place<<<(unsigned)ga, 256, 0, s>>>(A, agents);
     k_sort_small<<<(unsigned)num_sms * 8, 256, 0, s>>>(A);
     k_sort_large<<<(unsigned)num_sms, 1024, kBitmapWords * 4, s>>>(A);
+    if (two) cudaStreamWaitEvent(s, join, 0);
     k_epoch_end<<<1, 256, 0, s>>>(A, agents);
 }
 

@@ -317,7 +317,9 @@ void launch_guide(const Arena& A, cudaStream_t s);
 void launch_tile_scan(const Arena& A, int mode, cudaStream_t s);
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s);
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
-void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
+// side/fork/join (optional): the old-entry copy runs on `side` beside the new-entry placement and sorts
+void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s, cudaStream_t side = nullptr,
+                       cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 // refcompat functor: score components of the epoch (4 kernels) and the agent kernel
 constexpr int kRcScoreKernels = 4;
 void launch_rc_scores(const Arena& A, cudaStream_t s);
