@@ -7,12 +7,13 @@
 // Forward rows of new nodes were written by the agent kernel (append-only, sorted).  Backward rows
 // are rebuilt into the other buffer:
 //   len  : new_len = old_len + inc (inc = in-degree histogram of the epoch, filled by atomics in
-//          the agent kernel, which also returned each edge's rank); indeg += inc
+//          the agent kernel, which also returned each edge's rank); indeg += inc; the rows whose
+//          span starts a copy tile are recorded
 //   scan : per-replica exclusive scan of new_len -> new int64 offsets
-//   copy : old rows moved with one warp per 32 rows (load-balanced over the concatenated rows)
+//   copy : old entries moved in tiles of kCopyTile positions (on a side stream, beside place/sort)
 //   place: each new edge at new_off + old_len + rank
 //   sort : the appended part of a row holds distinct new-node ids in atomic order; rows with up to
-//          32 new entries are sorted by a register bitonic network in one warp, longer ones by a
+//          256 new entries are sorted by a register bitonic network in one warp, longer ones by a
 //          shared-memory bitmap over the epoch's new-id range.  Rows end up ascending, like the
 //          reference's std::set rows, and bit-identical run to run.
 #include "pg_engine.cuh"
