@@ -410,6 +410,24 @@ __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
     }
     A.indeg[slot] = 0;
     int heavy = 0;
+    if (rc && k >= 2) {
+        // a generator with many row entries makes a long 2-hop stream: such agents are listed for
+        // the CTA-wide pass (k_rc_big), mark = list slot + 1
+        double w3[3], alpha;
+        int32_t gen;
+        rc_agent_params(A.seed, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, rp.n, rp.rc_w, rp.rc_alpha, w3,
+                        &alpha, &gen);
+        const int64_t* fo = A.fwd_off + rp.obase;
+        const int64_t* bo = A.bwd_off_cur + rp.obase;
+        const int64_t gd = (fo[gen + 1] - fo[gen]) + (bo[gen + 1] - bo[gen]);
+        if (gd >= kRcBigGd) {
+            const unsigned long long q = atomicAdd(&A.st->rc_big_count, 1ull);
+            if (q < (unsigned long long)kRcBigCap) {
+                A.heavy_list[q] = (int32_t)a;
+                heavy = (int)q + 1;
+            }
+        }
+    }
     if (!rc && A.sampler == kSamplerThinning && rp.p_global < 1.0) {
         // the anchors (the same draw the agent kernel makes): flag the hubs among them, whose
         // hub-pair rows are the only ones read, and mark the agent heavy when an anchor is a hub or
@@ -545,6 +563,88 @@ __global__ void __launch_bounds__(kAgentWarps * 32) k_agents_rc(Arena A, int64_t
         if (q >= agents) break;
         process_agent_rc(A, q, A.kk[q], S);
     }
+}
+
+// The 2-hop streams of the refcompat agents the setup listed (long generator rows), one CTA per
+// agent: the warps take the 32-entry chunks of every group's stream in turn, each keeping its own top
+// min(k, kKMax) of its part of the stream with the keys, validity and duplicate rule of the
+// one-warp path; warp 0 merges the lists (dropping entries that two warps both reached) and stores
+// the sorted ids and the stream's counters for k_agents_rc.
+constexpr int kRcBigWarps = 8;
+
+__global__ void __launch_bounds__(kRcBigWarps * 32) k_rc_big(Arena A) {
+    __shared__ RcSmem sm[kRcBigWarps];
+    __shared__ int s_nb[kRcBigWarps];
+    __shared__ long long s_cnt[2];
+    __shared__ long long s_item;
+    if (A.st->error) return;
+    const int warp = threadIdx.x >> 5, lane = lane_id();
+    RcSmem& S = sm[warp];
+    const long long listed = (long long)A.st->rc_big_count;
+    const long long total = listed < kRcBigCap ? listed : kRcBigCap;
+    while (true) {
+        if (threadIdx.x == 0) s_item = (long long)atomicAdd(&A.st->rc_big_queue, 1ull);
+        if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0;
+        __syncthreads();
+        const long long it = s_item;
+        if (it >= total) break;
+        const int64_t a = A.heavy_list[it];
+        const int r = replica_of_agent(A.rep, A.R, a);
+        const Replica& rp = A.rep[r];
+        const int64_t al = a - rp.abase;
+        RcCtx X;
+        X.fo = A.fwd_off + rp.obase;
+        X.fc = A.fwd_col + rp.ebase;
+        X.bo = A.bwd_off_cur + rp.obase;
+        X.bc = A.bwd_col_cur + rp.ebase;
+        X.pa = A.rc_pa + rp.nbase;
+        X.rec = A.rc_rec + rp.nbase;
+        X.fit = A.rc_fit + rp.nbase;
+        X.seed = A.seed;
+        X.rep = (uint32_t)(r + A.rep_base);
+        X.ep = (uint32_t)A.st->epoch;
+        X.unit = (uint32_t)al;
+        double alpha;
+        rc_agent_params(A.seed, X.rep, X.ep, X.unit, rp.n, rp.rc_w, rp.rc_alpha, X.w3, &alpha, &X.gen);
+        X.gf0 = X.fo[X.gen];
+        X.glf = X.fo[X.gen + 1] - X.gf0;
+        X.gb0 = X.bo[X.gen];
+        X.gd = X.glf + (X.bo[X.gen + 1] - X.gb0);
+        const int k = A.kk[a];
+        const int kcap = k < kKMax ? k : kKMax;
+        int nb = 0;
+        long long rows = 0, elems = 0;
+        rc_2hop_slice(X, 32 * warp, 32 * kRcBigWarps, warp == 0, kcap, nb, rows, elems, S);
+        if (lane == 0) {
+            s_nb[warp] = nb;
+            atomicAdd((unsigned long long*)&s_cnt[0], (unsigned long long)rows);
+            atomicAdd((unsigned long long*)&s_cnt[1], (unsigned long long)elems);
+        }
+        __syncthreads();
+        if (warp == 0) {
+            for (int w = 1; w < kRcBigWarps; ++w) {
+                const int nw = s_nb[w];
+                for (int q0 = 0; q0 < nw; q0 += 32) {
+                    const int q = q0 + lane;
+                    const bool v = q < nw;
+                    rc_topk_offer(v, v ? sm[w].bk[q] : 0.0f, v ? sm[w].bi[q] : 0, kcap, nb, S);
+                }
+            }
+            int32_t* ids = A.rc_big_id + it * kKMax;
+            for (int q = lane; q < nb; q += 32) ids[q] = S.bi[q];
+            if (lane == 0) {
+                long long* meta = A.rc_big_meta + it * 3;
+                meta[0] = nb;
+                meta[1] = s_cnt[0];
+                meta[2] = s_cnt[1];
+            }
+        }
+        __syncthreads();  // the lists and counters are reused by the next agent
+    }
+}
+
+void launch_rc_big(const Arena& A, int num_sms, cudaStream_t s) {
+    k_rc_big<<<(unsigned)num_sms * 2, kRcBigWarps * 32, 0, s>>>(A);
 }
 
 static int g_blocks_rc = 0;

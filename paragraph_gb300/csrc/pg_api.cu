@@ -110,6 +110,8 @@ struct pg_ctx {
     DBuf<int32_t> src_tmp;  // sources of an edge range being copied out
     // refcompat functor
     DBuf<double> rc_pa, rc_rec, rc_fit, rc_rtab, rc_agent;
+    DBuf<int32_t> rc_big_id;
+    DBuf<long long> rc_big_meta;
     DBuf<int32_t> rc_lag, rc_dur, rc_cnt;
     DBuf<uint64_t> rc_ftab;
     DBuf<unsigned long long> rc_acc;
@@ -249,6 +251,8 @@ Arena make_arena(pg_ctx* c) {
     A.rc_acc = c->rc_acc.p;
     A.rc_cnt = c->rc_cnt.p;
     A.rc_agent = c->rc_agent.p;
+    A.rc_big_id = c->rc_big_id.p;
+    A.rc_big_meta = c->rc_big_meta.p;
     return A;
 }
 
@@ -528,6 +532,10 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->hlist, (int64_t)R * kHeavyMax));
     if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
         PG_CUDA(c, dalloc(c->rc_pa, S));
+        if (!c->rc_big_id.p) {
+            PG_CUDA(c, dalloc(c->rc_big_id, (int64_t)kRcBigCap * kKMax));
+            PG_CUDA(c, dalloc(c->rc_big_meta, (int64_t)kRcBigCap * 3));
+        }
         PG_CUDA(c, dalloc(c->rc_rec, S));
         PG_CUDA(c, dalloc(c->rc_fit, S));
         PG_CUDA(c, dalloc(c->rc_lag, S));
@@ -752,13 +760,14 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
         launch_agent_setup(A, agents, s);
         PG_STAGE("agent setup");
         if (events) record_event(ev[2], s);
+        launch_rc_big(A, c->num_sms, s);
         launch_rc_agents(A, agents, c->num_sms, s);
         PG_STAGE("refcompat agents");
         if (events) record_event(ev[3], s);
         launch_bwd_append(A, agents, c->num_sms, s, c->side, c->fork, c->join);
         PG_STAGE("backward append");
         if (events) record_event(ev[4], s);
-        c->launches += kPaEpochKernels - 4 - 2 + kRcScoreKernels + 1;
+        c->launches += kPaEpochKernels - 4 - 2 + kRcScoreKernels + 2;
         return PG_OK;
     }
     // the hub index reads only the CSR and the weights and guide table only node attributes: the
@@ -999,6 +1008,8 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->rc_fit);
     dfree(c->rc_rtab);
     dfree(c->rc_agent);
+    dfree(c->rc_big_id);
+    dfree(c->rc_big_meta);
     dfree(c->rc_lag);
     dfree(c->rc_dur);
     dfree(c->rc_cnt);

@@ -25,6 +25,8 @@ constexpr int kErChunk = 65536;      // ids per ER Philox stream
 constexpr int kSortMid = 256;        // appended segments up to this length sort in one warp's registers
 constexpr int kBitmapWords = 40960;  // 160 KiB of shared bitmap in the large-segment sort
 #define PG_MAX_ANCHORS_DEV 4
+constexpr int kRcBigGd = 64;         // refcompat generators with this many row entries: a CTA per 2-hop stream
+constexpr int kRcBigCap = 16384;     // such agents per epoch (the rest keep the one-warp path)
 constexpr int kGBits = 13;           // per-warp global hash for anchor rows too large for shared memory
 constexpr int kZCap = 1024;          // 1-hop frontier entries kept in shared memory per warp
 constexpr int kCopyTile = 4096;      // backward entries per copy tile
@@ -96,6 +98,7 @@ struct EpochState {
     unsigned long long queue_big;
     unsigned long long big_count;
     unsigned long long heavy_count;  // agents the small thinning kernel takes first
+    unsigned long long rc_big_count, rc_big_queue;  // refcompat agents with a CTA-wide 2-hop pass
     unsigned long long sort_small_count;
     unsigned long long sort_large_count;
     unsigned long long sort_scratch;
@@ -150,6 +153,8 @@ struct Arena {
     int32_t* heavy_list;       // [agent cap] agents with a hub or a large frontier (k <= kKSmall)
     int32_t* heavy_mark;       // [agent cap] 1 when the agent is on heavy_list
     int32_t* zbig;             // [agent-kernel warp slots][1 << kGBits] rows of anchors too large for H
+    int32_t* rc_big_id;        // [kRcBigCap][kKMax] sorted top of each listed refcompat agent's 2-hop stream
+    long long* rc_big_meta;    // [kRcBigCap][3] entries, rows, elements of that stream
     int32_t* tile_row;         // [copy tiles] row holding the first position of each copy tile
     int64_t* len_tmp;          // [slots]
     uint64_t* tilesum;         // [ntiles]
@@ -323,6 +328,7 @@ void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t
 // refcompat functor: score components of the epoch (4 kernels) and the agent kernel
 constexpr int kRcScoreKernels = 4;
 void launch_rc_scores(const Arena& A, cudaStream_t s);
+void launch_rc_big(const Arena& A, int num_sms, cudaStream_t s);
 void launch_rc_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
 cudaError_t init_rc_kernels();
 void launch_er_epoch(const Arena& A, int64_t delta, double p, int64_t n, int64_t* cnt,

@@ -29,6 +29,8 @@ __global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, in
         st->queue_big = 0;
         st->big_count = 0;
         st->heavy_count = 0;
+        st->rc_big_count = 0;
+        st->rc_big_queue = 0;
         st->sort_small_count = 0;
         st->sort_large_count = 0;
         st->sort_scratch = 0;

@@ -66,6 +66,35 @@ def test_refcompat_bit_exact(gpu, case):
             _compare(eng, og)
 
 
+def test_refcompat_long_generator_rows_bit_exact(gpu):
+    """Generators with 64 or more row entries: their agents' 2-hop streams are walked by a whole CTA
+    (warps splitting the generator's groups, their top lists merged) before the agent kernel."""
+    base = W.rc_seed(3000, 10, seed=4)
+    rng = np.random.default_rng(8)
+    pop = rng.choice(3000, 400, replace=False)
+    extra = rng.integers(60, 260, size=400)
+    src = np.concatenate([base.src] + [rng.integers(0, 3000, size=d).astype(np.int32) for d in extra])
+    dst = np.concatenate([base.dst] + [np.full(d, v, np.int32) for v, d in zip(pop, extra)])
+    keep = src != dst
+    g = W.SeedGraph(base.pub, base.fitness, src[keep], dst[keep])
+    bag, rec = W.rc_tables(seed=6, bag_mean=30.0)
+    rc = RCParams(growth_rate=0.08, same_year=0.1)
+    eng, og = _run_both(g, rc, bag, rec, 3)
+    with eng:
+        for _ in range(3):
+            eng.grow_epoch()
+            og.rc_epoch()
+            np.testing.assert_array_equal(eng.arrivals(), og.arrivals())
+            np.testing.assert_array_equal(eng.rc_agents(), og.rc_agents())
+            st, so = eng.stats(), og.stats()
+            for k in ("rows_expanded", "elems_streamed", "draws"):
+                assert st[k] == so[k], k
+            _compare(eng, og)
+        ind, outd = eng.degrees()
+        gens = eng.rc_agents()[:, 4].astype(np.int64)
+        assert ((ind + outd)[gens] >= 64).sum() > 10  # the CTA-wide path was taken
+
+
 def test_refcompat_planted_papers_and_checkpoint(gpu):
     g = W.rc_seed(2000, 8, seed=9)
     bag, rec = W.rc_tables(seed=2, bag_mean=20.0)
