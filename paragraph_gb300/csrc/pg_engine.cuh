@@ -25,7 +25,7 @@ constexpr int kErChunk = 65536;      // ids per ER Philox stream
 constexpr int kSortMid = 256;        // appended segments up to this length sort in one warp's registers
 constexpr int kBitmapWords = 40960;  // 160 KiB of shared bitmap in the large-segment sort
 #define PG_MAX_ANCHORS_DEV 4
-constexpr int kRcBigGd = 64;         // refcompat generators with this many row entries: a CTA per 2-hop stream
+constexpr int kRcBigGd = 32;         // refcompat generators with this many row entries: a CTA per 2-hop stream
 constexpr int kRcBigCap = 16384;     // such agents per epoch (the rest keep the one-warp path)
 constexpr int kGBits = 13;           // per-warp global hash for anchor rows too large for shared memory
 constexpr int kZCap = 1024;          // 1-hop frontier entries kept in shared memory per warp

@@ -67,7 +67,7 @@ def test_refcompat_bit_exact(gpu, case):
 
 
 def test_refcompat_long_generator_rows_bit_exact(gpu):
-    """Generators with 64 or more row entries: their agents' 2-hop streams are walked by a whole CTA
+    """Generators with 32 or more row entries: their agents' 2-hop streams are walked by a whole CTA
     (warps splitting the generator's groups, their top lists merged) before the agent kernel."""
     base = W.rc_seed(3000, 10, seed=4)
     rng = np.random.default_rng(8)
@@ -92,7 +92,7 @@ def test_refcompat_long_generator_rows_bit_exact(gpu):
             _compare(eng, og)
         ind, outd = eng.degrees()
         gens = eng.rc_agents()[:, 4].astype(np.int64)
-        assert ((ind + outd)[gens] >= 64).sum() > 10  # the CTA-wide path was taken
+        assert ((ind + outd)[gens] >= 32).sum() > 10  # the CTA-wide path was taken
 
 
 def test_refcompat_planted_papers_and_checkpoint(gpu):
