@@ -68,7 +68,8 @@ def test_refcompat_bit_exact(gpu, case):
 
 def test_refcompat_long_generator_rows_bit_exact(gpu):
     """Generators with 32 or more row entries: their agents' 2-hop streams are walked by a whole CTA
-    (warps splitting the generator's groups, their top lists merged) before the agent kernel."""
+    (warps splitting each group's stream by 32-entry chunks, their top lists merged) before the
+    agent kernel."""
     base = W.rc_seed(3000, 10, seed=4)
     rng = np.random.default_rng(8)
     pop = rng.choice(3000, 400, replace=False)
