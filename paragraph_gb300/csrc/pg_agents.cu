@@ -568,7 +568,8 @@ __global__ void __launch_bounds__(kAgentWarps * 32) k_agents_rc(Arena A, int64_t
 // The 2-hop streams of the refcompat agents the setup listed (long generator rows), one CTA per
 // agent: the warps take the 32-entry chunks of every group's stream in turn, each keeping its own top
 // min(k, kKMax) of its part of the stream with the keys, validity and duplicate rule of the
-// one-warp path; warp 0 merges the lists (dropping entries that two warps both reached) and stores
+// one-warp path; the lists are merged pairwise (dropping entries that two warps both reached; the
+// k smallest distinct (key, id) pairs do not depend on the merge order) and warp 0 stores
 // the sorted ids and the stream's counters for k_agents_rc.
 constexpr int kRcBigWarps = 8;
 
@@ -621,15 +622,21 @@ __global__ void __launch_bounds__(kRcBigWarps * 32) k_rc_big(Arena A) {
             atomicAdd((unsigned long long*)&s_cnt[1], (unsigned long long)elems);
         }
         __syncthreads();
-        if (warp == 0) {
-            for (int w = 1; w < kRcBigWarps; ++w) {
+        // pairwise merges, log2(warps) rounds: warp w takes warp w + h's list when w % 2h == 0
+        for (int h = 1; h < kRcBigWarps; h <<= 1) {
+            if ((warp & (2 * h - 1)) == 0) {
+                const int w = warp + h;
                 const int nw = s_nb[w];
                 for (int q0 = 0; q0 < nw; q0 += 32) {
                     const int q = q0 + lane;
                     const bool v = q < nw;
                     rc_topk_offer(v, v ? sm[w].bk[q] : 0.0f, v ? sm[w].bi[q] : 0, kcap, nb, S);
                 }
+                if (lane == 0) s_nb[warp] = nb;
             }
+            __syncthreads();
+        }
+        if (warp == 0) {
             int32_t* ids = A.rc_big_id + it * kKMax;
             for (int q = lane; q < nb; q += 32) ids[q] = S.bi[q];
             if (lane == 0) {

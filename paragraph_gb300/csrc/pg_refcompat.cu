@@ -27,6 +27,10 @@ __device__ __forceinline__ void add128(uint64_t& hi, uint64_t& lo, uint64_t h2, 
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_rc_node(Arena A) {
+    // The age histogram and the 128-bit sums are gathered per CTA in shared memory, then added
+    // to the replica's totals once per CTA (integer sums: the order does not change them).
+    __shared__ int s_age[kRcAgeMax];
+    __shared__ unsigned long long s_sum[kTileThreads / 32][4];
     if (A.st->error) return;
     const int t = blockIdx.x;
     const int r = A.tile_rep[t];
@@ -34,6 +38,9 @@ __global__ void __launch_bounds__(kTileThreads) k_rc_node(Arena A) {
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
     if (v0 >= rp.n) return;
     const int64_t ep = A.st->epoch;
+    const int rec_len = rp.rc_rec_len;
+    for (int i = threadIdx.x; i < rec_len; i += kTileThreads) s_age[i] = 0;
+    __syncthreads();
     uint64_t sph = 0, spl = 0, sfh = 0, sfl = 0;
 #pragma unroll
     for (int i = 0; i < kTile / kTileThreads; ++i) {
@@ -50,9 +57,8 @@ __global__ void __launch_bounds__(kTileThreads) k_rc_node(Arena A) {
         add128(sph, spl, ah, alo);
         add128(sfh, sfl, fh, flo);
         const int64_t age = ep - A.pub[slot];
-        if (age >= 0 && age < rp.rc_rec_len) atomicAdd(&A.rc_cnt[(int64_t)r * kRcAgeMax + age], 1);
+        if (age >= 0 && age < rec_len) atomicAdd(&s_age[age], 1);
     }
-    // warp sums, then one exact 128-bit atomic accumulation per warp
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
         const uint64_t a = __shfl_xor_sync(0xffffffffu, sph, d), b = __shfl_xor_sync(0xffffffffu, spl, d);
@@ -61,6 +67,18 @@ __global__ void __launch_bounds__(kTileThreads) k_rc_node(Arena A) {
         add128(sfh, sfl, c, e);
     }
     if (lane_id() == 0) {
+        unsigned long long* w = s_sum[threadIdx.x >> 5];
+        w[0] = spl;
+        w[1] = sph;
+        w[2] = sfl;
+        w[3] = sfh;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kTileThreads / 32; ++w) {
+            add128(sph, spl, s_sum[w][1], s_sum[w][0]);
+            add128(sfh, sfl, s_sum[w][3], s_sum[w][2]);
+        }
         unsigned long long* acc = A.rc_acc + (int64_t)r * 4;
         const unsigned long long o0 = atomicAdd(&acc[0], (unsigned long long)spl);
         if (o0 + spl < o0) atomicAdd(&acc[1], 1ull);
@@ -69,6 +87,8 @@ __global__ void __launch_bounds__(kTileThreads) k_rc_node(Arena A) {
         if (o2 + sfl < o2) atomicAdd(&acc[3], 1ull);
         atomicAdd(&acc[3], (unsigned long long)sfh);
     }
+    for (int i = threadIdx.x; i < rec_len; i += kTileThreads)
+        if (s_age[i]) atomicAdd(&A.rc_cnt[(int64_t)r * kRcAgeMax + i], s_age[i]);
 }
 
 __global__ void k_rc_norm(Arena A) {
