@@ -411,8 +411,8 @@ __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
     A.indeg[slot] = 0;
     int heavy = 0;
     if (rc && k >= 2) {
-        // a generator with many row entries makes a long 2-hop stream: such agents are listed for
-        // the CTA-wide pass (k_rc_big), mark = list slot + 1
+        // a generator with many row entries, or a few long ones, makes a long 2-hop stream: such
+        // agents are listed for the CTA-wide pass (k_rc_big), mark = list slot + 1
         double w3[3], alpha;
         int32_t gen;
         rc_agent_params(A.seed, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, rp.n, rp.rc_w, rp.rc_alpha, w3,
@@ -420,7 +420,22 @@ __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
         const int64_t* fo = A.fwd_off + rp.obase;
         const int64_t* bo = A.bwd_off_cur + rp.obase;
         const int64_t gd = (fo[gen + 1] - fo[gen]) + (bo[gen + 1] - bo[gen]);
-        if (gd >= kRcBigGd) {
+        bool big = gd >= kRcBigGd;
+        if (!big) {
+            const int32_t* fc = A.fwd_col + rp.ebase;
+            const int32_t* bc = A.bwd_col_cur + rp.ebase;
+            int64_t len = 0;
+            for (int64_t e = fo[gen]; e < fo[gen + 1]; ++e) {
+                const int32_t y = fc[e];
+                len += (fo[y + 1] - fo[y]) + (bo[y + 1] - bo[y]);
+            }
+            for (int64_t e = bo[gen]; e < bo[gen + 1]; ++e) {
+                const int32_t y = bc[e];
+                len += (fo[y + 1] - fo[y]) + (bo[y + 1] - bo[y]);
+            }
+            big = len >= kRcBigStream;
+        }
+        if (big) {
             const unsigned long long q = atomicAdd(&A.st->rc_big_count, 1ull);
             if (q < (unsigned long long)kRcBigCap) {
                 A.heavy_list[q] = (int32_t)a;

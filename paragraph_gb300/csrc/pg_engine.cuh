@@ -26,6 +26,7 @@ constexpr int kSortMid = 256;        // appended segments up to this length sort
 constexpr int kBitmapWords = 40960;  // 160 KiB of shared bitmap in the large-segment sort
 #define PG_MAX_ANCHORS_DEV 4
 constexpr int kRcBigGd = 32;         // refcompat generators with this many row entries: a CTA per 2-hop stream
+constexpr int kRcBigStream = 1024;  // ... or a 2-hop stream (the rows of the generator's rows) this long
 constexpr int kRcBigCap = 16384;     // such agents per epoch (the rest keep the one-warp path)
 constexpr int kGBits = 13;           // per-warp global hash for anchor rows too large for shared memory
 constexpr int kZCap = 1024;          // 1-hop frontier entries kept in shared memory per warp

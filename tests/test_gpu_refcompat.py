@@ -28,6 +28,21 @@ def _run_both(g, rc, bag, rec, epochs, seed=77, planted=None):
     return eng, og
 
 
+# cut-offs of the CTA-wide 2-hop pass: generator row entries, entries of the generator's rows' rows
+_BIG_GD, _BIG_STREAM = 32, 1024
+
+
+def _row_stats(og):
+    """Per node of the current graph: row entries and the length of its 2-hop stream."""
+    ind, outd = og.degrees()
+    deg = (ind + outd).astype(np.int64)
+    stream = np.zeros(len(deg), np.int64)
+    for which in (0, 1):
+        off, col = og.csr(which)
+        np.add.at(stream, np.repeat(np.arange(len(off) - 1), np.diff(off)), deg[col])
+    return deg, stream
+
+
 def _compare(eng, og):
     assert eng.counts() == (og.n, og.m)
     for which in (0, 1):
@@ -53,10 +68,16 @@ def test_refcompat_bit_exact(gpu, case):
     rc = RCParams(pa_weight=case["w"][0], rec_weight=case["w"][1], fit_weight=case["w"][2],
                   alpha=case["alpha"], same_year=case["same_year"], growth_rate=case["growth"])
     eng, og = _run_both(g, rc, bag, rec, case["epochs"])
+    routes = np.zeros(2, np.int64)  # agents with a 2-hop stream: one warp, a CTA
     with eng:
         for _ in range(case["epochs"]):
+            deg, stream = _row_stats(og)
             nn, ne = eng.grow_epoch()
             og.rc_epoch()
+            ag = og.rc_agents()
+            gen = ag[ag[:, 5] >= 2, 4].astype(np.int64)
+            cta = (deg[gen] >= _BIG_GD) | (stream[gen] >= _BIG_STREAM)
+            routes += (int((~cta).sum()), int(cta.sum()))
             assert ne == og.epoch_edges()[1]
             np.testing.assert_array_equal(eng.arrivals(), og.arrivals())
             np.testing.assert_array_equal(eng.rc_agents(), og.rc_agents())
@@ -64,12 +85,14 @@ def test_refcompat_bit_exact(gpu, case):
             for k in ("rows_expanded", "elems_streamed", "draws", "nodes_weighted"):
                 assert st[k] == so[k], k
             _compare(eng, og)
+    if case["n0"] >= 400:
+        assert routes.min() > 0, routes  # both routes of the 2-hop walk were checked
 
 
 def test_refcompat_long_generator_rows_bit_exact(gpu):
-    """Generators with 32 or more row entries: their agents' 2-hop streams are walked by a whole CTA
-    (warps splitting each group's stream by 32-entry chunks, their top lists merged) before the
-    agent kernel."""
+    """Generators with 32 or more row entries, or whose rows' rows hold 1024 or more entries: their
+    agents' 2-hop streams are walked by a whole CTA (warps splitting each group's stream by 32-entry
+    chunks, their top lists merged) before the agent kernel."""
     base = W.rc_seed(3000, 10, seed=4)
     rng = np.random.default_rng(8)
     pop = rng.choice(3000, 400, replace=False)
@@ -93,7 +116,7 @@ def test_refcompat_long_generator_rows_bit_exact(gpu):
             _compare(eng, og)
         ind, outd = eng.degrees()
         gens = eng.rc_agents()[:, 4].astype(np.int64)
-        assert ((ind + outd)[gens] >= 32).sum() > 10  # the CTA-wide path was taken
+        assert ((ind + outd)[gens] >= _BIG_GD).sum() > 10  # the CTA-wide path was taken
 
 
 def test_refcompat_planted_papers_and_checkpoint(gpu):
