@@ -580,7 +580,7 @@ __global__ void __launch_bounds__(kAgentWarps * 32) k_agents_rc(Arena A, int64_t
     }
 }
 
-// The 2-hop streams of the refcompat agents the setup listed (long generator rows), one CTA per
+// The 2-hop streams of the refcompat agents the setup listed (long streams), one CTA per
 // agent: the warps take the 32-entry chunks of every group's stream in turn, each keeping its own top
 // min(k, kKMax) of its part of the stream with the keys, validity and duplicate rule of the
 // one-warp path; the lists are merged pairwise (dropping entries that two warps both reached; the
