@@ -217,8 +217,11 @@ void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t
         k_unique_compact<<<grid, 256, 0, s>>>(sorted, m, flag, pos, bits, uk, fc, fcnt);
         // number of unique edges
         cudaMemcpyAsync(u_out, pos + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        u = *u_out;
+        u = cudaStreamSynchronize(s) == cudaSuccess ? *u_out : 0;
+        // at most m unique edges; anything else means the sequence above failed (the caller reports
+        // the error), and the count must not size the next sort
+        if (u < 0 || u > m) u = 0;
+        *u_out = u;
         if (u > 0) {
             unsigned long long* other = sorted == k0 ? k1 : k0;
             unsigned long long* bsorted = radix_sort(uk, other, u, 0, bits, hist, off, blocksum, s);
