@@ -176,6 +176,12 @@ PG_HD double rint_(double x) {
 }
 
 // ---------------------------------------------------------------- fp32 exp / log
+// The library's own elementary functions, the same code on host and device so that keys and
+// weights are bit-identical in the oracle.  exp: Cody-Waite reduction x = k ln2 + r with ln 2 split
+// into a high and a low part, then the Taylor series of e^r (coefficients 1/n!) by Horner's rule
+// and the scale 2^k.  log: x = 2^e m with m in (sqrt(2)/2, sqrt(2)], then
+// log m = 2 atanh(s) = 2 (s + s^3/3 + s^5/5 + ...) with s = (m - 1)/(m + 1), plus e ln 2.
+// The CPU tests hold them within 2 ulp of the correctly rounded values.
 constexpr float kLog2eF = 0x1.715476p+0f;
 constexpr float kLn2HiF = 0x1.62e430p-1f;
 constexpr float kLn2LoF = -0x1.05c610p-29f;
