@@ -3,6 +3,9 @@
 The scores use exact 128-bit integer sums, the keys and the uniform fill the same Philox streams,
 so the bar is bit-exact: both CSRs, in-degrees, new-paper attributes, citations in arrival order,
 the per-paper draws (weights, alpha, generator, out-degree) and the counters."""
+import re
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -28,8 +31,13 @@ def _run_both(g, rc, bag, rec, epochs, seed=77, planted=None):
     return eng, og
 
 
+def _engine_constant(name):
+    src = (Path(__file__).resolve().parents[1] / "paragraph_gb300" / "csrc" / "pg_engine.cuh").read_text()
+    return int(re.search(rf"constexpr int {name} = (\d+);", src).group(1))
+
+
 # cut-offs of the CTA-wide 2-hop pass: generator row entries, entries of the generator's rows' rows
-_BIG_GD, _BIG_STREAM = 32, 1024
+_BIG_GD, _BIG_STREAM = _engine_constant("kRcBigGd"), _engine_constant("kRcBigStream")
 
 
 def _row_stats(og):
