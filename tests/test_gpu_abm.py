@@ -1,7 +1,7 @@
 """The `abm` driver end to end on the GPU: reference-format input files in, reference-format edge
 list and attribute file out, checked against the CPU oracle grown from the same inputs.
 
-The driver draws the seed papers' fitness itself and writes it to the attribute file
+The `abm` program draws the seed papers' fitness itself and writes it to the attribute file
 (fit_peak_value), so the oracle is seeded from that column; ids are mapped as the reference maps
 them (sequence ids in ascending original id, new papers max id + 1, + 2, ...)."""
 import subprocess
