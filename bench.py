@@ -147,6 +147,15 @@ def reduce_sum(dist, x: float) -> float:
     return float(t.item())
 
 
+def workload_config(g) -> dict:
+    """The workload as both arms name it (the reference arm times a bounded sample of it, stated in
+    its cpu_baseline.sample)."""
+    return {"workload": WORKLOAD, "seed_nodes": g.n, "seed_citations": g.m,
+            "epochs_per_step": EPOCHS, "growth": 0.03, "mean_out_degree": 30,
+            "alpha": 1.0, "tau": 5.0, "gamma": 1.0, "beta": 4.0, "anchors": 3,
+            "l2": "inputs larger than L2 (CSR 0.5-0.9 GB)", "parallelism": "replicas only"}
+
+
 def seed_graph(seed: int):
     from paragraph_gb300 import workloads as W
 
@@ -167,7 +176,7 @@ def traffic_per_agent_byte() -> float | None:
 
 # ------------------------------------------------------------------ CPU legs (oracle)
 def cpu_sample(g, prm, seed: int, max_epochs: int = 3, budget_s: float = 12.0,
-               sampler: int = 1) -> dict:
+               sampler: int = 1, threads: int = 0) -> dict:
     """Time the OpenMP oracle (all host threads) on the first epochs of the workload.
 
     sampler 1 (default) is the reference's algorithm -- enumerate each agent's 2-hop neighbourhood
@@ -179,7 +188,7 @@ def cpu_sample(g, prm, seed: int, max_epochs: int = 3, budget_s: float = 12.0,
     og.load(g.pub, g.fitness, g.src, g.dst)
     og.set_params(**prm.__dict__)
     og.set_sampler(sampler)
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     edges, secs, epochs = 0, 0.0, 0
     while epochs < max_epochs and (epochs == 0 or secs < budget_s):
         m0 = og.m
@@ -231,11 +240,14 @@ def run_reference(args) -> None:
             "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32/u64/f32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "step": "epoch 0 of the workload from the seed",
-                       "parallelism": "replicas only"},
+            "config": workload_config(g),
             "cpu_baseline": {"value": v, "unit": "citations/s", "cores": threads, "kind": "port",
-                             "sample": "epoch 0 of the workload per step; CPU oracle (the "
-                                       "reference cannot be built: cuCollections is absent)"},
+                             "sample": "epoch 0 of the workload per step (the 30-epoch step is "
+                                       "out of reach: the enumerated 2-hop balls grow to millions "
+                                       "of nodes per agent), the reference's algorithm (2-hop "
+                                       "enumeration, ES top-k) in the CPU oracle on all host "
+                                       "threads; the reference itself cannot be built "
+                                       "(cuCollections is absent)"},
             "e2e": {"value": v, "unit": "citations/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "gpu_launches": 0}
@@ -315,6 +327,8 @@ def run_ours(args) -> None:
 
     if rank != 0:
         eng.close()
+        if not args.no_extra:
+            extra_lines(args, world, rank, local, dist)
         return
     peak, peak_kind = peaks()
     achieved = agents_bytes / (agents_ms / 1000.0) / 1e9 if agents_ms > 0 else 0.0
@@ -325,10 +339,7 @@ def run_ours(args) -> None:
         "value": value, "unit": "citations/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32/u64/f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "seed_nodes": g.n, "seed_citations": g.m,
-                   "epochs_per_step": EPOCHS, "growth": 0.03, "mean_out_degree": 30,
-                   "alpha": 1.0, "tau": 5.0, "gamma": 1.0, "beta": 4.0, "anchors": 3,
-                   "l2": "inputs larger than L2 (CSR 0.5-0.9 GB)", "parallelism": "replicas only"},
+        "config": workload_config(g),
         "roofline": {"bound": "hbm", "kernel": "k_agents", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / peak if peak else None,
@@ -341,8 +352,37 @@ def run_ours(args) -> None:
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_sample(g, prm, seed, sampler=1)
         line["cpu_thinning"] = cpu_sample(g, prm, seed, sampler=0, max_epochs=2, budget_s=5.0)
+        line["cpu_baseline_1thread"] = cpu_sample(g, prm, seed, sampler=1, max_epochs=1, threads=1)
     eng.close()
+    if not args.no_extra:
+        line["ensemble"], line["loglik"] = extra_lines(args, world, rank, local, dist)
     print(json.dumps(line), flush=True)
+
+
+def extra_lines(args, world, rank, local, dist) -> tuple[dict | None, dict | None]:
+    """The batched-ensemble and calibration measurements in short form for the default line (5
+    timed steps each, their own CUDA-event timing and serial loops; see --ensemble and --loglik for
+    the full lines)."""
+    import copy
+
+    a = copy.copy(args)
+    a.steps, a.warmup = min(args.steps, 5), 3
+    ens = ensemble_measure(a, world, rank, local, dist, with_cpu=False)
+    lik = loglik_measure(a, world, rank, local, dist, with_cpu=not args.no_cpu)
+    if ens is None or lik is None:
+        return None, None
+    e = {"value": ens["value"], "unit": ens["unit"], "workload": ENS_WORKLOAD,
+         "serial_speedup": ens["serial"]["speedup_device"],
+         "serial_speedup_wall": ens["serial"]["speedup_wall"],
+         "citations_per_s": ens["citations_per_s"], "e2e": ens["e2e"],
+         "gpu_launches_per_step": ens["gpu_launches"] / a.steps, "steps": a.steps}
+    cb = lik.get("cpu_baseline") or {}
+    l = {"value": lik["value"], "unit": lik["unit"], "workload": LIK_WORKLOAD,
+         "serial_speedup": lik["serial"]["speedup"], "e2e": lik["e2e"],
+         "grad_rel_err_vs_fp64": cb.get("grad_rel_err_vs_fp64"),
+         "loglik_rel_err_vs_fp64": cb.get("loglik_rel_err_vs_fp64"),
+         "roofline_frac": lik["roofline"]["frac"], "steps": a.steps}
+    return e, l
 
 
 ENS_REPLICAS, ENS_EPOCHS = 256, 10
@@ -350,13 +390,18 @@ ENS_WORKLOAD = "ensemble_256_replicas_5k_200k_10_epochs_3pct"
 
 
 def run_ensemble(args) -> None:
+    line = ensemble_measure(args, *dist_setup(), with_cpu=not args.no_cpu)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def ensemble_measure(args, world, rank, local, dist, with_cpu: bool = True) -> dict | None:
     """Batched ensemble: 256 replicas (seed sizes log-uniform in [5k, 200k], per-replica alpha,
     tau, gamma, beta, Poisson(20), 3 % growth) grown 10 epochs in ONE context -- one launch of each
     epoch kernel over all replicas, the 10 epochs captured as one CUDA graph, launch shape picked by
     the engine's autotuner.  The same replicas grown serially, one single-replica context each
     (the plain per-replica method), give the serial time.  An eval is one replica grown 10 epochs.
-    Under torchrun the replicas are split across ranks (no exchange)."""
-    world, rank, local, dist = dist_setup()
+    Under torchrun the replicas are split across ranks (no exchange).  Returns rank 0's line."""
     from paragraph_gb300 import GrowthEngine
     from paragraph_gb300 import workloads as W
 
@@ -440,7 +485,7 @@ def run_ensemble(args) -> None:
                "d2h_bytes_per_step": int(reduce_sum(dist, float(d2h))),
                "citations_per_s": reduce_sum(dist, float(ne)) / dt}
     if rank != 0:
-        return
+        return None
     value = evals / (dev_ms_max / 1000.0)
     line = {
         "metric": "ensemble evals/sec (replica grown 10 epochs)",
@@ -461,9 +506,9 @@ def run_ensemble(args) -> None:
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
-    if not args.no_cpu:
+    if with_cpu:
         line["cpu_baseline"] = ensemble_cpu_sample(reps_all, args.seed)
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def ensemble_cpu_sample(reps, seed: int, budget_s: float = 12.0) -> dict:
@@ -506,12 +551,18 @@ def lik_bytes(st: dict, trace, points: int) -> int:
 
 
 def run_loglik(args) -> None:
+    line = loglik_measure(args, *dist_setup(), with_cpu=not args.no_cpu)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def loglik_measure(args, world, rank, local, dist, with_cpu: bool = True) -> dict | None:
     """Differentiable calibration: a PA trace grown on the GPU from a 200,000-node seed over 10
     epochs at theta* = (1, 5, 1, 4) (Poisson(20), 3 % growth, 3 anchors); one step evaluates the
     log-likelihood (forward) and its gradient (adjoint) at 64 parameter points drawn from
     alpha~U[0.5,1.5], tau~U[2,10], gamma~U[0.5,2], beta~U[1,8] in one batch.  The serial method
-    calls the same pair once per point.  Under torchrun the points are split across ranks."""
-    world, rank, local, dist = dist_setup()
+    calls the same pair once per point.  Under torchrun the points are split across ranks.  Returns
+    rank 0's line."""
     from paragraph_gb300 import GrowthEngine
     from paragraph_gb300 import workloads as W
 
@@ -565,7 +616,7 @@ def run_loglik(args) -> None:
                "d2h_bytes_per_step": int(reduce_sum(dist, float(8 * 5 * len(pts))))}
     if rank != 0:
         eng.close()
-        return
+        return None
     peak, peak_kind = peaks()
     nbytes = lik_bytes(st, trace, len(pts))
     achieved = nbytes / ((ms_f + ms_b) / args.steps / 1000.0) / 1e9
@@ -594,10 +645,10 @@ def run_loglik(args) -> None:
         "gpu_launches": 8 * args.steps,
         "clocks": clocks.summary(),
     }
-    if not args.no_cpu:
+    if with_cpu:
         line["cpu_baseline"] = loglik_cpu_sample(trace, pts_all, ll, gr)
     eng.close()
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def loglik_cpu_sample(trace, pts, ll_gpu, gr_gpu, budget_points: int = 2) -> dict:
@@ -849,6 +900,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default line without the nested ensemble and calibration measurements")
     ap.add_argument("--sampler", type=int, default=0, help="0 thinning, 1 neighbourhood enumeration")
     ap.add_argument("--epoch-report", action="store_true", help="per-epoch stage report instead")
     ap.add_argument("--report-epochs", type=int, default=EPOCHS)

@@ -281,6 +281,17 @@ pg_status pg_get_tuning(const pg_ctx* ctx, pg_tuning* tuning);
  * count, else PG_ERR_STATE. */
 pg_status pg_autotune(pg_ctx* ctx, int32_t num_epochs, pg_tuning* best, double* best_ms);
 
+/* ---- failure-path hook (no counterpart in the reference, which turns any CUDA error into exit
+ * status 1, src/kernel.cu:1761-1764) ----
+ * The thinning agent kernel stages candidate rows with asynchronous bulk copies and waits for each
+ * on an mbarrier with a bounded number of polls (default 2^22).  This sets the bound of the FIRST
+ * wait on each staged chunk; polls = 0 makes every first wait give up at once, negative restores
+ * the default.  A wait that gives up sets the device error word (the epoch then returns
+ * PG_ERR_TIMEOUT and the context refuses growth until pg_restore or a reload); the warp then waits
+ * again, with the full bound, for its copies in flight, so none is left running when it stops.
+ * For tests of that path; results of epochs that succeed do not depend on it. */
+pg_status pg_set_wait_limit(pg_ctx* ctx, int64_t polls);
+
 /* ---- log-likelihood of a growth trace and its adjoint (no counterpart in the reference) ----
  * A trace is a seed graph followed by epochs of agents; agent a (node epoch_nodes[0] + a, in the
  * epoch whose node range holds it) drew its citations c_1..c_k in the recorded order by
@@ -321,10 +332,10 @@ pg_status pg_loglik_bwd(pg_ctx* ctx, int32_t batch, const double* theta, const d
 #define PG_NOALLOC_MAX_TASKS (1 << 18)
 /* No counterpart in the reference: an Erdos-Renyi epoch's edge list written into device buffers
  * the caller owns, without allocating device memory.  It is for callers that must not call
- * cudaMalloc/cudaFree at this point -- e.g. a program timing or capturing other device work, or a
- * runtime that only hands out pre-sized buffers.  The edges equal those pg_er_epoch appends for
+ * cudaMalloc/cudaFree at this point -- e.g. a program timing other device work, or a runtime that
+ * only hands out pre-sized buffers.  The edges equal those pg_er_epoch appends for
  * the same seed, epoch, n_existing (pre-epoch nodes), delta and p: sources n_existing + i, targets
- * in [0, n_existing), ordered by (source, target).  Scratch is a fixed 2 MiB device array inside
+ * in [0, n_existing), ordered by (source, target).  Scratch is a fixed 4 MiB device array inside
  * the library (held by every GPU that loads it until the process exits); delta *
  * ceil(n_existing/65536) above PG_NOALLOC_MAX_TASKS is rejected with PG_ERR_CAPACITY.  The first
  * call on a device looks up that array's device address, so make it before any stream capture.

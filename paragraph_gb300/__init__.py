@@ -40,7 +40,7 @@ EXPORTED = [
     "pg_timer_start", "pg_timer_stop", "pg_checkpoint", "pg_restore", "pg_er_generate_noalloc",
     "pg_set_tuning", "pg_get_tuning", "pg_autotune", "pg_copy_anchors", "pg_trace_load",
     "pg_loglik_fwd", "pg_loglik_bwd", "pg_rc_configure", "pg_rc_set_nodes", "pg_rc_copy_agents",
-    "pg_rc_bag_table", "pg_rc_fitness_table", "pg_format_edges",
+    "pg_rc_bag_table", "pg_rc_fitness_table", "pg_format_edges", "pg_set_wait_limit",
 ]
 
 
@@ -248,6 +248,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_rc_bag_table": (i32, [vp, i64, vp]),
         "pg_rc_fitness_table": (i32, [vp]),
         "pg_format_edges": (i32, [vp, i32, vp, i64, vp, i64, P(i64)]),
+        "pg_set_wait_limit": (i32, [vp, i64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -528,6 +529,12 @@ class GrowthEngine:
         (results never depend on them)."""
         t = _Tuning(agent_ctas_per_sm, small_hash, copy_ctas_per_sm, lik_chunk_agents)
         self._check(self._lib.pg_set_tuning(self._ctx, C.byref(t)))
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Failure-path hook: polls of the first bounded wait on each staged copy of the agent
+        kernel (0: give up at once, < 0: the default).  A wait that gives up fails the epoch with
+        PG_ERR_TIMEOUT."""
+        self._check(self._lib.pg_set_wait_limit(self._ctx, int(polls)))
 
     def tuning(self) -> dict:
         t = _Tuning()

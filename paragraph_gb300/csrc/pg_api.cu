@@ -134,6 +134,7 @@ struct pg_ctx {
     Checkpoint ckpt;
     LikState lik;
     pg_tuning tune{};
+    uint32_t first_wait_polls = kWaitPolls;  // pg_set_wait_limit (failure-path tests)
     std::string err;
 };
 
@@ -240,6 +241,7 @@ Arena make_arena(pg_ctx* c) {
     A.tune_small_hash = c->tune.small_hash;
     A.tune_copy_ctas = c->tune.copy_ctas_per_sm;
     A.rep_base = c->cfg.replica_base;
+    A.first_wait_polls = c->first_wait_polls;
     A.weight_model = c->cfg.weight_model;
     A.rc_pa = c->rc_pa.p;
     A.rc_rec = c->rc_rec.p;
@@ -1636,6 +1638,16 @@ pg_status pg_set_tuning(pg_ctx* c, const pg_tuning* t) {
     if (std::memcmp(&c->tune, t, sizeof(pg_tuning)) != 0) {
         c->tune = *t;
         destroy_graph_exec(c);  // captured launches carry the old grid sizes
+    }
+    return PG_OK;
+}
+
+pg_status pg_set_wait_limit(pg_ctx* c, int64_t polls) {
+    if (!c) return PG_ERR_ARG;
+    const uint32_t v = polls < 0 ? kWaitPolls : (uint32_t)std::min<int64_t>(polls, kWaitPolls);
+    if (v != c->first_wait_polls) {
+        c->first_wait_polls = v;
+        destroy_graph_exec(c);  // captured launches carry the old bound
     }
     return PG_OK;
 }

@@ -38,6 +38,7 @@ constexpr int kHeavyBins = 24;       // log2-degree histogram bins 10..33
 constexpr int kRcAgeMax = 1024;      // recency probabilities by age 0..1023 (refcompat)
 constexpr int kRcFitMax = 1000;      // peak fitness values 1..1000 (refcompat)
 constexpr uint32_t kRcFillBlocks = 1u << 20;  // Philox blocks a uniform fill may use
+constexpr uint32_t kWaitPolls = 1u << 22;     // polls of a bounded wait on an asynchronous copy
 
 enum Sampler : int32_t {
     kSamplerThinning = 0,   // Poisson thinning against ball membership (default)
@@ -192,6 +193,8 @@ struct Arena {
     int32_t tune_small_hash;   // 1: 1024-slot frontier hash in the k <= 64 kernel, 0: 2048
     int32_t tune_copy_ctas;    // backward-copy CTAs per SM
     int32_t rep_base;          // RNG replica index of replica 0 (pg_config.replica_base)
+    uint32_t first_wait_polls; // polls of the first bounded wait on each staged copy (pg_set_wait_limit)
+    uint32_t pad_wp;
 };
 
 // Guide table of a replica's CDF (total Wq over n nodes): bucket g covers [g 2^gs, (g+1) 2^gs),

@@ -5,14 +5,15 @@
 // or a runtime that hands out pre-sized buffers and forbids allocation inside its callbacks.  For
 // them this file provides one entry point that generates an Erdos-Renyi epoch's edge list into
 // buffers the caller already owns.  Its only scratch (per-task edge counts, their exclusive scan
-// and the scan's block sums) lives in a fixed file-scope __device__ array, so no cudaMalloc,
-// cudaFree or allocating library routine is ever called.
+// and the scan's block sums, each in its own region) lives in a fixed file-scope __device__ array,
+// so no cudaMalloc, cudaFree or allocating library routine is ever called.
 //
 // The edges are the ones pg_er_epoch appends for the same (seed, epoch, n_existing, delta, p):
 // the same Philox streams, the same 2^16-id chunks, the same library log, the same
 // (source, target) order.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 
 #include "../../include/paragraph_gb300.h"
@@ -24,11 +25,14 @@ namespace {
 constexpr int64_t kNoAllocMaxTasks = PG_NOALLOC_MAX_TASKS;
 constexpr int64_t kNoAllocBlocks = (kNoAllocMaxTasks + 1023) / 1024 + 2;
 
-// counts (turned into offsets in place, entry [tasks] = total) followed by the scan's block sums.
-// Every GPU that loads the library holds this array until the process exits.
-static __device__ __align__(256) int64_t g_noalloc_scratch[kNoAllocMaxTasks + 1 + kNoAllocBlocks];
+// Three regions: per-task counts [kNoAllocMaxTasks], their exclusive scan [kNoAllocMaxTasks + 1]
+// (entry [tasks] = total) and the scan's block sums.  Every GPU that loads the library holds this
+// array (about 4 MiB) until the process exits.
+constexpr int64_t kNoAllocWords = 2 * kNoAllocMaxTasks + 1 + kNoAllocBlocks;
+static __device__ __align__(256) int64_t g_noalloc_scratch[kNoAllocWords];
 
-int64_t* g_scratch_addr[64] = {nullptr};
+// Device address of the array, looked up once per device; several host threads may call.
+std::atomic<int64_t*> g_scratch_addr[64] = {};
 
 __device__ __forceinline__ int64_t walk(uint64_t seed, uint32_t ep, int64_t i, int64_t c, int64_t n,
                                         double inv_l, int64_t src, int32_t* out_src,
@@ -75,12 +79,14 @@ __global__ void __launch_bounds__(256) k_na_emit(uint64_t seed, uint32_t ep, int
 pg_status scratch_for_current_device(int64_t** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PG_ERR_CUDA;
-    if (!g_scratch_addr[dev]) {
+    int64_t* a = g_scratch_addr[dev].load(std::memory_order_acquire);
+    if (!a) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return PG_ERR_CUDA;
-        g_scratch_addr[dev] = static_cast<int64_t*>(p);
+        a = static_cast<int64_t*>(p);
+        g_scratch_addr[dev].store(a, std::memory_order_release);  // every thread stores the same value
     }
-    *out = g_scratch_addr[dev];
+    *out = a;
     return PG_OK;
 }
 
@@ -108,20 +114,22 @@ extern "C" pg_status pg_er_generate_noalloc(uint64_t seed, int64_t epoch, int64_
     pg_status s = scratch_for_current_device(&scratch);
     if (s != PG_OK) return s;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    int64_t* cnt = scratch;                       // [tasks + 1], scanned in place
-    int64_t* blocksum = scratch + kNoAllocMaxTasks + 1;
+    int64_t* cnt = scratch;                          // [tasks]
+    int64_t* off = scratch + kNoAllocMaxTasks;        // [tasks + 1], exclusive scan of cnt
+    int64_t* blocksum = off + kNoAllocMaxTasks + 1;   // [scan blocks + 1]
     const uint32_t ep = (uint32_t)epoch;
     int64_t g = (tasks + 255) / 256;
     if (g > 4096) g = 4096;
     k_na_count<<<(unsigned)g, 256, 0, st>>>(seed, ep, n_existing, tasks, chunks, inv_l, cnt);
-    launch_scan_i64(cnt, cnt, tasks, blocksum, st);
+    launch_scan_i64(cnt, off, tasks, blocksum, st);
+    if (cudaGetLastError() != cudaSuccess) return PG_ERR_CUDA;  // *num_edges stays 0
     int64_t total = 0;
-    if (cudaMemcpyAsync(&total, cnt + tasks, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+    if (cudaMemcpyAsync(&total, off + tasks, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return PG_ERR_CUDA;
     *num_edges = total;
     if (total > capacity) return PG_ERR_CAPACITY;  // nothing written
-    k_na_emit<<<(unsigned)g, 256, 0, st>>>(seed, ep, n_existing, tasks, chunks, inv_l, cnt, d_src, d_dst);
+    k_na_emit<<<(unsigned)g, 256, 0, st>>>(seed, ep, n_existing, tasks, chunks, inv_l, off, d_src, d_dst);
     if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) return PG_ERR_CUDA;
     return PG_OK;
 }

@@ -33,7 +33,7 @@ struct BallAux {
     int32_t na;
 };
 
-constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a bulk-copy barrier before giving up
+constexpr uint32_t kWaitLimit = kWaitPolls;  // polls of a bulk-copy barrier before giving up
 constexpr int kTestU = 4;                  // entries per lane and step of the membership scan
 
 // STAGE: adjacency entries per stage buffer (two per warp; 1024 in the small-hash k <= 64 kernel,
@@ -74,9 +74,9 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t 
         : "memory");
     return ok != 0;
 }
-// Bounded wait for the phase with the given parity; false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitLimit; ++i)
+// Bounded wait for the phase with the given parity; false when `limit` polls ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
+    for (uint32_t i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -559,10 +559,11 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             if (c + 1 < nchunk && issue(c0 + kStage, buf ^ 1)) armed |= 2u >> buf;
             if (!((armed >> buf) & 1u)) continue;
             armed &= ~(1u << buf);
-            const bool ok = mbar_wait(&S.bar[buf], (phase >> buf) & 1u);
+            const bool ok = mbar_wait(&S.bar[buf], (phase >> buf) & 1u, A.first_wait_polls);
             phase ^= 1u << buf;
             if (!__all_sync(kFull, ok)) {
-                // give the copies in flight a second bounded wait, then abandon the warp
+                // give the copies in flight a second bounded wait (the full limit, whatever the
+                // first wait's), then abandon the warp
                 if (lane == 0) atomicOr(&A.st->error, kErrTimeout);
                 mbar_wait(&S.bar[buf], ((phase >> buf) & 1u) ^ 1u);
                 if (armed) mbar_wait(&S.bar[buf ^ 1], (phase >> (buf ^ 1)) & 1u);

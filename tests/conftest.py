@@ -44,3 +44,15 @@ def gpu(built, has_gpu):
     if not has_gpu:
         pytest.fail("GPU test collected on a machine without a GPU (run with -m 'not gpu')")
     return True
+
+
+def pytest_terminal_summary(terminalreporter):
+    """Print the p-values the distribution tests recorded (shown even in quiet runs)."""
+    try:
+        import law
+    except ImportError:
+        return
+    if law.PVALUES:
+        terminalreporter.write_sep("-", "distribution tests: p-values")
+        for name, p in law.PVALUES:
+            terminalreporter.write_line(f"p = {p:.4g}  {name}")

@@ -50,6 +50,32 @@ def test_noalloc_matches_er_epoch_twice(gpu):
         np.testing.assert_array_equal(dst, ref_dst)
 
 
+def test_noalloc_allocates_no_device_memory(gpu):
+    """After a first call (which looks up the scratch array's address), a call of another shape
+    changes neither the device's free memory nor torch's reserved pool: nothing is allocated."""
+    torch = pytest.importorskip("torch")
+    lib = pg.load_library()
+    cap = 400_000
+    src = torch.empty(cap, dtype=torch.int32, device="cuda")
+    dst = torch.empty(cap, dtype=torch.int32, device="cuda")
+    count = C.c_int64(-1)
+
+    def call(seed, n0, delta, p):
+        st = lib.pg_er_generate_noalloc(seed, 0, n0, delta, p, C.c_void_p(src.data_ptr()),
+                                        C.c_void_p(dst.data_ptr()), cap, C.byref(count), None)
+        assert st == pg.PG_OK and 0 < count.value <= cap
+
+    call(9, 90_000, 1500, 1e-3)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    reserved0 = torch.cuda.memory_reserved()
+    call(10, 260_000, 700, 2e-3)  # more chunks per node, a different task count
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_reserved() == reserved0
+
+
 def test_noalloc_rejects_oversized_and_small_capacity(gpu):
     lib = pg.load_library()
     count = C.c_int64(-1)
