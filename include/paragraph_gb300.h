@@ -244,6 +244,30 @@ pg_status pg_copy_anchors(pg_ctx* ctx, int32_t replica, int32_t* anchors);
 pg_status pg_format_edges(pg_ctx* ctx, int32_t replica, const int64_t* ids, int64_t n_ids, char* out,
                           int64_t cap, int64_t* bytes);
 
+/* The rows of the attribute file (Graph::WriteAttributes, src/graph.cu:1057-1218, without its
+ * header line), formatted on the device, one line per node v of the replica:
+ *   id,type,year,pa_weight,rec_weight,fit_weight,fit_lag_duration,fit_peak_value,
+ *   fit_peak_duration,alpha,in_degree,out_degree,assigned_out_degree,planted_line,generators
+ * The weights and alpha print as C's "%.10g", the peak as "%d" of the fitness (peak_integer != 0,
+ * the refcompat model's integer peaks) or "%.9g" of the fp32 fitness; nodes v < num_seed are
+ * typed "seed" with generators "no_generators", the rest "agent" with their generator ids joined
+ * by ';' ("-1" when none).  Year, fitness and degrees are the replica's own; the caller gives the
+ * printed ids and the per-paper columns.  out == NULL only reports the size in *bytes; a smaller
+ * buffer gives PG_ERR_CAPACITY. */
+typedef struct {
+    int64_t num_nodes;         /* the replica's node count */
+    int64_t num_seed;          /* nodes typed "seed" (the loaded graph) */
+    const int64_t* ids;        /* [num_nodes] printed node ids */
+    const double* draws;       /* [num_nodes][4] pa, rec, fit weight, alpha (-1 where absent) */
+    const int32_t* ints;       /* [num_nodes][4] fitness lag, peak duration, assigned out-degree,
+                                  planted-papers line (-1 where absent) */
+    const int64_t* generators; /* [num_nodes][4] printed ids of each agent's generators, -1 unused */
+    int32_t peak_integer;      /* 1: the peak column is "%d" of the fitness; 0: "%.9g" */
+    int32_t reserved;
+} pg_attr_rows;
+pg_status pg_format_attributes(pg_ctx* ctx, int32_t replica, const pg_attr_rows* rows, char* out,
+                               int64_t cap, int64_t* bytes);
+
 /* ---- measurement ---- */
 /* enable != 0 records CUDA events around every kernel group of each epoch (default on). */
 pg_status pg_set_timing(pg_ctx* ctx, int32_t enable);
@@ -359,6 +383,9 @@ double pg_log_host(double x);
 double pg_exp_host(double x);
 /* Version string of the build. */
 const char* pg_version(void);
+/* C's "%.<precision>g" of x (precision 1..13) into out (at least 32 bytes), returning the length:
+ * the conversion pg_format_attributes runs on the device, compiled for the host. */
+int32_t pg_format_g_host(double x, int32_t precision, char* out);
 
 #ifdef __cplusplus
 }

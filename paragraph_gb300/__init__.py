@@ -41,6 +41,7 @@ EXPORTED = [
     "pg_set_tuning", "pg_get_tuning", "pg_autotune", "pg_copy_anchors", "pg_trace_load",
     "pg_loglik_fwd", "pg_loglik_bwd", "pg_rc_configure", "pg_rc_set_nodes", "pg_rc_copy_agents",
     "pg_rc_bag_table", "pg_rc_fitness_table", "pg_format_edges", "pg_set_wait_limit",
+    "pg_format_attributes", "pg_format_g_host",
 ]
 
 
@@ -104,6 +105,12 @@ class _Stats(C.Structure):
         ("run_adj_scanned", C.c_int64), ("lik_ball_elems", C.c_int64),
         ("lik_adj_entries", C.c_int64), ("lik_citations", C.c_int64), ("lik_ms_fwd", C.c_double),
         ("lik_ms_bwd", C.c_double)]
+
+
+class _AttrRows(C.Structure):
+    _fields_ = [("num_nodes", C.c_int64), ("num_seed", C.c_int64), ("ids", C.c_void_p),
+                ("draws", C.c_void_p), ("ints", C.c_void_p), ("generators", C.c_void_p),
+                ("peak_integer", C.c_int32), ("reserved", C.c_int32)]
 
 
 class _Tuning(C.Structure):
@@ -249,6 +256,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_rc_fitness_table": (i32, [vp]),
         "pg_format_edges": (i32, [vp, i32, vp, i64, vp, i64, P(i64)]),
         "pg_set_wait_limit": (i32, [vp, i64]),
+        "pg_format_attributes": (i32, [vp, i32, P(_AttrRows), vp, i64, P(i64)]),
+        "pg_format_g_host": (i32, [C.c_double, i32, C.c_char_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -453,6 +462,24 @@ class GrowthEngine:
         buf = C.create_string_buffer(max(size.value, 1))
         self._check(self._lib.pg_format_edges(self._ctx, replica, _ptr(ids), len(ids), buf,
                                               size.value, C.byref(size)))
+        return buf.raw[:size.value]
+
+    def format_attributes(self, ids, draws, ints, generators, num_seed: int, peak_integer: bool,
+                          replica: int = 0) -> bytes:
+        """The attribute-file rows (Graph::WriteAttributes) formatted on the device: ids[n],
+        draws[n, 4] (pa, rec, fit weight, alpha), ints[n, 4] (lag, duration, assigned out-degree,
+        planted line), generators[n, 4] (printed ids, -1 unused); nodes below num_seed are seeds."""
+        ids = np.ascontiguousarray(ids, np.int64)
+        draws = np.ascontiguousarray(draws, np.float64)
+        ints = np.ascontiguousarray(ints, np.int32)
+        gens = np.ascontiguousarray(generators, np.int64)
+        rows = _AttrRows(len(ids), int(num_seed), ids.ctypes.data, draws.ctypes.data, ints.ctypes.data,
+                         gens.ctypes.data, 1 if peak_integer else 0, 0)
+        size = C.c_int64()
+        self._check(self._lib.pg_format_attributes(self._ctx, replica, C.byref(rows), None, 0, C.byref(size)))
+        buf = C.create_string_buffer(max(size.value, 1))
+        self._check(self._lib.pg_format_attributes(self._ctx, replica, C.byref(rows), buf, size.value,
+                                                   C.byref(size)))
         return buf.raw[:size.value]
 
     def last_epoch_edges(self, replica: int = 0) -> tuple[np.ndarray, np.ndarray]:

@@ -384,7 +384,9 @@ int run(int argc, char** argv) {
     std::vector<int32_t> lag((size_t)n0, 0), dur((size_t)n0, 1000), plant_line((size_t)n0, -1), gen((size_t)n0, -1),
         assigned((size_t)n0, -1);
     std::vector<double> wpa((size_t)n0, -1.0), wrec((size_t)n0, -1.0), wfit((size_t)n0, -1.0), walpha((size_t)n0, -1.0);
-    std::vector<std::string> gen_str((size_t)n0, "no_generators");
+    // generators of each agent as sequence ids, up to 4 (the anchors of the baseline model, the
+    // generator of refcompat), -1 unused
+    std::vector<int32_t> gens((size_t)n0 * 4, -1);
     std::ofstream elog;
     if (o.has("--epoch-log")) elog.open(o.str("--epoch-log"));
     log.info("start year " + std::to_string(start_year) + ", " + std::to_string(cycles) + " cycles, model " +
@@ -431,7 +433,7 @@ int run(int argc, char** argv) {
         lag.resize((size_t)(n + nn), 0);
         dur.resize((size_t)(n + nn), 1000);
         plant_line.resize((size_t)(n + nn), -1);
-        gen_str.resize((size_t)(n + nn));
+        gens.resize((size_t)(n + nn) * 4, -1);
         if (rc) {
             std::vector<double> ag((size_t)nn * 6);
             PG_TRY(ctx, pg_rc_copy_agents(ctx, 0, ag.data()));
@@ -442,6 +444,7 @@ int run(int argc, char** argv) {
                 wfit[v] = ag[(size_t)a * 6 + 2];
                 walpha[v] = ag[(size_t)a * 6 + 3];
                 gen[v] = (int32_t)ag[(size_t)a * 6 + 4];
+                gens[v * 4] = gen[v];
                 assigned[v] = (int32_t)ag[(size_t)a * 6 + 5];
             }
             // planted papers of this cycle (ABM::PlantNodes, includes/abm.cuh:486-504)
@@ -465,16 +468,7 @@ int run(int argc, char** argv) {
             std::vector<int32_t> anc((size_t)nn * 4);
             PG_TRY(ctx, pg_copy_anchors(ctx, 0, anc.data()));
             for (int64_t a = 0; a < nn; ++a) gen[(size_t)(n + a)] = anc[(size_t)a * 4];
-            for (int64_t a = 0; a < nn; ++a) {
-                std::string s;
-                for (int i = 0; i < 4; ++i) {
-                    const int32_t x = anc[(size_t)a * 4 + i];
-                    if (x < 0) continue;
-                    if (!s.empty()) s += ";";
-                    s += std::to_string(x < (int32_t)orig.size() ? orig[(size_t)x] : (int64_t)x);
-                }
-                gen_str[(size_t)(n + a)] = s;
-            }
+            std::copy(anc.begin(), anc.end(), gens.begin() + (ptrdiff_t)(n * 4));
         }
         pg_stats st{};
         pg_get_stats(ctx, &st);
@@ -523,29 +517,40 @@ int run(int argc, char** argv) {
                    "fit_peak_duration,alpha,in_degree,out_degree,assigned_out_degree,"
                    "planted_nodes_line_number,generator_node_string\n",
                    f);
+        // the rows are formatted on the device (pg_format_attributes): the per-paper columns go
+        // up, year, fitness and degrees are the arena's own
+        std::vector<double> draws((size_t)n * 4);
+        std::vector<int32_t> ints((size_t)n * 4);
+        std::vector<int64_t> gid((size_t)n * 4, -1);
         for (int64_t v = 0; v < n; ++v) {
+            const size_t u = (size_t)v;
             const bool agent = v >= n0;
-            const long long id = (long long)orig[(size_t)v];
-            // refcompat: the integer peak fitness; baseline and ER: the fp32 fitness (9 digits
-            // round-trip it exactly)
-            char peak[32];
-            if (rc)
-                std::snprintf(peak, sizeof(peak), "%d", (int)fits[(size_t)v]);
-            else
-                std::snprintf(peak, sizeof(peak), "%.9g", (double)fits[(size_t)v]);
-            if (!agent) {
-                std::fprintf(f, "%lld,seed,%d,-1,-1,-1,%d,%s,%d,-1,%d,%d,-1,-1,no_generators\n", id, pubs[(size_t)v],
-                             rc ? lag[(size_t)v] : -1, peak, rc ? dur[(size_t)v] : -1, indeg[(size_t)v], outdeg[(size_t)v]);
-            } else {
-                std::string g = gen_str[(size_t)v];
-                if (rc || g.empty())
-                    g = gen[(size_t)v] >= 0 ? std::to_string(orig[(size_t)gen[(size_t)v]]) : "-1";
-                std::fprintf(f, "%lld,agent,%d,%.10g,%.10g,%.10g,%d,%s,%d,%.10g,%d,%d,%d,%d,%s\n", id, pubs[(size_t)v],
-                             wpa[(size_t)v], wrec[(size_t)v], wfit[(size_t)v], rc ? lag[(size_t)v] : -1, peak,
-                             rc ? dur[(size_t)v] : -1, walpha[(size_t)v], indeg[(size_t)v], outdeg[(size_t)v],
-                             rc ? assigned[(size_t)v] : outdeg[(size_t)v], plant_line[(size_t)v], g.c_str());
+            draws[u * 4 + 0] = agent ? wpa[u] : -1.0;
+            draws[u * 4 + 1] = agent ? wrec[u] : -1.0;
+            draws[u * 4 + 2] = agent ? wfit[u] : -1.0;
+            draws[u * 4 + 3] = agent ? walpha[u] : -1.0;
+            ints[u * 4 + 0] = rc ? lag[u] : -1;
+            ints[u * 4 + 1] = rc ? dur[u] : -1;
+            ints[u * 4 + 2] = agent ? (rc ? assigned[u] : outdeg[u]) : -1;
+            ints[u * 4 + 3] = agent ? plant_line[u] : -1;
+            for (int i = 0; agent && i < 4; ++i) {
+                const int32_t x = gens[u * 4 + (size_t)i];
+                if (x >= 0) gid[u * 4 + (size_t)i] = orig[(size_t)x];
             }
         }
+        pg_attr_rows rows{};
+        rows.num_nodes = n;
+        rows.num_seed = n0;
+        rows.ids = orig.data();
+        rows.draws = draws.data();
+        rows.ints = ints.data();
+        rows.generators = gid.data();
+        rows.peak_integer = rc ? 1 : 0;  // refcompat: the integer peak; else the fp32 fitness, "%.9g"
+        int64_t bytes = 0;
+        PG_TRY(ctx, pg_format_attributes(ctx, 0, &rows, nullptr, 0, &bytes));
+        std::vector<char> txt((size_t)std::max<int64_t>(bytes, 1));
+        PG_TRY(ctx, pg_format_attributes(ctx, 0, &rows, txt.data(), bytes, &bytes));
+        std::fwrite(txt.data(), 1, (size_t)bytes, f);
         std::fclose(f);
     }
     if (o.has("--output-nodelist")) {

@@ -1622,6 +1622,9 @@ pg_status pg_restore(pg_ctx* c) {
         PG_CUDA(c, cudaMemcpyAsync(c->bwd_col[par].p + h.ebase, k.bwd_col.p + h.ebase, 4 * (size_t)h.m, d2d, s));
     }
     PG_CUDA(c, cudaMemsetAsync(c->inc.p, 0, 4 * (size_t)c->S, s));
+    // the saved state is consistent: clear the error word a failed epoch left set
+    PG_CUDA(c, cudaMemsetAsync(reinterpret_cast<char*>(c->st.p) + offsetof(EpochState, error), 0,
+                               sizeof(uint32_t), s));
     PG_CUDA(c, cudaStreamSynchronize(s));
     c->epoch = k.epoch;
     c->parity = par;
@@ -1911,6 +1914,82 @@ pg_status pg_format_edges(pg_ctx* c, int32_t replica, const int64_t* ids, int64_
                                             std::to_string(total));
     PG_CUDA(c, dalloc(t.txt, std::max<int64_t>(total, 1)));
     launch_text_write(fo, fc, n, m, t.did.p, t.off.p, t.txt.p, c->num_sms, c->stream);
+    PG_CUDA(c, cudaGetLastError());
+    PG_CUDA(c, cudaMemcpyAsync(out, t.txt.p, (size_t)total, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+
+pg_status pg_format_attributes(pg_ctx* c, int32_t replica, const pg_attr_rows* rows, char* out, int64_t cap,
+                               int64_t* bytes) {
+    if (!c || !rows || !bytes) return PG_ERR_ARG;
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (replica < 0 || replica >= c->R) return fail(c, PG_ERR_ARG, "replica out of range");
+    const HostRep& h = c->hrep[(size_t)replica];
+    const int64_t n = h.n;
+    if (rows->num_nodes != n) return fail(c, PG_ERR_ARG, "rows must describe every node of the replica");
+    if (rows->num_seed < 0 || rows->num_seed > n) return fail(c, PG_ERR_ARG, "num_seed out of range");
+    if (!rows->ids || !rows->draws || !rows->ints || (!rows->generators && rows->num_seed < n))
+        return fail(c, PG_ERR_ARG, "ids, draws, ints and generators are required");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    struct Tmp {
+        DBuf<int64_t> did, gen, off, bs;
+        DBuf<double> draws;
+        DBuf<int32_t> ints, len;
+        DBuf<char> txt;
+        ~Tmp() {
+            dfree(did);
+            dfree(gen);
+            dfree(off);
+            dfree(bs);
+            dfree(draws);
+            dfree(ints);
+            dfree(len);
+            dfree(txt);
+        }
+    } t;
+    const size_t nn = (size_t)std::max<int64_t>(n, 1);
+    PG_CUDA(c, dalloc(t.did, n));
+    PG_CUDA(c, dalloc(t.draws, 4 * n));
+    PG_CUDA(c, dalloc(t.ints, 4 * n));
+    PG_CUDA(c, dalloc(t.gen, 4 * n));
+    PG_CUDA(c, dalloc(t.len, n));
+    PG_CUDA(c, dalloc(t.off, n + 1));
+    PG_CUDA(c, dalloc(t.bs, scan_blocks_needed(std::max<int64_t>(n, 1)) + 2));
+    PG_CUDA(c, cudaMemcpyAsync(t.did.p, rows->ids, 8 * nn, cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(t.draws.p, rows->draws, 32 * nn, cudaMemcpyHostToDevice, c->stream));
+    PG_CUDA(c, cudaMemcpyAsync(t.ints.p, rows->ints, 16 * nn, cudaMemcpyHostToDevice, c->stream));
+    if (rows->num_seed < n) {
+        const int64_t k = n - rows->num_seed;  // only the agents' generator rows are read
+        PG_CUDA(c, cudaMemcpyAsync(t.gen.p + 4 * rows->num_seed, rows->generators + 4 * rows->num_seed,
+                                   32 * (size_t)k, cudaMemcpyHostToDevice, c->stream));
+    }
+    AttrCols C{};
+    C.n = n;
+    C.n_seed = rows->num_seed;
+    C.ids = t.did.p;
+    C.draws = t.draws.p;
+    C.ints = t.ints.p;
+    C.gens = t.gen.p;
+    C.pub = c->pub.p + h.nbase;
+    C.fit = c->fit.p + h.nbase;
+    C.indeg = c->indeg.p + h.nbase;
+    C.fo = c->fwd_off.p + h.obase;
+    C.peak_int = rows->peak_integer ? 1 : 0;
+    cudaGetLastError();
+    launch_attr_text(C, t.len.p, nullptr, nullptr, c->num_sms, c->stream);
+    launch_scan_i32_to_i64(t.len.p, t.off.p, n, t.bs.p, c->stream);
+    PG_CUDA(c, cudaGetLastError());
+    int64_t total = 0;
+    PG_CUDA(c, cudaMemcpyAsync(&total, t.off.p + n, 8, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    *bytes = total;
+    if (!out) return PG_OK;
+    if (cap < total)
+        return fail(c, PG_ERR_CAPACITY, "the output buffer holds " + std::to_string(cap) + " bytes, the text needs " +
+                                            std::to_string(total));
+    PG_CUDA(c, dalloc(t.txt, std::max<int64_t>(total, 1)));
+    launch_attr_text(C, nullptr, t.off.p, t.txt.p, c->num_sms, c->stream);
     PG_CUDA(c, cudaGetLastError());
     PG_CUDA(c, cudaMemcpyAsync(out, t.txt.p, (size_t)total, cudaMemcpyDeviceToHost, c->stream));
     PG_CUDA(c, cudaStreamSynchronize(c->stream));

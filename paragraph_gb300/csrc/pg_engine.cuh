@@ -348,6 +348,21 @@ void launch_text_len(const int64_t* fo, const int32_t* fc, int64_t n, int64_t m,
                      int num_sms, cudaStream_t s);
 void launch_text_write(const int64_t* fo, const int32_t* fc, int64_t n, int64_t m, const int64_t* ids,
                        const int64_t* off, char* out, int num_sms, cudaStream_t s);
+// the attribute file as text on the device (pg_text.cu); out == nullptr: line lengths into len
+struct AttrCols {  // columns of the attribute file (device pointers)
+    int64_t n, n_seed;
+    const int64_t* ids;     // [n]
+    const double* draws;    // [n][4] pa, rec, fit weight, alpha
+    const int32_t* ints;    // [n][4] lag, duration, assigned out-degree, planted line
+    const int64_t* gens;    // [n][4] generator ids, -1 unused
+    const int32_t* pub;
+    const float* fit;
+    const int32_t* indeg;
+    const int64_t* fo;      // forward offsets: the out-degree of v is fo[v + 1] - fo[v]
+    int32_t peak_int;
+};
+void launch_attr_text(const AttrCols& C, int32_t* len, const int64_t* off, char* out, int num_sms,
+                      cudaStream_t s);
 // the source of every edge in [first, first + count) of a forward CSR, from its offsets
 void launch_edge_sources(const int64_t* fo, int64_t n, int64_t first, int64_t count, int32_t* out,
                          int num_sms, cudaStream_t s);

@@ -3,10 +3,19 @@
 // this is the density of the sampling law the growth step draws from
 // (w_j beta^[j in N_a], successive sampling without replacement).
 //
-// Weights: w_j = 2^(x2_j), x2_j = log2(e) (gamma log f_j + alpha log(indeg_j+1) - (t-t_j)/tau) in
-// fp32 (per-point constants pre-multiplied by log2 e), evaluated by the special-function unit
-// (PTX ex2.approx.ftz.f32, relative error < 2^-22; results below 2^-126 flush to zero).  The same
-// weight function feeds every sum below, so the normalisers and the citations' prefix sums agree.
+// Weights: w_j = 2^(x2_j), x2_j = log2(e) (gamma log f_j + alpha log(indeg_j+1) - (t-t_j)/tau), the
+// exponent carried as an unevaluated fp32 pair h + l: the per-point constants are split into fp32
+// high and low parts, log(indeg+1) is stored as a high/low pair, and the products and the sum of
+// the two discrete terms (log-degree, age) keep their rounding errors (FMA residuals, Knuth's
+// two-sum).  A plain fp32 exponent would round alpha log2 e, log2 e / tau and log(d+1) once for all
+// nodes that share them -- an error that does not average out over the trace and that moves the
+// gradient by the Hessian times a 2^-24 shift of theta (about 1e-5 of the gradient at the
+// generating point).  2^(h + l) is then evaluated in fp32 arithmetic (exp2_acc: exact reduction by
+// the nearest integer, Taylor series of e^t, |t| < 0.35), not by the special-function unit: the
+// unit's ex2.approx has a relative error up to 2^-22 that varies with the argument's fraction, and
+// that error, shared by every citation of a node, moved the gradient at the generating point by
+// about 1e-5 of its norm.  Weights below 2^-126 are flushed to zero.  The same weight function
+// feeds every sum below, so the normalisers and the citations' prefix sums agree.
 //
 // Per launch (forward or adjoint):
 //   k_lik_global      per epoch: sum_{j<n_e} w_j (forward) or sum_j w_j g_j (adjoint), one CTA per
@@ -29,6 +38,7 @@ namespace pg {
 namespace {
 
 constexpr double kLn2d = 0x1.62e42fefa39efp-1;
+constexpr float kLn2f = 0x1.62e430p-1f;
 
 struct Kahan {
     float s = 0.f, c = 0.f;
@@ -56,27 +66,62 @@ __device__ __forceinline__ int64_t bwd_cut(const LikTrace& T, int64_t x, int64_t
     return lo;
 }
 
-// 2^x on the special-function unit (PTX ex2.approx.ftz.f32).
-__device__ __forceinline__ float ex2_sfu(float x) {
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-// Per-point constants of the weight exponent in base 2.
+// Per-point constants of the weight exponent in base 2, each as an fp32 high part and the fp32
+// remainder of its FP64 value.
 struct LikC {
-    float al2, ga2, it2;  // alpha log2 e, gamma log2 e, log2 e / tau
+    float al2, ga2, it2;     // alpha log2 e, gamma log2 e, log2 e / tau (high parts)
+    float al2l, ga2l, it2l;  // their remainders
 };
 __device__ __forceinline__ LikC lik_c(const double* pp) {
     LikC c;
-    c.al2 = (float)(pp[0] * kLog2e);
-    c.ga2 = (float)(pp[2] * kLog2e);
-    c.it2 = (float)(pp[1] * kLog2e);
+    const double a = pp[0] * kLog2e, g = pp[2] * kLog2e, t = pp[1] * kLog2e;
+    c.al2 = (float)a;
+    c.ga2 = (float)g;
+    c.it2 = (float)t;
+    c.al2l = (float)(a - (double)c.al2);
+    c.ga2l = (float)(g - (double)c.ga2);
+    c.it2l = (float)(t - (double)c.it2);
     return c;
 }
-// x2 = log2 of the weight: ga2 log f + al2 log(d+1) - it2 (t - t_j)
-__device__ __forceinline__ float lik_x2(const float4 f, const LikC& c) {
-    return __fmaf_rn(c.ga2, f.x, __fmaf_rn(c.al2, f.y, -(f.z * c.it2)));
+// a + b = s + err exactly (Knuth's two-sum; the build neither contracts nor reassociates)
+__device__ __forceinline__ float two_sum(float a, float b, float& err) {
+    const float s = a + b;
+    const float bb = s - a;
+    err = (a - (s - bb)) + (b - bb);
+    return s;
+}
+// log2 of the weight, ga2 log f + al2 log(d+1) - it2 (t - t_j), as h + l.  Features: f.x = log f,
+// f.y + f.w = log(d+1) (high, low), f.z = t - t_j (an exact integer).
+struct X2 {
+    float h, l;
+};
+__device__ __forceinline__ X2 lik_x2(const float4 f, const LikC& c) {
+    const float p1 = c.al2 * f.y, e1 = __fmaf_rn(c.al2, f.y, -p1);
+    const float p2 = c.it2 * f.z, e2 = __fmaf_rn(c.it2, f.z, -p2);
+    float e3;
+    const float s = two_sum(p1, -p2, e3);
+    X2 x;
+    x.h = __fmaf_rn(c.ga2, f.x, s);
+    x.l = ((e1 - e2) + e3) + __fmaf_rn(c.al2, f.w, __fmaf_rn(c.al2l, f.y, __fmaf_rn(c.ga2l, f.x, -(c.it2l * f.z))));
+    return x;
+}
+// 2^(h + l) for |l| < 2^-18: n = rint(h), f = h - n (exact), t = (f + l) ln 2 in [-0.35, 0.35],
+// e^t by its Taylor series through t^7/7! (truncation below 5e-9 relative), times 2^n built in the
+// exponent field; about 2 ulp in all, with rounding errors that do not depend on n.
+__device__ __forceinline__ float lik_w(const X2 x) {
+    const float n = rintf(x.h);
+    const int ni = (int)n;
+    if (ni < -126) return 0.0f;
+    const float t = __fmaf_rn(x.h - n, kLn2f, x.l * kLn2f);
+    float p = 1.0f / 5040.0f;
+    p = __fmaf_rn(p, t, 1.0f / 720.0f);
+    p = __fmaf_rn(p, t, 1.0f / 120.0f);
+    p = __fmaf_rn(p, t, 1.0f / 24.0f);
+    p = __fmaf_rn(p, t, 1.0f / 6.0f);
+    p = __fmaf_rn(p, t, 0.5f);
+    p = __fmaf_rn(p, t, 1.0f);
+    p = __fmaf_rn(p, t, 1.0f);
+    return p * __int_as_float((ni > 127 ? 255 : ni + 127) << 23);
 }
 
 // 1/D for D > 0 in FP64: Newton's iteration for the reciprocal, r' = r + r (1 - D r), started from
@@ -118,11 +163,12 @@ __global__ void __launch_bounds__(256) k_lik_features(LikTrace T) {
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ne;
          j += (int64_t)gridDim.x * blockDim.x) {
         const int64_t d = bwd_cut(T, j, ne) - T.bo[j];
+        const double ly = log_pg((double)(d + 1));
         float4 f;
         f.x = logf_pg(T.fit[j]);
-        f.y = logf_pg((float)(d + 1));
+        f.y = (float)ly;
         f.z = (float)(te - T.pub[j]);
-        f.w = 0.f;
+        f.w = (float)(ly - (double)f.y);
         F[j] = f;
     }
 }
@@ -142,7 +188,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_global(LikTrace T, LikBatch
         const float4* F = T.feat + (int64_t)e * T.n;
         for (int64_t j = lo + sub; j < hi; j += nsub) {
             const float4 f = F[j];
-            const float w = ex2_sfu(lik_x2(f, c));
+            const float w = lik_w(lik_x2(f, c));
             kadd(s, w);
             if (ADJ) {
                 kadd(t0, w * f.y);
@@ -343,8 +389,8 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
             const float4 f0 = F[i0], f1 = F[i1], f2 = F[i2], f3 = F[i3];
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-                const float w0 = ex2_sfu(lik_x2(f0, cq[p])), w1 = ex2_sfu(lik_x2(f1, cq[p])),
-                            w2 = ex2_sfu(lik_x2(f2, cq[p])), w3 = ex2_sfu(lik_x2(f3, cq[p]));
+                const float w0 = lik_w(lik_x2(f0, cq[p])), w1 = lik_w(lik_x2(f1, cq[p])),
+                            w2 = lik_w(lik_x2(f2, cq[p])), w3 = lik_w(lik_x2(f3, cq[p]));
                 kadd(s[p], (w0 + w1) + (w2 + w3));
                 if (ADJ) {
                     kadd(t0[p], __fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
@@ -357,7 +403,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
             const float4 f = F[Bl.ids[q]];
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-                const float w = ex2_sfu(lik_x2(f, cq[p]));
+                const float w = lik_w(lik_x2(f, cq[p]));
                 kadd(s[p], w);
                 if (ADJ) {
                     kadd(t0[p], w * f.y);
@@ -407,8 +453,8 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
             for (int i = 0; i < k; ++i) {
                 const bool in = Bl.cflag[c0 + i] != 0;
                 const float4 f = F[T.cites[c0 + i]];
-                const float x2 = lik_x2(f, c);
-                const float w = ex2_sfu(x2);
+                const X2 x2 = lik_x2(f, c);
+                const float w = lik_w(x2);
                 const double W = in ? (double)w * beta : (double)w;
                 if (!ADJ) {
                     // log D_i - log Z_a = log(1 - u), u = P_i / Z_a in [0, 1)
@@ -418,7 +464,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
                         lr = (double)log1m_pg((float)u);
                     else
                         lr = log_pg(Z - Pc) - logZ;
-                    const double x = (double)x2 * kLn2d;
+                    const double x = ((double)x2.h + (double)x2.l) * kLn2d;
                     l += (in ? x + lbe : x) - (logZ + lr);
                 } else {
                     const double D = Z - Pc;

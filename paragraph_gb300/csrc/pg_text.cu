@@ -8,6 +8,7 @@
 // writes the digits, so a 60M-edge graph becomes text in a few milliseconds and leaves the device
 // in one copy.
 #include "pg_engine.cuh"
+#include "pg_fmt.cuh"
 
 namespace pg {
 
@@ -105,4 +106,113 @@ void launch_text_write(const int64_t* fo, const int32_t* fc, int64_t n, int64_t 
     k_text_write<<<(unsigned)g, 256, 0, s>>>(fo, fc, n, m, ids, off, out);
 }
 
+
+// ---------------------------------------------------------------- the attribute file
+// Restates Graph::WriteAttributes (src/graph.cu:1057-1218): one line per node,
+//   id,type,year,pa_weight,rec_weight,fit_weight,fit_lag_duration,fit_peak_value,
+//   fit_peak_duration,alpha,in_degree,out_degree,assigned_out_degree,planted_line,generators
+// with the weights and alpha as "%.10g", the peak as "%d" (refcompat's integer peak) or "%.9g" of
+// the fp32 fitness, seeds typed "seed" with "no_generators", agents typed "agent" with their
+// generator ids joined by ';' ("-1" when there is none).  Year, fitness and degrees come from the
+// arena; the per-paper draws, printed ids and generators from the caller.  Pass 1 measures every
+// line (no output buffer), the scan places them, pass 2 writes them.
+
+struct LineOut {
+    char* p;  // null: count only
+    int n;
+    __device__ __forceinline__ void put(char c) {
+        if (p) p[n] = c;
+        ++n;
+    }
+    __device__ __forceinline__ void str(const char* s) {
+        while (*s) put(*s++);
+    }
+    __device__ __forceinline__ void dec(int64_t v) {
+        const int l = dec_len(v);
+        if (p) dec_write(p + n, v, l);
+        n += l;
+    }
+    __device__ __forceinline__ void g(double x, int prec) {
+        char b[32];
+        const int l = fmt_g(x, prec, b);
+        for (int i = 0; i < l; ++i) put(b[i]);
+    }
+};
+
+__device__ int attr_line(const AttrCols& C, int64_t v, char* p) {
+    LineOut o{p, 0};
+    const bool seed = v < C.n_seed;
+    const double* d = C.draws + v * 4;
+    const int32_t* q = C.ints + v * 4;
+    o.dec(C.ids[v]);
+    o.str(seed ? ",seed," : ",agent,");
+    o.dec(C.pub[v]);
+    for (int i = 0; i < 3; ++i) {
+        o.put(',');
+        o.g(d[i], 10);
+    }
+    o.put(',');
+    o.dec(q[0]);
+    o.put(',');
+    if (C.peak_int)
+        o.dec((int64_t)(int32_t)C.fit[v]);
+    else
+        o.g((double)C.fit[v], 9);
+    o.put(',');
+    o.dec(q[1]);
+    o.put(',');
+    o.g(d[3], 10);
+    o.put(',');
+    o.dec(C.indeg[v]);
+    o.put(',');
+    o.dec(C.fo[v + 1] - C.fo[v]);
+    o.put(',');
+    o.dec(q[2]);
+    o.put(',');
+    o.dec(q[3]);
+    o.put(',');
+    if (seed) {
+        o.str("no_generators");
+    } else {
+        int k = 0;
+        for (int i = 0; i < 4; ++i) {
+            const int64_t gid = C.gens[v * 4 + i];
+            if (gid < 0) continue;
+            if (k++) o.put(';');
+            o.dec(gid);
+        }
+        if (!k) o.str("-1");
+    }
+    o.put('\n');
+    return o.n;
+}
+
+__global__ void __launch_bounds__(128) k_attr_len(AttrCols C, int32_t* len) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < C.n; v += (int64_t)gridDim.x * blockDim.x)
+        len[v] = attr_line(C, v, nullptr);
+}
+
+__global__ void __launch_bounds__(128) k_attr_write(AttrCols C, const int64_t* off, char* out) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < C.n; v += (int64_t)gridDim.x * blockDim.x)
+        attr_line(C, v, out + off[v]);
+}
+
+void launch_attr_text(const AttrCols& C, int32_t* len, const int64_t* off, char* out, int num_sms,
+                      cudaStream_t s) {
+    if (C.n <= 0) return;
+    int64_t g = (C.n + 127) / 128;
+    if (g > (int64_t)num_sms * 16) g = (int64_t)num_sms * 16;
+    if (out)
+        k_attr_write<<<(unsigned)g, 128, 0, s>>>(C, off, out);
+    else
+        k_attr_len<<<(unsigned)g, 128, 0, s>>>(C, len);
+}
+
 }  // namespace pg
+
+// C's "%.<precision>g" of x (the device attribute writer's conversion, compiled for the host).
+extern "C" int32_t pg_format_g_host(double x, int32_t precision, char* out) {
+    if (precision < 1) precision = 1;
+    if (precision > 13) precision = 13;
+    return pg::fmt_g(x, precision, out);
+}

@@ -72,7 +72,7 @@ def test_refcompat_gpu_choices_follow_the_reference_rule(gpu):
     bag, rec = W.rc_tables(seed=seed, bag_mean=12.0)
     rc = RCParams(pa_weight=-1.0, rec_weight=-1.0, fit_weight=-1.0, alpha=-1.0,
                   fully_random=0.1, same_year=0.0, growth_rate=0.5)
-    with GrowthEngine(seed=seed + 1000, weight_model=PG_WEIGHTS_REFCOMPAT) as eng:
+    with GrowthEngine(seed=seed + 1000, weight_model=PG_WEIGHTS_REFCOMPAT, record_trace=True) as eng:
         eng.load_graph(g.pub, g.fitness, g.src, g.dst, PAParams(growth_rate=rc.growth_rate),
                        planned_epochs=1)
         eng.rc_configure(rc, bag, rec)

@@ -333,3 +333,36 @@ def test_format_edges_text(gpu):
         assert txt == expect
         with pytest.raises(PGError):
             eng.format_edges(ids[:-1])
+
+
+@pytest.mark.parametrize("peak_integer", [False, True])
+def test_format_attributes_text(gpu, peak_integer):
+    """The device attribute writer prints the same bytes as C's printf with the reference's row
+    format (Python's %-formatting follows the same rules and rounding)."""
+    g = W.plain_pa_seed(3000, 5, seed=8)
+    rng = np.random.default_rng(3)
+    with GrowthEngine(seed=4, record_trace=True) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, PAParams(fixed_new_nodes=700), planned_epochs=2)
+        eng.grow_epoch()
+        eng.grow_epoch()
+        n, _ = eng.counts()
+        n0 = g.n
+        ids = 10**12 + 7 * np.arange(n, dtype=np.int64) - 5
+        ids[0] = -3
+        draws = np.where(np.arange(n)[:, None] < n0, -1.0, rng.random((n, 4)) ** rng.integers(1, 30, (n, 4)))
+        draws[n0 + 1] = [0.0, 1.0, 0.5, 1e-300]
+        ints = rng.integers(-1, 3000, (n, 4)).astype(np.int32)
+        gens = np.where(rng.random((n, 4)) < 0.5, -1, rng.integers(0, 10**13, (n, 4)))
+        gens[n0 + 2] = -1
+        txt = eng.format_attributes(ids, draws, ints, gens, n0, peak_integer).decode()
+        pub, fit = eng.nodes()
+        ind, outd = eng.degrees()
+    lines = []
+    for v in range(n):
+        peak = "%d" % int(fit[v]) if peak_integer else "%.9g" % float(fit[v])
+        gen = ("no_generators" if v < n0 else
+               (";".join(str(x) for x in gens[v] if x >= 0) or "-1"))
+        lines.append("%d,%s,%d,%.10g,%.10g,%.10g,%d,%s,%d,%.10g,%d,%d,%d,%d,%s\n" % (
+            ids[v], "seed" if v < n0 else "agent", pub[v], draws[v, 0], draws[v, 1], draws[v, 2],
+            ints[v, 0], peak, ints[v, 1], draws[v, 3], ind[v], outd[v], ints[v, 2], ints[v, 3], gen))
+    assert txt == "".join(lines)
