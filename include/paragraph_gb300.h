@@ -180,6 +180,11 @@ pg_status pg_run_epochs(pg_ctx* ctx, int32_t num_epochs, int32_t use_graph, int6
 /* One Erdos-Renyi G(n,p) epoch on replica 0: delta new nodes, each linking to every pre-epoch node
  * with probability p, by geometric skips. */
 pg_status pg_er_epoch(pg_ctx* ctx, int64_t delta, double p, int64_t* new_edges);
+/* num_epochs ER epochs of delta new nodes each, enqueued without host synchronisation between them
+ * (the node counts of every epoch are known in advance; the arena is sized for the run from an
+ * 8-sigma bound on its edges, and a device check stops the run with PG_ERR_CAPACITY if it is
+ * exceeded).  Edges and graph equal num_epochs calls of pg_er_epoch. */
+pg_status pg_run_er_epochs(pg_ctx* ctx, int32_t num_epochs, int64_t delta, double p, int64_t* new_edges);
 /* Grow a single-replica context to hold at least n_cap nodes and m_cap citations before its
  * epochs run (ER epochs, whose edge count a PA plan does not cover, otherwise grow the arena
  * through the host when they outrun it).  No-op when the capacity suffices; growing the arena
@@ -345,6 +350,13 @@ typedef struct {
 pg_status pg_trace_load(pg_ctx* ctx, const pg_trace_desc* trace);
 /* log L at each of batch points theta[b] = (alpha, tau, gamma, beta) (row-major [batch][4]).  Saves
  * the per-agent normalisers Z_a for pg_loglik_bwd. */
+/* Weights of the next forward passes (and of the adjoint passes that follow them): exact = 0 takes
+ * 2^x from the GPU's special-function unit (relative error < 2^-22, the default, fastest); exact = 1
+ * from fp32 arithmetic accurate to about 2 ulp.  The unit's error is a smooth function of the
+ * argument that cancels in ratios of weights but leaves about 5e-6 of the gradient's norm where
+ * the gradient nearly vanishes (e.g. at a trace's generating parameters); exact = 1 removes it at
+ * about a third of the throughput. */
+pg_status pg_lik_set_exact_exp2(pg_ctx* ctx, int32_t exact);
 pg_status pg_loglik_fwd(pg_ctx* ctx, int32_t batch, const double* theta, double* loglik);
 /* Adjoint: grad[b][k] = dloglik[b] * d log L / d theta_k at the points of the last pg_loglik_fwd
  * (theta must be the same; dloglik NULL means all ones).  Weights are recomputed, not stored. */

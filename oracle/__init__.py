@@ -41,6 +41,7 @@ def _load() -> C.CDLL:
     sig = {
         "og_philox": (None, [vp, vp, vp]),
         "og_logf": (C.c_float, [C.c_float]),
+        "og_logf_max_ulp": (C.c_double, [C.c_float, C.c_float]),
         "og_expf": (C.c_float, [C.c_float]),
         "og_log": (C.c_double, [C.c_double]),
         "og_exp": (C.c_double, [C.c_double]),

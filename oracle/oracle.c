@@ -151,6 +151,22 @@ float og_logf(float x) {
     return fmaf(ef, 0x1.62e430p-1f, fmaf(ef, -0x1.05c610p-29f, lm));
 }
 
+double og_logf_max_ulp(float lo, float hi) {
+    uint32_t a = bits_of_f(lo), b = bits_of_f(hi);
+    double worst = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : worst)
+    for (int64_t i = (int64_t)a; i <= (int64_t)b; i++) {
+        const float x = f_from_bits((uint32_t)i);
+        const double t = log((double)x);
+        const float tf = (float)t;
+        if (tf == 0.0f) continue;
+        const double ulp = fabs((double)nextafterf(tf, 0.0f) - (double)tf);
+        const double e = fabs((double)og_logf(x) - t) / ulp;
+        if (e > worst) worst = e;
+    }
+    return worst;
+}
+
 double og_exp(double x) {
     if (isnan(x)) return x;
     if (x > 709.0) return INFINITY;

@@ -20,6 +20,9 @@ typedef struct og_graph og_graph;
 /* elementary building blocks (independent restatements) */
 void og_philox(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);
 float og_logf(float x);
+/* Largest error of og_logf over every float in [lo, hi] (0 < lo <= hi), in units in the last place
+ * of the correctly rounded result; the ER skip's fp32 estimate relies on it being below 2. */
+double og_logf_max_ulp(float lo, float hi);
 float og_expf(float x);
 double og_log(double x);
 double og_exp(double x);

@@ -41,7 +41,7 @@ EXPORTED = [
     "pg_set_tuning", "pg_get_tuning", "pg_autotune", "pg_copy_anchors", "pg_trace_load",
     "pg_loglik_fwd", "pg_loglik_bwd", "pg_rc_configure", "pg_rc_set_nodes", "pg_rc_copy_agents",
     "pg_rc_bag_table", "pg_rc_fitness_table", "pg_format_edges", "pg_set_wait_limit",
-    "pg_format_attributes", "pg_format_g_host",
+    "pg_format_attributes", "pg_format_g_host", "pg_run_er_epochs", "pg_lik_set_exact_exp2",
 ]
 
 
@@ -258,6 +258,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_set_wait_limit": (i32, [vp, i64]),
         "pg_format_attributes": (i32, [vp, i32, P(_AttrRows), vp, i64, P(i64)]),
         "pg_format_g_host": (i32, [C.c_double, i32, C.c_char_p]),
+        "pg_run_er_epochs": (i32, [vp, i32, i64, C.c_double, P(i64)]),
+        "pg_lik_set_exact_exp2": (i32, [vp, i32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -422,6 +424,12 @@ class GrowthEngine:
         self._check(self._lib.pg_er_epoch(self._ctx, delta, p, C.byref(ne)))
         return ne.value
 
+    def run_er_epochs(self, epochs: int, delta: int, p: float) -> int:
+        """`epochs` ER epochs of `delta` new nodes without host synchronisation between them."""
+        ne = C.c_int64()
+        self._check(self._lib.pg_run_er_epochs(self._ctx, int(epochs), int(delta), float(p), C.byref(ne)))
+        return ne.value
+
     def reserve(self, n_cap: int, m_cap: int) -> None:
         """Grow a single-replica context to n_cap nodes and m_cap citations ahead of its epochs."""
         self._check(self._lib.pg_reserve(self._ctx, int(n_cap), int(m_cap)))
@@ -584,6 +592,11 @@ class GrowthEngine:
                        _ptr(t.seed_dst), t.num_epochs, t.num_anchors, _ptr(t.epoch_nodes),
                        _ptr(t.epoch_t), _ptr(t.anchors), _ptr(t.cite_off), _ptr(t.cites))
         self._check(self._lib.pg_trace_load(self._ctx, C.byref(d)))
+
+    def set_lik_exact_exp2(self, exact: bool) -> None:
+        """Weights of the next likelihood passes from an fp32 exp2 accurate to ~2 ulp (True) or the
+        special-function unit's (False, default)."""
+        self._check(self._lib.pg_lik_set_exact_exp2(self._ctx, 1 if exact else 0))
 
     def loglik(self, theta) -> np.ndarray:
         """log L at each row (alpha, tau, gamma, beta) of theta (forward pass)."""

@@ -62,6 +62,8 @@ struct LikState {
     bool balls_cached = false;               // one chunk: built at load, reused by every pass
     int64_t ball_elems = 0, adj_entries = 0, citations = 0;
     std::vector<double> fwd_theta;  // points of the last forward pass
+    int32_t exact_exp2 = 0;         // pg_lik_set_exact_exp2
+    int32_t fwd_exact_exp2 = 0;     // the mode of the last forward pass (the adjoint reuses it)
 };
 
 struct Checkpoint {
@@ -95,7 +97,8 @@ struct pg_ctx {
     // device buffers
     DBuf<Replica> rep;
     DBuf<EpochState> st;
-    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, heavy_list, heavy_mark, e_dst, e_rank, arrivals, hlist, anchors, tile_row;
+    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, heavy_list, heavy_mark, e_dst, e_rank, arrivals, hlist, anchors, tile_row,
+        ev_pre;
     DBuf<int16_t> hslot;
     DBuf<uint64_t> hub2;
     DBuf<uint32_t> hub_need;
@@ -217,6 +220,7 @@ Arena make_arena(pg_ctx* c) {
     A.big_list = c->big_list.p;
     A.heavy_list = c->heavy_list.p;
     A.heavy_mark = c->heavy_mark.p;
+    A.ev_pre = c->ev_pre.p;
     A.tile_row = c->tile_row.p;
     A.len_tmp = c->len_tmp.p;
     A.tilesum = c->tilesum.p;
@@ -415,6 +419,8 @@ pg_status alloc_epoch_buffers(pg_ctx* c, int64_t agent_cap, int64_t edge_cap, in
         PG_CUDA(c, dalloc(c->big_list, agent_cap));
         PG_CUDA(c, dalloc(c->heavy_list, agent_cap));
         PG_CUDA(c, dalloc(c->heavy_mark, agent_cap));
+        if (c->cfg.sampler == PG_SAMPLER_THINNING && c->cfg.weight_model == PG_WEIGHTS_BASELINE)
+            PG_CUDA(c, dalloc(c->ev_pre, (int64_t)kPreEvents * agent_cap));
         PG_CUDA(c, dalloc(c->eoff, agent_cap + 1));
         if (c->cfg.record_trace) PG_CUDA(c, dalloc(c->anchors, 4 * agent_cap));
         if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) PG_CUDA(c, dalloc(c->rc_agent, 6 * agent_cap));
@@ -797,6 +803,8 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
     if (c->cfg.sampler == PG_SAMPLER_THINNING) {
         launch_hub_pairs(A, s);  // for the hubs the setup found among the anchors
         PG_STAGE("hub pairs");
+        launch_events(A, agents, c->num_sms, s);
+        PG_STAGE("events");
     }
     if (events) record_event(ev[2], s);
     launch_agents(A, agents, c->num_sms, s);
@@ -991,7 +999,7 @@ void pg_destroy(pg_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     destroy_graph_exec(c);
-    DBuf<int32_t>* i32[] = {&c->tile_rep, &c->tile_row, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list, &c->heavy_list, &c->heavy_mark,
+    DBuf<int32_t>* i32[] = {&c->tile_rep, &c->tile_row, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list, &c->heavy_list, &c->heavy_mark, &c->ev_pre,
                             &c->e_dst, &c->e_rank, &c->arrivals, &c->anchors, &c->fwd_col, &c->bwd_col[0],
                             &c->bwd_col[1]};
     for (auto* b : i32) dfree(*b);
@@ -1389,6 +1397,71 @@ pg_status pg_er_epoch(pg_ctx* c, int64_t delta, double p, int64_t* new_edges) {
     return PG_OK;
 }
 
+pg_status pg_run_er_epochs(pg_ctx* c, int32_t num_epochs, int64_t delta, double p, int64_t* new_edges) {
+    if (!c) return PG_ERR_ARG;
+    if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
+    if (c->R != 1) return fail(c, PG_ERR_ARG, "ER epochs run on single-replica contexts");
+    if (c->poisoned) return fail(c, PG_ERR_STATE, "an earlier epoch failed on the device; reload the graph");
+    if (num_epochs < 1 || delta <= 0 || std::isnan(p)) return fail(c, PG_ERR_ARG, "need num_epochs >= 1, delta > 0 and a numeric p");
+    if (p > 1.0) p = 1.0;
+    PG_CUDA(c, cudaSetDevice(c->device));
+    const int64_t n0 = c->hrep[0].n, m0 = c->hrep[0].m;
+    const double pe = p > 0.0 ? p : 0.0;
+    // every epoch's node count is known; edges are bounded per epoch by mean + 8 sigma
+    int64_t need_m = m0, max_eb = 0, max_tasks = 0;
+    for (int e = 0; e < num_epochs; ++e) {
+        const int64_t n = n0 + (int64_t)e * delta;
+        const double mu = (double)delta * (double)n * pe;
+        const int64_t eb = std::min<int64_t>((int64_t)std::ceil(mu + 8.0 * std::sqrt(mu) + 1024.0), delta * n);
+        need_m += eb;
+        max_eb = std::max(max_eb, eb);
+        max_tasks = std::max(max_tasks, delta * ((n + kErChunk - 1) / kErChunk));
+    }
+    pg_status s = ensure_capacity(c, n0 + (int64_t)num_epochs * delta, need_m);
+    if (s != PG_OK) return s;
+    s = alloc_epoch_buffers(c, delta, max_eb, max_tasks);
+    if (s != PG_OK) return s;
+    if (c->er_cnt.n < max_tasks + 1) PG_CUDA(c, dalloc(c->er_cnt, max_tasks + 1));
+    if (c->er_toff.n < max_tasks + 1) PG_CUDA(c, dalloc(c->er_toff, max_tasks + 1));
+    cudaStream_t st = c->stream;
+    const int p0 = c->parity;
+    const size_t cum0 = offsetof(EpochState, cum_rows_expanded);
+    PG_CUDA(c, cudaMemsetAsync(reinterpret_cast<char*>(c->st.p) + cum0, 0, sizeof(EpochState) - cum0, st));
+    cudaGetLastError();
+    if (c->timing) cudaEventRecord(c->ev[0], st);
+    for (int e = 0; e < num_epochs; ++e) {
+        Arena A = make_arena(c);
+        launch_epoch_begin_delta(A, c->epoch + e, delta, st);
+        launch_er_epoch(A, delta, p, n0 + (int64_t)e * delta, c->er_cnt.p, c->er_toff.p, c->num_sms, st);
+        launch_bwd_append(A, delta, c->num_sms, st, c->side, c->fork, c->join);
+        c->parity ^= 1;
+    }
+    if (c->timing) cudaEventRecord(c->ev[1], st);
+    c->parity = p0;
+    PG_CUDA(c, cudaGetLastError());
+    s = read_back(c);
+    if (s != PG_OK) return s;
+    s = device_error(c);
+    if (s != PG_OK) return s;
+    HostRep& h = c->hrep[0];
+    h.n = c->h_rep[0].n;
+    h.m = c->h_rep[0].m;
+    if (num_epochs % 2) c->parity ^= 1;
+    c->epoch += num_epochs;
+    c->rep_last_first[0] = h.m - (int64_t)c->h_st.edges;  // the last epoch's edges
+    c->rep_last_count[0] = (int64_t)c->h_st.edges;
+    fill_stats(c, delta, true);
+    c->stats.run_epochs = num_epochs;
+    c->stats.run_new_nodes = (int64_t)num_epochs * delta;
+    c->stats.run_new_edges = h.m - m0;
+    if (c->timing) {
+        c->stats.ms_er = c->stats.ms_total = ms_between(c->ev[0], c->ev[1]);
+        c->stats.ms_weights = c->stats.ms_setup = c->stats.ms_agents = c->stats.ms_csr = 0.0;
+    }
+    if (new_edges) *new_edges = h.m - m0;
+    return PG_OK;
+}
+
 pg_status pg_reserve(pg_ctx* c, int64_t n_cap, int64_t m_cap) {
     if (!c) return PG_ERR_ARG;
     if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
@@ -1642,6 +1715,13 @@ pg_status pg_set_tuning(pg_ctx* c, const pg_tuning* t) {
         c->tune = *t;
         destroy_graph_exec(c);  // captured launches carry the old grid sizes
     }
+    return PG_OK;
+}
+
+pg_status pg_lik_set_exact_exp2(pg_ctx* c, int32_t exact) {
+    if (!c) return PG_ERR_ARG;
+    if (exact != 0 && exact != 1) return fail(c, PG_ERR_ARG, "exact must be 0 or 1");
+    c->lik.exact_exp2 = exact;
     return PG_OK;
 }
 
@@ -2058,6 +2138,7 @@ LikBalls make_balls(const LikState& L, int64_t a0) {
 // One pass (forward or adjoint) over every group of <= 64 points; results[b * K + k].
 pg_status run_lik(pg_ctx* c, int32_t batch, const double* theta, int adjoint, double* results) {
     LikState& L = c->lik;
+    if (!adjoint) L.fwd_exact_exp2 = L.exact_exp2;
     const int groups = (batch + kLikMaxB - 1) / kLikMaxB;
     const int K = adjoint ? 4 : 1;
     const int64_t zneed = (int64_t)groups * std::max<int64_t>(L.agents, 1) * kLikMaxB;
@@ -2104,6 +2185,7 @@ pg_status run_lik(pg_ctx* c, int32_t batch, const double* theta, int adjoint, do
         P.BE = 1;
         while (P.BE < P.B) P.BE <<= 1;
         P.BW = std::min(P.BE, 32);
+        P.exact_exp2 = adjoint ? L.fwd_exact_exp2 : L.exact_exp2;
         P.theta = L.theta.p + 4 * (int64_t)g * kLikMaxB;
         P.pp = L.pp.p + 8 * (int64_t)g * kLikMaxB;
         P.zglob = L.zglob.p + (int64_t)g * L.epochs * kLikMaxB;

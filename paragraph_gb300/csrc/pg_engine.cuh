@@ -39,6 +39,7 @@ constexpr int kRcAgeMax = 1024;      // recency probabilities by age 0..1023 (re
 constexpr int kRcFitMax = 1000;      // peak fitness values 1..1000 (refcompat)
 constexpr uint32_t kRcFillBlocks = 1u << 20;  // Philox blocks a uniform fill may use
 constexpr uint32_t kWaitPolls = 1u << 22;     // polls of a bounded wait on an asynchronous copy
+constexpr int kPreEvents = 64;       // thinning events per agent drawn ahead by k_events (two batches)
 
 enum Sampler : int32_t {
     kSamplerThinning = 0,   // Poisson thinning against ball membership (default)
@@ -154,6 +155,7 @@ struct Arena {
     int32_t* big_list;         // [agent cap]
     int32_t* heavy_list;       // [agent cap] agents with a hub or a large frontier (k <= kKSmall)
     int32_t* heavy_mark;       // [agent cap] 1 when the agent is on heavy_list
+    int32_t* ev_pre;           // [agent cap][kPreEvents] first thinning events: node | global << 31, or null
     int32_t* zbig;             // [agent-kernel warp slots][1 << kGBits] rows of anchors too large for H
     int32_t* rc_big_id;        // [kRcBigCap][kKMax] sorted top of each listed refcompat agent's 2-hop stream
     long long* rc_big_meta;    // [kRcBigCap][3] entries, rows, elements of that stream
@@ -296,6 +298,30 @@ __device__ __forceinline__ T block_excl_scan(T v, T* smem_warp, T* total) {
     return out;
 }
 
+// Geometric skip of one ER draw, floor(log_pg(u) * inv_l) exactly, u = u01d(lo, hi), inv_l =
+// 1 / log(1 - p) <= 0.  An fp32 estimate y = logf_pg(u) * inv_l decides it unless an integer lies
+// within its error bound: |y - y64| <= |inv_l| 2^-24 (u rounded to fp32 moves log u by at most
+// 2^-24) + |y| 3 2^-23 (logf_pg is within 2 ulp on [2^-60, 1] -- checked there exhaustively --
+// plus the fp32 roundings of inv_l and of the product) + |y64| 2^-50 (the FP64 expression's own
+// error).  The bound used, d = |inv_l| 2^-23 + |y| 2^-20, is at least twice that and also covers
+// the roundings of y - d and y + d.  Only when floor(y - d) != floor(y + d) is the FP64 expression
+// evaluated (for about 2 d of the draws: under 0.3 % at p = 1e-3); a skip known to reach `cap` (the
+// chunk's remaining length) ends the walk whatever its exact value.  GB300's FP64 rate is a small
+// fraction of its FP32 rate, so the fp32 estimate is what makes the walk cheap.
+struct ErSkip {
+    double inv_l;  // 1 / log(1 - p)
+    float inv_f;   // inv_l rounded to fp32
+    float dabs;    // |inv_l| 2^-23, rounded up
+};
+__device__ __forceinline__ double er_skip(const ErSkip& K, uint32_t lo, uint32_t hi, float cap) {
+    const double u = u01d(lo, hi);
+    const float y = logf_pg((float)u) * K.inv_f;
+    const float d = __fmaf_rn(y, 0x1p-20f, K.dabs);
+    const float a = floorf(y - d);
+    if (a >= cap || a == floorf(y + d)) return (double)a;
+    return floor(log_pg(u) * K.inv_l);
+}
+
 // Replica of a global agent index: largest r with abase_r <= a.
 __device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64_t a) {
     int lo = 0, hi = R - 1;
@@ -314,9 +340,9 @@ __device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64
 // Kernels one PA epoch enqueues: epoch begin (1), weights + CDF (4), agent setup + offset scan +
 // check (5), agent kernels (2), backward append incl. epoch end (8).
 constexpr int kPaEpochKernels = 20;
-// Extra kernels of the thinning sampler: the CDF's guide table (1) and the hub index (histogram,
-// pick, collect, mask, hub pairs).
-constexpr int kThinKernels = 6;
+// Extra kernels of the thinning sampler: the CDF's guide table (1), the hub index (histogram,
+// pick, collect, mask, hub pairs) and the events drawn ahead (1).
+constexpr int kThinKernels = 7;
 void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s);
 void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cudaStream_t s);
 void launch_weights(const Arena& A, cudaStream_t s);
@@ -326,6 +352,8 @@ void launch_guide(const Arena& A, cudaStream_t s);
 void launch_tile_scan(const Arena& A, int mode, cudaStream_t s);
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s);
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
+// the first kPreEvents thinning events of every agent (after the guide table and the agent setup)
+void launch_events(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
 // side/fork/join (optional): the old-entry copy runs on `side` beside the new-entry placement and sorts
 void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s, cudaStream_t side = nullptr,
                        cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
@@ -337,6 +365,8 @@ void launch_rc_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t 
 cudaError_t init_rc_kernels();
 void launch_er_epoch(const Arena& A, int64_t delta, double p, int64_t n, int64_t* cnt,
                      int64_t* toff, int num_sms, cudaStream_t s);
+// the skip constants of probability p (host)
+ErSkip er_skip_constants(double p);
 // generic exclusive scan of n values; out has n+1 entries (out[n] = total)
 void launch_scan_i64(const int64_t* in, int64_t* out, int64_t n, int64_t* blocksum, cudaStream_t s);
 void launch_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_t* blocksum,

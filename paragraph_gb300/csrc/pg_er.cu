@@ -10,7 +10,9 @@
 // group of lanes walks it, drawing consecutive gaps together.  A count pass, an exclusive scan and
 // an emit pass that replays the same streams write the edges in (source, target) order with no
 // sort.
-// log is the library's own fp64 log, so the edge list is bit-identical to the CPU oracle.
+// The skip is floor(log(u) / log(1 - p)) with the library's own fp64 log, so the edge list is
+// bit-identical to the CPU oracle; an fp32 estimate with a proven error bound decides almost every
+// skip and the FP64 expression runs only when an integer lies within that bound (er_skip).
 #include "pg_engine.cuh"
 
 namespace pg {
@@ -18,7 +20,7 @@ namespace pg {
 constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ int64_t er_walk(const Arena& A, int64_t i, int64_t c, int64_t n,
-                                           double inv_l, int32_t* out, int64_t out_base,
+                                           const ErSkip& K, int32_t* out, int64_t out_base,
                                            int32_t* col_out, int64_t col_base) {
     const int64_t lo = c * kErChunk;
     const int64_t hi = lo + kErChunk < n ? lo + kErChunk : n;
@@ -28,9 +30,9 @@ __device__ __forceinline__ int64_t er_walk(const Arena& A, int64_t i, int64_t c,
     x.x[0] = x.x[1] = x.x[2] = x.x[3] = 0;
     for (uint32_t d = 0;; ++d) {
         if ((d & 1u) == 0) x = draw(A.seed, kStreamEr, (uint32_t)c, ep, (uint32_t)i, d >> 1);
-        const double u = (d & 1u) ? u01d(x.x[2], x.x[3]) : u01d(x.x[0], x.x[1]);
-        const double sk = floor(log_pg(u) * inv_l);
-        if (sk >= (double)(hi - pos - 1)) break;
+        const double rem = (double)(hi - pos - 1);
+        const double sk = (d & 1u) ? er_skip(K, x.x[2], x.x[3], (float)rem) : er_skip(K, x.x[0], x.x[1], (float)rem);
+        if (sk >= rem) break;
         pos = pos + 1 + (int64_t)sk;
         if (out) {
             out[out_base + cnt] = (int32_t)pos;
@@ -55,12 +57,12 @@ __global__ void __launch_bounds__(256) k_er_setup(Arena A, int64_t delta) {
 }
 
 __global__ void __launch_bounds__(256) k_er_count(Arena A, int64_t tasks, int64_t chunks,
-                                                  double inv_l, int64_t* cnt) {
+                                                  ErSkip K, int64_t* cnt) {
     if (A.st->error) return;
     const int64_t n = A.rep[0].n;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tasks;
          t += (int64_t)gridDim.x * blockDim.x)
-        cnt[t] = er_walk(A, t / chunks, t % chunks, n, inv_l, nullptr, 0, nullptr, 0);
+        cnt[t] = er_walk(A, t / chunks, t % chunks, n, K, nullptr, 0, nullptr, 0);
 }
 
 __global__ void k_er_check(Arena A, const int64_t* toff, int64_t tasks) {
@@ -72,7 +74,7 @@ __global__ void k_er_check(Arena A, const int64_t* toff, int64_t tasks) {
 }
 
 __global__ void __launch_bounds__(256) k_er_emit(Arena A, int64_t tasks, int64_t chunks,
-                                                 double inv_l, const int64_t* toff) {
+                                                 ErSkip K, const int64_t* toff) {
     if (A.st->error) return;
     const Replica& rp = A.rep[0];
     const int64_t n = rp.n;
@@ -81,7 +83,7 @@ __global__ void __launch_bounds__(256) k_er_emit(Arena A, int64_t tasks, int64_t
          t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = t / chunks, c = t % chunks;
         const int64_t e0 = toff[t];
-        const int64_t cnt = er_walk(A, i, c, n, inv_l, A.e_dst, e0, fcol, rp.m + e0);
+        const int64_t cnt = er_walk(A, i, c, n, K, A.e_dst, e0, fcol, rp.m + e0);
         if (A.arrivals)
             for (int64_t q = 0; q < cnt; ++q) A.arrivals[e0 + q] = A.e_dst[e0 + q];
         if (c == chunks - 1) A.fwd_off[rp.obase + n + i + 1] = rp.m + e0 + cnt;
@@ -95,7 +97,7 @@ __global__ void __launch_bounds__(256) k_er_emit(Arena A, int64_t tasks, int64_t
 // stays in the loop until all of its groups are done (the shuffles span the warp).
 template <int G>
 __device__ __forceinline__ int64_t er_walk_group(const Arena& A, bool live, int64_t i, int64_t c, int64_t n,
-                                                 double inv_l, int32_t* out, int64_t out_base,
+                                                 const ErSkip& K, int32_t* out, int64_t out_base,
                                                  int32_t* col_out, int64_t col_base) {
     const int lane = lane_id(), gl = lane & (G - 1);
     const unsigned gm = G == 32 ? kFull : (((1u << G) - 1u) << (lane & ~(G - 1)));
@@ -109,8 +111,8 @@ __device__ __forceinline__ int64_t er_walk_group(const Arena& A, bool live, int6
         if (act) {
             const uint32_t d = d0 + (uint32_t)gl;
             const u32x4 x = draw(A.seed, kStreamEr, (uint32_t)c, ep, (uint32_t)i, d >> 1);
-            const double u = (d & 1u) ? u01d(x.x[2], x.x[3]) : u01d(x.x[0], x.x[1]);
-            const double sk = floor(log_pg(u) * inv_l);
+            const double sk = (d & 1u) ? er_skip(K, x.x[2], x.x[3], (float)kErChunk)
+                                       : er_skip(K, x.x[0], x.x[1], (float)kErChunk);
             step = sk < 1099511627776.0 ? (int64_t)sk + 1 : ((int64_t)1 << 40);  // 2^40: past any chunk
         }
         int64_t incl = step;
@@ -137,7 +139,7 @@ __device__ __forceinline__ int64_t er_walk_group(const Arena& A, bool live, int6
 }
 
 template <int G>
-__global__ void __launch_bounds__(256) k_er_count_g(Arena A, int64_t tasks, int64_t chunks, double inv_l,
+__global__ void __launch_bounds__(256) k_er_count_g(Arena A, int64_t tasks, int64_t chunks, ErSkip K,
                                                     int64_t* cnt) {
     if (A.st->error) return;
     const int64_t n = A.rep[0].n;
@@ -148,13 +150,13 @@ __global__ void __launch_bounds__(256) k_er_count_g(Arena A, int64_t tasks, int6
         const int64_t t = b + (lane_id() / G);
         const bool live = t < tasks;
         const int64_t tt = live ? t : 0;
-        const int64_t c0 = er_walk_group<G>(A, live, tt / chunks, tt % chunks, n, inv_l, nullptr, 0, nullptr, 0);
+        const int64_t c0 = er_walk_group<G>(A, live, tt / chunks, tt % chunks, n, K, nullptr, 0, nullptr, 0);
         if (live && (lane_id() & (G - 1)) == 0) cnt[t] = c0;
     }
 }
 
 template <int G>
-__global__ void __launch_bounds__(256) k_er_emit_g(Arena A, int64_t tasks, int64_t chunks, double inv_l,
+__global__ void __launch_bounds__(256) k_er_emit_g(Arena A, int64_t tasks, int64_t chunks, ErSkip K,
                                                    const int64_t* toff) {
     if (A.st->error) return;
     const Replica& rp = A.rep[0];
@@ -169,7 +171,7 @@ __global__ void __launch_bounds__(256) k_er_emit_g(Arena A, int64_t tasks, int64
         const int64_t tt = live ? t : 0;
         const int64_t i = tt / chunks, c = tt % chunks;
         const int64_t e0 = toff[tt];
-        const int64_t cnt = er_walk_group<G>(A, live, i, c, n, inv_l, A.e_dst, e0, fcol, rp.m + e0);
+        const int64_t cnt = er_walk_group<G>(A, live, i, c, n, K, A.e_dst, e0, fcol, rp.m + e0);
         if (live && (lane_id() & (G - 1)) == 0 && c == chunks - 1) A.fwd_off[rp.obase + n + i + 1] = rp.m + e0 + cnt;
     }
 }
@@ -179,6 +181,15 @@ __global__ void __launch_bounds__(256) k_er_eoff(Arena A, const int64_t* toff, i
     if (A.st->error) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i <= delta) A.eoff[i] = toff[i * chunks];
+}
+
+ErSkip er_skip_constants(double p) {
+    ErSkip K;
+    K.inv_l = 1.0 / log_pg(1.0 - (p < 1.0 ? p : 1.0));
+    K.inv_f = (float)K.inv_l;
+    const float a = (float)(fabs(K.inv_l) * 0x1p-23);
+    K.dabs = nextafterf(a, INFINITY);  // rounded up
+    return K;
 }
 
 // Count, scan and emit; the caller then runs the backward append.
@@ -193,7 +204,7 @@ void launch_er_epoch(const Arena& A, int64_t delta, double p, int64_t n, int64_t
         k_er_eoff<<<(unsigned)((delta + 256) / 256), 256, 0, s>>>(A, toff, delta, chunks);
         return;
     }
-    const double inv_l = 1.0 / log_pg(1.0 - (p < 1.0 ? p : 1.0));
+    const ErSkip K = er_skip_constants(p);
     // lanes per task: about the expected successes of a full chunk (1: one thread walks a task)
     const double mu = (double)(n < kErChunk ? n : kErChunk) * (p < 1.0 ? p : 1.0);
     int G = 1;
@@ -202,22 +213,22 @@ void launch_er_epoch(const Arena& A, int64_t delta, double p, int64_t n, int64_t
     if (g > (int64_t)num_sms * 32) g = (int64_t)num_sms * 32;
     if (g < 1) g = 1;
     switch (G) {
-        case 1: k_er_count<<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, cnt); break;
-        case 2: k_er_count_g<2><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, cnt); break;
-        case 4: k_er_count_g<4><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, cnt); break;
-        case 8: k_er_count_g<8><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, cnt); break;
-        case 16: k_er_count_g<16><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, cnt); break;
-        default: k_er_count_g<32><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, cnt); break;
+        case 1: k_er_count<<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
+        case 2: k_er_count_g<2><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
+        case 4: k_er_count_g<4><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
+        case 8: k_er_count_g<8><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
+        case 16: k_er_count_g<16><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
+        default: k_er_count_g<32><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
     }
     launch_scan_i64(cnt, toff, tasks, A.blocksum, s);
     k_er_check<<<1, 32, 0, s>>>(A, toff, tasks);
     switch (G) {
-        case 1: k_er_emit<<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, toff); break;
-        case 2: k_er_emit_g<2><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, toff); break;
-        case 4: k_er_emit_g<4><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, toff); break;
-        case 8: k_er_emit_g<8><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, toff); break;
-        case 16: k_er_emit_g<16><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, toff); break;
-        default: k_er_emit_g<32><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, inv_l, toff); break;
+        case 1: k_er_emit<<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
+        case 2: k_er_emit_g<2><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
+        case 4: k_er_emit_g<4><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
+        case 8: k_er_emit_g<8><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
+        case 16: k_er_emit_g<16><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
+        default: k_er_emit_g<32><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
     }
     k_er_eoff<<<(unsigned)((delta + 256) / 256), 256, 0, s>>>(A, toff, delta, chunks);
 }

@@ -5,17 +5,20 @@
 //
 // Weights: w_j = 2^(x2_j), x2_j = log2(e) (gamma log f_j + alpha log(indeg_j+1) - (t-t_j)/tau), the
 // exponent carried as an unevaluated fp32 pair h + l: the per-point constants are split into fp32
-// high and low parts, log(indeg+1) is stored as a high/low pair, and the products and the sum of
-// the two discrete terms (log-degree, age) keep their rounding errors (FMA residuals, Knuth's
-// two-sum).  A plain fp32 exponent would round alpha log2 e, log2 e / tau and log(d+1) once for all
-// nodes that share them -- an error that does not average out over the trace and that moves the
-// gradient by the Hessian times a 2^-24 shift of theta (about 1e-5 of the gradient at the
-// generating point).  2^(h + l) is then evaluated in fp32 arithmetic (exp2_acc: exact reduction by
-// the nearest integer, Taylor series of e^t, |t| < 0.35), not by the special-function unit: the
-// unit's ex2.approx has a relative error up to 2^-22 that varies with the argument's fraction, and
-// that error, shared by every citation of a node, moved the gradient at the generating point by
-// about 1e-5 of its norm.  Weights below 2^-126 are flushed to zero.  The same weight function
-// feeds every sum below, so the normalisers and the citations' prefix sums agree.
+// high and low parts and log(indeg+1) is stored as a high/low pair.  A plain fp32 exponent rounds
+// alpha log2 e, log2 e / tau and log(d+1) once for all nodes that share them -- an error that does
+// not average out over the trace and moves the gradient by the Hessian times a 2^-24 shift of
+// theta (about 1e-5 of the gradient at the generating point, where the gradient is small).  The
+// products enter h through FMAs whose one rounding also involves the continuous fitness term, so
+// what remains differs from node to node.  2^h comes from the special-function unit (PTX
+// ex2.approx.ftz.f32, relative error < 2^-22; results below 2^-126 flush to zero) and is scaled
+// by 1 + l ln 2; or, with exact_exp2, from exp2_exact (fp32 arithmetic, about 2 ulp).  The unit's
+// error is a smooth periodic function of the argument's fraction; it cancels in every ratio of
+// weights but leaves about 5e-6 of the gradient's norm where the gradient nearly vanishes (the
+// generating point of a trace), which exp2_exact removes at some 35 % of the throughput.  The same
+// weight function feeds every sum below, so the normalisers and the citations' prefix sums agree.  The per-epoch sums over all nodes are shared by every agent of
+// the epoch, so they are accumulated in FP64 (an fp32 partial's rounding would be common to all
+// of the epoch's citations); the per-agent ball sums use compensated fp32.
 //
 // Per launch (forward or adjoint):
 //   k_lik_global      per epoch: sum_{j<n_e} w_j (forward) or sum_j w_j g_j (adjoint), one CTA per
@@ -83,12 +86,11 @@ __device__ __forceinline__ LikC lik_c(const double* pp) {
     c.it2l = (float)(t - (double)c.it2);
     return c;
 }
-// a + b = s + err exactly (Knuth's two-sum; the build neither contracts nor reassociates)
-__device__ __forceinline__ float two_sum(float a, float b, float& err) {
-    const float s = a + b;
-    const float bb = s - a;
-    err = (a - (s - bb)) + (b - bb);
-    return s;
+// 2^x on the special-function unit (PTX ex2.approx.ftz.f32).
+__device__ __forceinline__ float ex2_sfu(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 // log2 of the weight, ga2 log f + al2 log(d+1) - it2 (t - t_j), as h + l.  Features: f.x = log f,
 // f.y + f.w = log(d+1) (high, low), f.z = t - t_j (an exact integer).
@@ -96,19 +98,15 @@ struct X2 {
     float h, l;
 };
 __device__ __forceinline__ X2 lik_x2(const float4 f, const LikC& c) {
-    const float p1 = c.al2 * f.y, e1 = __fmaf_rn(c.al2, f.y, -p1);
-    const float p2 = c.it2 * f.z, e2 = __fmaf_rn(c.it2, f.z, -p2);
-    float e3;
-    const float s = two_sum(p1, -p2, e3);
     X2 x;
-    x.h = __fmaf_rn(c.ga2, f.x, s);
-    x.l = ((e1 - e2) + e3) + __fmaf_rn(c.al2, f.w, __fmaf_rn(c.al2l, f.y, __fmaf_rn(c.ga2l, f.x, -(c.it2l * f.z))));
+    x.h = __fmaf_rn(c.al2, f.y, __fmaf_rn(-c.it2, f.z, c.ga2 * f.x));
+    x.l = __fmaf_rn(c.al2, f.w, __fmaf_rn(c.al2l, f.y, __fmaf_rn(c.ga2l, f.x, -(c.it2l * f.z))));
     return x;
 }
-// 2^(h + l) for |l| < 2^-18: n = rint(h), f = h - n (exact), t = (f + l) ln 2 in [-0.35, 0.35],
-// e^t by its Taylor series through t^7/7! (truncation below 5e-9 relative), times 2^n built in the
-// exponent field; about 2 ulp in all, with rounding errors that do not depend on n.
-__device__ __forceinline__ float lik_w(const X2 x) {
+// 2^(h + l) for |l| < 2^-18 in fp32 arithmetic: n = rint(h), f = h - n (exact), t = (f + l) ln 2
+// in [-0.35, 0.35], e^t by its Taylor series through t^7/7! (truncation below 5e-9 relative), times
+// 2^n built in the exponent field: about 2 ulp, with rounding errors that vary from node to node.
+__device__ __forceinline__ float exp2_exact(const X2 x) {
     const float n = rintf(x.h);
     const int ni = (int)n;
     if (ni < -126) return 0.0f;
@@ -122,6 +120,14 @@ __device__ __forceinline__ float lik_w(const X2 x) {
     p = __fmaf_rn(p, t, 1.0f);
     p = __fmaf_rn(p, t, 1.0f);
     return p * __int_as_float((ni > 127 ? 255 : ni + 127) << 23);
+}
+// the weight 2^(h + l): EXACT selects exp2_exact, else the special-function unit's 2^h scaled by
+// 1 + l ln 2 + O(l^2)
+template <bool EXACT>
+__device__ __forceinline__ float lik_w(const X2 x) {
+    if (EXACT) return exp2_exact(x);
+    const float e = ex2_sfu(x.h);
+    return __fmaf_rn(e, x.l * kLn2f, e);
 }
 
 // 1/D for D > 0 in FP64: Newton's iteration for the reciprocal, r' = r + r (1 - D r), started from
@@ -173,7 +179,7 @@ __global__ void __launch_bounds__(256) k_lik_features(LikTrace T) {
     }
 }
 
-template <bool ADJ>
+template <bool ADJ, bool EXACT>
 __global__ void __launch_bounds__(kLikThreads) k_lik_global(LikTrace T, LikBatch P) {
     __shared__ double red[kLikThreads * 4];
     const int e = blockIdx.y, tid = threadIdx.x;
@@ -181,26 +187,26 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_global(LikTrace T, LikBatch
     const int64_t lo = (int64_t)blockIdx.x * kLikChunk;
     const int BE = P.BE, B = P.B;
     const int b = tid & (BE - 1), sub = tid / BE, nsub = kLikThreads / BE;
-    Kahan s, t0, t1, t2;
+    double s = 0.0, t0 = 0.0, t1 = 0.0, t2 = 0.0;
     if (b < B && lo < ne) {
         const LikC c = lik_c(P.pp + b * 8);
         const int64_t hi = ne < lo + kLikChunk ? ne : lo + kLikChunk;
         const float4* F = T.feat + (int64_t)e * T.n;
         for (int64_t j = lo + sub; j < hi; j += nsub) {
             const float4 f = F[j];
-            const float w = lik_w(lik_x2(f, c));
-            kadd(s, w);
+            const double w = (double)lik_w<EXACT>(lik_x2(f, c));
+            s += w;
             if (ADJ) {
-                kadd(t0, w * f.y);
-                kadd(t1, w * f.z);
-                kadd(t2, w * f.x);
+                t0 = __fma_rn(w, (double)f.y, t0);
+                t1 = __fma_rn(w, (double)f.z, t1);
+                t2 = __fma_rn(w, (double)f.x, t2);
             }
         }
     }
-    red[tid * 4 + 0] = kval(s);
-    red[tid * 4 + 1] = kval(t0);
-    red[tid * 4 + 2] = kval(t1);
-    red[tid * 4 + 3] = kval(t2);
+    red[tid * 4 + 0] = s;
+    red[tid * 4 + 1] = t0;
+    red[tid * 4 + 2] = t1;
+    red[tid * 4 + 3] = t2;
     __syncthreads();
     if (sub == 0 && b < B) {
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
@@ -358,7 +364,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_ball(LikTrace T, LikBalls B
 // per lane, FP64 across slices.  The citations are then walked in draw order by the slice-0 lane
 // of each point with FP64 running sums:  D_i = Z_a - P_i,  log D_i = log Z_a + log(1 - P_i / Z_a),
 // and in the adjoint g_i - (dZ_a - dP_i) / D_i.
-template <bool ADJ, int NP>
+template <bool ADJ, int NP, bool EXACT>
 __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P, LikBalls Bl,
                                                           int64_t a0, int64_t a1) {
     const int lane = threadIdx.x & 31;
@@ -389,8 +395,8 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
             const float4 f0 = F[i0], f1 = F[i1], f2 = F[i2], f3 = F[i3];
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-                const float w0 = lik_w(lik_x2(f0, cq[p])), w1 = lik_w(lik_x2(f1, cq[p])),
-                            w2 = lik_w(lik_x2(f2, cq[p])), w3 = lik_w(lik_x2(f3, cq[p]));
+                const float w0 = lik_w<EXACT>(lik_x2(f0, cq[p])), w1 = lik_w<EXACT>(lik_x2(f1, cq[p])),
+                            w2 = lik_w<EXACT>(lik_x2(f2, cq[p])), w3 = lik_w<EXACT>(lik_x2(f3, cq[p]));
                 kadd(s[p], (w0 + w1) + (w2 + w3));
                 if (ADJ) {
                     kadd(t0[p], __fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
@@ -403,7 +409,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
             const float4 f = F[Bl.ids[q]];
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-                const float w = lik_w(lik_x2(f, cq[p]));
+                const float w = lik_w<EXACT>(lik_x2(f, cq[p]));
                 kadd(s[p], w);
                 if (ADJ) {
                     kadd(t0[p], w * f.y);
@@ -454,7 +460,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
                 const bool in = Bl.cflag[c0 + i] != 0;
                 const float4 f = F[T.cites[c0 + i]];
                 const X2 x2 = lik_x2(f, c);
-                const float w = lik_w(x2);
+                const float w = lik_w<EXACT>(x2);
                 const double W = in ? (double)w * beta : (double)w;
                 if (!ADJ) {
                     // log D_i - log Z_a = log(1 - u), u = P_i / Z_a in [0, 1)
@@ -515,8 +521,8 @@ cudaError_t init_lik_kernels(int bitmap_words, int* ball_per_sm, int* eval_per_s
     int b0 = 1, b1 = 1, v0 = 1, v1 = 1;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_lik_ball<false>, kLikThreads, smem);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_lik_ball<true>, kLikThreads, smem);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v0, k_lik_eval<false, 2>, kLikThreads, 0);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v1, k_lik_eval<true, 2>, kLikThreads, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v0, k_lik_eval<false, 2, false>, kLikThreads, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v1, k_lik_eval<true, 2, false>, kLikThreads, 0);
     *ball_per_sm = b0 < b1 ? (b0 < 1 ? 1 : b0) : (b1 < 1 ? 1 : b1);
     eval_per_sm[0] = v0 < 1 ? 1 : v0;
     eval_per_sm[1] = v1 < 1 ? 1 : v1;
@@ -537,11 +543,18 @@ void launch_lik_ball(const LikTrace& T, const LikBalls& Bl, int emit, int64_t a0
 void launch_lik_global(const LikTrace& T, const LikBatch& P, int adjoint, cudaStream_t s) {
     const dim3 gg((unsigned)T.chunks, (unsigned)T.epochs);
     const unsigned gs = (unsigned)((T.epochs * P.B + 127) / 128);
+    const bool x = P.exact_exp2 != 0;
     if (adjoint) {
-        k_lik_global<true><<<gg, kLikThreads, 0, s>>>(T, P);
+        if (x)
+            k_lik_global<true, true><<<gg, kLikThreads, 0, s>>>(T, P);
+        else
+            k_lik_global<true, false><<<gg, kLikThreads, 0, s>>>(T, P);
         k_lik_global_sum<true><<<gs, 128, 0, s>>>(T, P);
     } else {
-        k_lik_global<false><<<gg, kLikThreads, 0, s>>>(T, P);
+        if (x)
+            k_lik_global<false, true><<<gg, kLikThreads, 0, s>>>(T, P);
+        else
+            k_lik_global<false, false><<<gg, kLikThreads, 0, s>>>(T, P);
         k_lik_global_sum<false><<<gs, 128, 0, s>>>(T, P);
     }
 }
@@ -554,17 +567,21 @@ void launch_lik_eval(const LikTrace& T, const LikBatch& P, const LikBalls& Bl, i
     const int64_t warps = (a1 - a0) * groups;
     int64_t g = (warps + kLikThreads / 32 - 1) / (kLikThreads / 32);
     if (g > grid) g = grid;
+    const unsigned gu = (unsigned)g;
+    const bool x = P.exact_exp2 != 0;
+#define PG_LIK_EVAL(ADJ, NP, EX) k_lik_eval<ADJ, NP, EX><<<gu, kLikThreads, 0, s>>>(T, P, Bl, a0, a1)
     if (adjoint) {
         if (two)
-            k_lik_eval<true, 2><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+            x ? PG_LIK_EVAL(true, 2, true) : PG_LIK_EVAL(true, 2, false);
         else
-            k_lik_eval<true, 1><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+            x ? PG_LIK_EVAL(true, 1, true) : PG_LIK_EVAL(true, 1, false);
     } else {
         if (two)
-            k_lik_eval<false, 2><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+            x ? PG_LIK_EVAL(false, 2, true) : PG_LIK_EVAL(false, 2, false);
         else
-            k_lik_eval<false, 1><<<(unsigned)g, kLikThreads, 0, s>>>(T, P, Bl, a0, a1);
+            x ? PG_LIK_EVAL(false, 1, true) : PG_LIK_EVAL(false, 1, false);
     }
+#undef PG_LIK_EVAL
 }
 
 void launch_lik_sum(const LikTrace& T, const LikBatch& P, int adjoint, cudaStream_t s) {

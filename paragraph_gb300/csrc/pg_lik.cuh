@@ -45,7 +45,7 @@ struct LikBatch {
     int32_t B;           // points in this launch (<= kLikMaxB)
     int32_t BE;          // global pass: B rounded up to a power of two (threads per node slice)
     int32_t BW;          // agent pass: points per warp, min(32, B) rounded up to a power of two
-    int32_t pad;
+    int32_t exact_exp2;  // 1: weights from exp2_exact (fp32, ~2 ulp), 0: the special-function unit
     const double* theta; // [B][4] alpha, tau, gamma, beta
     const double* pp;    // [B][8] alpha, 1/tau, gamma, beta, log beta, 1/beta, 1/tau^2, tau
     double* zglob;       // [epochs][B]      sum_{j<n_e} w_j          (forward writes)

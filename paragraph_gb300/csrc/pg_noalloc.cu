@@ -35,7 +35,7 @@ static __device__ __align__(256) int64_t g_noalloc_scratch[kNoAllocWords];
 std::atomic<int64_t*> g_scratch_addr[64] = {};
 
 __device__ __forceinline__ int64_t walk(uint64_t seed, uint32_t ep, int64_t i, int64_t c, int64_t n,
-                                        double inv_l, int64_t src, int32_t* out_src,
+                                        const ErSkip& K, int64_t src, int32_t* out_src,
                                         int32_t* out_dst, int64_t base) {
     const int64_t lo = c * kErChunk;
     const int64_t hi = lo + kErChunk < n ? lo + kErChunk : n;
@@ -44,9 +44,9 @@ __device__ __forceinline__ int64_t walk(uint64_t seed, uint32_t ep, int64_t i, i
     x.x[0] = x.x[1] = x.x[2] = x.x[3] = 0;
     for (uint32_t d = 0;; ++d) {
         if ((d & 1u) == 0) x = draw(seed, kStreamEr, (uint32_t)c, ep, (uint32_t)i, d >> 1);
-        const double u = (d & 1u) ? u01d(x.x[2], x.x[3]) : u01d(x.x[0], x.x[1]);
-        const double sk = floor(log_pg(u) * inv_l);
-        if (sk >= (double)(hi - pos - 1)) break;
+        const double rem = (double)(hi - pos - 1);
+        const double sk = (d & 1u) ? er_skip(K, x.x[2], x.x[3], (float)rem) : er_skip(K, x.x[0], x.x[1], (float)rem);
+        if (sk >= rem) break;
         pos = pos + 1 + (int64_t)sk;
         if (out_dst) {
             out_src[base + cnt] = (int32_t)src;
@@ -58,20 +58,20 @@ __device__ __forceinline__ int64_t walk(uint64_t seed, uint32_t ep, int64_t i, i
 }
 
 __global__ void __launch_bounds__(256) k_na_count(uint64_t seed, uint32_t ep, int64_t n,
-                                                  int64_t tasks, int64_t chunks, double inv_l,
+                                                  int64_t tasks, int64_t chunks, ErSkip K,
                                                   int64_t* cnt) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tasks;
          t += (int64_t)gridDim.x * blockDim.x)
-        cnt[t] = walk(seed, ep, t / chunks, t % chunks, n, inv_l, 0, nullptr, nullptr, 0);
+        cnt[t] = walk(seed, ep, t / chunks, t % chunks, n, K, 0, nullptr, nullptr, 0);
 }
 
 __global__ void __launch_bounds__(256) k_na_emit(uint64_t seed, uint32_t ep, int64_t n,
-                                                 int64_t tasks, int64_t chunks, double inv_l,
+                                                 int64_t tasks, int64_t chunks, ErSkip K,
                                                  const int64_t* off, int32_t* src, int32_t* dst) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tasks;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = t / chunks;
-        walk(seed, ep, i, t % chunks, n, inv_l, n + i, src, dst, off[t]);
+        walk(seed, ep, i, t % chunks, n, K, n + i, src, dst, off[t]);
     }
 }
 
@@ -108,8 +108,7 @@ extern "C" pg_status pg_er_generate_noalloc(uint64_t seed, int64_t epoch, int64_
     if (delta > kNoAllocMaxTasks / chunks) return PG_ERR_CAPACITY;  // scratch holds one count per task
     const int64_t tasks = delta * chunks;
     if (!(p > 0.0)) return PG_OK;  // no edges
-    const double pe = p < 1.0 ? p : 1.0;
-    const double inv_l = 1.0 / log_pg(1.0 - pe);
+    const ErSkip K = er_skip_constants(p);
     int64_t* scratch = nullptr;
     pg_status s = scratch_for_current_device(&scratch);
     if (s != PG_OK) return s;
@@ -120,7 +119,7 @@ extern "C" pg_status pg_er_generate_noalloc(uint64_t seed, int64_t epoch, int64_
     const uint32_t ep = (uint32_t)epoch;
     int64_t g = (tasks + 255) / 256;
     if (g > 4096) g = 4096;
-    k_na_count<<<(unsigned)g, 256, 0, st>>>(seed, ep, n_existing, tasks, chunks, inv_l, cnt);
+    k_na_count<<<(unsigned)g, 256, 0, st>>>(seed, ep, n_existing, tasks, chunks, K, cnt);
     launch_scan_i64(cnt, off, tasks, blocksum, st);
     if (cudaGetLastError() != cudaSuccess) return PG_ERR_CUDA;  // *num_edges stays 0
     int64_t total = 0;
@@ -129,7 +128,7 @@ extern "C" pg_status pg_er_generate_noalloc(uint64_t seed, int64_t epoch, int64_
         return PG_ERR_CUDA;
     *num_edges = total;
     if (total > capacity) return PG_ERR_CAPACITY;  // nothing written
-    k_na_emit<<<(unsigned)g, 256, 0, st>>>(seed, ep, n_existing, tasks, chunks, inv_l, off, d_src, d_dst);
+    k_na_emit<<<(unsigned)g, 256, 0, st>>>(seed, ep, n_existing, tasks, chunks, K, off, d_src, d_dst);
     if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) return PG_ERR_CUDA;
     return PG_OK;
 }

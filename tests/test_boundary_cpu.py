@@ -106,3 +106,15 @@ def test_create_rejects_bad_config_without_gpu_calls(built):
     cfg = pg._Config(0, 0, 1, 0, 0, 0, 0)  # zero replicas
     assert lib.pg_create(C.byref(ctx), C.byref(cfg)) == pg.PG_ERR_ARG
     assert lib.pg_status_string(pg.PG_ERR_CAPACITY) == b"capacity exceeded"
+
+
+def test_fp32_log_error_bound_holds_exhaustively(built):
+    """The ER skip decides floor(log(u) / log(1 - p)) from an fp32 estimate whose error bound
+    assumes the library's fp32 log is within 2 ulp on [2^-60, 1]; every float there is checked
+    (the oracle's copy, which is bit-identical to the library's, computes the maximum)."""
+    assert O._load().og_logf_max_ulp(2.0 ** -60, 1.0) < 2.0
+    rng = np.random.default_rng(4)
+    xs = np.concatenate([rng.random(2000), 2.0 ** -rng.uniform(0, 60, 2000)]).astype(np.float32)
+    lib = pg.load_library()
+    for x in xs.tolist():
+        assert np.float32(lib.pg_logf_host(x)).view(np.uint32) == np.float32(O.logf(x)).view(np.uint32)

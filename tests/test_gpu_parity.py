@@ -215,7 +215,7 @@ def test_checkpoint_restore_regrows_identically(gpu):
             np.testing.assert_array_equal(c1, c2)
         st = eng.stats()
         assert st["run_epochs"] == 8 and st["run_new_edges"] == e2
-        assert st["run_kernel_launches"] == 8 * (20 + 6)  # thinning adds the guide table and hub index
+        assert st["run_kernel_launches"] == 8 * (20 + 7)  # thinning adds the guide table, hub index and events
 
 
 def test_tuning_never_changes_results(gpu):
@@ -366,3 +366,28 @@ def test_format_attributes_text(gpu, peak_integer):
             ids[v], "seed" if v < n0 else "agent", pub[v], draws[v, 0], draws[v, 1], draws[v, 2],
             ints[v, 0], peak, ints[v, 1], draws[v, 3], ind[v], outd[v], ints[v, 2], ints[v, 3], gen))
     assert txt == "".join(lines)
+
+
+@pytest.mark.parametrize("p", [1e-5, 1e-3])
+def test_run_er_epochs_matches_single_epochs(gpu, p):
+    """Ten ER epochs enqueued without host synchronisation grow the same graph as ten single-epoch
+    calls, and the last epoch's edges are reported the same way."""
+    s = W.er_seed(100_000)
+    res = []
+    for multi in (False, True):
+        with GrowthEngine(seed=42) as eng:
+            eng.load_graph(s.pub, s.fitness, s.src, s.dst)
+            if multi:
+                ne = eng.run_er_epochs(10, 10_000, p)
+            else:
+                ne = sum(eng.er_epoch(10_000, p) for _ in range(10))
+            res.append((ne, eng.counts(), [eng.csr(w) for w in (0, 1)], eng.last_epoch_edges(),
+                        eng.degrees()[0]))
+    (n1, c1, csr1, last1, ind1), (n2, c2, csr2, last2, ind2) = res
+    assert n1 == n2 and c1 == c2
+    for (o1, k1), (o2, k2) in zip(csr1, csr2):
+        np.testing.assert_array_equal(o1, o2)
+        np.testing.assert_array_equal(k1, k2)
+    for x, y in zip(last1, last2):
+        np.testing.assert_array_equal(x, y)
+    np.testing.assert_array_equal(ind1, ind2)
