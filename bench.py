@@ -733,7 +733,7 @@ def run_small_configs(args) -> None:
                 # room for the 10 epochs' expected edges (1.45e10 p in all) with an 8-sigma margin
                 n0, m0 = eng.counts()
                 mu = [10_000 * (n0 + 10_000 * t) * p for t in range(10)]
-                eng.reserve(n0 + 100_000, int(m0 + sum(x + 8 * x ** 0.5 + 1024 for x in mu)))
+                eng.reserve(n0 + 100_000, m0 + sum(int(np.ceil(x + 8 * x ** 0.5 + 1024)) + 1 for x in mu))
                 eng.sync()
                 eng.timer_start()
                 e = eng.run_er_epochs(10, 10_000, p)  # the 10 epochs without host synchronisation

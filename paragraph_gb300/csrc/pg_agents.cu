@@ -728,7 +728,7 @@ __global__ void __launch_bounds__(256) k_events(Arena A, int64_t agents) {
             else
                 lo = mid + 1;
         }
-        const bool glob = u01d(x.x[2], x.x[3]) <= rp.p_global;
+        const bool glob = u01d_at_most(x.x[2], x.x[3], rp.glob_thr);
         A.ev_pre[idx] = (int32_t)((uint32_t)lo | (glob ? 0x80000000u : 0u));
     }
 }

@@ -281,6 +281,7 @@ Replica to_device_rep(const HostRep& h) {
     r.fixed_new = h.prm.fixed_new_nodes;
     r.anchors = h.prm.num_anchors;
     r.p_global = 1.0 / h.prm.beta;
+    r.glob_thr = global_threshold(r.p_global);
     r.heavy_thr = 0x7fffffff;
     if (h.rc) {
         const bool fixed = h.rcp.pa_weight >= 0.0 && h.rcp.rec_weight >= 0.0 && h.rcp.fit_weight >= 0.0;
@@ -1155,6 +1156,7 @@ pg_status pg_set_params(pg_ctx* c, int32_t replica, const pg_pa_params* p) {
     dr.tau = fresh.tau;
     dr.beta_m1 = fresh.beta_m1;
     dr.p_global = fresh.p_global;
+    dr.glob_thr = fresh.glob_thr;
     dr.growth_rate = fresh.growth_rate;
     dr.fixed_new = fresh.fixed_new;
     dr.anchors = fresh.anchors;

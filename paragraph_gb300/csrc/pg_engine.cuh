@@ -73,6 +73,7 @@ struct Replica {
     float alpha, gamma, tau, pad0;
     double beta_m1;
     double p_global;  // 1 / beta: probability that a thinning event is a global (always kept) one
+    uint64_t glob_thr;  // u01d(lo, hi) <= p_global  <=>  (hi:lo >> 11) + 1 <= glob_thr (global_threshold)
     double growth_rate;
     int64_t fixed_new;
     int32_t anchors;
@@ -198,6 +199,11 @@ struct Arena {
     uint32_t first_wait_polls; // polls of the first bounded wait on each staged copy (pg_set_wait_limit)
     uint32_t pad_wp;
 };
+
+// u01d(lo, hi) <= p compared in integers: u = (v + 1) 2^-53 with v the draw's top 53 bits, and
+// p 2^53 is exact in double, so u <= p  <=>  v + 1 <= floor(p 2^53) (every draw for p >= 1).
+PG_HD uint64_t global_threshold(double p) { return p >= 1.0 ? (1ull << 53) : (p > 0.0 ? (uint64_t)(p * 0x1p53) : 0ull); }
+PG_HD bool u01d_at_most(uint32_t lo, uint32_t hi, uint64_t thr) { return (u64of(lo, hi) >> 11) + 1u <= thr; }
 
 // Guide table of a replica's CDF (total Wq over n nodes): bucket g covers [g 2^gs, (g+1) 2^gs),
 // with gs the smallest shift that leaves at most n buckets, so there are more than n/2 of them and

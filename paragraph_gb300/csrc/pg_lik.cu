@@ -56,6 +56,20 @@ __device__ __forceinline__ void kadd(Kahan& k, float v) {
 }
 __device__ __forceinline__ double kval(const Kahan& k) { return (double)k.s - (double)k.c; }
 
+// A ball-sum accumulator: compensated fp32 (the default) or, in the exact mode, FP64.
+template <bool EXACT>
+struct BallAcc {
+    Kahan k;
+    double d = 0.0;
+    __device__ __forceinline__ void add(float v) {
+        if (EXACT)
+            d += (double)v;
+        else
+            kadd(k, v);
+    }
+    __device__ __forceinline__ double value() const { return EXACT ? d : kval(k); }
+};
+
 // First position of x's backward row whose source is >= ne (rows ascending).
 __device__ __forceinline__ int64_t bwd_cut(const LikTrace& T, int64_t x, int64_t ne) {
     int64_t lo = T.bo[x], hi = T.bo[x + 1];
@@ -388,7 +402,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
         const int e = T.agent_epoch[a];
         const float4* F = T.feat + (int64_t)e * T.n;
         const int64_t j0 = Bl.boff[a] - Bl.base, j1 = Bl.boff[a + 1] - Bl.base;
-        Kahan s[NP], t0[NP], t1[NP], t2[NP];
+        BallAcc<EXACT> s[NP], t0[NP], t1[NP], t2[NP];
         int64_t q = j0 + sl;
         for (; q + 3 * SL < j1; q += 4 * SL) {
             const int32_t i0 = Bl.ids[q], i1 = Bl.ids[q + SL], i2 = Bl.ids[q + 2 * SL], i3 = Bl.ids[q + 3 * SL];
@@ -397,11 +411,26 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
             for (int p = 0; p < NP; ++p) {
                 const float w0 = lik_w<EXACT>(lik_x2(f0, cq[p])), w1 = lik_w<EXACT>(lik_x2(f1, cq[p])),
                             w2 = lik_w<EXACT>(lik_x2(f2, cq[p])), w3 = lik_w<EXACT>(lik_x2(f3, cq[p]));
-                kadd(s[p], (w0 + w1) + (w2 + w3));
-                if (ADJ) {
-                    kadd(t0[p], __fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
-                    kadd(t1[p], __fmaf_rn(w3, f3.z, __fmaf_rn(w2, f2.z, __fmaf_rn(w1, f1.z, w0 * f0.z))));
-                    kadd(t2[p], __fmaf_rn(w3, f3.x, __fmaf_rn(w2, f2.x, __fmaf_rn(w1, f1.x, w0 * f0.x))));
+                if (EXACT) {
+                    // every element in FP64
+                    const float wv[4] = {w0, w1, w2, w3};
+                    const float4 fv[4] = {f0, f1, f2, f3};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        s[p].add(wv[u]);
+                        if (ADJ) {
+                            t0[p].d = __fma_rn((double)wv[u], (double)fv[u].y, t0[p].d);
+                            t1[p].d = __fma_rn((double)wv[u], (double)fv[u].z, t1[p].d);
+                            t2[p].d = __fma_rn((double)wv[u], (double)fv[u].x, t2[p].d);
+                        }
+                    }
+                } else {
+                    s[p].add((w0 + w1) + (w2 + w3));
+                    if (ADJ) {
+                        t0[p].add(__fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
+                        t1[p].add(__fmaf_rn(w3, f3.z, __fmaf_rn(w2, f2.z, __fmaf_rn(w1, f1.z, w0 * f0.z))));
+                        t2[p].add(__fmaf_rn(w3, f3.x, __fmaf_rn(w2, f2.x, __fmaf_rn(w1, f1.x, w0 * f0.x))));
+                    }
                 }
             }
         }
@@ -410,17 +439,26 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
                 const float w = lik_w<EXACT>(lik_x2(f, cq[p]));
-                kadd(s[p], w);
-                if (ADJ) {
-                    kadd(t0[p], w * f.y);
-                    kadd(t1[p], w * f.z);
-                    kadd(t2[p], w * f.x);
+                if (EXACT) {
+                    s[p].add(w);
+                    if (ADJ) {
+                        t0[p].d = __fma_rn((double)w, (double)f.y, t0[p].d);
+                        t1[p].d = __fma_rn((double)w, (double)f.z, t1[p].d);
+                        t2[p].d = __fma_rn((double)w, (double)f.x, t2[p].d);
+                    }
+                } else {
+                    s[p].add(w);
+                    if (ADJ) {
+                        t0[p].add(w * f.y);
+                        t1[p].add(w * f.z);
+                        t2[p].add(w * f.x);
+                    }
                 }
             }
         }
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-            double S = kval(s[p]), T0 = kval(t0[p]), T1 = kval(t1[p]), T2 = kval(t2[p]);
+            double S = s[p].value(), T0 = t0[p].value(), T1 = t1[p].value(), T2 = t2[p].value();
             for (int o = BW; o < 32; o <<= 1) {
                 S += __shfl_xor_sync(0xffffffffu, S, o);
                 if (ADJ) {

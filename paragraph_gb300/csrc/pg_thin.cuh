@@ -452,7 +452,6 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
 
     // ---------------------------------------------------------------- events
     const uint64_t Wq = rp.wq_total;
-    const double pg = rp.p_global;
     int nch = 0;
     long long events = 0, tests = 0, scanned = 0;
     const int maxev = 64 * k + 256;
@@ -482,7 +481,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                     lo = mid + 1;
             }
             j = (int)lo;
-            glob = u01d(x.x[2], x.x[3]) <= pg;
+            glob = u01d_at_most(x.x[2], x.x[3], rp.glob_thr);
         }
         // The 32 events of the batch are decided together, with the result of taking them one
         // at a time in event order: an event whose node was already chosen is skipped, a boost
@@ -745,7 +744,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                 lo = L > 0 ? pL1 + 1 : lo;
             }
             const int j = (int)lo;
-            const bool glob = u01d(x.x[2], x.x[3]) <= pg;
+            const bool glob = u01d_at_most(x.x[2], x.x[3], rp.glob_thr);
             ++events;
             if (!glob) {
                 ++tests;
