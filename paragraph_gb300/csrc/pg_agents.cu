@@ -697,49 +697,6 @@ void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s) {
     k_edges_check<<<1, 256, 0, s>>>(A, agents);
 }
 
-// The first kPreEvents thinning events of every agent, drawn ahead of the agent kernel: one thread
-// per (agent, event) makes the same Philox draw, guide-table read and CDF search the agent's warp
-// would make, so the warp starts each of its first two batches from one coalesced load instead of
-// a chain of dependent ones.  Stored as node | (global event) << 31.
-__global__ void __launch_bounds__(256) k_events(Arena A, int64_t agents) {
-    if (A.st->error) return;
-    const int64_t total = agents * kPreEvents;
-    const uint32_t ep = (uint32_t)A.st->epoch;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t a = idx / kPreEvents;
-        const uint32_t ev = (uint32_t)(idx % kPreEvents);
-        const int r = replica_of_agent(A.rep, A.R, a);
-        const Replica& rp = A.rep[r];
-        const int64_t n = rp.n;
-        const uint64_t Wq = rp.wq_total;
-        const int gs = guide_shift(Wq, n);
-        const int64_t used = Wq ? (int64_t)((Wq - 1) >> gs) + 1 : 0;
-        const int32_t* guide = A.guide + rp.nbase;
-        const uint64_t* cdf = A.cdf + rp.nbase;
-        const u32x4 x = draw(A.seed, kStreamGlobal, (uint32_t)(r + A.rep_base), ep, (uint32_t)(a - rp.abase), ev);
-        const uint64_t y = mulhi64(u64of(x.x[0], x.x[1]), Wq);
-        const int64_t g = (int64_t)(y >> gs);
-        int64_t lo = guide[g], hi = g + 1 < used ? guide[g + 1] : n - 1;
-        while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if (cdf[mid] > y)
-                hi = mid;
-            else
-                lo = mid + 1;
-        }
-        const bool glob = u01d_at_most(x.x[2], x.x[3], rp.glob_thr);
-        A.ev_pre[idx] = (int32_t)((uint32_t)lo | (glob ? 0x80000000u : 0u));
-    }
-}
-
-void launch_events(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) {
-    if (agents <= 0 || !A.ev_pre) return;
-    int64_t g = (agents * kPreEvents + 255) / 256;
-    if (g > (int64_t)num_sms * 16) g = (int64_t)num_sms * 16;
-    k_events<<<(unsigned)g, 256, 0, s>>>(A, agents);
-}
-
 // Occupancy of the persistent agent kernels; called once per process before any capture.
 cudaError_t init_agent_kernels() {
     if (g_blocks[0][0]) return cudaSuccess;

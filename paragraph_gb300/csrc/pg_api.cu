@@ -97,8 +97,7 @@ struct pg_ctx {
     // device buffers
     DBuf<Replica> rep;
     DBuf<EpochState> st;
-    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, heavy_list, heavy_mark, e_dst, e_rank, arrivals, hlist, anchors, tile_row,
-        ev_pre;
+    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, heavy_list, heavy_mark, e_dst, e_rank, arrivals, hlist, anchors, tile_row;
     DBuf<int16_t> hslot;
     DBuf<uint64_t> hub2;
     DBuf<uint32_t> hub_need;
@@ -220,7 +219,6 @@ Arena make_arena(pg_ctx* c) {
     A.big_list = c->big_list.p;
     A.heavy_list = c->heavy_list.p;
     A.heavy_mark = c->heavy_mark.p;
-    A.ev_pre = c->ev_pre.p;
     A.tile_row = c->tile_row.p;
     A.len_tmp = c->len_tmp.p;
     A.tilesum = c->tilesum.p;
@@ -420,8 +418,6 @@ pg_status alloc_epoch_buffers(pg_ctx* c, int64_t agent_cap, int64_t edge_cap, in
         PG_CUDA(c, dalloc(c->big_list, agent_cap));
         PG_CUDA(c, dalloc(c->heavy_list, agent_cap));
         PG_CUDA(c, dalloc(c->heavy_mark, agent_cap));
-        if (c->cfg.sampler == PG_SAMPLER_THINNING && c->cfg.weight_model == PG_WEIGHTS_BASELINE)
-            PG_CUDA(c, dalloc(c->ev_pre, (int64_t)kPreEvents * agent_cap));
         PG_CUDA(c, dalloc(c->eoff, agent_cap + 1));
         if (c->cfg.record_trace) PG_CUDA(c, dalloc(c->anchors, 4 * agent_cap));
         if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) PG_CUDA(c, dalloc(c->rc_agent, 6 * agent_cap));
@@ -804,8 +800,6 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
     if (c->cfg.sampler == PG_SAMPLER_THINNING) {
         launch_hub_pairs(A, s);  // for the hubs the setup found among the anchors
         PG_STAGE("hub pairs");
-        launch_events(A, agents, c->num_sms, s);
-        PG_STAGE("events");
     }
     if (events) record_event(ev[2], s);
     launch_agents(A, agents, c->num_sms, s);
@@ -1000,7 +994,7 @@ void pg_destroy(pg_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     destroy_graph_exec(c);
-    DBuf<int32_t>* i32[] = {&c->tile_rep, &c->tile_row, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list, &c->heavy_list, &c->heavy_mark, &c->ev_pre,
+    DBuf<int32_t>* i32[] = {&c->tile_rep, &c->tile_row, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list, &c->heavy_list, &c->heavy_mark,
                             &c->e_dst, &c->e_rank, &c->arrivals, &c->anchors, &c->fwd_col, &c->bwd_col[0],
                             &c->bwd_col[1]};
     for (auto* b : i32) dfree(*b);

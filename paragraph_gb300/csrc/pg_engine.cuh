@@ -39,7 +39,6 @@ constexpr int kRcAgeMax = 1024;      // recency probabilities by age 0..1023 (re
 constexpr int kRcFitMax = 1000;      // peak fitness values 1..1000 (refcompat)
 constexpr uint32_t kRcFillBlocks = 1u << 20;  // Philox blocks a uniform fill may use
 constexpr uint32_t kWaitPolls = 1u << 22;     // polls of a bounded wait on an asynchronous copy
-constexpr int kPreEvents = 64;       // thinning events per agent drawn ahead by k_events (two batches)
 
 enum Sampler : int32_t {
     kSamplerThinning = 0,   // Poisson thinning against ball membership (default)
@@ -156,7 +155,6 @@ struct Arena {
     int32_t* big_list;         // [agent cap]
     int32_t* heavy_list;       // [agent cap] agents with a hub or a large frontier (k <= kKSmall)
     int32_t* heavy_mark;       // [agent cap] 1 when the agent is on heavy_list
-    int32_t* ev_pre;           // [agent cap][kPreEvents] first thinning events: node | global << 31, or null
     int32_t* zbig;             // [agent-kernel warp slots][1 << kGBits] rows of anchors too large for H
     int32_t* rc_big_id;        // [kRcBigCap][kKMax] sorted top of each listed refcompat agent's 2-hop stream
     long long* rc_big_meta;    // [kRcBigCap][3] entries, rows, elements of that stream
@@ -346,9 +344,9 @@ __device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64
 // Kernels one PA epoch enqueues: epoch begin (1), weights + CDF (4), agent setup + offset scan +
 // check (5), agent kernels (2), backward append incl. epoch end (8).
 constexpr int kPaEpochKernels = 20;
-// Extra kernels of the thinning sampler: the CDF's guide table (1), the hub index (histogram,
-// pick, collect, mask, hub pairs) and the events drawn ahead (1).
-constexpr int kThinKernels = 7;
+// Extra kernels of the thinning sampler: the CDF's guide table (1) and the hub index (histogram,
+// pick, collect, mask, hub pairs).
+constexpr int kThinKernels = 6;
 void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s);
 void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cudaStream_t s);
 void launch_weights(const Arena& A, cudaStream_t s);
@@ -358,8 +356,6 @@ void launch_guide(const Arena& A, cudaStream_t s);
 void launch_tile_scan(const Arena& A, int mode, cudaStream_t s);
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s);
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
-// the first kPreEvents thinning events of every agent (after the guide table and the agent setup)
-void launch_events(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
 // side/fork/join (optional): the old-entry copy runs on `side` beside the new-entry placement and sorts
 void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s, cudaStream_t side = nullptr,
                        cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);

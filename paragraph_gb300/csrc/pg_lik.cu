@@ -56,20 +56,6 @@ __device__ __forceinline__ void kadd(Kahan& k, float v) {
 }
 __device__ __forceinline__ double kval(const Kahan& k) { return (double)k.s - (double)k.c; }
 
-// A ball-sum accumulator: compensated fp32 (the default) or, in the exact mode, FP64.
-template <bool EXACT>
-struct BallAcc {
-    Kahan k;
-    double d = 0.0;
-    __device__ __forceinline__ void add(float v) {
-        if (EXACT)
-            d += (double)v;
-        else
-            kadd(k, v);
-    }
-    __device__ __forceinline__ double value() const { return EXACT ? d : kval(k); }
-};
-
 // First position of x's backward row whose source is >= ne (rows ascending).
 __device__ __forceinline__ int64_t bwd_cut(const LikTrace& T, int64_t x, int64_t ne) {
     int64_t lo = T.bo[x], hi = T.bo[x + 1];
@@ -111,10 +97,31 @@ __device__ __forceinline__ float ex2_sfu(float x) {
 struct X2 {
     float h, l;
 };
+// a + b = s + err exactly (Knuth's two-sum; the build neither contracts nor reassociates)
+__device__ __forceinline__ float two_sum(float a, float b, float& err) {
+    const float s = a + b;
+    const float bb = s - a;
+    err = (a - (s - bb)) + (b - bb);
+    return s;
+}
+template <bool EXACT>
 __device__ __forceinline__ X2 lik_x2(const float4 f, const LikC& c) {
     X2 x;
-    x.h = __fmaf_rn(c.al2, f.y, __fmaf_rn(-c.it2, f.z, c.ga2 * f.x));
-    x.l = __fmaf_rn(c.al2, f.w, __fmaf_rn(c.al2l, f.y, __fmaf_rn(c.ga2l, f.x, -(c.it2l * f.z))));
+    if (EXACT) {
+        // every product and sum keeps its rounding error (FMA residuals, two-sums): h + l is the
+        // exponent to about 2^-40, so no node's weight carries a fixed error of its own
+        const float p3 = c.ga2 * f.x, e3 = __fmaf_rn(c.ga2, f.x, -p3);
+        const float p1 = c.al2 * f.y, e1 = __fmaf_rn(c.al2, f.y, -p1);
+        const float p2 = -c.it2 * f.z, e2 = __fmaf_rn(-c.it2, f.z, -p2);
+        float r1, r2;
+        const float s1 = two_sum(p3, p1, r1);
+        x.h = two_sum(s1, p2, r2);
+        x.l = ((e1 + e2) + (e3 + (r1 + r2))) +
+              __fmaf_rn(c.al2, f.w, __fmaf_rn(c.al2l, f.y, __fmaf_rn(c.ga2l, f.x, -(c.it2l * f.z))));
+    } else {
+        x.h = __fmaf_rn(c.al2, f.y, __fmaf_rn(-c.it2, f.z, c.ga2 * f.x));
+        x.l = __fmaf_rn(c.al2, f.w, __fmaf_rn(c.al2l, f.y, __fmaf_rn(c.ga2l, f.x, -(c.it2l * f.z))));
+    }
     return x;
 }
 // 2^(h + l) for |l| < 2^-18 in fp32 arithmetic: n = rint(h), f = h - n (exact), t = (f + l) ln 2
@@ -208,7 +215,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_global(LikTrace T, LikBatch
         const float4* F = T.feat + (int64_t)e * T.n;
         for (int64_t j = lo + sub; j < hi; j += nsub) {
             const float4 f = F[j];
-            const double w = (double)lik_w<EXACT>(lik_x2(f, c));
+            const double w = (double)lik_w<EXACT>(lik_x2<EXACT>(f, c));
             s += w;
             if (ADJ) {
                 t0 = __fma_rn(w, (double)f.y, t0);
@@ -402,35 +409,20 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
         const int e = T.agent_epoch[a];
         const float4* F = T.feat + (int64_t)e * T.n;
         const int64_t j0 = Bl.boff[a] - Bl.base, j1 = Bl.boff[a + 1] - Bl.base;
-        BallAcc<EXACT> s[NP], t0[NP], t1[NP], t2[NP];
+        Kahan s[NP], t0[NP], t1[NP], t2[NP];
         int64_t q = j0 + sl;
         for (; q + 3 * SL < j1; q += 4 * SL) {
             const int32_t i0 = Bl.ids[q], i1 = Bl.ids[q + SL], i2 = Bl.ids[q + 2 * SL], i3 = Bl.ids[q + 3 * SL];
             const float4 f0 = F[i0], f1 = F[i1], f2 = F[i2], f3 = F[i3];
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-                const float w0 = lik_w<EXACT>(lik_x2(f0, cq[p])), w1 = lik_w<EXACT>(lik_x2(f1, cq[p])),
-                            w2 = lik_w<EXACT>(lik_x2(f2, cq[p])), w3 = lik_w<EXACT>(lik_x2(f3, cq[p]));
-                if (EXACT) {
-                    // every element in FP64
-                    const float wv[4] = {w0, w1, w2, w3};
-                    const float4 fv[4] = {f0, f1, f2, f3};
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        s[p].add(wv[u]);
-                        if (ADJ) {
-                            t0[p].d = __fma_rn((double)wv[u], (double)fv[u].y, t0[p].d);
-                            t1[p].d = __fma_rn((double)wv[u], (double)fv[u].z, t1[p].d);
-                            t2[p].d = __fma_rn((double)wv[u], (double)fv[u].x, t2[p].d);
-                        }
-                    }
-                } else {
-                    s[p].add((w0 + w1) + (w2 + w3));
-                    if (ADJ) {
-                        t0[p].add(__fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
-                        t1[p].add(__fmaf_rn(w3, f3.z, __fmaf_rn(w2, f2.z, __fmaf_rn(w1, f1.z, w0 * f0.z))));
-                        t2[p].add(__fmaf_rn(w3, f3.x, __fmaf_rn(w2, f2.x, __fmaf_rn(w1, f1.x, w0 * f0.x))));
-                    }
+                const float w0 = lik_w<EXACT>(lik_x2<EXACT>(f0, cq[p])), w1 = lik_w<EXACT>(lik_x2<EXACT>(f1, cq[p])),
+                            w2 = lik_w<EXACT>(lik_x2<EXACT>(f2, cq[p])), w3 = lik_w<EXACT>(lik_x2<EXACT>(f3, cq[p]));
+                kadd(s[p], (w0 + w1) + (w2 + w3));
+                if (ADJ) {
+                    kadd(t0[p], __fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
+                    kadd(t1[p], __fmaf_rn(w3, f3.z, __fmaf_rn(w2, f2.z, __fmaf_rn(w1, f1.z, w0 * f0.z))));
+                    kadd(t2[p], __fmaf_rn(w3, f3.x, __fmaf_rn(w2, f2.x, __fmaf_rn(w1, f1.x, w0 * f0.x))));
                 }
             }
         }
@@ -438,27 +430,18 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
             const float4 f = F[Bl.ids[q]];
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-                const float w = lik_w<EXACT>(lik_x2(f, cq[p]));
-                if (EXACT) {
-                    s[p].add(w);
-                    if (ADJ) {
-                        t0[p].d = __fma_rn((double)w, (double)f.y, t0[p].d);
-                        t1[p].d = __fma_rn((double)w, (double)f.z, t1[p].d);
-                        t2[p].d = __fma_rn((double)w, (double)f.x, t2[p].d);
-                    }
-                } else {
-                    s[p].add(w);
-                    if (ADJ) {
-                        t0[p].add(w * f.y);
-                        t1[p].add(w * f.z);
-                        t2[p].add(w * f.x);
-                    }
+                const float w = lik_w<EXACT>(lik_x2<EXACT>(f, cq[p]));
+                kadd(s[p], w);
+                if (ADJ) {
+                    kadd(t0[p], w * f.y);
+                    kadd(t1[p], w * f.z);
+                    kadd(t2[p], w * f.x);
                 }
             }
         }
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-            double S = s[p].value(), T0 = t0[p].value(), T1 = t1[p].value(), T2 = t2[p].value();
+            double S = kval(s[p]), T0 = kval(t0[p]), T1 = kval(t1[p]), T2 = kval(t2[p]);
             for (int o = BW; o < 32; o <<= 1) {
                 S += __shfl_xor_sync(0xffffffffu, S, o);
                 if (ADJ) {
@@ -497,7 +480,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
             for (int i = 0; i < k; ++i) {
                 const bool in = Bl.cflag[c0 + i] != 0;
                 const float4 f = F[T.cites[c0 + i]];
-                const X2 x2 = lik_x2(f, c);
+                const X2 x2 = lik_x2<EXACT>(f, c);
                 const float w = lik_w<EXACT>(x2);
                 const double W = in ? (double)w * beta : (double)w;
                 if (!ADJ) {

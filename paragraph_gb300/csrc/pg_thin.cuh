@@ -461,28 +461,19 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     const int64_t used = Wq ? (int64_t)((Wq - 1) >> gs) + 1 : 0;
     const unsigned below = (1u << lane) - 1u;
     for (int i0 = 0; i0 < maxev && nch < k; i0 += 32) {
-        int j;
-        bool glob;
-        if (A.ev_pre && i0 < kPreEvents) {
-            // drawn ahead by k_events (the same draw and search)
-            const uint32_t e = (uint32_t)A.ev_pre[a * kPreEvents + i0 + lane];
-            j = (int)(e & 0x7FFFFFFFu);
-            glob = (e >> 31) != 0u;
-        } else {
-            const u32x4 x = draw(A.seed, kStreamGlobal, rep, ep, unit, (uint32_t)(i0 + lane));
-            const uint64_t y = mulhi64(u64of(x.x[0], x.x[1]), Wq);
-            const int64_t g = (int64_t)(y >> gs);
-            int64_t lo = guide[g], hi = g + 1 < used ? guide[g + 1] : n - 1;
-            while (lo < hi) {
-                const int64_t mid = (lo + hi) >> 1;
-                if (cdf[mid] > y)
-                    hi = mid;
-                else
-                    lo = mid + 1;
-            }
-            j = (int)lo;
-            glob = u01d_at_most(x.x[2], x.x[3], rp.glob_thr);
+        const u32x4 x = draw(A.seed, kStreamGlobal, rep, ep, unit, (uint32_t)(i0 + lane));
+        const uint64_t y = mulhi64(u64of(x.x[0], x.x[1]), Wq);
+        const int64_t g = (int64_t)(y >> gs);
+        int64_t lo = guide[g], hi = g + 1 < used ? guide[g + 1] : n - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (cdf[mid] > y)
+                hi = mid;
+            else
+                lo = mid + 1;
         }
+        const int j = (int)lo;
+        const bool glob = u01d_at_most(x.x[2], x.x[3], rp.glob_thr);
         // The 32 events of the batch are decided together, with the result of taking them one
         // at a time in event order: an event whose node was already chosen is skipped, a boost
         // event is tested for membership, and the first k acceptances end the draw.
