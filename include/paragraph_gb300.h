@@ -300,6 +300,10 @@ typedef struct {
                                   balls per chunk, so every likelihood pass rebuilds them chunk by
                                   chunk; 0: as many as fit in a quarter of free device memory (one
                                   chunk = built once and reused by every pass) */
+    int32_t epoch_kernel;      /* 1: each epoch of the thinning sampler with the baseline weights is
+                                  ONE persistent cooperative kernel over all replicas (every stage
+                                  a phase, grid barriers between them); 0: the sequence of stage
+                                  kernels.  Ignored (0) where the device cannot launch it. */
 } pg_tuning;
 pg_status pg_set_tuning(pg_ctx* ctx, const pg_tuning* tuning);
 pg_status pg_get_tuning(const pg_ctx* ctx, pg_tuning* tuning);

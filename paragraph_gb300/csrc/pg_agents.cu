@@ -23,6 +23,9 @@
 
 #include "pg_engine.cuh"
 #include "pg_rc.cuh"
+#include "pg_scan.cuh"
+#include "pg_weights.cuh"
+#include "pg_csr.cuh"
 
 namespace pg {
 
@@ -370,9 +373,9 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
 #include "pg_rc_agent.cuh"
 
 // ---------------------------------------------------------------- setup: out-degree + new nodes
-__global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
+__device__ __forceinline__ void d_agent_setup(const Arena& A, int64_t agents, int vb) {
     if (A.st->error) return;
-    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t a = (int64_t)vb * blockDim.x + threadIdx.x;
     if (a >= agents) return;
     const int r = replica_of_agent(A.rep, A.R, a);
     const Replica& rp = A.rep[r];
@@ -478,8 +481,10 @@ __global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) {
     }
 }
 
+__global__ void __launch_bounds__(256) k_agent_setup(Arena A, int64_t agents) { d_agent_setup(A, agents, blockIdx.x); }
+
 // After the edge-offset scan: totals and capacity checks.
-__global__ void k_edges_check(Arena A, int64_t agents) {
+__device__ __forceinline__ void d_edges_check(const Arena& A, int64_t agents) {
     if (A.st->error) return;
     const int64_t E = A.eoff[agents];
     if (threadIdx.x == 0) {
@@ -493,6 +498,8 @@ __global__ void k_edges_check(Arena A, int64_t agents) {
     }
 }
 
+__global__ void k_edges_check(Arena A, int64_t agents) { d_edges_check(A, agents); }
+
 // entries per stage buffer of the thinning sampler (two buffers per warp)
 template <int KCAP, bool HSMALL>
 struct ThinStage {
@@ -505,25 +512,28 @@ constexpr size_t thin_smem_bytes() {
     return sizeof(ThinSmem<KCAP, HCAP, ThinStage<KCAP, HSMALL>::value>) * kAgentWarps;
 }
 
+// The agent loop of one warp.  Thinning variants: the warp's shared memory is dsm + warp * stride
+// (the calling kernel's dynamic shared memory; stride >= sizeof of this variant's ThinSmem); the
+// enumeration variants use static shared memory.
 template <int KCAP, bool BIG, bool THIN, bool HSMALL = false>
-__global__ void __launch_bounds__(kAgentWarps * 32, 4) k_agents(Arena A, int64_t agents) {
+__device__ __forceinline__ void d_agents(const Arena& A, int64_t agents, unsigned char* dsm, size_t stride) {
     // frontier hash capacity: 2048 slots for the common small-k kernel (1024 in the HSMALL variant,
     // which fits more CTAs per SM), 1024 for the k <= 256 one so that four warps stay within 48 KiB
     // of static shared memory
     constexpr int HCAP = (KCAP <= kKSmall && !HSMALL) ? 2 * kZCap : kZCap;
     constexpr int STAGE = ThinStage<KCAP, HSMALL>::value;
     using Smem = typename std::conditional<THIN, ThinSmem<KCAP, HCAP, STAGE>, AgentSmem<KCAP>>::type;
-    Smem* smem;
+    Smem* sp;
     if constexpr (THIN) {
-        // the thinning variants hold two stage buffers per warp and go past 48 KiB: dynamic
-        extern __shared__ __align__(16) unsigned char agent_dsm[];
-        smem = reinterpret_cast<Smem*>(agent_dsm);
+        sp = reinterpret_cast<Smem*>(dsm + (threadIdx.x >> 5) * stride);
     } else {
         __shared__ Smem agent_ssm[kAgentWarps];
-        smem = agent_ssm;
+        sp = &agent_ssm[threadIdx.x >> 5];
+        (void)dsm;
+        (void)stride;
     }
     if (A.st->error) return;
-    Smem& S = smem[threadIdx.x >> 5];
+    Smem& S = *sp;
     const int lane = lane_id();
     // the small thinning kernel walks the heavy list, then every agent not on it
     constexpr bool kHeavyFirst = THIN && !BIG;
@@ -564,6 +574,24 @@ __global__ void __launch_bounds__(kAgentWarps * 32, 4) k_agents(Arena A, int64_t
         } else
             process_agent<KCAP>(A, a, k, S);
     }
+    if constexpr (THIN) {
+        // every copy this warp issued has been waited for: the barriers' memory can be reused
+        __syncwarp();
+        if (lane == 0) {
+            mbar_inval(&S.bar[0]);
+            mbar_inval(&S.bar[1]);
+        }
+        __syncwarp();
+    }
+}
+
+template <int KCAP, bool BIG, bool THIN, bool HSMALL = false>
+__global__ void __launch_bounds__(kAgentWarps * 32, 4) k_agents(Arena A, int64_t agents) {
+    // the thinning variants hold two stage buffers per warp and go past 48 KiB: dynamic
+    extern __shared__ __align__(16) unsigned char agent_dsm[];
+    constexpr int HCAP = (KCAP <= kKSmall && !HSMALL) ? 2 * kZCap : kZCap;
+    constexpr size_t stride = sizeof(ThinSmem<KCAP, HCAP, ThinStage<KCAP, HSMALL>::value>);
+    d_agents<KCAP, BIG, THIN, HSMALL>(A, agents, agent_dsm, stride);
 }
 
 __global__ void __launch_bounds__(kAgentWarps * 32) k_agents_rc(Arena A, int64_t agents) {
@@ -593,7 +621,7 @@ __global__ void __launch_bounds__(kRcBigWarps * 32) k_rc_big(Arena A) {
     __shared__ int s_nb[kRcBigWarps];
     __shared__ long long s_cnt[2];
     __shared__ long long s_item;
-    if (A.st->error) return;
+    if (cta_error(A)) return;
     const int warp = threadIdx.x >> 5, lane = lane_id();
     RcSmem& S = sm[warp];
     const long long listed = (long long)A.st->rc_big_count;
@@ -724,7 +752,9 @@ int64_t agent_warp_slots(int num_sms) {
     int mb = g_blocks_hsmall;
     for (auto& row : g_blocks)
         for (int b : row) mb = b > mb ? b : mb;
-    return (int64_t)num_sms * mb * kAgentWarps;
+    const int64_t sep = (int64_t)num_sms * mb * kAgentWarps;
+    const int64_t per = (int64_t)(2 * num_sms) * 8;  // the epoch kernel: 2 CTAs of 8 warps per SM at most
+    return sep > per ? sep : per;
 }
 
 int agent_occupancy(int thin, int small_hash) {
@@ -752,6 +782,180 @@ void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) 
         k_agents<kKSmall, false, false><<<(unsigned)grid, th, 0, s>>>(A, agents);
         k_agents<kKMax, true, false><<<gbig, th, 0, s>>>(A, agents);
     }
+}
+
+
+// ---------------------------------------------------------------- one persistent kernel per epoch
+// The thinning epoch of every replica as ONE cooperative launch (one CTA pair per SM, all CTAs
+// resident), instead of the two dozen launches above.  The phases are the same device bodies the
+// separate kernels run -- tiles and blocks walked by the CTAs in turn, single-CTA steps on one CTA,
+// grid-stride loops as they are -- so every result is bit-identical to the launch sequence.  A grid
+// barrier separates dependent phases; independent stages share a phase (the hub index beside the
+// weights and the CDF, the old-entry copy beside the placement of the new ones).  Each barrier
+// wait is bounded: on expiry the CTA sets the timeout bit of the error word and goes on, and every
+// later phase sees the bit and skips its work, so the launch always ends.
+constexpr int kEpochThreads = 256;
+constexpr int kEpochWarps = kEpochThreads / 32;
+constexpr uint32_t kGridWaitPolls = 1u << 24;  // with a 64 ns back-off: about a second at least
+
+__device__ __forceinline__ void grid_sync(const Arena& A) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* gen = &A.st->gbar_gen;
+        const unsigned int g = *gen;
+        __threadfence();
+        if (atomicAdd(&A.st->gbar_count, 1u) == gridDim.x - 1) {
+            atomicExch(&A.st->gbar_count, 0u);
+            __threadfence();
+            atomicAdd(&A.st->gbar_gen, 1u);
+        } else {
+            for (uint32_t i = 0; *gen == g; ++i) {
+                if (i >= kGridWaitPolls) {
+                    atomicOr(&A.st->error, kErrTimeout);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// per-warp shared memory of the agent phase: the larger of the two thinning variants
+constexpr size_t kEpochWarpSmem =
+    sizeof(ThinSmem<kKSmall, 2 * kZCap, ThinStage<kKSmall, false>::value>) >
+            sizeof(ThinSmem<kKMax, kZCap, ThinStage<kKMax, false>::value>)
+        ? sizeof(ThinSmem<kKSmall, 2 * kZCap, ThinStage<kKSmall, false>::value>)
+        : sizeof(ThinSmem<kKMax, kZCap, ThinStage<kKMax, false>::value>);
+constexpr size_t kEpochSmem = kEpochWarps * kEpochWarpSmem > (size_t)kCopySmemBytes
+                                  ? kEpochWarps * kEpochWarpSmem
+                                  : (size_t)kCopySmemBytes;
+
+__global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epoch, int64_t agents, int G) {
+    extern __shared__ __align__(16) unsigned char ep_dsm[];
+    const int T = A.ntiles;
+    const int hub_items = A.R * kHeavyMax * G;
+    // epoch start: new-node counts, agent and copy-tile offsets
+    if (blockIdx.x == 0) d_epoch_begin(A, epoch, -1);
+    grid_sync(A);
+    // hub histogram and weights
+    for (int t = blockIdx.x; t < T; t += gridDim.x) {
+        d_hub_hist(A, t);
+        d_weights(A, t);
+        __syncthreads();
+    }
+    grid_sync(A);
+    // hub threshold; tile-local CDF scans
+    if (blockIdx.x == 0) d_hub_pick(A);
+    for (int t = blockIdx.x; t < T; t += gridDim.x) {
+        d_cdf_tiles(A, t);
+        __syncthreads();
+    }
+    grid_sync(A);
+    // hubs; tile offsets of the CDF (on the last CTA, so CTA 0 is not the only one with extra work)
+    for (int t = blockIdx.x; t < T; t += gridDim.x) d_hub_collect(A, t);
+    if (blockIdx.x == gridDim.x - 1) d_tile_scan(A, 0);
+    grid_sync(A);
+    // hub masks; CDF offsets and guide marks
+    for (int i = blockIdx.x; i < hub_items; i += gridDim.x) d_hub_mask(A, G, i);
+    for (int t = blockIdx.x; t < T; t += gridDim.x) {
+        d_cdf_add(A, t);
+        __syncthreads();
+    }
+    grid_sync(A);
+    // guide table; per-agent out-degrees, new nodes, heavy lists
+    for (int t = blockIdx.x; t < T; t += gridDim.x) {
+        d_guide_fill(A, t);
+        __syncthreads();
+    }
+    const int setup_blocks = (int)((agents + 255) / 256);
+    for (int b = blockIdx.x; b < setup_blocks; b += gridDim.x) d_agent_setup(A, agents, b);
+    grid_sync(A);
+    // edge offsets: exclusive scan of the out-degrees (reduce, block sums, apply)
+    const int nb = (int)((agents + kScanBlock - 1) / kScanBlock);
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        d_scan_reduce<int32_t>(A.kk, agents, A.blocksum, b);
+        __syncthreads();
+    }
+    grid_sync(A);
+    if (blockIdx.x == 0) d_scan_blocksums(A.blocksum, nb);
+    grid_sync(A);
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        d_scan_apply<int32_t>(A.kk, agents, A.blocksum, nb, A.eoff, b);
+        __syncthreads();
+    }
+    grid_sync(A);
+    // capacity check; hub-pair rows for the hub anchors
+    if (blockIdx.x == 0) d_edges_check(A, agents);
+    for (int i = blockIdx.x; i < hub_items; i += gridDim.x) {
+        d_hub_pairs(A, G, i);
+        __syncthreads();
+    }
+    grid_sync(A);
+    // the agents: k <= 256 queue, then the k <= 64 queue (heavy list first)
+    d_agents<kKMax, true, true>(A, agents, ep_dsm, kEpochWarpSmem);
+    d_agents<kKSmall, false, true>(A, agents, ep_dsm, kEpochWarpSmem);
+    grid_sync(A);
+    // backward append: new lengths, their scan, new offsets
+    for (int t = blockIdx.x; t < T; t += gridDim.x) {
+        d_bwd_len(A, t);
+        __syncthreads();
+    }
+    grid_sync(A);
+    if (blockIdx.x == 0) d_tile_scan(A, 1);
+    grid_sync(A);
+    for (int t = blockIdx.x; t < T; t += gridDim.x) {
+        d_bwd_off(A, t);
+        __syncthreads();
+    }
+    grid_sync(A);
+    // old entries to their new positions, new entries placed (disjoint positions)
+    {
+        int64_t* s_oc = reinterpret_cast<int64_t*>(ep_dsm);
+        int64_t* s_sh = s_oc + (kCopyRows + 1);
+        int16_t* s_blk = reinterpret_cast<int16_t*>(s_sh + kCopyRows);
+        d_bwd_copy(A, s_oc, s_sh, s_blk);
+    }
+    d_bwd_place(A, agents);
+    grid_sync(A);
+    // appended segments sorted
+    d_sort_small(A);
+    __syncthreads();
+    d_sort_large(A, reinterpret_cast<uint32_t*>(ep_dsm), (int64_t)(kEpochSmem / 4));
+    grid_sync(A);
+    if (blockIdx.x == 0) d_epoch_end(A, agents);
+}
+
+static int g_epoch_ctas = 0;
+
+cudaError_t init_epoch_kernel(int num_sms) {
+    if (g_epoch_ctas) return cudaSuccess;
+    int dev = 0, coop = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_epoch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEpochSmem);
+    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_epoch, kEpochThreads, kEpochSmem);
+    if (e != cudaSuccess || !coop || per_sm < 1) {
+        cudaGetLastError();
+        g_epoch_ctas = -1;  // not available on this device: the launch sequence is used
+        return cudaSuccess;
+    }
+    g_epoch_ctas = num_sms * (per_sm < 2 ? per_sm : 2);
+    return cudaSuccess;
+}
+
+int epoch_kernel_ctas() { return g_epoch_ctas > 0 ? g_epoch_ctas : 0; }
+
+cudaError_t launch_epoch_kernel(const Arena& A, int64_t epoch, int64_t agents, cudaStream_t s) {
+    if (g_epoch_ctas <= 0) return cudaErrorNotSupported;
+    Arena a = A;
+    int G = A.R >= 64 ? 1 : 64 / A.R;
+    void* args[] = {&a, &epoch, &agents, &G};
+    return cudaLaunchCooperativeKernel((const void*)k_epoch, dim3((unsigned)g_epoch_ctas), dim3(kEpochThreads), args,
+                                       kEpochSmem, s);
 }
 
 }  // namespace pg

@@ -755,6 +755,27 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
         return fail(c, PG_ERR_CUDA, std::string("launch error in ") + name + ": " + cudaGetErrorString(e)); \
     }
     if (events) record_event(ev[0], s);
+    if (c->cfg.weight_model == PG_WEIGHTS_BASELINE && c->cfg.sampler == PG_SAMPLER_THINNING && c->tune.epoch_kernel &&
+        epoch_kernel_ctas() > 0) {
+        // the whole epoch as one persistent cooperative kernel (its stages are phases; the stage
+        // events all fall on its two ends, so the epoch counts as agent time)
+        PG_CUDA(c, cudaMemsetAsync(&c->st.p->gbar_count, 0, sizeof(unsigned int), s));
+        if (events) {
+            record_event(ev[1], s);
+            record_event(ev[2], s);
+        }
+        e = launch_epoch_kernel(A, epoch, agents, s);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(c, PG_ERR_CUDA, std::string("launch error in the epoch kernel: ") + cudaGetErrorString(e));
+        }
+        if (events) {
+            record_event(ev[3], s);
+            record_event(ev[4], s);
+        }
+        c->launches += 1;
+        return PG_OK;
+    }
     launch_epoch_begin(A, epoch, 1, s);
     PG_STAGE("epoch begin");
     if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
@@ -970,6 +991,8 @@ pg_status pg_create(pg_ctx** out, const pg_config* cfg) {
     if (e == cudaSuccess) e = dalloc(c->st, 1);
     if (e == cudaSuccess) e = init_agent_kernels();
     if (e == cudaSuccess) e = init_csr_kernels();
+    if (e == cudaSuccess && cfg->weight_model == PG_WEIGHTS_BASELINE && cfg->sampler == PG_SAMPLER_THINNING)
+        e = init_epoch_kernel(c->num_sms);
     if (e == cudaSuccess && cfg->weight_model == PG_WEIGHTS_REFCOMPAT) e = init_rc_kernels();
     // one global hash per resident agent warp, for anchors whose rows overflow the shared one
     if (e == cudaSuccess && cfg->weight_model == PG_WEIGHTS_BASELINE && cfg->sampler == PG_SAMPLER_THINNING)
@@ -1705,7 +1728,8 @@ pg_status pg_restore(pg_ctx* c) {
 pg_status pg_set_tuning(pg_ctx* c, const pg_tuning* t) {
     if (!c) return PG_ERR_ARG;
     if (!t || t->agent_ctas_per_sm < 0 || t->agent_ctas_per_sm > 32 || t->copy_ctas_per_sm < 0 ||
-        t->copy_ctas_per_sm > 64 || (t->small_hash != 0 && t->small_hash != 1) || t->lik_chunk_agents < 0)
+        t->copy_ctas_per_sm > 64 || (t->small_hash != 0 && t->small_hash != 1) || t->lik_chunk_agents < 0 ||
+        (t->epoch_kernel != 0 && t->epoch_kernel != 1))
         return fail(c, PG_ERR_ARG, "tuning out of range");
     if (std::memcmp(&c->tune, t, sizeof(pg_tuning)) != 0) {
         c->tune = *t;
@@ -1738,8 +1762,9 @@ pg_status pg_get_tuning(const pg_ctx* c, pg_tuning* t) {
 }
 
 // Coordinate search: agent-kernel shape (frontier hash capacity x CTAs per SM) first, then the
-// backward-copy grid.  Each candidate runs the same epochs from the same saved state twice, as a
-// captured graph (the second run, a replay, is the one timed).
+// backward-copy grid, then the whole epoch as one persistent kernel.  Each candidate runs the same
+// epochs from the same saved state twice, as a captured graph (the second run, a replay, is the
+// one timed).
 pg_status pg_autotune(pg_ctx* c, int32_t num_epochs, pg_tuning* best, double* best_ms) {
     if (!c) return PG_ERR_ARG;
     if (num_epochs < 1) return fail(c, PG_ERR_ARG, "num_epochs must be >= 1");
@@ -1804,6 +1829,12 @@ pg_status pg_autotune(pg_ctx* c, int32_t num_epochs, pg_tuning* best, double* be
         pg_tuning t = agent_best;
         t.copy_ctas_per_sm = copies[i];
         if (t.copy_ctas_per_sm == (agent_best.copy_ctas_per_sm ? agent_best.copy_ctas_per_sm : 8)) continue;
+        s = trial(t);
+    }
+    // the whole epoch as one persistent kernel (its own launch shape: two CTAs of 8 warps per SM)
+    if (s == PG_OK && thin && c->cfg.weight_model == PG_WEIGHTS_BASELINE && epoch_kernel_ctas() > 0) {
+        pg_tuning t = start;
+        t.epoch_kernel = 1;
         s = trial(t);
     }
     // leave the graph as it was and the best tuning in force

@@ -1,4 +1,5 @@
-// pg_csr.cu -- device CSR append of one epoch's edges (stage e).
+// pg_csr.cuh -- device CSR append of one epoch's edges (stage e; part of the epoch translation unit,
+// pg_agents.cu).
 //
 // Replaces the reference's per-epoch host work: sorting new_edges_vec, inserting into
 // std::map<int, std::set<int>> adjacency (src/kernel.cu:1766-1810), updating in-degrees
@@ -16,16 +17,17 @@
 //          256 new entries are sorted by a register bitonic network in one warp, longer ones by a
 //          shared-memory bitmap over the epoch's new-id range.  Rows end up ascending, like the
 //          reference's std::set rows, and bit-identical run to run.
+#pragma once
 #include "pg_engine.cuh"
 
 namespace pg {
 
 constexpr unsigned kFullMask = 0xffffffffu;
 
-__global__ void __launch_bounds__(kTileThreads) k_bwd_len(Arena A) {
+__device__ __forceinline__ void d_bwd_len(const Arena& A, int vb) {
     __shared__ uint64_t sw[33];
-    if (A.st->error) return;
-    const int t = blockIdx.x;
+    if (cta_error(A)) return;
+    const int t = vb;
     const int r = A.tile_rep[t];
     const Replica& rp = A.rep[r];
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
@@ -74,10 +76,12 @@ __global__ void __launch_bounds__(kTileThreads) k_bwd_len(Arena A) {
     if (threadIdx.x == 0) A.tilesum[t] = tot;
 }
 
-__global__ void __launch_bounds__(kTileThreads) k_bwd_off(Arena A) {
+__global__ void __launch_bounds__(kTileThreads) k_bwd_len(Arena A) { d_bwd_len(A, blockIdx.x); }
+
+__device__ __forceinline__ void d_bwd_off(const Arena& A, int vb) {
     __shared__ int64_t sw[33];
-    if (A.st->error) return;
-    const int t = blockIdx.x;
+    if (cta_error(A)) return;
+    const int t = vb;
     const int r = A.tile_rep[t];
     const Replica& rp = A.rep[r];
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
@@ -102,6 +106,8 @@ __global__ void __launch_bounds__(kTileThreads) k_bwd_off(Arena A) {
     }
 }
 
+__global__ void __launch_bounds__(kTileThreads) k_bwd_off(Arena A) { d_bwd_off(A, blockIdx.x); }
+
 // Largest v in [lo, hi] with off[v] <= p (the row holding position p).
 __device__ __forceinline__ int64_t row_of(const int64_t* off, int64_t lo, int64_t hi, int64_t p) {
     while (lo < hi) {
@@ -124,11 +130,11 @@ __device__ __forceinline__ int64_t row_of(const int64_t* off, int64_t lo, int64_
 constexpr int kCopyRows = 2048;
 constexpr int kCopyBlocks = kCopyTile / 32;
 
-__global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
-    __shared__ int64_t s_oc[kCopyRows + 1];  // old offsets of the tile's rows, and the next one
-    __shared__ int64_t s_sh[kCopyRows];      // new minus old offset of the tile's rows
-    __shared__ int16_t s_blk[kCopyBlocks];   // row (tile-relative) holding each block's first position
-    if (A.st->error) return;
+// s_oc [kCopyRows + 1]: old offsets of the tile's rows, and the next one; s_sh [kCopyRows]: new minus
+// old offset of the tile's rows; s_blk [kCopyBlocks]: row (tile-relative) holding each block's first
+// position -- shared memory of the calling CTA (kCopySmemBytes in all)
+__device__ __forceinline__ void d_bwd_copy(const Arena& A, int64_t* s_oc, int64_t* s_sh, int16_t* s_blk) {
+    if (cta_error(A)) return;
     const int64_t total = (int64_t)A.st->copy_tiles;
     unsigned long long moved = 0;
     for (int64_t t = blockIdx.x; t < total; t += gridDim.x) {
@@ -208,8 +214,17 @@ __global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
     if (threadIdx.x == 0 && moved) atomicAdd(&A.st->bwd_moved, moved);
 }
 
+constexpr int kCopySmemBytes = 8 * (kCopyRows + 1) + 8 * kCopyRows + 2 * kCopyBlocks;
+
+__global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
+    __shared__ int64_t s_oc[kCopyRows + 1];
+    __shared__ int64_t s_sh[kCopyRows];
+    __shared__ int16_t s_blk[kCopyBlocks];
+    d_bwd_copy(A, s_oc, s_sh, s_blk);
+}
+
 // One warp per agent: place its edges at new_off[dst] + old_len(dst) + rank.
-__global__ void __launch_bounds__(256) k_bwd_place(Arena A, int64_t agents) {
+__device__ __forceinline__ void d_bwd_place(const Arena& A, int64_t agents) {
     if (A.st->error) return;
     const int lane = lane_id();
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -229,6 +244,8 @@ __global__ void __launch_bounds__(256) k_bwd_place(Arena A, int64_t agents) {
         }
     }
 }
+
+__global__ void __launch_bounds__(256) k_bwd_place(Arena A, int64_t agents) { d_bwd_place(A, agents); }
 
 __device__ __forceinline__ void seg_bounds(const Arena& A, int64_t slot, const Replica*& rpp,
                                            int64_t& start, int64_t& len) {
@@ -256,7 +273,7 @@ __device__ __forceinline__ void warp_sort_segment(int32_t* seg, int64_t len, int
 
 // Rows with 2..kSortMid appended entries: one warp, bitonic network in registers (1, 2, 4 or 8
 // entries per lane).
-__global__ void __launch_bounds__(256) k_sort_small(Arena A) {
+__device__ __forceinline__ void d_sort_small(const Arena& A) {
     if (A.st->error) return;
     const int lane = lane_id();
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -279,14 +296,16 @@ __global__ void __launch_bounds__(256) k_sort_small(Arena A) {
     }
 }
 
-// Rows with more than kSortMid appended entries: one CTA, shared bitmap over [n, n + delta).
-__global__ void __launch_bounds__(1024) k_sort_large(Arena A) {
-    extern __shared__ uint32_t bm[];
+__global__ void __launch_bounds__(256) k_sort_small(Arena A) { d_sort_small(A); }
+
+// Rows with more than kSortMid appended entries: one CTA, shared bitmap bm of bm_words words over
+// [n, n + delta), in chunks when the range is longer.
+__device__ __forceinline__ void d_sort_large(const Arena& A, uint32_t* bm, int64_t bm_words) {
     __shared__ int64_t sw[33];
     __shared__ int64_t outpos;
-    if (A.st->error) return;
+    if (cta_error(A)) return;
     const int64_t cnt = (int64_t)A.st->sort_large_count;
-    constexpr int64_t kBits = (int64_t)kBitmapWords * 32;
+    const int64_t kBits = bm_words * 32;
     for (int64_t i = blockIdx.x; i < cnt; i += gridDim.x) {
         const int64_t slot = A.sort_large[i];
         const Replica* rp;
@@ -333,7 +352,12 @@ __global__ void __launch_bounds__(1024) k_sort_large(Arena A) {
     }
 }
 
-__global__ void k_epoch_end(Arena A, int64_t agents) {
+__global__ void __launch_bounds__(1024) k_sort_large(Arena A) {
+    extern __shared__ uint32_t bm[];
+    d_sort_large(A, bm, kBitmapWords);
+}
+
+__device__ __forceinline__ void d_epoch_end(const Arena& A, int64_t agents) {
     EpochState* st = A.st;
     if (st->error) return;
     for (int r = threadIdx.x; r < A.R; r += blockDim.x) {
@@ -354,6 +378,8 @@ __global__ void k_epoch_end(Arena A, int64_t agents) {
         st->cum_adj_scanned += st->adj_scanned;
     }
 }
+
+__global__ void k_epoch_end(Arena A, int64_t agents) { d_epoch_end(A, agents); }
 
 // The large-segment sort uses 160 KiB of dynamic shared memory; called once per process.
 cudaError_t init_csr_kernels() {

@@ -123,6 +123,10 @@ struct EpochState {
     unsigned long long cum_new_nodes;
     unsigned long long cum_epochs;
     unsigned long long cum_adj_scanned;
+    // grid barrier of the persistent epoch kernel: arrivals (back to 0 after every barrier, reset
+    // by the host before each launch) and generation
+    unsigned int gbar_count;
+    unsigned int gbar_gen;
 };
 
 // Device pointers of the arena (passed by value to kernels).
@@ -326,6 +330,11 @@ __device__ __forceinline__ double er_skip(const ErSkip& K, uint32_t lo, uint32_t
     return floor(log_pg(u) * K.inv_l);
 }
 
+// The device error word as one value for the whole CTA (a barrier and an OR of every thread's
+// read): a body that synchronises its CTA must not let some threads return on an error bit another
+// CTA set a moment later while the rest go on to a barrier.
+__device__ __forceinline__ bool cta_error(const Arena& A) { return __syncthreads_or(A.st->error != 0u) != 0; }
+
 // Replica of a global agent index: largest r with abase_r <= a.
 __device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64_t a) {
     int lo = 0, hi = R - 1;
@@ -356,6 +365,12 @@ void launch_guide(const Arena& A, cudaStream_t s);
 void launch_tile_scan(const Arena& A, int mode, cudaStream_t s);
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s);
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
+// The whole thinning PA epoch (baseline weights) as one cooperative persistent kernel: every stage
+// above as a phase, grid barriers between dependent phases.  epoch_kernel_ctas() is its grid (0
+// when the device cannot run it); launch_epoch_kernel returns the launch's error.
+cudaError_t init_epoch_kernel(int num_sms);
+int epoch_kernel_ctas();
+cudaError_t launch_epoch_kernel(const Arena& A, int64_t epoch, int64_t agents, cudaStream_t s);
 // side/fork/join (optional): the old-entry copy runs on `side` beside the new-entry placement and sorts
 void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t s, cudaStream_t side = nullptr,
                        cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);

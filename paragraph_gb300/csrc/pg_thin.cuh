@@ -56,6 +56,9 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) {
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
+__device__ __forceinline__ void mbar_inval(unsigned long long* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
@@ -356,7 +359,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             for (int i = 0; i < PG_MAX_ANCHORS_DEV; ++i)
                 if ((bigm >> i) & 1u) tb += dd[i];
             if (tb <= (3 << kGBits) / 4) {
-                G = A.zbig + (((int64_t)blockIdx.x * kAgentWarps + (threadIdx.x >> 5)) << kGBits);
+                G = A.zbig + (((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) << kGBits);
                 int4* g4 = reinterpret_cast<int4*>(G);
                 for (int q = lane; q < (1 << kGBits) / 4; q += 32) g4[q] = make_int4(-1, -1, -1, -1);
                 __syncwarp();

@@ -1,4 +1,4 @@
-// pg_weights.cu -- epoch start, per-node weights and the segmented fixed-point CDF.
+// pg_weights.cuh -- epoch start, per-node weights and the segmented fixed-point CDF.
 //
 // Restates the per-epoch score preparation of execute() (src/kernel.cu:1698-1706;
 // FillInDegreeArr/FillFitnessArr/FillRecencyArr/CalculateScores, src/abm.cu:112-208,324-338),
@@ -12,11 +12,12 @@
 //
 // HBM roofline per node: read fitness, indeg, pub (12 B), write w (4 B); read w (4 B), write cdf
 // (8 B); cdf read+write in the offset pass (16 B).
+#pragma once
 #include "pg_engine.cuh"
 
 namespace pg {
 
-__global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, int64_t delta_override) {
+__device__ __forceinline__ void d_epoch_begin(const Arena& A, int64_t epoch, int64_t delta_override) {
     __shared__ int64_t sw[33];
     __shared__ int64_t carry, ccarry;
     EpochState* st = A.st;
@@ -42,7 +43,7 @@ __global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, in
         st->adj_scanned = 0;
     }
     __syncthreads();
-    for (int base = 0; base < A.R; base += 1024) {
+    for (int base = 0; base < A.R; base += blockDim.x) {
         const int r = base + threadIdx.x;
         int64_t d = 0;
         if (r < A.R) {
@@ -83,13 +84,15 @@ __global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, in
     }
 }
 
+__global__ void __launch_bounds__(1024) k_epoch_begin(Arena A, int64_t epoch, int64_t delta_override) { d_epoch_begin(A, epoch, delta_override); }
+
 // w_j for active nodes; per-replica max (as float bits, valid for non-negative floats) and count
 // of positive weights.
-__global__ void __launch_bounds__(kTileThreads) k_weights(Arena A) {
+__device__ __forceinline__ void d_weights(const Arena& A, int vb) {
     __shared__ uint32_t s_max[kTileThreads / 32];
     __shared__ int s_cnt[kTileThreads / 32], s_act[kTileThreads / 32];
-    if (A.st->error) return;
-    const int t = blockIdx.x;
+    if (cta_error(A)) return;
+    const int t = vb;
     const int r = A.tile_rep[t];
     const Replica& rp = A.rep[r];
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
@@ -151,11 +154,13 @@ __global__ void __launch_bounds__(kTileThreads) k_weights(Arena A) {
     }
 }
 
+__global__ void __launch_bounds__(kTileThreads) k_weights(Arena A) { d_weights(A, blockIdx.x); }
+
 // q_j = quantise(w_j, s_r); tile-local inclusive scan into cdf, tile total into tilesum.
-__global__ void __launch_bounds__(kTileThreads) k_cdf_tiles(Arena A) {
+__device__ __forceinline__ void d_cdf_tiles(const Arena& A, int vb) {
     __shared__ uint64_t sw[33];
-    const int t = blockIdx.x;
-    if (A.st->error) return;
+    const int t = vb;
+    if (cta_error(A)) return;
     const int r = A.tile_rep[t];
     const Replica& rp = A.rep[r];
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
@@ -189,17 +194,19 @@ __global__ void __launch_bounds__(kTileThreads) k_cdf_tiles(Arena A) {
     if (threadIdx.x == 0) A.tilesum[t] = tot;
 }
 
+__global__ void __launch_bounds__(kTileThreads) k_cdf_tiles(Arena A) { d_cdf_tiles(A, blockIdx.x); }
+
 // One CTA: tileoff[t] = sum of tilesum over the earlier tiles of the same replica (mod 2^64, which
 // is exact because every replica's own total is below 2^63).  mode 0 stores each replica's total in
 // wq_total; mode 1 leaves replicas untouched.
-__global__ void __launch_bounds__(1024) k_tile_scan(Arena A, int mode) {
+__device__ __forceinline__ void d_tile_scan(const Arena& A, int mode) {
     __shared__ uint64_t sw[33];
     __shared__ uint64_t carry;
-    if (A.st->error) return;
+    if (cta_error(A)) return;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     const int T = A.ntiles;
-    for (int base = 0; base < T; base += 1024) {
+    for (int base = 0; base < T; base += blockDim.x) {
         const int i = base + threadIdx.x;
         const uint64_t v = i < T ? A.tilesum[i] : 0;
         uint64_t tot;
@@ -210,7 +217,7 @@ __global__ void __launch_bounds__(1024) k_tile_scan(Arena A, int mode) {
         __syncthreads();
     }
     // per-replica base and total; tilesum[] is free now and holds the bases
-    for (int r = threadIdx.x; r < A.R; r += 1024) {
+    for (int r = threadIdx.x; r < A.R; r += blockDim.x) {
         const Replica& rp = A.rep[r];
         const uint64_t b = A.tileoff[rp.tbase];
         const int e = rp.tbase + rp.ntiles;
@@ -219,14 +226,16 @@ __global__ void __launch_bounds__(1024) k_tile_scan(Arena A, int mode) {
         if (mode == 0) A.rep[r].wq_total = end - b;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < T; i += 1024) A.tileoff[i] -= A.tilesum[A.tile_rep[i]];
+    for (int i = threadIdx.x; i < T; i += blockDim.x) A.tileoff[i] -= A.tilesum[A.tile_rep[i]];
 }
+
+__global__ void __launch_bounds__(1024) k_tile_scan(Arena A, int mode) { d_tile_scan(A, mode); }
 
 // Tile offsets into the CDF, and the guide table's marks: node v whose CDF interval
 // [cdf[v-1], cdf[v]) contains bucket starts g 2^gs marks the first of them, guide[g] = v.
-__global__ void __launch_bounds__(kTileThreads) k_cdf_add(Arena A) {
-    if (A.st->error) return;
-    const int t = blockIdx.x;
+__device__ __forceinline__ void d_cdf_add(const Arena& A, int vb) {
+    if (cta_error(A)) return;
+    const int t = vb;
     const int r = A.tile_rep[t];
     const Replica& rp = A.rep[r];
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
@@ -260,14 +269,16 @@ __global__ void __launch_bounds__(kTileThreads) k_cdf_add(Arena A) {
     }
 }
 
+__global__ void __launch_bounds__(kTileThreads) k_cdf_add(Arena A) { d_cdf_add(A, blockIdx.x); }
+
 // Guide table fill: guide[g] = smallest v with cdf[v] > g 2^gs, for g < used(Wq, n).  Each tile of
 // buckets takes the running maximum of its marks, starting from the node that owns its first
 // bucket (one binary search per tile), so no tile waits for another.
-__global__ void __launch_bounds__(kTileThreads) k_guide_fill(Arena A) {
+__device__ __forceinline__ void d_guide_fill(const Arena& A, int vb) {
     __shared__ int32_t wmax[kTileThreads / 32];
     __shared__ int32_t carry;
-    if (A.st->error) return;
-    const int t = blockIdx.x;
+    if (cta_error(A)) return;
+    const int t = vb;
     const int r = A.tile_rep[t];
     const Replica& rp = A.rep[r];
     const uint64_t Wq = rp.wq_total;
@@ -319,6 +330,8 @@ __global__ void __launch_bounds__(kTileThreads) k_guide_fill(Arena A) {
     *gp = m;
 }
 
+__global__ void __launch_bounds__(kTileThreads) k_guide_fill(Arena A) { d_guide_fill(A, blockIdx.x); }
+
 // ---------------------------------------------------------------- hub index
 // Ball membership of a high-degree node j needs adj(j) intersected with the agent's 1-hop
 // frontier, which is expensive when j has millions of neighbours.  Each epoch, up to 64 nodes of
@@ -331,9 +344,9 @@ __device__ __forceinline__ int64_t degree_of(const Arena& A, const Replica& rp, 
     return (fo[v + 1] - fo[v]) + (bo[v + 1] - bo[v]);
 }
 
-__global__ void __launch_bounds__(kTileThreads) k_hub_hist(Arena A) {
+__device__ __forceinline__ void d_hub_hist(const Arena& A, int vb) {
     if (A.st->error) return;
-    const int t = blockIdx.x;
+    const int t = vb;
     const int r = A.tile_rep[t];
     Replica& rp = A.rep[r];
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
@@ -366,7 +379,9 @@ __global__ void __launch_bounds__(kTileThreads) k_hub_hist(Arena A) {
     }
 }
 
-__global__ void k_hub_pick(Arena A) {
+__global__ void __launch_bounds__(kTileThreads) k_hub_hist(Arena A) { d_hub_hist(A, blockIdx.x); }
+
+__device__ __forceinline__ void d_hub_pick(const Arena& A) {
     if (A.st->error) return;
     for (int r = threadIdx.x; r < A.R; r += blockDim.x) {
         Replica& rp = A.rep[r];
@@ -385,9 +400,11 @@ __global__ void k_hub_pick(Arena A) {
     for (int64_t i = threadIdx.x; i < (int64_t)A.R * (kHeavyMax / 32); i += blockDim.x) A.hub_need[i] = 0u;
 }
 
-__global__ void __launch_bounds__(kTileThreads) k_hub_collect(Arena A) {
+__global__ void k_hub_pick(Arena A) { d_hub_pick(A); }
+
+__device__ __forceinline__ void d_hub_collect(const Arena& A, int vb) {
     if (A.st->error) return;
-    const int t = blockIdx.x;
+    const int t = vb;
     const int r = A.tile_rep[t];
     Replica& rp = A.rep[r];
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
@@ -414,10 +431,12 @@ __global__ void __launch_bounds__(kTileThreads) k_hub_collect(Arena A) {
     }
 }
 
+__global__ void __launch_bounds__(kTileThreads) k_hub_collect(Arena A) { d_hub_collect(A, blockIdx.x); }
+
 // G CTAs per (replica, hub bit) split the hub's neighbours: mark every neighbour of the hub.
-__global__ void __launch_bounds__(256) k_hub_mask(Arena A, int G) {
+__device__ __forceinline__ void d_hub_mask(const Arena& A, int G, int vb) {
     if (A.st->error) return;
-    const int item = blockIdx.x / G, g = blockIdx.x % G;
+    const int item = vb / G, g = vb % G;
     const int r = item / kHeavyMax, b = item % kHeavyMax;
     const Replica& rp = A.rep[r];
     if (b >= rp.heavy_count || b >= kHeavyMax) return;
@@ -432,11 +451,13 @@ __global__ void __launch_bounds__(256) k_hub_mask(Arena A, int G) {
     }
 }
 
+__global__ void __launch_bounds__(256) k_hub_mask(Arena A, int G) { d_hub_mask(A, G, blockIdx.x); }
+
 // hub2[b] = OR of hmask over the hub's neighbours: the hubs sharing a neighbour with hub b.
-__global__ void __launch_bounds__(256) k_hub_pairs(Arena A, int G) {
+__device__ __forceinline__ void d_hub_pairs(const Arena& A, int G, int vb) {
     __shared__ unsigned long long acc[kMaskWords];
-    if (A.st->error) return;
-    const int item = blockIdx.x / G, g = blockIdx.x % G;
+    if (cta_error(A)) return;
+    const int item = vb / G, g = vb % G;
     const int r = item / kHeavyMax, b = item % kHeavyMax;
     const Replica& rp = A.rep[r];
     if (b >= rp.heavy_count || b >= kHeavyMax) return;
@@ -469,6 +490,8 @@ __global__ void __launch_bounds__(256) k_hub_pairs(Arena A, int G) {
         atomicOr((unsigned long long*)&A.hub2[((int64_t)r * kHeavyMax + b) * kMaskWords + threadIdx.x],
                  acc[threadIdx.x]);
 }
+
+__global__ void __launch_bounds__(256) k_hub_pairs(Arena A, int G) { d_hub_pairs(A, G, blockIdx.x); }
 
 void launch_hubs(const Arena& A, int num_sms, cudaStream_t s) {
     (void)num_sms;

@@ -5,7 +5,8 @@
   three epochs (the oracle's thinning sampler takes about a second per epoch on 16 cores).  This is
   the skewed graph whose hubs exercise the hub masks and the hub-pair rows.
 * Batched ensemble: all 256 replicas (seeds log-uniform in [5,000, 200,000], per-replica alpha,
-  tau, gamma, beta) grown 10 epochs in one context from one captured graph; the replicas with the
+  tau, gamma, beta) grown 10 epochs in one context, one persistent kernel per epoch, from one
+  captured graph; the replicas with the
   largest and smallest seeds and with the extreme values of each parameter are compared with
   oracles grown alone.
 * Calibration trace: 200,000-node seed, 10 epochs at theta* = (1, 5, 1, 4); the GPU trace equals
@@ -92,6 +93,7 @@ def test_ensemble_config_full_size(gpu):
         pick |= {int(prm[:, c].argmax()), int(prm[:, c].argmin())}
     with GrowthEngine(seed=42, replicas=len(reps)) as eng:
         eng.load_replicas(reps)
+        eng.set_tuning(epoch_kernel=1)  # one persistent kernel per epoch over all 256 replicas
         eng.run_epochs(10, use_graph=True)
         for r in sorted(pick):
             ri = reps[r]

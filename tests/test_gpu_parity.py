@@ -180,10 +180,14 @@ def test_run_epochs_graph_matches_sequential(gpu):
                 np.testing.assert_array_equal(x, y)
 
 
-def test_replicas_match_independent_oracles(gpu):
+@pytest.mark.parametrize("epoch_kernel", [0, 1])
+def test_replicas_match_independent_oracles(gpu, epoch_kernel):
+    """Replicas of one context, grown by the sequence of stage kernels or by one persistent kernel
+    per epoch, each equal the oracle grown alone."""
     reps = W.ensemble_inputs(replicas=5, lo=500, hi=4000, epochs=3, seed=11)
     with GrowthEngine(seed=77, replicas=len(reps)) as eng:
         eng.load_replicas(reps)
+        eng.set_tuning(epoch_kernel=epoch_kernel)
         ogs = []
         for r, ri in enumerate(reps):
             og = O.OracleGraph(77, r)
@@ -216,6 +220,14 @@ def test_checkpoint_restore_regrows_identically(gpu):
         st = eng.stats()
         assert st["run_epochs"] == 8 and st["run_new_edges"] == e2
         assert st["run_kernel_launches"] == 8 * (20 + 6)  # thinning adds the guide table and hub index
+        # the same run as one persistent kernel per epoch: same graph, one launch per epoch
+        eng.set_tuning(epoch_kernel=1)
+        eng.restore()
+        assert eng.run_epochs(8, use_graph=True) == e1
+        for (o1, c1), (o2, c2) in zip(a, [eng.csr(w) for w in (0, 1)]):
+            np.testing.assert_array_equal(o1, o2)
+            np.testing.assert_array_equal(c1, c2)
+        assert eng.stats()["run_kernel_launches"] == 8
 
 
 def test_tuning_never_changes_results(gpu):
@@ -224,7 +236,7 @@ def test_tuning_never_changes_results(gpu):
     reps = W.ensemble_inputs(replicas=6, lo=2000, hi=20000, epochs=4, seed=21)
     tunings = [dict(), dict(agent_ctas_per_sm=2), dict(small_hash=1),
                dict(small_hash=1, agent_ctas_per_sm=3, copy_ctas_per_sm=4),
-               dict(copy_ctas_per_sm=16)]
+               dict(copy_ctas_per_sm=16), dict(epoch_kernel=1)]
     ref = None
     with GrowthEngine(seed=31, replicas=len(reps)) as eng:
         eng.load_replicas(reps)
