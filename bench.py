@@ -375,7 +375,8 @@ def extra_lines(args, world, rank, local, dist) -> tuple[dict | None, dict | Non
          "serial_speedup": ens["serial"]["speedup_device"],
          "serial_speedup_wall": ens["serial"]["speedup_wall"],
          "citations_per_s": ens["citations_per_s"], "e2e": ens["e2e"],
-         "gpu_launches_per_step": ens["gpu_launches"] / a.steps, "steps": a.steps}
+         "gpu_launches_per_step": ens["gpu_launches"] / a.steps, "steps": a.steps,
+         "tuning": ens["config"]["tuning"], "device_ms_per_step": ens["config"]["device_ms_per_step"]}
     cb = lik.get("cpu_baseline") or {}
     l = {"value": lik["value"], "unit": lik["unit"], "workload": LIK_WORKLOAD,
          "serial_speedup": lik["serial"]["speedup"], "e2e": lik["e2e"],
@@ -437,7 +438,22 @@ def ensemble_measure(args, world, rank, local, dist, with_cpu: bool = True) -> d
     wall_max = reduce_max(dist, wall)
     evals = reduce_sum(dist, float(len(reps) * args.steps))
     edges_all = reduce_sum(dist, float(edges))
+    # the other way of running an epoch (one persistent kernel, or the stage-kernel sequence),
+    # timed the same way for comparison
+    other = dict(tuned)
+    other["epoch_kernel"] = 1 - int(tuned.get("epoch_kernel", 0))
+    eng.set_tuning(**other)
+    step()  # captures its graph
+    other_ms = 0.0
+    for _ in range(args.steps):
+        eng.restore()
+        eng.run_epochs(ENS_EPOCHS, use_graph=True)
+        other_ms += eng.stats()["ms_total"]
+    other_ms = reduce_max(dist, other_ms) / args.steps
+    eng.set_tuning(**tuned)
     eng.close()
+    per_step = {"tuned": dev_ms_max / args.steps,
+                ("epoch_kernel" if other["epoch_kernel"] else "launch_sequence"): other_ms}
 
     # serial: the plain per-replica method, one context and one 10-epoch graph run per replica
     ser_dev_ms, ser_wall = 0.0, 0.0
@@ -494,7 +510,8 @@ def ensemble_measure(args, world, rank, local, dist, with_cpu: bool = True) -> d
         "scaling": "weak", "vs_baseline": None, "dtype": "int32/u64/f32", "data": "synthetic",
         "config": {"workload": ENS_WORKLOAD, "replicas": ENS_REPLICAS, "epochs": ENS_EPOCHS,
                    "mean_out_degree": 20, "growth": 0.03, "tuning": tuned,
-                   "autotune_best_ms": tune_ms, "parallelism": "replicas only",
+                   "autotune_best_ms": tune_ms, "device_ms_per_step": per_step,
+                   "parallelism": "replicas only",
                    "l2": "inputs larger than L2 (all replicas' CSRs, several GB)"},
         "citations_per_s": edges_all / (dev_ms_max / 1000.0),
         "wall_evals_per_s": evals / wall_max,
