@@ -208,7 +208,7 @@ typedef struct {
 /* Configures replica `replica` of a PG_WEIGHTS_REFCOMPAT context after pg_load_graph (whose
  * fitness values are the seed papers' peak fitness; lag 0, duration 1000): the parameters, the
  * out-degree bag (ABM::ReadOutDegreeBag, src/abm.cu:70-89; values clipped to [0, 256], out-degrees
- * to [1, min(256, n-1)]) and the recency probabilities rec[age] for age 0..rec_len-1, rec_len <= 1024
+ * to [1, min(250, n-1)], 250 being the reference's per-paper citation capacity, src/kernel.cu:1151) and the recency probabilities rec[age] for age 0..rec_len-1, rec_len <= 1024
  * (ABM::ReadRecencyProbabilities, src/abm.cu:91-110).  pg_grow_epoch / pg_run_epochs then run the
  * reference's per-paper rule on the device. */
 pg_status pg_rc_configure(pg_ctx* ctx, int32_t replica, const pg_rc_params* params, const int32_t* bag,

@@ -1560,7 +1560,8 @@ int og_rc_epoch(og_graph* g, int threads) {
     g->rc_agents = (double*)malloc(sizeof(double) * 6 * (size_t)delta);
     int64_t rows_exp = 0, elems = 0, draws = 0;
     int failed = 0;
-    int dmax = n - 1 < OG_TABLE - 1 ? (int)(n - 1) : OG_TABLE - 1;
+    /* the reference's per-paper citation capacity (src/kernel.cu:1151) */
+    int dmax = n - 1 < 250 ? (int)(n - 1) : 250;
     if (threads > 0) omp_set_num_threads(threads);
 #pragma omp parallel reduction(+ : rows_exp, elems, draws) reduction(| : failed)
     {

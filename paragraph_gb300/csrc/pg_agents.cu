@@ -388,7 +388,7 @@ __device__ __forceinline__ void d_agent_setup(const Arena& A, int64_t agents, in
                                   u64of(x.x[0], x.x[1]));
     int64_t k = kraw < 1 ? 1 : kraw;
     if (rc) {
-        const int64_t kmax = rp.n - 1 < kKMax ? rp.n - 1 : kKMax;
+        const int64_t kmax = rp.n - 1 < kRcMaxOutDegree ? rp.n - 1 : kRcMaxOutDegree;
         if (k > kmax) k = kmax;
     } else {
         if (k > rp.n) k = rp.n;
@@ -822,11 +822,12 @@ __device__ __forceinline__ void grid_sync(const Arena& A) {
     __syncthreads();
 }
 
-// per-warp shared memory of the agent phase: the larger of the two thinning variants
+// per-warp shared memory of the agent phase: the larger of the two thinning variants it runs (the
+// k <= 64 one with the 1024-slot frontier and 1024-entry stages)
 constexpr size_t kEpochWarpSmem =
-    sizeof(ThinSmem<kKSmall, 2 * kZCap, ThinStage<kKSmall, false>::value>) >
+    sizeof(ThinSmem<kKSmall, kZCap, ThinStage<kKSmall, true>::value>) >
             sizeof(ThinSmem<kKMax, kZCap, ThinStage<kKMax, false>::value>)
-        ? sizeof(ThinSmem<kKSmall, 2 * kZCap, ThinStage<kKSmall, false>::value>)
+        ? sizeof(ThinSmem<kKSmall, kZCap, ThinStage<kKSmall, true>::value>)
         : sizeof(ThinSmem<kKMax, kZCap, ThinStage<kKMax, false>::value>);
 constexpr size_t kEpochSmem = kEpochWarps * kEpochWarpSmem > (size_t)kCopySmemBytes
                                   ? kEpochWarps * kEpochWarpSmem
@@ -895,7 +896,7 @@ __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epo
     grid_sync(A);
     // the agents: k <= 256 queue, then the k <= 64 queue (heavy list first)
     d_agents<kKMax, true, true>(A, agents, ep_dsm, kEpochWarpSmem);
-    d_agents<kKSmall, false, true>(A, agents, ep_dsm, kEpochWarpSmem);
+    d_agents<kKSmall, false, true, true>(A, agents, ep_dsm, kEpochWarpSmem);
     grid_sync(A);
     // backward append: new lengths, their scan, new offsets
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
@@ -915,7 +916,7 @@ __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epo
         int64_t* s_oc = reinterpret_cast<int64_t*>(ep_dsm);
         int64_t* s_sh = s_oc + (kCopyRows + 1);
         int16_t* s_blk = reinterpret_cast<int16_t*>(s_sh + kCopyRows);
-        d_bwd_copy(A, s_oc, s_sh, s_blk);
+        d_bwd_copy<32>(A, s_oc, s_sh, s_blk);
     }
     d_bwd_place(A, agents);
     grid_sync(A);

@@ -1913,7 +1913,7 @@ pg_status pg_rc_configure(pg_ctx* c, int32_t replica, const pg_rc_params* p, con
     h.bag_table.assign(kTableEntries, 0);
     rc_bag_table_host(bag, bag_len, h.bag_table.data());
     int32_t kmax = 1;
-    for (int64_t i = 0; i < bag_len; ++i) kmax = std::max(kmax, std::min<int32_t>(bag[i], kKMax));
+    for (int64_t i = 0; i < bag_len; ++i) kmax = std::max(kmax, std::min<int32_t>(bag[i], kRcMaxOutDegree));
     h.kmax = kmax;
     h.rtab.assign(rec, rec + rec_len);
     destroy_graph_exec(c);

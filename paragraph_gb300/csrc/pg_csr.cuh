@@ -133,6 +133,9 @@ constexpr int kCopyBlocks = kCopyTile / 32;
 // s_oc [kCopyRows + 1]: old offsets of the tile's rows, and the next one; s_sh [kCopyRows]: new minus
 // old offset of the tile's rows; s_blk [kCopyBlocks]: row (tile-relative) holding each block's first
 // position -- shared memory of the calling CTA (kCopySmemBytes in all)
+// KU positions per thread are in flight at once (their loads issued before any is placed): 8 in
+// the stage kernel, more in the epoch kernel, whose CTAs are fewer per SM.
+template <int KU>
 __device__ __forceinline__ void d_bwd_copy(const Arena& A, int64_t* s_oc, int64_t* s_sh, int16_t* s_blk) {
     if (cta_error(A)) return;
     const int64_t total = (int64_t)A.st->copy_tiles;
@@ -178,8 +181,7 @@ __device__ __forceinline__ void d_bwd_copy(const Arena& A, int64_t* s_oc, int64_
             __syncthreads();
             const int last = (int)nr - 1;
             const int nblk = (int)((p1 - p0 + 31) >> 5);
-            // eight positions per thread in flight: their loads are issued before any is placed
-            constexpr int kU = 8;
+            constexpr int kU = KU;
             for (int64_t pb = p0 + threadIdx.x; pb < p1; pb += kU * (int64_t)blockDim.x) {
                 int32_t val[kU];
 #pragma unroll
@@ -220,7 +222,7 @@ __global__ void __launch_bounds__(256) k_bwd_copy(Arena A) {
     __shared__ int64_t s_oc[kCopyRows + 1];
     __shared__ int64_t s_sh[kCopyRows];
     __shared__ int16_t s_blk[kCopyBlocks];
-    d_bwd_copy(A, s_oc, s_sh, s_blk);
+    d_bwd_copy<8>(A, s_oc, s_sh, s_blk);
 }
 
 // One warp per agent: place its edges at new_off[dst] + old_len(dst) + rank.

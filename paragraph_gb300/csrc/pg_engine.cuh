@@ -19,6 +19,7 @@ constexpr int kTile = 1024;          // slots per scan tile
 constexpr int kTileThreads = 256;    // threads per tile CTA (4 slots each)
 constexpr int kKSmall = 64;          // agents with k <= 64 use the small-capacity path
 constexpr int kKMax = 256;           // PG_MAX_OUT_DEGREE
+constexpr int kRcMaxOutDegree = 250; // refcompat: the reference's per-paper citation capacity (src/kernel.cu:1151)
 constexpr int kTableEntries = kKMax + 1;
 constexpr int kAgentWarps = 4;       // warps per CTA in the agent kernel
 constexpr int kErChunk = 65536;      // ids per ER Philox stream
