@@ -99,7 +99,7 @@ struct AgentCtx {
     const float* w;
     const int64_t* fwd_off;
     const int32_t* fwd_col;
-    const int64_t* bwd_off;
+    const BRow* bwd_row;
     const int32_t* bwd_col;
     uint64_t seed;
     uint32_t rep, ep, unit;
@@ -182,8 +182,8 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
     C.w = A.w + rp.nbase;
     C.fwd_off = A.fwd_off + rp.obase;
     C.fwd_col = A.fwd_col + rp.ebase;
-    C.bwd_off = A.bwd_off_cur + rp.obase;
-    C.bwd_col = A.bwd_col_cur + rp.ebase;
+    C.bwd_row = A.brow + rp.nbase;
+    C.bwd_col = A.bcol + rp.bbase;
     C.seed = A.seed;
     C.rep = (uint32_t)(r + A.rep_base);
     C.ep = (uint32_t)A.st->epoch;
@@ -292,7 +292,8 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
         for (int ai = 0; ai < na; ++ai) {
             const int x = __shfl_sync(kFull, anchor, ai);
             const int64_t fb = C.fwd_off[x], fe = C.fwd_off[x + 1];
-            const int64_t bb = C.bwd_off[x], be = C.bwd_off[x + 1];
+            int64_t bb, be;
+            bspan(C.bwd_row, x, bb, be);
             const int64_t lf = fe - fb;
             const int64_t deg1 = lf + (be - bb);
             rows += deg1;
@@ -312,8 +313,9 @@ __device__ void process_agent(const Arena& A, int64_t a, int k, AgentSmem<KCAP>&
                 if (valid) {
                     yf = C.fwd_off[y];
                     ylf = C.fwd_off[y + 1] - yf;
-                    yb = C.bwd_off[y];
-                    ylen = ylf + (C.bwd_off[y + 1] - yb);
+                    int64_t ye;
+                    bspan(C.bwd_row, y, yb, ye);
+                    ylen = ylf + (ye - yb);
                 }
                 const int64_t incl = warp_incl_scan<int64_t>(ylen);
                 const int64_t total = __shfl_sync(kFull, incl, 31);
@@ -421,20 +423,22 @@ __device__ __forceinline__ void d_agent_setup(const Arena& A, int64_t agents, in
         rc_agent_params(A.seed, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, rp.n, rp.rc_w, rp.rc_alpha, w3,
                         &alpha, &gen);
         const int64_t* fo = A.fwd_off + rp.obase;
-        const int64_t* bo = A.bwd_off_cur + rp.obase;
-        const int64_t gd = (fo[gen + 1] - fo[gen]) + (bo[gen + 1] - bo[gen]);
+        const BRow* br = A.brow + rp.nbase;
+        int64_t gb0, gb1;
+        bspan(br, gen, gb0, gb1);
+        const int64_t gd = (fo[gen + 1] - fo[gen]) + (gb1 - gb0);
         bool big = gd >= kRcBigGd;
         if (!big) {
             const int32_t* fc = A.fwd_col + rp.ebase;
-            const int32_t* bc = A.bwd_col_cur + rp.ebase;
+            const int32_t* bc = A.bcol + rp.bbase;
             int64_t len = 0;
             for (int64_t e = fo[gen]; e < fo[gen + 1]; ++e) {
                 const int32_t y = fc[e];
-                len += (fo[y + 1] - fo[y]) + (bo[y + 1] - bo[y]);
+                len += (fo[y + 1] - fo[y]) + blen(br, y);
             }
-            for (int64_t e = bo[gen]; e < bo[gen + 1]; ++e) {
+            for (int64_t e = gb0; e < gb1; ++e) {
                 const int32_t y = bc[e];
-                len += (fo[y + 1] - fo[y]) + (bo[y + 1] - bo[y]);
+                len += (fo[y + 1] - fo[y]) + blen(br, y);
             }
             big = len >= kRcBigStream;
         }
@@ -453,7 +457,7 @@ __device__ __forceinline__ void d_agent_setup(const Arena& A, int64_t agents, in
         // memberships against global rows); heavy agents are taken first, so none starts late
         const u32x4 xa = draw(A.seed, kStreamAnchor, (uint32_t)(r + A.rep_base), ep, (uint32_t)al, 0);
         const int64_t* fo = A.fwd_off + rp.obase;
-        const int64_t* bo = A.bwd_off_cur + rp.obase;
+        const BRow* br = A.brow + rp.nbase;
         int64_t zsize = rp.anchors;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -464,7 +468,7 @@ __device__ __forceinline__ void d_agent_setup(const Arena& A, int64_t agents, in
                 atomicOr(&A.hub_need[(int64_t)r * (kHeavyMax / 32) + (hs >> 5)], 1u << (hs & 31));
                 heavy = 1;
             } else {
-                zsize += (fo[x + 1] - fo[x]) + (bo[x + 1] - bo[x]);
+                zsize += (fo[x + 1] - fo[x]) + blen(br, x);
             }
         }
         if (zsize > kZCap / 2) heavy = 1;
@@ -639,8 +643,8 @@ __global__ void __launch_bounds__(kRcBigWarps * 32) k_rc_big(Arena A) {
         RcCtx X;
         X.fo = A.fwd_off + rp.obase;
         X.fc = A.fwd_col + rp.ebase;
-        X.bo = A.bwd_off_cur + rp.obase;
-        X.bc = A.bwd_col_cur + rp.ebase;
+        X.br = A.brow + rp.nbase;
+        X.bc = A.bcol + rp.bbase;
         X.pa = A.rc_pa + rp.nbase;
         X.rec = A.rc_rec + rp.nbase;
         X.fit = A.rc_fit + rp.nbase;
@@ -652,8 +656,9 @@ __global__ void __launch_bounds__(kRcBigWarps * 32) k_rc_big(Arena A) {
         rc_agent_params(A.seed, X.rep, X.ep, X.unit, rp.n, rp.rc_w, rp.rc_alpha, X.w3, &alpha, &X.gen);
         X.gf0 = X.fo[X.gen];
         X.glf = X.fo[X.gen + 1] - X.gf0;
-        X.gb0 = X.bo[X.gen];
-        X.gd = X.glf + (X.bo[X.gen + 1] - X.gb0);
+        int64_t gb1;
+        bspan(X.br, X.gen, X.gb0, gb1);
+        X.gd = X.glf + (gb1 - X.gb0);
         const int k = A.kk[a];
         const int kcap = k < kKMax ? k : kKMax;
         int nb = 0;
@@ -829,9 +834,7 @@ constexpr size_t kEpochWarpSmem =
             sizeof(ThinSmem<kKMax, kZCap, ThinStage<kKMax, false>::value>)
         ? sizeof(ThinSmem<kKSmall, kZCap, ThinStage<kKSmall, true>::value>)
         : sizeof(ThinSmem<kKMax, kZCap, ThinStage<kKMax, false>::value>);
-constexpr size_t kEpochSmem = kEpochWarps * kEpochWarpSmem > (size_t)kCopySmemBytes
-                                  ? kEpochWarps * kEpochWarpSmem
-                                  : (size_t)kCopySmemBytes;
+constexpr size_t kEpochSmem = kEpochWarps * kEpochWarpSmem;
 
 __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epoch, int64_t agents, int G) {
     extern __shared__ __align__(16) unsigned char ep_dsm[];
@@ -898,26 +901,11 @@ __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epo
     d_agents<kKMax, true, true>(A, agents, ep_dsm, kEpochWarpSmem);
     d_agents<kKSmall, false, true, true>(A, agents, ep_dsm, kEpochWarpSmem);
     grid_sync(A);
-    // backward append: new lengths, their scan, new offsets
-    for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        d_bwd_len(A, t);
-        __syncthreads();
-    }
+    // backward append: the cited rows' new lengths, new spans for the rows that outgrew theirs
+    d_bwd_grow(A, agents);
     grid_sync(A);
-    if (blockIdx.x == 0) d_tile_scan(A, 1);
-    grid_sync(A);
-    for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        d_bwd_off(A, t);
-        __syncthreads();
-    }
-    grid_sync(A);
-    // old entries to their new positions, new entries placed (disjoint positions)
-    {
-        int64_t* s_oc = reinterpret_cast<int64_t*>(ep_dsm);
-        int64_t* s_sh = s_oc + (kCopyRows + 1);
-        int16_t* s_blk = reinterpret_cast<int16_t*>(s_sh + kCopyRows);
-        d_bwd_copy<32>(A, s_oc, s_sh, s_blk);
-    }
+    // the moved rows' old entries copied, new entries placed (disjoint positions)
+    d_bwd_reloc(A);
     d_bwd_place(A, agents);
     grid_sync(A);
     // appended segments sorted

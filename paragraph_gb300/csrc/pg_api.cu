@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <string>
 #include <thread>
@@ -28,6 +29,7 @@ namespace {
 
 struct HostRep {
     int64_t nbase, obase, ebase, n_cap, m_cap, n, m;
+    int64_t bbase = 0, b_cap = 0, b_top = 0;  // backward region (b_top: as laid out at load)
     int32_t tbase, ntiles;
     pg_pa_params prm;
     // refcompat functor (pg_rc_configure)
@@ -69,11 +71,12 @@ struct LikState {
 struct Checkpoint {
     bool valid = false;
     int64_t epoch = 0;
-    int parity = 0;
     std::vector<HostRep> hrep;
-    DBuf<int32_t> pub, indeg, fwd_col, bwd_col, rc_lag, rc_dur;
+    std::vector<int64_t> b_top;  // backward entries in use per replica
+    DBuf<int32_t> pub, indeg, fwd_col, bcol, rc_lag, rc_dur;
     DBuf<float> fit;
-    DBuf<int64_t> fwd_off, bwd_off;
+    DBuf<int64_t> fwd_off;
+    DBuf<BRow> brow;
     DBuf<Replica> rep;
 };
 
@@ -90,14 +93,14 @@ struct pg_ctx {
     bool loaded = false;
     bool poisoned = false;  // a kernel reported an error mid-epoch; reload before growing again
     int64_t epoch = 0;
-    int parity = 0;  // which backward buffer is current
     std::vector<HostRep> hrep;
     int64_t S = 0, T = 0, M = 0;  // slots, tiles, edge slots
+    int64_t B = 0;                // backward-region entries (all replicas)
     int64_t agent_cap = 0, edge_cap = 0, blocks_cap = 0;
     // device buffers
     DBuf<Replica> rep;
     DBuf<EpochState> st;
-    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, heavy_list, heavy_mark, e_dst, e_rank, arrivals, hlist, anchors, tile_row;
+    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, heavy_list, heavy_mark, e_dst, e_rank, arrivals, hlist, anchors;
     DBuf<int16_t> hslot;
     DBuf<uint64_t> hub2;
     DBuf<uint32_t> hub_need;
@@ -106,9 +109,10 @@ struct pg_ctx {
     DBuf<float> fit, w;
     DBuf<uint64_t> cdf, tilesum, tileoff, tables;
     DBuf<int32_t> guide;
-    DBuf<int64_t> fwd_off, bwd_off[2], len_tmp, sort_small, sort_large, sort_large_off, eoff,
-        blocksum, er_cnt, er_toff;
-    DBuf<int32_t> fwd_col, bwd_col[2];
+    DBuf<int64_t> fwd_off, len_tmp, sort_small, sort_large, sort_large_off, eoff, blocksum, er_cnt, er_toff;
+    DBuf<int32_t> fwd_col, bcol;
+    DBuf<BRow> brow;
+    DBuf<longlong2> reloc;  // copy tasks of the backward rows that move in an epoch
     DBuf<int32_t> src_tmp;  // sources of an edge range being copied out
     // refcompat functor
     DBuf<double> rc_pa, rc_rec, rc_fit, rc_rtab, rc_agent;
@@ -132,7 +136,7 @@ struct pg_ctx {
     // CUDA graph of a multi-epoch run
     cudaGraphExec_t gexec = nullptr;
     int64_t g_epoch0 = -1;
-    int g_parity0 = -1, g_epochs = 0;
+    int g_epochs = 0;
     Checkpoint ckpt;
     LikState lik;
     pg_tuning tune{};
@@ -205,10 +209,10 @@ Arena make_arena(pg_ctx* c) {
     A.inc = c->inc.p;
     A.fwd_off = c->fwd_off.p;
     A.fwd_col = c->fwd_col.p;
-    A.bwd_off_cur = c->bwd_off[c->parity].p;
-    A.bwd_col_cur = c->bwd_col[c->parity].p;
-    A.bwd_off_nxt = c->bwd_off[c->parity ^ 1].p;
-    A.bwd_col_nxt = c->bwd_col[c->parity ^ 1].p;
+    A.brow = c->brow.p;
+    A.bcol = c->bcol.p;
+    A.reloc = c->reloc.p;
+    A.reloc_cap = c->reloc.n;
     A.tables = c->tables.p;
     A.kk = c->kk.p;
     A.eoff = c->eoff.p;
@@ -219,7 +223,6 @@ Arena make_arena(pg_ctx* c) {
     A.big_list = c->big_list.p;
     A.heavy_list = c->heavy_list.p;
     A.heavy_mark = c->heavy_mark.p;
-    A.tile_row = c->tile_row.p;
     A.len_tmp = c->len_tmp.p;
     A.tilesum = c->tilesum.p;
     A.tileoff = c->tileoff.p;
@@ -267,6 +270,9 @@ Replica to_device_rep(const HostRep& h) {
     r.ebase = h.ebase;
     r.n_cap = h.n_cap;
     r.m_cap = h.m_cap;
+    r.bbase = h.bbase;
+    r.b_cap = h.b_cap;
+    r.b_top = (unsigned long long)h.b_top;
     r.n = h.n;
     r.m = h.m;
     r.tbase = h.tbase;
@@ -373,10 +379,10 @@ void free_checkpoint(Checkpoint& k) {
     dfree(k.pub);
     dfree(k.indeg);
     dfree(k.fwd_col);
-    dfree(k.bwd_col);
+    dfree(k.bcol);
     dfree(k.fit);
     dfree(k.fwd_off);
-    dfree(k.bwd_off);
+    dfree(k.brow);
     dfree(k.rep);
     dfree(k.rc_lag);
     dfree(k.rc_dur);
@@ -413,6 +419,8 @@ pg_status alloc_epoch_buffers(pg_ctx* c, int64_t agent_cap, int64_t edge_cap, in
     // buffers that must grow grow by half again, so a run of growing epochs reallocates rarely
     if (agent_cap > c->agent_cap) agent_cap = std::max<int64_t>(agent_cap, c->agent_cap + c->agent_cap / 2);
     if (edge_cap > c->edge_cap) edge_cap = std::max<int64_t>(edge_cap, c->edge_cap + c->edge_cap / 2);
+    // a captured run carries the buffers' addresses: any reallocation retires it
+    if (agent_cap > c->agent_cap || edge_cap > c->edge_cap || blocks > c->blocks_cap) destroy_graph_exec(c);
     if (agent_cap > c->agent_cap) {
         PG_CUDA(c, dalloc(c->kk, agent_cap));
         PG_CUDA(c, dalloc(c->big_list, agent_cap));
@@ -433,6 +441,13 @@ pg_status alloc_epoch_buffers(pg_ctx* c, int64_t agent_cap, int64_t edge_cap, in
         PG_CUDA(c, dalloc(c->blocksum, blocks));
         c->blocks_cap = blocks;
     }
+    // copy tasks of the backward rows that move in one epoch: a moved row is a cited one (at most
+    // one per edge) and its old entries, at most the replica's m, split into kRelocChunk chunks
+    const int64_t reloc = c->edge_cap + c->M / kRelocChunk + c->R + 1;
+    if (reloc > c->reloc.n) {
+        destroy_graph_exec(c);
+        PG_CUDA(c, dalloc(c->reloc, reloc + reloc / 2));
+    }
     return PG_OK;
 }
 
@@ -450,7 +465,7 @@ struct HostGraph {
 pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<HostGraph>& hg,
                        const pg_replica_desc* raw = nullptr) {
     const int R = (int)reps.size();
-    int64_t S = 0, T = 0, M = 0;
+    int64_t S = 0, T = 0, M = 0, B = 0;
     for (int r = 0; r < R; ++r) {
         HostRep& h = reps[r];
         h.n_cap = round_up(std::max<int64_t>(h.n_cap, h.n + 1), kTile);
@@ -465,6 +480,11 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         // (the agent kernel's bulk copies) starts and ends inside its replica's region
         h.m_cap = round_up(std::max<int64_t>(h.m_cap, h.m + 1), 4);
         M += h.m_cap;
+        // backward region: growable rows (BRow), 16-byte aligned; bregion_entries bounds every
+        // span the rows can take while the replica stays within n_cap nodes and m_cap edges
+        h.bbase = B;
+        h.b_cap = bregion_entries(h.n_cap, h.m_cap);
+        B += h.b_cap;
     }
     // a single replica's raw edges are uploaded and checked before the arena is touched (a bad
     // edge list leaves the loaded graph intact); the build below reuses the upload
@@ -505,6 +525,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     c->S = S;
     c->T = T;
     c->M = M;
+    c->B = B;
     destroy_graph_exec(c);
     c->ckpt.valid = false;
     PG_CUDA(c, dalloc(c->rep, R));
@@ -518,17 +539,14 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->w, S));
     PG_CUDA(c, dalloc(c->cdf, S));
     PG_CUDA(c, dalloc(c->guide, S));
-    PG_CUDA(c, dalloc(c->tile_row, M / kCopyTile + 2 * (int64_t)R + 2));
     PG_CUDA(c, dalloc(c->len_tmp, S));
     PG_CUDA(c, dalloc(c->sort_small, S));
     PG_CUDA(c, dalloc(c->sort_large, S));
     PG_CUDA(c, dalloc(c->sort_large_off, S));
     PG_CUDA(c, dalloc(c->fwd_off, S + R));
-    PG_CUDA(c, dalloc(c->bwd_off[0], S + R));
-    PG_CUDA(c, dalloc(c->bwd_off[1], S + R));
     PG_CUDA(c, dalloc(c->fwd_col, M));
-    PG_CUDA(c, dalloc(c->bwd_col[0], M));
-    PG_CUDA(c, dalloc(c->bwd_col[1], M));
+    PG_CUDA(c, dalloc(c->brow, S));
+    PG_CUDA(c, dalloc(c->bcol, B));
     PG_CUDA(c, dalloc(c->tables, (int64_t)R * kTableEntries));
     PG_CUDA(c, dalloc(c->hslot, S));
     PG_CUDA(c, dalloc(c->hmask, S * kMaskWords));
@@ -564,13 +582,42 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, cudaMemsetAsync(c->hslot.p, 0xFF, 2 * (size_t)S, c->stream));
     PG_CUDA(c, cudaMemsetAsync(c->inc.p, 0, sizeof(int32_t) * (size_t)S, c->stream));
     PG_CUDA(c, cudaMemsetAsync(c->w.p, 0, sizeof(float) * (size_t)S, c->stream));
-    c->parity = 0;
+    // empty rows everywhere: slots of nodes not yet born hold {0, 0, 0} until their first citation
+    PG_CUDA(c, cudaMemsetAsync(c->brow.p, 0, sizeof(BRow) * (size_t)S, c->stream));
     std::vector<int32_t> trep((size_t)T);
     std::vector<Replica> drep((size_t)R);
     std::vector<uint64_t> tabs((size_t)R * kTableEntries);
-    // scratch of the device CSR build: raw edges of one replica and the sort buffers
+    // scratch of the device CSR build: raw edges of one replica and the sort buffers; the
+    // offset-form backward CSR each replica is built or uploaded in before its rows are laid out
     DBuf<char> scratch;
     DBuf<uint32_t> berr;
+    DBuf<int64_t> t_bo, t_caps, t_begs, t_bsum;
+    DBuf<int32_t> t_bc;
+    struct Temps {
+        std::vector<std::function<void()>> f;
+        ~Temps() {
+            for (auto& g : f) g();
+        }
+    } temps;
+    temps.f.push_back([&]() {
+        dfree(t_bo);
+        dfree(t_caps);
+        dfree(t_begs);
+        dfree(t_bsum);
+        dfree(t_bc);
+    });
+    {
+        int64_t nn = 1, mm = 1;
+        for (int r = 0; r < R; ++r) {
+            nn = std::max<int64_t>(nn, reps[r].n);
+            mm = std::max<int64_t>(mm, raw ? raw[r].num_edges : reps[r].m);
+        }
+        PG_CUDA(c, dalloc(t_bo, nn + 1));
+        PG_CUDA(c, dalloc(t_caps, nn + 1));
+        PG_CUDA(c, dalloc(t_begs, nn + 1));
+        PG_CUDA(c, dalloc(t_bsum, scan_blocks_needed(nn + 1) + 2));
+        PG_CUDA(c, dalloc(t_bc, mm));
+    }
     if (raw) {
         int64_t mm = 1, nn = 1;
         for (int r = 0; r < R; ++r) {
@@ -613,8 +660,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             int64_t u = 0;
             cudaGetLastError();
             launch_build_csr(raw_src.p, raw_dst.p, d.num_edges, (int64_t)n, scratch.p, c->fwd_off.p + h.obase,
-                             c->fwd_col.p + h.ebase, c->bwd_off[0].p + h.obase, c->bwd_col[0].p + h.ebase,
-                             c->indeg.p + h.nbase, &u, berr.p, c->stream);
+                             c->fwd_col.p + h.ebase, t_bo.p, t_bc.p, c->indeg.p + h.nbase, &u, berr.p, c->stream);
             PG_CUDA(c, cudaGetLastError());
             PG_CUDA(c, cudaStreamSynchronize(c->stream));
             uint32_t be = 0;
@@ -626,12 +672,23 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase, g.fit.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
             PG_CUDA(c, cudaMemcpyAsync(c->indeg.p + h.nbase, g.indeg.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
             PG_CUDA(c, cudaMemcpyAsync(c->fwd_off.p + h.obase, g.fo.data(), 8 * (n + 1), cudaMemcpyHostToDevice, c->stream));
-            PG_CUDA(c, cudaMemcpyAsync(c->bwd_off[0].p + h.obase, g.bo.data(), 8 * (n + 1), cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(t_bo.p, g.bo.data(), 8 * (n + 1), cudaMemcpyHostToDevice, c->stream));
             if (m) {
                 PG_CUDA(c, cudaMemcpyAsync(c->fwd_col.p + h.ebase, g.fc.data(), 4 * m, cudaMemcpyHostToDevice, c->stream));
-                PG_CUDA(c, cudaMemcpyAsync(c->bwd_col[0].p + h.ebase, g.bc.data(), 4 * m, cudaMemcpyHostToDevice, c->stream));
+                PG_CUDA(c, cudaMemcpyAsync(t_bc.p, g.bc.data(), 4 * m, cudaMemcpyHostToDevice, c->stream));
             }
         }
+        // the backward rows with room to grow
+        int64_t laid = 0;
+        if (n) {
+            launch_brow_layout(t_bo.p, t_bc.p, (int64_t)n, h.m, t_caps.p, t_begs.p, t_bsum.p, c->brow.p + h.nbase,
+                               c->bcol.p + h.bbase, c->stream);
+            PG_CUDA(c, cudaGetLastError());
+            PG_CUDA(c, cudaMemcpyAsync(&laid, t_begs.p + n, 8, cudaMemcpyDeviceToHost, c->stream));
+            PG_CUDA(c, cudaStreamSynchronize(c->stream));
+        }
+        if (laid < 0 || laid > h.b_cap) return fail(c, PG_ERR_CUDA, "backward row layout out of range");
+        h.b_top = laid;
         drep[(size_t)r] = to_device_rep(h);
     }
     if (raw) {
@@ -655,6 +712,37 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     return PG_OK;
 }
 
+// Replica r's backward CSR in offset form on the host (off: n + 1 entries, col: m): the rows and
+// the used part of the region read back, then compacted in node order.  Either output may be null.
+pg_status backward_offset_form(pg_ctx* c, int r, int64_t* off, int32_t* col) {
+    const HostRep& h = c->hrep[(size_t)r];
+    const size_t n = (size_t)h.n;
+    Replica dr{};
+    PG_CUDA(c, cudaMemcpyAsync(&dr, c->rep.p + r, sizeof(Replica), cudaMemcpyDeviceToHost, c->stream));
+    std::vector<BRow> rows(n);
+    if (n) PG_CUDA(c, cudaMemcpyAsync(rows.data(), c->brow.p + h.nbase, sizeof(BRow) * n, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    const int64_t top = (int64_t)dr.b_top;
+    if (top < 0 || top > h.b_cap) return fail(c, PG_ERR_STATE, "backward region state out of range");
+    std::vector<int32_t> reg;
+    if (col && top) {
+        reg.resize((size_t)top);
+        PG_CUDA(c, cudaMemcpyAsync(reg.data(), c->bcol.p + h.bbase, 4 * (size_t)top, cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    int64_t o = 0;
+    for (size_t v = 0; v < n; ++v) {
+        const BRow& w = rows[v];
+        if (w.len < 0 || w.beg < 0 || w.beg + w.len > top || o + w.len > h.m)
+            return fail(c, PG_ERR_STATE, "backward row out of range");
+        if (off) off[v] = o;
+        if (col && w.len) std::memcpy(col + o, reg.data() + w.beg, 4 * (size_t)w.len);
+        o += w.len;
+    }
+    if (off) off[n] = o;
+    return PG_OK;
+}
+
 // Host copy of replica r's current graph (used when an R == 1 context grows).
 pg_status download_graph(pg_ctx* c, int r, HostGraph& g) {
     const HostRep& h = c->hrep[(size_t)r];
@@ -670,11 +758,7 @@ pg_status download_graph(pg_ctx* c, int r, HostGraph& g) {
     PG_CUDA(c, cudaMemcpyAsync(g.fit.data(), c->fit.p + h.nbase, 4 * n, cudaMemcpyDeviceToHost, c->stream));
     PG_CUDA(c, cudaMemcpyAsync(g.indeg.data(), c->indeg.p + h.nbase, 4 * n, cudaMemcpyDeviceToHost, c->stream));
     PG_CUDA(c, cudaMemcpyAsync(g.fo.data(), c->fwd_off.p + h.obase, 8 * (n + 1), cudaMemcpyDeviceToHost, c->stream));
-    PG_CUDA(c, cudaMemcpyAsync(g.bo.data(), c->bwd_off[c->parity].p + h.obase, 8 * (n + 1), cudaMemcpyDeviceToHost, c->stream));
-    if (m) {
-        PG_CUDA(c, cudaMemcpyAsync(g.fc.data(), c->fwd_col.p + h.ebase, 4 * m, cudaMemcpyDeviceToHost, c->stream));
-        PG_CUDA(c, cudaMemcpyAsync(g.bc.data(), c->bwd_col[c->parity].p + h.ebase, 4 * m, cudaMemcpyDeviceToHost, c->stream));
-    }
+    if (m) PG_CUDA(c, cudaMemcpyAsync(g.fc.data(), c->fwd_col.p + h.ebase, 4 * m, cudaMemcpyDeviceToHost, c->stream));
     if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
         g.lag.resize(n);
         g.dur.resize(n);
@@ -682,7 +766,7 @@ pg_status download_graph(pg_ctx* c, int r, HostGraph& g) {
         PG_CUDA(c, cudaMemcpyAsync(g.dur.data(), c->rc_dur.p + h.nbase, 4 * n, cudaMemcpyDeviceToHost, c->stream));
     }
     PG_CUDA(c, cudaStreamSynchronize(c->stream));
-    return PG_OK;
+    return backward_offset_form(c, r, g.bo.data(), g.bc.data());
 }
 
 // Make sure an R == 1 context can hold `need_n` nodes and `need_m` edges.
@@ -904,7 +988,6 @@ pg_status finish_epoch(pg_ctx* c, const std::vector<int64_t>& deltas, bool er) {
         c->rep_last_count[(size_t)r] = h.m - c->rep_last_first[(size_t)r];
         nn += deltas[(size_t)r];
     }
-    c->parity ^= 1;
     c->epoch += 1;
     fill_stats(c, nn, er);
     return PG_OK;
@@ -1017,11 +1100,12 @@ void pg_destroy(pg_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     destroy_graph_exec(c);
-    DBuf<int32_t>* i32[] = {&c->tile_rep, &c->tile_row, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list, &c->heavy_list, &c->heavy_mark,
-                            &c->e_dst, &c->e_rank, &c->arrivals, &c->anchors, &c->fwd_col, &c->bwd_col[0],
-                            &c->bwd_col[1]};
+    DBuf<int32_t>* i32[] = {&c->tile_rep, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list, &c->heavy_list, &c->heavy_mark,
+                            &c->e_dst, &c->e_rank, &c->arrivals, &c->anchors, &c->fwd_col, &c->bcol};
     for (auto* b : i32) dfree(*b);
-    DBuf<int64_t>* i64[] = {&c->fwd_off, &c->bwd_off[0], &c->bwd_off[1], &c->len_tmp,
+    dfree(c->brow);
+    dfree(c->reloc);
+    DBuf<int64_t>* i64[] = {&c->fwd_off, &c->len_tmp,
                             &c->sort_small, &c->sort_large, &c->sort_large_off, &c->eoff,
                             &c->blocksum, &c->er_cnt, &c->er_toff};
     for (auto* b : i64) dfree(*b);
@@ -1268,7 +1352,6 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
     pg_status s = plan_run(c, num_epochs, agents, max_agents, max_edges);
     if (s != PG_OK) return s;
     const int64_t e0 = c->epoch;
-    const int p0 = c->parity;
     const bool events = c->timing;
     if (events && (int64_t)c->run_ev.size() < 5 * (int64_t)num_epochs) {
         const size_t have = c->run_ev.size();
@@ -1282,16 +1365,13 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
         // clear the run totals (captured as a memset node, so every replay clears them too)
         const size_t cum0 = offsetof(EpochState, cum_rows_expanded);
         cudaMemsetAsync(reinterpret_cast<char*>(c->st.p) + cum0, 0, sizeof(EpochState) - cum0, c->stream);
-        for (int e = 0; e < num_epochs && es == PG_OK; ++e) {
+        for (int e = 0; e < num_epochs && es == PG_OK; ++e)
             es = enqueue_pa_epoch(c, e0 + e, agents[(size_t)e], events ? &c->run_ev[(size_t)e * 5] : nullptr);
-            c->parity ^= 1;
-        }
-        c->parity = p0;
         return es;
     };
     cudaGetLastError();  // errors of earlier, unrelated calls are not this run's
     if (use_graph) {
-        if (!(c->gexec && c->g_epoch0 == e0 && c->g_parity0 == p0 && c->g_epochs == num_epochs)) {
+        if (!(c->gexec && c->g_epoch0 == e0 && c->g_epochs == num_epochs)) {
             destroy_graph_exec(c);
             cudaGraph_t graph;
             PG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -1306,7 +1386,6 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
             cudaGraphDestroy(graph);
             if (ce != cudaSuccess) return fail(c, PG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
             c->g_epoch0 = e0;
-            c->g_parity0 = p0;
             c->g_epochs = num_epochs;
         }
         PG_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
@@ -1331,7 +1410,6 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
         h.n = c->h_rep[(size_t)r].n;
         h.m = c->h_rep[(size_t)r].m;
     }
-    if (num_epochs % 2) c->parity ^= 1;
     c->epoch = e0 + num_epochs;
     fill_stats(c, nn, false);
     pg_stats& S = c->stats;
@@ -1443,7 +1521,6 @@ pg_status pg_run_er_epochs(pg_ctx* c, int32_t num_epochs, int64_t delta, double 
     if (c->er_cnt.n < max_tasks + 1) PG_CUDA(c, dalloc(c->er_cnt, max_tasks + 1));
     if (c->er_toff.n < max_tasks + 1) PG_CUDA(c, dalloc(c->er_toff, max_tasks + 1));
     cudaStream_t st = c->stream;
-    const int p0 = c->parity;
     const size_t cum0 = offsetof(EpochState, cum_rows_expanded);
     PG_CUDA(c, cudaMemsetAsync(reinterpret_cast<char*>(c->st.p) + cum0, 0, sizeof(EpochState) - cum0, st));
     cudaGetLastError();
@@ -1453,10 +1530,8 @@ pg_status pg_run_er_epochs(pg_ctx* c, int32_t num_epochs, int64_t delta, double 
         launch_epoch_begin_delta(A, c->epoch + e, delta, st);
         launch_er_epoch(A, delta, p, n0 + (int64_t)e * delta, c->er_cnt.p, c->er_toff.p, c->num_sms, st);
         launch_bwd_append(A, delta, c->num_sms, st, c->side, c->fork, c->join);
-        c->parity ^= 1;
     }
     if (c->timing) cudaEventRecord(c->ev[1], st);
-    c->parity = p0;
     PG_CUDA(c, cudaGetLastError());
     s = read_back(c);
     if (s != PG_OK) return s;
@@ -1465,7 +1540,6 @@ pg_status pg_run_er_epochs(pg_ctx* c, int32_t num_epochs, int64_t delta, double 
     HostRep& h = c->hrep[0];
     h.n = c->h_rep[0].n;
     h.m = c->h_rep[0].m;
-    if (num_epochs % 2) c->parity ^= 1;
     c->epoch += num_epochs;
     c->rep_last_first[0] = h.m - (int64_t)c->h_st.edges;  // the last epoch's edges
     c->rep_last_count[0] = (int64_t)c->h_st.edges;
@@ -1563,12 +1637,11 @@ pg_status pg_copy_csr(pg_ctx* c, int32_t replica, int32_t which, int64_t* off, i
     if (which != 0 && which != 1) return fail(c, PG_ERR_ARG, "which must be 0 or 1");
     const HostRep& h = c->hrep[(size_t)replica];
     PG_CUDA(c, cudaSetDevice(c->device));
-    const int64_t* o = which ? c->bwd_off[c->parity].p : c->fwd_off.p;
-    const int32_t* cl = which ? c->bwd_col[c->parity].p : c->fwd_col.p;
+    if (which) return backward_offset_form(c, replica, off, col);
     if (off)
-        PG_CUDA(c, cudaMemcpyAsync(off, o + h.obase, 8 * (size_t)(h.n + 1), cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(off, c->fwd_off.p + h.obase, 8 * (size_t)(h.n + 1), cudaMemcpyDeviceToHost, c->stream));
     if (col && h.m)
-        PG_CUDA(c, cudaMemcpyAsync(col, cl + h.ebase, 4 * (size_t)h.m, cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(col, c->fwd_col.p + h.ebase, 4 * (size_t)h.m, cudaMemcpyDeviceToHost, c->stream));
     PG_CUDA(c, cudaStreamSynchronize(c->stream));
     return PG_OK;
 }
@@ -1654,12 +1727,20 @@ pg_status pg_checkpoint(pg_ctx* c) {
         PG_CUDA(c, dalloc(k.indeg, c->S));
         PG_CUDA(c, dalloc(k.fit, c->S));
         PG_CUDA(c, dalloc(k.fwd_off, c->S + c->R));
-        PG_CUDA(c, dalloc(k.bwd_off, c->S + c->R));
+        PG_CUDA(c, dalloc(k.brow, c->S));
         PG_CUDA(c, dalloc(k.rep, c->R));
     }
-    if (k.fwd_col.n != c->M) {
-        PG_CUDA(c, dalloc(k.fwd_col, c->M));
-        PG_CUDA(c, dalloc(k.bwd_col, c->M));
+    if (k.fwd_col.n != c->M) PG_CUDA(c, dalloc(k.fwd_col, c->M));
+    if (k.bcol.n != c->B) PG_CUDA(c, dalloc(k.bcol, c->B));
+    // the backward entries in use per replica (the device bump pointers)
+    std::vector<Replica> dr((size_t)c->R);
+    PG_CUDA(c, cudaMemcpyAsync(dr.data(), c->rep.p, sizeof(Replica) * (size_t)c->R, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(c, cudaStreamSynchronize(s));
+    k.b_top.assign((size_t)c->R, 0);
+    for (int r = 0; r < c->R; ++r) {
+        const int64_t top = (int64_t)dr[(size_t)r].b_top;
+        if (top < 0 || top > c->hrep[(size_t)r].b_cap) return fail(c, PG_ERR_STATE, "backward region state out of range");
+        k.b_top[(size_t)r] = top;
     }
     const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
     if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
@@ -1674,16 +1755,16 @@ pg_status pg_checkpoint(pg_ctx* c) {
     PG_CUDA(c, cudaMemcpyAsync(k.indeg.p, c->indeg.p, 4 * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(k.fit.p, c->fit.p, 4 * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(k.fwd_off.p, c->fwd_off.p, 8 * (size_t)(c->S + c->R), d2d, s));
-    PG_CUDA(c, cudaMemcpyAsync(k.bwd_off.p, c->bwd_off[c->parity].p, 8 * (size_t)(c->S + c->R), d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(k.brow.p, c->brow.p, sizeof(BRow) * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(k.rep.p, c->rep.p, sizeof(Replica) * (size_t)c->R, d2d, s));
-    for (const HostRep& h : c->hrep) {
-        if (!h.m) continue;
-        PG_CUDA(c, cudaMemcpyAsync(k.fwd_col.p + h.ebase, c->fwd_col.p + h.ebase, 4 * (size_t)h.m, d2d, s));
-        PG_CUDA(c, cudaMemcpyAsync(k.bwd_col.p + h.ebase, c->bwd_col[c->parity].p + h.ebase, 4 * (size_t)h.m, d2d, s));
+    for (int r = 0; r < c->R; ++r) {
+        const HostRep& h = c->hrep[(size_t)r];
+        if (h.m) PG_CUDA(c, cudaMemcpyAsync(k.fwd_col.p + h.ebase, c->fwd_col.p + h.ebase, 4 * (size_t)h.m, d2d, s));
+        const int64_t top = k.b_top[(size_t)r];
+        if (top) PG_CUDA(c, cudaMemcpyAsync(k.bcol.p + h.bbase, c->bcol.p + h.bbase, 4 * (size_t)top, d2d, s));
     }
     PG_CUDA(c, cudaStreamSynchronize(s));
     k.epoch = c->epoch;
-    k.parity = c->parity;
     k.hrep = c->hrep;
     k.valid = true;
     return PG_OK;
@@ -1692,12 +1773,10 @@ pg_status pg_checkpoint(pg_ctx* c) {
 pg_status pg_restore(pg_ctx* c) {
     if (!c) return PG_ERR_ARG;
     Checkpoint& k = c->ckpt;
-    if (!k.valid || k.pub.n != c->S || k.fwd_col.n != c->M)
+    if (!k.valid || k.pub.n != c->S || k.fwd_col.n != c->M || k.bcol.n != c->B)
         return fail(c, PG_ERR_STATE, "no checkpoint matches the current arena");
     cudaStream_t s = c->stream;
     const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
-    // the checkpoint's backward copy goes into the buffer that was current when it was taken
-    const int par = k.parity;
     if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT && k.rc_lag.n == c->S) {
         PG_CUDA(c, cudaMemcpyAsync(c->rc_lag.p, k.rc_lag.p, 4 * (size_t)c->S, d2d, s));
         PG_CUDA(c, cudaMemcpyAsync(c->rc_dur.p, k.rc_dur.p, 4 * (size_t)c->S, d2d, s));
@@ -1706,12 +1785,13 @@ pg_status pg_restore(pg_ctx* c) {
     PG_CUDA(c, cudaMemcpyAsync(c->indeg.p, k.indeg.p, 4 * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(c->fit.p, k.fit.p, 4 * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(c->fwd_off.p, k.fwd_off.p, 8 * (size_t)(c->S + c->R), d2d, s));
-    PG_CUDA(c, cudaMemcpyAsync(c->bwd_off[par].p, k.bwd_off.p, 8 * (size_t)(c->S + c->R), d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(c->brow.p, k.brow.p, sizeof(BRow) * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(c->rep.p, k.rep.p, sizeof(Replica) * (size_t)c->R, d2d, s));
-    for (const HostRep& h : k.hrep) {
-        if (!h.m) continue;
-        PG_CUDA(c, cudaMemcpyAsync(c->fwd_col.p + h.ebase, k.fwd_col.p + h.ebase, 4 * (size_t)h.m, d2d, s));
-        PG_CUDA(c, cudaMemcpyAsync(c->bwd_col[par].p + h.ebase, k.bwd_col.p + h.ebase, 4 * (size_t)h.m, d2d, s));
+    for (size_t r = 0; r < k.hrep.size(); ++r) {
+        const HostRep& h = k.hrep[r];
+        if (h.m) PG_CUDA(c, cudaMemcpyAsync(c->fwd_col.p + h.ebase, k.fwd_col.p + h.ebase, 4 * (size_t)h.m, d2d, s));
+        const int64_t top = k.b_top[r];
+        if (top) PG_CUDA(c, cudaMemcpyAsync(c->bcol.p + h.bbase, k.bcol.p + h.bbase, 4 * (size_t)top, d2d, s));
     }
     PG_CUDA(c, cudaMemsetAsync(c->inc.p, 0, 4 * (size_t)c->S, s));
     // the saved state is consistent: clear the error word a failed epoch left set
@@ -1719,7 +1799,6 @@ pg_status pg_restore(pg_ctx* c) {
                                sizeof(uint32_t), s));
     PG_CUDA(c, cudaStreamSynchronize(s));
     c->epoch = k.epoch;
-    c->parity = par;
     c->hrep = k.hrep;
     c->poisoned = false;
     return PG_OK;

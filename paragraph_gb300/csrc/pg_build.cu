@@ -235,4 +235,55 @@ void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t
     cudaMemcpyAsync(indeg, bcnt, (size_t)n * 4, cudaMemcpyDeviceToDevice, s);
 }
 
+// ---------------------------------------------------------------- growable backward rows
+// The engine keeps backward rows with room to grow (BRow).  From a backward CSR in offset form
+// (bo: n + 1 offsets, bc: its columns), row v gets brow_cap(len) entries -- none when empty -- at
+// the exclusive scan of those spans, and its entries are copied there.
+__global__ void __launch_bounds__(256) k_brow_caps(const int64_t* bo, int64_t n, int64_t* caps) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t len = bo[v + 1] - bo[v];
+        caps[v] = len > 0 ? brow_cap(len) : 0;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_brow_rows(const int64_t* bo, const int64_t* begs, int64_t n, BRow* brow) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t len = bo[v + 1] - bo[v];
+        BRow r;
+        r.beg = len > 0 ? begs[v] : 0;
+        r.len = (int32_t)len;
+        r.cap = (int32_t)(len > 0 ? begs[v + 1] - begs[v] : 0);
+        brow[v] = r;
+    }
+}
+
+// entry p of the offset form goes to its row's span: the row is the last v with bo[v] <= p
+__global__ void __launch_bounds__(256) k_brow_cols(const int64_t* bo, const int32_t* bc, const int64_t* begs,
+                                                   int64_t n, int64_t m, int32_t* out) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
+        int64_t lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (bo[mid] <= p)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        out[begs[lo] + (p - bo[lo])] = bc[p];
+    }
+}
+
+void launch_brow_layout(const int64_t* bo, const int32_t* bc, int64_t n, int64_t m, int64_t* caps,
+                        int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcol, cudaStream_t s) {
+    if (n <= 0) return;
+    const unsigned gn = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
+    k_brow_caps<<<gn, 256, 0, s>>>(bo, n, caps);
+    launch_scan_i64(caps, begs, n, blocksum, s);
+    k_brow_rows<<<gn, 256, 0, s>>>(bo, begs, n, brow);
+    if (m > 0) {
+        const unsigned gm = (unsigned)std::min<int64_t>((m + 255) / 256, 152 * 16);
+        k_brow_cols<<<gm, 256, 0, s>>>(bo, bc, begs, n, m, bcol);
+    }
+}
+
 }  // namespace pg

@@ -3,10 +3,12 @@
 // Layout in HBM (one arena per context, R replicas):
 //   node slot arrays (pub, fitness, indeg, w, cdf, inc) are indexed nbase_r + v, v < n_cap_r; every
 //   nbase_r is a multiple of kTile so a scan tile never spans two replicas;
-//   offset arrays (fwd_off, bwd_off) hold n_cap_r + 1 int64 entries at obase_r = nbase_r + r and
-//   are LOCAL to the replica's edge region;
-//   column arrays (fwd_col, bwd_col) hold replica-local int32 node ids at ebase_r + offset.
-// Backward offsets and columns are double-buffered: each epoch writes the other copy.
+//   forward offsets (fwd_off) hold n_cap_r + 1 int64 entries at obase_r = nbase_r + r and are LOCAL
+//   to the replica's edge region; forward columns (fwd_col) hold replica-local int32 node ids at
+//   ebase_r + offset (rows appended in node order, never moved);
+//   backward rows (brow, one 16-byte BRow per node slot) point into the replica's backward region
+//   (bcol at bbase_r, b_cap_r entries): a row has room for `cap` entries and holds `len` at `beg`,
+//   and grows in place until full, when it moves to twice its length at the region's bump pointer.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -31,7 +33,7 @@ constexpr int kRcBigStream = 1024;  // ... or a 2-hop stream (the rows of the ge
 constexpr int kRcBigCap = 16384;     // such agents per epoch (the rest keep the one-warp path)
 constexpr int kGBits = 13;           // per-warp global hash for anchor rows too large for shared memory
 constexpr int kZCap = 1024;          // 1-hop frontier entries kept in shared memory per warp
-constexpr int kCopyTile = 4096;      // backward entries per copy tile
+constexpr int kRelocChunk = 4096;    // backward entries per copy task of a moved row
 constexpr int kHeavyMax = 256;       // hubs per replica with a bit in the per-node hub mask
 constexpr int kMaskWords = kHeavyMax / 64;
 constexpr int kHeavyMinLog = 10;     // only nodes with degree >= 2^10 can be hubs
@@ -54,10 +56,28 @@ enum : uint32_t {
     kErrTimeout = 8u,  // a bounded wait on an asynchronous copy ran out
 };
 
+// Backward row of a node: entries bcol[bbase + beg, bbase + beg + len), room for cap entries.  beg
+// and cap are multiples of 4, so a row starts on a 16-byte boundary; an empty row has cap 0.
+struct __align__(16) BRow {
+    long long beg;
+    int32_t len;
+    int32_t cap;
+};
+
+// Room given to a backward row that must hold L >= 1 entries: 2L rounded up to a multiple of 4.  A
+// row that outgrows its room moves, so its earlier spans c_0 < c_1 < ... < c_k satisfy
+// c_i < L_(i+1) <= c_(i+1) / 2: together they take less than 2 c_k <= 4 L + 4 entries (L its final
+// length), and a region of 4 m + 4 n entries (m edges, n nodes at most) never runs out.  Each entry
+// moves O(1) times amortised.
+PG_HD int64_t brow_cap(int64_t L) { return (2 * L + 3) & ~3ll; }
+PG_HD int64_t bregion_entries(int64_t n_cap, int64_t m_cap) { return 4 * m_cap + 4 * n_cap + 4; }
+
 struct Replica {
     // static layout
     int64_t nbase, obase, ebase;
     int64_t n_cap, m_cap;
+    int64_t bbase, b_cap;           // backward region: first entry and size
+    unsigned long long b_top;       // backward region: entries handed out (bump pointer)
     // state
     int64_t n, m;
     // this epoch
@@ -81,7 +101,6 @@ struct Replica {
     int32_t heavy_thr;
     int32_t heavy_count;
     int32_t heavy_hist[kHeavyBins];
-    int64_t ctbase;  // first backward-copy tile of the replica this epoch
     // refcompat functor (weight model PG_WEIGHTS_REFCOMPAT)
     double rc_w[3];   // pa, rec, fit weights, normalised; rc_w[0] < 0: drawn per agent
     double rc_alpha;  // share of the neighbourhood budget from the 1-hop set; < 0: per agent
@@ -112,7 +131,7 @@ struct EpochState {
     unsigned long long draws;
     unsigned long long bwd_moved;
     unsigned long long nodes_weighted;
-    unsigned long long copy_tiles;  // backward-copy tiles of the epoch (all replicas)
+    unsigned long long reloc_count; // copy tasks of the backward rows that moved this epoch
     unsigned long long adj_scanned; // adjacency entries examined by membership tests
     // run totals, accumulated by the epoch-end kernel and cleared by the host at run start
     unsigned long long cum_rows_expanded;
@@ -145,10 +164,8 @@ struct Arena {
     int32_t* inc;
     int64_t* fwd_off;
     int32_t* fwd_col;
-    int64_t* bwd_off_cur;
-    int32_t* bwd_col_cur;
-    int64_t* bwd_off_nxt;
-    int32_t* bwd_col_nxt;
+    BRow* brow;                // [slots] backward row of each node
+    int32_t* bcol;             // backward regions of all replicas
     const uint64_t* tables;    // [R][kTableEntries]
     // per-epoch buffers
     int32_t* kk;               // [agent cap] out-degree per agent
@@ -163,14 +180,15 @@ struct Arena {
     int32_t* zbig;             // [agent-kernel warp slots][1 << kGBits] rows of anchors too large for H
     int32_t* rc_big_id;        // [kRcBigCap][kKMax] sorted top of each listed refcompat agent's 2-hop stream
     long long* rc_big_meta;    // [kRcBigCap][3] entries, rows, elements of that stream
-    int32_t* tile_row;         // [copy tiles] row holding the first position of each copy tile
-    int64_t* len_tmp;          // [slots]
+    longlong2* reloc;          // [reloc_cap] moved-row copy tasks: (source, destination << 16 | length)
+    int64_t reloc_cap;
+    int64_t* len_tmp;          // [slots] where a row's new entries of the epoch start
     uint64_t* tilesum;         // [ntiles]
     uint64_t* tileoff;         // [ntiles]
     int64_t* blocksum;         // [scan blocks]
-    int64_t* sort_small;       // [slots] packed (slot << 8 | len)
+    int64_t* sort_small;       // [slots] packed (slot << 9 | new entries)
     int64_t* sort_large;       // [slots] slot
-    int64_t* sort_large_off;   // [slots] scratch offset
+    int64_t* sort_large_off;   // [slots] packed (scratch offset << 32 | new entries)
     int16_t* hslot;            // [slots] hub bit of the node or -1
     uint64_t* hmask;           // [slots][kMaskWords] bit b set when hub b is adjacent to the node
     uint64_t* hub2;            // [R][kHeavyMax][kMaskWords] hubs sharing a neighbour with hub b
@@ -197,7 +215,7 @@ struct Arena {
     // launch tuning (results do not depend on it)
     int32_t tune_agent_ctas;   // agent-kernel CTAs per SM, 0 = occupancy limit
     int32_t tune_small_hash;   // 1: 1024-slot frontier hash in the k <= 64 kernel, 0: 2048
-    int32_t tune_copy_ctas;    // backward-copy CTAs per SM
+    int32_t tune_copy_ctas;    // moved-row copy CTAs per SM
     int32_t rep_base;          // RNG replica index of replica 0 (pg_config.replica_base)
     uint32_t first_wait_polls; // polls of the first bounded wait on each staged copy (pg_set_wait_limit)
     uint32_t pad_wp;
@@ -235,6 +253,14 @@ PG_HD int guide_shift(uint64_t Wq, int64_t n) {
 // ---------------------------------------------------------------- warp helpers
 #if defined(__CUDACC__)
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// Bounds [b, e) of backward row x (one 16-byte load), relative to the replica's region.
+__device__ __forceinline__ void bspan(const BRow* br, int64_t x, int64_t& b, int64_t& e) {
+    const longlong2 q = *reinterpret_cast<const longlong2*>(br + x);
+    b = q.x;
+    e = q.x + (int64_t)(int32_t)(uint32_t)(unsigned long long)q.y;
+}
+__device__ __forceinline__ int64_t blen(const BRow* br, int64_t x) { return br[x].len; }
 
 template <typename T>
 __device__ __forceinline__ T warp_incl_scan(T v) {
@@ -352,8 +378,9 @@ __device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64
 
 // ---------------------------------------------------------------- host launchers
 // Kernels one PA epoch enqueues: epoch begin (1), weights + CDF (4), agent setup + offset scan +
-// check (5), agent kernels (2), backward append incl. epoch end (8).
-constexpr int kPaEpochKernels = 20;
+// check (5), agent kernels (2), backward append incl. epoch end (6: grow, moved-row copy, place,
+// two sorts, end).
+constexpr int kPaEpochKernels = 18;
 // Extra kernels of the thinning sampler: the CDF's guide table (1) and the hub index (histogram,
 // pick, collect, mask, hub pairs).
 constexpr int kThinKernels = 6;
@@ -421,6 +448,11 @@ size_t build_scratch_bytes(int64_t m, int64_t n);
 void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,
                       int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_out,
                       uint32_t* err, cudaStream_t s);
+// growable backward rows from an offset-form backward CSR (pg_build.cu): caps n, begs n + 1 (begs[n]
+// = entries laid out), blocksum scan_blocks_needed(n) + 2 entries of scratch; brow/bcol: the
+// replica's rows and region
+void launch_brow_layout(const int64_t* bo, const int32_t* bc, int64_t n, int64_t m, int64_t* caps,
+                        int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcol, cudaStream_t s);
 // resident CTAs per SM of the k <= 64 agent kernel (after init_agent_kernels)
 int agent_occupancy(int thin, int small_hash);
 int64_t agent_warp_slots(int num_sms);

@@ -20,9 +20,12 @@ struct RcSmem {
     int32_t out[kKMax]; // sorted row (emit)
 };
 
-__device__ __forceinline__ bool rc_in_rows(const int64_t* fo, const int32_t* fc, const int64_t* bo,
+__device__ __forceinline__ bool rc_in_rows(const int64_t* fo, const int32_t* fc, const BRow* br,
                                            const int32_t* bc, int32_t g, int32_t v) {
-    return contains(fc, fo[g], fo[g + 1], v) || contains(bc, bo[g], bo[g + 1], v);
+    if (contains(fc, fo[g], fo[g + 1], v)) return true;
+    int64_t b0, b1;
+    bspan(br, g, b0, b1);
+    return contains(bc, b0, b1, v);
 }
 
 // Offer one candidate per lane to the top-k list.  When more than two pass the list's threshold
@@ -120,7 +123,7 @@ __device__ __forceinline__ void rc_topk_offer(bool valid, float key, int id, int
 struct RcCtx {
     const int64_t* fo;
     const int32_t* fc;
-    const int64_t* bo;
+    const BRow* br;
     const int32_t* bc;
     const double* pa;
     const double* rec;
@@ -153,8 +156,9 @@ __device__ __forceinline__ void rc_2hop_slice(const RcCtx& X, int64_t cfirst, in
         if (y >= 0) {
             yf0 = X.fo[y];
             ylf = X.fo[y + 1] - yf0;
-            yb0 = X.bo[y];
-            yd = ylf + (X.bo[y + 1] - yb0);
+            int64_t yb1;
+            bspan(X.br, y, yb0, yb1);
+            yd = ylf + (yb1 - yb0);
         }
         const int64_t incl = warp_incl_scan(yd);
         const int64_t tot = __shfl_sync(kFull, incl, 31);
@@ -179,7 +183,7 @@ __device__ __forceinline__ void rc_2hop_slice(const RcCtx& X, int64_t cfirst, in
             if (t < tot) {
                 const int64_t x = t - oys;
                 z = x < olf ? X.fc[of0 + x] : X.bc[ob0 + (x - olf)];
-                valid = z != X.gen && !rc_in_rows(X.fo, X.fc, X.bo, X.bc, X.gen, z);
+                valid = z != X.gen && !rc_in_rows(X.fo, X.fc, X.br, X.bc, X.gen, z);
                 if (valid)
                     key = rc_key(X.seed, X.rep, X.ep, X.unit, z,
                                  X.w3[0] * X.pa[z] + X.w3[1] * X.rec[z] + X.w3[2] * X.fit[z]);
@@ -199,8 +203,8 @@ __device__ void process_agent_rc(const Arena& A, int64_t a, int k, RcSmem& S) {
     const uint32_t ep = (uint32_t)A.st->epoch, unit = (uint32_t)al, rep = (uint32_t)(r + A.rep_base);
     const int64_t* fo = A.fwd_off + rp.obase;
     const int32_t* fc = A.fwd_col + rp.ebase;
-    const int64_t* bo = A.bwd_off_cur + rp.obase;
-    const int32_t* bc = A.bwd_col_cur + rp.ebase;
+    const BRow* br = A.brow + rp.nbase;
+    const int32_t* bc = A.bcol + rp.bbase;
     const double* pa = A.rc_pa + rp.nbase;
     const double* rec = A.rc_rec + rp.nbase;
     const double* fit = A.rc_fit + rp.nbase;
@@ -222,8 +226,10 @@ __device__ void process_agent_rc(const Arena& A, int64_t a, int k, RcSmem& S) {
     int in_t = rem1 > 0 ? (int)ceil((double)rem1 * alpha) : 0;
     if (in_t > rem1) in_t = rem1 > 0 ? rem1 : 0;
     long long rows = 1, elems = 0, draws = 0;
-    const int64_t gf0 = fo[gen], glf = fo[gen + 1] - gf0, gb0 = bo[gen];
-    const int64_t gd = glf + (bo[gen + 1] - gb0);
+    const int64_t gf0 = fo[gen], glf = fo[gen + 1] - gf0;
+    int64_t gb0, gb1;
+    bspan(br, gen, gb0, gb1);
+    const int64_t gd = glf + (gb1 - gb0);
 
     // ---- the 1-hop set
     int in = 0;
@@ -257,7 +263,7 @@ __device__ void process_agent_rc(const Arena& A, int64_t a, int k, RcSmem& S) {
         RcCtx X;
         X.fo = fo;
         X.fc = fc;
-        X.bo = bo;
+        X.br = br;
         X.bc = bc;
         X.pa = pa;
         X.rec = rec;

@@ -100,7 +100,7 @@ struct Mask {
 struct Ball {
     const int64_t* fo;
     const int32_t* fc;
-    const int64_t* bo;
+    const BRow* br;
     const int32_t* bc;
     const int16_t* hslot;             // hub bit of the node or -1
     const unsigned long long* hmask;  // [node][kMaskWords]
@@ -202,8 +202,10 @@ __device__ __forceinline__ bool in_z(const Ball& B, int32_t v) {
         for (int i = 0; i < X.na; ++i) {
             if (!X.big[i]) continue;
             const int x = X.anchors[i];
-            if (contains(B.fc, B.fo[x], B.fo[x + 1], v) || contains(B.bc, B.bo[x], B.bo[x + 1], v))
-                return true;
+            if (contains(B.fc, B.fo[x], B.fo[x + 1], v)) return true;
+            int64_t b0, b1;
+            bspan(B.br, x, b0, b1);
+            if (contains(B.bc, b0, b1, v)) return true;
         }
     }
     if (B.any_ha) {
@@ -222,9 +224,14 @@ __device__ bool member_rows_warp(const Ball& B, int32_t j, long long& examined) 
     const int lane = lane_id();
     examined = 0;
     for (int dir = 0; dir < 2; ++dir) {
-        const int64_t* off = dir ? B.bo : B.fo;
         const int32_t* col = dir ? B.bc : B.fc;
-        const int64_t p0 = off[j], p1 = off[j + 1];
+        int64_t p0, p1;
+        if (dir) {
+            bspan(B.br, j, p0, p1);
+        } else {
+            p0 = B.fo[j];
+            p1 = B.fo[j + 1];
+        }
         for (int64_t p = p0; p < p1; p += 128) {
             int32_t v[4];
 #pragma unroll
@@ -275,8 +282,8 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     Ball B;
     B.fo = A.fwd_off + rp.obase;
     B.fc = A.fwd_col + rp.ebase;
-    B.bo = A.bwd_off_cur + rp.obase;
-    B.bc = A.bwd_col_cur + rp.ebase;
+    B.br = A.brow + rp.nbase;
+    B.bc = A.bcol + rp.bbase;
     B.hslot = A.hslot + rp.nbase;
     B.hmask = reinterpret_cast<const unsigned long long*>(A.hmask) + rp.nbase * kMaskWords;
     B.H = S.H;
@@ -311,9 +318,14 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
         int64_t r_st = 0, r_len = 0;
         int r_hs = -1;
         if (has_row) {
-            const int64_t* off = (lane & 1) ? B.bo : B.fo;
-            r_st = off[xrow];
-            r_len = off[xrow + 1] - r_st;
+            int64_t r_end;
+            if (lane & 1) {
+                bspan(B.br, xrow, r_st, r_end);
+            } else {
+                r_st = B.fo[xrow];
+                r_end = B.fo[xrow + 1];
+            }
+            r_len = r_end - r_st;
             r_hs = hub_slot(B, xrow);
         }
         int64_t dd[PG_MAX_ANCHORS_DEV];
@@ -492,7 +504,9 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             // the node's hub slot and row bounds are loaded before the frontier probe, so the
             // global loads overlap the shared-memory hash lookups
             const int hs = hub_slot(B, j);
-            const int64_t jf0 = B.fo[j], jf1 = B.fo[j + 1], jb0 = B.bo[j], jb1 = B.bo[j + 1];
+            const int64_t jf0 = B.fo[j], jf1 = B.fo[j + 1];
+            int64_t jb0, jb1;
+            bspan(B.br, j, jb0, jb1);
             if (GENERAL ? in_z(B, j) : hash_contains(S.H, kHBits, j)) {
                 mem = true;
             } else if (hs >= 0) {

@@ -19,11 +19,11 @@ namespace pg {
 
 __device__ __forceinline__ void d_epoch_begin(const Arena& A, int64_t epoch, int64_t delta_override) {
     __shared__ int64_t sw[33];
-    __shared__ int64_t carry, ccarry;
+    __shared__ int64_t carry;
     EpochState* st = A.st;
     if (threadIdx.x == 0) {
         carry = 0;
-        ccarry = 0;
+        st->reloc_count = 0;
         st->epoch = epoch;
         st->edges = 0;
         st->queue_small = 0;
@@ -69,16 +69,8 @@ __device__ __forceinline__ void d_epoch_begin(const Arena& A, int64_t epoch, int
         __syncthreads();
         if (threadIdx.x == 0) carry += tot;
         __syncthreads();
-        const int64_t ct = r < A.R ? (A.rep[r].m + kCopyTile - 1) / kCopyTile : 0;
-        int64_t ctot;
-        const int64_t cex = block_excl_scan<int64_t>(ct, sw, &ctot);
-        if (r < A.R) A.rep[r].ctbase = ccarry + cex;
-        __syncthreads();
-        if (threadIdx.x == 0) ccarry += ctot;
-        __syncthreads();
     }
     if (threadIdx.x == 0) {
-        st->copy_tiles = (unsigned long long)ccarry;
         st->agents = carry;
         if (carry > A.agent_cap) atomicOr(&st->error, kErrCapacity);
     }
@@ -340,8 +332,7 @@ __global__ void __launch_bounds__(kTileThreads) k_guide_fill(Arena A) { d_guide_
 // nodes are hubs only changes speed, never a result.
 __device__ __forceinline__ int64_t degree_of(const Arena& A, const Replica& rp, int64_t v) {
     const int64_t* fo = A.fwd_off + rp.obase;
-    const int64_t* bo = A.bwd_off_cur + rp.obase;
-    return (fo[v + 1] - fo[v]) + (bo[v + 1] - bo[v]);
+    return (fo[v + 1] - fo[v]) + blen(A.brow + rp.nbase, v);
 }
 
 __device__ __forceinline__ void d_hub_hist(const Arena& A, int vb) {
@@ -444,9 +435,17 @@ __device__ __forceinline__ void d_hub_mask(const Arena& A, int G, int vb) {
     const unsigned long long bit = 1ull << (b & 63);
     const int64_t stride = (int64_t)G * blockDim.x;
     for (int dir = 0; dir < 2; ++dir) {
-        const int64_t* off = (dir ? A.bwd_off_cur : A.fwd_off) + rp.obase;
-        const int32_t* col = (dir ? A.bwd_col_cur : A.fwd_col) + rp.ebase;
-        for (int64_t p = off[h] + (int64_t)g * blockDim.x + threadIdx.x; p < off[h + 1]; p += stride)
+        int64_t p0, p1;
+        const int32_t* col;
+        if (dir) {
+            bspan(A.brow + rp.nbase, h, p0, p1);
+            col = A.bcol + rp.bbase;
+        } else {
+            p0 = A.fwd_off[rp.obase + h];
+            p1 = A.fwd_off[rp.obase + h + 1];
+            col = A.fwd_col + rp.ebase;
+        }
+        for (int64_t p = p0 + (int64_t)g * blockDim.x + threadIdx.x; p < p1; p += stride)
             atomicOr((unsigned long long*)&A.hmask[(rp.nbase + col[p]) * kMaskWords + (b >> 6)], bit);
     }
 }
@@ -471,9 +470,17 @@ __device__ __forceinline__ void d_hub_pairs(const Arena& A, int G, int vb) {
 #pragma unroll
     for (int w = 0; w < kMaskWords; ++w) m[w] = 0;
     for (int dir = 0; dir < 2; ++dir) {
-        const int64_t* off = (dir ? A.bwd_off_cur : A.fwd_off) + rp.obase;
-        const int32_t* col = (dir ? A.bwd_col_cur : A.fwd_col) + rp.ebase;
-        for (int64_t p = off[h] + (int64_t)g * blockDim.x + threadIdx.x; p < off[h + 1]; p += stride) {
+        int64_t p0, p1;
+        const int32_t* col;
+        if (dir) {
+            bspan(A.brow + rp.nbase, h, p0, p1);
+            col = A.bcol + rp.bbase;
+        } else {
+            p0 = A.fwd_off[rp.obase + h];
+            p1 = A.fwd_off[rp.obase + h + 1];
+            col = A.fwd_col + rp.ebase;
+        }
+        for (int64_t p = p0 + (int64_t)g * blockDim.x + threadIdx.x; p < p1; p += stride) {
             const uint64_t* hm = A.hmask + (rp.nbase + col[p]) * kMaskWords;
 #pragma unroll
             for (int w = 0; w < kMaskWords; ++w) m[w] |= hm[w];
