@@ -294,7 +294,8 @@ pg_status pg_restore(pg_ctx* ctx);
 /* ---- launch tuning (no counterpart in the reference; results never depend on it) ---- */
 typedef struct {
     int32_t agent_ctas_per_sm; /* CTAs per SM of the k <= 64 agent kernel; 0 = occupancy limit */
-    int32_t small_hash;        /* 1: 1024-slot frontier hash per warp in that kernel, 0: 2048 */
+    int32_t small_hash;        /* shape of that kernel: 0 a 2048-slot frontier hash per warp and
+                                  512-entry stage buffers; 1 1024 slots, 1024-entry stages */
     int32_t copy_ctas_per_sm;  /* CTAs per SM of the backward-CSR copy; 0 = default (8) */
     int32_t lik_chunk_agents;  /* > 0: pg_trace_load keeps at most this many agents' neighbourhood
                                   balls per chunk, so every likelihood pass rebuilds them chunk by

@@ -504,28 +504,31 @@ __device__ __forceinline__ void d_edges_check(const Arena& A, int64_t agents) {
 
 __global__ void k_edges_check(Arena A, int64_t agents) { d_edges_check(A, agents); }
 
-// entries per stage buffer of the thinning sampler (two buffers per warp)
-template <int KCAP, bool HSMALL>
+// Shapes of the k <= 64 thinning kernel (pg_tuning.small_hash = HS): 0 -- a 2048-slot frontier hash
+// and 512-entry stage buffers; 1 -- 1024 slots and 1024-entry stages; both 4 CTAs per SM.  The
+// k <= 256 kernel always has 1024 slots and 512-entry stages.  (A third shape, 1024 slots and
+// 512-entry stages at 5 CTAs per SM with 96 registers, was measured 9 % slower on the PA workload
+// than shape 0 and was not picked by the tuner for the ensemble.)
+template <int KCAP, int HS>
 struct ThinStage {
-    static constexpr int value = (KCAP <= kKSmall && HSMALL) ? 1024 : 512;
+    static constexpr int value = (KCAP <= kKSmall && HS == 1) ? 1024 : 512;
 };
-
-template <int KCAP, bool HSMALL>
-constexpr size_t thin_smem_bytes() {
-    constexpr int HCAP = (KCAP <= kKSmall && !HSMALL) ? 2 * kZCap : kZCap;
-    return sizeof(ThinSmem<KCAP, HCAP, ThinStage<KCAP, HSMALL>::value>) * kAgentWarps;
+template <int KCAP, int HS>
+struct ThinHash {
+    static constexpr int value = (KCAP <= kKSmall && HS == 0) ? 2 * kZCap : kZCap;
+};
+template <int KCAP, int HS>
+__host__ __device__ constexpr size_t thin_smem_bytes() {
+    return sizeof(ThinSmem<KCAP, ThinHash<KCAP, HS>::value, ThinStage<KCAP, HS>::value>) * kAgentWarps;
 }
 
 // The agent loop of one warp.  Thinning variants: the warp's shared memory is dsm + warp * stride
 // (the calling kernel's dynamic shared memory; stride >= sizeof of this variant's ThinSmem); the
 // enumeration variants use static shared memory.
-template <int KCAP, bool BIG, bool THIN, bool HSMALL = false>
+template <int KCAP, bool BIG, bool THIN, int HS = 0>
 __device__ __forceinline__ void d_agents(const Arena& A, int64_t agents, unsigned char* dsm, size_t stride) {
-    // frontier hash capacity: 2048 slots for the common small-k kernel (1024 in the HSMALL variant,
-    // which fits more CTAs per SM), 1024 for the k <= 256 one so that four warps stay within 48 KiB
-    // of static shared memory
-    constexpr int HCAP = (KCAP <= kKSmall && !HSMALL) ? 2 * kZCap : kZCap;
-    constexpr int STAGE = ThinStage<KCAP, HSMALL>::value;
+    constexpr int HCAP = ThinHash<KCAP, HS>::value;
+    constexpr int STAGE = ThinStage<KCAP, HS>::value;
     using Smem = typename std::conditional<THIN, ThinSmem<KCAP, HCAP, STAGE>, AgentSmem<KCAP>>::type;
     Smem* sp;
     if constexpr (THIN) {
@@ -589,13 +592,12 @@ __device__ __forceinline__ void d_agents(const Arena& A, int64_t agents, unsigne
     }
 }
 
-template <int KCAP, bool BIG, bool THIN, bool HSMALL = false>
+template <int KCAP, bool BIG, bool THIN, int HS = 0>
 __global__ void __launch_bounds__(kAgentWarps * 32, 4) k_agents(Arena A, int64_t agents) {
     // the thinning variants hold two stage buffers per warp and go past 48 KiB: dynamic
     extern __shared__ __align__(16) unsigned char agent_dsm[];
-    constexpr int HCAP = (KCAP <= kKSmall && !HSMALL) ? 2 * kZCap : kZCap;
-    constexpr size_t stride = sizeof(ThinSmem<KCAP, HCAP, ThinStage<KCAP, HSMALL>::value>);
-    d_agents<KCAP, BIG, THIN, HSMALL>(A, agents, agent_dsm, stride);
+    constexpr size_t stride = thin_smem_bytes<KCAP, HS>() / kAgentWarps;
+    d_agents<KCAP, BIG, THIN, HS>(A, agents, agent_dsm, stride);
 }
 
 __global__ void __launch_bounds__(kAgentWarps * 32) k_agents_rc(Arena A, int64_t agents) {
@@ -721,7 +723,7 @@ void launch_rc_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t 
 }
 
 static int g_blocks[2][2] = {{0, 0}, {0, 0}};  // [thin][big]
-static int g_blocks_hsmall = 0;                 // thinning, k <= 64, 1024-slot frontier
+static int g_blocks_hs[2] = {0, 0};             // thinning, k <= 64, by shape (small_hash)
 
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s) {
     if (agents <= 0) return;
@@ -737,24 +739,27 @@ cudaError_t init_agent_kernels() {
     const int th = kAgentWarps * 32;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[0][0], k_agents<kKSmall, false, false>, th, 0);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[0][1], k_agents<kKMax, true, false>, th, 0);
-    constexpr size_t ds = thin_smem_bytes<kKSmall, false>(), db = thin_smem_bytes<kKMax, false>(),
-                     dh = thin_smem_bytes<kKSmall, true>();
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents<kKSmall, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ds);
+    constexpr size_t d0 = thin_smem_bytes<kKSmall, 0>(), d1 = thin_smem_bytes<kKSmall, 1>(),
+                     db = thin_smem_bytes<kKMax, 0>();
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents<kKSmall, false, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d0);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents<kKSmall, false, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d1);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents<kKMax, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)db);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents<kKSmall, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dh);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[1][0], k_agents<kKSmall, false, true>, th, ds);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_hs[0], k_agents<kKSmall, false, true, 0>, th, d0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_hs[1], k_agents<kKSmall, false, true, 1>, th, d1);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks[1][1], k_agents<kKMax, true, true>, th, db);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_hsmall, k_agents<kKSmall, false, true, true>, th, dh);
+    g_blocks[1][0] = g_blocks_hs[0];
     for (auto& row : g_blocks)
         for (int& b : row)
             if (b < 1) b = 1;
-    if (g_blocks_hsmall < 1) g_blocks_hsmall = 1;
+    for (int& b : g_blocks_hs)
+        if (b < 1) b = 1;
     return e;
 }
 
 // Warps of the agent kernels that can be resident at once (the rows of the global anchor table).
 int64_t agent_warp_slots(int num_sms) {
-    int mb = g_blocks_hsmall;
+    int mb = 1;
+    for (int b : g_blocks_hs) mb = b > mb ? b : mb;
     for (auto& row : g_blocks)
         for (int b : row) mb = b > mb ? b : mb;
     const int64_t sep = (int64_t)num_sms * mb * kAgentWarps;
@@ -763,14 +768,15 @@ int64_t agent_warp_slots(int num_sms) {
 }
 
 int agent_occupancy(int thin, int small_hash) {
-    return thin ? (small_hash ? g_blocks_hsmall : g_blocks[1][0]) : g_blocks[0][0];
+    if (!thin) return g_blocks[0][0];
+    return g_blocks_hs[small_hash == 1 ? 1 : 0];
 }
 
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) {
     if (agents <= 0) return;
     const int t = A.sampler == kSamplerThinning ? 1 : 0;
-    const bool hs = t && A.tune_small_hash;
-    int per_sm = t ? (hs ? g_blocks_hsmall : g_blocks[1][0]) : g_blocks[0][0];
+    const int hs = t && A.tune_small_hash == 1 ? 1 : 0;
+    int per_sm = agent_occupancy(t, hs);
     if (A.tune_agent_ctas > 0 && A.tune_agent_ctas < per_sm) per_sm = A.tune_agent_ctas;
     int64_t need = (agents + kAgentWarps - 1) / kAgentWarps;
     int64_t grid = (int64_t)num_sms * per_sm;
@@ -778,11 +784,11 @@ void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s) 
     const unsigned gbig = (unsigned)num_sms * g_blocks[t][1];
     const int th = kAgentWarps * 32;
     if (t) {
-        if (hs)
-            k_agents<kKSmall, false, true, true><<<(unsigned)grid, th, thin_smem_bytes<kKSmall, true>(), s>>>(A, agents);
+        if (hs == 1)
+            k_agents<kKSmall, false, true, 1><<<(unsigned)grid, th, thin_smem_bytes<kKSmall, 1>(), s>>>(A, agents);
         else
-            k_agents<kKSmall, false, true><<<(unsigned)grid, th, thin_smem_bytes<kKSmall, false>(), s>>>(A, agents);
-        k_agents<kKMax, true, true><<<gbig, th, thin_smem_bytes<kKMax, false>(), s>>>(A, agents);
+            k_agents<kKSmall, false, true, 0><<<(unsigned)grid, th, thin_smem_bytes<kKSmall, 0>(), s>>>(A, agents);
+        k_agents<kKMax, true, true><<<gbig, th, thin_smem_bytes<kKMax, 0>(), s>>>(A, agents);
     } else {
         k_agents<kKSmall, false, false><<<(unsigned)grid, th, 0, s>>>(A, agents);
         k_agents<kKMax, true, false><<<gbig, th, 0, s>>>(A, agents);
@@ -830,10 +836,8 @@ __device__ __forceinline__ void grid_sync(const Arena& A) {
 // per-warp shared memory of the agent phase: the larger of the two thinning variants it runs (the
 // k <= 64 one with the 1024-slot frontier and 1024-entry stages)
 constexpr size_t kEpochWarpSmem =
-    sizeof(ThinSmem<kKSmall, kZCap, ThinStage<kKSmall, true>::value>) >
-            sizeof(ThinSmem<kKMax, kZCap, ThinStage<kKMax, false>::value>)
-        ? sizeof(ThinSmem<kKSmall, kZCap, ThinStage<kKSmall, true>::value>)
-        : sizeof(ThinSmem<kKMax, kZCap, ThinStage<kKMax, false>::value>);
+    thin_smem_bytes<kKSmall, 1>() > thin_smem_bytes<kKMax, 0>() ? thin_smem_bytes<kKSmall, 1>() / kAgentWarps
+                                                                  : thin_smem_bytes<kKMax, 0>() / kAgentWarps;
 constexpr size_t kEpochSmem = kEpochWarps * kEpochWarpSmem;
 
 __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epoch, int64_t agents, int G) {
@@ -899,7 +903,7 @@ __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epo
     grid_sync(A);
     // the agents: k <= 256 queue, then the k <= 64 queue (heavy list first)
     d_agents<kKMax, true, true>(A, agents, ep_dsm, kEpochWarpSmem);
-    d_agents<kKSmall, false, true, true>(A, agents, ep_dsm, kEpochWarpSmem);
+    d_agents<kKSmall, false, true, 1>(A, agents, ep_dsm, kEpochWarpSmem);
     grid_sync(A);
     // backward append: the cited rows' new lengths, new spans for the rows that outgrew theirs
     d_bwd_grow(A, agents);

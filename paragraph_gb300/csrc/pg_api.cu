@@ -73,7 +73,7 @@ struct Checkpoint {
     int64_t epoch = 0;
     std::vector<HostRep> hrep;
     std::vector<int64_t> b_top;  // backward entries in use per replica
-    DBuf<int32_t> pub, indeg, fwd_col, bcol, rc_lag, rc_dur;
+    DBuf<int32_t> pub, indeg, fwd_col, bcol, bcap, rc_lag, rc_dur;
     DBuf<float> fit;
     DBuf<int64_t> fwd_off;
     DBuf<BRow> brow;
@@ -110,7 +110,7 @@ struct pg_ctx {
     DBuf<uint64_t> cdf, tilesum, tileoff, tables;
     DBuf<int32_t> guide;
     DBuf<int64_t> fwd_off, len_tmp, sort_small, sort_large, sort_large_off, eoff, blocksum, er_cnt, er_toff;
-    DBuf<int32_t> fwd_col, bcol;
+    DBuf<int32_t> fwd_col, bcol, bcap;
     DBuf<BRow> brow;
     DBuf<longlong2> reloc;  // copy tasks of the backward rows that move in an epoch
     DBuf<int32_t> src_tmp;  // sources of an edge range being copied out
@@ -210,6 +210,7 @@ Arena make_arena(pg_ctx* c) {
     A.fwd_off = c->fwd_off.p;
     A.fwd_col = c->fwd_col.p;
     A.brow = c->brow.p;
+    A.bcap = c->bcap.p;
     A.bcol = c->bcol.p;
     A.reloc = c->reloc.p;
     A.reloc_cap = c->reloc.n;
@@ -383,6 +384,7 @@ void free_checkpoint(Checkpoint& k) {
     dfree(k.fit);
     dfree(k.fwd_off);
     dfree(k.brow);
+    dfree(k.bcap);
     dfree(k.rep);
     dfree(k.rc_lag);
     dfree(k.rc_dur);
@@ -485,6 +487,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         h.bbase = B;
         h.b_cap = bregion_entries(h.n_cap, h.m_cap);
         B += h.b_cap;
+        if (h.b_cap > kBRegionMax) return fail(c, PG_ERR_CAPACITY, "replica too large for the backward region");
     }
     // a single replica's raw edges are uploaded and checked before the arena is touched (a bad
     // edge list leaves the loaded graph intact); the build below reuses the upload
@@ -546,6 +549,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->fwd_off, S + R));
     PG_CUDA(c, dalloc(c->fwd_col, M));
     PG_CUDA(c, dalloc(c->brow, S));
+    PG_CUDA(c, dalloc(c->bcap, S));
     PG_CUDA(c, dalloc(c->bcol, B));
     PG_CUDA(c, dalloc(c->tables, (int64_t)R * kTableEntries));
     PG_CUDA(c, dalloc(c->hslot, S));
@@ -584,6 +588,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, cudaMemsetAsync(c->w.p, 0, sizeof(float) * (size_t)S, c->stream));
     // empty rows everywhere: slots of nodes not yet born hold {0, 0, 0} until their first citation
     PG_CUDA(c, cudaMemsetAsync(c->brow.p, 0, sizeof(BRow) * (size_t)S, c->stream));
+    PG_CUDA(c, cudaMemsetAsync(c->bcap.p, 0, sizeof(int32_t) * (size_t)S, c->stream));
     std::vector<int32_t> trep((size_t)T);
     std::vector<Replica> drep((size_t)R);
     std::vector<uint64_t> tabs((size_t)R * kTableEntries);
@@ -682,7 +687,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         int64_t laid = 0;
         if (n) {
             launch_brow_layout(t_bo.p, t_bc.p, (int64_t)n, h.m, t_caps.p, t_begs.p, t_bsum.p, c->brow.p + h.nbase,
-                               c->bcol.p + h.bbase, c->stream);
+                               c->bcap.p + h.nbase, c->bcol.p + h.bbase, c->stream);
             PG_CUDA(c, cudaGetLastError());
             PG_CUDA(c, cudaMemcpyAsync(&laid, t_begs.p + n, 8, cudaMemcpyDeviceToHost, c->stream));
             PG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -733,10 +738,10 @@ pg_status backward_offset_form(pg_ctx* c, int r, int64_t* off, int32_t* col) {
     int64_t o = 0;
     for (size_t v = 0; v < n; ++v) {
         const BRow& w = rows[v];
-        if (w.len < 0 || w.beg < 0 || w.beg + w.len > top || o + w.len > h.m)
-            return fail(c, PG_ERR_STATE, "backward row out of range");
+        const int64_t beg = (int64_t)w.beg4 << 2;
+        if (w.len < 0 || beg + w.len > top || o + w.len > h.m) return fail(c, PG_ERR_STATE, "backward row out of range");
         if (off) off[v] = o;
-        if (col && w.len) std::memcpy(col + o, reg.data() + w.beg, 4 * (size_t)w.len);
+        if (col && w.len) std::memcpy(col + o, reg.data() + beg, 4 * (size_t)w.len);
         o += w.len;
     }
     if (off) off[n] = o;
@@ -1101,7 +1106,7 @@ void pg_destroy(pg_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     destroy_graph_exec(c);
     DBuf<int32_t>* i32[] = {&c->tile_rep, &c->pub, &c->indeg, &c->inc, &c->kk, &c->big_list, &c->heavy_list, &c->heavy_mark,
-                            &c->e_dst, &c->e_rank, &c->arrivals, &c->anchors, &c->fwd_col, &c->bcol};
+                            &c->e_dst, &c->e_rank, &c->arrivals, &c->anchors, &c->fwd_col, &c->bcol, &c->bcap};
     for (auto* b : i32) dfree(*b);
     dfree(c->brow);
     dfree(c->reloc);
@@ -1728,6 +1733,7 @@ pg_status pg_checkpoint(pg_ctx* c) {
         PG_CUDA(c, dalloc(k.fit, c->S));
         PG_CUDA(c, dalloc(k.fwd_off, c->S + c->R));
         PG_CUDA(c, dalloc(k.brow, c->S));
+        PG_CUDA(c, dalloc(k.bcap, c->S));
         PG_CUDA(c, dalloc(k.rep, c->R));
     }
     if (k.fwd_col.n != c->M) PG_CUDA(c, dalloc(k.fwd_col, c->M));
@@ -1756,6 +1762,7 @@ pg_status pg_checkpoint(pg_ctx* c) {
     PG_CUDA(c, cudaMemcpyAsync(k.fit.p, c->fit.p, 4 * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(k.fwd_off.p, c->fwd_off.p, 8 * (size_t)(c->S + c->R), d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(k.brow.p, c->brow.p, sizeof(BRow) * (size_t)c->S, d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(k.bcap.p, c->bcap.p, sizeof(int32_t) * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(k.rep.p, c->rep.p, sizeof(Replica) * (size_t)c->R, d2d, s));
     for (int r = 0; r < c->R; ++r) {
         const HostRep& h = c->hrep[(size_t)r];
@@ -1786,6 +1793,7 @@ pg_status pg_restore(pg_ctx* c) {
     PG_CUDA(c, cudaMemcpyAsync(c->fit.p, k.fit.p, 4 * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(c->fwd_off.p, k.fwd_off.p, 8 * (size_t)(c->S + c->R), d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(c->brow.p, k.brow.p, sizeof(BRow) * (size_t)c->S, d2d, s));
+    PG_CUDA(c, cudaMemcpyAsync(c->bcap.p, k.bcap.p, sizeof(int32_t) * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(c->rep.p, k.rep.p, sizeof(Replica) * (size_t)c->R, d2d, s));
     for (size_t r = 0; r < k.hrep.size(); ++r) {
         const HostRep& h = k.hrep[r];

@@ -246,14 +246,15 @@ __global__ void __launch_bounds__(256) k_brow_caps(const int64_t* bo, int64_t n,
     }
 }
 
-__global__ void __launch_bounds__(256) k_brow_rows(const int64_t* bo, const int64_t* begs, int64_t n, BRow* brow) {
+__global__ void __launch_bounds__(256) k_brow_rows(const int64_t* bo, const int64_t* begs, int64_t n, BRow* brow,
+                                                   int32_t* bcap) {
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
         const int64_t len = bo[v + 1] - bo[v];
         BRow r;
-        r.beg = len > 0 ? begs[v] : 0;
+        r.beg4 = len > 0 ? (uint32_t)(begs[v] >> 2) : 0u;
         r.len = (int32_t)len;
-        r.cap = (int32_t)(len > 0 ? begs[v + 1] - begs[v] : 0);
         brow[v] = r;
+        bcap[v] = (int32_t)(len > 0 ? begs[v + 1] - begs[v] : 0);
     }
 }
 
@@ -274,12 +275,12 @@ __global__ void __launch_bounds__(256) k_brow_cols(const int64_t* bo, const int3
 }
 
 void launch_brow_layout(const int64_t* bo, const int32_t* bc, int64_t n, int64_t m, int64_t* caps,
-                        int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcol, cudaStream_t s) {
+                        int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcap, int32_t* bcol, cudaStream_t s) {
     if (n <= 0) return;
     const unsigned gn = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
     k_brow_caps<<<gn, 256, 0, s>>>(bo, n, caps);
     launch_scan_i64(caps, begs, n, blocksum, s);
-    k_brow_rows<<<gn, 256, 0, s>>>(bo, begs, n, brow);
+    k_brow_rows<<<gn, 256, 0, s>>>(bo, begs, n, brow, bcap);
     if (m > 0) {
         const unsigned gm = (unsigned)std::min<int64_t>((m + 255) / 256, 152 * 16);
         k_brow_cols<<<gm, 256, 0, s>>>(bo, bc, begs, n, m, bcol);

@@ -8,7 +8,7 @@
 // Forward rows of new nodes were written by the agent kernel (append-only, sorted).  Backward rows
 // grow in place (BRow: room for cap entries, len used), so an epoch touches only the rows it
 // appends to:
-//   grow : one warp per agent; each cited node is handled once, by its edge of rank 0 (the agent
+//   grow : one thread per edge; each cited node is handled once, by its edge of rank 0 (the agent
 //          kernel's in-degree increment returned each edge's rank among the node's new entries):
 //          new length = old + inc; a row without room for it takes a new span of brow_cap(new)
 //          entries from the region's bump pointer (one reservation per warp step) and lists its old
@@ -28,78 +28,102 @@ namespace pg {
 
 constexpr unsigned kFullMask = 0xffffffffu;
 
+// Replica of epoch edge e: the last replica whose edges start at or before e.
+__device__ __forceinline__ int replica_of_edge(const Arena& A, int64_t e) {
+    int lo = 0, hi = A.R - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.eoff[A.rep[mid].abase] <= e)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// One thread per epoch edge, 32 consecutive edges per warp step; the edge of rank 0 handles its row.
 __device__ __forceinline__ void d_bwd_grow(const Arena& A, int64_t agents) {
     if (A.st->error) return;
     const int lane = lane_id();
+    const unsigned below = (1u << lane) - 1u;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t E = A.eoff[agents];
     unsigned long long moved = 0;
-    for (int64_t a = warp; a < agents; a += nwarps) {
-        const int r = replica_of_agent(A.rep, A.R, a);
+    for (int64_t eb = warp * 32; eb < E; eb += nwarps * 32) {
+        const int64_t e = eb + lane;
+        const int r = A.R == 1 ? 0 : replica_of_edge(A, e < E ? e : E - 1);
         Replica& rp = A.rep[r];
-        const int64_t e0 = A.eoff[a], e1 = A.eoff[a + 1];
-        for (int64_t eb = e0; eb < e1; eb += 32) {
-            const int64_t e = eb + lane;
-            bool mine = e < e1 && A.e_rank[e] == 0;
-            int64_t slot = 0, nl = 0, need = 0;
-            int ic = 0;
-            BRow rw{0, 0, 0};
-            if (mine) {
-                slot = rp.nbase + A.e_dst[e];
-                ic = A.inc[slot];
-                rw = A.brow[slot];
-                nl = (int64_t)rw.len + ic;
-                if (nl > rw.cap) need = brow_cap(nl);
+        bool mine = e < E && A.e_rank[e] == 0;
+        int64_t slot = 0, nl = 0, need = 0, nch = 0;
+        int ic = 0;
+        BRow rw{0u, 0};
+        if (mine) {
+            slot = rp.nbase + A.e_dst[e];
+            ic = A.inc[slot];
+            rw = A.brow[slot];
+            nl = (int64_t)rw.len + ic;
+            if (nl > A.bcap[slot]) {
+                need = brow_cap(nl);
+                nch = (rw.len + kRelocChunk - 1) / kRelocChunk;
             }
-            // one reservation of the region's bump pointer for the warp's moving rows
-            const int64_t incl = warp_incl_scan<int64_t>(need);
-            const int64_t tot = __shfl_sync(kFullMask, incl, 31);
-            int64_t base = 0;
-            if (tot) {
-                if (lane == 31) base = (int64_t)atomicAdd(&rp.b_top, (unsigned long long)tot);
-                base = __shfl_sync(kFullMask, base, 31);
-                if (base + tot > rp.b_cap) {  // the region is sized so that this cannot happen
-                    if (lane == 0) atomicOr(&A.st->error, kErrCapacity);
-                    mine = false;
-                }
+        }
+        // the step's reservations, one atomic each where the warp lies in one replica: region
+        // spans, copy tasks, sort-list entries and large-sort scratch
+        const bool uni = __all_sync(kFullMask, r == __shfl_sync(kFullMask, r, 0));
+        const int64_t incl = warp_incl_scan<int64_t>(need);
+        const int64_t tot = __shfl_sync(kFullMask, incl, 31);
+        const int64_t cincl = warp_incl_scan<int64_t>(nch);
+        const int64_t ctot = __shfl_sync(kFullMask, cincl, 31);
+        const bool small = mine && ic >= 2 && ic <= kSortMid, large = mine && ic > kSortMid;
+        const unsigned bs = __ballot_sync(kFullMask, small), bl = __ballot_sync(kFullMask, large);
+        const int64_t sincl = warp_incl_scan<int64_t>(large ? ic : 0);
+        const int64_t stot = __shfl_sync(kFullMask, sincl, 31);
+        int64_t base = 0, cbase = 0, sbase = 0, lbase = 0, scbase = 0;
+        if (lane == 0) {
+            if (uni && tot) base = (int64_t)atomicAdd(&rp.b_top, (unsigned long long)tot);
+            if (ctot) cbase = (int64_t)atomicAdd(&A.st->reloc_count, (unsigned long long)ctot);
+            if (bs) sbase = (int64_t)atomicAdd(&A.st->sort_small_count, (unsigned long long)__popc(bs));
+            if (bl) {
+                lbase = (int64_t)atomicAdd(&A.st->sort_large_count, (unsigned long long)__popc(bl));
+                scbase = (int64_t)atomicAdd(&A.st->sort_scratch, (unsigned long long)stot);
             }
-            if (!mine) continue;
-            const int64_t old = rw.len;
-            if (need) {
-                const int64_t nb = base + incl - need;
-                if (old > 0) {
-                    const int64_t nch = (old + kRelocChunk - 1) / kRelocChunk;
-                    const int64_t q = (int64_t)atomicAdd(&A.st->reloc_count, (unsigned long long)nch);
-                    if (q + nch > A.reloc_cap) {
-                        atomicOr(&A.st->error, kErrCapacity);
-                        continue;
-                    }
-                    for (int64_t c = 0; c < nch; ++c) {
-                        const int64_t off = c * kRelocChunk;
-                        const int64_t len = old - off < kRelocChunk ? old - off : kRelocChunk;
-                        A.reloc[q + c] = make_longlong2(rp.bbase + rw.beg + off, ((rp.bbase + nb + off) << 16) | len);
-                    }
-                    moved += (unsigned long long)old;
-                }
-                rw.beg = nb;
-                rw.cap = (int32_t)need;
+        }
+        base = __shfl_sync(kFullMask, base, 0);
+        cbase = __shfl_sync(kFullMask, cbase, 0);
+        sbase = __shfl_sync(kFullMask, sbase, 0);
+        lbase = __shfl_sync(kFullMask, lbase, 0);
+        scbase = __shfl_sync(kFullMask, scbase, 0);
+        int64_t nb = base + incl - need;
+        if (!uni && need) nb = (int64_t)atomicAdd(&rp.b_top, (unsigned long long)need);
+        // the region and the task list are sized so that neither can run out
+        const bool room = (uni ? base + tot : (need ? nb + need : 0)) <= rp.b_cap && cbase + ctot <= A.reloc_cap;
+        if (!room) atomicOr(&A.st->error, kErrCapacity);
+        if (!mine || !room) continue;
+        const int64_t old = rw.len;
+        int64_t beg = (int64_t)rw.beg4 << 2;
+        if (need) {
+            const int64_t q = cbase + cincl - nch;
+            for (int64_t c = 0; c < nch; ++c) {
+                const int64_t off = c * kRelocChunk;
+                const int64_t len = old - off < kRelocChunk ? old - off : kRelocChunk;
+                A.reloc[q + c] = make_longlong2(rp.bbase + beg + off, ((rp.bbase + nb + off) << 16) | len);
             }
-            A.len_tmp[slot] = rw.beg + old;
-            rw.len = (int32_t)nl;
-            A.brow[slot] = rw;
-            A.indeg[slot] += ic;
-            A.inc[slot] = 0;
-            if (ic >= 2) {
-                if (ic <= kSortMid) {
-                    const unsigned long long q = atomicAdd(&A.st->sort_small_count, 1ull);
-                    A.sort_small[q] = (slot << 9) | (int64_t)ic;
-                } else {
-                    const unsigned long long q = atomicAdd(&A.st->sort_large_count, 1ull);
-                    A.sort_large[q] = slot;
-                    A.sort_large_off[q] = ((int64_t)atomicAdd(&A.st->sort_scratch, (unsigned long long)ic) << 32) |
-                                          (int64_t)ic;
-                }
-            }
+            moved += (unsigned long long)old;
+            beg = nb;
+            rw.beg4 = (uint32_t)(nb >> 2);
+            A.bcap[slot] = (int32_t)need;
+        }
+        A.len_tmp[slot] = beg + old;
+        rw.len = (int32_t)nl;
+        A.brow[slot] = rw;
+        A.indeg[slot] += ic;
+        A.inc[slot] = 0;
+        if (small) A.sort_small[sbase + __popc(bs & below)] = (slot << 9) | (int64_t)ic;
+        if (large) {
+            const int64_t q = lbase + __popc(bl & below);
+            A.sort_large[q] = slot;
+            A.sort_large_off[q] = ((scbase + sincl - ic) << 32) | (int64_t)ic;
         }
     }
     moved = warp_sum(moved);
@@ -171,7 +195,7 @@ __device__ __forceinline__ void seg_bounds(const Arena& A, int64_t slot, int64_t
     const Replica& rp = A.rep[r];
     rpp = &rp;
     const BRow rw = A.brow[slot];
-    start = rp.bbase + rw.beg + rw.len - added;
+    start = rp.bbase + ((int64_t)rw.beg4 << 2) + rw.len - added;
 }
 
 template <int R>

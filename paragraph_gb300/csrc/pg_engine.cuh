@@ -6,9 +6,10 @@
 //   forward offsets (fwd_off) hold n_cap_r + 1 int64 entries at obase_r = nbase_r + r and are LOCAL
 //   to the replica's edge region; forward columns (fwd_col) hold replica-local int32 node ids at
 //   ebase_r + offset (rows appended in node order, never moved);
-//   backward rows (brow, one 16-byte BRow per node slot) point into the replica's backward region
-//   (bcol at bbase_r, b_cap_r entries): a row has room for `cap` entries and holds `len` at `beg`,
-//   and grows in place until full, when it moves to twice its length at the region's bump pointer.
+//   backward rows (brow, one 8-byte BRow per node slot, and bcap, the room of each) point into the
+//   replica's backward region (bcol at bbase_r, b_cap_r entries): a row holds `len` entries from
+//   its 16-byte-aligned start and grows in place until its room is full, when it moves to twice
+//   its length at the region's bump pointer.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -56,13 +57,14 @@ enum : uint32_t {
     kErrTimeout = 8u,  // a bounded wait on an asynchronous copy ran out
 };
 
-// Backward row of a node: entries bcol[bbase + beg, bbase + beg + len), room for cap entries.  beg
-// and cap are multiples of 4, so a row starts on a 16-byte boundary; an empty row has cap 0.
-struct __align__(16) BRow {
-    long long beg;
+// Backward row of a node: entries bcol[bbase + 4 beg4, bbase + 4 beg4 + len), so every row starts on
+// a 16-byte boundary; its room (a multiple of 4 entries, 0 for an empty row) is kept apart in bcap,
+// which only the append reads, so the record the samplers load per node is 8 bytes.
+struct __align__(8) BRow {
+    uint32_t beg4;
     int32_t len;
-    int32_t cap;
 };
+constexpr int64_t kBRegionMax = (int64_t)1 << 34;  // entries a backward region may span (beg4 is 32-bit)
 
 // Room given to a backward row that must hold L >= 1 entries: 2L rounded up to a multiple of 4.  A
 // row that outgrows its room moves, so its earlier spans c_0 < c_1 < ... < c_k satisfy
@@ -165,6 +167,7 @@ struct Arena {
     int64_t* fwd_off;
     int32_t* fwd_col;
     BRow* brow;                // [slots] backward row of each node
+    int32_t* bcap;             // [slots] room of each backward row (entries)
     int32_t* bcol;             // backward regions of all replicas
     const uint64_t* tables;    // [R][kTableEntries]
     // per-epoch buffers
@@ -254,11 +257,11 @@ PG_HD int guide_shift(uint64_t Wq, int64_t n) {
 #if defined(__CUDACC__)
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
-// Bounds [b, e) of backward row x (one 16-byte load), relative to the replica's region.
+// Bounds [b, e) of backward row x (one 8-byte load), relative to the replica's region.
 __device__ __forceinline__ void bspan(const BRow* br, int64_t x, int64_t& b, int64_t& e) {
-    const longlong2 q = *reinterpret_cast<const longlong2*>(br + x);
-    b = q.x;
-    e = q.x + (int64_t)(int32_t)(uint32_t)(unsigned long long)q.y;
+    const uint2 q = *reinterpret_cast<const uint2*>(br + x);
+    b = (int64_t)q.x << 2;
+    e = b + (int64_t)(int32_t)q.y;
 }
 __device__ __forceinline__ int64_t blen(const BRow* br, int64_t x) { return br[x].len; }
 
@@ -452,7 +455,7 @@ void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t
 // = entries laid out), blocksum scan_blocks_needed(n) + 2 entries of scratch; brow/bcol: the
 // replica's rows and region
 void launch_brow_layout(const int64_t* bo, const int32_t* bc, int64_t n, int64_t m, int64_t* caps,
-                        int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcol, cudaStream_t s);
+                        int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcap, int32_t* bcol, cudaStream_t s);
 // resident CTAs per SM of the k <= 64 agent kernel (after init_agent_kernels)
 int agent_occupancy(int thin, int small_hash);
 int64_t agent_warp_slots(int num_sms);
