@@ -420,6 +420,7 @@ def ensemble_measure(args, world, rank, local, dist, with_cpu: bool = True) -> d
     eng.load_replicas(reps)
     tuned, tune_ms = eng.autotune(ENS_EPOCHS)
     eng.checkpoint()
+    m_seed = [eng.counts(r)[1] for r in range(len(reps))]
 
     def step():
         eng.restore()
@@ -427,6 +428,7 @@ def ensemble_measure(args, world, rank, local, dist, with_cpu: bool = True) -> d
 
     for _ in range(args.warmup):
         step()
+    new_edges = [eng.counts(r)[1] - m_seed[r] for r in range(len(reps))]
     barrier(dist)
     edges, dev_ms, wall = 0, 0.0, 0.0
     launches = 0
@@ -488,18 +490,34 @@ def ensemble_measure(args, world, rank, local, dist, with_cpu: bool = True) -> d
     # end to end: host inputs -> load -> 10 epochs -> every new citation back on the host
     e2e = None
     if not args.no_e2e:
+        import dataclasses
+
+        import torch
+
+        # page-locked host buffers, filled before the timed region (as in the PA line): the
+        # replicas' raw inputs in, every new citation (source, target) out, each replica's at its
+        # own offset
+        def pinned(a):
+            return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+        preps = [dataclasses.replace(r, pub_epoch=pinned(r.pub_epoch), fitness=pinned(r.fitness),
+                                     src=pinned(r.src), dst=pinned(r.dst)) for r in reps]
+        ofs = np.concatenate([[0], np.cumsum(new_edges)])
+        out_s = torch.empty(int(ofs[-1]) + 1, dtype=torch.int32).pin_memory().numpy()
+        out_d = torch.empty(int(ofs[-1]) + 1, dtype=torch.int32).pin_memory().numpy()
         t0 = time.perf_counter()
         h2d = d2h = 0
         with GrowthEngine(seed=args.seed, replicas=len(reps), device=local) as e2:
             e2.set_tuning(**tuned)
-            e2.load_replicas(reps)
+            e2.load_replicas(preps)
             m0 = [e2.counts(r) for r in range(len(reps))]
             ne = e2.run_epochs(ENS_EPOCHS, use_graph=True)
             for r in range(len(reps)):
                 n0_, mm0 = m0[r]
                 n1, m1 = e2.counts(r)
-                e2.edges(mm0, m1 - mm0, r)
-                h2d += 4 * n0_ * 3 + 8 * (n0_ + 1) * 2 + 4 * mm0 * 2
+                o = int(ofs[r])
+                e2.edges(mm0, m1 - mm0, r, out=(out_s[o:o + m1 - mm0], out_d[o:o + m1 - mm0]))
+                h2d += 4 * n0_ * 2 + 4 * len(reps[r].src) * 2  # publication epochs, fitness, raw edges
                 d2h += 8 * (m1 - mm0)  # sources (expanded on the device) and targets
         dt = reduce_max(dist, time.perf_counter() - t0)
         e2e = {"value": reduce_sum(dist, float(len(reps))) / dt, "unit": "evals/s",

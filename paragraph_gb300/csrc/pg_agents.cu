@@ -861,18 +861,20 @@ __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epo
         __syncthreads();
     }
     grid_sync(A);
-    // hubs; tile offsets of the CDF (on the last CTA, so CTA 0 is not the only one with extra work)
+    // hubs leaving and joining; tile offsets of the CDF (on the last CTA, so CTA 0 is not the only
+    // one with extra work)
     for (int t = blockIdx.x; t < T; t += gridDim.x) d_hub_collect(A, t);
     if (blockIdx.x == gridDim.x - 1) d_tile_scan(A, 0);
     grid_sync(A);
-    // hub masks; CDF offsets and guide marks
-    for (int i = blockIdx.x; i < hub_items; i += gridDim.x) d_hub_mask(A, G, i);
+    // hub bits; CDF offsets and guide marks
+    if (blockIdx.x == 0) d_hub_assign(A);
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
         d_cdf_add(A, t);
         __syncthreads();
     }
     grid_sync(A);
-    // guide table; per-agent out-degrees, new nodes, heavy lists
+    // bits cleared by the hubs that left; guide table; per-agent out-degrees, new nodes, heavy lists
+    for (int i = blockIdx.x; i < hub_items; i += gridDim.x) d_hub_mask<false>(A, G, i);
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
         d_guide_fill(A, t);
         __syncthreads();
@@ -880,7 +882,9 @@ __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epo
     const int setup_blocks = (int)((agents + 255) / 256);
     for (int b = blockIdx.x; b < setup_blocks; b += gridDim.x) d_agent_setup(A, agents, b);
     grid_sync(A);
-    // edge offsets: exclusive scan of the out-degrees (reduce, block sums, apply)
+    // bits set by the hubs that joined; edge offsets: exclusive scan of the out-degrees (reduce,
+    // block sums, apply)
+    for (int i = blockIdx.x; i < hub_items; i += gridDim.x) d_hub_mask<true>(A, G, i);
     const int nb = (int)((agents + kScanBlock - 1) / kScanBlock);
     for (int b = blockIdx.x; b < nb; b += gridDim.x) {
         d_scan_reduce<int32_t>(A.kk, agents, A.blocksum, b);

@@ -100,7 +100,8 @@ struct pg_ctx {
     // device buffers
     DBuf<Replica> rep;
     DBuf<EpochState> st;
-    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, heavy_list, heavy_mark, e_dst, e_rank, arrivals, hlist, anchors;
+    DBuf<int32_t> tile_rep, pub, indeg, inc, kk, big_list, heavy_list, heavy_mark, e_dst, e_rank, arrivals, hlist, anchors,
+        hub_rem, hub_add, hub_cand;
     DBuf<int16_t> hslot;
     DBuf<uint64_t> hub2;
     DBuf<uint32_t> hub_need;
@@ -242,6 +243,9 @@ Arena make_arena(pg_ctx* c) {
     A.hub_need = c->hub_need.p;
     A.zbig = c->zbig.p;
     A.hlist = c->hlist.p;
+    A.hub_rem = c->hub_rem.p;
+    A.hub_add = c->hub_add.p;
+    A.hub_cand = c->hub_cand.p;
     A.sampler = c->cfg.sampler;
     A.tune_agent_ctas = c->tune.agent_ctas_per_sm;
     A.tune_small_hash = c->tune.small_hash;
@@ -318,28 +322,6 @@ pg_status check_params(pg_ctx* c, const pg_pa_params& p) {
 }
 
 // Index of the first edge with an endpoint outside [0, n), or -1; chunks on all host threads.
-int64_t first_bad_edge(const int32_t* src, const int32_t* dst, int64_t m, int64_t n) {
-    if (m <= 0) return -1;
-    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::thread::hardware_concurrency(),
-                                                               (m + (1 << 20) - 1) >> 20));
-    std::vector<int64_t> first((size_t)nt, -1);
-    auto work = [&](int t) {
-        const int64_t a = m * t / nt, b = m * (t + 1) / nt;
-        for (int64_t e = a; e < b; ++e)
-            if (src[e] < 0 || src[e] >= n || dst[e] < 0 || dst[e] >= n) {
-                first[(size_t)t] = e;
-                return;
-            }
-    };
-    std::vector<std::thread> pool;
-    for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
-    work(0);
-    for (auto& th : pool) th.join();
-    for (int64_t f : first)
-        if (f >= 0) return f;
-    return -1;
-}
-
 // Sorted, duplicate-free CSR from an edge list (Graph::AddEdge set semantics).
 void host_csr(int64_t n, int64_t m, const int32_t* src, const int32_t* dst,
               std::vector<int64_t>& off, std::vector<int32_t>& col) {
@@ -489,41 +471,49 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         B += h.b_cap;
         if (h.b_cap > kBRegionMax) return fail(c, PG_ERR_CAPACITY, "replica too large for the backward region");
     }
-    // a single replica's raw edges are uploaded and checked before the arena is touched (a bad
-    // edge list leaves the loaded graph intact); the build below reuses the upload
+    // every replica's raw edges are uploaded (each at its offset in one staging buffer) and checked
+    // on the device before the arena is touched, so a bad edge list leaves the loaded graph intact;
+    // the builds below read the staged edges
     DBuf<int32_t> raw_src, raw_dst;
-    bool raw_up = false;
-    if (raw && R == 1 && raw[0].num_edges > 0) {
-        const pg_replica_desc& d = raw[0];
+    std::vector<int64_t> raw_off((size_t)R + 1, 0);
+    if (raw) {
+        for (int r = 0; r < R; ++r) raw_off[(size_t)r + 1] = raw_off[(size_t)r] + std::max<int64_t>(raw[r].num_edges, 0);
+        const int64_t tot = raw_off[(size_t)R];
         DBuf<unsigned long long> first;
         auto drop = [&]() {
             dfree(raw_src);
             dfree(raw_dst);
             dfree(first);
         };
-        cudaError_t e = dalloc(raw_src, d.num_edges);
-        if (e == cudaSuccess) e = dalloc(raw_dst, d.num_edges);
-        if (e == cudaSuccess) e = dalloc(first, 1);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(raw_src.p, d.src, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(raw_dst.p, d.dst, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream);
-        unsigned long long bad = ~0ull;
-        if (e == cudaSuccess) {
-            launch_first_bad_edge(raw_src.p, raw_dst.p, d.num_edges, d.num_nodes, first.p, c->stream);
-            e = cudaMemcpyAsync(&bad, first.p, sizeof(bad), cudaMemcpyDeviceToHost, c->stream);
+        cudaError_t e = dalloc(raw_src, std::max<int64_t>(tot, 1));
+        if (e == cudaSuccess) e = dalloc(raw_dst, std::max<int64_t>(tot, 1));
+        if (e == cudaSuccess) e = dalloc(first, R);
+        for (int r = 0; r < R && e == cudaSuccess; ++r) {
+            const pg_replica_desc& d = raw[r];
+            const size_t o = (size_t)raw_off[(size_t)r];
+            if (d.num_edges > 0) {
+                e = cudaMemcpyAsync(raw_src.p + o, d.src, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(raw_dst.p + o, d.dst, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream);
+            }
+            if (e == cudaSuccess)
+                launch_first_bad_edge(raw_src.p + o, raw_dst.p + o, d.num_edges, d.num_nodes, first.p + r, c->stream);
         }
+        std::vector<unsigned long long> bad((size_t)R, ~0ull);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(bad.data(), first.p, sizeof(unsigned long long) * (size_t)R, cudaMemcpyDeviceToHost, c->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         dfree(first);
         if (e != cudaSuccess) {
             drop();
             return fail(c, PG_ERR_CUDA, std::string("edge upload: ") + cudaGetErrorString(e));
         }
-        if (bad != ~0ull) {
-            drop();
-            return fail(c, PG_ERR_ARG, "edge endpoint out of range at index " + std::to_string(bad));
-        }
-        raw_up = true;
+        for (int r = 0; r < R; ++r)
+            if (bad[(size_t)r] != ~0ull) {
+                drop();
+                return fail(c, PG_ERR_ARG, "edge endpoint out of range at index " + std::to_string(bad[(size_t)r]) +
+                                               (R > 1 ? " of replica " + std::to_string(r) : std::string()));
+            }
     }
     c->S = S;
     c->T = T;
@@ -557,6 +547,9 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->hub2, (int64_t)R * kHeavyMax * kMaskWords));
     PG_CUDA(c, dalloc(c->hub_need, (int64_t)R * (kHeavyMax / 32)));
     PG_CUDA(c, dalloc(c->hlist, (int64_t)R * kHeavyMax));
+    PG_CUDA(c, dalloc(c->hub_rem, (int64_t)R * kHeavyMax));
+    PG_CUDA(c, dalloc(c->hub_add, (int64_t)R * kHeavyMax));
+    PG_CUDA(c, dalloc(c->hub_cand, (int64_t)R * kHeavyMax));
     if (c->cfg.weight_model == PG_WEIGHTS_REFCOMPAT) {
         PG_CUDA(c, dalloc(c->rc_pa, S));
         if (!c->rc_big_id.p) {
@@ -594,9 +587,11 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     std::vector<uint64_t> tabs((size_t)R * kTableEntries);
     // scratch of the device CSR build: raw edges of one replica and the sort buffers; the
     // offset-form backward CSR each replica is built or uploaded in before its rows are laid out
+    // (every replica is enqueued without a host synchronisation: unique-edge counts, row-layout
+    // sizes and error words per replica stay on the device and are read back once at the end)
     DBuf<char> scratch;
     DBuf<uint32_t> berr;
-    DBuf<int64_t> t_bo, t_caps, t_begs, t_bsum;
+    DBuf<int64_t> t_bo, t_caps, t_begs, t_bsum, t_u, t_laid;
     DBuf<int32_t> t_bc;
     struct Temps {
         std::vector<std::function<void()>> f;
@@ -610,6 +605,8 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         dfree(t_begs);
         dfree(t_bsum);
         dfree(t_bc);
+        dfree(t_u);
+        dfree(t_laid);
     });
     {
         int64_t nn = 1, mm = 1;
@@ -622,6 +619,9 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         PG_CUDA(c, dalloc(t_begs, nn + 1));
         PG_CUDA(c, dalloc(t_bsum, scan_blocks_needed(nn + 1) + 2));
         PG_CUDA(c, dalloc(t_bc, mm));
+        PG_CUDA(c, dalloc(t_u, R));
+        PG_CUDA(c, dalloc(t_laid, R));
+        PG_CUDA(c, cudaMemsetAsync(t_laid.p, 0, 8 * (size_t)R, c->stream));
     }
     if (raw) {
         int64_t mm = 1, nn = 1;
@@ -630,12 +630,8 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             nn = std::max<int64_t>(nn, raw[r].num_nodes);
         }
         PG_CUDA(c, dalloc(scratch, (int64_t)build_scratch_bytes(mm, nn)));
-        if (!raw_up) {
-            PG_CUDA(c, dalloc(raw_src, mm));
-            PG_CUDA(c, dalloc(raw_dst, mm));
-        }
-        PG_CUDA(c, dalloc(berr, 1));
-        PG_CUDA(c, cudaMemsetAsync(berr.p, 0, 4, c->stream));
+        PG_CUDA(c, dalloc(berr, R));
+        PG_CUDA(c, cudaMemsetAsync(berr.p, 0, 4 * (size_t)R, c->stream));
     }
     for (int r = 0; r < R; ++r) {
         HostRep& h = reps[r];
@@ -658,20 +654,12 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             const pg_replica_desc& d = raw[r];
             PG_CUDA(c, cudaMemcpyAsync(c->pub.p + h.nbase, d.pub_epoch, 4 * n, cudaMemcpyHostToDevice, c->stream));
             PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase, d.fitness, 4 * n, cudaMemcpyHostToDevice, c->stream));
-            if (d.num_edges > 0 && !raw_up) {
-                PG_CUDA(c, cudaMemcpyAsync(raw_src.p, d.src, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream));
-                PG_CUDA(c, cudaMemcpyAsync(raw_dst.p, d.dst, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream));
-            }
-            int64_t u = 0;
             cudaGetLastError();
-            launch_build_csr(raw_src.p, raw_dst.p, d.num_edges, (int64_t)n, scratch.p, c->fwd_off.p + h.obase,
-                             c->fwd_col.p + h.ebase, t_bo.p, t_bc.p, c->indeg.p + h.nbase, &u, berr.p, c->stream);
+            const size_t o = (size_t)raw_off[(size_t)r];
+            launch_build_csr(raw_src.p + o, raw_dst.p + o, d.num_edges, (int64_t)n, scratch.p, c->fwd_off.p + h.obase,
+                             c->fwd_col.p + h.ebase, t_bo.p, t_bc.p, c->indeg.p + h.nbase, t_u.p + r, berr.p + r,
+                             c->stream);
             PG_CUDA(c, cudaGetLastError());
-            PG_CUDA(c, cudaStreamSynchronize(c->stream));
-            uint32_t be = 0;
-            PG_CUDA(c, cudaMemcpy(&be, berr.p, 4, cudaMemcpyDeviceToHost));
-            if (be) return fail(c, PG_ERR_ARG, "edge endpoint out of range in replica " + std::to_string(r));
-            h.m = u;
         } else {
             PG_CUDA(c, cudaMemcpyAsync(c->pub.p + h.nbase, g.pub.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
             PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase, g.fit.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
@@ -683,25 +671,43 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
                 PG_CUDA(c, cudaMemcpyAsync(t_bc.p, g.bc.data(), 4 * m, cudaMemcpyHostToDevice, c->stream));
             }
         }
-        // the backward rows with room to grow
-        int64_t laid = 0;
+        // the backward rows with room to grow (h.m bounds the entries; the layout reads the count)
         if (n) {
             launch_brow_layout(t_bo.p, t_bc.p, (int64_t)n, h.m, t_caps.p, t_begs.p, t_bsum.p, c->brow.p + h.nbase,
                                c->bcap.p + h.nbase, c->bcol.p + h.bbase, c->stream);
             PG_CUDA(c, cudaGetLastError());
-            PG_CUDA(c, cudaMemcpyAsync(&laid, t_begs.p + n, 8, cudaMemcpyDeviceToHost, c->stream));
-            PG_CUDA(c, cudaStreamSynchronize(c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(t_laid.p + r, t_begs.p + n, 8, cudaMemcpyDeviceToDevice, c->stream));
         }
-        if (laid < 0 || laid > h.b_cap) return fail(c, PG_ERR_CUDA, "backward row layout out of range");
-        h.b_top = laid;
-        drep[(size_t)r] = to_device_rep(h);
     }
-    if (raw) {
+    {
+        std::vector<int64_t> us((size_t)R, 0), laid((size_t)R, 0);
+        std::vector<uint32_t> be((size_t)R, 0);
+        if (raw) {
+            PG_CUDA(c, cudaMemcpyAsync(us.data(), t_u.p, 8 * (size_t)R, cudaMemcpyDeviceToHost, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(be.data(), berr.p, 4 * (size_t)R, cudaMemcpyDeviceToHost, c->stream));
+        }
+        PG_CUDA(c, cudaMemcpyAsync(laid.data(), t_laid.p, 8 * (size_t)R, cudaMemcpyDeviceToHost, c->stream));
         PG_CUDA(c, cudaStreamSynchronize(c->stream));
-        dfree(scratch);
-        dfree(raw_src);
-        dfree(raw_dst);
-        dfree(berr);
+        if (raw) {
+            dfree(scratch);
+            dfree(raw_src);
+            dfree(raw_dst);
+            dfree(berr);
+        }
+        for (int r = 0; r < R; ++r) {
+            HostRep& h = reps[r];
+            if (raw) {
+                if (be[(size_t)r]) return fail(c, PG_ERR_ARG, "edge endpoint out of range in replica " + std::to_string(r));
+                // at most the raw edge count; anything else means the sequence above failed
+                if (us[(size_t)r] < 0 || us[(size_t)r] > raw[r].num_edges)
+                    return fail(c, PG_ERR_CUDA, "seed CSR build failed in replica " + std::to_string(r));
+                h.m = us[(size_t)r];
+            }
+            if (laid[(size_t)r] < 0 || laid[(size_t)r] > h.b_cap)
+                return fail(c, PG_ERR_CUDA, "backward row layout out of range");
+            h.b_top = laid[(size_t)r];
+            drep[(size_t)r] = to_device_rep(h);
+        }
     }
     PG_CUDA(c, cudaMemcpyAsync(c->tile_rep.p, trep.data(), 4 * (size_t)T, cudaMemcpyHostToDevice, c->stream));
     PG_CUDA(c, cudaMemcpyAsync(c->rep.p, drep.data(), sizeof(Replica) * (size_t)R, cudaMemcpyHostToDevice, c->stream));
@@ -1136,6 +1142,9 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->tileoff);
     dfree(c->tables);
     dfree(c->hlist);
+    dfree(c->hub_rem);
+    dfree(c->hub_add);
+    dfree(c->hub_cand);
     dfree(c->hslot);
     dfree(c->hmask);
     dfree(c->hub2);
@@ -1174,13 +1183,8 @@ pg_status pg_load_replicas(pg_ctx* c, const pg_replica_desc* descs, int32_t num)
         if (d.num_nodes <= 0 || d.num_nodes > (int64_t)INT32_MAX / 2) return fail(c, PG_ERR_ARG, "num_nodes out of range");
         if (d.num_edges < 0 || (d.num_edges > 0 && (!d.src || !d.dst))) return fail(c, PG_ERR_ARG, "bad edge arrays");
         if (!d.pub_epoch || !d.fitness) return fail(c, PG_ERR_ARG, "pub_epoch and fitness are required");
-        // endpoints checked before the arena is touched, so a bad edge list leaves the loaded graph
-        // intact: on all host threads here for several replicas, on the device (after the upload
-        // the build needs anyway) for one
-        if (num > 1) {
-            const int64_t bad = first_bad_edge(d.src, d.dst, d.num_edges, d.num_nodes);
-            if (bad >= 0) return fail(c, PG_ERR_ARG, "edge endpoint out of range at index " + std::to_string(bad));
-        }
+        // the endpoints are checked on the device after the upload the build needs anyway, before
+        // the arena is touched (upload_arena)
     }
     // the CSRs are built on the device from the raw edges (upload_arena); the plan below uses the
     // raw edge count, an upper bound on the unique edges
@@ -1795,6 +1799,9 @@ pg_status pg_restore(pg_ctx* c) {
     PG_CUDA(c, cudaMemcpyAsync(c->brow.p, k.brow.p, sizeof(BRow) * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(c->bcap.p, k.bcap.p, sizeof(int32_t) * (size_t)c->S, d2d, s));
     PG_CUDA(c, cudaMemcpyAsync(c->rep.p, k.rep.p, sizeof(Replica) * (size_t)c->R, d2d, s));
+    // the hub index is not part of the checkpoint: the next epoch rebuilds it
+    PG_CUDA(c, cudaMemset2DAsync(reinterpret_cast<char*>(c->rep.p) + offsetof(Replica, hub_valid), sizeof(Replica), 0,
+                                 sizeof(int32_t), (size_t)c->R, s));
     for (size_t r = 0; r < k.hrep.size(); ++r) {
         const HostRep& h = k.hrep[r];
         if (h.m) PG_CUDA(c, cudaMemcpyAsync(c->fwd_col.p + h.ebase, k.fwd_col.p + h.ebase, 4 * (size_t)h.m, d2d, s));

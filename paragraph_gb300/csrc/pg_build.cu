@@ -8,8 +8,12 @@
 //                   (per pass: tile histograms, one scan over [digit][tile], stable scatter)
 //   k_unique_*      duplicates collapse (Graph::AddEdge set semantics), forward columns and
 //                   per-source counts; counts -> int64 offsets by the engine's scan
-//   radix passes    the unique keys stably re-sorted on the target field only, which orders them
-//                   by (target, source): backward columns and in-degrees.
+//   radix passes    the keys stably re-sorted on the target field only, which orders the unique
+//                   ones by (target, source) and puts the duplicates (marked) last: backward
+//                   columns and in-degrees.
+// Nothing is read back on the way: the unique count stays on the device (u_dev) and bounds the
+// later kernels there, so the replicas of a context are built one after another without a host
+// synchronisation.
 // Rows come out ascending, as the reference's std::set rows.  Every step is integer work, so the
 // result equals the host construction bit for bit.
 #include <algorithm>
@@ -98,28 +102,39 @@ __global__ void __launch_bounds__(256) k_unique_flags(const unsigned long long* 
         flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
 }
 
-// Compact the unique keys (sorted by source, then target) and count the edges of every source.
+// The unique keys (sorted by source, then target) as forward columns, and the edges of every source.
 __global__ void __launch_bounds__(256) k_unique_compact(const unsigned long long* keys, int64_t m, const int32_t* flag,
-                                                        const int64_t* pos, int bits, unsigned long long* ukeys,
-                                                        int32_t* fcol, int32_t* fcnt) {
+                                                        const int64_t* pos, int bits, int32_t* fcol, int32_t* fcnt) {
     const unsigned long long mask = (1ull << bits) - 1ull;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         if (!flag[i]) continue;
         const unsigned long long k = keys[i];
         const int64_t p = pos[i];
-        ukeys[p] = k;
         fcol[p] = (int32_t)(k & mask);
         atomicAdd(&fcnt[(int64_t)(k >> bits)], 1);
     }
 }
 
-// Keys sorted by (target, source): backward columns (sources) and per-target counts.
-__global__ void __launch_bounds__(256) k_backward_cols(const unsigned long long* keys, int64_t u, int bits,
-                                                       int32_t* bcol, int32_t* bcnt) {
+// Keys for the backward sort, one per sorted key: a unique edge as source << (bits + 1) | target,
+// a duplicate as all ones, whose low bits + 1 bits exceed every target, so it sorts last.
+__global__ void __launch_bounds__(256) k_backward_keys(const unsigned long long* keys, int64_t m, const int32_t* flag,
+                                                       int bits, unsigned long long* bkeys) {
     const unsigned long long mask = (1ull << bits) - 1ull;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long k = keys[i];
+        bkeys[i] = flag[i] ? (((k >> bits) << (bits + 1)) | (k & mask)) : ~0ull;
+    }
+}
+
+// Keys sorted by (target, source), the u_dev unique ones first: backward columns (sources) and
+// per-target counts.
+__global__ void __launch_bounds__(256) k_backward_cols(const unsigned long long* keys, const int64_t* u_dev, int bits,
+                                                       int32_t* bcol, int32_t* bcnt) {
+    const unsigned long long mask = (1ull << (bits + 1)) - 1ull;
+    const int64_t u = *u_dev;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < u; i += (int64_t)gridDim.x * blockDim.x) {
         const unsigned long long k = keys[i];
-        bcol[i] = (int32_t)(k >> bits);
+        bcol[i] = (int32_t)(k >> (bits + 1));
         atomicAdd(&bcnt[(int64_t)(k & mask)], 1);
     }
 }
@@ -179,10 +194,10 @@ size_t build_scratch_bytes(int64_t m, int64_t n) {
 }
 
 // Builds replica CSRs on the device.  src/dst: m raw device edges; outputs: fo/fc/bo/bc (the
-// replica's regions), indeg (n entries).  Returns the number of unique edges through *u_out (read
-// back by the caller after a sync).  Scratch layout is carved from `scratch`.
+// replica's regions), indeg (n entries), the number of unique edges in *u_dev (device memory; bo[n]
+// holds it too).  Scratch layout is carved from `scratch`.
 void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,
-                      int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_out,
+                      int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_dev,
                       uint32_t* err, cudaStream_t s) {
     const int64_t e = m > 0 ? m : 1;
     const int64_t scan = build_scan_entries(e) + 1;
@@ -208,27 +223,19 @@ void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t
     cudaMemsetAsync(fcnt, 0, (size_t)(n + 1) * 4, s);
     cudaMemsetAsync(bcnt, 0, (size_t)(n + 1) * 4, s);
     const unsigned grid = (unsigned)std::min<int64_t>((e + 255) / 256, 152 * 16);
-    int64_t u = 0;
     if (m > 0) {
         k_edge_keys<<<grid, 256, 0, s>>>(src, dst, m, n, bits, k0, err);
         unsigned long long* sorted = radix_sort(k0, k1, m, 0, 2 * bits, hist, off, blocksum, s);
         k_unique_flags<<<grid, 256, 0, s>>>(sorted, m, flag);
         launch_scan_i32_to_i64(flag, pos, m, blocksum, s);
-        k_unique_compact<<<grid, 256, 0, s>>>(sorted, m, flag, pos, bits, uk, fc, fcnt);
-        // number of unique edges
-        cudaMemcpyAsync(u_out, pos + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
-        u = cudaStreamSynchronize(s) == cudaSuccess ? *u_out : 0;
-        // at most m unique edges; anything else means the sequence above failed (the caller reports
-        // the error), and the count must not size the next sort
-        if (u < 0 || u > m) u = 0;
-        *u_out = u;
-        if (u > 0) {
-            unsigned long long* other = sorted == k0 ? k1 : k0;
-            unsigned long long* bsorted = radix_sort(uk, other, u, 0, bits, hist, off, blocksum, s);
-            k_backward_cols<<<grid, 256, 0, s>>>(bsorted, u, bits, bc, bcnt);
-        }
+        k_unique_compact<<<grid, 256, 0, s>>>(sorted, m, flag, pos, bits, fc, fcnt);
+        cudaMemcpyAsync(u_dev, pos + m, sizeof(int64_t), cudaMemcpyDeviceToDevice, s);  // unique edges
+        k_backward_keys<<<grid, 256, 0, s>>>(sorted, m, flag, bits, uk);
+        unsigned long long* other = sorted == k0 ? k1 : k0;
+        unsigned long long* bsorted = radix_sort(uk, other, m, 0, bits + 1, hist, off, blocksum, s);
+        k_backward_cols<<<grid, 256, 0, s>>>(bsorted, u_dev, bits, bc, bcnt);
     } else {
-        *u_out = 0;
+        cudaMemsetAsync(u_dev, 0, sizeof(int64_t), s);
     }
     launch_scan_i32_to_i64(fcnt, fo, n, blocksum, s);
     launch_scan_i32_to_i64(bcnt, bo, n, blocksum, s);
@@ -258,10 +265,12 @@ __global__ void __launch_bounds__(256) k_brow_rows(const int64_t* bo, const int6
     }
 }
 
-// entry p of the offset form goes to its row's span: the row is the last v with bo[v] <= p
+// entry p of the offset form goes to its row's span: the row is the last v with bo[v] <= p (bo[n],
+// the entry count, is read on the device; m only bounds it)
 __global__ void __launch_bounds__(256) k_brow_cols(const int64_t* bo, const int32_t* bc, const int64_t* begs,
                                                    int64_t n, int64_t m, int32_t* out) {
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t mm = bo[n] < m ? bo[n] : m;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < mm; p += (int64_t)gridDim.x * blockDim.x) {
         int64_t lo = 0, hi = n - 1;
         while (lo < hi) {
             const int64_t mid = (lo + hi + 1) >> 1;

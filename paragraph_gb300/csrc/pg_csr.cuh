@@ -169,7 +169,9 @@ __device__ __forceinline__ void d_bwd_reloc(const Arena& A) {
 
 __global__ void __launch_bounds__(256) k_bwd_reloc(Arena A) { d_bwd_reloc(A); }
 
-// One warp per agent: each edge at its row's start of new entries + rank.
+// One warp per agent: each edge at its row's start of new entries + rank.  The agent is a new node:
+// its hub-index entry is written here (no hub bit, and a mask of the hubs it cites), so the next
+// epoch's hub index only has to move the hubs that changed.
 __device__ __forceinline__ void d_bwd_place(const Arena& A, int64_t agents) {
     if (A.st->error) return;
     const int lane = lane_id();
@@ -182,7 +184,31 @@ __device__ __forceinline__ void d_bwd_place(const Arena& A, int64_t agents) {
         const int64_t e0 = A.eoff[a], e1 = A.eoff[a + 1];
         int32_t* bc = A.bcol + rp.bbase;
         const int64_t* st = A.len_tmp + rp.nbase;
-        for (int64_t e = e0 + lane; e < e1; e += 32) bc[st[A.e_dst[e]] + A.e_rank[e]] = src;
+        unsigned hm[2 * kMaskWords] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        for (int64_t e = e0 + lane; e < e1; e += 32) {
+            const int32_t j = A.e_dst[e];
+            bc[st[j] + A.e_rank[e]] = src;
+            const int hs = A.hslot[rp.nbase + j];
+            if (hs >= 0) {
+#pragma unroll
+                for (int w = 0; w < 2 * kMaskWords; ++w)
+                    if ((hs >> 5) == w) hm[w] |= 1u << (hs & 31);
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < 2 * kMaskWords; ++w) hm[w] = __reduce_or_sync(kFullMask, hm[w]);
+        if (lane < kMaskWords) {
+            const int64_t slot = rp.nbase + src;
+            unsigned lo = hm[0], hi = hm[1];
+#pragma unroll
+            for (int w = 1; w < kMaskWords; ++w)
+                if (lane == w) {
+                    lo = hm[2 * w];
+                    hi = hm[2 * w + 1];
+                }
+            A.hmask[slot * kMaskWords + lane] = ((unsigned long long)hi << 32) | lo;
+            if (lane == 0) A.hslot[slot] = -1;
+        }
     }
 }
 
@@ -292,9 +318,11 @@ __device__ __forceinline__ void d_sort_large(const Arena& A, uint32_t* bm, int64
     }
 }
 
-__global__ void __launch_bounds__(1024) k_sort_large(Arena A) {
+// bm_words: the bitmap of this launch (dynamic shared memory), enough for the epoch's new-id range
+// where that fits, so several CTAs share an SM
+__global__ void __launch_bounds__(256) k_sort_large(Arena A, int64_t bm_words) {
     extern __shared__ uint32_t bm[];
-    d_sort_large(A, bm, kBitmapWords);
+    d_sort_large(A, bm, bm_words);
 }
 
 __device__ __forceinline__ void d_epoch_end(const Arena& A, int64_t agents) {
@@ -345,7 +373,10 @@ void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t
     if (two) cudaEventRecord(join, side);
     k_bwd_place<<<(unsigned)ga, 256, 0, s>>>(A, agents);
     k_sort_small<<<(unsigned)num_sms * 8, 256, 0, s>>>(A);
-    k_sort_large<<<(unsigned)num_sms, 1024, kBitmapWords * 4, s>>>(A);
+    // a replica's new ids span at most the epoch's agents
+    int64_t words = (agents + 31) / 32 + 1;
+    if (words > kBitmapWords) words = kBitmapWords;
+    k_sort_large<<<(unsigned)num_sms * 4, 256, (size_t)words * 4, s>>>(A, words);
     if (two) cudaStreamWaitEvent(s, join, 0);
     k_epoch_end<<<1, 256, 0, s>>>(A, agents);
 }

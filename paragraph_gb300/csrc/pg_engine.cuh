@@ -99,9 +99,14 @@ struct Replica {
     double growth_rate;
     int64_t fixed_new;
     int32_t anchors;
-    // hub index of the epoch: nodes with degree >= heavy_thr get one of <= kHeavyMax mask bits
+    // hub index of the epoch: nodes with degree >= heavy_thr get one of <= kHeavyMax mask bits; the
+    // bits and masks carry over from epoch to epoch while hub_valid (cleared by a load or restore)
     int32_t heavy_thr;
-    int32_t heavy_count;
+    int32_t heavy_count;  // highest bit in use + 1
+    int32_t hub_valid;
+    int32_t hub_full;     // this epoch rebuilds the index from scratch
+    int32_t hub_nadd;     // nodes that become hubs this epoch
+    int32_t hub_pad;
     int32_t heavy_hist[kHeavyBins];
     // refcompat functor (weight model PG_WEIGHTS_REFCOMPAT)
     double rc_w[3];   // pa, rec, fit weights, normalised; rc_w[0] < 0: drawn per agent
@@ -196,7 +201,10 @@ struct Arena {
     uint64_t* hmask;           // [slots][kMaskWords] bit b set when hub b is adjacent to the node
     uint64_t* hub2;            // [R][kHeavyMax][kMaskWords] hubs sharing a neighbour with hub b
     uint32_t* hub_need;        // [R][kHeavyMax / 32] hubs some agent of the epoch has as anchor
-    int32_t* hlist;            // [R][kHeavyMax] hub node ids
+    int32_t* hlist;            // [R][kHeavyMax] hub node of each bit, -1 when the bit is free
+    int32_t* hub_rem;          // [R][kHeavyMax] node leaving bit b this epoch, or -1
+    int32_t* hub_add;          // [R][kHeavyMax] node taking bit b this epoch, or -1
+    int32_t* hub_cand;         // [R][kHeavyMax] nodes that become hubs this epoch
     // refcompat functor (null unless the context uses PG_WEIGHTS_REFCOMPAT)
     double* rc_pa;             // [slots] score components of the epoch
     double* rc_rec;
@@ -385,8 +393,8 @@ __device__ __forceinline__ int replica_of_agent(const Replica* rep, int R, int64
 // two sorts, end).
 constexpr int kPaEpochKernels = 18;
 // Extra kernels of the thinning sampler: the CDF's guide table (1) and the hub index (histogram,
-// pick, collect, mask, hub pairs).
-constexpr int kThinKernels = 6;
+// pick, collect, bit assignment, mask clears, mask sets, hub pairs).
+constexpr int kThinKernels = 8;
 void launch_epoch_begin(const Arena& A, int64_t epoch, int pa_mode, cudaStream_t s);
 void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cudaStream_t s);
 void launch_weights(const Arena& A, cudaStream_t s);
@@ -449,7 +457,7 @@ void launch_first_bad_edge(const int32_t* src, const int32_t* dst, int64_t m, in
                            cudaStream_t s);
 size_t build_scratch_bytes(int64_t m, int64_t n);
 void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,
-                      int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_out,
+                      int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_dev,
                       uint32_t* err, cudaStream_t s);
 // growable backward rows from an offset-form backward CSR (pg_build.cu): caps n, begs n + 1 (begs[n]
 // = entries laid out), blocksum scan_blocks_needed(n) + 2 entries of scratch; brow/bcol: the

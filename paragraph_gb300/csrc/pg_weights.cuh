@@ -326,10 +326,16 @@ __global__ void __launch_bounds__(kTileThreads) k_guide_fill(Arena A) { d_guide_
 
 // ---------------------------------------------------------------- hub index
 // Ball membership of a high-degree node j needs adj(j) intersected with the agent's 1-hop
-// frontier, which is expensive when j has millions of neighbours.  Each epoch, up to 64 nodes of
-// largest degree per replica become hubs; hmask[v] has bit b set when hub b is adjacent to v, so an
-// agent ORs hmask over its frontier once and answers "hub b in my ball?" with one bit test.  Which
-// nodes are hubs only changes speed, never a result.
+// frontier, which is expensive when j has millions of neighbours.  Each epoch the nodes of degree
+// >= heavy_thr become hubs (at most kHeavyMax per replica, the highest log2-degree bins); each holds
+// one bit, and hmask[v] has bit b set when hub b is adjacent to v, so an agent ORs hmask over its
+// frontier once and answers "hub b in my ball?" with one bit test.  Which nodes are hubs only changes
+// speed, never a result.
+// The index is kept from epoch to epoch.  Adjacency only grows by new nodes' edges, and a new node
+// is never a hub, so the placement of an epoch's edges writes each new node's mask from the hubs it
+// cites; the next epoch then only moves the hubs that changed: a node that left the hub set clears
+// its bit on its neighbours, a node that joined takes a free bit and sets it on its neighbours.  A
+// load or restore clears hub_valid and the next epoch rebuilds the whole index.
 __device__ __forceinline__ int64_t degree_of(const Arena& A, const Replica& rp, int64_t v) {
     const int64_t* fo = A.fwd_off + rp.obase;
     return (fo[v + 1] - fo[v]) + blen(A.brow + rp.nbase, v);
@@ -342,8 +348,7 @@ __device__ __forceinline__ void d_hub_hist(const Arena& A, int vb) {
     Replica& rp = A.rep[r];
     const int64_t v0 = (int64_t)(t - rp.tbase) * kTile;
     if (v0 >= rp.n) return;
-    // the degrees of the thread's nodes are loaded before the resets are stored (the stores could
-    // otherwise alias the later loads and serialise them)
+    const bool full = !rp.hub_valid;
     constexpr int kPer = kTile / kTileThreads;
     int64_t dg[kPer];
 #pragma unroll
@@ -355,12 +360,14 @@ __device__ __forceinline__ void d_hub_hist(const Arena& A, int vb) {
     for (int i = 0; i < kPer; ++i) {
         const int64_t v = v0 + threadIdx.x + i * kTileThreads;
         if (v >= rp.n) continue;
-        const int64_t slot = rp.nbase + v;
-        A.hslot[slot] = -1;
-        static_assert(kMaskWords == 4, "hub mask row of 32 bytes");
-        ulonglong2* hm = reinterpret_cast<ulonglong2*>(A.hmask + slot * kMaskWords);
-        hm[0] = make_ulonglong2(0ull, 0ull);
-        hm[1] = make_ulonglong2(0ull, 0ull);
+        if (full) {  // the degrees were loaded first: these stores could otherwise delay them
+            const int64_t slot = rp.nbase + v;
+            A.hslot[slot] = -1;
+            static_assert(kMaskWords == 4, "hub mask row of 32 bytes");
+            ulonglong2* hm = reinterpret_cast<ulonglong2*>(A.hmask + slot * kMaskWords);
+            hm[0] = make_ulonglong2(0ull, 0ull);
+            hm[1] = make_ulonglong2(0ull, 0ull);
+        }
         const int64_t d = dg[i];
         if (d >= (1 << kHeavyMinLog)) {
             int b = 63 - __clzll((unsigned long long)d) - kHeavyMinLog;
@@ -373,7 +380,7 @@ __device__ __forceinline__ void d_hub_hist(const Arena& A, int vb) {
 __global__ void __launch_bounds__(kTileThreads) k_hub_hist(Arena A) { d_hub_hist(A, blockIdx.x); }
 
 __device__ __forceinline__ void d_hub_pick(const Arena& A) {
-    if (A.st->error) return;
+    if (cta_error(A)) return;
     for (int r = threadIdx.x; r < A.R; r += blockDim.x) {
         Replica& rp = A.rep[r];
         int thr = 0x7fffffff, cum = 0;
@@ -383,7 +390,15 @@ __device__ __forceinline__ void d_hub_pick(const Arena& A) {
             if (rp.heavy_hist[b]) thr = 1 << (b + kHeavyMinLog);
         }
         rp.heavy_thr = thr;
-        rp.heavy_count = 0;
+        rp.hub_nadd = 0;
+        rp.hub_full = !rp.hub_valid;
+        rp.hub_valid = 1;
+    }
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < (int64_t)A.R * kHeavyMax; i += blockDim.x) {
+        A.hub_rem[i] = -1;
+        A.hub_add[i] = -1;
+        if (A.rep[i / kHeavyMax].hub_full) A.hlist[i] = -1;
     }
     // hub-pair masks are OR-accumulated by k_hub_pairs, for the hubs the agent setup flags
     const int64_t words = (int64_t)A.R * kHeavyMax * kMaskWords;
@@ -393,6 +408,7 @@ __device__ __forceinline__ void d_hub_pick(const Arena& A) {
 
 __global__ void k_hub_pick(Arena A) { d_hub_pick(A); }
 
+// Nodes leaving the hub set give up their bit (hub_rem), nodes joining it are listed (hub_cand).
 __device__ __forceinline__ void d_hub_collect(const Arena& A, int vb) {
     if (A.st->error) return;
     const int t = vb;
@@ -403,35 +419,96 @@ __device__ __forceinline__ void d_hub_collect(const Arena& A, int vb) {
     const int64_t thr = rp.heavy_thr;
     constexpr int kPer = kTile / kTileThreads;
     int64_t dg[kPer];
+    int hs[kPer];
 #pragma unroll
     for (int i = 0; i < kPer; ++i) {
         const int64_t v = v0 + threadIdx.x + i * kTileThreads;
         dg[i] = v < rp.n ? degree_of(A, rp, v) : 0;
+        hs[i] = v < rp.n ? A.hslot[rp.nbase + v] : -1;
     }
 #pragma unroll
     for (int i = 0; i < kPer; ++i) {
         const int64_t v = v0 + threadIdx.x + i * kTileThreads;
         if (v >= rp.n) continue;
-        if (dg[i] >= thr) {
-            const int b = atomicAdd(&rp.heavy_count, 1);
-            if (b < kHeavyMax) {
-                A.hslot[rp.nbase + v] = (int16_t)b;
-                A.hlist[(int64_t)r * kHeavyMax + b] = (int32_t)v;
-            }
+        const bool want = dg[i] >= thr;
+        if (hs[i] >= 0 && !want) {
+            A.hub_rem[(int64_t)r * kHeavyMax + hs[i]] = (int32_t)v;
+            A.hslot[rp.nbase + v] = -1;
+        } else if (hs[i] < 0 && want) {
+            const int q = atomicAdd(&rp.hub_nadd, 1);
+            if (q < kHeavyMax) A.hub_cand[(int64_t)r * kHeavyMax + q] = (int32_t)v;
         }
     }
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_hub_collect(Arena A) { d_hub_collect(A, blockIdx.x); }
 
-// G CTAs per (replica, hub bit) split the hub's neighbours: mark every neighbour of the hub.
+// Bits of the epoch, one warp per replica: the bits given up are freed, and the q-th joining node
+// takes the q-th free bit.  (At most kHeavyMax nodes have degree >= heavy_thr, so there are always
+// enough free bits.)
+__device__ __forceinline__ void d_hub_assign(const Arena& A) {
+    if (A.st->error) return;
+    const int lane = lane_id();
+    for (int r = threadIdx.x >> 5; r < A.R; r += blockDim.x >> 5) {
+        Replica& rp = A.rep[r];
+        int32_t* hl = A.hlist + (int64_t)r * kHeavyMax;
+        const int32_t* rem = A.hub_rem + (int64_t)r * kHeavyMax;
+        unsigned freew[kHeavyMax / 32];
+#pragma unroll
+        for (int w = 0; w < kHeavyMax / 32; ++w) {
+            const int b = w * 32 + lane;
+            const bool fr = hl[b] < 0 || rem[b] >= 0;
+            if (rem[b] >= 0) hl[b] = -1;
+            freew[w] = __ballot_sync(0xffffffffu, fr);
+        }
+        const int nadd = rp.hub_nadd < kHeavyMax ? rp.hub_nadd : kHeavyMax;
+        for (int q = lane; q < nadd; q += 32) {
+            // the q-th free bit
+            int left = q, b = -1;
+#pragma unroll
+            for (int w = 0; w < kHeavyMax / 32; ++w) {
+                const int c = __popc(freew[w]);
+                if (b < 0 && left < c) {
+                    unsigned m = freew[w];
+                    for (int k = 0; k < left; ++k) m &= m - 1u;
+                    b = w * 32 + __ffs(m) - 1;
+                }
+                if (b < 0) left -= c;
+            }
+            if (b >= 0) {
+                const int32_t v = A.hub_cand[(int64_t)r * kHeavyMax + q];
+                hl[b] = v;
+                A.hub_add[(int64_t)r * kHeavyMax + b] = v;
+                A.hslot[rp.nbase + v] = (int16_t)b;
+            } else {
+                atomicOr(&A.st->error, kErrCapacity);  // cannot happen: see above
+            }
+        }
+        __syncwarp();
+        int top = 0;
+#pragma unroll
+        for (int w = 0; w < kHeavyMax / 32; ++w) {
+            const unsigned used = __ballot_sync(0xffffffffu, hl[w * 32 + lane] >= 0);
+            if (used) top = w * 32 + 32 - __clz((int)used);
+        }
+        if (lane == 0) rp.heavy_count = top;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_hub_assign(Arena A) { d_hub_assign(A); }
+
+// G CTAs per (replica, hub bit) split a hub's neighbours.  SET = false: the node that left bit b
+// clears it on its neighbours; SET = true: the node that took bit b sets it (the clears of an epoch
+// all finish before its sets, so a bit freed and taken again in one epoch ends up right).
+template <bool SET>
 __device__ __forceinline__ void d_hub_mask(const Arena& A, int G, int vb) {
     if (A.st->error) return;
     const int item = vb / G, g = vb % G;
     const int r = item / kHeavyMax, b = item % kHeavyMax;
+    if (r >= A.R) return;
     const Replica& rp = A.rep[r];
-    if (b >= rp.heavy_count || b >= kHeavyMax) return;
-    const int64_t h = A.hlist[(int64_t)r * kHeavyMax + b];
+    const int64_t h = (SET ? A.hub_add : A.hub_rem)[(int64_t)r * kHeavyMax + b];
+    if (h < 0) return;
     const unsigned long long bit = 1ull << (b & 63);
     const int64_t stride = (int64_t)G * blockDim.x;
     for (int dir = 0; dir < 2; ++dir) {
@@ -445,12 +522,18 @@ __device__ __forceinline__ void d_hub_mask(const Arena& A, int G, int vb) {
             p1 = A.fwd_off[rp.obase + h + 1];
             col = A.fwd_col + rp.ebase;
         }
-        for (int64_t p = p0 + (int64_t)g * blockDim.x + threadIdx.x; p < p1; p += stride)
-            atomicOr((unsigned long long*)&A.hmask[(rp.nbase + col[p]) * kMaskWords + (b >> 6)], bit);
+        for (int64_t p = p0 + (int64_t)g * blockDim.x + threadIdx.x; p < p1; p += stride) {
+            unsigned long long* w = (unsigned long long*)&A.hmask[(rp.nbase + col[p]) * kMaskWords + (b >> 6)];
+            if (SET)
+                atomicOr(w, bit);
+            else
+                atomicAnd(w, ~bit);
+        }
     }
 }
 
-__global__ void __launch_bounds__(256) k_hub_mask(Arena A, int G) { d_hub_mask(A, G, blockIdx.x); }
+template <bool SET>
+__global__ void __launch_bounds__(256) k_hub_mask(Arena A, int G) { d_hub_mask<SET>(A, G, blockIdx.x); }
 
 // hub2[b] = OR of hmask over the hub's neighbours: the hubs sharing a neighbour with hub b.
 __device__ __forceinline__ void d_hub_pairs(const Arena& A, int G, int vb) {
@@ -458,13 +541,14 @@ __device__ __forceinline__ void d_hub_pairs(const Arena& A, int G, int vb) {
     if (cta_error(A)) return;
     const int item = vb / G, g = vb % G;
     const int r = item / kHeavyMax, b = item % kHeavyMax;
+    if (r >= A.R) return;
     const Replica& rp = A.rep[r];
-    if (b >= rp.heavy_count || b >= kHeavyMax) return;
+    const int64_t h = A.hlist[(int64_t)r * kHeavyMax + b];
+    if (h < 0) return;
     // only an agent whose anchor is hub b reads its row
     if (!((A.hub_need[(int64_t)r * (kHeavyMax / 32) + (b >> 5)] >> (b & 31)) & 1u)) return;
     if (threadIdx.x < kMaskWords) acc[threadIdx.x] = 0;
     __syncthreads();
-    const int64_t h = A.hlist[(int64_t)r * kHeavyMax + b];
     const int64_t stride = (int64_t)G * blockDim.x;
     unsigned long long m[kMaskWords];
 #pragma unroll
@@ -506,7 +590,9 @@ void launch_hubs(const Arena& A, int num_sms, cudaStream_t s) {
     k_hub_hist<<<A.ntiles, kTileThreads, 0, s>>>(A);
     k_hub_pick<<<1, 256, 0, s>>>(A);
     k_hub_collect<<<A.ntiles, kTileThreads, 0, s>>>(A);
-    k_hub_mask<<<(unsigned)(A.R * kHeavyMax * G), 256, 0, s>>>(A, G);
+    k_hub_assign<<<1, 256, 0, s>>>(A);
+    k_hub_mask<false><<<(unsigned)(A.R * kHeavyMax * G), 256, 0, s>>>(A, G);
+    k_hub_mask<true><<<(unsigned)(A.R * kHeavyMax * G), 256, 0, s>>>(A, G);
 }
 
 void launch_hub_pairs(const Arena& A, cudaStream_t s) {

@@ -202,6 +202,41 @@ def test_replicas_match_independent_oracles(gpu, epoch_kernel):
             _compare_state(eng, og, replica=r)
 
 
+def test_hub_index_carried_over_epochs(gpu):
+    """The hub index is kept from epoch to epoch and only the hubs that change are moved.  On this
+    seed (300k nodes, Pareto(1.5) in-degrees, 5 % growth) nodes pass degree 1024 and join the hub
+    set every epoch, and at epoch 5 more than 256 nodes have passed it, so the threshold doubles and
+    about 170 hubs leave at once.  Every epoch's counters, arrivals and CSRs equal the oracle's; a
+    restore at epoch 3 (which makes the next epoch rebuild the index) regrows the same graph."""
+    g = W.pareto_seed(300_000, 1.5, 16.0, seed=3)
+    prm = PAParams(mean_out_degree=30.0, growth_rate=0.05, fixed_new_nodes=0)
+    counts = []
+    with GrowthEngine(seed=5, record_trace=True) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=7)
+        og = _oracle_for(g, prm, 5, sampler=PG_SAMPLER_THINNING)
+        for e in range(7):
+            ind, outd = eng.degrees()
+            deg = ind.astype(np.int64) + outd
+            counts.append(int((deg >= 1024).sum()))
+            if e == 3:
+                eng.checkpoint()
+            eng.grow_epoch()
+            og.pa_epoch()
+            st, so = eng.stats(), og.stats()
+            for k in ("nodes_weighted", "rows_expanded", "draws", "adj_scanned"):
+                assert st[k] == so[k], (e, k)
+            np.testing.assert_array_equal(eng.arrivals(), og.arrivals())
+        _compare_state(eng, og)
+        final = [eng.csr(w) for w in (0, 1)]
+        eng.restore()
+        eng.run_epochs(4, use_graph=True)
+        for (o1, c1), (o2, c2) in zip(final, [eng.csr(w) for w in (0, 1)]):
+            np.testing.assert_array_equal(o1, o2)
+            np.testing.assert_array_equal(c1, c2)
+        og.close()
+    assert counts[0] < counts[1] < counts[4] <= 256 < counts[5], counts
+
+
 def test_checkpoint_restore_regrows_identically(gpu):
     g = W.plain_pa_seed(4000, 10, seed=9)
     prm = PAParams(mean_out_degree=20.0, growth_rate=0.03, fixed_new_nodes=0)
@@ -219,7 +254,7 @@ def test_checkpoint_restore_regrows_identically(gpu):
             np.testing.assert_array_equal(c1, c2)
         st = eng.stats()
         assert st["run_epochs"] == 8 and st["run_new_edges"] == e2
-        assert st["run_kernel_launches"] == 8 * (18 + 6)  # thinning adds the guide table and hub index
+        assert st["run_kernel_launches"] == 8 * (18 + 8)  # thinning adds the guide table and hub index
         # the same run as one persistent kernel per epoch: same graph, one launch per epoch
         eng.set_tuning(epoch_kernel=1)
         eng.restore()
@@ -313,6 +348,28 @@ def test_device_seed_load_matches_host_construction(gpu, n):
         # the rejected edge list left the loaded graph as it was
         assert eng.counts() == before
         _compare_state(eng, og)
+
+
+def test_bad_edge_in_one_replica_leaves_the_loaded_replicas(gpu):
+    """All replicas' raw edges are staged and checked on the device before the arena is rebuilt: an
+    endpoint out of range in one replica is reported with its index and replica, and the replicas
+    loaded before stay as they were."""
+    import dataclasses
+
+    reps = W.ensemble_inputs(replicas=3, lo=500, hi=2000, epochs=1, seed=4)
+    with GrowthEngine(seed=2, replicas=3) as eng:
+        eng.load_replicas(reps)
+        before = [eng.csr(w, r) for r in range(3) for w in (0, 1)]
+        dst = reps[1].dst.copy()
+        dst[5] = len(reps[1].pub_epoch)  # one past the last node
+        bad = list(reps)
+        bad[1] = dataclasses.replace(reps[1], dst=dst)
+        with pytest.raises(PGError, match="out of range at index 5 of replica 1"):
+            eng.load_replicas(bad)
+        for (o1, c1), (o2, c2) in zip(before, [eng.csr(w, r) for r in range(3) for w in (0, 1)]):
+            np.testing.assert_array_equal(o1, o2)
+            np.testing.assert_array_equal(c1, c2)
+        eng.run_epochs(1)  # still usable
 
 
 def test_edges_into_caller_buffers(gpu):
