@@ -116,7 +116,7 @@ typedef struct {
     int64_t rows_expanded;     /* adjacency rows (fwd+bwd pairs) read by the neighbourhood stage */
     int64_t elems_streamed;    /* neighbourhood elements keyed (with multiplicity) */
     int64_t draws;             /* global-race draws */
-    int64_t bwd_moved;         /* old backward-CSR entries moved by the append */
+    int64_t bwd_moved;         /* old backward entries copied because their row outgrew its room */
     int64_t bytes_alg;         /* algorithmic bytes of the epoch (per-stage byte model of the engine) */
     int64_t bytes_alg_agents;  /* algorithmic bytes of the agent kernel alone */
     double ms_total;           /* device time of the whole epoch, CUDA events */
@@ -233,7 +233,8 @@ pg_status pg_copy_edges(pg_ctx* ctx, int32_t replica, int64_t first, int64_t cou
                         int32_t* src, int32_t* dst);
 pg_status pg_copy_degrees(pg_ctx* ctx, int32_t replica, int32_t* indeg, int32_t* outdeg);
 pg_status pg_copy_nodes(pg_ctx* ctx, int32_t replica, int32_t* pub_epoch, float* fitness);
-/* which: 0 forward (out-edges), 1 backward (in-edges).  off has n+1 entries, col m. */
+/* which: 0 forward (out-edges), 1 backward (in-edges).  off has n+1 entries, col m.  The backward
+ * rows are kept with room to grow in the device arena; this returns them compacted in node order. */
 pg_status pg_copy_csr(pg_ctx* ctx, int32_t replica, int32_t which, int64_t* off, int32_t* col);
 /* Citations of the last epoch in arrival order ([count] as from pg_epoch_edges); needs
  * record_trace. */
@@ -296,7 +297,7 @@ typedef struct {
     int32_t agent_ctas_per_sm; /* CTAs per SM of the k <= 64 agent kernel; 0 = occupancy limit */
     int32_t small_hash;        /* shape of that kernel: 0 a 2048-slot frontier hash per warp and
                                   512-entry stage buffers; 1 1024 slots, 1024-entry stages */
-    int32_t copy_ctas_per_sm;  /* CTAs per SM of the backward-CSR copy; 0 = default (8) */
+    int32_t copy_ctas_per_sm;  /* CTAs per SM of the copy of moved backward rows; 0 = default (8) */
     int32_t lik_chunk_agents;  /* > 0: pg_trace_load keeps at most this many agents' neighbourhood
                                   balls per chunk, so every likelihood pass rebuilds them chunk by
                                   chunk; 0: as many as fit in a quarter of free device memory (one

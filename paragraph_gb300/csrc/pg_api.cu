@@ -959,9 +959,11 @@ int64_t agent_bytes(bool thin, int64_t rows, int64_t elems, int64_t draws, int64
     return 32 * rows + 8 * elems + 32 * draws + 16 * edges;
 }
 int64_t weight_bytes(int64_t nodes) { return 44 * nodes; }
-int64_t csr_bytes(int64_t moved, int64_t edges, int64_t nodes, int64_t new_nodes) {
-    return 8 * moved + 12 * edges + 24 * (nodes + new_nodes);
-}
+// backward append: 8 B per entry of a row that moved (read and written), 32 B per new edge (its
+// target and rank read by the grow and place passes, its row's start of new entries read, the entry
+// written, its cited row's length, room and in-degree updated at most once per edge), 40 B per new
+// node (its hub mask and slot, its row)
+int64_t csr_bytes(int64_t moved, int64_t edges, int64_t new_nodes) { return 8 * moved + 32 * edges + 40 * new_nodes; }
 
 void fill_stats(pg_ctx* c, int64_t new_nodes, bool er) {
     pg_stats& S = c->stats;
@@ -982,7 +984,7 @@ void fill_stats(pg_ctx* c, int64_t new_nodes, bool er) {
     // ER: per edge 8 B edge-list write + 12 B CSR append; per new node 32 B (count + offsets)
     S.bytes_alg = er ? (8 * E + 12 * E + 32 * new_nodes + 8 * S.bwd_moved)
                      : ab + weight_bytes(S.nodes_weighted) +
-                           csr_bytes(S.bwd_moved, E, S.nodes_weighted, new_nodes);
+                           csr_bytes(S.bwd_moved, E, new_nodes);
 }
 
 pg_status finish_epoch(pg_ctx* c, const std::vector<int64_t>& deltas, bool er) {
@@ -1436,7 +1438,7 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
                                          S.run_elems_streamed, S.run_draws, S.run_new_edges,
                                          S.run_adj_scanned);
     S.run_bytes_alg = S.run_bytes_alg_agents + weight_bytes(S.run_nodes_weighted) +
-                      csr_bytes(S.run_bwd_moved, S.run_new_edges, S.run_nodes_weighted, S.run_new_nodes);
+                      csr_bytes(S.run_bwd_moved, S.run_new_edges, S.run_new_nodes);
     S.run_kernel_launches = c->launches;
     S.run_ms_weights = S.run_ms_setup = S.run_ms_agents = S.run_ms_csr = 0.0;
     if (events) {

@@ -319,8 +319,9 @@ __device__ __forceinline__ void d_sort_large(const Arena& A, uint32_t* bm, int64
 }
 
 // bm_words: the bitmap of this launch (dynamic shared memory), enough for the epoch's new-id range
-// where that fits, so several CTAs share an SM
-__global__ void __launch_bounds__(256) k_sort_large(Arena A, int64_t bm_words) {
+// where that fits, so two CTAs share an SM.  1024 threads per CTA: a hub's row can take tens of
+// thousands of new entries in one epoch, and that one row sets the kernel's length.
+__global__ void __launch_bounds__(1024) k_sort_large(Arena A, int64_t bm_words) {
     extern __shared__ uint32_t bm[];
     d_sort_large(A, bm, bm_words);
 }
@@ -376,7 +377,7 @@ void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t
     // a replica's new ids span at most the epoch's agents
     int64_t words = (agents + 31) / 32 + 1;
     if (words > kBitmapWords) words = kBitmapWords;
-    k_sort_large<<<(unsigned)num_sms * 4, 256, (size_t)words * 4, s>>>(A, words);
+    k_sort_large<<<(unsigned)num_sms * 2, 1024, (size_t)words * 4, s>>>(A, words);
     if (two) cudaStreamWaitEvent(s, join, 0);
     k_epoch_end<<<1, 256, 0, s>>>(A, agents);
 }
