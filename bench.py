@@ -799,7 +799,7 @@ def run_small_configs(args) -> None:
         print(json.dumps({
             "metric": "citation edges/sec (ER G(n,p) growth)", "value": edges / (ms / 1000.0),
             "unit": "citations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True, "dtype": "int32/f64 skips",
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "dtype": "int32/f32 skips (f64 near integers)",
             "data": "synthetic", "config": {"workload": "er_100k_seed_10x10000", "p": p},
             "timing": "10 epochs enqueued without host synchronisation (pg_run_er_epochs), device events around the step",
             "cpu_baseline": {"value": cpu_edges / cpu_s, "unit": "citations/s", "cores": threads,

@@ -306,6 +306,10 @@ typedef struct {
                                   ONE persistent cooperative kernel over all replicas (every stage
                                   a phase, grid barriers between them); 0: the sequence of stage
                                   kernels.  Ignored (0) where the device cannot launch it. */
+    int32_t er_slot_sigmas;    /* ER: each (new node, 2^16-id chunk) walk writes its edges into slots
+                                  reserved for mean + this many standard deviations + 8 of its
+                                  binomial count (0 = default 8); a walk with more edges finishes in
+                                  an overflow pass.  Small values send many walks there (tests). */
 } pg_tuning;
 pg_status pg_set_tuning(pg_ctx* ctx, const pg_tuning* tuning);
 pg_status pg_get_tuning(const pg_ctx* ctx, pg_tuning* tuning);

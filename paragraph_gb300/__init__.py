@@ -116,7 +116,7 @@ class _AttrRows(C.Structure):
 class _Tuning(C.Structure):
     _fields_ = [("agent_ctas_per_sm", C.c_int32), ("small_hash", C.c_int32),
                 ("copy_ctas_per_sm", C.c_int32), ("lik_chunk_agents", C.c_int32),
-                ("epoch_kernel", C.c_int32)]
+                ("epoch_kernel", C.c_int32), ("er_slot_sigmas", C.c_int32)]
 
 
 class _TraceDesc(C.Structure):
@@ -560,10 +560,13 @@ class GrowthEngine:
         self._check(self._lib.pg_restore(self._ctx))
 
     def set_tuning(self, agent_ctas_per_sm: int = 0, small_hash: int = 0,
-                   copy_ctas_per_sm: int = 0, lik_chunk_agents: int = 0, epoch_kernel: int = 0) -> None:
-        """Launch shape of the agent and backward-copy kernels, and the likelihood's ball chunking
-        (results never depend on them)."""
-        t = _Tuning(agent_ctas_per_sm, small_hash, copy_ctas_per_sm, lik_chunk_agents, epoch_kernel)
+                   copy_ctas_per_sm: int = 0, lik_chunk_agents: int = 0, epoch_kernel: int = 0,
+                   er_slot_sigmas: int = 0) -> None:
+        """Launch shape of the agent and moved-row copy kernels, the likelihood's ball chunking,
+        one persistent kernel per epoch, and the ER walks' slot reservation (results never depend
+        on them)."""
+        t = _Tuning(agent_ctas_per_sm, small_hash, copy_ctas_per_sm, lik_chunk_agents, epoch_kernel,
+                    er_slot_sigmas)
         self._check(self._lib.pg_set_tuning(self._ctx, C.byref(t)))
 
     def set_wait_limit(self, polls: int) -> None:

@@ -114,6 +114,8 @@ struct pg_ctx {
     DBuf<int32_t> fwd_col, bcol, bcap;
     DBuf<BRow> brow;
     DBuf<longlong2> reloc;  // copy tasks of the backward rows that move in an epoch
+    DBuf<int2> er_slots, er_ov;  // ER walks: (position, rank) slots of every task, overflow area
+    DBuf<int64_t> er_ovb;        // ER walks: start of each overflowing task's block
     DBuf<int32_t> src_tmp;  // sources of an edge range being copied out
     // refcompat functor
     DBuf<double> rc_pa, rc_rec, rc_fit, rc_rtab, rc_agent;
@@ -1118,6 +1120,9 @@ void pg_destroy(pg_ctx* c) {
     for (auto* b : i32) dfree(*b);
     dfree(c->brow);
     dfree(c->reloc);
+    dfree(c->er_slots);
+    dfree(c->er_ov);
+    dfree(c->er_ovb);
     DBuf<int64_t>* i64[] = {&c->fwd_off, &c->len_tmp,
                             &c->sort_small, &c->sort_large, &c->sort_large_off, &c->eoff,
                             &c->blocksum, &c->er_cnt, &c->er_toff};
@@ -1461,6 +1466,29 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
     return PG_OK;
 }
 
+namespace {
+// Buffers of ER epochs with at most `tasks` walks and `slots` reserved slots.
+pg_status ensure_er_buffers(pg_ctx* c, int64_t tasks, int64_t slots) {
+    if (c->er_cnt.n < tasks + 1) PG_CUDA(c, dalloc(c->er_cnt, tasks + 1));
+    if (c->er_toff.n < tasks + 1) PG_CUDA(c, dalloc(c->er_toff, tasks + 1));
+    if (c->er_ovb.n < tasks) PG_CUDA(c, dalloc(c->er_ovb, std::max<int64_t>(tasks, 1)));
+    if (c->er_slots.n < slots) PG_CUDA(c, dalloc(c->er_slots, std::max<int64_t>(slots, 1)));
+    const int64_t ov = std::max<int64_t>(slots, 1 << 16);
+    if (c->er_ov.n < ov) PG_CUDA(c, dalloc(c->er_ov, ov));
+    return PG_OK;
+}
+ErBuffers er_buffers(pg_ctx* c) {
+    ErBuffers B;
+    B.cnt = c->er_cnt.p;
+    B.toff = c->er_toff.p;
+    B.slots = c->er_slots.p;
+    B.ov = c->er_ov.p;
+    B.ov_cap = c->er_ov.n;
+    B.ovb = c->er_ovb.p;
+    return B;
+}
+}  // namespace
+
 pg_status pg_er_epoch(pg_ctx* c, int64_t delta, double p, int64_t* new_edges) {
     if (!c) return PG_ERR_ARG;
     if (!c->loaded) return fail(c, PG_ERR_STATE, "no graph loaded");
@@ -1481,13 +1509,14 @@ pg_status pg_er_epoch(pg_ctx* c, int64_t delta, double p, int64_t* new_edges) {
     if (s != PG_OK) return s;
     s = alloc_epoch_buffers(c, delta, eb, tasks);
     if (s != PG_OK) return s;
-    if (c->er_cnt.n < tasks + 1) PG_CUDA(c, dalloc(c->er_cnt, tasks + 1));
-    if (c->er_toff.n < tasks + 1) PG_CUDA(c, dalloc(c->er_toff, tasks + 1));
+    const ErPlan plan = er_plan(n, delta, p, c->tune.er_slot_sigmas);
+    s = ensure_er_buffers(c, plan.tasks, delta * plan.per_node);
+    if (s != PG_OK) return s;
     Arena A = make_arena(c);
     cudaStream_t st = c->stream;
     if (c->timing) cudaEventRecord(c->ev[0], st);
     launch_epoch_begin_delta(A, c->epoch, delta, st);
-    launch_er_epoch(A, delta, p, n, c->er_cnt.p, c->er_toff.p, c->num_sms, st);
+    launch_er_epoch(A, delta, p, plan, er_buffers(c), c->num_sms, st);
     if (c->timing) cudaEventRecord(c->ev[1], st);
     launch_bwd_append(A, delta, c->num_sms, st, c->side, c->fork, c->join);
     if (c->timing) cudaEventRecord(c->ev[2], st);
@@ -1516,21 +1545,24 @@ pg_status pg_run_er_epochs(pg_ctx* c, int32_t num_epochs, int64_t delta, double 
     const int64_t n0 = c->hrep[0].n, m0 = c->hrep[0].m;
     const double pe = p > 0.0 ? p : 0.0;
     // every epoch's node count is known; edges are bounded per epoch by mean + 8 sigma
-    int64_t need_m = m0, max_eb = 0, max_tasks = 0;
+    int64_t need_m = m0, max_eb = 0, max_tasks = 0, max_slots = 0;
+    std::vector<ErPlan> plans((size_t)num_epochs);
     for (int e = 0; e < num_epochs; ++e) {
         const int64_t n = n0 + (int64_t)e * delta;
         const double mu = (double)delta * (double)n * pe;
         const int64_t eb = std::min<int64_t>((int64_t)std::ceil(mu + 8.0 * std::sqrt(mu) + 1024.0), delta * n);
         need_m += eb;
         max_eb = std::max(max_eb, eb);
-        max_tasks = std::max(max_tasks, delta * ((n + kErChunk - 1) / kErChunk));
+        plans[(size_t)e] = er_plan(n, delta, p, c->tune.er_slot_sigmas);
+        max_tasks = std::max(max_tasks, plans[(size_t)e].tasks);
+        max_slots = std::max(max_slots, delta * plans[(size_t)e].per_node);
     }
     pg_status s = ensure_capacity(c, n0 + (int64_t)num_epochs * delta, need_m);
     if (s != PG_OK) return s;
     s = alloc_epoch_buffers(c, delta, max_eb, max_tasks);
     if (s != PG_OK) return s;
-    if (c->er_cnt.n < max_tasks + 1) PG_CUDA(c, dalloc(c->er_cnt, max_tasks + 1));
-    if (c->er_toff.n < max_tasks + 1) PG_CUDA(c, dalloc(c->er_toff, max_tasks + 1));
+    s = ensure_er_buffers(c, max_tasks, max_slots);
+    if (s != PG_OK) return s;
     cudaStream_t st = c->stream;
     const size_t cum0 = offsetof(EpochState, cum_rows_expanded);
     PG_CUDA(c, cudaMemsetAsync(reinterpret_cast<char*>(c->st.p) + cum0, 0, sizeof(EpochState) - cum0, st));
@@ -1539,7 +1571,7 @@ pg_status pg_run_er_epochs(pg_ctx* c, int32_t num_epochs, int64_t delta, double 
     for (int e = 0; e < num_epochs; ++e) {
         Arena A = make_arena(c);
         launch_epoch_begin_delta(A, c->epoch + e, delta, st);
-        launch_er_epoch(A, delta, p, n0 + (int64_t)e * delta, c->er_cnt.p, c->er_toff.p, c->num_sms, st);
+        launch_er_epoch(A, delta, p, plans[(size_t)e], er_buffers(c), c->num_sms, st);
         launch_bwd_append(A, delta, c->num_sms, st, c->side, c->fork, c->join);
     }
     if (c->timing) cudaEventRecord(c->ev[1], st);
@@ -1825,7 +1857,7 @@ pg_status pg_set_tuning(pg_ctx* c, const pg_tuning* t) {
     if (!c) return PG_ERR_ARG;
     if (!t || t->agent_ctas_per_sm < 0 || t->agent_ctas_per_sm > 32 || t->copy_ctas_per_sm < 0 ||
         t->copy_ctas_per_sm > 64 || (t->small_hash != 0 && t->small_hash != 1) || t->lik_chunk_agents < 0 ||
-        (t->epoch_kernel != 0 && t->epoch_kernel != 1))
+        (t->epoch_kernel != 0 && t->epoch_kernel != 1) || t->er_slot_sigmas < 0 || t->er_slot_sigmas > 64)
         return fail(c, PG_ERR_ARG, "tuning out of range");
     if (std::memcmp(&c->tune, t, sizeof(pg_tuning)) != 0) {
         c->tune = *t;

@@ -139,6 +139,7 @@ struct EpochState {
     unsigned long long bwd_moved;
     unsigned long long nodes_weighted;
     unsigned long long reloc_count; // copy tasks of the backward rows that moved this epoch
+    unsigned long long er_ov_count; // ER: overflow-area entries taken this epoch
     unsigned long long adj_scanned; // adjacency entries examined by membership tests
     // run totals, accumulated by the epoch-end kernel and cleared by the host at run start
     unsigned long long cum_rows_expanded;
@@ -419,8 +420,23 @@ void launch_rc_scores(const Arena& A, cudaStream_t s);
 void launch_rc_big(const Arena& A, int num_sms, cudaStream_t s);
 void launch_rc_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
 cudaError_t init_rc_kernels();
-void launch_er_epoch(const Arena& A, int64_t delta, double p, int64_t n, int64_t* cnt,
-                     int64_t* toff, int num_sms, cudaStream_t s);
+// ER epoch plan: tasks are (new node, 2^16-id chunk) pairs over n existing nodes; each task owns
+// s_full slots (s_last for the last chunk), laid out per_node apart
+struct ErPlan {
+    int64_t n, chunks, tasks;
+    int64_t s_full, s_last, per_node;
+};
+ErPlan er_plan(int64_t n, int64_t delta, double p, int sigmas);
+struct ErBuffers {
+    int64_t* cnt;    // [tasks + 1] successes per task
+    int64_t* toff;   // [tasks + 1] their exclusive scan
+    int2* slots;     // [delta * per_node] (position, rank) of each task's first successes
+    int2* ov;        // [ov_cap] the excess of the tasks that overflowed
+    int64_t ov_cap;
+    int64_t* ovb;    // [tasks] start of a task's overflow block
+};
+void launch_er_epoch(const Arena& A, int64_t delta, double p, const ErPlan& P, const ErBuffers& B, int num_sms,
+                     cudaStream_t s);
 // the skip constants of probability p (host)
 ErSkip er_skip_constants(double p);
 // generic exclusive scan of n values; out has n+1 entries (out[n] = total)

@@ -7,9 +7,13 @@
 // Work is O(edges): the gap to the next success is floor(log(u) / log(1-p)).  The id range of each
 // new node is cut into 2^16-id chunks with their own Philox stream, so a (node, chunk) task is
 // independent of how tasks are spread over threads; where a chunk expects several successes a
-// group of lanes walks it, drawing consecutive gaps together.  A count pass, an exclusive scan and
-// an emit pass that replays the same streams write the edges in (source, target) order with no
-// sort.
+// group of lanes walks it, drawing consecutive gaps together.  Every skip is walked once: each task
+// owns a block of slots sized for its binomial count (mean + sigmas standard deviations + 8, laid
+// out in closed form: all full chunks have the same size), the walk writes each success's position
+// and in-degree rank there and counts exactly; a task with more successes than slots (with the
+// default 8 sigmas, about never) is walked again by the overflow pass, which writes only its excess
+// into an overflow area.  A scan of the counts and a compaction pass then write the edges in
+// (source, target) order with no sort.
 // The skip is floor(log(u) / log(1 - p)) with the library's own fp64 log, so the edge list is
 // bit-identical to the CPU oracle; an fp32 estimate with a proven error bound decides almost every
 // skip and the FP64 expression runs only when an integer lies within that bound (er_skip).
@@ -19,9 +23,22 @@ namespace pg {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-__device__ __forceinline__ int64_t er_walk(const Arena& A, int64_t i, int64_t c, int64_t n,
-                                           const ErSkip& K, int32_t* out, int64_t out_base,
-                                           int32_t* col_out, int64_t col_base) {
+__device__ __forceinline__ int64_t er_slots_of(const ErPlan& P, int64_t c) { return c == P.chunks - 1 ? P.s_last : P.s_full; }
+__device__ __forceinline__ int64_t er_base_of(const ErPlan& P, int64_t i, int64_t c) { return i * P.per_node + c * P.s_full; }
+
+// One success of a task: its k-th edge at position pos, with its rank among the node's new entries.
+// Edges k < S go to the task's slots (pass 1), the others to its overflow block (overflow pass).
+__device__ __forceinline__ void er_put(const Arena& A, int64_t k, int64_t pos, int64_t S, int2* slots, int64_t sbase,
+                                       int2* ov, int64_t obase) {
+    if (slots && k < S)
+        slots[sbase + k] = make_int2((int32_t)pos, atomicAdd(&A.inc[A.rep[0].nbase + pos], 1));
+    else if (ov && k >= S)
+        ov[obase + k - S] = make_int2((int32_t)pos, atomicAdd(&A.inc[A.rep[0].nbase + pos], 1));
+}
+
+// One thread walks task (i, c): returns its successes.
+__device__ __forceinline__ int64_t er_walk(const Arena& A, int64_t i, int64_t c, int64_t n, const ErSkip& K,
+                                           int64_t S, int2* slots, int64_t sbase, int2* ov, int64_t obase) {
     const int64_t lo = c * kErChunk;
     const int64_t hi = lo + kErChunk < n ? lo + kErChunk : n;
     int64_t pos = lo - 1, cnt = 0;
@@ -34,11 +51,7 @@ __device__ __forceinline__ int64_t er_walk(const Arena& A, int64_t i, int64_t c,
         const double sk = (d & 1u) ? er_skip(K, x.x[2], x.x[3], (float)rem) : er_skip(K, x.x[0], x.x[1], (float)rem);
         if (sk >= rem) break;
         pos = pos + 1 + (int64_t)sk;
-        if (out) {
-            out[out_base + cnt] = (int32_t)pos;
-            col_out[col_base + cnt] = (int32_t)pos;
-            A.e_rank[out_base + cnt] = atomicAdd(&A.inc[A.rep[0].nbase + pos], 1);
-        }
+        er_put(A, cnt, pos, S, slots, sbase, ov, obase);
         ++cnt;
     }
     return cnt;
@@ -56,13 +69,14 @@ __global__ void __launch_bounds__(256) k_er_setup(Arena A, int64_t delta) {
     A.indeg[slot] = 0;
 }
 
-__global__ void __launch_bounds__(256) k_er_count(Arena A, int64_t tasks, int64_t chunks,
-                                                  ErSkip K, int64_t* cnt) {
+__global__ void __launch_bounds__(256) k_er_walk(Arena A, ErPlan P, ErSkip K, int64_t* cnt, int2* slots) {
     if (A.st->error) return;
     const int64_t n = A.rep[0].n;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tasks;
-         t += (int64_t)gridDim.x * blockDim.x)
-        cnt[t] = er_walk(A, t / chunks, t % chunks, n, K, nullptr, 0, nullptr, 0);
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < P.tasks;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / P.chunks, c = t % P.chunks;
+        cnt[t] = er_walk(A, i, c, n, K, er_slots_of(P, c), slots, er_base_of(P, i, c), nullptr, 0);
+    }
 }
 
 __global__ void k_er_check(Arena A, const int64_t* toff, int64_t tasks) {
@@ -73,20 +87,23 @@ __global__ void k_er_check(Arena A, const int64_t* toff, int64_t tasks) {
     if (E > A.edge_cap || rp.m + E > rp.m_cap) atomicOr(&A.st->error, kErrCapacity);
 }
 
-__global__ void __launch_bounds__(256) k_er_emit(Arena A, int64_t tasks, int64_t chunks,
-                                                 ErSkip K, const int64_t* toff) {
+// The tasks with more successes than slots walk again (one thread each: they are rare) and write
+// only their excess, into blocks of the overflow area reserved here.
+__global__ void __launch_bounds__(256) k_er_overflow(Arena A, ErPlan P, ErSkip K, const int64_t* cnt, int2* ov,
+                                                     int64_t ov_cap, int64_t* ovb) {
     if (A.st->error) return;
-    const Replica& rp = A.rep[0];
-    const int64_t n = rp.n;
-    int32_t* fcol = A.fwd_col + rp.ebase;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tasks;
+    const int64_t n = A.rep[0].n;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < P.tasks;
          t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = t / chunks, c = t % chunks;
-        const int64_t e0 = toff[t];
-        const int64_t cnt = er_walk(A, i, c, n, K, A.e_dst, e0, fcol, rp.m + e0);
-        if (A.arrivals)
-            for (int64_t q = 0; q < cnt; ++q) A.arrivals[e0 + q] = A.e_dst[e0 + q];
-        if (c == chunks - 1) A.fwd_off[rp.obase + n + i + 1] = rp.m + e0 + cnt;
+        const int64_t c = t % P.chunks, S = er_slots_of(P, c);
+        if (cnt[t] <= S) continue;
+        const int64_t ob = (int64_t)atomicAdd(&A.st->er_ov_count, (unsigned long long)(cnt[t] - S));
+        if (ob + cnt[t] - S > ov_cap) {
+            atomicOr(&A.st->error, kErrCapacity);
+            continue;
+        }
+        ovb[t] = ob;
+        er_walk(A, t / P.chunks, c, n, K, S, nullptr, 0, ov, ob);
     }
 }
 
@@ -97,8 +114,7 @@ __global__ void __launch_bounds__(256) k_er_emit(Arena A, int64_t tasks, int64_t
 // stays in the loop until all of its groups are done (the shuffles span the warp).
 template <int G>
 __device__ __forceinline__ int64_t er_walk_group(const Arena& A, bool live, int64_t i, int64_t c, int64_t n,
-                                                 const ErSkip& K, int32_t* out, int64_t out_base,
-                                                 int32_t* col_out, int64_t col_base) {
+                                                 const ErSkip& K, int64_t S, int2* slots, int64_t sbase) {
     const int lane = lane_id(), gl = lane & (G - 1);
     const unsigned gm = G == 32 ? kFull : (((1u << G) - 1u) << (lane & ~(G - 1)));
     const int64_t lo = c * kErChunk;
@@ -124,13 +140,7 @@ __device__ __forceinline__ int64_t er_walk_group(const Arena& A, bool live, int6
         const int64_t q = pos + incl;
         const bool ok = act && q < hi;  // a prefix of the group: positions increase along it
         const int nok = __popc(__ballot_sync(kFull, ok) & gm);
-        if (ok && out) {
-            const int64_t e = out_base + cnt + gl;
-            out[e] = (int32_t)q;
-            col_out[col_base + cnt + gl] = (int32_t)q;
-            A.e_rank[e] = atomicAdd(&A.inc[A.rep[0].nbase + q], 1);
-            if (A.arrivals) A.arrivals[e] = (int32_t)q;
-        }
+        if (ok) er_put(A, cnt + gl, q, S, slots, sbase, nullptr, 0);
         cnt += nok;
         pos = __shfl_sync(kFull, q, G - 1, G);
         if (nok < G) act = false;
@@ -139,40 +149,50 @@ __device__ __forceinline__ int64_t er_walk_group(const Arena& A, bool live, int6
 }
 
 template <int G>
-__global__ void __launch_bounds__(256) k_er_count_g(Arena A, int64_t tasks, int64_t chunks, ErSkip K,
-                                                    int64_t* cnt) {
+__global__ void __launch_bounds__(256) k_er_walk_g(Arena A, ErPlan P, ErSkip K, int64_t* cnt, int2* slots) {
     if (A.st->error) return;
     const int64_t n = A.rep[0].n;
     constexpr int per = 32 / G;  // tasks per warp and round
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t b = warp * per; b < tasks; b += nwarps * per) {
+    for (int64_t b = warp * per; b < P.tasks; b += nwarps * per) {
         const int64_t t = b + (lane_id() / G);
-        const bool live = t < tasks;
+        const bool live = t < P.tasks;
         const int64_t tt = live ? t : 0;
-        const int64_t c0 = er_walk_group<G>(A, live, tt / chunks, tt % chunks, n, K, nullptr, 0, nullptr, 0);
+        const int64_t i = tt / P.chunks, c = tt % P.chunks;
+        const int64_t c0 = er_walk_group<G>(A, live, i, c, n, K, er_slots_of(P, c), slots, er_base_of(P, i, c));
         if (live && (lane_id() & (G - 1)) == 0) cnt[t] = c0;
     }
 }
 
+// The edges of every task at their place in the epoch's edge list and the new forward rows, G lanes
+// per task (G = 1: one thread), from its slots and, past them, its overflow block.
 template <int G>
-__global__ void __launch_bounds__(256) k_er_emit_g(Arena A, int64_t tasks, int64_t chunks, ErSkip K,
-                                                   const int64_t* toff) {
+__global__ void __launch_bounds__(256) k_er_place(Arena A, ErPlan P, const int64_t* cnt, const int64_t* toff,
+                                                  const int2* slots, const int2* ov, const int64_t* ovb) {
     if (A.st->error) return;
     const Replica& rp = A.rep[0];
     const int64_t n = rp.n;
-    int32_t* fcol = A.fwd_col + rp.ebase;
+    int32_t* fcol = A.fwd_col + rp.ebase + rp.m;
     constexpr int per = 32 / G;
+    const int gl = lane_id() & (G - 1);
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t b = warp * per; b < tasks; b += nwarps * per) {
+    for (int64_t b = warp * per; b < P.tasks; b += nwarps * per) {
         const int64_t t = b + (lane_id() / G);
-        const bool live = t < tasks;
-        const int64_t tt = live ? t : 0;
-        const int64_t i = tt / chunks, c = tt % chunks;
-        const int64_t e0 = toff[tt];
-        const int64_t cnt = er_walk_group<G>(A, live, i, c, n, K, A.e_dst, e0, fcol, rp.m + e0);
-        if (live && (lane_id() & (G - 1)) == 0 && c == chunks - 1) A.fwd_off[rp.obase + n + i + 1] = rp.m + e0 + cnt;
+        if (t >= P.tasks) continue;
+        const int64_t i = t / P.chunks, c = t % P.chunks;
+        const int64_t S = er_slots_of(P, c), sb = er_base_of(P, i, c), k1 = cnt[t], e0 = toff[t];
+        const int64_t ob = k1 > S ? ovb[t] : 0;
+        for (int64_t k = gl; k < k1; k += G) {
+            const int2 v = k < S ? slots[sb + k] : ov[ob + k - S];
+            const int64_t e = e0 + k;
+            A.e_dst[e] = v.x;
+            A.e_rank[e] = v.y;
+            fcol[e] = v.x;
+            if (A.arrivals) A.arrivals[e] = v.x;
+        }
+        if (gl == 0 && c == P.chunks - 1) A.fwd_off[rp.obase + n + i + 1] = rp.m + e0 + k1;
     }
 }
 
@@ -192,45 +212,65 @@ ErSkip er_skip_constants(double p) {
     return K;
 }
 
-// Count, scan and emit; the caller then runs the backward append.
-void launch_er_epoch(const Arena& A, int64_t delta, double p, int64_t n, int64_t* cnt,
-                     int64_t* toff, int num_sms, cudaStream_t s) {
-    const int64_t chunks = (n + kErChunk - 1) / kErChunk;
-    const int64_t tasks = delta * chunks;
+ErPlan er_plan(int64_t n, int64_t delta, double p, int sigmas) {
+    ErPlan P;
+    P.n = n;
+    P.chunks = n > 0 ? (n + kErChunk - 1) / kErChunk : 0;
+    P.tasks = delta * P.chunks;
+    const int sg = sigmas > 0 ? sigmas : 8;
+    const double q = p < 0.0 ? 0.0 : (p > 1.0 ? 1.0 : p);
+    auto slots = [&](int64_t len) -> int64_t {
+        const double mu = (double)len * q;
+        const double sd = sqrt(mu * (1.0 - q));
+        int64_t s = (int64_t)ceil(mu + sg * sd) + 8;
+        return s < len ? s : len;
+    };
+    P.s_full = slots(kErChunk);
+    P.s_last = P.chunks > 0 ? slots(n - (P.chunks - 1) * kErChunk) : 0;
+    P.per_node = P.chunks > 0 ? (P.chunks - 1) * P.s_full + P.s_last : 0;
+    return P;
+}
+
+// Walk (counts and slots), scan, overflow, placement; the caller then runs the backward append.
+void launch_er_epoch(const Arena& A, int64_t delta, double p, const ErPlan& P, const ErBuffers& B, int num_sms,
+                     cudaStream_t s) {
     k_er_setup<<<(unsigned)((delta + 255) / 256), 256, 0, s>>>(A, delta);
-    if (!(p > 0.0)) {  // no edges: zero offsets keep the CSR append consistent
-        cudaMemsetAsync(toff, 0, sizeof(int64_t) * (size_t)(tasks + 1), s);
-        k_er_check<<<1, 32, 0, s>>>(A, toff, tasks);
-        k_er_eoff<<<(unsigned)((delta + 256) / 256), 256, 0, s>>>(A, toff, delta, chunks);
+    if (!(p > 0.0) || P.tasks == 0) {  // no edges: zero offsets keep the CSR append consistent
+        cudaMemsetAsync(B.toff, 0, sizeof(int64_t) * (size_t)(P.tasks + 1), s);
+        k_er_check<<<1, 32, 0, s>>>(A, B.toff, P.tasks);
+        k_er_eoff<<<(unsigned)((delta + 256) / 256), 256, 0, s>>>(A, B.toff, delta, P.chunks);
         return;
     }
     const ErSkip K = er_skip_constants(p);
     // lanes per task: about the expected successes of a full chunk (1: one thread walks a task)
-    const double mu = (double)(n < kErChunk ? n : kErChunk) * (p < 1.0 ? p : 1.0);
+    const double mu = (double)(P.n < kErChunk ? P.n : kErChunk) * (p < 1.0 ? p : 1.0);
     int G = 1;
     while (G < 32 && G < mu) G <<= 1;
-    int64_t g = (tasks * G + 255) / 256;
+    int64_t g = (P.tasks * G + 255) / 256;
     if (g > (int64_t)num_sms * 32) g = (int64_t)num_sms * 32;
     if (g < 1) g = 1;
     switch (G) {
-        case 1: k_er_count<<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
-        case 2: k_er_count_g<2><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
-        case 4: k_er_count_g<4><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
-        case 8: k_er_count_g<8><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
-        case 16: k_er_count_g<16><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
-        default: k_er_count_g<32><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, cnt); break;
+        case 1: k_er_walk<<<(unsigned)g, 256, 0, s>>>(A, P, K, B.cnt, B.slots); break;
+        case 2: k_er_walk_g<2><<<(unsigned)g, 256, 0, s>>>(A, P, K, B.cnt, B.slots); break;
+        case 4: k_er_walk_g<4><<<(unsigned)g, 256, 0, s>>>(A, P, K, B.cnt, B.slots); break;
+        case 8: k_er_walk_g<8><<<(unsigned)g, 256, 0, s>>>(A, P, K, B.cnt, B.slots); break;
+        case 16: k_er_walk_g<16><<<(unsigned)g, 256, 0, s>>>(A, P, K, B.cnt, B.slots); break;
+        default: k_er_walk_g<32><<<(unsigned)g, 256, 0, s>>>(A, P, K, B.cnt, B.slots); break;
     }
-    launch_scan_i64(cnt, toff, tasks, A.blocksum, s);
-    k_er_check<<<1, 32, 0, s>>>(A, toff, tasks);
+    launch_scan_i64(B.cnt, B.toff, P.tasks, A.blocksum, s);
+    k_er_check<<<1, 32, 0, s>>>(A, B.toff, P.tasks);
+    int64_t go = (P.tasks + 255) / 256;
+    if (go > (int64_t)num_sms * 8) go = (int64_t)num_sms * 8;
+    k_er_overflow<<<(unsigned)go, 256, 0, s>>>(A, P, K, B.cnt, B.ov, B.ov_cap, B.ovb);
     switch (G) {
-        case 1: k_er_emit<<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
-        case 2: k_er_emit_g<2><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
-        case 4: k_er_emit_g<4><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
-        case 8: k_er_emit_g<8><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
-        case 16: k_er_emit_g<16><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
-        default: k_er_emit_g<32><<<(unsigned)g, 256, 0, s>>>(A, tasks, chunks, K, toff); break;
+        case 1: k_er_place<1><<<(unsigned)g, 256, 0, s>>>(A, P, B.cnt, B.toff, B.slots, B.ov, B.ovb); break;
+        case 2: k_er_place<2><<<(unsigned)g, 256, 0, s>>>(A, P, B.cnt, B.toff, B.slots, B.ov, B.ovb); break;
+        case 4: k_er_place<4><<<(unsigned)g, 256, 0, s>>>(A, P, B.cnt, B.toff, B.slots, B.ov, B.ovb); break;
+        case 8: k_er_place<8><<<(unsigned)g, 256, 0, s>>>(A, P, B.cnt, B.toff, B.slots, B.ov, B.ovb); break;
+        case 16: k_er_place<16><<<(unsigned)g, 256, 0, s>>>(A, P, B.cnt, B.toff, B.slots, B.ov, B.ovb); break;
+        default: k_er_place<32><<<(unsigned)g, 256, 0, s>>>(A, P, B.cnt, B.toff, B.slots, B.ov, B.ovb); break;
     }
-    k_er_eoff<<<(unsigned)((delta + 256) / 256), 256, 0, s>>>(A, toff, delta, chunks);
+    k_er_eoff<<<(unsigned)((delta + 256) / 256), 256, 0, s>>>(A, B.toff, delta, P.chunks);
 }
 
 }  // namespace pg

@@ -24,6 +24,7 @@ __device__ __forceinline__ void d_epoch_begin(const Arena& A, int64_t epoch, int
     if (threadIdx.x == 0) {
         carry = 0;
         st->reloc_count = 0;
+        st->er_ov_count = 0;
         st->epoch = epoch;
         st->edges = 0;
         st->queue_small = 0;

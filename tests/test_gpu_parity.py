@@ -104,6 +104,39 @@ def test_er_bit_exact(gpu, p):
             assert og.m == delta * n0 + delta * (n0 + delta)
 
 
+@pytest.mark.parametrize("p", [2e-4, 1e-3, 5e-3])
+def test_er_overflow_pass_bit_exact(gpu, p):
+    """Each ER walk writes its edges into slots reserved for its binomial count; with the
+    reservation cut to one standard deviation (er_slot_sigmas=1) a few per cent of the walks have
+    more edges than slots and finish in the overflow pass.  The edges are still the oracle's, bit
+    for bit, and this test checks that walks did overflow."""
+    n0, delta = 100_000, 2000
+    s = W.er_seed(n0)
+    with GrowthEngine(seed=17) as eng:
+        eng.load_graph(s.pub, s.fitness, s.src, s.dst)
+        eng.set_tuning(er_slot_sigmas=1)
+        og = O.OracleGraph(17, 0)
+        og.load(s.pub, s.fitness, s.src, s.dst)
+        over = 0
+        for _ in range(2):
+            n = og.n
+            ne = eng.er_epoch(delta, p)
+            og.er_epoch(delta, p)
+            assert ne == og.epoch_edges()[1]
+            src, dst = og.last_epoch_edges()
+            np.testing.assert_array_equal(eng.last_epoch_edges()[1], dst)
+            # the slots of each (new node, 2^16-id chunk) walk, as the engine reserves them
+            chunk = 1 << 16
+            lens = np.minimum(chunk, n - chunk * np.arange((n + chunk - 1) // chunk))
+            mu = lens * p
+            slots = np.minimum(lens, np.ceil(mu + np.sqrt(mu * (1 - p))) + 8)
+            per = np.zeros((delta, len(lens)), np.int64)
+            np.add.at(per, (src - n, dst // chunk), 1)
+            over += int((per > slots[None, :]).sum())
+        _compare_state(eng, og)
+    assert over > 0
+
+
 def _popular_seed(n: int, popular: int, lo: int, hi: int, seed: int) -> W.SeedGraph:
     """Sparse background (4 random citations per node) plus `popular` nodes cited by lo..hi
     random others: more than 256 nodes with rows longer than the shared frontier, so many are
