@@ -320,9 +320,10 @@ def run_ours(args) -> None:
                 t0 = time.perf_counter()
                 e2.load_graph(hp, hf, hs, hd, prm, planned_epochs=EPOCHS)
                 n0, m0 = e2.counts()
-                ne = e2.run_epochs(EPOCHS, use_graph=False)
+                # every epoch's citations are written into the page-locked buffers while the
+                # following epochs run
+                ne, _ = e2.run_epochs_out(EPOCHS, out, use_graph=False)
                 n1, m1 = e2.counts()
-                src, dst = e2.edges(m0, m1 - m0, out=out)
                 dt = time.perf_counter() - t0
             e2e_edges += ne
             e2e_secs += dt
@@ -495,30 +496,29 @@ def ensemble_measure(args, world, rank, local, dist, with_cpu: bool = True) -> d
         import torch
 
         # page-locked host buffers, filled before the timed region (as in the PA line): the
-        # replicas' raw inputs in, every new citation (source, target) out, each replica's at its
-        # own offset
+        # replicas' raw inputs in, every new citation (source, target) out
         def pinned(a):
             return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
 
         preps = [dataclasses.replace(r, pub_epoch=pinned(r.pub_epoch), fitness=pinned(r.fitness),
                                      src=pinned(r.src), dst=pinned(r.dst)) for r in reps]
-        ofs = np.concatenate([[0], np.cumsum(new_edges)])
-        out_s = torch.empty(int(ofs[-1]) + 1, dtype=torch.int32).pin_memory().numpy()
-        out_d = torch.empty(int(ofs[-1]) + 1, dtype=torch.int32).pin_memory().numpy()
+        tot = int(sum(new_edges)) + 1
+        out_s = torch.empty(tot, dtype=torch.int32).pin_memory().numpy()
+        out_d = torch.empty(tot, dtype=torch.int32).pin_memory().numpy()
         t0 = time.perf_counter()
         h2d = d2h = 0
         with GrowthEngine(seed=args.seed, replicas=len(reps), device=local) as e2:
             e2.set_tuning(**tuned)
             e2.load_replicas(preps)
             m0 = [e2.counts(r) for r in range(len(reps))]
-            ne = e2.run_epochs(ENS_EPOCHS, use_graph=True)
+            # every epoch's citations, replica by replica, written into the page-locked buffers
+            # while the following epochs run
+            ne, _ = e2.run_epochs_out(ENS_EPOCHS, (out_s, out_d), use_graph=True)
             for r in range(len(reps)):
                 n0_, mm0 = m0[r]
                 n1, m1 = e2.counts(r)
-                o = int(ofs[r])
-                e2.edges(mm0, m1 - mm0, r, out=(out_s[o:o + m1 - mm0], out_d[o:o + m1 - mm0]))
                 h2d += 4 * n0_ * 2 + 4 * len(reps[r].src) * 2  # publication epochs, fitness, raw edges
-                d2h += 8 * (m1 - mm0)  # sources (expanded on the device) and targets
+                d2h += 8 * (m1 - mm0)  # sources and targets
         dt = reduce_max(dist, time.perf_counter() - t0)
         e2e = {"value": reduce_sum(dist, float(len(reps))) / dt, "unit": "evals/s",
                "h2d_bytes_per_step": int(reduce_sum(dist, float(h2d))),

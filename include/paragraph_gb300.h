@@ -177,6 +177,14 @@ pg_status pg_grow_epoch(pg_ctx* ctx, int64_t* new_nodes, int64_t* new_edges);
 /* num_epochs PA epochs without host synchronisation between them; use_graph != 0 captures the
  * whole run in one CUDA graph the first time and replays it afterwards. */
 pg_status pg_run_epochs(pg_ctx* ctx, int32_t num_epochs, int32_t use_graph, int64_t* new_edges);
+/* pg_run_epochs that also delivers every new citation (source, target) into src/dst (capacity
+ * entries each), epoch by epoch and, within an epoch, replica by replica in forward-CSR order; the
+ * per-epoch, per-replica counts go to counts[epoch * num_replicas + r] (may be NULL).  Page-locked
+ * buffers (cudaHostAlloc / cudaHostRegister) are written by the device while the next epoch runs,
+ * so the copy-out overlaps the growth; other buffers are filled after the run.  Replaces the
+ * reference's per-agent cudaMemcpy of the edges back to the host (includes/utils.cuh:151-200). */
+pg_status pg_run_epochs_out(pg_ctx* ctx, int32_t num_epochs, int32_t use_graph, int32_t* src, int32_t* dst,
+                            int64_t capacity, int64_t* counts, int64_t* new_edges);
 /* One Erdos-Renyi G(n,p) epoch on replica 0: delta new nodes, each linking to every pre-epoch node
  * with probability p, by geometric skips. */
 pg_status pg_er_epoch(pg_ctx* ctx, int64_t delta, double p, int64_t* new_edges);

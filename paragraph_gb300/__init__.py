@@ -33,7 +33,7 @@ MAX_OUT_DEGREE = 256
 EXPORTED = [
     "pg_create", "pg_destroy", "pg_last_error", "pg_status_string", "pg_load_graph",
     "pg_load_replicas", "pg_set_params", "pg_default_params", "pg_set_epoch", "pg_grow_epoch",
-    "pg_run_epochs", "pg_er_epoch", "pg_reserve", "pg_get_counts", "pg_epoch_edges", "pg_copy_edges",
+    "pg_run_epochs", "pg_run_epochs_out", "pg_er_epoch", "pg_reserve", "pg_get_counts", "pg_epoch_edges", "pg_copy_edges",
     "pg_copy_degrees", "pg_copy_nodes", "pg_copy_csr", "pg_copy_arrivals", "pg_set_timing",
     "pg_get_stats", "pg_sync", "pg_check_device", "pg_philox4x32_10", "pg_poisson_table",
     "pg_logf_host", "pg_expf_host", "pg_log_host", "pg_exp_host", "pg_version",
@@ -218,6 +218,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
         "pg_set_epoch": (i32, [vp, i64]),
         "pg_grow_epoch": (i32, [vp, P(i64), P(i64)]),
         "pg_run_epochs": (i32, [vp, i32, i32, P(i64)]),
+        "pg_run_epochs_out": (i32, [vp, i32, i32, vp, vp, i64, vp, P(i64)]),
         "pg_er_epoch": (i32, [vp, i64, C.c_double, P(i64)]),
         "pg_reserve": (i32, [vp, i64, i64]),
         "pg_get_counts": (i32, [vp, i32, P(i64), P(i64)]),
@@ -419,6 +420,21 @@ class GrowthEngine:
         ne = C.c_int64()
         self._check(self._lib.pg_run_epochs(self._ctx, epochs, 1 if use_graph else 0, C.byref(ne)))
         return ne.value
+
+    def run_epochs_out(self, epochs: int, out: tuple[np.ndarray, np.ndarray],
+                       use_graph: bool = True) -> tuple[int, np.ndarray]:
+        """run_epochs that also writes every new citation (source, target) into the caller's
+        int32 buffers `out`, epoch by epoch and replica by replica; page-locked buffers are written
+        from the device while the run goes on.  Returns (new citations, counts[epoch, replica])."""
+        s, d = out
+        if (s.dtype != np.int32 or d.dtype != np.int32 or not s.flags.c_contiguous
+                or not d.flags.c_contiguous or len(s) != len(d)):
+            raise PGError(PG_ERR_ARG, "out buffers must be contiguous int32 arrays of one length")
+        counts = np.zeros((epochs, self.replicas), np.int64)
+        ne = C.c_int64()
+        self._check(self._lib.pg_run_epochs_out(self._ctx, epochs, 1 if use_graph else 0, _ptr(s), _ptr(d),
+                                                len(s), _ptr(counts), C.byref(ne)))
+        return ne.value, counts
 
     def er_epoch(self, delta: int, p: float) -> int:
         ne = C.c_int64()

@@ -140,6 +140,13 @@ struct pg_ctx {
     cudaGraphExec_t gexec = nullptr;
     int64_t g_epoch0 = -1;
     int g_epochs = 0;
+    const void* g_out = nullptr;  // the output buffers a captured run writes to (baked into it)
+    // citation output of the current pg_run_epochs_out call (device-visible pointers; null otherwise)
+    int32_t* out_src = nullptr;
+    int32_t* out_dst = nullptr;
+    int64_t out_cap = 0, out_epochs = 0;
+    DBuf<int64_t> out_counts;
+    DBuf<int32_t> out_stage_src, out_stage_dst;  // staging when the caller's buffers are pageable
     Checkpoint ckpt;
     LikState lik;
     pg_tuning tune{};
@@ -175,6 +182,56 @@ cudaError_t dalloc(DBuf<T>& b, int64_t n) {
 template <typename T>
 void dfree(DBuf<T>& b) {
     if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+}
+
+// Temporaries of a load (raw edges, sort scratch, offset-form CSR) come from a stream-ordered pool
+// owned by the library: freeing them does not synchronise the device, and a later load in the same
+// process reuses the memory instead of mapping it again.  The pool keeps what it holds (release
+// threshold: unlimited) until the process ends: at most one load's temporaries, about 40 bytes per
+// raw edge.
+cudaMemPool_t temp_pool(int device) {
+    static cudaMemPool_t pools[64] = {};
+    if (device < 0 || device >= 64) return nullptr;
+    if (!pools[device]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        cudaMemPool_t p = nullptr;
+        if (cudaMemPoolCreate(&p, &props) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+        pools[device] = p;
+    }
+    return pools[device];
+}
+
+template <typename T>
+cudaError_t talloc(DBuf<T>& b, int64_t n, int device, cudaStream_t s) {
+    if (n <= 0) n = 1;
+    b.p = nullptr;
+    b.n = 0;
+    cudaMemPool_t pool = temp_pool(device);
+    cudaError_t e = pool ? cudaMallocFromPoolAsync((void**)&b.p, sizeof(T) * (size_t)n, pool, s)
+                         : cudaMalloc((void**)&b.p, sizeof(T) * (size_t)n);
+    if (e == cudaSuccess) b.n = n;
+    return e;
+}
+
+template <typename T>
+void tfree(DBuf<T>& b, int device, cudaStream_t s) {
+    if (b.p) {
+        if (temp_pool(device))
+            cudaFreeAsync(b.p, s);
+        else
+            cudaFree(b.p);
+    }
     b.p = nullptr;
     b.n = 0;
 }
@@ -248,6 +305,11 @@ Arena make_arena(pg_ctx* c) {
     A.hub_rem = c->hub_rem.p;
     A.hub_add = c->hub_add.p;
     A.hub_cand = c->hub_cand.p;
+    A.out_src = c->out_src;
+    A.out_dst = c->out_dst;
+    A.out_cap = c->out_cap;
+    A.out_counts = c->out_counts.p;
+    A.out_epochs = c->out_epochs;
     A.sampler = c->cfg.sampler;
     A.tune_agent_ctas = c->tune.agent_ctas_per_sm;
     A.tune_small_hash = c->tune.small_hash;
@@ -483,13 +545,13 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         const int64_t tot = raw_off[(size_t)R];
         DBuf<unsigned long long> first;
         auto drop = [&]() {
-            dfree(raw_src);
-            dfree(raw_dst);
-            dfree(first);
+            tfree(raw_src, c->device, c->stream);
+            tfree(raw_dst, c->device, c->stream);
+            tfree(first, c->device, c->stream);
         };
-        cudaError_t e = dalloc(raw_src, std::max<int64_t>(tot, 1));
-        if (e == cudaSuccess) e = dalloc(raw_dst, std::max<int64_t>(tot, 1));
-        if (e == cudaSuccess) e = dalloc(first, R);
+        cudaError_t e = talloc(raw_src, std::max<int64_t>(tot, 1), c->device, c->stream);
+        if (e == cudaSuccess) e = talloc(raw_dst, std::max<int64_t>(tot, 1), c->device, c->stream);
+        if (e == cudaSuccess) e = talloc(first, R, c->device, c->stream);
         for (int r = 0; r < R && e == cudaSuccess; ++r) {
             const pg_replica_desc& d = raw[r];
             const size_t o = (size_t)raw_off[(size_t)r];
@@ -505,7 +567,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(bad.data(), first.p, sizeof(unsigned long long) * (size_t)R, cudaMemcpyDeviceToHost, c->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-        dfree(first);
+        tfree(first, c->device, c->stream);
         if (e != cudaSuccess) {
             drop();
             return fail(c, PG_ERR_CUDA, std::string("edge upload: ") + cudaGetErrorString(e));
@@ -602,13 +664,17 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         }
     } temps;
     temps.f.push_back([&]() {
-        dfree(t_bo);
-        dfree(t_caps);
-        dfree(t_begs);
-        dfree(t_bsum);
-        dfree(t_bc);
-        dfree(t_u);
-        dfree(t_laid);
+        tfree(t_bo, c->device, c->stream);
+        tfree(t_caps, c->device, c->stream);
+        tfree(t_begs, c->device, c->stream);
+        tfree(t_bsum, c->device, c->stream);
+        tfree(t_bc, c->device, c->stream);
+        tfree(t_u, c->device, c->stream);
+        tfree(t_laid, c->device, c->stream);
+        tfree(scratch, c->device, c->stream);
+        tfree(raw_src, c->device, c->stream);
+        tfree(raw_dst, c->device, c->stream);
+        tfree(berr, c->device, c->stream);
     });
     {
         int64_t nn = 1, mm = 1;
@@ -616,13 +682,13 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             nn = std::max<int64_t>(nn, reps[r].n);
             mm = std::max<int64_t>(mm, raw ? raw[r].num_edges : reps[r].m);
         }
-        PG_CUDA(c, dalloc(t_bo, nn + 1));
-        PG_CUDA(c, dalloc(t_caps, nn + 1));
-        PG_CUDA(c, dalloc(t_begs, nn + 1));
-        PG_CUDA(c, dalloc(t_bsum, scan_blocks_needed(nn + 1) + 2));
-        PG_CUDA(c, dalloc(t_bc, mm));
-        PG_CUDA(c, dalloc(t_u, R));
-        PG_CUDA(c, dalloc(t_laid, R));
+        PG_CUDA(c, talloc(t_bo, nn + 1, c->device, c->stream));
+        PG_CUDA(c, talloc(t_caps, nn + 1, c->device, c->stream));
+        PG_CUDA(c, talloc(t_begs, nn + 1, c->device, c->stream));
+        PG_CUDA(c, talloc(t_bsum, scan_blocks_needed(nn + 1) + 2, c->device, c->stream));
+        PG_CUDA(c, talloc(t_bc, mm, c->device, c->stream));
+        PG_CUDA(c, talloc(t_u, R, c->device, c->stream));
+        PG_CUDA(c, talloc(t_laid, R, c->device, c->stream));
         PG_CUDA(c, cudaMemsetAsync(t_laid.p, 0, 8 * (size_t)R, c->stream));
     }
     if (raw) {
@@ -631,8 +697,8 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             mm = std::max<int64_t>(mm, raw[r].num_edges);
             nn = std::max<int64_t>(nn, raw[r].num_nodes);
         }
-        PG_CUDA(c, dalloc(scratch, (int64_t)build_scratch_bytes(mm, nn)));
-        PG_CUDA(c, dalloc(berr, R));
+        PG_CUDA(c, talloc(scratch, (int64_t)build_scratch_bytes(mm, nn), c->device, c->stream));
+        PG_CUDA(c, talloc(berr, R, c->device, c->stream));
         PG_CUDA(c, cudaMemsetAsync(berr.p, 0, 4 * (size_t)R, c->stream));
     }
     for (int r = 0; r < R; ++r) {
@@ -691,10 +757,10 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         PG_CUDA(c, cudaMemcpyAsync(laid.data(), t_laid.p, 8 * (size_t)R, cudaMemcpyDeviceToHost, c->stream));
         PG_CUDA(c, cudaStreamSynchronize(c->stream));
         if (raw) {
-            dfree(scratch);
-            dfree(raw_src);
-            dfree(raw_dst);
-            dfree(berr);
+            tfree(scratch, c->device, c->stream);
+            tfree(raw_src, c->device, c->stream);
+            tfree(raw_dst, c->device, c->stream);
+            tfree(berr, c->device, c->stream);
         }
         for (int r = 0; r < R; ++r) {
             HostRep& h = reps[r];
@@ -890,7 +956,7 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
         launch_bwd_append(A, agents, c->num_sms, s, c->side, c->fork, c->join);
         PG_STAGE("backward append");
         if (events) record_event(ev[4], s);
-        c->launches += kPaEpochKernels - 4 - 2 + kRcScoreKernels + 2;
+        c->launches += kPaEpochKernels - 4 - 2 + kRcScoreKernels + 2 + (c->out_src ? 1 : 0);
         return PG_OK;
     }
     // the hub index reads only the CSR and the weights and guide table only node attributes: the
@@ -927,7 +993,7 @@ pg_status enqueue_pa_epoch(pg_ctx* c, int64_t epoch, int64_t agents, cudaEvent_t
     PG_STAGE("backward append");
     if (events) record_event(ev[4], s);
 #undef PG_STAGE
-    c->launches += kPaEpochKernels;
+    c->launches += kPaEpochKernels + (c->out_src ? 1 : 0);
     return PG_OK;
 }
 
@@ -1121,6 +1187,9 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->brow);
     dfree(c->reloc);
     dfree(c->er_slots);
+    dfree(c->out_counts);
+    dfree(c->out_stage_src);
+    dfree(c->out_stage_dst);
     dfree(c->er_ov);
     dfree(c->er_ovb);
     DBuf<int64_t>* i64[] = {&c->fwd_off, &c->len_tmp,
@@ -1387,7 +1456,7 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
     };
     cudaGetLastError();  // errors of earlier, unrelated calls are not this run's
     if (use_graph) {
-        if (!(c->gexec && c->g_epoch0 == e0 && c->g_epochs == num_epochs)) {
+        if (!(c->gexec && c->g_epoch0 == e0 && c->g_epochs == num_epochs && c->g_out == (const void*)c->out_src)) {
             destroy_graph_exec(c);
             cudaGraph_t graph;
             PG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -1403,6 +1472,7 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
             if (ce != cudaSuccess) return fail(c, PG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
             c->g_epoch0 = e0;
             c->g_epochs = num_epochs;
+            c->g_out = c->out_src;
         }
         PG_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
     } else {
@@ -1463,6 +1533,57 @@ pg_status pg_run_epochs(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int64_
     }
     S.new_edges = total;
     if (new_edges) *new_edges = total;
+    return PG_OK;
+}
+
+pg_status pg_run_epochs_out(pg_ctx* c, int32_t num_epochs, int32_t use_graph, int32_t* src, int32_t* dst,
+                            int64_t capacity, int64_t* counts, int64_t* new_edges) {
+    if (!c) return PG_ERR_ARG;
+    if (!src || !dst || capacity < 0) return fail(c, PG_ERR_ARG, "output buffers required");
+    if (num_epochs < 1) return fail(c, PG_ERR_ARG, "num_epochs must be >= 1");
+    PG_CUDA(c, cudaSetDevice(c->device));
+    // page-locked buffers mapped into the device's address space are written by the device during
+    // the run; any other buffers get a device staging copy, read back after the run
+    auto mapped = [&](void* p) -> void* {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+    };
+    int32_t* ds = static_cast<int32_t*>(mapped(src));
+    int32_t* dd = static_cast<int32_t*>(mapped(dst));
+    const bool staged = !(ds && dd);
+    const int64_t cap = std::max<int64_t>(capacity, 1);
+    if (staged) {
+        if (c->out_stage_src.n < cap) PG_CUDA(c, dalloc(c->out_stage_src, cap));
+        if (c->out_stage_dst.n < cap) PG_CUDA(c, dalloc(c->out_stage_dst, cap));
+        ds = c->out_stage_src.p;
+        dd = c->out_stage_dst.p;
+    }
+    const int64_t nc = (int64_t)num_epochs * c->R;
+    if (c->out_counts.n < nc) {
+        destroy_graph_exec(c);
+        PG_CUDA(c, dalloc(c->out_counts, nc));
+    }
+    c->out_src = ds;
+    c->out_dst = dd;
+    c->out_cap = capacity;
+    c->out_epochs = num_epochs;
+    int64_t ne = 0;
+    pg_status s = pg_run_epochs(c, num_epochs, use_graph, &ne);
+    c->out_src = c->out_dst = nullptr;
+    c->out_cap = c->out_epochs = 0;
+    if (s != PG_OK) return s;
+    if (staged && ne > 0) {
+        PG_CUDA(c, cudaMemcpyAsync(src, ds, 4 * (size_t)ne, cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(dst, dd, 4 * (size_t)ne, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (counts)
+        PG_CUDA(c, cudaMemcpyAsync(counts, c->out_counts.p, 8 * (size_t)nc, cudaMemcpyDeviceToHost, c->stream));
+    PG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (new_edges) *new_edges = ne;
     return PG_OK;
 }
 

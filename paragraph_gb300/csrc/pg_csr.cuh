@@ -214,6 +214,42 @@ __device__ __forceinline__ void d_bwd_place(const Arena& A, int64_t agents) {
 
 __global__ void __launch_bounds__(256) k_bwd_place(Arena A, int64_t agents) { d_bwd_place(A, agents); }
 
+// A run's citation output (pg_run_epochs_out): one warp per agent writes the agent's citations,
+// (source, target), at the run's running count; the first CTA records the epoch's count per
+// replica.  The targets are read from the epoch's edge list, which the next epoch overwrites, so the
+// stream order puts this before the epoch end.
+__device__ __forceinline__ void d_copy_out(const Arena& A, int64_t agents) {
+    if (!A.out_src || A.st->error) return;
+    const int64_t base = (int64_t)A.st->out_count;
+    const int64_t E = A.eoff[agents];
+    if (base + E > A.out_cap) {
+        if (threadIdx.x == 0) atomicOr(&A.st->error, kErrCapacity);
+        return;
+    }
+    if (blockIdx.x == 0) {
+        const int64_t k = (int64_t)A.st->cum_epochs;
+        for (int r = threadIdx.x; r < A.R && k < A.out_epochs; r += blockDim.x) {
+            const Replica& rp = A.rep[r];
+            A.out_counts[k * A.R + r] = A.eoff[rp.abase + rp.delta] - A.eoff[rp.abase];
+        }
+    }
+    const int lane = lane_id();
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t a = warp; a < agents; a += nwarps) {
+        const int r = replica_of_agent(A.rep, A.R, a);
+        const Replica& rp = A.rep[r];
+        const int32_t src = (int32_t)(rp.n + (a - rp.abase));
+        const int64_t e0 = A.eoff[a], e1 = A.eoff[a + 1];
+        for (int64_t e = e0 + lane; e < e1; e += 32) {
+            A.out_src[base + e] = src;
+            A.out_dst[base + e] = A.e_dst[e];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_copy_out(Arena A, int64_t agents) { d_copy_out(A, agents); }
+
 // The epoch's `added` entries of the row in `slot` (the row's last ones): replica and first entry.
 __device__ __forceinline__ void seg_bounds(const Arena& A, int64_t slot, int64_t added, const Replica*& rpp,
                                            int64_t& start) {
@@ -345,6 +381,7 @@ __device__ __forceinline__ void d_epoch_end(const Arena& A, int64_t agents) {
         st->cum_new_nodes += (unsigned long long)agents;
         st->cum_epochs += 1;
         st->cum_adj_scanned += st->adj_scanned;
+        if (A.out_src) st->out_count += (unsigned long long)A.eoff[agents];
     }
 }
 
@@ -371,6 +408,7 @@ void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t
         cudaStreamWaitEvent(side, fork, 0);
     }
     k_bwd_reloc<<<(unsigned)(num_sms * copy_per_sm), 256, 0, two ? side : s>>>(A);
+    if (A.out_src) k_copy_out<<<(unsigned)(num_sms * 8), 256, 0, two ? side : s>>>(A, agents);
     if (two) cudaEventRecord(join, side);
     k_bwd_place<<<(unsigned)ga, 256, 0, s>>>(A, agents);
     k_sort_small<<<(unsigned)num_sms * 8, 256, 0, s>>>(A);

@@ -151,6 +151,7 @@ struct EpochState {
     unsigned long long cum_new_nodes;
     unsigned long long cum_epochs;
     unsigned long long cum_adj_scanned;
+    unsigned long long out_count;   // citations streamed to the run's output buffers so far
     // grid barrier of the persistent epoch kernel: arrivals (back to 0 after every barrier, reset
     // by the host before each launch) and generation
     unsigned int gbar_count;
@@ -231,6 +232,14 @@ struct Arena {
     int32_t rep_base;          // RNG replica index of replica 0 (pg_config.replica_base)
     uint32_t first_wait_polls; // polls of the first bounded wait on each staged copy (pg_set_wait_limit)
     uint32_t pad_wp;
+    // citation output of a run (pg_run_epochs_out), null otherwise: every epoch's new citations,
+    // (source, target) replica by replica, written from the device at out_count; per-epoch,
+    // per-replica counts at out_counts[epoch of the run * R + r]
+    int32_t* out_src;
+    int32_t* out_dst;
+    int64_t out_cap;
+    int64_t* out_counts;
+    int64_t out_epochs;
 };
 
 // u01d(lo, hi) <= p compared in integers: u = (v + 1) 2^-53 with v the draw's top 53 bits, and

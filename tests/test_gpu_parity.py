@@ -405,6 +405,42 @@ def test_bad_edge_in_one_replica_leaves_the_loaded_replicas(gpu):
         eng.run_epochs(1)  # still usable
 
 
+@pytest.mark.parametrize("pinned,replicas,epoch_kernel", [(True, 1, 0), (False, 3, 0), (True, 3, 1)])
+def test_run_epochs_out_streams_every_citation(gpu, pinned, replicas, epoch_kernel):
+    """pg_run_epochs_out delivers every new citation, epoch by epoch and replica by replica, into
+    the caller's buffers: written from the device during the run when they are page-locked, read
+    back after the run otherwise.  Each (epoch, replica) block equals that replica's new forward
+    rows of the epoch."""
+    reps = W.ensemble_inputs(replicas=replicas, lo=2000, hi=8000, epochs=4, seed=12)
+    cap = 400_000
+    if pinned:
+        torch = pytest.importorskip("torch")
+        out = (torch.empty(cap, dtype=torch.int32).pin_memory().numpy(),
+               torch.empty(cap, dtype=torch.int32).pin_memory().numpy())
+    else:
+        out = (np.empty(cap, np.int32), np.empty(cap, np.int32))
+    with GrowthEngine(seed=6, replicas=replicas) as eng:
+        eng.load_replicas(reps)
+        eng.set_tuning(epoch_kernel=epoch_kernel)
+        n0 = [eng.counts(r)[0] for r in range(replicas)]
+        m0 = [eng.counts(r)[1] for r in range(replicas)]
+        ne, counts = eng.run_epochs_out(4, out)
+        assert ne == counts.sum() > 0
+        pos = 0
+        done = list(m0)
+        for e in range(4):
+            for r in range(replicas):
+                k = int(counts[e, r])
+                s_ref, d_ref = eng.edges(done[r], k, r)
+                np.testing.assert_array_equal(out[0][pos:pos + k], s_ref)
+                np.testing.assert_array_equal(out[1][pos:pos + k], d_ref)
+                assert (s_ref >= n0[r]).all()
+                done[r] += k
+                pos += k
+        assert pos == ne
+        assert done == [eng.counts(r)[1] for r in range(replicas)]
+
+
 def test_edges_into_caller_buffers(gpu):
     g = W.plain_pa_seed(2000, 5, seed=2)
     with GrowthEngine(seed=3) as eng:
