@@ -506,9 +506,10 @@ __global__ void k_edges_check(Arena A, int64_t agents) { d_edges_check(A, agents
 
 // Shapes of the k <= 64 thinning kernel (pg_tuning.small_hash = HS): 0 -- a 2048-slot frontier hash
 // and 512-entry stage buffers; 1 -- 1024 slots and 1024-entry stages; both 4 CTAs per SM.  The
-// k <= 256 kernel always has 1024 slots and 512-entry stages.  (A third shape, 1024 slots and
-// 512-entry stages at 5 CTAs per SM with 96 registers, was measured 9 % slower on the PA workload
-// than shape 0 and was not picked by the tuner for the ensemble.)
+// k <= 256 kernel always has 1024 slots and 512-entry stages.  Shapes with more resident warps were
+// measured on the PA workload and were slower: 1024 slots and 512-entry stages at 5 CTAs per SM (96
+// registers) by 9 %, and 2048 slots and 256-entry stages at 5 CTAs per SM with the heavy agents'
+// instance out of line (the lean one then fits 96 registers) by 8 %.
 template <int KCAP, int HS>
 struct ThinStage {
     static constexpr int value = (KCAP <= kKSmall && HS == 1) ? 1024 : 512;

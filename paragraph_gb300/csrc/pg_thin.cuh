@@ -36,17 +36,20 @@ struct BallAux {
 constexpr uint32_t kWaitLimit = kWaitPolls;  // polls of a bulk-copy barrier before giving up
 constexpr int kTestU = 4;                  // entries per lane and step of the membership scan
 
-// STAGE: adjacency entries per stage buffer (two per warp; 1024 in the small-hash k <= 64 kernel,
-// 512 in the others); the struct lives in dynamic shared memory, one per warp
+// STAGE: adjacency entries per stage buffer (two per warp); the struct lives in dynamic shared
+// memory, one per warp.  The exact continuation's lists (chosen ids and their cumulative quantised
+// weights) are only used after the event loop, when no copy is in flight, so they share the stage
+// buffers' memory (a proxy fence orders them before the next agent's bulk copies).
 template <int KCAP, int HCAP, int STAGE>
 struct ThinSmem {
+    static_assert(2 * STAGE * 4 >= KCAP * 12, "continuation lists must fit the stage buffers");
     __align__(16) int32_t stage[2][STAGE];  // candidate rows, two buffers filled by bulk copies
     int32_t H[HCAP];  // frontier hash set, -1 = empty
     int32_t arr[KCAP];
-    int32_t c_id[KCAP];
-    uint64_t c_cq[KCAP];
     BallAux aux;
     unsigned long long bar[2];  // mbarriers of the two stage buffers
+    __device__ int32_t* c_id() { return &stage[0][0]; }
+    __device__ uint64_t* c_cq() { return reinterpret_cast<uint64_t*>(&stage[0][0] + 2 * KCAP); }
 };
 
 // ---- bulk asynchronous copies (the TMA engine's cp.async.bulk) into shared memory
@@ -466,6 +469,10 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
     }
 
     // ---------------------------------------------------------------- events
+    // the previous agent's continuation lists were written over the stage buffers by the generic
+    // proxy: order those writes before this agent's bulk copies into the same memory
+    fence_proxy_async();
+    __syncwarp();
     const uint64_t Wq = rp.wq_total;
     int nch = 0;
     long long events = 0, tests = 0, scanned = 0;
@@ -698,20 +705,20 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                 const int j = S.arr[q];
                 const uint64_t qj = cdf[j] - (j > 0 ? cdf[j - 1] : 0);
                 int pos = nc;
-                while (pos > 0 && S.c_id[pos - 1] > j) {
-                    S.c_id[pos] = S.c_id[pos - 1];
-                    S.c_cq[pos] = S.c_cq[pos - 1];
+                while (pos > 0 && S.c_id()[pos - 1] > j) {
+                    S.c_id()[pos] = S.c_id()[pos - 1];
+                    S.c_cq()[pos] = S.c_cq()[pos - 1];
                     --pos;
                 }
-                S.c_id[pos] = j;
-                S.c_cq[pos] = qj;
+                S.c_id()[pos] = j;
+                S.c_cq()[pos] = qj;
                 ++nc;
                 R -= qj;
             }
             uint64_t acc = 0;
             for (int q = 0; q < nc; ++q) {
-                acc += S.c_cq[q];
-                S.c_cq[q] = acc;
+                acc += S.c_cq()[q];
+                S.c_cq()[q] = acc;
             }
         }
         __syncwarp();
@@ -729,12 +736,12 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                 int cl = 0, ch = nc;
                 while (cl < ch) {
                     const int mid = (cl + ch) >> 1;
-                    if (S.c_id[mid] <= p)
+                    if (S.c_id()[mid] <= p)
                         cl = mid + 1;
                     else
                         ch = mid;
                 }
-                const uint64_t cp = cl ? S.c_cq[cl - 1] : 0;
+                const uint64_t cp = cl ? S.c_cq()[cl - 1] : 0;
                 const unsigned m = __ballot_sync(kFull, (cdf[p] - cp) > y);
                 if (m == 0) {
                     if (lane == 0) atomicOr(&A.st->error, kErrArg);
@@ -763,7 +770,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             }
             const uint64_t qj = cdf[j] - (j > 0 ? cdf[j - 1] : 0);
             int below = 0;
-            for (int q = lane; q < nc; q += 32) below += S.c_id[q] < j ? 1 : 0;
+            for (int q = lane; q < nc; q += 32) below += S.c_id()[q] < j ? 1 : 0;
             const int pos = __reduce_add_sync(kFull, below);
             for (int top = nc; top > pos; top -= 32) {
                 const int q = top - 1 - lane;
@@ -771,19 +778,19 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                 int tid = 0;
                 uint64_t tq = 0;
                 if (act) {
-                    tid = S.c_id[q];
-                    tq = S.c_cq[q];
+                    tid = S.c_id()[q];
+                    tq = S.c_cq()[q];
                 }
                 __syncwarp();
                 if (act) {
-                    S.c_id[q + 1] = tid;
-                    S.c_cq[q + 1] = tq + qj;
+                    S.c_id()[q + 1] = tid;
+                    S.c_cq()[q + 1] = tq + qj;
                 }
                 __syncwarp();
             }
             if (lane == 0) {
-                S.c_id[pos] = j;
-                S.c_cq[pos] = (pos > 0 ? S.c_cq[pos - 1] : 0) + qj;
+                S.c_id()[pos] = j;
+                S.c_cq()[pos] = (pos > 0 ? S.c_cq()[pos - 1] : 0) + qj;
                 S.arr[nch] = j;
             }
             __syncwarp();
