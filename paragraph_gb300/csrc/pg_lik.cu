@@ -388,6 +388,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_ball(LikTrace T, LikBalls B
 template <bool ADJ, int NP, bool EXACT>
 __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P, LikBalls Bl,
                                                           int64_t a0, int64_t a1) {
+    __shared__ float4 lik_stage[kLikThreads / 32][32];
     const int lane = threadIdx.x & 31;
     const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -410,7 +411,52 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
         const float4* F = T.feat + (int64_t)e * T.n;
         const int64_t j0 = Bl.boff[a] - Bl.base, j1 = Bl.boff[a + 1] - Bl.base;
         Kahan s[NP], t0[NP], t1[NP], t2[NP];
-        int64_t q = j0 + sl;
+        if constexpr (NP == 2) {
+            // the ball in batches of 32: lane l loads element l's id and feature row, the next
+            // batch's loads are issued before this batch is summed, and the rows are read back
+            // from the warp's shared buffer in the same groups of four (same sums) as below
+            float4* buf = lik_stage[threadIdx.x >> 5];
+            float4 cur = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (j0 + lane < j1) cur = F[Bl.ids[j0 + lane]];
+            for (int64_t b0 = j0; b0 < j1; b0 += 32) {
+                const int cnt = j1 - b0 < 32 ? (int)(j1 - b0) : 32;
+                float4 nxt = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (b0 + 32 + lane < j1) nxt = F[Bl.ids[b0 + 32 + lane]];
+                __syncwarp();
+                buf[lane] = cur;
+                __syncwarp();
+                int i = 0;
+                for (; i + 3 < cnt; i += 4) {
+                    const float4 f0 = buf[i], f1 = buf[i + 1], f2 = buf[i + 2], f3 = buf[i + 3];
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) {
+                        const float w0 = lik_w<EXACT>(lik_x2<EXACT>(f0, cq[p])), w1 = lik_w<EXACT>(lik_x2<EXACT>(f1, cq[p])),
+                                    w2 = lik_w<EXACT>(lik_x2<EXACT>(f2, cq[p])), w3 = lik_w<EXACT>(lik_x2<EXACT>(f3, cq[p]));
+                        kadd(s[p], (w0 + w1) + (w2 + w3));
+                        if (ADJ) {
+                            kadd(t0[p], __fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
+                            kadd(t1[p], __fmaf_rn(w3, f3.z, __fmaf_rn(w2, f2.z, __fmaf_rn(w1, f1.z, w0 * f0.z))));
+                            kadd(t2[p], __fmaf_rn(w3, f3.x, __fmaf_rn(w2, f2.x, __fmaf_rn(w1, f1.x, w0 * f0.x))));
+                        }
+                    }
+                }
+                for (; i < cnt; ++i) {
+                    const float4 f = buf[i];
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) {
+                        const float w = lik_w<EXACT>(lik_x2<EXACT>(f, cq[p]));
+                        kadd(s[p], w);
+                        if (ADJ) {
+                            kadd(t0[p], w * f.y);
+                            kadd(t1[p], w * f.z);
+                            kadd(t2[p], w * f.x);
+                        }
+                    }
+                }
+                cur = nxt;
+            }
+        }
+        int64_t q = NP == 2 ? j1 : j0 + sl;
         for (; q + 3 * SL < j1; q += 4 * SL) {
             const int32_t i0 = Bl.ids[q], i1 = Bl.ids[q + SL], i2 = Bl.ids[q + 2 * SL], i3 = Bl.ids[q + 3 * SL];
             const float4 f0 = F[i0], f1 = F[i1], f2 = F[i2], f3 = F[i3];
