@@ -151,6 +151,48 @@ __device__ __forceinline__ float lik_w(const X2 x) {
     return __fmaf_rn(e, x.l * kLn2f, e);
 }
 
+// Double-float numbers (a pair of fp32, h + l with |l| <= ulp(h) / 2; Dekker 1971, Knuth's two-sum):
+// about 44 significant bits from fp32 arithmetic.  The citation loops run in them: GB300's FP64
+// rate is a small fraction of its fp32 rate, and FP64 there cost as much as the ball sums.
+struct DF {
+    float h, l;
+};
+__device__ __forceinline__ DF df_of(double x) {
+    DF r;
+    r.h = (float)x;
+    r.l = (float)(x - (double)r.h);
+    return r;
+}
+__device__ __forceinline__ double df_val(const DF a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ DF df_norm(float s, float e) {  // s + e as a pair, any magnitudes
+    float r;
+    const float h = two_sum(s, e, r);
+    return DF{h, r};
+}
+__device__ __forceinline__ DF df_add(const DF a, const DF b) {
+    float e;
+    const float s = two_sum(a.h, b.h, e);
+    return df_norm(s, e + (a.l + b.l));
+}
+__device__ __forceinline__ DF df_neg(const DF a) { return DF{-a.h, -a.l}; }
+__device__ __forceinline__ DF df_mul(const DF a, const DF b) {
+    const float p = a.h * b.h;
+    const float e = __fmaf_rn(a.h, b.h, -p);
+    return df_norm(p, __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e)));
+}
+__device__ __forceinline__ DF df_mulf(const DF a, float b) {
+    const float p = a.h * b;
+    const float e = __fmaf_rn(a.h, b, -p);
+    return df_norm(p, __fmaf_rn(a.l, b, e));
+}
+__device__ __forceinline__ bool df_gt(const DF a, const DF b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
+// 1/a for a > 0: the fp32 reciprocal r, then one Newton step r + r (1 - a r) in double-float
+__device__ __forceinline__ DF df_recip(const DF a) {
+    const float r = 1.0f / a.h;
+    const DF e = df_add(DF{1.0f, 0.0f}, df_neg(df_mulf(a, r)));
+    return df_add(DF{r, 0.0f}, df_mulf(e, r));
+}
+
 // 1/D for D > 0 in FP64: Newton's iteration for the reciprocal, r' = r + r (1 - D r), started from
 // the fp32 reciprocal of the special-function unit (relative error < 2^-22); one step squares the
 // error (< 2^-44).  Outside the fp32 normal range the plain FP64 division is used.
@@ -386,7 +428,7 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_ball(LikTrace T, LikBalls B
 // of each point with FP64 running sums:  D_i = Z_a - P_i,  log D_i = log Z_a + log(1 - P_i / Z_a),
 // and in the adjoint g_i - (dZ_a - dP_i) / D_i.
 template <bool ADJ, int NP, bool EXACT>
-__global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P, LikBalls Bl,
+__global__ void __launch_bounds__(kLikThreads, ADJ ? 2 : 3) k_lik_eval(LikTrace T, LikBatch P, LikBalls Bl,
                                                           int64_t a0, int64_t a1) {
     __shared__ float4 lik_stage[kLikThreads / 32][32];
     const int lane = threadIdx.x & 31;
@@ -520,42 +562,65 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_eval(LikTrace T, LikBatch P
                 atomicOr(P.error, 2u);
                 continue;
             }
-            const double logZ = ADJ ? 0.0 : log_pg(Z), invZ = ADJ ? 0.0 : 1.0 / Z;
-            double Pc = 0.0, l = 0.0;
-            double dP[4] = {0.0, 0.0, 0.0, 0.0}, g[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int i = 0; i < k; ++i) {
-                const bool in = Bl.cflag[c0 + i] != 0;
-                const float4 f = F[T.cites[c0 + i]];
-                const X2 x2 = lik_x2<EXACT>(f, c);
-                const float w = lik_w<EXACT>(x2);
-                const double W = in ? (double)w * beta : (double)w;
-                if (!ADJ) {
-                    // log D_i - log Z_a = log(1 - u), u = P_i / Z_a in [0, 1)
-                    const double u = Pc * invZ;
-                    double lr;
-                    if (u < 0.5)
-                        lr = (double)log1m_pg((float)u);
-                    else
-                        lr = log_pg(Z - Pc) - logZ;
-                    const double x = ((double)x2.h + (double)x2.l) * kLn2d;
-                    l += (in ? x + lbe : x) - (logZ + lr);
-                } else {
-                    const double D = Z - Pc;
-                    const double id = recip_nr(D > W ? D : W);
-                    const double gk[4] = {(double)f.y, (double)f.z * itau2, (double)f.x, in ? ibe : 0.0};
-#pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) {
-                        g[kk] += gk[kk] - (dz[kk] - dP[kk]) * id;
-                        dP[kk] += W * gk[kk];
-                    }
-                }
-                Pc += W;
-            }
+            // the citations in draw order, in fp32 / double-float arithmetic (FP64 only per agent
+            // and in the rare u >= 1/2 case): W_i = w_i beta^[in ball], P the weight drawn before
             if (!ADJ) {
+                // l_a = ln2 sum x_i + n_in log beta - (k log Z_a + sum log(1 - u_i)), u_i = P_i / Z_a;
+                // the sums of x_i (its two parts), of log(1 - u_i) and of P compensated in fp32
+                const double logZ = log_pg(Z);
+                const float invZ = 1.0f / (float)Z, betaf = (float)beta;
+                Kahan sh, sl, slr, pc;
+                double lr_far = 0.0;
+                int n_in = 0;
+                for (int i = 0; i < k; ++i) {
+                    const bool in = Bl.cflag[c0 + i] != 0;
+                    const float4 f = F[T.cites[c0 + i]];
+                    const X2 x2 = lik_x2<EXACT>(f, c);
+                    const float w = lik_w<EXACT>(x2);
+                    const float W = in ? w * betaf : w;
+                    const float u = (pc.s - pc.c) * invZ;
+                    if (u < 0.5f)
+                        kadd(slr, log1m_pg(u));
+                    else  // 1 - u is small: log(Z - P) - log Z from the FP64 difference
+                        lr_far += log_pg(Z - kval(pc)) - logZ;
+                    kadd(sh, x2.h);
+                    kadd(sl, x2.l);
+                    n_in += in ? 1 : 0;
+                    kadd(pc, W);
+                }
+                const double l = (kval(sh) + kval(sl)) * kLn2d + (double)n_in * lbe -
+                                 ((double)k * logZ + kval(slr) + lr_far);
                 P.out[a * P.B + b] = l;
             } else {
+                // g_k = sum_i [gk_i - (dZ_k - dP_k,i) / D_i],  D_i = Z_a - P_i,  dP_k,i = sum_{j<i} W_j gk_j
+                const DF Zd = df_of(Z), betad = df_of(beta), itau2d = df_of(itau2), ibed = df_of(ibe);
+                DF dzd[4], dP[4], g[4];
 #pragma unroll
-                for (int kk = 0; kk < 4; ++kk) P.out[(a * P.B + b) * 4 + kk] = g[kk];
+                for (int kk = 0; kk < 4; ++kk) {
+                    dzd[kk] = df_of(dz[kk]);
+                    dP[kk] = DF{0.0f, 0.0f};
+                    g[kk] = DF{0.0f, 0.0f};
+                }
+                DF Pc{0.0f, 0.0f};
+                for (int i = 0; i < k; ++i) {
+                    const bool in = Bl.cflag[c0 + i] != 0;
+                    const float4 f = F[T.cites[c0 + i]];
+                    const X2 x2 = lik_x2<EXACT>(f, c);
+                    const float w = lik_w<EXACT>(x2);
+                    const DF W = in ? df_mulf(betad, w) : DF{w, 0.0f};
+                    const DF D = df_add(Zd, df_neg(Pc));
+                    const DF id = df_recip(df_gt(D, W) ? D : W);
+                    const DF gk[4] = {DF{f.y, 0.0f}, df_mulf(itau2d, f.z), DF{f.x, 0.0f}, in ? ibed : DF{0.0f, 0.0f}};
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const DF t = df_mul(df_add(dzd[kk], df_neg(dP[kk])), id);
+                        g[kk] = df_add(g[kk], df_add(gk[kk], df_neg(t)));
+                        dP[kk] = df_add(dP[kk], df_mul(W, gk[kk]));
+                    }
+                    Pc = df_add(Pc, W);
+                }
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) P.out[(a * P.B + b) * 4 + kk] = df_val(g[kk]);
             }
         }
     }
