@@ -845,7 +845,7 @@ __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epo
     extern __shared__ __align__(16) unsigned char ep_dsm[];
     const int T = A.ntiles;
     const int hub_items = A.R * kHeavyMax * G;
-    // epoch start: new-node counts, agent and copy-tile offsets
+    // epoch start: new-node counts and agent offsets
     if (blockIdx.x == 0) d_epoch_begin(A, epoch, -1);
     grid_sync(A);
     // hub histogram and weights
@@ -865,7 +865,7 @@ __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epo
     // hubs leaving and joining; tile offsets of the CDF (on the last CTA, so CTA 0 is not the only
     // one with extra work)
     for (int t = blockIdx.x; t < T; t += gridDim.x) d_hub_collect(A, t);
-    if (blockIdx.x == gridDim.x - 1) d_tile_scan(A, 0);
+    if (blockIdx.x == gridDim.x - 1) d_tile_scan(A);
     grid_sync(A);
     // hub bits; CDF offsets and guide marks
     if (blockIdx.x == 0) d_hub_assign(A);

@@ -411,7 +411,6 @@ void launch_weights(const Arena& A, cudaStream_t s);
 void launch_hubs(const Arena& A, int num_sms, cudaStream_t s);
 void launch_hub_pairs(const Arena& A, cudaStream_t s);
 void launch_guide(const Arena& A, cudaStream_t s);
-void launch_tile_scan(const Arena& A, int mode, cudaStream_t s);
 void launch_agent_setup(const Arena& A, int64_t agents, cudaStream_t s);
 void launch_agents(const Arena& A, int64_t agents, int num_sms, cudaStream_t s);
 // The whole thinning PA epoch (baseline weights) as one cooperative persistent kernel: every stage

@@ -190,9 +190,8 @@ __device__ __forceinline__ void d_cdf_tiles(const Arena& A, int vb) {
 __global__ void __launch_bounds__(kTileThreads) k_cdf_tiles(Arena A) { d_cdf_tiles(A, blockIdx.x); }
 
 // One CTA: tileoff[t] = sum of tilesum over the earlier tiles of the same replica (mod 2^64, which
-// is exact because every replica's own total is below 2^63).  mode 0 stores each replica's total in
-// wq_total; mode 1 leaves replicas untouched.
-__device__ __forceinline__ void d_tile_scan(const Arena& A, int mode) {
+// is exact because every replica's own total is below 2^63); each replica's total goes to wq_total.
+__device__ __forceinline__ void d_tile_scan(const Arena& A) {
     __shared__ uint64_t sw[33];
     __shared__ uint64_t carry;
     if (cta_error(A)) return;
@@ -216,13 +215,13 @@ __device__ __forceinline__ void d_tile_scan(const Arena& A, int mode) {
         const int e = rp.tbase + rp.ntiles;
         const uint64_t end = e < T ? A.tileoff[e] : carry;
         A.tilesum[r] = b;
-        if (mode == 0) A.rep[r].wq_total = end - b;
+        A.rep[r].wq_total = end - b;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < T; i += blockDim.x) A.tileoff[i] -= A.tilesum[A.tile_rep[i]];
 }
 
-__global__ void __launch_bounds__(1024) k_tile_scan(Arena A, int mode) { d_tile_scan(A, mode); }
+__global__ void __launch_bounds__(1024) k_tile_scan(Arena A) { d_tile_scan(A); }
 
 // Tile offsets into the CDF, and the guide table's marks: node v whose CDF interval
 // [cdf[v-1], cdf[v]) contains bucket starts g 2^gs marks the first of them, guide[g] = v.
@@ -610,14 +609,10 @@ void launch_epoch_begin_delta(const Arena& A, int64_t epoch, int64_t delta, cuda
     k_epoch_begin<<<1, 1024, 0, s>>>(A, epoch, delta);
 }
 
-void launch_tile_scan(const Arena& A, int mode, cudaStream_t s) {
-    k_tile_scan<<<1, 1024, 0, s>>>(A, mode);
-}
-
 void launch_weights(const Arena& A, cudaStream_t s) {
     k_weights<<<A.ntiles, kTileThreads, 0, s>>>(A);
     k_cdf_tiles<<<A.ntiles, kTileThreads, 0, s>>>(A);
-    k_tile_scan<<<1, 1024, 0, s>>>(A, 0);
+    k_tile_scan<<<1, 1024, 0, s>>>(A);
     k_cdf_add<<<A.ntiles, kTileThreads, 0, s>>>(A);
 }
 
