@@ -691,15 +691,37 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         PG_CUDA(c, talloc(t_laid, R, c->device, c->stream));
         PG_CUDA(c, cudaMemsetAsync(t_laid.p, 0, 8 * (size_t)R, c->stream));
     }
+    // several replicas' seeds are built as one graph over the arena's slots (launch_build_all); one
+    // replica's by the build per replica below
+    const bool batched = raw && R > 1;
+    DBuf<int64_t> t_ro;
+    temps.f.push_back([&]() { tfree(t_ro, c->device, c->stream); });
     if (raw) {
         int64_t mm = 1, nn = 1;
         for (int r = 0; r < R; ++r) {
             mm = std::max<int64_t>(mm, raw[r].num_edges);
             nn = std::max<int64_t>(nn, raw[r].num_nodes);
         }
-        PG_CUDA(c, talloc(scratch, (int64_t)build_scratch_bytes(mm, nn), c->device, c->stream));
+        const size_t sb = batched ? build_all_scratch_bytes(raw_off[(size_t)R], S) : build_scratch_bytes(mm, nn);
+        PG_CUDA(c, talloc(scratch, (int64_t)sb, c->device, c->stream));
         PG_CUDA(c, talloc(berr, R, c->device, c->stream));
         PG_CUDA(c, cudaMemsetAsync(berr.p, 0, 4 * (size_t)R, c->stream));
+    }
+    if (batched) {
+        // the tile map and the replicas' bases first: the build cuts its result by them
+        for (int r = 0; r < R; ++r) {
+            for (int t = 0; t < reps[r].ntiles; ++t) trep[(size_t)reps[r].tbase + t] = r;
+            drep[(size_t)r] = to_device_rep(reps[r]);
+        }
+        PG_CUDA(c, talloc(t_ro, R + 1, c->device, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(t_ro.p, raw_off.data(), 8 * (size_t)(R + 1), cudaMemcpyHostToDevice, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(c->tile_rep.p, trep.data(), 4 * (size_t)T, cudaMemcpyHostToDevice, c->stream));
+        PG_CUDA(c, cudaMemcpyAsync(c->rep.p, drep.data(), sizeof(Replica) * (size_t)R, cudaMemcpyHostToDevice, c->stream));
+        cudaGetLastError();
+        launch_build_all(raw_src.p, raw_dst.p, raw_off[(size_t)R], t_ro.p, R, S, c->tile_rep.p, c->rep.p, scratch.p,
+                         c->fwd_off.p, c->fwd_col.p, c->brow.p, c->bcap.p, c->bcol.p, c->indeg.p, t_u.p, t_laid.p,
+                         berr.p, c->stream);
+        PG_CUDA(c, cudaGetLastError());
     }
     for (int r = 0; r < R; ++r) {
         HostRep& h = reps[r];
@@ -722,6 +744,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             const pg_replica_desc& d = raw[r];
             PG_CUDA(c, cudaMemcpyAsync(c->pub.p + h.nbase, d.pub_epoch, 4 * n, cudaMemcpyHostToDevice, c->stream));
             PG_CUDA(c, cudaMemcpyAsync(c->fit.p + h.nbase, d.fitness, 4 * n, cudaMemcpyHostToDevice, c->stream));
+            if (batched) continue;
             cudaGetLastError();
             const size_t o = (size_t)raw_off[(size_t)r];
             launch_build_csr(raw_src.p + o, raw_dst.p + o, d.num_edges, (int64_t)n, scratch.p, c->fwd_off.p + h.obase,

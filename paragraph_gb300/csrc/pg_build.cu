@@ -296,4 +296,135 @@ void launch_brow_layout(const int64_t* bo, const int32_t* bc, int64_t n, int64_t
     }
 }
 
+// ---------------------------------------------------------------- all replicas in one build
+// A context of many replicas builds its seeds as ONE graph over the arena's node slots: every raw
+// edge is rewritten to slot ids (replica base + node), the whole edge list goes through the build
+// above once (keys of slot ids never collide across replicas), and the result is cut into the
+// replicas' regions: forward offsets relative to each replica's first slot, forward columns at the
+// replica's edge region, backward rows laid out per replica region (each replica's rows packed from
+// the start of its region, as a build per replica would), in-degrees straight into the slot array.
+// A few dozen launches in all instead of a few dozen per replica.
+
+// raw edges [off[r], off[r+1]) belong to replica r: ids += the replica's first slot
+__global__ void __launch_bounds__(256) k_raw_to_slots(int32_t* src, int32_t* dst, int64_t m, const int64_t* off, int R,
+                                                      const Replica* rep) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < m; g += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = R - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= g)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const int32_t nb = (int32_t)rep[lo].nbase;
+        src[g] += nb;
+        dst[g] += nb;
+    }
+}
+
+// forward offsets of every replica from the slot-wide ones
+__global__ void __launch_bounds__(256) k_fwd_offsets(const int64_t* go, int64_t S, const int32_t* tile_rep,
+                                                     const Replica* rep, int64_t* fwd_off) {
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < S; s += (int64_t)gridDim.x * blockDim.x) {
+        const Replica& rp = rep[tile_rep[s / kTile]];
+        const int64_t v = s - rp.nbase;
+        if (v <= rp.n) fwd_off[rp.obase + v] = go[s] - go[rp.nbase];
+    }
+}
+
+// forward columns: unique edge p (slot-wide order) to its replica's edge region, as a local id
+__global__ void __launch_bounds__(256) k_fwd_columns(const int64_t* go, const int32_t* gc, int64_t S, int64_t m,
+                                                     const int32_t* tile_rep, const Replica* rep, int32_t* fwd_col) {
+    const int64_t u = go[S] < m ? go[S] : m;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < u; p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t d = gc[p];
+        const Replica& rp = rep[tile_rep[d / kTile]];
+        fwd_col[rp.ebase + (p - go[rp.nbase])] = d - (int32_t)rp.nbase;
+    }
+}
+
+// backward rows of every slot: the span starts relative to the replica's first slot's
+__global__ void __launch_bounds__(256) k_brow_rows_all(const int64_t* bo, const int64_t* gbeg, int64_t S,
+                                                       const int32_t* tile_rep, const Replica* rep, BRow* brow,
+                                                       int32_t* bcap) {
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < S; s += (int64_t)gridDim.x * blockDim.x) {
+        const Replica& rp = rep[tile_rep[s / kTile]];
+        const int64_t len = bo[s + 1] - bo[s];
+        BRow r;
+        r.beg4 = len > 0 ? (uint32_t)((gbeg[s] - gbeg[rp.nbase]) >> 2) : 0u;
+        r.len = (int32_t)len;
+        brow[s] = r;
+        bcap[s] = (int32_t)(len > 0 ? gbeg[s + 1] - gbeg[s] : 0);
+    }
+}
+
+// backward entry i (slot-wide order): the row is the last slot with bo[s] <= i
+__global__ void __launch_bounds__(256) k_brow_cols_all(const int64_t* bo, const int32_t* bc, const int64_t* gbeg,
+                                                       int64_t S, int64_t m, const int32_t* tile_rep,
+                                                       const Replica* rep, int32_t* bcol) {
+    const int64_t u = bo[S] < m ? bo[S] : m;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < u; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t lo = 0, hi = S - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (bo[mid] <= i)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const Replica& rp = rep[tile_rep[lo / kTile]];
+        bcol[rp.bbase + (gbeg[lo] - gbeg[rp.nbase]) + (i - bo[lo])] = bc[i] - (int32_t)rp.nbase;
+    }
+}
+
+// per replica: unique edges and backward entries laid out
+__global__ void k_rep_totals(const int64_t* go, const int64_t* gbeg, int R, const Replica* rep, int64_t* u,
+                             int64_t* laid) {
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        const Replica& rp = rep[r];
+        u[r] = go[rp.nbase + rp.n_cap] - go[rp.nbase];
+        laid[r] = gbeg[rp.nbase + rp.n_cap] - gbeg[rp.nbase];
+    }
+}
+
+size_t build_all_scratch_bytes(int64_t m, int64_t S) {
+    // the pieces launch_build_all carves, each rounded up to 256 bytes
+    return build_scratch_bytes(m, S) + (size_t)(S + 1) * 8 * 4 + (size_t)(m > 0 ? m : 1) * 4 * 2 + 8 +
+           (size_t)(scan_blocks_needed(S + 1) + 2) * 8 + 256 * 10;
+}
+
+void launch_build_all(int32_t* src, int32_t* dst, int64_t m, const int64_t* raw_off, int R, int64_t S,
+                      const int32_t* tile_rep, const Replica* rep, void* scratch, int64_t* fwd_off, int32_t* fwd_col,
+                      BRow* brow, int32_t* bcap, int32_t* bcol, int32_t* indeg, int64_t* u, int64_t* laid, uint32_t* err,
+                      cudaStream_t s) {
+    char* p = reinterpret_cast<char*>(scratch);
+    auto take = [&](size_t bytes) {
+        char* q = p;
+        p += (bytes + 255) & ~(size_t)255;
+        return q;
+    };
+    const int64_t e = m > 0 ? m : 1;
+    int64_t* go = reinterpret_cast<int64_t*>(take((size_t)(S + 1) * 8));
+    int64_t* bo = reinterpret_cast<int64_t*>(take((size_t)(S + 1) * 8));
+    int64_t* caps = reinterpret_cast<int64_t*>(take((size_t)(S + 1) * 8));
+    int64_t* gbeg = reinterpret_cast<int64_t*>(take((size_t)(S + 1) * 8));
+    int32_t* gc = reinterpret_cast<int32_t*>(take((size_t)e * 4));
+    int32_t* bc = reinterpret_cast<int32_t*>(take((size_t)e * 4));
+    int64_t* ucount = reinterpret_cast<int64_t*>(take(8));
+    void* inner = take(build_scratch_bytes(m, S));
+    int64_t* blocksum = reinterpret_cast<int64_t*>(take((size_t)(scan_blocks_needed(S + 1) + 2) * 8));
+    const unsigned gm = (unsigned)std::min<int64_t>((e + 255) / 256, 152 * 16);
+    const unsigned gs = (unsigned)std::min<int64_t>((S + 255) / 256, 152 * 16);
+    if (m > 0) k_raw_to_slots<<<gm, 256, 0, s>>>(src, dst, m, raw_off, R, rep);
+    launch_build_csr(src, dst, m, S, inner, go, gc, bo, bc, indeg, ucount, err, s);
+    k_fwd_offsets<<<gs, 256, 0, s>>>(go, S, tile_rep, rep, fwd_off);
+    if (m > 0) k_fwd_columns<<<gm, 256, 0, s>>>(go, gc, S, m, tile_rep, rep, fwd_col);
+    k_brow_caps<<<gs, 256, 0, s>>>(bo, S, caps);
+    launch_scan_i64(caps, gbeg, S, blocksum, s);
+    k_brow_rows_all<<<gs, 256, 0, s>>>(bo, gbeg, S, tile_rep, rep, brow, bcap);
+    if (m > 0) k_brow_cols_all<<<gm, 256, 0, s>>>(bo, bc, gbeg, S, m, tile_rep, rep, bcol);
+    k_rep_totals<<<1, 256, 0, s>>>(go, gbeg, R, rep, u, laid);
+}
+
 }  // namespace pg

@@ -488,6 +488,15 @@ void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t
 // replica's rows and region
 void launch_brow_layout(const int64_t* bo, const int32_t* bc, int64_t n, int64_t m, int64_t* caps,
                         int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcap, int32_t* bcol, cudaStream_t s);
+// the seeds of all replicas as one build over the arena's node slots (pg_build.cu): raw edges
+// src/dst (replica r's at [raw_off[r], raw_off[r+1]), rewritten in place to slot ids), the device
+// Replica array and tile map already uploaded; u/laid receive each replica's unique edges and
+// backward entries laid out
+size_t build_all_scratch_bytes(int64_t m, int64_t S);
+void launch_build_all(int32_t* src, int32_t* dst, int64_t m, const int64_t* raw_off, int R, int64_t S,
+                      const int32_t* tile_rep, const Replica* rep, void* scratch, int64_t* fwd_off, int32_t* fwd_col,
+                      BRow* brow, int32_t* bcap, int32_t* bcol, int32_t* indeg, int64_t* u, int64_t* laid, uint32_t* err,
+                      cudaStream_t s);
 // resident CTAs per SM of the k <= 64 agent kernel (after init_agent_kernels)
 int agent_occupancy(int thin, int small_hash);
 int64_t agent_warp_slots(int num_sms);
