@@ -110,7 +110,7 @@ struct pg_ctx {
     DBuf<float> fit, w;
     DBuf<uint64_t> cdf, tilesum, tileoff, tables;
     DBuf<int32_t> guide;
-    DBuf<int64_t> fwd_off, len_tmp, sort_small, sort_large, sort_large_off, eoff, blocksum, er_cnt, er_toff;
+    DBuf<int64_t> fwd_off, new_start, sort_small, sort_large, sort_large_off, eoff, blocksum, er_cnt, er_toff;
     DBuf<int32_t> fwd_col, bcol, bcap;
     DBuf<BRow> brow;
     DBuf<longlong2> reloc;  // copy tasks of the backward rows that move in an epoch
@@ -284,7 +284,7 @@ Arena make_arena(pg_ctx* c) {
     A.big_list = c->big_list.p;
     A.heavy_list = c->heavy_list.p;
     A.heavy_mark = c->heavy_mark.p;
-    A.len_tmp = c->len_tmp.p;
+    A.new_start = c->new_start.p;
     A.tilesum = c->tilesum.p;
     A.tileoff = c->tileoff.p;
     A.blocksum = c->blocksum.p;
@@ -596,7 +596,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     PG_CUDA(c, dalloc(c->w, S));
     PG_CUDA(c, dalloc(c->cdf, S));
     PG_CUDA(c, dalloc(c->guide, S));
-    PG_CUDA(c, dalloc(c->len_tmp, S));
+    PG_CUDA(c, dalloc(c->new_start, S));
     PG_CUDA(c, dalloc(c->sort_small, S));
     PG_CUDA(c, dalloc(c->sort_large, S));
     PG_CUDA(c, dalloc(c->sort_large_off, S));
@@ -1215,7 +1215,7 @@ void pg_destroy(pg_ctx* c) {
     dfree(c->out_stage_dst);
     dfree(c->er_ov);
     dfree(c->er_ovb);
-    DBuf<int64_t>* i64[] = {&c->fwd_off, &c->len_tmp,
+    DBuf<int64_t>* i64[] = {&c->fwd_off, &c->new_start,
                             &c->sort_small, &c->sort_large, &c->sort_large_off, &c->eoff,
                             &c->blocksum, &c->er_cnt, &c->er_toff};
     for (auto* b : i64) dfree(*b);

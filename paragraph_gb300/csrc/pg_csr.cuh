@@ -13,7 +13,7 @@
 //          new length = old + inc; a row without room for it takes a new span of brow_cap(new)
 //          entries from the region's bump pointer (one reservation per warp step) and lists its old
 //          entries for the copy in chunks of kRelocChunk; where the epoch's entries start goes to
-//          len_tmp; indeg += inc; rows with two or more new entries are listed for the sort
+//          new_start; indeg += inc; rows with two or more new entries are listed for the sort
 //   copy : the listed chunks moved in 16-byte vectors (on a side stream, beside place and sort)
 //   place: each new edge at its row's start of new entries + rank
 //   sort : the appended part of a row holds distinct new-node ids in atomic order; rows with up to
@@ -114,7 +114,7 @@ __device__ __forceinline__ void d_bwd_grow(const Arena& A, int64_t agents) {
             rw.beg4 = (uint32_t)(nb >> 2);
             A.bcap[slot] = (int32_t)need;
         }
-        A.len_tmp[slot] = beg + old;
+        A.new_start[slot] = beg + old;
         rw.len = (int32_t)nl;
         A.brow[slot] = rw;
         A.indeg[slot] += ic;
@@ -183,7 +183,7 @@ __device__ __forceinline__ void d_bwd_place(const Arena& A, int64_t agents) {
         const int32_t src = (int32_t)(rp.n + (a - rp.abase));
         const int64_t e0 = A.eoff[a], e1 = A.eoff[a + 1];
         int32_t* bc = A.bcol + rp.bbase;
-        const int64_t* st = A.len_tmp + rp.nbase;
+        const int64_t* st = A.new_start + rp.nbase;
         unsigned hm[2 * kMaskWords] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
         for (int64_t e = e0 + lane; e < e1; e += 32) {
             const int32_t j = A.e_dst[e];

@@ -192,7 +192,7 @@ struct Arena {
     long long* rc_big_meta;    // [kRcBigCap][3] entries, rows, elements of that stream
     longlong2* reloc;          // [reloc_cap] moved-row copy tasks: (source, destination << 16 | length)
     int64_t reloc_cap;
-    int64_t* len_tmp;          // [slots] where a row's new entries of the epoch start
+    int64_t* new_start;        // [slots] where a row's new entries of the epoch start
     uint64_t* tilesum;         // [ntiles]
     uint64_t* tileoff;         // [ntiles]
     int64_t* blocksum;         // [scan blocks]
