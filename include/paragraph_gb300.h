@@ -181,7 +181,9 @@ pg_status pg_run_epochs(pg_ctx* ctx, int32_t num_epochs, int32_t use_graph, int6
  * entries each), epoch by epoch and, within an epoch, replica by replica in forward-CSR order; the
  * per-epoch, per-replica counts go to counts[epoch * num_replicas + r] (may be NULL).  Page-locked
  * buffers (cudaHostAlloc / cudaHostRegister) are written by the device while the next epoch runs,
- * so the copy-out overlaps the growth; other buffers are filled after the run.  Replaces the
+ * so the copy-out overlaps the growth; other buffers are filled after the run.  An epoch whose
+ * citations do not fit the remaining capacity is grown but not written: the call then returns
+ * PG_ERR_CAPACITY with *new_edges = the citations written (the context stays usable).  Replaces the
  * reference's per-agent cudaMemcpy of the edges back to the host (includes/utils.cuh:151-200). */
 pg_status pg_run_epochs_out(pg_ctx* ctx, int32_t num_epochs, int32_t use_graph, int32_t* src, int32_t* dst,
                             int64_t capacity, int64_t* counts, int64_t* new_edges);

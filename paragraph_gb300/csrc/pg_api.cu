@@ -1590,6 +1590,7 @@ pg_status pg_run_epochs_out(pg_ctx* c, int32_t num_epochs, int32_t use_graph, in
         destroy_graph_exec(c);
         PG_CUDA(c, dalloc(c->out_counts, nc));
     }
+    PG_CUDA(c, cudaMemsetAsync(c->out_counts.p, 0, 8 * (size_t)nc, c->stream));  // epochs not written stay 0
     c->out_src = ds;
     c->out_dst = dd;
     c->out_cap = capacity;
@@ -1599,6 +1600,9 @@ pg_status pg_run_epochs_out(pg_ctx* c, int32_t num_epochs, int32_t use_graph, in
     c->out_src = c->out_dst = nullptr;
     c->out_cap = c->out_epochs = 0;
     if (s != PG_OK) return s;
+    // epochs whose citations did not fit the buffers were grown all the same; the caller learns of it
+    const bool short_out = c->h_st.out_short != 0;
+    if (short_out) ne = (int64_t)c->h_st.out_count;
     if (staged && ne > 0) {
         PG_CUDA(c, cudaMemcpyAsync(src, ds, 4 * (size_t)ne, cudaMemcpyDeviceToHost, c->stream));
         PG_CUDA(c, cudaMemcpyAsync(dst, dd, 4 * (size_t)ne, cudaMemcpyDeviceToHost, c->stream));
@@ -1607,6 +1611,10 @@ pg_status pg_run_epochs_out(pg_ctx* c, int32_t num_epochs, int32_t use_graph, in
         PG_CUDA(c, cudaMemcpyAsync(counts, c->out_counts.p, 8 * (size_t)nc, cudaMemcpyDeviceToHost, c->stream));
     PG_CUDA(c, cudaStreamSynchronize(c->stream));
     if (new_edges) *new_edges = ne;
+    if (short_out)
+        return fail(c, PG_ERR_CAPACITY, "output buffers hold " + std::to_string(capacity) + " citations; the run made " +
+                                            std::to_string(c->h_st.out_count + c->h_st.out_short) +
+                                            " (the graph grew; the epochs that did not fit were not written)");
     return PG_OK;
 }
 

@@ -222,8 +222,8 @@ __device__ __forceinline__ void d_copy_out(const Arena& A, int64_t agents) {
     if (!A.out_src || A.st->error) return;
     const int64_t base = (int64_t)A.st->out_count;
     const int64_t E = A.eoff[agents];
-    if (base + E > A.out_cap) {
-        if (threadIdx.x == 0) atomicOr(&A.st->error, kErrCapacity);
+    if (base + E > A.out_cap) {  // the buffers are full: the growth goes on, the host reports it
+        if (blockIdx.x == 0 && threadIdx.x == 0) A.st->out_short += (unsigned long long)E;
         return;
     }
     if (blockIdx.x == 0) {
@@ -381,7 +381,8 @@ __device__ __forceinline__ void d_epoch_end(const Arena& A, int64_t agents) {
         st->cum_new_nodes += (unsigned long long)agents;
         st->cum_epochs += 1;
         st->cum_adj_scanned += st->adj_scanned;
-        if (A.out_src) st->out_count += (unsigned long long)A.eoff[agents];
+        if (A.out_src && st->out_count + (unsigned long long)A.eoff[agents] <= (unsigned long long)A.out_cap)
+            st->out_count += (unsigned long long)A.eoff[agents];
     }
 }
 

@@ -152,6 +152,7 @@ struct EpochState {
     unsigned long long cum_epochs;
     unsigned long long cum_adj_scanned;
     unsigned long long out_count;   // citations streamed to the run's output buffers so far
+    unsigned long long out_short;   // citations that did not fit them (the run goes on; nothing is written past them)
     // grid barrier of the persistent epoch kernel: arrivals (back to 0 after every barrier, reset
     // by the host before each launch) and generation
     unsigned int gbar_count;

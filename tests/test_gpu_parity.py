@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from paragraph_gb300 import (PG_SAMPLER_ENUMERATE, PG_SAMPLER_THINNING, GrowthEngine, PGError,
+from paragraph_gb300 import (PG_ERR_CAPACITY, PG_SAMPLER_ENUMERATE, PG_SAMPLER_THINNING, GrowthEngine, PGError,
                              PAParams, ReplicaInput)
 from paragraph_gb300 import workloads as W
 
@@ -439,6 +439,27 @@ def test_run_epochs_out_streams_every_citation(gpu, pinned, replicas, epoch_kern
                 pos += k
         assert pos == ne
         assert done == [eng.counts(r)[1] for r in range(replicas)]
+
+
+def test_run_epochs_out_reports_short_buffers(gpu):
+    """Buffers too small for the run: the epochs that fit are written, the rest are grown but not
+    written, the call reports PG_ERR_CAPACITY, and the context stays usable."""
+    g = W.plain_pa_seed(4000, 10, seed=2)
+    prm = PAParams(mean_out_degree=20.0, growth_rate=0.05, fixed_new_nodes=0)
+    out = (np.empty(5000, np.int32), np.empty(5000, np.int32))  # about one epoch's citations
+    with GrowthEngine(seed=3) as eng:
+        eng.load_graph(g.pub, g.fitness, g.src, g.dst, prm, planned_epochs=5)
+        m0 = eng.counts()[1]
+        with pytest.raises(PGError) as err:
+            eng.run_epochs_out(4, out)
+        assert err.value.status == PG_ERR_CAPACITY
+        m1 = eng.counts()[1]
+        assert m1 > m0 + 5000  # all four epochs were grown
+        first = eng.edges(m0, 2000)
+        np.testing.assert_array_equal(out[0][:2000], first[0])
+        np.testing.assert_array_equal(out[1][:2000], first[1])
+        eng.grow_epoch()  # not poisoned
+        assert eng.counts()[1] > m1
 
 
 def test_edges_into_caller_buffers(gpu):
