@@ -193,18 +193,6 @@ __device__ __forceinline__ DF df_recip(const DF a) {
     return df_add(DF{r, 0.0f}, df_mulf(e, r));
 }
 
-// 1/D for D > 0 in FP64: Newton's iteration for the reciprocal, r' = r + r (1 - D r), started from
-// the fp32 reciprocal of the special-function unit (relative error < 2^-22); one step squares the
-// error (< 2^-44).  Outside the fp32 normal range the plain FP64 division is used.
-__device__ __forceinline__ double recip_nr(double D) {
-    if (!(D > 1e-30 && D < 1e30)) return 1.0 / D;
-    float rf;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"((float)D));
-    const double r = (double)rf;
-    const double e = __fma_rn(-D, r, 1.0);
-    return __fma_rn(r, e, r);
-}
-
 // log(1 - u) for u in [0, 0.5): -2 atanh(t), t = u / (2 - u) in [0, 1/3), by the odd Taylor series
 // of atanh, t + t^3/3 + ... + t^17/17 (truncation below 1e-9 relative at t = 1/3).
 __device__ __forceinline__ float log1m_pg(float u) {

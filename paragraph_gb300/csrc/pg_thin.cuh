@@ -87,12 +87,16 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t pari
     return false;
 }
 // bytes (a multiple of 16, both addresses 16-byte aligned) from global to shared memory, counted
-// on the barrier's transaction bytes
+// on the barrier's transaction bytes.  The copied rows are read once per test, so they are marked
+// first to leave L2 (evict-first policy): the per-node records, CDF and hub masks that every
+// event reads stay resident instead.
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
     asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
             smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
         : "memory");
 }
 
@@ -429,7 +433,8 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                 const int64_t st = __shfl_sync(kFull, r_st, L), e0 = __shfl_sync(kFull, excl, L);
                 ih[u] = __shfl_sync(kFull, into, L);
                 ok[u] = p < T;
-                v[u] = ok[u] ? ((L & 1) ? B.bc : B.fc)[st + (p - e0)] : 0;
+                // streaming load: the anchor rows are read once per agent
+                v[u] = ok[u] ? __ldcs(&((L & 1) ? B.bc : B.fc)[st + (p - e0)]) : 0;
             }
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
