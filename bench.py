@@ -641,6 +641,21 @@ def loglik_measure(args, world, rank, local, dist, with_cpu: bool = True) -> dic
         eng.loglik(p[None])
         eng.loglik_grad(p[None])
     ser_ms = reduce_max(dist, eng.timer_stop())
+    # the exact arithmetic (fp32 exp2 to ~2 ulp, ball weights and products summed one by one): the
+    # same batch and the same serial loop
+    eng.set_lik_exact_exp2(True)
+    for _ in range(max(1, args.warmup)):
+        step()
+    eng.timer_start()
+    for _ in range(args.steps):
+        step()
+    ms_x = reduce_max(dist, eng.timer_stop())
+    eng.timer_start()
+    for p in pts:
+        eng.loglik(p[None])
+        eng.loglik_grad(p[None])
+    ser_x = reduce_max(dist, eng.timer_stop())
+    eng.set_lik_exact_exp2(False)
     # end to end: host trace -> device, forward + adjoint, results on the host (wall clock)
     e2e = None
     if not args.no_e2e:
@@ -682,6 +697,11 @@ def loglik_measure(args, world, rank, local, dist, with_cpu: bool = True) -> dic
                      "note": "at 64 points the passes are bound by the per-point exp of every ball "
                              "element, not by HBM"},
         "serial": {"ms_per_step": ser_ms, "speedup": ser_ms / (ms_max / args.steps)},
+        "exact_arithmetic": {"value": evals / (ms_x / 1000.0), "unit": "gradient evals/s",
+                             "ms_per_step": ms_x / args.steps, "serial_ms_per_step": ser_x,
+                             "speedup": ser_x / (ms_x / args.steps),
+                             "note": "pg_lik_set_exact_exp2(1): gradient within 1e-6 of the FP64 "
+                                     "oracle at the generating point as well"},
         "e2e": e2e,
         "gpu_launches": 8 * args.steps,
         "clocks": clocks.summary(),

@@ -368,15 +368,17 @@ typedef struct {
 } pg_trace_desc;
 /* Copies the trace to the device (a trace and the growth state coexist in one context). */
 pg_status pg_trace_load(pg_ctx* ctx, const pg_trace_desc* trace);
+/* Arithmetic of the next forward passes (and of the adjoint passes that follow them): exact = 0
+ * (the default, fastest) takes 2^x from the GPU's special-function unit (relative error < 2^-22)
+ * of an exponent rounded once per node; exact = 1 carries the exponent and log f without rounding
+ * of their own, takes 2^x from fp32 arithmetic accurate to about 2 ulp and sums every ball weight
+ * and product on its own into compensated sums.  The per-node roundings of exact = 0 do not
+ * average out and leave about 1e-5 of the gradient's norm where the gradient nearly vanishes (at a
+ * trace's generating parameters; 1e-7 elsewhere); exact = 1 keeps the gradient within 1e-6 of the
+ * FP64 value there too, at about a third of the throughput. */
+pg_status pg_lik_set_exact_exp2(pg_ctx* ctx, int32_t exact);
 /* log L at each of batch points theta[b] = (alpha, tau, gamma, beta) (row-major [batch][4]).  Saves
  * the per-agent normalisers Z_a for pg_loglik_bwd. */
-/* Weights of the next forward passes (and of the adjoint passes that follow them): exact = 0 takes
- * 2^x from the GPU's special-function unit (relative error < 2^-22, the default, fastest); exact = 1
- * from fp32 arithmetic accurate to about 2 ulp.  The unit's error is a smooth function of the
- * argument that cancels in ratios of weights but leaves about 5e-6 of the gradient's norm where
- * the gradient nearly vanishes (e.g. at a trace's generating parameters); exact = 1 removes it at
- * about a third of the throughput. */
-pg_status pg_lik_set_exact_exp2(pg_ctx* ctx, int32_t exact);
 pg_status pg_loglik_fwd(pg_ctx* ctx, int32_t batch, const double* theta, double* loglik);
 /* Adjoint: grad[b][k] = dloglik[b] * d log L / d theta_k at the points of the last pg_loglik_fwd
  * (theta must be the same; dloglik NULL means all ones).  Weights are recomputed, not stored. */

@@ -614,8 +614,11 @@ class GrowthEngine:
         self._check(self._lib.pg_trace_load(self._ctx, C.byref(d)))
 
     def set_lik_exact_exp2(self, exact: bool) -> None:
-        """Weights of the next likelihood passes from an fp32 exp2 accurate to ~2 ulp (True) or the
-        special-function unit's (False, default)."""
+        """Arithmetic of the next likelihood passes: True carries the weight exponent without
+        rounding of its own, takes 2^x from an fp32 exp2 accurate to ~2 ulp and sums every ball
+        weight and product on its own (the gradient stays within 1e-6 of the FP64 value even where
+        it nearly vanishes); False (default) uses the special-function unit's exp2 of a once-rounded
+        exponent and pairwise ball sums, about three times as fast."""
         self._check(self._lib.pg_lik_set_exact_exp2(self._ctx, 1 if exact else 0))
 
     def loglik(self, theta) -> np.ndarray:

@@ -66,6 +66,7 @@ struct LikState {
     std::vector<double> fwd_theta;  // points of the last forward pass
     int32_t exact_exp2 = 0;         // pg_lik_set_exact_exp2
     int32_t fwd_exact_exp2 = 0;     // the mode of the last forward pass (the adjoint reuses it)
+    int32_t feat_exact = 0;         // the layout of the feature rows (the mode they were built for)
 };
 
 struct Checkpoint {
@@ -2445,7 +2446,15 @@ LikBalls make_balls(const LikState& L, int64_t a0) {
 // One pass (forward or adjoint) over every group of <= 64 points; results[b * K + k].
 pg_status run_lik(pg_ctx* c, int32_t batch, const double* theta, int adjoint, double* results) {
     LikState& L = c->lik;
-    if (!adjoint) L.fwd_exact_exp2 = L.exact_exp2;
+    if (!adjoint) {
+        L.fwd_exact_exp2 = L.exact_exp2;
+        if (L.feat_exact != L.exact_exp2) {  // the rows follow the mode; the adjoint keeps the forward's
+            cudaGetLastError();
+            launch_lik_features(make_trace(c), L.exact_exp2, c->num_sms, c->stream);
+            PG_CUDA(c, cudaGetLastError());
+            L.feat_exact = L.exact_exp2;
+        }
+    }
     const int groups = (batch + kLikMaxB - 1) / kLikMaxB;
     const int K = adjoint ? 4 : 1;
     const int64_t zneed = (int64_t)groups * std::max<int64_t>(L.agents, 1) * kLikMaxB;
@@ -2619,8 +2628,9 @@ pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
     L.eval_grid[0] = c->num_sms * eval_sm[0];
     L.eval_grid[1] = c->num_sms * eval_sm[1];
     cudaGetLastError();
-    launch_lik_features(make_trace(c), c->num_sms, c->stream);
+    launch_lik_features(make_trace(c), L.exact_exp2, c->num_sms, c->stream);
     PG_CUDA(c, cudaGetLastError());
+    L.feat_exact = L.exact_exp2;
     // balls: sizes first, then as many agents' balls per chunk as memory allows
     const int64_t na = std::max<int64_t>(agents, 1);
     PG_CUDA(c, dalloc(L.bcnt, na));

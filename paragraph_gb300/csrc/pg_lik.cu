@@ -5,20 +5,25 @@
 //
 // Weights: w_j = 2^(x2_j), x2_j = log2(e) (gamma log f_j + alpha log(indeg_j+1) - (t-t_j)/tau), the
 // exponent carried as an unevaluated fp32 pair h + l: the per-point constants are split into fp32
-// high and low parts and log(indeg+1) is stored as a high/low pair.  A plain fp32 exponent rounds
-// alpha log2 e, log2 e / tau and log(d+1) once for all nodes that share them -- an error that does
-// not average out over the trace and moves the gradient by the Hessian times a 2^-24 shift of
-// theta (about 1e-5 of the gradient at the generating point, where the gradient is small).  The
-// products enter h through FMAs whose one rounding also involves the continuous fitness term, so
-// what remains differs from node to node.  2^h comes from the special-function unit (PTX
-// ex2.approx.ftz.f32, relative error < 2^-22; results below 2^-126 flush to zero) and is scaled
-// by 1 + l ln 2; or, with exact_exp2, from exp2_exact (fp32 arithmetic, about 2 ulp).  The unit's
-// error is a smooth periodic function of the argument's fraction; it cancels in every ratio of
-// weights but leaves about 5e-6 of the gradient's norm where the gradient nearly vanishes (the
-// generating point of a trace), which exp2_exact removes at some 35 % of the throughput.  The same
-// weight function feeds every sum below, so the normalisers and the citations' prefix sums agree.  The per-epoch sums over all nodes are shared by every agent of
-// the epoch, so they are accumulated in FP64 (an fp32 partial's rounding would be common to all
-// of the epoch's citations); the per-agent ball sums use compensated fp32.
+// high and low parts and log(indeg+1) is stored as a high/low pair.  A feature or constant rounded
+// once to fp32 is a fixed error of every node that shares it -- it does not average out over the
+// trace and moves the gradient by the Hessian times a 2^-24 shift of the data or of theta, which
+// shows where the gradient nearly vanishes (the generating point of a trace).  Two arithmetic
+// modes:
+//   default     h by one FMA chain (its roundings are dropped), log f in fp32, 2^h from the
+//               special-function unit (PTX ex2.approx.ftz.f32, relative error < 2^-22; results
+//               below 2^-126 flush to zero) scaled by 1 + l ln 2, ball sums pairwise over four
+//               weights: ~1e-5 of the gradient's norm at the generating point of a 200k-node trace,
+//               1e-7 elsewhere;
+//   exact_exp2  every product and sum of the exponent keeps its rounding error, log f is an FP64 log
+//               carried as high part plus packed remainder, 2^(h + l) from exp2_exact (fp32
+//               arithmetic, about 2 ulp), and every ball weight and product is summed on its own
+//               (BallSum): ~3e-7 of the gradient's norm there, at about a third of the throughput.
+// The same weight function feeds every sum below, so the normalisers and the citations' prefix
+// sums agree: an error that is a smooth function of the weight (such as the unit's) largely
+// cancels between them.  The per-epoch sums over all nodes are shared by every agent of the epoch, so they are
+// accumulated in FP64 (an fp32 partial's rounding would be common to all of the epoch's
+// citations); the per-agent ball sums use compensated fp32.
 //
 // Per launch (forward or adjoint):
 //   k_lik_global      per epoch: sum_{j<n_e} w_j (forward) or sum_j w_j g_j (adjoint), one CTA per
@@ -35,6 +40,8 @@
 //                     reads only the forward's per-agent Z_a.
 //   k_lik_sum         agents -> totals per point (fixed order).
 #include "pg_lik.cuh"
+
+#include <cuda_fp16.h>
 
 namespace pg {
 
@@ -56,6 +63,52 @@ __device__ __forceinline__ void kadd(Kahan& k, float v) {
 }
 __device__ __forceinline__ double kval(const Kahan& k) { return (double)k.s - (double)k.c; }
 
+// A ball's sums for one point: S = sum w (and, in the adjoint, sum w g for the three continuous
+// features).  Default: four weights summed pairwise, products in FMA chains, then compensated fp32.
+// EXACT: every weight and every rounded product enters the compensated sums on its own and the
+// products' rounding errors (FMA residuals) are summed beside them, so a ball sum keeps no
+// rounding of its own above the compensated sum's (these per-agent errors otherwise reach ~3e-6
+// of the gradient where it nearly vanishes).
+template <bool ADJ, bool EXACT>
+struct BallSum {
+    Kahan s, t0, t1, t2;
+    float r0 = 0.f, r1 = 0.f, r2 = 0.f;
+    __device__ __forceinline__ void add1(const float w, const float4 f) {
+        kadd(s, w);
+        if (ADJ) {
+            const float p0 = w * f.y, p1 = w * f.z, p2 = w * f.x;
+            kadd(t0, p0);
+            kadd(t1, p1);
+            kadd(t2, p2);
+            if (EXACT) {
+                r0 += __fmaf_rn(w, f.y, -p0);
+                r1 += __fmaf_rn(w, f.z, -p1);
+                r2 += __fmaf_rn(w, f.x, -p2);
+            }
+        }
+    }
+    __device__ __forceinline__ void add4(const float w0, const float w1, const float w2, const float w3,
+                                         const float4 f0, const float4 f1, const float4 f2, const float4 f3) {
+        if (EXACT) {
+            add1(w0, f0);
+            add1(w1, f1);
+            add1(w2, f2);
+            add1(w3, f3);
+            return;
+        }
+        kadd(s, (w0 + w1) + (w2 + w3));
+        if (ADJ) {
+            kadd(t0, __fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
+            kadd(t1, __fmaf_rn(w3, f3.z, __fmaf_rn(w2, f2.z, __fmaf_rn(w1, f1.z, w0 * f0.z))));
+            kadd(t2, __fmaf_rn(w3, f3.x, __fmaf_rn(w2, f2.x, __fmaf_rn(w1, f1.x, w0 * f0.x))));
+        }
+    }
+    __device__ __forceinline__ double S() const { return kval(s); }
+    __device__ __forceinline__ double T0() const { return kval(t0) + (double)r0; }
+    __device__ __forceinline__ double T1() const { return kval(t1) + (double)r1; }
+    __device__ __forceinline__ double T2() const { return kval(t2) + (double)r2; }
+};
+
 // First position of x's backward row whose source is >= ne (rows ascending).
 __device__ __forceinline__ int64_t bwd_cut(const LikTrace& T, int64_t x, int64_t ne) {
     int64_t lo = T.bo[x], hi = T.bo[x + 1];
@@ -70,10 +123,12 @@ __device__ __forceinline__ int64_t bwd_cut(const LikTrace& T, int64_t x, int64_t
 }
 
 // Per-point constants of the weight exponent in base 2, each as an fp32 high part and the fp32
-// remainder of its FP64 value.
+// remainder of its FP64 value; al2s and ga2s scale the exact layout's packed low parts (stored
+// times 2^24) back.
 struct LikC {
     float al2, ga2, it2;     // alpha log2 e, gamma log2 e, log2 e / tau (high parts)
     float al2l, ga2l, it2l;  // their remainders
+    float al2s, ga2s;        // al2 2^-24, ga2 2^-24 (exact)
 };
 __device__ __forceinline__ LikC lik_c(const double* pp) {
     LikC c;
@@ -84,7 +139,23 @@ __device__ __forceinline__ LikC lik_c(const double* pp) {
     c.al2l = (float)(a - (double)c.al2);
     c.ga2l = (float)(g - (double)c.ga2);
     c.it2l = (float)(t - (double)c.it2);
+    c.al2s = c.al2 * 0x1p-24f;
+    c.ga2s = c.ga2 * 0x1p-24f;
     return c;
+}
+
+// The exact layout's fourth word: the fp32 remainders of log(d+1) (low half) and of log f (high
+// half), each times 2^24 as an IEEE half.  A remainder is at most 2^-25 of its high part, so 11 bits
+// of it carry the pair to about 2^-35.
+__device__ __forceinline__ float lik_pack_lows(float ly_rem24, float lx_rem24) {
+    const uint32_t y = __half_as_ushort(__float2half_rn(ly_rem24));
+    const uint32_t x = __half_as_ushort(__float2half_rn(lx_rem24));
+    return __uint_as_float(y | (x << 16));
+}
+__device__ __forceinline__ void lik_unpack_lows(float w, float& ly_rem24, float& lx_rem24) {
+    const uint32_t b = __float_as_uint(w);
+    ly_rem24 = __half2float(__ushort_as_half((unsigned short)(b & 0xFFFFu)));
+    lx_rem24 = __half2float(__ushort_as_half((unsigned short)(b >> 16)));
 }
 // 2^x on the special-function unit (PTX ex2.approx.ftz.f32).
 __device__ __forceinline__ float ex2_sfu(float x) {
@@ -92,8 +163,10 @@ __device__ __forceinline__ float ex2_sfu(float x) {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-// log2 of the weight, ga2 log f + al2 log(d+1) - it2 (t - t_j), as h + l.  Features: f.x = log f,
-// f.y + f.w = log(d+1) (high, low), f.z = t - t_j (an exact integer).
+// log2 of the weight, ga2 log f + al2 log(d+1) - it2 (t - t_j), as h + l.  Features: f.y = log(d+1)
+// (fp32 high part), f.z = t - t_j (an exact integer); default layout: f.x = log f in fp32 (logf_pg),
+// f.w = the remainder of log(d+1); exact layout: f.x = the fp32 high part of the FP64 log f,
+// f.w = both logs' remainders, packed (lik_pack_lows).
 struct X2 {
     float h, l;
 };
@@ -103,6 +176,16 @@ __device__ __forceinline__ float two_sum(float a, float b, float& err) {
     const float bb = s - a;
     err = (a - (s - bb)) + (b - bb);
     return s;
+}
+// the low-order terms of the exponent: the constants' remainders times the features' high parts,
+// the constants times the features' remainders (the exact layout also carries log f's)
+template <bool EXACT>
+__device__ __forceinline__ float lik_tail(const float4 f, const LikC& c) {
+    const float base = __fmaf_rn(c.al2l, f.y, __fmaf_rn(c.ga2l, f.x, -(c.it2l * f.z)));
+    if (!EXACT) return __fmaf_rn(c.al2, f.w, base);
+    float ly, lx;
+    lik_unpack_lows(f.w, ly, lx);
+    return __fmaf_rn(c.al2s, ly, __fmaf_rn(c.ga2s, lx, base));
 }
 template <bool EXACT>
 __device__ __forceinline__ X2 lik_x2(const float4 f, const LikC& c) {
@@ -116,11 +199,10 @@ __device__ __forceinline__ X2 lik_x2(const float4 f, const LikC& c) {
         float r1, r2;
         const float s1 = two_sum(p3, p1, r1);
         x.h = two_sum(s1, p2, r2);
-        x.l = ((e1 + e2) + (e3 + (r1 + r2))) +
-              __fmaf_rn(c.al2, f.w, __fmaf_rn(c.al2l, f.y, __fmaf_rn(c.ga2l, f.x, -(c.it2l * f.z))));
+        x.l = ((e1 + e2) + (e3 + (r1 + r2))) + lik_tail<true>(f, c);
     } else {
         x.h = __fmaf_rn(c.al2, f.y, __fmaf_rn(-c.it2, f.z, c.ga2 * f.x));
-        x.l = __fmaf_rn(c.al2, f.w, __fmaf_rn(c.al2l, f.y, __fmaf_rn(c.ga2l, f.x, -(c.it2l * f.z))));
+        x.l = lik_tail<false>(f, c);
     }
     return x;
 }
@@ -212,6 +294,8 @@ __device__ __forceinline__ float log1m_pg(float u) {
 
 }  // namespace
 
+// EXACT selects the exact layout (see lik_x2)
+template <bool EXACT>
 __global__ void __launch_bounds__(256) k_lik_features(LikTrace T) {
     const int e = blockIdx.y;
     const int64_t ne = T.epoch_nodes[e];
@@ -222,10 +306,16 @@ __global__ void __launch_bounds__(256) k_lik_features(LikTrace T) {
         const int64_t d = bwd_cut(T, j, ne) - T.bo[j];
         const double ly = log_pg((double)(d + 1));
         float4 f;
-        f.x = logf_pg(T.fit[j]);
         f.y = (float)ly;
         f.z = (float)(te - T.pub[j]);
-        f.w = (float)(ly - (double)f.y);
+        if (EXACT) {
+            const double lx = log_pg((double)T.fit[j]);
+            f.x = (float)lx;
+            f.w = lik_pack_lows((float)((ly - (double)f.y) * 0x1p24), (float)((lx - (double)f.x) * 0x1p24));
+        } else {
+            f.x = logf_pg(T.fit[j]);
+            f.w = (float)(ly - (double)f.y);
+        }
         F[j] = f;
     }
 }
@@ -440,7 +530,7 @@ __global__ void __launch_bounds__(kLikThreads, ADJ ? 2 : 3) k_lik_eval(LikTrace 
         const int e = T.agent_epoch[a];
         const float4* F = T.feat + (int64_t)e * T.n;
         const int64_t j0 = Bl.boff[a] - Bl.base, j1 = Bl.boff[a + 1] - Bl.base;
-        Kahan s[NP], t0[NP], t1[NP], t2[NP];
+        BallSum<ADJ, EXACT> acc[NP];
         if constexpr (NP == 2) {
             // the ball in batches of 32: lane l loads element l's id and feature row, the next
             // batch's loads are issued before this batch is summed, and the rows are read back
@@ -462,26 +552,13 @@ __global__ void __launch_bounds__(kLikThreads, ADJ ? 2 : 3) k_lik_eval(LikTrace 
                     for (int p = 0; p < NP; ++p) {
                         const float w0 = lik_w<EXACT>(lik_x2<EXACT>(f0, cq[p])), w1 = lik_w<EXACT>(lik_x2<EXACT>(f1, cq[p])),
                                     w2 = lik_w<EXACT>(lik_x2<EXACT>(f2, cq[p])), w3 = lik_w<EXACT>(lik_x2<EXACT>(f3, cq[p]));
-                        kadd(s[p], (w0 + w1) + (w2 + w3));
-                        if (ADJ) {
-                            kadd(t0[p], __fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
-                            kadd(t1[p], __fmaf_rn(w3, f3.z, __fmaf_rn(w2, f2.z, __fmaf_rn(w1, f1.z, w0 * f0.z))));
-                            kadd(t2[p], __fmaf_rn(w3, f3.x, __fmaf_rn(w2, f2.x, __fmaf_rn(w1, f1.x, w0 * f0.x))));
-                        }
+                        acc[p].add4(w0, w1, w2, w3, f0, f1, f2, f3);
                     }
                 }
                 for (; i < cnt; ++i) {
                     const float4 f = buf[i];
 #pragma unroll
-                    for (int p = 0; p < NP; ++p) {
-                        const float w = lik_w<EXACT>(lik_x2<EXACT>(f, cq[p]));
-                        kadd(s[p], w);
-                        if (ADJ) {
-                            kadd(t0[p], w * f.y);
-                            kadd(t1[p], w * f.z);
-                            kadd(t2[p], w * f.x);
-                        }
-                    }
+                    for (int p = 0; p < NP; ++p) acc[p].add1(lik_w<EXACT>(lik_x2<EXACT>(f, cq[p])), f);
                 }
                 cur = nxt;
             }
@@ -494,30 +571,22 @@ __global__ void __launch_bounds__(kLikThreads, ADJ ? 2 : 3) k_lik_eval(LikTrace 
             for (int p = 0; p < NP; ++p) {
                 const float w0 = lik_w<EXACT>(lik_x2<EXACT>(f0, cq[p])), w1 = lik_w<EXACT>(lik_x2<EXACT>(f1, cq[p])),
                             w2 = lik_w<EXACT>(lik_x2<EXACT>(f2, cq[p])), w3 = lik_w<EXACT>(lik_x2<EXACT>(f3, cq[p]));
-                kadd(s[p], (w0 + w1) + (w2 + w3));
-                if (ADJ) {
-                    kadd(t0[p], __fmaf_rn(w3, f3.y, __fmaf_rn(w2, f2.y, __fmaf_rn(w1, f1.y, w0 * f0.y))));
-                    kadd(t1[p], __fmaf_rn(w3, f3.z, __fmaf_rn(w2, f2.z, __fmaf_rn(w1, f1.z, w0 * f0.z))));
-                    kadd(t2[p], __fmaf_rn(w3, f3.x, __fmaf_rn(w2, f2.x, __fmaf_rn(w1, f1.x, w0 * f0.x))));
-                }
+                acc[p].add4(w0, w1, w2, w3, f0, f1, f2, f3);
             }
         }
         for (; q < j1; q += SL) {
             const float4 f = F[Bl.ids[q]];
 #pragma unroll
-            for (int p = 0; p < NP; ++p) {
-                const float w = lik_w<EXACT>(lik_x2<EXACT>(f, cq[p]));
-                kadd(s[p], w);
-                if (ADJ) {
-                    kadd(t0[p], w * f.y);
-                    kadd(t1[p], w * f.z);
-                    kadd(t2[p], w * f.x);
-                }
-            }
+            for (int p = 0; p < NP; ++p) acc[p].add1(lik_w<EXACT>(lik_x2<EXACT>(f, cq[p])), f);
         }
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-            double S = kval(s[p]), T0 = kval(t0[p]), T1 = kval(t1[p]), T2 = kval(t2[p]);
+            double S = acc[p].S(), T0 = 0.0, T1 = 0.0, T2 = 0.0;
+            if (ADJ) {
+                T0 = acc[p].T0();
+                T1 = acc[p].T1();
+                T2 = acc[p].T2();
+            }
             for (int o = BW; o < 32; o <<= 1) {
                 S += __shfl_xor_sync(0xffffffffu, S, o);
                 if (ADJ) {
@@ -709,11 +778,15 @@ void launch_lik_sum(const LikTrace& T, const LikBatch& P, int adjoint, cudaStrea
     k_lik_sum<<<(unsigned)(P.B * K), 256, 0, s>>>(P.out, T.agents, P.B, K, P.res);
 }
 
-void launch_lik_features(const LikTrace& T, int num_sms, cudaStream_t s) {
+void launch_lik_features(const LikTrace& T, int exact, int num_sms, cudaStream_t s) {
     int64_t gx = (T.n + 255) / 256;
     if (gx > (int64_t)num_sms * 8) gx = (int64_t)num_sms * 8;
     if (gx < 1) gx = 1;
-    k_lik_features<<<dim3((unsigned)gx, (unsigned)T.epochs), 256, 0, s>>>(T);
+    const dim3 grid((unsigned)gx, (unsigned)T.epochs);
+    if (exact)
+        k_lik_features<true><<<grid, 256, 0, s>>>(T);
+    else
+        k_lik_features<false><<<grid, 256, 0, s>>>(T);
 }
 
 }  // namespace pg

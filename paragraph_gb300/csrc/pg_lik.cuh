@@ -3,7 +3,8 @@
 //
 // The trace lives in its own buffers beside the growth arena:
 //   final graph as forward and backward CSR (rows sorted ascending), int64 offsets;
-//   feat[e][j] = (log f_j, log(indeg_e(j)+1), t_e - t_j, 0) for every trace epoch e and node j < n_e,
+//   feat[e][j] = (log f_j, log(indeg_e(j)+1), t_e - t_j, low parts) for every trace epoch e and node j < n_e
+//   in the layout of the arithmetic mode of the last forward pass,
 //   one float4 per (epoch, node) so a weight is one 16-byte gather and one exp;
 //   per agent: its epoch, anchors [4] and citations in draw order (cite offsets int64).
 // indeg_e(j) is the number of in-edges of j from nodes < n_e: the prefix of j's backward row below
@@ -71,7 +72,8 @@ struct LikBalls {
 size_t lik_ball_smem(int bitmap_words);
 // resident CTAs per SM: ball kernels (*ball_per_sm), forward and adjoint pass (eval_per_sm[2])
 cudaError_t init_lik_kernels(int bitmap_words, int* ball_per_sm, int* eval_per_sm);
-void launch_lik_features(const LikTrace& T, int num_sms, cudaStream_t s);
+// the feature rows in the layout of the arithmetic mode (exact: packed low parts of both logs)
+void launch_lik_features(const LikTrace& T, int exact, int num_sms, cudaStream_t s);
 // emit = 0: ball sizes into Bl.cnt / Bl.adj; 1: ball ids and citation flags
 void launch_lik_ball(const LikTrace& T, const LikBalls& Bl, int emit, int64_t a0, int64_t a1, int grid,
                      cudaStream_t s);

@@ -120,10 +120,19 @@ def test_calibration_config_full_size(gpu):
         eng.load_trace(tg)
         ll = eng.loglik(pts)
         gr = eng.loglik_grad(pts)
+        eng.set_lik_exact_exp2(True)
+        lx = eng.loglik(pts)
+        gx = eng.loglik_grad(pts)
     llo, gro = O.loglik(to, pts)
     rel_ll = np.abs(ll - llo) / np.abs(llo)
     rel_g = np.linalg.norm(gr - gro, axis=1) / np.linalg.norm(gro, axis=1)
-    msg = f"loglik {rel_ll.max():.3g}, grad (8 points) {rel_g[1:].max():.3g}, grad (theta*) {rel_g[0]:.3g}"
-    assert rel_ll.max() <= 1e-7, msg
+    rel_lx = np.abs(lx - llo) / np.abs(llo)
+    rel_gx = np.linalg.norm(gx - gro, axis=1) / np.linalg.norm(gro, axis=1)
+    msg = (f"loglik {rel_ll.max():.3g}, grad (8 points) {rel_g[1:].max():.3g}, grad (theta*) {rel_g[0]:.3g}; "
+           f"exact: loglik {rel_lx.max():.3g}, grad (8 points) {rel_gx[1:].max():.3g}, grad (theta*) {rel_gx[0]:.3g}")
+    print(msg)
+    assert rel_ll.max() <= 1e-7 and rel_lx.max() <= 1e-7, msg
     assert rel_g[1:].max() <= 1e-6, msg
     assert rel_g[0] <= 1e-5, msg
+    # the exact arithmetic meets the gradient bound at the generating point too
+    assert rel_gx.max() <= 1e-6, msg
