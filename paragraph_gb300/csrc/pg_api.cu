@@ -491,8 +491,9 @@ pg_status alloc_epoch_buffers(pg_ctx* c, int64_t agent_cap, int64_t edge_cap, in
         c->blocks_cap = blocks;
     }
     // copy tasks of the backward rows that move in one epoch: a moved row is a cited one (at most
-    // one per edge) and its old entries, at most the replica's m, split into kRelocChunk chunks
-    const int64_t reloc = c->edge_cap + c->M / kRelocChunk + c->R + 1;
+    // one per edge); its old entries (at most the replica's m) and forward row copy (at most m + 3 n
+    // over all rows) split into kRelocChunk chunks
+    const int64_t reloc = c->edge_cap + (2 * c->M + 3 * c->S) / kRelocChunk + c->R + 1;
     if (reloc > c->reloc.n) {
         destroy_graph_exec(c);
         PG_CUDA(c, dalloc(c->reloc, reloc + reloc / 2));
@@ -765,8 +766,9 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         }
         // the backward rows with room to grow (h.m bounds the entries; the layout reads the count)
         if (n) {
-            launch_brow_layout(t_bo.p, t_bc.p, (int64_t)n, h.m, t_caps.p, t_begs.p, t_bsum.p, c->brow.p + h.nbase,
-                               c->bcap.p + h.nbase, c->bcol.p + h.bbase, c->stream);
+            launch_brow_layout(t_bo.p, t_bc.p, c->fwd_off.p + h.obase, c->fwd_col.p + h.ebase, (int64_t)n, h.m,
+                               t_caps.p, t_begs.p, t_bsum.p, c->brow.p + h.nbase, c->bcap.p + h.nbase,
+                               c->bcol.p + h.bbase, c->stream);
             PG_CUDA(c, cudaGetLastError());
             PG_CUDA(c, cudaMemcpyAsync(t_laid.p + r, t_begs.p + n, 8, cudaMemcpyDeviceToDevice, c->stream));
         }

@@ -244,30 +244,33 @@ void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t
 
 // ---------------------------------------------------------------- growable backward rows
 // The engine keeps backward rows with room to grow (BRow).  From a backward CSR in offset form
-// (bo: n + 1 offsets, bc: its columns), row v gets brow_cap(len) entries -- none when empty -- at
-// the exclusive scan of those spans, and its entries are copied there.
-__global__ void __launch_bounds__(256) k_brow_caps(const int64_t* bo, int64_t n, int64_t* caps) {
+// (bo: n + 1 offsets, bc: its columns) and the forward offsets fo, row v of length L > 0 gets a span
+// of brow_span(L, P) entries, P = fwd_prefix(out-degree), at the exclusive scan of the spans: its
+// forward row copy ends at the span start + P (= 4 beg4), its backward entries follow.  A row with
+// no backward entry gets no span.
+__global__ void __launch_bounds__(256) k_brow_caps(const int64_t* bo, const int64_t* fo, int64_t n, int64_t* caps) {
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
         const int64_t len = bo[v + 1] - bo[v];
-        caps[v] = len > 0 ? brow_cap(len) : 0;
+        caps[v] = len > 0 ? brow_span(len, fwd_prefix(fo[v + 1] - fo[v])) : 0;
     }
 }
 
-__global__ void __launch_bounds__(256) k_brow_rows(const int64_t* bo, const int64_t* begs, int64_t n, BRow* brow,
-                                                   int32_t* bcap) {
+__global__ void __launch_bounds__(256) k_brow_rows(const int64_t* bo, const int64_t* fo, const int64_t* begs, int64_t n,
+                                                   BRow* brow, int32_t* bcap) {
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
         const int64_t len = bo[v + 1] - bo[v];
+        const int64_t P = len > 0 ? fwd_prefix(fo[v + 1] - fo[v]) : 0;
         BRow r;
-        r.beg4 = len > 0 ? (uint32_t)(begs[v] >> 2) : 0u;
+        r.beg4 = len > 0 ? (uint32_t)((begs[v] + P) >> 2) : 0u;
         r.len = (int32_t)len;
         brow[v] = r;
-        bcap[v] = (int32_t)(len > 0 ? begs[v + 1] - begs[v] : 0);
+        bcap[v] = (int32_t)(len > 0 ? begs[v + 1] - begs[v] - P : 0);
     }
 }
 
 // entry p of the offset form goes to its row's span: the row is the last v with bo[v] <= p (bo[n],
 // the entry count, is read on the device; m only bounds it)
-__global__ void __launch_bounds__(256) k_brow_cols(const int64_t* bo, const int32_t* bc, const int64_t* begs,
+__global__ void __launch_bounds__(256) k_brow_cols(const int64_t* bo, const int32_t* bc, const BRow* brow,
                                                    int64_t n, int64_t m, int32_t* out) {
     const int64_t mm = bo[n] < m ? bo[n] : m;
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < mm; p += (int64_t)gridDim.x * blockDim.x) {
@@ -279,20 +282,38 @@ __global__ void __launch_bounds__(256) k_brow_cols(const int64_t* bo, const int3
             else
                 hi = mid - 1;
         }
-        out[begs[lo] + (p - bo[lo])] = bc[p];
+        out[((int64_t)brow[lo].beg4 << 2) + (p - bo[lo])] = bc[p];
     }
 }
 
-void launch_brow_layout(const int64_t* bo, const int32_t* bc, int64_t n, int64_t m, int64_t* caps,
-                        int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcap, int32_t* bcol, cudaStream_t s) {
+// the forward row copies in front of the laid-out rows: one warp per node with a span
+__global__ void __launch_bounds__(256) k_brow_prefix(const int64_t* fo, const int32_t* fc, const BRow* brow, int64_t n,
+                                                     int32_t* out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = warp; v < n; v += nwarps) {
+        const BRow r = brow[v];
+        if (r.len <= 0) continue;
+        const int64_t f0 = fo[v], o = fo[v + 1] - f0;
+        int32_t* dst = out + ((int64_t)r.beg4 << 2) - o;
+        for (int64_t i = lane; i < o; i += 32) dst[i] = fc[f0 + i];
+    }
+}
+
+void launch_brow_layout(const int64_t* bo, const int32_t* bc, const int64_t* fo, const int32_t* fc, int64_t n,
+                        int64_t m, int64_t* caps, int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcap,
+                        int32_t* bcol, cudaStream_t s) {
     if (n <= 0) return;
     const unsigned gn = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
-    k_brow_caps<<<gn, 256, 0, s>>>(bo, n, caps);
+    k_brow_caps<<<gn, 256, 0, s>>>(bo, fo, n, caps);
     launch_scan_i64(caps, begs, n, blocksum, s);
-    k_brow_rows<<<gn, 256, 0, s>>>(bo, begs, n, brow, bcap);
+    k_brow_rows<<<gn, 256, 0, s>>>(bo, fo, begs, n, brow, bcap);
     if (m > 0) {
         const unsigned gm = (unsigned)std::min<int64_t>((m + 255) / 256, 152 * 16);
-        k_brow_cols<<<gm, 256, 0, s>>>(bo, bc, begs, n, m, bcol);
+        k_brow_cols<<<gm, 256, 0, s>>>(bo, bc, brow, n, m, bcol);
+        const unsigned gw = (unsigned)std::min<int64_t>((n + 7) / 8, 152 * 16);
+        k_brow_prefix<<<gw, 256, 0, s>>>(fo, fc, brow, n, bcol);
     }
 }
 
@@ -344,23 +365,42 @@ __global__ void __launch_bounds__(256) k_fwd_columns(const int64_t* go, const in
     }
 }
 
-// backward rows of every slot: the span starts relative to the replica's first slot's
-__global__ void __launch_bounds__(256) k_brow_rows_all(const int64_t* bo, const int64_t* gbeg, int64_t S,
-                                                       const int32_t* tile_rep, const Replica* rep, BRow* brow,
-                                                       int32_t* bcap) {
+// backward rows of every slot: the span starts relative to the replica's first slot's, the forward
+// row copy (prefix P) first
+__global__ void __launch_bounds__(256) k_brow_rows_all(const int64_t* bo, const int64_t* go, const int64_t* gbeg,
+                                                       int64_t S, const int32_t* tile_rep, const Replica* rep,
+                                                       BRow* brow, int32_t* bcap) {
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < S; s += (int64_t)gridDim.x * blockDim.x) {
         const Replica& rp = rep[tile_rep[s / kTile]];
         const int64_t len = bo[s + 1] - bo[s];
+        const int64_t P = len > 0 ? fwd_prefix(go[s + 1] - go[s]) : 0;
         BRow r;
-        r.beg4 = len > 0 ? (uint32_t)((gbeg[s] - gbeg[rp.nbase]) >> 2) : 0u;
+        r.beg4 = len > 0 ? (uint32_t)((gbeg[s] - gbeg[rp.nbase] + P) >> 2) : 0u;
         r.len = (int32_t)len;
         brow[s] = r;
-        bcap[s] = (int32_t)(len > 0 ? gbeg[s + 1] - gbeg[s] : 0);
+        bcap[s] = (int32_t)(len > 0 ? gbeg[s + 1] - gbeg[s] - P : 0);
+    }
+}
+
+// forward row copies of every slot with a span (slot-wide columns hold slot ids: made local)
+__global__ void __launch_bounds__(256) k_brow_prefix_all(const int64_t* go, const int32_t* gc, const BRow* brow,
+                                                         int64_t S, const int32_t* tile_rep, const Replica* rep,
+                                                         int32_t* bcol) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp; s < S; s += nwarps) {
+        const BRow r = brow[s];
+        if (r.len <= 0) continue;
+        const Replica& rp = rep[tile_rep[s / kTile]];
+        const int64_t f0 = go[s], o = go[s + 1] - f0;
+        int32_t* dst = bcol + rp.bbase + ((int64_t)r.beg4 << 2) - o;
+        for (int64_t i = lane; i < o; i += 32) dst[i] = gc[f0 + i] - (int32_t)rp.nbase;
     }
 }
 
 // backward entry i (slot-wide order): the row is the last slot with bo[s] <= i
-__global__ void __launch_bounds__(256) k_brow_cols_all(const int64_t* bo, const int32_t* bc, const int64_t* gbeg,
+__global__ void __launch_bounds__(256) k_brow_cols_all(const int64_t* bo, const int32_t* bc, const BRow* brow,
                                                        int64_t S, int64_t m, const int32_t* tile_rep,
                                                        const Replica* rep, int32_t* bcol) {
     const int64_t u = bo[S] < m ? bo[S] : m;
@@ -374,7 +414,7 @@ __global__ void __launch_bounds__(256) k_brow_cols_all(const int64_t* bo, const 
                 hi = mid - 1;
         }
         const Replica& rp = rep[tile_rep[lo / kTile]];
-        bcol[rp.bbase + (gbeg[lo] - gbeg[rp.nbase]) + (i - bo[lo])] = bc[i] - (int32_t)rp.nbase;
+        bcol[rp.bbase + ((int64_t)brow[lo].beg4 << 2) + (i - bo[lo])] = bc[i] - (int32_t)rp.nbase;
     }
 }
 
@@ -420,10 +460,14 @@ void launch_build_all(int32_t* src, int32_t* dst, int64_t m, const int64_t* raw_
     launch_build_csr(src, dst, m, S, inner, go, gc, bo, bc, indeg, ucount, err, s);
     k_fwd_offsets<<<gs, 256, 0, s>>>(go, S, tile_rep, rep, fwd_off);
     if (m > 0) k_fwd_columns<<<gm, 256, 0, s>>>(go, gc, S, m, tile_rep, rep, fwd_col);
-    k_brow_caps<<<gs, 256, 0, s>>>(bo, S, caps);
+    k_brow_caps<<<gs, 256, 0, s>>>(bo, go, S, caps);
     launch_scan_i64(caps, gbeg, S, blocksum, s);
-    k_brow_rows_all<<<gs, 256, 0, s>>>(bo, gbeg, S, tile_rep, rep, brow, bcap);
-    if (m > 0) k_brow_cols_all<<<gm, 256, 0, s>>>(bo, bc, gbeg, S, m, tile_rep, rep, bcol);
+    k_brow_rows_all<<<gs, 256, 0, s>>>(bo, go, gbeg, S, tile_rep, rep, brow, bcap);
+    if (m > 0) {
+        k_brow_cols_all<<<gm, 256, 0, s>>>(bo, bc, brow, S, m, tile_rep, rep, bcol);
+        const unsigned gw = (unsigned)std::min<int64_t>((S + 7) / 8, 152 * 16);
+        k_brow_prefix_all<<<gw, 256, 0, s>>>(go, gc, brow, S, tile_rep, rep, bcol);
+    }
     k_rep_totals<<<1, 256, 0, s>>>(go, gbeg, R, rep, u, laid);
 }
 

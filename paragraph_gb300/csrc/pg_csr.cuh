@@ -10,11 +10,14 @@
 // appends to:
 //   grow : one thread per edge; each cited node is handled once, by its edge of rank 0 (the agent
 //          kernel's in-degree increment returned each edge's rank among the node's new entries):
-//          new length = old + inc; a row without room for it takes a new span of brow_cap(new)
-//          entries from the region's bump pointer (one reservation per warp step) and lists its old
-//          entries for the copy in chunks of kRelocChunk; where the epoch's entries start goes to
-//          new_start; indeg += inc; rows with two or more new entries are listed for the sort
-//   copy : the listed chunks moved in 16-byte vectors (on a side stream, beside place and sort)
+//          new length = old + inc; a row without room for it takes a new span of
+//          brow_span(new, P) entries from the region's bump pointer (one reservation per warp step,
+//          P = fwd_prefix(out-degree)) and lists for the copy, in chunks of kRelocChunk, its old
+//          span's forward row copy and entries -- or, at its first citation, its forward row from
+//          the forward CSR; where the epoch's entries start goes to new_start; indeg += inc; rows
+//          with two or more new entries are listed for the sort
+//   copy : the listed chunks moved in 16-byte vectors, forward rows entry by entry (on a side
+//          stream, beside place and sort)
 //   place: each new edge at its row's start of new entries + rank
 //   sort : the appended part of a row holds distinct new-node ids in atomic order; rows with up to
 //          256 new entries are sorted by a register bitonic network in one warp, longer ones by a
@@ -55,17 +58,24 @@ __device__ __forceinline__ void d_bwd_grow(const Arena& A, int64_t agents) {
         const int r = A.R == 1 ? 0 : replica_of_edge(A, e < E ? e : E - 1);
         Replica& rp = A.rep[r];
         bool mine = e < E && A.e_rank[e] == 0;
-        int64_t slot = 0, nl = 0, need = 0, nch = 0;
+        int64_t slot = 0, nl = 0, need = 0, nch = 0, f0 = 0, o = 0, P = 0, mv = 0;
         int ic = 0;
         BRow rw{0u, 0};
         if (mine) {
-            slot = rp.nbase + A.e_dst[e];
+            const int32_t v = A.e_dst[e];
+            slot = rp.nbase + v;
             ic = A.inc[slot];
             rw = A.brow[slot];
             nl = (int64_t)rw.len + ic;
             if (nl > A.bcap[slot]) {
-                need = brow_cap(nl);
-                nch = (rw.len + kRelocChunk - 1) / kRelocChunk;
+                const int64_t* fo = A.fwd_off + rp.obase;
+                f0 = fo[v];
+                o = fo[v + 1] - f0;
+                P = fwd_prefix(o);
+                need = brow_span(nl, P);
+                // a row with a span moves its prefix and entries; a first span copies the forward row
+                mv = rw.len > 0 ? P + rw.len : o;
+                nch = (mv + kRelocChunk - 1) / kRelocChunk;
             }
         }
         // the step's reservations, one atomic each where the warp lies in one replica: region
@@ -103,16 +113,20 @@ __device__ __forceinline__ void d_bwd_grow(const Arena& A, int64_t agents) {
         const int64_t old = rw.len;
         int64_t beg = (int64_t)rw.beg4 << 2;
         if (need) {
+            // moves: from the old span's start (4 beg4 - P), both spans 16-byte aligned; first spans:
+            // from the forward CSR (a negative source, -1 - index) to the o entries before 4 beg4
             const int64_t q = cbase + cincl - nch;
+            const int64_t src0 = old > 0 ? rp.bbase + beg - P : -1 - (rp.ebase + f0);
+            const int64_t dst0 = rp.bbase + nb + (old > 0 ? 0 : P - o);
             for (int64_t c = 0; c < nch; ++c) {
                 const int64_t off = c * kRelocChunk;
-                const int64_t len = old - off < kRelocChunk ? old - off : kRelocChunk;
-                A.reloc[q + c] = make_longlong2(rp.bbase + beg + off, ((rp.bbase + nb + off) << 16) | len);
+                const int64_t len = mv - off < kRelocChunk ? mv - off : kRelocChunk;
+                A.reloc[q + c] = make_longlong2(old > 0 ? src0 + off : src0 - off, ((dst0 + off) << 16) | len);
             }
-            moved += (unsigned long long)old;
-            beg = nb;
-            rw.beg4 = (uint32_t)(nb >> 2);
-            A.bcap[slot] = (int32_t)need;
+            moved += (unsigned long long)mv;
+            beg = nb + P;
+            rw.beg4 = (uint32_t)(beg >> 2);
+            A.bcap[slot] = (int32_t)(need - P);
         }
         A.new_start[slot] = beg + old;
         rw.len = (int32_t)nl;
@@ -132,10 +146,12 @@ __device__ __forceinline__ void d_bwd_grow(const Arena& A, int64_t agents) {
 
 __global__ void __launch_bounds__(256) k_bwd_grow(Arena A, int64_t agents) { d_bwd_grow(A, agents); }
 
-// The old entries of the rows that moved, one listed chunk (at most kRelocChunk entries) per warp:
-// source and destination are 16-byte aligned, the copy goes in int4 vectors with eight of them per
-// lane in flight, and the chunk's last (len mod 4) entries one by one -- the vector past them would
-// overwrite the row's first new entries, which the placement writes at the same time.
+// The old spans of the rows that moved (forward row copy and entries), one listed chunk (at most
+// kRelocChunk entries) per warp: source and destination are 16-byte aligned, the copy goes in int4
+// vectors with eight of them per lane in flight, and the chunk's last (len mod 4) entries one by
+// one -- the vector past them would overwrite the row's first new entries, which the placement
+// writes at the same time.  A chunk with a negative source (-1 - index) is a first span's forward
+// row, copied entry by entry from the forward CSR (no alignment in common).
 __device__ __forceinline__ void d_bwd_reloc(const Arena& A) {
     if (A.st->error) return;
     const int lane = lane_id();
@@ -147,6 +163,11 @@ __device__ __forceinline__ void d_bwd_reloc(const Arena& A) {
         const longlong2 t = A.reloc[i];
         const int64_t src = t.x, dst = t.y >> 16;
         const int len = (int)(t.y & 0xffff);
+        if (src < 0) {
+            const int32_t* f = A.fwd_col + (-1 - src);
+            for (int j = lane; j < len; j += 32) A.bcol[dst + j] = f[j];
+            continue;
+        }
         const int nv = len >> 2;
         const int4* s4 = reinterpret_cast<const int4*>(A.bcol + src);
         int4* d4 = reinterpret_cast<int4*>(A.bcol + dst);

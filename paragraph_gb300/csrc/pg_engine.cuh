@@ -60,19 +60,32 @@ enum : uint32_t {
 // Backward row of a node: entries bcol[bbase + 4 beg4, bbase + 4 beg4 + len), so every row starts on
 // a 16-byte boundary; its room (a multiple of 4 entries, 0 for an empty row) is kept apart in bcap,
 // which only the append reads, so the record the samplers load per node is 8 bytes.
+//
+// A node's span in the region, once the node has been cited (len > 0):
+//   [ pad | forward row copy (o entries) | backward entries (len) | room ]
+//   ^ span start (16-byte aligned)        ^ 4 beg4 (16-byte aligned)
+// where o is the node's out-degree and pad + o = fwd_prefix(o).  The copy makes the node's
+// forward and backward rows one contiguous window, so the thinning sampler stages a tested
+// candidate with one bulk copy instead of two.  A node never cited has no span (len = 0, beg4 = 0,
+// room 0): its forward row is read from the forward CSR.
 struct __align__(8) BRow {
     uint32_t beg4;
     int32_t len;
 };
 constexpr int64_t kBRegionMax = (int64_t)1 << 34;  // entries a backward region may span (beg4 is 32-bit)
 
-// Room given to a backward row that must hold L >= 1 entries: 2L rounded up to a multiple of 4.  A
-// row that outgrows its room moves, so its earlier spans c_0 < c_1 < ... < c_k satisfy
-// c_i < L_(i+1) <= c_(i+1) / 2: together they take less than 2 c_k <= 4 L + 4 entries (L its final
-// length), and a region of 4 m + 4 n entries (m edges, n nodes at most) never runs out.  Each entry
-// moves O(1) times amortised.
+// Room given to a backward row that must hold L >= 1 entries: 2L rounded up to a multiple of 4.
 PG_HD int64_t brow_cap(int64_t L) { return (2 * L + 3) & ~3ll; }
-PG_HD int64_t bregion_entries(int64_t n_cap, int64_t m_cap) { return 4 * m_cap + 4 * n_cap + 4; }
+// Entries before 4 beg4 that hold the forward row copy of a node of out-degree o.
+PG_HD int64_t fwd_prefix(int64_t o) { return (o + 3) & ~3ll; }
+// Span of a cited row of L >= 1 backward entries and prefix P: brow_cap(L + P); its room (entries
+// from 4 beg4) is the span minus P, at least 2 L + P.  A row that outgrows its room moves to a new
+// span, so the totals T_k = L_k + P of its spans c_k = brow_cap(T_k) satisfy
+// c_k < T_(k+1) <= c_(k+1) / 2: together the spans take less than 2 c_K <= 4 (L + P) + 6 entries (L
+// the final length).  Over all rows (sum of L <= m, sum of P <= m + 3 n) a region of 8 m + 18 n + 4
+// entries never runs out; each entry moves O(1) times amortised.
+PG_HD int64_t brow_span(int64_t L, int64_t P) { return brow_cap(L + P); }
+PG_HD int64_t bregion_entries(int64_t n_cap, int64_t m_cap) { return 8 * m_cap + 18 * n_cap + 4; }
 
 struct Replica {
     // static layout
@@ -484,11 +497,13 @@ size_t build_scratch_bytes(int64_t m, int64_t n);
 void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,
                       int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_dev,
                       uint32_t* err, cudaStream_t s);
-// growable backward rows from an offset-form backward CSR (pg_build.cu): caps n, begs n + 1 (begs[n]
-// = entries laid out), blocksum scan_blocks_needed(n) + 2 entries of scratch; brow/bcol: the
-// replica's rows and region
-void launch_brow_layout(const int64_t* bo, const int32_t* bc, int64_t n, int64_t m, int64_t* caps,
-                        int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcap, int32_t* bcol, cudaStream_t s);
+// growable backward rows from an offset-form backward CSR (pg_build.cu), with the forward row copies
+// in front of them (fo/fc: the replica's forward CSR): caps n, begs n + 1 (begs[n] = entries laid
+// out), blocksum scan_blocks_needed(n) + 2 entries of scratch; brow/bcol: the replica's rows and
+// region
+void launch_brow_layout(const int64_t* bo, const int32_t* bc, const int64_t* fo, const int32_t* fc, int64_t n,
+                        int64_t m, int64_t* caps, int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcap,
+                        int32_t* bcol, cudaStream_t s);
 // the seeds of all replicas as one build over the arena's node slots (pg_build.cu): raw edges
 // src/dst (replica r's at [raw_off[r], raw_off[r+1]), rewritten in place to slot ids), the device
 // Replica array and tile map already uploaded; u/laid receive each replica's unique edges and

@@ -511,7 +511,9 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
         const unsigned bm = __ballot_sync(kFull, !glob);
         bool mem = false, scan = false;
         long long ex = 0;
-        int64_t d = 0, f0 = 0, lf = 0, b0 = 0;
+        int64_t d = 0, W = 0;
+        int lead = 0;                // entries of the window before the row's first
+        const int32_t* wsrc = B.fc;  // the window's first entry
         if (lane == __ffs(grp) - 1 && !pre && (grp & bm)) {
             // the node's hub slot and row bounds are loaded before the frontier probe, so the
             // global loads overlap the shared-memory hash lookups
@@ -524,22 +526,30 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             } else if (hs >= 0) {
                 mem = (B.X->hm[hs >> 6] >> (hs & 63)) & 1ull;
             } else {
-                f0 = jf0;
-                lf = jf1 - jf0;
-                b0 = jb0;
-                d = lf + (jb1 - jb0);
+                const int64_t lf = jf1 - jf0, lb = jb1 - jb0;
+                d = lf + lb;
                 scan = d > 0;
                 ex = d;  // a miss examines both rows
+                if (lb > 0) {
+                    // a cited node: its forward row copy ends where its backward entries begin
+                    // (16-byte aligned), so both rows are one window of the backward region
+                    const int64_t P = fwd_prefix(lf);
+                    wsrc = B.bc + (jb0 - P);
+                    lead = (int)(P - lf);
+                    W = P + ((lb + 3) & ~3ll);
+                } else if (lf > 0) {
+                    // never cited: the forward row in the forward CSR (edge regions are multiples of
+                    // 4 entries, so the aligned window stays inside the replica's)
+                    const int64_t fa0 = jf0 & ~3ll;
+                    wsrc = B.fc + fa0;
+                    lead = (int)(jf0 - fa0);
+                    W = ((jf0 + lf + 3) & ~3ll) - fa0;
+                }
             }
         }
         // The rows of every node under test are staged into shared memory by bulk asynchronous
-        // copies of 16-byte-aligned windows around them (forward window, then backward window,
-        // lane after lane), kStage entries per chunk; each row keeps its first hit, and a row with
-        // a hit copies nothing more.
-        const int64_t lb = d - lf;
-        const int64_t fa0 = f0 & ~3ll, fw = lf > 0 ? (((f0 + lf + 3) & ~3ll) - fa0) : 0;
-        const int64_t ba0 = b0 & ~3ll, bw = lb > 0 ? (((b0 + lb + 3) & ~3ll) - ba0) : 0;
-        const int64_t W = scan ? fw + bw : 0;
+        // copies of their 16-byte-aligned windows (lane after lane), kStage entries per chunk; each
+        // row keeps its first hit, and a row with a hit copies nothing more.
         const int64_t wincl = warp_incl_scan(W);
         const int64_t wx = wincl - W;
         const int64_t DW = __shfl_sync(kFull, wincl, 31);
@@ -561,19 +571,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             __syncwarp();
             if (lane == 0) mbar_expect_tx(&S.bar[buf], total);
             __syncwarp();
-            if (s1 > s0) {
-                const int64_t fe = wx + fw;
-                if (s0 < fe) {
-                    const int64_t e1 = s1 < fe ? s1 : fe;
-                    bulk_g2s(&S.stage[buf][s0 - c0], B.fc + fa0 + (s0 - wx), (uint32_t)(e1 - s0) * 4u,
-                             &S.bar[buf]);
-                }
-                if (s1 > fe) {
-                    const int64_t e0 = s0 > fe ? s0 : fe;
-                    bulk_g2s(&S.stage[buf][e0 - c0], B.bc + ba0 + (e0 - fe), (uint32_t)(s1 - e0) * 4u,
-                             &S.bar[buf]);
-                }
-            }
+            if (s1 > s0) bulk_g2s(&S.stage[buf][s0 - c0], wsrc + (s0 - wx), (uint32_t)(s1 - s0) * 4u, &S.bar[buf]);
             return true;
         };
         // chunks are double-buffered: chunk c+1 is in flight while chunk c is tested
@@ -603,8 +601,7 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
             // row has no hit yet and the entry is the row's own (not window padding).  Entries of
             // a row whose hit came in an earlier chunk (copied before the hit was known) or of a
             // row not copied at all (stale) are tested too and their hits dropped.  Chunk
-            // position q maps to row position q + fx0 in the forward window (q < qf), q + bx0 in
-            // the backward one.
+            // position q maps to row position q + x0 (forward row first, then backward).
             const int nq = (int)(DW - c0 < kStage ? DW - c0 : kStage);
             for (int i0 = 0; i0 < nq; i0 += 32 * kTestU) {
                 bool hit[kTestU];
@@ -649,13 +646,11 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                 for (int u = 0; u < kTestU; ++u) anyhit |= hit[u];
                 if (!__any_sync(kFull, anyhit)) continue;
                 // a step with hits: this lane's window in chunk coordinates (computed only here)
-                const int64_t wlo64 = wx - c0, whi64 = wx + W - c0, qf64 = wx + fw - c0;
+                const int64_t wlo64 = wx - c0, whi64 = wx + W - c0;
                 const int wlo = (int)(wlo64 < -1 ? -1 : (wlo64 > kStage ? kStage : wlo64));
                 const int whi = (int)(whi64 < -1 ? -1 : (whi64 > kStage ? kStage : whi64));
-                const int qf = (int)(qf64 < -1 ? -1 : (qf64 > kStage ? kStage : qf64));
-                const int fx0 = (int)((c0 - wx) + (fa0 - f0));
-                const int bx0 = (int)(lf + (c0 - wx - fw) + (ba0 - b0));
-                const int lf32 = (int)lf, d32 = (int)d;
+                const int x0 = (int)((c0 - wx) - lead);
+                const int d32 = (int)d;
 #pragma unroll
                 for (int u = 0; u < kTestU; ++u) {
                     unsigned hm = __ballot_sync(kFull, hit[u]);
@@ -663,9 +658,8 @@ __device__ bool process_agent_thin(const Arena& A, int64_t a, int k, ThinSmem<KC
                         const int qh = i0 + 32 * u + __ffs(hm) - 1;
                         hm &= hm - 1u;
                         if (qh >= wlo && qh < whi && mp == d) {
-                            const bool fwd = qh < qf;
-                            const int x = qh + (fwd ? fx0 : bx0);
-                            if (fwd ? (x >= 0 && x < lf32) : (x >= lf32 && x < d32)) mp = x;
+                            const int x = qh + x0;
+                            if (x >= 0 && x < d32) mp = x;
                         }
                     }
                 }
