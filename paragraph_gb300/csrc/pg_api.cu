@@ -562,14 +562,21 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
                 if (e == cudaSuccess)
                     e = cudaMemcpyAsync(raw_dst.p + o, d.dst, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream);
             }
-            if (e == cudaSuccess)
-                launch_first_bad_edge(raw_src.p + o, raw_dst.p + o, d.num_edges, d.num_nodes, first.p + r, c->stream);
         }
+        // every list's endpoints in one launch: the lists' offsets and node counts go up together
+        DBuf<int64_t> chk;
+        std::vector<int64_t> chk_h(raw_off);
+        for (int r = 0; r < R; ++r) chk_h.push_back(raw[r].num_nodes);
+        if (e == cudaSuccess) e = talloc(chk, (int64_t)chk_h.size(), c->device, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(chk.p, chk_h.data(), 8 * chk_h.size(), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) launch_first_bad_edge_all(raw_src.p, raw_dst.p, tot, chk.p, chk.p + R + 1, R, first.p, c->stream);
         std::vector<unsigned long long> bad((size_t)R, ~0ull);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(bad.data(), first.p, sizeof(unsigned long long) * (size_t)R, cudaMemcpyDeviceToHost, c->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         tfree(first, c->device, c->stream);
+        tfree(chk, c->device, c->stream);
         if (e != cudaSuccess) {
             drop();
             return fail(c, PG_ERR_CUDA, std::string("edge upload: ") + cudaGetErrorString(e));

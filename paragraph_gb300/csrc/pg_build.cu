@@ -58,41 +58,88 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long
 }
 
 // Stable scatter: key k of tile t with digit d goes to off[d * tiles + t] + (number of earlier keys
-// of the tile with digit d).  The tile is walked in chunks of 256 keys in order; inside a chunk a key
-// is ranked among its warp's equal digits (match), warps are ordered by a per-chunk table.
+// of the tile with digit d).  Each warp owns a contiguous segment of the tile (kSortPerLane keys per
+// lane, walked 32 at a time in order).  First pass: the warp counts its segment's digits (match:
+// the leader of each group of equal digits adds the group's size).  After one barrier the counts
+// become each (warp, digit) run's start in the tile's digit order (the exclusive scan of the tile's
+// digit counts, then the earlier warps').  Second pass: the warp walks its segment again (the keys
+// come from L1/L2) and places each key at its run's running position plus its place in the group,
+// in shared memory.  The runs are then written out in tile order, consecutive threads writing
+// consecutive keys of a run (coalesced).
+constexpr int kSortPerLane = kSortTile / kSortThreads;  // 16
+static_assert(kSortThreads == kRadix, "one thread per digit in the run-start scan");
 __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned long long* keys, int64_t m,
                                                                 int shift, int dmask, int64_t tiles,
                                                                 const int64_t* off, unsigned long long* out) {
     constexpr int W = kSortThreads / 32;
-    __shared__ int64_t run[kRadix];        // keys of each digit placed by earlier chunks
-    __shared__ int wcnt[W][kRadix];        // this chunk: keys of each digit per warp
+    __shared__ unsigned long long tile[kSortTile];  // the tile's keys in digit order
+    __shared__ int64_t gbase[kRadix];               // global position of the digit's run minus its start
+    __shared__ int wcnt[W][kRadix];                 // per warp: digit counts, then running positions
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = blockIdx.x;
-    for (int d = threadIdx.x; d < kRadix; d += kSortThreads) run[d] = off[(int64_t)d * tiles + t];
     const int64_t base = t * kSortTile;
-    for (int c = 0; c < kSortTile; c += kSortThreads) {
-        for (int i = threadIdx.x; i < W * kRadix; i += kSortThreads) (&wcnt[0][0])[i] = 0;
-        __syncthreads();
-        const int64_t k = base + c + threadIdx.x;
-        const bool valid = k < m;
-        const unsigned long long key = valid ? keys[k] : 0ull;
-        const int d = valid ? (int)((key >> shift) & dmask) : kRadix;  // kRadix: no digit
+    const int cnt = (int)(m - base < kSortTile ? m - base : kSortTile);
+    const int seg = warp * 32 * kSortPerLane;
+    const unsigned below = (1u << lane) - 1u;
+    for (int i = threadIdx.x; i < W * kRadix; i += kSortThreads) (&wcnt[0][0])[i] = 0;
+    __syncthreads();
+    for (int j = 0; j < kSortPerLane; ++j) {
+        const int q = seg + 32 * j + lane;
+        const int d = q < cnt ? (int)((keys[base + q] >> shift) & dmask) : kRadix;  // kRadix: no digit
         const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const int rank = __popc(peers & ((1u << lane) - 1u));
-        if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            int before = 0;
-            for (int w = 0; w < warp; ++w) before += wcnt[w][d];
-            out[run[d] + before + rank] = key;
+        if (d < kRadix && lane == __ffs(peers) - 1) wcnt[warp][d] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // run starts: digit d's run of warp w begins at (keys of digits < d) + (keys of digit d in warps
+    // < w); one thread per digit, the digits' totals scanned by the first warp's shuffles
+    {
+        const int d = threadIdx.x;  // kSortThreads == kRadix
+        int tot = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w) tot += wcnt[w][d];
+        // exclusive scan of tot over the 256 digits: per-warp shuffle scan, then the warps' sums
+        int incl = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
         }
+        __shared__ int wsum[W];
+        if (lane == 31) wsum[warp] = incl;
         __syncthreads();
-        for (int dd = threadIdx.x; dd < kRadix; dd += kSortThreads) {
-            int s = 0;
-            for (int w = 0; w < W; ++w) s += wcnt[w][dd];
-            run[dd] += s;
+        int prior = 0;
+        for (int w = 0; w < warp; ++w) prior += wsum[w];
+        int acc = prior + incl - tot;  // this digit's start in the tile's digit order
+        gbase[d] = off[(int64_t)d * tiles + t] - acc;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const int c = wcnt[w][d];
+            wcnt[w][d] = acc;
+            acc += c;
         }
-        __syncthreads();
+    }
+    __syncthreads();
+    for (int j = 0; j < kSortPerLane; ++j) {
+        const int q = seg + 32 * j + lane;
+        const bool valid = q < cnt;
+        const unsigned long long key = valid ? keys[base + q] : 0ull;
+        const int d = valid ? (int)((key >> shift) & dmask) : kRadix;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int leader = __ffs(peers) - 1;
+        int pos = 0;
+        if (valid && lane == leader) {
+            pos = wcnt[warp][d];
+            wcnt[warp][d] = pos + __popc(peers);
+        }
+        pos = __shfl_sync(0xffffffffu, pos, leader);
+        if (valid) tile[pos + __popc(peers & below)] = key;
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += kSortThreads) {
+        const unsigned long long key = tile[i];
+        out[gbase[(int)((key >> shift) & dmask)] + i] = key;
     }
 }
 
@@ -103,14 +150,17 @@ __global__ void __launch_bounds__(256) k_unique_flags(const unsigned long long* 
 }
 
 // The unique keys (sorted by source, then target) as forward columns, and the edges of every source.
+// fsrc (may be null): the source of every unique edge, for the callers that lay rows out per entry.
 __global__ void __launch_bounds__(256) k_unique_compact(const unsigned long long* keys, int64_t m, const int32_t* flag,
-                                                        const int64_t* pos, int bits, int32_t* fcol, int32_t* fcnt) {
+                                                        const int64_t* pos, int bits, int32_t* fcol, int32_t* fcnt,
+                                                        int32_t* fsrc) {
     const unsigned long long mask = (1ull << bits) - 1ull;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         if (!flag[i]) continue;
         const unsigned long long k = keys[i];
         const int64_t p = pos[i];
         fcol[p] = (int32_t)(k & mask);
+        if (fsrc) fsrc[p] = (int32_t)(k >> bits);
         atomicAdd(&fcnt[(int64_t)(k >> bits)], 1);
     }
 }
@@ -127,14 +177,15 @@ __global__ void __launch_bounds__(256) k_backward_keys(const unsigned long long*
 }
 
 // Keys sorted by (target, source), the u_dev unique ones first: backward columns (sources) and
-// per-target counts.
+// per-target counts; btgt (may be null): the target of every backward entry.
 __global__ void __launch_bounds__(256) k_backward_cols(const unsigned long long* keys, const int64_t* u_dev, int bits,
-                                                       int32_t* bcol, int32_t* bcnt) {
+                                                       int32_t* bcol, int32_t* bcnt, int32_t* btgt) {
     const unsigned long long mask = (1ull << (bits + 1)) - 1ull;
     const int64_t u = *u_dev;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < u; i += (int64_t)gridDim.x * blockDim.x) {
         const unsigned long long k = keys[i];
         bcol[i] = (int32_t)(k >> (bits + 1));
+        if (btgt) btgt[i] = (int32_t)(k & mask);
         atomicAdd(&bcnt[(int64_t)(k & mask)], 1);
     }
 }
@@ -152,6 +203,33 @@ void launch_first_bad_edge(const int32_t* src, const int32_t* dst, int64_t m, in
     if (m <= 0) return;
     const unsigned grid = (unsigned)std::min<int64_t>((m + 255) / 256, 152 * 16);
     k_first_bad_edge<<<grid, 256, 0, s>>>(src, dst, m, n, first);
+}
+
+// The same check for many edge lists at once: list r is [off[r], off[r + 1]) with ids below nodes[r];
+// first[r] receives the first bad index of list r, relative to off[r] (~0 when none).
+__global__ void __launch_bounds__(256) k_first_bad_edge_all(const int32_t* src, const int32_t* dst, const int64_t* off,
+                                                            const int64_t* nodes, int R, unsigned long long* first) {
+    const int64_t m = off[R];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = R - 1;  // the last list starting at or before i
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= i)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const uint32_t n = (uint32_t)nodes[lo];
+        if ((uint32_t)src[i] >= n || (uint32_t)dst[i] >= n) atomicMin(&first[lo], (unsigned long long)(i - off[lo]));
+    }
+}
+
+void launch_first_bad_edge_all(const int32_t* src, const int32_t* dst, int64_t m, const int64_t* off,
+                               const int64_t* nodes, int R, unsigned long long* first, cudaStream_t s) {
+    cudaMemsetAsync(first, 0xFF, sizeof(unsigned long long) * (size_t)R, s);
+    if (m <= 0) return;
+    const unsigned grid = (unsigned)std::min<int64_t>((m + 255) / 256, 152 * 16);
+    k_first_bad_edge_all<<<grid, 256, 0, s>>>(src, dst, off, nodes, R, first);
 }
 
 int64_t build_radix_tiles(int64_t m) { return (m + kSortTile - 1) / kSortTile; }
@@ -198,7 +276,7 @@ size_t build_scratch_bytes(int64_t m, int64_t n) {
 // holds it too).  Scratch layout is carved from `scratch`.
 void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,
                       int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_dev,
-                      uint32_t* err, cudaStream_t s) {
+                      uint32_t* err, cudaStream_t s, int32_t* fsrc, int32_t* btgt) {
     const int64_t e = m > 0 ? m : 1;
     const int64_t scan = build_scan_entries(e) + 1;
     char* p = reinterpret_cast<char*>(scratch);
@@ -228,12 +306,12 @@ void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t
         unsigned long long* sorted = radix_sort(k0, k1, m, 0, 2 * bits, hist, off, blocksum, s);
         k_unique_flags<<<grid, 256, 0, s>>>(sorted, m, flag);
         launch_scan_i32_to_i64(flag, pos, m, blocksum, s);
-        k_unique_compact<<<grid, 256, 0, s>>>(sorted, m, flag, pos, bits, fc, fcnt);
+        k_unique_compact<<<grid, 256, 0, s>>>(sorted, m, flag, pos, bits, fc, fcnt, fsrc);
         cudaMemcpyAsync(u_dev, pos + m, sizeof(int64_t), cudaMemcpyDeviceToDevice, s);  // unique edges
         k_backward_keys<<<grid, 256, 0, s>>>(sorted, m, flag, bits, uk);
         unsigned long long* other = sorted == k0 ? k1 : k0;
         unsigned long long* bsorted = radix_sort(uk, other, m, 0, bits + 1, hist, off, blocksum, s);
-        k_backward_cols<<<grid, 256, 0, s>>>(bsorted, u_dev, bits, bc, bcnt);
+        k_backward_cols<<<grid, 256, 0, s>>>(bsorted, u_dev, bits, bc, bcnt, btgt);
     } else {
         cudaMemsetAsync(u_dev, 0, sizeof(int64_t), s);
     }
@@ -382,39 +460,31 @@ __global__ void __launch_bounds__(256) k_brow_rows_all(const int64_t* bo, const 
     }
 }
 
-// forward row copies of every slot with a span (slot-wide columns hold slot ids: made local)
-__global__ void __launch_bounds__(256) k_brow_prefix_all(const int64_t* go, const int32_t* gc, const BRow* brow,
-                                                         int64_t S, const int32_t* tile_rep, const Replica* rep,
-                                                         int32_t* bcol) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t s = warp; s < S; s += nwarps) {
-        const BRow r = brow[s];
+// forward row copies of every slot with a span, one thread per unique forward edge p (slot-wide
+// order; fsrc[p] its source slot, gc[p] its target slot, made local)
+__global__ void __launch_bounds__(256) k_brow_prefix_all(const int64_t* go, const int32_t* gc, const int32_t* fsrc,
+                                                         const BRow* brow, int64_t S, int64_t m,
+                                                         const int32_t* tile_rep, const Replica* rep, int32_t* bcol) {
+    const int64_t u = go[S] < m ? go[S] : m;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < u; p += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t sl = fsrc[p];
+        const BRow r = brow[sl];
         if (r.len <= 0) continue;
-        const Replica& rp = rep[tile_rep[s / kTile]];
-        const int64_t f0 = go[s], o = go[s + 1] - f0;
-        int32_t* dst = bcol + rp.bbase + ((int64_t)r.beg4 << 2) - o;
-        for (int64_t i = lane; i < o; i += 32) dst[i] = gc[f0 + i] - (int32_t)rp.nbase;
+        const Replica& rp = rep[tile_rep[sl / kTile]];
+        const int64_t f0 = go[sl], o = go[sl + 1] - f0;
+        bcol[rp.bbase + ((int64_t)r.beg4 << 2) - o + (p - f0)] = gc[p] - (int32_t)rp.nbase;
     }
 }
 
-// backward entry i (slot-wide order): the row is the last slot with bo[s] <= i
-__global__ void __launch_bounds__(256) k_brow_cols_all(const int64_t* bo, const int32_t* bc, const BRow* brow,
-                                                       int64_t S, int64_t m, const int32_t* tile_rep,
+// backward entry i (slot-wide order) of the row of slot btgt[i]
+__global__ void __launch_bounds__(256) k_brow_cols_all(const int64_t* bo, const int32_t* bc, const int32_t* btgt,
+                                                       const BRow* brow, int64_t S, int64_t m, const int32_t* tile_rep,
                                                        const Replica* rep, int32_t* bcol) {
     const int64_t u = bo[S] < m ? bo[S] : m;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < u; i += (int64_t)gridDim.x * blockDim.x) {
-        int64_t lo = 0, hi = S - 1;
-        while (lo < hi) {
-            const int64_t mid = (lo + hi + 1) >> 1;
-            if (bo[mid] <= i)
-                lo = mid;
-            else
-                hi = mid - 1;
-        }
-        const Replica& rp = rep[tile_rep[lo / kTile]];
-        bcol[rp.bbase + ((int64_t)brow[lo].beg4 << 2) + (i - bo[lo])] = bc[i] - (int32_t)rp.nbase;
+        const int64_t sl = btgt[i];
+        const Replica& rp = rep[tile_rep[sl / kTile]];
+        bcol[rp.bbase + ((int64_t)brow[sl].beg4 << 2) + (i - bo[sl])] = bc[i] - (int32_t)rp.nbase;
     }
 }
 
@@ -430,8 +500,8 @@ __global__ void k_rep_totals(const int64_t* go, const int64_t* gbeg, int R, cons
 
 size_t build_all_scratch_bytes(int64_t m, int64_t S) {
     // the pieces launch_build_all carves, each rounded up to 256 bytes
-    return build_scratch_bytes(m, S) + (size_t)(S + 1) * 8 * 4 + (size_t)(m > 0 ? m : 1) * 4 * 2 + 8 +
-           (size_t)(scan_blocks_needed(S + 1) + 2) * 8 + 256 * 10;
+    return build_scratch_bytes(m, S) + (size_t)(S + 1) * 8 * 4 + (size_t)(m > 0 ? m : 1) * 4 * 4 + 8 +
+           (size_t)(scan_blocks_needed(S + 1) + 2) * 8 + 256 * 12;
 }
 
 void launch_build_all(int32_t* src, int32_t* dst, int64_t m, const int64_t* raw_off, int R, int64_t S,
@@ -451,22 +521,23 @@ void launch_build_all(int32_t* src, int32_t* dst, int64_t m, const int64_t* raw_
     int64_t* gbeg = reinterpret_cast<int64_t*>(take((size_t)(S + 1) * 8));
     int32_t* gc = reinterpret_cast<int32_t*>(take((size_t)e * 4));
     int32_t* bc = reinterpret_cast<int32_t*>(take((size_t)e * 4));
+    int32_t* fsrc = reinterpret_cast<int32_t*>(take((size_t)e * 4));
+    int32_t* btgt = reinterpret_cast<int32_t*>(take((size_t)e * 4));
     int64_t* ucount = reinterpret_cast<int64_t*>(take(8));
     void* inner = take(build_scratch_bytes(m, S));
     int64_t* blocksum = reinterpret_cast<int64_t*>(take((size_t)(scan_blocks_needed(S + 1) + 2) * 8));
     const unsigned gm = (unsigned)std::min<int64_t>((e + 255) / 256, 152 * 16);
     const unsigned gs = (unsigned)std::min<int64_t>((S + 255) / 256, 152 * 16);
     if (m > 0) k_raw_to_slots<<<gm, 256, 0, s>>>(src, dst, m, raw_off, R, rep);
-    launch_build_csr(src, dst, m, S, inner, go, gc, bo, bc, indeg, ucount, err, s);
+    launch_build_csr(src, dst, m, S, inner, go, gc, bo, bc, indeg, ucount, err, s, fsrc, btgt);
     k_fwd_offsets<<<gs, 256, 0, s>>>(go, S, tile_rep, rep, fwd_off);
     if (m > 0) k_fwd_columns<<<gm, 256, 0, s>>>(go, gc, S, m, tile_rep, rep, fwd_col);
     k_brow_caps<<<gs, 256, 0, s>>>(bo, go, S, caps);
     launch_scan_i64(caps, gbeg, S, blocksum, s);
     k_brow_rows_all<<<gs, 256, 0, s>>>(bo, go, gbeg, S, tile_rep, rep, brow, bcap);
     if (m > 0) {
-        k_brow_cols_all<<<gm, 256, 0, s>>>(bo, bc, brow, S, m, tile_rep, rep, bcol);
-        const unsigned gw = (unsigned)std::min<int64_t>((S + 7) / 8, 152 * 16);
-        k_brow_prefix_all<<<gw, 256, 0, s>>>(go, gc, brow, S, tile_rep, rep, bcol);
+        k_brow_cols_all<<<gm, 256, 0, s>>>(bo, bc, btgt, brow, S, m, tile_rep, rep, bcol);
+        k_brow_prefix_all<<<gm, 256, 0, s>>>(go, gc, fsrc, brow, S, m, tile_rep, rep, bcol);
     }
     k_rep_totals<<<1, 256, 0, s>>>(go, gbeg, R, rep, u, laid);
 }

@@ -493,10 +493,16 @@ void launch_edge_sources(const int64_t* fo, int64_t n, int64_t first, int64_t co
 // device CSR construction from a raw edge list (pg_build.cu)
 void launch_first_bad_edge(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, unsigned long long* first,
                            cudaStream_t s);
+// the check over R edge lists at once (list r at [off[r], off[r + 1]) of src/dst, m = off[R], ids
+// below nodes[r]; off and nodes in device memory); first[r] relative to off[r]
+void launch_first_bad_edge_all(const int32_t* src, const int32_t* dst, int64_t m, const int64_t* off,
+                               const int64_t* nodes, int R, unsigned long long* first, cudaStream_t s);
 size_t build_scratch_bytes(int64_t m, int64_t n);
+// fsrc / btgt (may be null): the source of every unique forward edge, the target of every backward
+// entry (m entries each)
 void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, void* scratch,
                       int64_t* fo, int32_t* fc, int64_t* bo, int32_t* bc, int32_t* indeg, int64_t* u_dev,
-                      uint32_t* err, cudaStream_t s);
+                      uint32_t* err, cudaStream_t s, int32_t* fsrc = nullptr, int32_t* btgt = nullptr);
 // growable backward rows from an offset-form backward CSR (pg_build.cu), with the forward row copies
 // in front of them (fo/fc: the replica's forward CSR): caps n, begs n + 1 (begs[n] = entries laid
 // out), blocksum scan_blocks_needed(n) + 2 entries of scratch; brow/bcol: the replica's rows and
