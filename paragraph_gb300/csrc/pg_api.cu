@@ -554,23 +554,41 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         cudaError_t e = talloc(raw_src, std::max<int64_t>(tot, 1), c->device, c->stream);
         if (e == cudaSuccess) e = talloc(raw_dst, std::max<int64_t>(tot, 1), c->device, c->stream);
         if (e == cudaSuccess) e = talloc(first, R, c->device, c->stream);
+        // edge lists in page-locked host memory (mapped into the device's address space) are read by
+        // the gather kernel directly; any other list is copied into the staging arrays first
+        auto mapped = [](const void* p) -> const void* {
+            cudaPointerAttributes a{};
+            if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+                cudaGetLastError();
+                return nullptr;
+            }
+            return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+        };
+        // the gather's table: list offsets (R + 1), node counts (R), source / target arrays (2 R)
+        std::vector<int64_t> chk_h(raw_off);
+        for (int r = 0; r < R; ++r) chk_h.push_back(raw[r].num_nodes);
         for (int r = 0; r < R && e == cudaSuccess; ++r) {
             const pg_replica_desc& d = raw[r];
             const size_t o = (size_t)raw_off[(size_t)r];
-            if (d.num_edges > 0) {
+            const void* ms = d.num_edges > 0 ? mapped(d.src) : nullptr;
+            const void* md = d.num_edges > 0 ? mapped(d.dst) : nullptr;
+            if (d.num_edges > 0 && !(ms && md)) {
                 e = cudaMemcpyAsync(raw_src.p + o, d.src, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream);
                 if (e == cudaSuccess)
                     e = cudaMemcpyAsync(raw_dst.p + o, d.dst, 4 * (size_t)d.num_edges, cudaMemcpyHostToDevice, c->stream);
+                ms = raw_src.p + o;
+                md = raw_dst.p + o;
             }
+            chk_h.push_back((int64_t)(uintptr_t)ms);
+            chk_h.push_back((int64_t)(uintptr_t)md);
         }
-        // every list's endpoints in one launch: the lists' offsets and node counts go up together
         DBuf<int64_t> chk;
-        std::vector<int64_t> chk_h(raw_off);
-        for (int r = 0; r < R; ++r) chk_h.push_back(raw[r].num_nodes);
         if (e == cudaSuccess) e = talloc(chk, (int64_t)chk_h.size(), c->device, c->stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(chk.p, chk_h.data(), 8 * chk_h.size(), cudaMemcpyHostToDevice, c->stream);
-        if (e == cudaSuccess) launch_first_bad_edge_all(raw_src.p, raw_dst.p, tot, chk.p, chk.p + R + 1, R, first.p, c->stream);
+        if (e == cudaSuccess)
+            launch_gather_edges(tot, chk.p, chk.p + R + 1, chk.p + 2 * R + 1, R, raw_src.p, raw_dst.p, first.p,
+                                c->stream);
         std::vector<unsigned long long> bad((size_t)R, ~0ull);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(bad.data(), first.p, sizeof(unsigned long long) * (size_t)R, cudaMemcpyDeviceToHost, c->stream);

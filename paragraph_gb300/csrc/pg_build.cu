@@ -205,10 +205,14 @@ void launch_first_bad_edge(const int32_t* src, const int32_t* dst, int64_t m, in
     k_first_bad_edge<<<grid, 256, 0, s>>>(src, dst, m, n, first);
 }
 
-// The same check for many edge lists at once: list r is [off[r], off[r + 1]) with ids below nodes[r];
-// first[r] receives the first bad index of list r, relative to off[r] (~0 when none).
-__global__ void __launch_bounds__(256) k_first_bad_edge_all(const int32_t* src, const int32_t* dst, const int64_t* off,
-                                                            const int64_t* nodes, int R, unsigned long long* first) {
+// Many edge lists at once: list r is [off[r], off[r + 1]) of the staging arrays src/dst, with ids
+// below nodes[r]; its source and target arrays are at ptr[2 r] and ptr[2 r + 1] -- page-locked host
+// memory mapped into the device's address space (read here directly, over the host link) or the
+// staging arrays themselves (already copied there).  Every edge is written to the staging arrays
+// and its endpoints are checked; first[r] receives the first bad index of list r, relative to
+// off[r] (~0 when none).
+__global__ void __launch_bounds__(256) k_gather_edges(const int64_t* off, const int64_t* nodes, const int64_t* ptr,
+                                                      int R, int32_t* src, int32_t* dst, unsigned long long* first) {
     const int64_t m = off[R];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         int lo = 0, hi = R - 1;  // the last list starting at or before i
@@ -219,17 +223,22 @@ __global__ void __launch_bounds__(256) k_first_bad_edge_all(const int32_t* src, 
             else
                 hi = mid - 1;
         }
+        const int64_t j = i - off[lo];
+        const int32_t s = reinterpret_cast<const int32_t*>(ptr[2 * lo])[j];
+        const int32_t d = reinterpret_cast<const int32_t*>(ptr[2 * lo + 1])[j];
+        src[i] = s;
+        dst[i] = d;
         const uint32_t n = (uint32_t)nodes[lo];
-        if ((uint32_t)src[i] >= n || (uint32_t)dst[i] >= n) atomicMin(&first[lo], (unsigned long long)(i - off[lo]));
+        if ((uint32_t)s >= n || (uint32_t)d >= n) atomicMin(&first[lo], (unsigned long long)j);
     }
 }
 
-void launch_first_bad_edge_all(const int32_t* src, const int32_t* dst, int64_t m, const int64_t* off,
-                               const int64_t* nodes, int R, unsigned long long* first, cudaStream_t s) {
+void launch_gather_edges(int64_t m, const int64_t* off, const int64_t* nodes, const int64_t* ptr, int R, int32_t* src,
+                         int32_t* dst, unsigned long long* first, cudaStream_t s) {
     cudaMemsetAsync(first, 0xFF, sizeof(unsigned long long) * (size_t)R, s);
     if (m <= 0) return;
     const unsigned grid = (unsigned)std::min<int64_t>((m + 255) / 256, 152 * 16);
-    k_first_bad_edge_all<<<grid, 256, 0, s>>>(src, dst, off, nodes, R, first);
+    k_gather_edges<<<grid, 256, 0, s>>>(off, nodes, ptr, R, src, dst, first);
 }
 
 int64_t build_radix_tiles(int64_t m) { return (m + kSortTile - 1) / kSortTile; }

@@ -493,10 +493,12 @@ void launch_edge_sources(const int64_t* fo, int64_t n, int64_t first, int64_t co
 // device CSR construction from a raw edge list (pg_build.cu)
 void launch_first_bad_edge(const int32_t* src, const int32_t* dst, int64_t m, int64_t n, unsigned long long* first,
                            cudaStream_t s);
-// the check over R edge lists at once (list r at [off[r], off[r + 1]) of src/dst, m = off[R], ids
-// below nodes[r]; off and nodes in device memory); first[r] relative to off[r]
-void launch_first_bad_edge_all(const int32_t* src, const int32_t* dst, int64_t m, const int64_t* off,
-                               const int64_t* nodes, int R, unsigned long long* first, cudaStream_t s);
+// R edge lists gathered into the staging arrays src/dst and checked in one launch (list r at
+// [off[r], off[r + 1]), m = off[R], ids below nodes[r], read from ptr[2 r] / ptr[2 r + 1]: mapped
+// page-locked host memory or the staging arrays; off, nodes and ptr in device memory); first[r]
+// relative to off[r]
+void launch_gather_edges(int64_t m, const int64_t* off, const int64_t* nodes, const int64_t* ptr, int R, int32_t* src,
+                         int32_t* dst, unsigned long long* first, cudaStream_t s);
 size_t build_scratch_bytes(int64_t m, int64_t n);
 // fsrc / btgt (may be null): the source of every unique forward edge, the target of every backward
 // entry (m entries each)
