@@ -405,6 +405,38 @@ def test_bad_edge_in_one_replica_leaves_the_loaded_replicas(gpu):
         eng.run_epochs(1)  # still usable
 
 
+def test_page_locked_edge_lists_load_like_pageable_ones(gpu):
+    """Edge lists in page-locked host memory are read by the device directly (the others are
+    copied first): a mix of both loads to the same CSRs as pageable lists, and a bad endpoint in a
+    page-locked list is reported with its index and replica."""
+    import dataclasses
+
+    torch = pytest.importorskip("torch")
+
+    def pinned(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+    reps = W.ensemble_inputs(replicas=4, lo=500, hi=3000, epochs=1, seed=8)
+    mixed = [dataclasses.replace(r, src=pinned(r.src), dst=pinned(r.dst)) if i % 2 == 0 else r
+             for i, r in enumerate(reps)]
+    with GrowthEngine(seed=2, replicas=4) as a, GrowthEngine(seed=2, replicas=4) as b:
+        a.load_replicas(reps)
+        b.load_replicas(mixed)
+        for r in range(4):
+            for w in (0, 1):
+                (o1, c1), (o2, c2) = a.csr(w, r), b.csr(w, r)
+                np.testing.assert_array_equal(o1, o2)
+                np.testing.assert_array_equal(c1, c2)
+        dst = mixed[2].dst.copy()  # a page-locked copy of replica 2's targets
+        dst = pinned(dst)
+        dst[7] = -1
+        bad = list(mixed)
+        bad[2] = dataclasses.replace(mixed[2], dst=dst)
+        with pytest.raises(PGError, match="out of range at index 7 of replica 2"):
+            b.load_replicas(bad)
+        b.run_epochs(1)  # the loaded replicas are still usable
+
+
 @pytest.mark.parametrize("pinned,replicas,epoch_kernel", [(True, 1, 0), (False, 3, 0), (True, 3, 1)])
 def test_run_epochs_out_streams_every_citation(gpu, pinned, replicas, epoch_kernel):
     """pg_run_epochs_out delivers every new citation, epoch by epoch and replica by replica, into
