@@ -386,43 +386,6 @@ pg_status check_params(pg_ctx* c, const pg_pa_params& p) {
     return PG_OK;
 }
 
-// Index of the first edge with an endpoint outside [0, n), or -1; chunks on all host threads.
-// Sorted, duplicate-free CSR from an edge list (Graph::AddEdge set semantics).
-void host_csr(int64_t n, int64_t m, const int32_t* src, const int32_t* dst,
-              std::vector<int64_t>& off, std::vector<int32_t>& col) {
-    off.assign((size_t)n + 1, 0);
-    for (int64_t e = 0; e < m; ++e) off[(size_t)src[e] + 1]++;
-    for (int64_t v = 0; v < n; ++v) off[(size_t)v + 1] += off[(size_t)v];
-    col.resize((size_t)std::max<int64_t>(m, 1));
-    std::vector<int64_t> cur(off.begin(), off.end() - 1);
-    for (int64_t e = 0; e < m; ++e) col[(size_t)cur[(size_t)src[e]]++] = dst[e];
-    int64_t wpos = 0;
-    for (int64_t v = 0; v < n; ++v) {
-        const int64_t b = off[(size_t)v], e = off[(size_t)v + 1];
-        std::sort(col.begin() + b, col.begin() + e);
-        off[(size_t)v] = wpos;
-        for (int64_t i = b; i < e; ++i)
-            if (i == b || col[(size_t)i] != col[(size_t)i - 1]) col[(size_t)wpos++] = col[(size_t)i];
-    }
-    off[(size_t)n] = wpos;
-    col.resize((size_t)std::max<int64_t>(wpos, 1));
-}
-
-// Backward CSR (in-edges) of a forward CSR; rows come out ascending because sources are visited
-// in order.
-void host_transpose(int64_t n, const std::vector<int64_t>& fo, const std::vector<int32_t>& fc,
-                    std::vector<int64_t>& bo, std::vector<int32_t>& bc) {
-    const int64_t m = fo[(size_t)n];
-    bo.assign((size_t)n + 1, 0);
-    for (int64_t i = 0; i < m; ++i) bo[(size_t)fc[(size_t)i] + 1]++;
-    for (int64_t v = 0; v < n; ++v) bo[(size_t)v + 1] += bo[(size_t)v];
-    bc.resize((size_t)std::max<int64_t>(m, 1));
-    std::vector<int64_t> cur(bo.begin(), bo.end() - 1);
-    for (int64_t v = 0; v < n; ++v)
-        for (int64_t i = fo[(size_t)v]; i < fo[(size_t)v + 1]; ++i)
-            bc[(size_t)cur[(size_t)fc[(size_t)i]]++] = (int32_t)v;
-}
-
 void free_checkpoint(Checkpoint& k) {
     dfree(k.pub);
     dfree(k.indeg);
@@ -2618,10 +2581,6 @@ pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
             src[(size_t)(t->num_seed_edges + p)] = (int32_t)(n0 + a);
             dst[(size_t)(t->num_seed_edges + p)] = t->cites[p];
         }
-    std::vector<int64_t> fo, bo;
-    std::vector<int32_t> fc, bc;
-    host_csr(n, m, src.data(), dst.data(), fo, fc);
-    host_transpose(n, fo, fc, bo, bc);
     LikState& L = c->lik;
     free_lik(L);
     L.n = n;
@@ -2637,10 +2596,52 @@ pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
     pg_status s = PG_OK;
     if ((s = upload(c, L.epoch_nodes, t->epoch_nodes, (int64_t)E + 1)) != PG_OK) return s;
     if ((s = upload(c, L.epoch_t, t->epoch_t, (int64_t)E)) != PG_OK) return s;
-    if ((s = upload(c, L.fo, fo.data(), n + 1)) != PG_OK) return s;
-    if ((s = upload(c, L.fc, fc.data(), (int64_t)fc.size())) != PG_OK) return s;
-    if ((s = upload(c, L.bo, bo.data(), n + 1)) != PG_OK) return s;
-    if ((s = upload(c, L.bc, bc.data(), (int64_t)bc.size())) != PG_OK) return s;
+    // the final graph's forward and backward CSR, built on the device from the edge list (rows
+    // ascending, duplicate edges collapsed: the same rows as the host construction)
+    {
+        PG_CUDA(c, dalloc(L.fo, n + 1));
+        PG_CUDA(c, dalloc(L.fc, std::max<int64_t>(m, 1)));
+        PG_CUDA(c, dalloc(L.bo, n + 1));
+        PG_CUDA(c, dalloc(L.bc, std::max<int64_t>(m, 1)));
+        DBuf<int32_t> t_src, t_dst, t_indeg;
+        DBuf<int64_t> t_u;
+        DBuf<uint32_t> t_err;
+        DBuf<char> t_scratch;
+        struct Temps {  // released on every path
+            pg_ctx* c;
+            DBuf<int32_t>*a, *b, *d;
+            DBuf<int64_t>* u;
+            DBuf<uint32_t>* e;
+            DBuf<char>* s;
+            ~Temps() {
+                tfree(*a, c->device, c->stream);
+                tfree(*b, c->device, c->stream);
+                tfree(*d, c->device, c->stream);
+                tfree(*u, c->device, c->stream);
+                tfree(*e, c->device, c->stream);
+                tfree(*s, c->device, c->stream);
+            }
+        } temps{c, &t_src, &t_dst, &t_indeg, &t_u, &t_err, &t_scratch};
+        PG_CUDA(c, talloc(t_src, std::max<int64_t>(m, 1), c->device, c->stream));
+        PG_CUDA(c, talloc(t_dst, std::max<int64_t>(m, 1), c->device, c->stream));
+        PG_CUDA(c, talloc(t_indeg, n, c->device, c->stream));
+        PG_CUDA(c, talloc(t_u, 1, c->device, c->stream));
+        PG_CUDA(c, talloc(t_err, 1, c->device, c->stream));
+        PG_CUDA(c, talloc(t_scratch, (int64_t)build_scratch_bytes(m, n), c->device, c->stream));
+        PG_CUDA(c, cudaMemsetAsync(t_err.p, 0, sizeof(uint32_t), c->stream));
+        if (m) {
+            PG_CUDA(c, cudaMemcpyAsync(t_src.p, src.data(), 4 * (size_t)m, cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(t_dst.p, dst.data(), 4 * (size_t)m, cudaMemcpyHostToDevice, c->stream));
+        }
+        cudaGetLastError();
+        launch_build_csr(t_src.p, t_dst.p, m, n, t_scratch.p, L.fo.p, L.fc.p, L.bo.p, L.bc.p, t_indeg.p, t_u.p,
+                         t_err.p, c->stream);
+        PG_CUDA(c, cudaGetLastError());
+        uint32_t berr = 0;
+        PG_CUDA(c, cudaMemcpyAsync(&berr, t_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+        PG_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (berr) return fail(c, PG_ERR_ARG, "trace edge endpoint out of range");
+    }
     if ((s = upload(c, L.fit, t->fitness, n)) != PG_OK) return s;
     if ((s = upload(c, L.pub, t->pub_epoch, n)) != PG_OK) return s;
     if ((s = upload(c, L.anchors, t->anchors, 4 * std::max<int64_t>(agents, 1) * (agents > 0))) != PG_OK) return s;
