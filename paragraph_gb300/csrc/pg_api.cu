@@ -2568,19 +2568,10 @@ pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
         }
     }
     PG_CUDA(c, cudaSetDevice(c->device));
-    // final graph = seed edges + every agent's citations
+    // final graph = seed edges + every agent's citations (assembled on the device below)
     const int64_t mc = t->cite_off[agents];
-    const int64_t m = t->num_seed_edges + mc;
-    std::vector<int32_t> src((size_t)std::max<int64_t>(m, 1)), dst((size_t)std::max<int64_t>(m, 1));
-    if (t->num_seed_edges) {
-        std::memcpy(src.data(), t->seed_src, 4 * (size_t)t->num_seed_edges);
-        std::memcpy(dst.data(), t->seed_dst, 4 * (size_t)t->num_seed_edges);
-    }
-    for (int64_t a = 0; a < agents; ++a)
-        for (int64_t p = t->cite_off[a]; p < t->cite_off[a + 1]; ++p) {
-            src[(size_t)(t->num_seed_edges + p)] = (int32_t)(n0 + a);
-            dst[(size_t)(t->num_seed_edges + p)] = t->cites[p];
-        }
+    const int64_t ns = t->num_seed_edges;
+    const int64_t m = ns + mc;
     LikState& L = c->lik;
     free_lik(L);
     L.n = n;
@@ -2596,8 +2587,10 @@ pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
     pg_status s = PG_OK;
     if ((s = upload(c, L.epoch_nodes, t->epoch_nodes, (int64_t)E + 1)) != PG_OK) return s;
     if ((s = upload(c, L.epoch_t, t->epoch_t, (int64_t)E)) != PG_OK) return s;
-    // the final graph's forward and backward CSR, built on the device from the edge list (rows
-    // ascending, duplicate edges collapsed: the same rows as the host construction)
+    if ((s = upload(c, L.coff, t->cite_off, agents + 1)) != PG_OK) return s;
+    if ((s = upload(c, L.cites, t->cites, mc)) != PG_OK) return s;
+    // the final graph's forward and backward CSR, built on the device from the edge list: the seed
+    // edges, then every agent's citations (rows ascending, duplicate edges collapsed)
     {
         PG_CUDA(c, dalloc(L.fo, n + 1));
         PG_CUDA(c, dalloc(L.fc, std::max<int64_t>(m, 1)));
@@ -2629,11 +2622,12 @@ pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
         PG_CUDA(c, talloc(t_err, 1, c->device, c->stream));
         PG_CUDA(c, talloc(t_scratch, (int64_t)build_scratch_bytes(m, n), c->device, c->stream));
         PG_CUDA(c, cudaMemsetAsync(t_err.p, 0, sizeof(uint32_t), c->stream));
-        if (m) {
-            PG_CUDA(c, cudaMemcpyAsync(t_src.p, src.data(), 4 * (size_t)m, cudaMemcpyHostToDevice, c->stream));
-            PG_CUDA(c, cudaMemcpyAsync(t_dst.p, dst.data(), 4 * (size_t)m, cudaMemcpyHostToDevice, c->stream));
+        if (ns) {
+            PG_CUDA(c, cudaMemcpyAsync(t_src.p, t->seed_src, 4 * (size_t)ns, cudaMemcpyHostToDevice, c->stream));
+            PG_CUDA(c, cudaMemcpyAsync(t_dst.p, t->seed_dst, 4 * (size_t)ns, cudaMemcpyHostToDevice, c->stream));
         }
         cudaGetLastError();
+        launch_trace_edges(L.coff.p, L.cites.p, agents, n0, ns, t_src.p, t_dst.p, c->num_sms, c->stream);
         launch_build_csr(t_src.p, t_dst.p, m, n, t_scratch.p, L.fo.p, L.fc.p, L.bo.p, L.bc.p, t_indeg.p, t_u.p,
                          t_err.p, c->stream);
         PG_CUDA(c, cudaGetLastError());
@@ -2645,8 +2639,6 @@ pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
     if ((s = upload(c, L.fit, t->fitness, n)) != PG_OK) return s;
     if ((s = upload(c, L.pub, t->pub_epoch, n)) != PG_OK) return s;
     if ((s = upload(c, L.anchors, t->anchors, 4 * std::max<int64_t>(agents, 1) * (agents > 0))) != PG_OK) return s;
-    if ((s = upload(c, L.coff, t->cite_off, agents + 1)) != PG_OK) return s;
-    if ((s = upload(c, L.cites, t->cites, mc)) != PG_OK) return s;
     if ((s = upload(c, L.agent_epoch, aep.data(), agents)) != PG_OK) return s;
     PG_CUDA(c, dalloc(L.feat, (int64_t)E * n));
     PG_CUDA(c, dalloc(L.err, 1));

@@ -778,6 +778,29 @@ void launch_lik_sum(const LikTrace& T, const LikBatch& P, int adjoint, cudaStrea
     k_lik_sum<<<(unsigned)(P.B * K), 256, 0, s>>>(P.out, T.agents, P.B, K, P.res);
 }
 
+// one warp per agent
+__global__ void __launch_bounds__(256) k_trace_edges(const int64_t* coff, const int32_t* cites, int64_t agents,
+                                                     int64_t n0, int64_t ns, int32_t* src, int32_t* dst) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t a = warp; a < agents; a += nwarps) {
+        const int64_t p1 = coff[a + 1];
+        for (int64_t p = coff[a] + lane; p < p1; p += 32) {
+            src[ns + p] = (int32_t)(n0 + a);
+            dst[ns + p] = cites[p];
+        }
+    }
+}
+
+void launch_trace_edges(const int64_t* coff, const int32_t* cites, int64_t agents, int64_t n0, int64_t ns,
+                        int32_t* src, int32_t* dst, int num_sms, cudaStream_t s) {
+    if (agents <= 0) return;
+    int64_t g = (agents + 7) / 8;
+    if (g > (int64_t)num_sms * 16) g = (int64_t)num_sms * 16;
+    k_trace_edges<<<(unsigned)g, 256, 0, s>>>(coff, cites, agents, n0, ns, src, dst);
+}
+
 void launch_lik_features(const LikTrace& T, int exact, int num_sms, cudaStream_t s) {
     int64_t gx = (T.n + 255) / 256;
     if (gx > (int64_t)num_sms * 8) gx = (int64_t)num_sms * 8;

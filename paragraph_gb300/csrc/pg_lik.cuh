@@ -72,6 +72,10 @@ struct LikBalls {
 size_t lik_ball_smem(int bitmap_words);
 // resident CTAs per SM: ball kernels (*ball_per_sm), forward and adjoint pass (eval_per_sm[2])
 cudaError_t init_lik_kernels(int bitmap_words, int* ball_per_sm, int* eval_per_sm);
+// a trace's citations as edges: edge ns + p, for citation p of agent a (coff: agents + 1 offsets),
+// is (n0 + a, cites[p]); the seed edges fill [0, ns) beforehand
+void launch_trace_edges(const int64_t* coff, const int32_t* cites, int64_t agents, int64_t n0, int64_t ns,
+                        int32_t* src, int32_t* dst, int num_sms, cudaStream_t s);
 // the feature rows in the layout of the arithmetic mode (exact: packed low parts of both logs)
 void launch_lik_features(const LikTrace& T, int exact, int num_sms, cudaStream_t s);
 // emit = 0: ball sizes into Bl.cnt / Bl.adj; 1: ball ids and citation flags
