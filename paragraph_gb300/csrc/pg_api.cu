@@ -647,6 +647,8 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     DBuf<uint32_t> berr;
     DBuf<int64_t> t_bo, t_caps, t_begs, t_bsum, t_u, t_laid;
     DBuf<int32_t> t_bc;
+    DBuf<int64_t> t_ro;
+    DBuf<int32_t> t_fsrc, t_btgt;  // one replica's raw build: every entry's row, for the row layout
     struct Temps {
         std::vector<std::function<void()>> f;
         ~Temps() {
@@ -684,8 +686,11 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
     // several replicas' seeds are built as one graph over the arena's slots (launch_build_all); one
     // replica's by the build per replica below
     const bool batched = raw && R > 1;
-    DBuf<int64_t> t_ro;
     temps.f.push_back([&]() { tfree(t_ro, c->device, c->stream); });
+    temps.f.push_back([&]() {
+        tfree(t_fsrc, c->device, c->stream);
+        tfree(t_btgt, c->device, c->stream);
+    });
     if (raw) {
         int64_t mm = 1, nn = 1;
         for (int r = 0; r < R; ++r) {
@@ -694,6 +699,10 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         }
         const size_t sb = batched ? build_all_scratch_bytes(raw_off[(size_t)R], S) : build_scratch_bytes(mm, nn);
         PG_CUDA(c, talloc(scratch, (int64_t)sb, c->device, c->stream));
+        if (!batched) {
+            PG_CUDA(c, talloc(t_fsrc, mm, c->device, c->stream));
+            PG_CUDA(c, talloc(t_btgt, mm, c->device, c->stream));
+        }
         PG_CUDA(c, talloc(berr, R, c->device, c->stream));
         PG_CUDA(c, cudaMemsetAsync(berr.p, 0, 4 * (size_t)R, c->stream));
     }
@@ -739,7 +748,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
             const size_t o = (size_t)raw_off[(size_t)r];
             launch_build_csr(raw_src.p + o, raw_dst.p + o, d.num_edges, (int64_t)n, scratch.p, c->fwd_off.p + h.obase,
                              c->fwd_col.p + h.ebase, t_bo.p, t_bc.p, c->indeg.p + h.nbase, t_u.p + r, berr.p + r,
-                             c->stream);
+                             c->stream, t_fsrc.p, t_btgt.p);
             PG_CUDA(c, cudaGetLastError());
         } else {
             PG_CUDA(c, cudaMemcpyAsync(c->pub.p + h.nbase, g.pub.data(), 4 * n, cudaMemcpyHostToDevice, c->stream));
@@ -756,7 +765,7 @@ pg_status upload_arena(pg_ctx* c, std::vector<HostRep>& reps, const std::vector<
         if (n) {
             launch_brow_layout(t_bo.p, t_bc.p, c->fwd_off.p + h.obase, c->fwd_col.p + h.ebase, (int64_t)n, h.m,
                                t_caps.p, t_begs.p, t_bsum.p, c->brow.p + h.nbase, c->bcap.p + h.nbase,
-                               c->bcol.p + h.bbase, c->stream);
+                               c->bcol.p + h.bbase, c->stream, raw ? t_fsrc.p : nullptr, raw ? t_btgt.p : nullptr);
             PG_CUDA(c, cudaGetLastError());
             PG_CUDA(c, cudaMemcpyAsync(t_laid.p + r, t_begs.p + n, 8, cudaMemcpyDeviceToDevice, c->stream));
         }

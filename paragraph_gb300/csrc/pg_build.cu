@@ -388,9 +388,32 @@ __global__ void __launch_bounds__(256) k_brow_prefix(const int64_t* fo, const in
     }
 }
 
+// the same two copies when the CSR build gave every entry its row: backward entry i belongs to row
+// btgt[i], forward entry p to row fsrc[p] (no search)
+__global__ void __launch_bounds__(256) k_brow_cols_rows(const int64_t* bo, const int32_t* bc, const int32_t* btgt,
+                                                        const BRow* brow, int64_t n, int64_t m, int32_t* out) {
+    const int64_t u = bo[n] < m ? bo[n] : m;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < u; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = btgt[i];
+        out[((int64_t)brow[v].beg4 << 2) + (i - bo[v])] = bc[i];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_brow_prefix_rows(const int64_t* fo, const int32_t* fc, const int32_t* fsrc,
+                                                          const BRow* brow, int64_t n, int64_t m, int32_t* out) {
+    const int64_t u = fo[n] < m ? fo[n] : m;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < u; p += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = fsrc[p];
+        const BRow r = brow[v];
+        if (r.len <= 0) continue;
+        const int64_t f0 = fo[v], o = fo[v + 1] - f0;
+        out[((int64_t)r.beg4 << 2) - o + (p - f0)] = fc[p];
+    }
+}
+
 void launch_brow_layout(const int64_t* bo, const int32_t* bc, const int64_t* fo, const int32_t* fc, int64_t n,
                         int64_t m, int64_t* caps, int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcap,
-                        int32_t* bcol, cudaStream_t s) {
+                        int32_t* bcol, cudaStream_t s, const int32_t* fsrc, const int32_t* btgt) {
     if (n <= 0) return;
     const unsigned gn = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
     k_brow_caps<<<gn, 256, 0, s>>>(bo, fo, n, caps);
@@ -398,9 +421,16 @@ void launch_brow_layout(const int64_t* bo, const int32_t* bc, const int64_t* fo,
     k_brow_rows<<<gn, 256, 0, s>>>(bo, fo, begs, n, brow, bcap);
     if (m > 0) {
         const unsigned gm = (unsigned)std::min<int64_t>((m + 255) / 256, 152 * 16);
-        k_brow_cols<<<gm, 256, 0, s>>>(bo, bc, brow, n, m, bcol);
-        const unsigned gw = (unsigned)std::min<int64_t>((n + 7) / 8, 152 * 16);
-        k_brow_prefix<<<gw, 256, 0, s>>>(fo, fc, brow, n, bcol);
+        if (btgt)
+            k_brow_cols_rows<<<gm, 256, 0, s>>>(bo, bc, btgt, brow, n, m, bcol);
+        else
+            k_brow_cols<<<gm, 256, 0, s>>>(bo, bc, brow, n, m, bcol);
+        if (fsrc) {
+            k_brow_prefix_rows<<<gm, 256, 0, s>>>(fo, fc, fsrc, brow, n, m, bcol);
+        } else {
+            const unsigned gw = (unsigned)std::min<int64_t>((n + 7) / 8, 152 * 16);
+            k_brow_prefix<<<gw, 256, 0, s>>>(fo, fc, brow, n, bcol);
+        }
     }
 }
 

@@ -509,9 +509,10 @@ void launch_build_csr(const int32_t* src, const int32_t* dst, int64_t m, int64_t
 // in front of them (fo/fc: the replica's forward CSR): caps n, begs n + 1 (begs[n] = entries laid
 // out), blocksum scan_blocks_needed(n) + 2 entries of scratch; brow/bcol: the replica's rows and
 // region
+// (fsrc / btgt, when not null: every forward entry's and backward entry's row, from launch_build_csr)
 void launch_brow_layout(const int64_t* bo, const int32_t* bc, const int64_t* fo, const int32_t* fc, int64_t n,
                         int64_t m, int64_t* caps, int64_t* begs, int64_t* blocksum, BRow* brow, int32_t* bcap,
-                        int32_t* bcol, cudaStream_t s);
+                        int32_t* bcol, cudaStream_t s, const int32_t* fsrc = nullptr, const int32_t* btgt = nullptr);
 // the seeds of all replicas as one build over the arena's node slots (pg_build.cu): raw edges
 // src/dst (replica r's at [raw_off[r], raw_off[r+1]), rewritten in place to slot ids), the device
 // Replica array and tile map already uploaded; u/laid receive each replica's unique edges and
