@@ -514,8 +514,9 @@ def ensemble_measure(args, world, rank, local, dist, with_cpu: bool = True) -> d
             e2.load_replicas(preps)
             m0 = [e2.counts(r) for r in range(len(reps))]
             # every epoch's citations, replica by replica, written into the page-locked buffers
-            # while the following epochs run
-            ne, _ = e2.run_epochs_out(ENS_EPOCHS, (out_s, out_d), use_graph=True)
+            # while the following epochs run (a single run: launched directly, as in the PA line --
+            # capturing and instantiating a graph costs more than it saves once)
+            ne, _ = e2.run_epochs_out(ENS_EPOCHS, (out_s, out_d), use_graph=False)
             t1 = time.perf_counter()
             for r in range(len(reps)):
                 n0_, mm0 = m0[r]
