@@ -2665,7 +2665,29 @@ pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
     PG_CUDA(c, dalloc(L.bcnt, na));
     PG_CUDA(c, dalloc(L.badj, na));
     PG_CUDA(c, dalloc(L.cflag, std::max<int64_t>(mc, 1)));
-    launch_lik_ball(make_trace(c), make_balls(L, 0), 0, 0, agents, L.ball_grid, c->stream);
+    // the count pass keeps every agent's bitmaps when they fit an eighth of free memory, so that
+    // the emit pass reads them back instead of walking the rows a second time
+    DBuf<uint32_t> bmap;
+    struct BmapGuard {
+        pg_ctx* c;
+        DBuf<uint32_t>* b;
+        ~BmapGuard() { tfree(*b, c->device, c->stream); }
+    } bmap_guard{c, &bmap};
+    const int64_t pass_ids = (int64_t)L.words * 32;
+    const int64_t bstride = (nmax + pass_ids - 1) / pass_ids * L.words;
+    {
+        size_t free0 = 0, total0 = 0;
+        PG_CUDA(c, cudaMemGetInfo(&free0, &total0));
+        if ((double)std::max<int64_t>(agents, 1) * (double)bstride * 4.0 <= (double)free0 / 8.0 &&
+            talloc(bmap, std::max<int64_t>(agents, 1) * bstride, c->device, c->stream) != cudaSuccess) {
+            cudaGetLastError();  // no room after all: the emit pass walks the rows
+            bmap.p = nullptr;
+        }
+    }
+    LikBalls count_balls = make_balls(L, 0);
+    count_balls.bmap = bmap.p;
+    count_balls.bmap_stride = bstride;
+    launch_lik_ball(make_trace(c), count_balls, 0, 0, agents, L.ball_grid, c->stream);
     PG_CUDA(c, cudaGetLastError());
     std::vector<int64_t> cnt((size_t)na, 0), adj((size_t)na, 0);
     if (agents > 0) {
@@ -2703,7 +2725,10 @@ pg_status pg_trace_load(pg_ctx* c, const pg_trace_desc* t) {
     PG_CUDA(c, dalloc(L.bids, chunk_max));
     L.balls_cached = L.ball_chunks.size() == 1;
     if (L.balls_cached) {
-        launch_lik_ball(make_trace(c), make_balls(L, 0), 1, 0, agents, L.ball_grid, c->stream);
+        LikBalls emit_balls = make_balls(L, 0);
+        emit_balls.bmap = bmap.p;
+        emit_balls.bmap_stride = bstride;
+        launch_lik_ball(make_trace(c), emit_balls, 1, 0, agents, L.ball_grid, c->stream);
         PG_CUDA(c, cudaGetLastError());
     }
     PG_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -431,30 +431,39 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_ball(LikTrace T, LikBalls B
         for (int64_t lo = 0; lo < ne; lo += pass_ids) {
             const int64_t hi = ne < lo + pass_ids ? ne : lo + pass_ids;
             const int nw = (int)((hi - lo + 31) >> 5);
-            for (int w = tid; w < nw; w += kLikThreads) bits[w] = 0u;
-            __syncthreads();
-            auto mark = [&](int64_t v) {
-                if (v >= lo && v < hi) {
-                    const int64_t o = v - lo;
-                    atomicOr(&bits[o >> 5], 1u << (o & 31));
+            uint32_t* cache = Bl.bmap ? Bl.bmap + a * Bl.bmap_stride + (lo / pass_ids) * T.bitmap_words : nullptr;
+            if (EMIT && cache) {
+                // the count pass left this agent's bitmap: no row walk
+                for (int w = tid; w < nw; w += kLikThreads) bits[w] = cache[w];
+                __syncthreads();
+            } else {
+                for (int w = tid; w < nw; w += kLikThreads) bits[w] = 0u;
+                __syncthreads();
+                auto mark = [&](int64_t v) {
+                    if (v >= lo && v < hi) {
+                        const int64_t o = v - lo;
+                        atomicOr(&bits[o >> 5], 1u << (o & 31));
+                    }
+                };
+                if (tid < na) mark(anc[tid]);
+                // every 1-hop node y (one warp each) and the rows of y
+                for (int64_t q = warp; q < L1; q += kLikThreads / 32) {
+                    int sg = 0;
+                    while (seg[sg + 1] <= q) ++sg;
+                    const int32_t* col = (sg & 1) ? T.bc : T.fc;
+                    const int64_t y = col[rowb[sg] + (q - seg[sg])];
+                    if (lane == 0) mark(y);
+                    const int64_t f1 = T.fo[y + 1];
+                    for (int64_t p = T.fo[y] + lane; p < f1; p += 32) mark(T.fc[p]);
+                    const int64_t b1 = bwd_cut(T, y, ne);
+                    for (int64_t p = T.bo[y] + lane; p < b1; p += 32) mark(T.bc[p]);
+                    if (!EMIT && lane == 0 && lo == 0)
+                        atomicAdd(&adj_read, (unsigned long long)((f1 - T.fo[y]) + (b1 - T.bo[y])));
                 }
-            };
-            if (tid < na) mark(anc[tid]);
-            // every 1-hop node y (one warp each) and the rows of y
-            for (int64_t q = warp; q < L1; q += kLikThreads / 32) {
-                int sg = 0;
-                while (seg[sg + 1] <= q) ++sg;
-                const int32_t* col = (sg & 1) ? T.bc : T.fc;
-                const int64_t y = col[rowb[sg] + (q - seg[sg])];
-                if (lane == 0) mark(y);
-                const int64_t f1 = T.fo[y + 1];
-                for (int64_t p = T.fo[y] + lane; p < f1; p += 32) mark(T.fc[p]);
-                const int64_t b1 = bwd_cut(T, y, ne);
-                for (int64_t p = T.bo[y] + lane; p < b1; p += 32) mark(T.bc[p]);
-                if (!EMIT && lane == 0 && lo == 0)
-                    atomicAdd(&adj_read, (unsigned long long)((f1 - T.fo[y]) + (b1 - T.bo[y])));
+                __syncthreads();
+                if (!EMIT && cache)
+                    for (int w = tid; w < nw; w += kLikThreads) cache[w] = bits[w];
             }
-            __syncthreads();
             if (EMIT) {
                 for (int i = tid; i < k; i += kLikThreads) {
                     const int64_t c = T.cites[c0 + i];

@@ -67,6 +67,10 @@ struct LikBalls {
     uint8_t* cflag;       // [citations] 1 when the cited node is in the citing agent's ball
     int64_t* cnt;         // [agents] ball sizes (count pass)
     int64_t* adj;         // [agents] adjacency entries read to build each ball (count pass)
+    // optional: every agent's bitmaps, written by the count pass and read by the emit pass instead
+    // of walking the rows again (agent a's bitmap of pass i at bmap + a bmap_stride + i bitmap_words)
+    uint32_t* bmap;
+    int64_t bmap_stride;
 };
 
 size_t lik_ball_smem(int bitmap_words);
