@@ -7,7 +7,9 @@
 // the reference's ES top-k over the neighbourhood (src/abm.cu:461-565) -- at a cost that does not
 // depend on the ball's size.  The 32 lanes evaluate 32 events at once (Philox + guide-table CDF
 // search); the acceptances are then taken in event order.  The rows of all boost candidates of a
-// batch are staged into shared memory by bulk copies and tested together.
+// batch are staged into shared memory by bulk copies and tested together: one copy per candidate,
+// since a cited node's backward span carries a copy of its forward row in front of its backward
+// entries (a node never cited is its forward row alone).
 //
 // Ball membership, the 2-hop BFS of GetOneAndTwoHopNeighborhood (src/abm.cu:577-682) answered on
 // demand instead of materialised:
