@@ -916,7 +916,7 @@ __global__ void __launch_bounds__(kEpochThreads, 2) k_epoch(Arena A, int64_t epo
     // the moved rows' old entries copied, new entries placed (disjoint positions)
     d_bwd_reloc(A);
     d_bwd_place(A, agents);
-    d_copy_out(A, agents);
+    d_copy_out(A, agents, reinterpret_cast<int32_t*>(ep_dsm));  // this phase uses no other shared memory
     grid_sync(A);
     // appended segments sorted
     d_sort_small(A);

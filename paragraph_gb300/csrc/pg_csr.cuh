@@ -235,11 +235,15 @@ __device__ __forceinline__ void d_bwd_place(const Arena& A, int64_t agents) {
 
 __global__ void __launch_bounds__(256) k_bwd_place(Arena A, int64_t agents) { d_bwd_place(A, agents); }
 
-// A run's citation output (pg_run_epochs_out): one warp per agent writes the agent's citations,
-// (source, target), at the run's running count; the first CTA records the epoch's count per
-// replica.  The targets are read from the epoch's edge list, which the next epoch overwrites, so the
-// stream order puts this before the epoch end.
-__device__ __forceinline__ void d_copy_out(const Arena& A, int64_t agents) {
+// A run's citation output (pg_run_epochs_out): the epoch's citations, (source, target), at the
+// run's running count, written in whole lines -- the writes cross the host link, where a partial
+// line costs as much as a full one.  Each CTA takes kCopyTile consecutive edges: the targets are
+// copied straight through; the sources (the citing agents' node ids, one run per agent) are first
+// laid out in `stage` (kCopyTile ints of shared memory) from the agents whose edges meet the tile.
+// The first CTA records the epoch's count per replica.  The targets are read from the epoch's edge
+// list, which the next epoch overwrites, so the stream order puts this before the epoch end.
+constexpr int kCopyTile = 2048;
+__device__ __forceinline__ void d_copy_out(const Arena& A, int64_t agents, int32_t* stage) {
     if (!A.out_src || A.st->error) return;
     const int64_t base = (int64_t)A.st->out_count;
     const int64_t E = A.eoff[agents];
@@ -254,22 +258,46 @@ __device__ __forceinline__ void d_copy_out(const Arena& A, int64_t agents) {
             A.out_counts[k * A.R + r] = A.eoff[rp.abase + rp.delta] - A.eoff[rp.abase];
         }
     }
-    const int lane = lane_id();
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t a = warp; a < agents; a += nwarps) {
-        const int r = replica_of_agent(A.rep, A.R, a);
-        const Replica& rp = A.rep[r];
-        const int32_t src = (int32_t)(rp.n + (a - rp.abase));
-        const int64_t e0 = A.eoff[a], e1 = A.eoff[a + 1];
-        for (int64_t e = e0 + lane; e < e1; e += 32) {
-            A.out_src[base + e] = src;
+    __shared__ int64_t span[2];  // the tile's first and last agent
+    // the last agent whose edges start at or before edge e
+    auto agent_of = [&](int64_t e) -> int64_t {
+        int64_t lo = 0, hi = agents - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (A.eoff[mid] <= e)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        return lo;
+    };
+    for (int64_t t0 = (int64_t)blockIdx.x * kCopyTile; t0 < E; t0 += (int64_t)gridDim.x * kCopyTile) {
+        const int64_t t1 = E < t0 + kCopyTile ? E : t0 + kCopyTile;
+        if (threadIdx.x == 0) {
+            span[0] = agent_of(t0);
+            span[1] = agent_of(t1 - 1);
+        }
+        __syncthreads();
+        for (int64_t a = span[0] + threadIdx.x; a <= span[1]; a += blockDim.x) {
+            const int r = replica_of_agent(A.rep, A.R, a);
+            const Replica& rp = A.rep[r];
+            const int32_t src = (int32_t)(rp.n + (a - rp.abase));
+            const int64_t lo = A.eoff[a] > t0 ? A.eoff[a] : t0, hi = A.eoff[a + 1] < t1 ? A.eoff[a + 1] : t1;
+            for (int64_t e = lo; e < hi; ++e) stage[e - t0] = src;
+        }
+        __syncthreads();
+        for (int64_t e = t0 + threadIdx.x; e < t1; e += blockDim.x) {
+            A.out_src[base + e] = stage[e - t0];
             A.out_dst[base + e] = A.e_dst[e];
         }
+        __syncthreads();  // the stage is rewritten by the next tile
     }
 }
 
-__global__ void __launch_bounds__(256) k_copy_out(Arena A, int64_t agents) { d_copy_out(A, agents); }
+__global__ void __launch_bounds__(256) k_copy_out(Arena A, int64_t agents) {
+    __shared__ int32_t stage[kCopyTile];
+    d_copy_out(A, agents, stage);
+}
 
 // The epoch's `added` entries of the row in `slot` (the row's last ones): replica and first entry.
 __device__ __forceinline__ void seg_bounds(const Arena& A, int64_t slot, int64_t added, const Replica*& rpp,
@@ -430,7 +458,9 @@ void launch_bwd_append(const Arena& A, int64_t agents, int num_sms, cudaStream_t
         cudaStreamWaitEvent(side, fork, 0);
     }
     k_bwd_reloc<<<(unsigned)(num_sms * copy_per_sm), 256, 0, two ? side : s>>>(A);
-    if (A.out_src) k_copy_out<<<(unsigned)(num_sms * 8), 256, 0, two ? side : s>>>(A, agents);
+    // one CTA per SM: the copy is bound by the host link, and the placement and sorts beside it
+    // keep the rest of the SMs
+    if (A.out_src) k_copy_out<<<(unsigned)num_sms, 256, 0, two ? side : s>>>(A, agents);
     if (two) cudaEventRecord(join, side);
     k_bwd_place<<<(unsigned)ga, 256, 0, s>>>(A, agents);
     k_sort_small<<<(unsigned)num_sms * 8, 256, 0, s>>>(A);
